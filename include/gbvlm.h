@@ -1,0 +1,272 @@
+/*
+ * gbvlm -- GB300-native vortex-lattice hot path, C ABI.
+ *
+ * One entry point per operator of the tinyvlm plugin API (class vlm::Backend
+ * and its BLAS/LU helpers, vlm/include/vlm_backend.hpp:13-136) in both of the
+ * reference's precisions, plus the simulation drivers (vlm/include/vlm.hpp)
+ * and the batched steady solver.  Each declaration cites the reference
+ * interface it replaces.
+ *
+ * Conventions (identical to the reference's tensors, vlm/include/vlm_memory.hpp):
+ *  - every array is column-major (first index fastest) and contiguous;
+ *  - per surface m (a half wing mirrored in y = 0):
+ *      wing vertices  (ns+1, nc+1, 4)   x, y, z, w planes
+ *      panel vectors  (ns, nc, 3)       colloc, normals, velocities, forces
+ *      panel scalars  (ns, nc)          areas, gamma, gamma_delta, dgamma_dt
+ *      wake vertices  (ns+1, nwv, 4)    newest row at index nwv-1-iteration
+ *      wake gamma     (ns, nwv-1)
+ *  - the LHS is (n, n) with leading dimension ld: row = collocation point,
+ *    column = influencing ring; surface blocks are contiguous;
+ *  - multi-surface arguments are HOST arrays holding one DEVICE pointer per
+ *    surface (the reference's MultiTensorView);
+ *  - scalars returned through a host pointer are read back synchronously,
+ *    like the reference's scalar-returning backend calls; every other call
+ *    is asynchronous on `stream` (0 = legacy default stream);
+ *  - every function returns GBVLM_OK or an error code; gbvlm_last_error()
+ *    gives the message.  The reference prints and exits instead
+ *    (vlm_backend_cuda.cu:21-29); callers that want that behaviour test the
+ *    return code.
+ */
+#ifndef GBVLM_H
+#define GBVLM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gbvlm_stream; /* same handle as cudaStream_t */
+
+enum {
+    GBVLM_OK = 0,
+    GBVLM_ERR_ARG = 1,      /* invalid argument (sizes, null pointers, too many surfaces) */
+    GBVLM_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    GBVLM_ERR_SINGULAR = 3, /* exact zero pivot met in an LU factorisation */
+    GBVLM_ERR_NOMEM = 4,    /* device allocation failed */
+    GBVLM_ERR_IO = 5,       /* mesh file could not be read */
+    GBVLM_ERR_STATE = 6     /* handle used out of order */
+};
+
+#define GBVLM_MAX_SURFACES 16
+
+/* Sizes of one surface: ns spanwise panels, nc chordwise panels, nwv wake
+ * vertex rows (0 when the call does not touch the wake). */
+typedef struct {
+    int64_t ns, nc, nwv;
+} gbvlm_dims;
+
+const char* gbvlm_last_error(void);
+int gbvlm_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Backend operators.  Replaces the pure virtuals of vlm::Backend
+ * (vlm/include/vlm_backend.hpp:31-55); semantics follow the CPU backend
+ * vlm/backends/cpu/src/vlm_backend_cpu.cpp (f32) and vlm_backend_cpud.cpp (f64).
+ * ------------------------------------------------------------------------- */
+
+/* Backend::lhs_assemble (vlm_backend.hpp:31/45; vlm_backend_cpu.cpp:84-148).
+ * lhs += AIC; the trailing-edge columns also get the wake ring rows
+ * nwv-2-c, c < iteration (Kutta condition).  Zero lhs first. */
+int gbvlm_lhs_assemble_f32(float* lhs, int64_t ld, int32_t nsurf, const gbvlm_dims* dims,
+                           const float* const* colloc, const float* const* normals,
+                           const float* const* verts_wing, const float* const* verts_wake,
+                           int32_t iteration, float sigma, gbvlm_stream stream);
+int gbvlm_lhs_assemble_f64(double* lhs, int64_t ld, int32_t nsurf, const gbvlm_dims* dims,
+                           const double* const* colloc, const double* const* normals,
+                           const double* const* verts_wing, const double* const* verts_wake,
+                           int32_t iteration, double sigma, gbvlm_stream stream);
+
+/* Backend::rhs_assemble_velocities (vlm_backend.hpp:32/46; vlm_backend_cpu.cpp:156-179).
+ * rhs[p] += -(V_p . n_p), surfaces packed in order. */
+int gbvlm_rhs_assemble_velocities_f32(float* rhs, int32_t nsurf, const gbvlm_dims* dims,
+                                      const float* const* normals, const float* const* velocities,
+                                      gbvlm_stream stream);
+int gbvlm_rhs_assemble_velocities_f64(double* rhs, int32_t nsurf, const gbvlm_dims* dims,
+                                      const double* const* normals, const double* const* velocities,
+                                      gbvlm_stream stream);
+
+/* Backend::rhs_assemble_wake_influence (vlm_backend.hpp:33/47; vlm_backend_cpu.cpp:181-224).
+ * rhs[p] -= (sum over the last `iteration` wake ring rows of every lifting
+ * surface of gamma_r v_r(colloc_p)) . n_p.  The f32 variant keeps the
+ * reference's 5000-row window.  lifting is a host array of nsurf flags. */
+int gbvlm_rhs_assemble_wake_influence_f32(float* rhs, int32_t nsurf, const gbvlm_dims* dims,
+                                          const float* const* gamma_wake, const float* const* colloc,
+                                          const float* const* normals, const float* const* verts_wake,
+                                          const int32_t* lifting, int32_t iteration, float sigma,
+                                          gbvlm_stream stream);
+int gbvlm_rhs_assemble_wake_influence_f64(double* rhs, int32_t nsurf, const gbvlm_dims* dims,
+                                          const double* const* gamma_wake, const double* const* colloc,
+                                          const double* const* normals, const double* const* verts_wake,
+                                          const int32_t* lifting, int32_t iteration, double sigma,
+                                          gbvlm_stream stream);
+
+/* Backend::forces_steady (vlm_backend.hpp:34/48; vlm_backend_cpu.cpp:276-297), rho = 1. */
+int gbvlm_forces_steady_f32(int64_t ns, int64_t nc, const float* verts_wing, const float* gamma_delta,
+                            const float* velocities, float* forces, gbvlm_stream stream);
+int gbvlm_forces_steady_f64(int64_t ns, int64_t nc, const double* verts_wing, const double* gamma_delta,
+                            const double* velocities, double* forces, gbvlm_stream stream);
+
+/* Backend::forces_unsteady (vlm_backend.hpp:35/49; vlm_backend_cpu.cpp:299-321), rho = 1. */
+int gbvlm_forces_unsteady_f32(int64_t ns, int64_t nc, const float* verts_wing, const float* gamma_delta,
+                              const float* dgamma_dt, const float* velocities, const float* areas,
+                              const float* normals, float* forces, gbvlm_stream stream);
+int gbvlm_forces_unsteady_f64(int64_t ns, int64_t nc, const double* verts_wing, const double* gamma_delta,
+                              const double* dgamma_dt, const double* velocities, const double* areas,
+                              const double* normals, double* forces, gbvlm_stream stream);
+
+/* Backend::coeff_cl (vlm_backend.hpp:36/50; vlm_backend_cpu.cpp:323-338).
+ * lift_axis, freestream: host float[3]/double[3].  Sums in double with
+ * compensation.  *out is written synchronously. */
+int gbvlm_coeff_cl_f32(int64_t ns, int64_t nc, const float* forces, const float* lift_axis,
+                       const float* freestream, float rho, float area, float* out, gbvlm_stream stream);
+int gbvlm_coeff_cl_f64(int64_t ns, int64_t nc, const double* forces, const double* lift_axis,
+                       const double* freestream, double rho, double area, double* out, gbvlm_stream stream);
+
+/* Backend::coeff_cm (vlm_backend.hpp:37/51; vlm_backend_cpu.cpp:340-362).  out: host [3]. */
+int gbvlm_coeff_cm_f32(int64_t ns, int64_t nc, const float* forces, const float* verts_wing,
+                       const float* ref_pt, const float* freestream, float rho, float area, float mac,
+                       float* out, gbvlm_stream stream);
+int gbvlm_coeff_cm_f64(int64_t ns, int64_t nc, const double* forces, const double* verts_wing,
+                       const double* ref_pt, const double* freestream, double rho, double area, double mac,
+                       double* out, gbvlm_stream stream);
+
+/* Backend::mesh_metrics (vlm_backend.hpp:38/52; vlm_backend_cpu.cpp:391-433):
+ * normals, areas and collocation points with the high-AoA factor. */
+int gbvlm_mesh_metrics_f32(float alpha_rad, int32_t nsurf, const gbvlm_dims* dims,
+                           const float* const* verts_wing, float* const* colloc, float* const* normals,
+                           float* const* areas, gbvlm_stream stream);
+int gbvlm_mesh_metrics_f64(double alpha_rad, int32_t nsurf, const gbvlm_dims* dims,
+                           const double* const* verts_wing, double* const* colloc, double* const* normals,
+                           double* const* areas, gbvlm_stream stream);
+
+/* Backend::mesh_mac (vlm_backend.hpp:39/53; vlm_backend_cpu.cpp:443-468). *out synchronous. */
+int gbvlm_mesh_mac_f32(int64_t ns, int64_t nc, const float* verts_wing, const float* areas, float* out,
+                       gbvlm_stream stream);
+int gbvlm_mesh_mac_f64(int64_t ns, int64_t nc, const double* verts_wing, const double* areas, double* out,
+                       gbvlm_stream stream);
+
+/* Backend::gamma_wake_from_coeffs (vlm_backend.hpp:40/54; vlm_backend_cpu.cpp:470-503).
+ * gamma_wake (ns, ncols), coeffs (ns, 2*harmonics+1); fills the last
+ * `iteration` columns. */
+int gbvlm_gamma_wake_from_coeffs_f32(float* gamma_wake, int64_t ns, int64_t ncols, const float* coeffs,
+                                     int32_t harmonics, float tn, float omega, float dt, int64_t iteration,
+                                     gbvlm_stream stream);
+int gbvlm_gamma_wake_from_coeffs_f64(double* gamma_wake, int64_t ns, int64_t ncols, const double* coeffs,
+                                     int32_t harmonics, double tn, double omega, double dt, int64_t iteration,
+                                     gbvlm_stream stream);
+
+/* Backend::sum (vlm_backend.hpp:41-42/55-56; vlm_backend_cpu.cpp:506-523). *out synchronous. */
+int gbvlm_sum_f32(const float* x, int64_t n, float* out, gbvlm_stream stream);
+int gbvlm_sum_f64(const double* x, int64_t n, double* out, gbvlm_stream stream);
+
+/* Backend::displace_wing (vlm_backend.hpp:59/66; vlm_backend.cpp:50-69):
+ * verts = verts_init . T^T per surface; transforms: device 4x4 column-major. */
+int gbvlm_displace_wing_f32(int32_t nsurf, const gbvlm_dims* dims, const float* const* transforms,
+                            float* const* verts_wing, const float* const* verts_wing_init, gbvlm_stream stream);
+int gbvlm_displace_wing_f64(int32_t nsurf, const gbvlm_dims* dims, const double* const* transforms,
+                            double* const* verts_wing, const double* const* verts_wing_init, gbvlm_stream stream);
+
+/* Backend::wake_shed (vlm_backend.hpp:60/67; vlm_backend.cpp:43-47):
+ * wing trailing-edge vertex row -> wake row nwv-1-iteration. */
+int gbvlm_wake_shed_f32(int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_wing,
+                        float* const* verts_wake, int32_t iteration, gbvlm_stream stream);
+int gbvlm_wake_shed_f64(int32_t nsurf, const gbvlm_dims* dims, const double* const* verts_wing,
+                        double* const* verts_wake, int32_t iteration, gbvlm_stream stream);
+
+/* Free-wake roll-up: ispc::kernel_rollup (vlm_backend_cpu_kernels.ispc:215-271),
+ * whose caller the reference comments out (vlm_backend_cpu.cpp:226-274).
+ * Moves wake vertex rows [nwv-iteration, nwv) of every surface by dt times
+ * the velocity of all wing rings (gamma_wing (ns,nc)) and of the last
+ * `iteration` ring rows of every lifting wake.  Positions are read before
+ * any is written. */
+int gbvlm_wake_rollup_f32(int32_t nsurf, const gbvlm_dims* dims, float* const* verts_wake,
+                          const float* const* verts_wing, const float* const* gamma_wing,
+                          const float* const* gamma_wake, const int32_t* lifting, float sigma, float dt,
+                          int32_t iteration, gbvlm_stream stream);
+int gbvlm_wake_rollup_f64(int32_t nsurf, const gbvlm_dims* dims, double* const* verts_wake,
+                          const double* const* verts_wing, const double* const* gamma_wing,
+                          const double* const* gamma_wake, const int32_t* lifting, double sigma, double dt,
+                          int32_t iteration, gbvlm_stream stream);
+
+/* Trefftz-plane induced drag: ispc::kernel_trefftz_cd
+ * (vlm_backend_cpu_kernels.ispc:273-323) divided by |V|^2 * area as its
+ * commented caller does (vlm_backend_cpu.cpp:364-369).  *out synchronous. */
+int gbvlm_trefftz_cd_f32(int64_t ns, int64_t nwv, const float* verts_wake, const float* gamma_wake,
+                         const float* freestream, float area, float sigma, float* out, gbvlm_stream stream);
+int gbvlm_trefftz_cd_f64(int64_t ns, int64_t nwv, const double* verts_wake, const double* gamma_wake,
+                         const double* freestream, double area, double sigma, double* out, gbvlm_stream stream);
+
+/* Circulation post-processing of one surface after a solve, fused
+ * (vlm/src/vlm.cpp:442-458): gamma = x[0:ns*nc]; gamma_delta = gamma with
+ * the previous chordwise row subtracted; if gamma_wake is not null, the
+ * trailing-edge row goes to wake column `wake_col`; if dgamma_dt is not null,
+ * dgamma_dt = (gamma - gamma_prev) / dt.  gamma_prev is then left untouched. */
+int gbvlm_gamma_update_f32(int64_t ns, int64_t nc, const float* x, float* gamma, float* gamma_delta,
+                           float* gamma_wake, int64_t wake_col, const float* gamma_prev, float* dgamma_dt,
+                           float dt, gbvlm_stream stream);
+int gbvlm_gamma_update_f64(int64_t ns, int64_t nc, const double* x, double* gamma, double* gamma_delta,
+                           double* gamma_wake, int64_t wake_col, const double* gamma_prev, double* dgamma_dt,
+                           double dt, gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Dense LU.  Replaces vlm::LU (vlm_backend.hpp:99-119): CPU LAPACKE
+ * ?getrf/?getrs (vlm_backend_cpu_lapack.cpp:17-94), CUDA cuSOLVER
+ * (vlm_backend_cuda_solvers.cu:39-102).  Partial pivoting (LAPACK pivot
+ * order: largest |a|, first index on ties); ipiv is 0-based on device.
+ * ------------------------------------------------------------------------- */
+typedef struct gbvlm_lu_s* gbvlm_lu;
+int gbvlm_lu_create(gbvlm_lu* out);
+int gbvlm_lu_destroy(gbvlm_lu h);
+/* LU::init: reserve workspace for an n x n matrix */
+int gbvlm_lu_init(gbvlm_lu h, int64_t n);
+/* LU::factorize: A (n x n, leading dimension ld) overwritten by L\U */
+int gbvlm_lu_factor_f32(gbvlm_lu h, float* A, int64_t n, int64_t ld, gbvlm_stream stream);
+int gbvlm_lu_factor_f64(gbvlm_lu h, double* A, int64_t n, int64_t ld, gbvlm_stream stream);
+/* LU::solve: X (n x nrhs, leading dimension ldx) overwritten by A^-1 X */
+int gbvlm_lu_solve_f32(gbvlm_lu h, const float* A, int64_t n, int64_t ld, float* X, int64_t ldx,
+                       int64_t nrhs, gbvlm_stream stream);
+int gbvlm_lu_solve_f64(gbvlm_lu h, const double* A, int64_t n, int64_t ld, double* X, int64_t ldx,
+                       int64_t nrhs, gbvlm_stream stream);
+/* Mixed precision: solve A x = b with the float LU of A (from
+ * gbvlm_lu_factor_f32 of a copy) and `iters` steps of iterative refinement
+ * whose residual b - A x is formed in double from the unfactored float A.
+ * b, x: double (n x nrhs).  Returns the final max-norm relative residual
+ * correction in *last_update when not null (synchronous only then). */
+int gbvlm_lu_solve_refined(gbvlm_lu h, const float* LU, const float* A, int64_t n, int64_t ld,
+                           const double* B, double* X, int64_t nrhs, int32_t iters, double* last_update,
+                           gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Simulation drivers (vlm/include/vlm.hpp), device-resident.
+ * ------------------------------------------------------------------------- */
+typedef struct gbvlm_vlm_s* gbvlm_vlm;
+
+/* Results of one steady solve.  cl follows VLM::run (vlm/src/vlm.cpp:97-151);
+ * cdi is the Trefftz drag (area-weighted like CL) and cm the
+ * coeff_cm_multibody moment about ref_pt, which VLM::run leaves at zero. */
+typedef struct {
+    double cl, cdi, cm[3];
+} gbvlm_coeffs;
+
+/* VLM(backend, meshes) (vlm/src/vlm.cpp:17-58).  verts_init: HOST arrays,
+ * one (ns+1, nc+1, 4) float array per surface, already quarter-chord
+ * shifted (the plot3d reader does it, gbvlm_read_plot3d).  precision: 32
+ * runs the reference's float semantics; 64 the plain per-solve double
+ * path. */
+int gbvlm_vlm_create(gbvlm_vlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                     int32_t precision);
+int gbvlm_vlm_destroy(gbvlm_vlm h);
+/* VLM::run(FlowData) (vlm/src/vlm.cpp:97-151) plus CDi and CM.
+ * gamma_out: optional HOST double array of n entries (surfaces packed). */
+int gbvlm_vlm_run(gbvlm_vlm h, double alpha, double beta, double u_inf, double rho, const double* ref_pt,
+                  gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream);
+
+/* plot3d reader (vlm/src/vlm_mesh.cpp:34-123): dims first (verts == NULL),
+ * then the vertices into a HOST float (ns+1, nc+1, 4) array. */
+int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBVLM_H */

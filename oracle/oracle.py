@@ -1,0 +1,394 @@
+"""Oracle (test infrastructure only): CPU restatement of the tinyvlm
+vortex-lattice hot path, used by ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` as the checker.  The product never
+imports this module.
+
+Heavy per-element kernels run in C (``vlm_oracle.c``, built by ``build.py``);
+the drivers below restate the reference's simulation drivers in numpy, and the
+dense factor/solve calls LAPACK ``?getrf/?getrs`` through scipy -- the same
+LAPACK routines the reference's CPU backend calls through LAPACKE
+(vlm/backends/cpu/src/vlm_backend_cpu_lapack.cpp:40-94; scipy bundles
+OpenBLAS, the reference pins OpenBLAS 0.3.26/0.3.29 in packages/openblas.lua).
+
+Array conventions (identical memory layout to the reference's column-major
+tensors, vlm/include/vlm_memory.hpp:306-319):
+  wing vertices  numpy (4, nc+1, ns+1)  == reference (ns+1, nc+1, 4)
+  panel vectors  numpy (3, nc, ns)      == reference (ns, nc, 3)
+  panel scalars  numpy (nc, ns)         == reference (ns, nc)
+  wake vertices  numpy (4, nwv, ns+1)   == reference (ns+1, nwv, 4)
+  wake gamma     numpy (nwv-1, ns)      == reference (ns, nwv-1)
+  LHS            numpy (n, n) Fortran order, A[row=colloc, col=ring]
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+PI_F = np.float32(3.141593)  # vlm/include/vlm_types.hpp:22
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        for pre, ct in (("f", ctypes.c_float), ("d", ctypes.c_double)):
+            P = ctypes.c_void_p
+            I64, I32 = ctypes.c_int64, ctypes.c_int32
+            getattr(L, "orc_sum_" + pre).restype = ct
+            getattr(L, "orc_mesh_mac_" + pre).restype = ct
+            getattr(L, "orc_coeff_cl_" + pre).restype = ct
+            getattr(L, "orc_trefftz_cd_" + pre).restype = ct
+            getattr(L, "orc_trefftz_cd_" + pre).argtypes = [P, I64, I64, I64, P, ct]
+            getattr(L, "orc_influence_" + pre).argtypes = [I64, P, P, I64, P, I64, I64, P, I64, ct]
+            getattr(L, "orc_wake_influence_" + pre).argtypes = [P, I64, P, I64, P, I64, I64, I64, P, P, ct, I32]
+        L.orc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _sfx(dtype):
+    return "f" if np.dtype(dtype) == np.float32 else "d"
+
+
+def _ct(dtype):
+    return ctypes.c_float if np.dtype(dtype) == np.float32 else ctypes.c_double
+
+
+def _p(a):
+    assert a.flags["C_CONTIGUOUS"] or a.flags["F_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _parr(arrs):
+    return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+def _i64(vals):
+    return (ctypes.c_int64 * len(vals))(*vals)
+
+
+def _i32(vals):
+    return (ctypes.c_int32 * len(vals))(*vals)
+
+
+def num_threads():
+    return lib().orc_num_threads()
+
+
+# ---------------------------------------------------------------------------
+# flow data, vlm/src/vlm_utils.cpp:5-19, vlm/src/vlm_data.cpp:8-13
+# ---------------------------------------------------------------------------
+def freestream(u_inf, alpha, beta, dtype=np.float32):
+    T = np.dtype(dtype).type
+    u, a, b = T(u_inf), T(alpha), T(beta)
+    return np.array([u * np.cos(a) * np.cos(b), -(u * np.cos(a) * np.sin(b)), u * np.sin(a)], dtype=dtype)
+
+
+def lift_axis(fs):
+    T = fs.dtype.type
+    c = np.array([fs[1] * T(0) - fs[2] * T(1), fs[2] * T(0) - fs[0] * T(0), fs[0] * T(1) - fs[1] * T(0)], dtype=fs.dtype)
+    return c / np.sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2])
+
+
+def translation(t, dtype):
+    """Column-major 4x4 translation (vlm/include/vlm_kinematics.hpp translation_matrix)."""
+    m = np.eye(4, dtype=dtype)
+    m[0:3, 3] = t
+    return np.asfortranarray(m)
+
+
+# ---------------------------------------------------------------------------
+# plot3d reader and quarter-chord shift, vlm/src/vlm_mesh.cpp:16-92
+# ---------------------------------------------------------------------------
+def read_plot3d(path, qc=True, dtype=np.float32):
+    tok = open(path).read().split()
+    if int(tok[0]) != 1:
+        raise RuntimeError("Only single block plot3d mesh is supported")
+    ni, nj, nk = int(tok[1]), int(tok[2]), int(tok[3])
+    if nk != 1:
+        raise RuntimeError("Only 2D plot3d mesh is supported")
+    vals = np.array(tok[4:4 + 3 * ni * nj], dtype=np.float64).astype(dtype)
+    v = np.zeros((4, ni, nj), dtype=dtype)  # reference (nj, ni, 4): span index fastest
+    for k in range(3):
+        v[k] = vals[k * ni * nj:(k + 1) * ni * nj].reshape(nj, ni).T
+    v[3] = 1
+    if np.any(v[1, 1:, 0] != v[1, 0, 0]):
+        raise RuntimeError("Mesh vertices should be ordered in chordwise direction")
+    if qc:
+        quarter_chord(v)
+    return v
+
+
+def quarter_chord(v):
+    """vlm_mesh.cpp:16-32, in place on (4, nc+1, ns+1)."""
+    T = v.dtype.type
+    for j in range(v.shape[1] - 1):
+        v[0:3, j, :] = T(0.75) * v[0:3, j, :] + T(0.25) * v[0:3, j + 1, :]
+    j = v.shape[1] - 2
+    v[0:3, j + 1, :] = (T(4) / T(3)) * v[0:3, j + 1, :] - (T(1) / T(3)) * v[0:3, j, :]
+
+
+# ---------------------------------------------------------------------------
+# Backend operators (thin wrappers over the C restatement)
+# ---------------------------------------------------------------------------
+def dims(verts):
+    return [v.shape[2] - 1 for v in verts], [v.shape[1] - 1 for v in verts]
+
+
+def mesh_metrics(alpha, verts, dtype):
+    T = np.dtype(dtype).type
+    out = []
+    for v in verts:
+        ns, nc = v.shape[2] - 1, v.shape[1] - 1
+        col = np.zeros((3, nc, ns), dtype)
+        nor = np.zeros((3, nc, ns), dtype)
+        ar = np.zeros((nc, ns), dtype)
+        getattr(lib(), "orc_mesh_metrics_" + _sfx(dtype))(_ct(dtype)(T(alpha)), ctypes.c_int64(ns), ctypes.c_int64(nc),
+                                                          _p(v), _p(col), _p(nor), _p(ar))
+        out.append((col, nor, ar))
+    return [o[0] for o in out], [o[1] for o in out], [o[2] for o in out]
+
+
+def lhs_assemble(lhs, colloc, normals, verts_wing, verts_wake, iteration, sigma=0.0):
+    dt = lhs.dtype
+    ns, nc = dims(verts_wing)
+    nwv = [w.shape[1] for w in verts_wake]
+    getattr(lib(), "orc_lhs_assemble_" + _sfx(dt))(
+        _p(lhs), ctypes.c_int64(lhs.shape[0]), ctypes.c_int32(len(ns)), _i64(ns), _i64(nc), _i64(nwv),
+        _parr(colloc), _parr(normals), _parr(verts_wing), _parr(verts_wake), ctypes.c_int32(iteration),
+        _ct(dt)(sigma))
+
+
+def rhs_assemble_velocities(rhs, normals, velocities):
+    ns = [n.shape[2] for n in normals]
+    nc = [n.shape[1] for n in normals]
+    getattr(lib(), "orc_rhs_assemble_velocities_" + _sfx(rhs.dtype))(
+        _p(rhs), ctypes.c_int32(len(ns)), _i64(ns), _i64(nc), _parr(normals), _parr(velocities))
+
+
+def rhs_assemble_wake_influence(rhs, gamma_wake, colloc, normals, verts_wake, lifting, iteration, sigma=0.0):
+    ns = [n.shape[2] for n in normals]
+    nc = [n.shape[1] for n in normals]
+    nwv = [w.shape[1] for w in verts_wake]
+    getattr(lib(), "orc_rhs_assemble_wake_influence_" + _sfx(rhs.dtype))(
+        _p(rhs), ctypes.c_int32(len(ns)), _i64(ns), _i64(nc), _i64(nwv), _parr(gamma_wake), _parr(colloc),
+        _parr(normals), _parr(verts_wake), _i32([1 if l else 0 for l in lifting]), ctypes.c_int32(iteration),
+        _ct(rhs.dtype)(sigma))
+
+
+def wake_rollup(verts_wake, verts_wing, gamma_wing, gamma_wake, lifting, dt, iteration, sigma=0.0):
+    d = verts_wake[0].dtype
+    ns, nc = dims(verts_wing)
+    nwv = [w.shape[1] for w in verts_wake]
+    scratch = [w.copy() for w in verts_wake]
+    getattr(lib(), "orc_wake_rollup_" + _sfx(d))(
+        ctypes.c_int32(len(ns)), _i64(ns), _i64(nc), _i64(nwv), _parr(verts_wake), _parr(verts_wing),
+        _parr(gamma_wing), _parr(gamma_wake), _parr(scratch), _i32([1 if l else 0 for l in lifting]),
+        _ct(d)(sigma), _ct(d)(dt), ctypes.c_int32(iteration))
+
+
+def forces_steady(verts, gamma_delta, velocities):
+    d = verts.dtype
+    nc, ns = gamma_delta.shape
+    f = np.zeros((3, nc, ns), d)
+    getattr(lib(), "orc_forces_steady_" + _sfx(d))(ctypes.c_int64(ns), ctypes.c_int64(nc), _p(verts),
+                                                   _p(gamma_delta), _p(velocities), _p(f))
+    return f
+
+
+def forces_unsteady(verts, gamma_delta, dgamma_dt, velocities, areas, normals):
+    d = verts.dtype
+    nc, ns = gamma_delta.shape
+    f = np.zeros((3, nc, ns), d)
+    getattr(lib(), "orc_forces_unsteady_" + _sfx(d))(ctypes.c_int64(ns), ctypes.c_int64(nc), _p(verts),
+                                                     _p(gamma_delta), _p(dgamma_dt), _p(velocities), _p(areas),
+                                                     _p(normals), _p(f))
+    return f
+
+
+def coeff_cl(forces, lift, fs, rho, area):
+    d = forces.dtype
+    _, nc, ns = forces.shape
+    T = d.type
+    return T(getattr(lib(), "orc_coeff_cl_" + _sfx(d))(ctypes.c_int64(ns), ctypes.c_int64(nc), _p(forces),
+                                                       _p(np.ascontiguousarray(lift, d)),
+                                                       _p(np.ascontiguousarray(fs, d)), _ct(d)(rho), _ct(d)(area)))
+
+
+def coeff_cm(forces, verts, ref_pt, fs, rho, area, mac):
+    d = forces.dtype
+    _, nc, ns = forces.shape
+    out = np.zeros(3, d)
+    getattr(lib(), "orc_coeff_cm_" + _sfx(d))(ctypes.c_int64(ns), ctypes.c_int64(nc), _p(forces), _p(verts),
+                                              _p(np.ascontiguousarray(ref_pt, d)), _p(np.ascontiguousarray(fs, d)),
+                                              _ct(d)(rho), _ct(d)(area), _ct(d)(mac), _p(out))
+    return out
+
+
+def asum(x):
+    d = x.dtype
+    return d.type(getattr(lib(), "orc_sum_" + _sfx(d))(ctypes.c_int64(x.size), _p(x)))
+
+
+def mesh_mac(verts, areas):
+    d = verts.dtype
+    nc, ns = areas.shape
+    return d.type(getattr(lib(), "orc_mesh_mac_" + _sfx(d))(ctypes.c_int64(ns), ctypes.c_int64(nc), _p(verts), _p(areas)))
+
+
+def trefftz_cd(verts_wake, gamma_wake, sigma=0.0):
+    d = verts_wake.dtype
+    _, nwv, n = verts_wake.shape
+    return d.type(getattr(lib(), "orc_trefftz_cd_" + _sfx(d))(_p(verts_wake), n * nwv, nwv, n, _p(gamma_wake),
+                                                              _ct(d)(sigma)))
+
+
+def gamma_wake_from_coeffs(gamma_wake, coeffs, harmonics, tn, omega, dt, iteration):
+    d = gamma_wake.dtype
+    ncols, ns = gamma_wake.shape
+    T = d.type
+    getattr(lib(), "orc_gamma_wake_from_coeffs_" + _sfx(d))(
+        ctypes.c_int64(ns), ctypes.c_int64(ncols), _p(gamma_wake), _p(np.asfortranarray(coeffs, d)),
+        ctypes.c_int32(harmonics), _ct(d)(T(tn)), _ct(d)(T(omega)), _ct(d)(T(dt)), ctypes.c_int64(iteration))
+
+
+def displace_wing(transform, verts, verts_init):
+    d = verts.dtype
+    nv = verts.shape[1] * verts.shape[2]
+    getattr(lib(), "orc_displace_wing_" + _sfx(d))(ctypes.c_int64(nv), _p(np.asfortranarray(transform, d)),
+                                                   _p(verts), _p(verts_init))
+
+
+def wake_shed(verts_wing, verts_wake, iteration):
+    """vlm/src/vlm_backend.cpp:43-47: wing TE vertex row -> wake row -1-iteration."""
+    for w, k in zip(verts_wing, verts_wake):
+        k[:, k.shape[1] - 1 - iteration, :] = w[:, -1, :]
+
+
+def lu_factor(A):
+    """LAPACK ?getrf (vlm_backend_cpu_lapack.cpp:40-50)."""
+    from scipy.linalg import lapack
+    f = lapack.sgetrf if A.dtype == np.float32 else lapack.dgetrf
+    lu, piv, info = f(A, overwrite_a=True)
+    if info != 0:
+        raise RuntimeError("getrf failed: info=%d" % info)
+    return lu, piv
+
+
+def lu_solve(lu, piv, b):
+    """LAPACK ?getrs (vlm_backend_cpu_lapack.cpp:52-64)."""
+    from scipy.linalg import lapack
+    f = lapack.sgetrs if lu.dtype == np.float32 else lapack.dgetrs
+    x, info = f(lu, piv, b)
+    if info != 0:
+        raise RuntimeError("getrs failed: info=%d" % info)
+    return x
+
+
+# ---------------------------------------------------------------------------
+# Multibody coefficient reductions, vlm/src/vlm_backend.cpp:72-139
+# ---------------------------------------------------------------------------
+def coeff_cl_multibody(forces, areas, fs, rho):
+    T = fs.dtype.type
+    cl, total = T(0), T(0)
+    la = lift_axis(fs)
+    for f, a in zip(forces, areas):
+        area = asum(a)
+        cl += coeff_cl(f, la, fs, rho, area) * area
+        total += area
+    return T(cl / total)
+
+
+def coeff_cm_multibody(forces, verts, areas, ref_pt, fs, rho):
+    T = fs.dtype.type
+    cm = np.zeros(3, fs.dtype)
+    ta, tm = T(0), T(0)
+    for f, v, a in zip(forces, verts, areas):
+        area = asum(a)
+        mac = mesh_mac(v, a)
+        cm += coeff_cm(f, v, ref_pt, fs, rho, area, mac) * area * mac
+        ta += area
+        tm += mac
+    return cm / (ta * tm)
+
+
+def gamma_delta(gamma):
+    """Chordwise delta (vlm/src/vlm.cpp:138-140): d[:, 1:] = g[:, 1:] - g[:, :-1]."""
+    d = gamma.copy()
+    d[1:, :] -= gamma[:-1, :]
+    return d
+
+
+# ---------------------------------------------------------------------------
+# Steady VLM driver, vlm/src/vlm.cpp:60-151 (plus CDi and CM outputs)
+# ---------------------------------------------------------------------------
+def vlm_run(verts_init, alpha, beta=0.0, u_inf=1.0, rho=1.0, dtype=np.float32, sigma=0.0,
+            ref_pt=(0.0, 0.0, 0.0), return_state=False):
+    """One steady solve with the reference's semantics.
+
+    Returns dict(cl, cdi, cm, gamma) where gamma is a list of (nc, ns) arrays.
+    CL follows VLM::run.  CDi is the Trefftz-plane drag of the (dead in the
+    reference) kernel_trefftz_cd normalised as its commented caller does,
+    area-weighted over surfaces like CL; CM is coeff_cm_multibody about
+    ``ref_pt``, which VLM::run leaves at zero.
+    """
+    T = np.dtype(dtype).type
+    verts_init = [np.ascontiguousarray(v, dtype) for v in verts_init]
+    verts = [v.copy() for v in verts_init]
+    ns, nc = dims(verts)
+    n = sum(a * b for a, b in zip(ns, nc))
+    fs = freestream(u_inf, alpha, beta, dtype)
+    wake = []
+    for s in ns:
+        w = np.zeros((4, 2, s + 1), dtype)
+        w[3] = 1
+        wake.append(w)
+    a32 = T(alpha)
+    tr = translation(np.array([T(-100.0) * T(u_inf) * np.cos(a32), T(0), T(-100.0) * T(u_inf) * np.sin(a32)], dtype),
+                     dtype)
+    wake_shed(verts, wake, 0)
+    for v, vi in zip(verts, verts_init):
+        displace_wing(tr, v, vi)
+    wake_shed(verts, wake, 1)
+    colloc, normals, areas = mesh_metrics(alpha, verts, dtype)
+    lhs = np.zeros((n, n), dtype, order="F")
+    lhs_assemble(lhs, colloc, normals, verts, wake, 1, sigma)
+    vel = []
+    for s, c in zip(ns, nc):
+        v = np.empty((3, c, s), dtype)
+        v[0], v[1], v[2] = fs[0], fs[1], fs[2]
+        vel.append(v)
+    rhs = np.zeros(n, dtype)
+    rhs_assemble_velocities(rhs, normals, vel)
+    A = lhs.copy(order="F") if return_state else lhs
+    lu, piv = lu_factor(A)
+    x = lu_solve(lu, piv, rhs)
+    gam, deltas, gwake = [], [], []
+    off = 0
+    for s, c in zip(ns, nc):
+        g = x[off:off + s * c].reshape(c, s).copy()
+        off += s * c
+        gam.append(g)
+        deltas.append(gamma_delta(g))
+        gw = np.zeros((1, s), dtype)
+        gw[0] = g[-1]
+        gwake.append(gw)
+    forces = [forces_steady(v, d, u) for v, d, u in zip(verts, deltas, vel)]
+    cl = coeff_cl_multibody(forces, areas, fs, T(rho))
+    cm = coeff_cm_multibody(forces, verts, areas, np.asarray(ref_pt, dtype), fs, T(rho))
+    cdi_num, area_tot = T(0), T(0)
+    for w, gw, a in zip(wake, gwake, areas):
+        area = asum(a)
+        cdi_num += trefftz_cd(w, gw, sigma) / (np.dot(fs, fs) * area) * area
+        area_tot += area
+    out = dict(cl=cl, cdi=T(cdi_num / area_tot), cm=cm, gamma=gam)
+    if return_state:
+        out.update(lhs=lhs, rhs=rhs, colloc=colloc, normals=normals, areas=areas, verts=verts, wake=wake,
+                   forces=forces)
+    return out

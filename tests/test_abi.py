@@ -1,0 +1,36 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/gbvlm.h declares (no compute calls: runs without a GPU)."""
+import os
+import re
+
+from tinyvlm_gb300 import _lib, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gbvlm.h")
+
+
+def declared():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbvlm_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_parses():
+    names = declared()
+    assert "gbvlm_lhs_assemble_f32" in names and "gbvlm_lu_factor_f64" in names
+    assert len(names) > 40
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    missing = [n for n in declared() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_python_prototypes_cover_header():
+    names = set(declared())
+    assert names <= set(_lib.exported_names()) | {"gbvlm_last_error", "gbvlm_version"}, \
+        names - set(_lib.exported_names())
+
+
+def test_library_is_in_tree():
+    assert os.path.dirname(build.LIB) == os.path.dirname(os.path.abspath(_lib.__file__))

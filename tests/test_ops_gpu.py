@@ -1,0 +1,246 @@
+"""Parity of every gbvlm operator (called through the C ABI) with the oracle.
+
+float kernels keep the reference's float semantics; tolerances below are
+float rounding bounds (different but equally valid operation order and FMA
+contraction), double kernels are held to 1e-9."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.helpers import aero_inputs, close, synthetic_wake, wing
+from tinyvlm_gb300 import backend as B
+
+pytestmark = pytest.mark.gpu
+
+DT = [(np.float32, torch.float32), (np.float64, torch.float64)]
+# AIC tolerance: relative 2e-4 plus 2e-5 of the column-set max for float;
+# the double kernel matches the double oracle to ~1e-12
+TOL = {np.float32: (2e-4, 2e-5), np.float64: (1e-9, 1e-12)}
+
+
+def T(a, dev="cuda"):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def H(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("npd,td", DT)
+@pytest.mark.parametrize("kind", ["rect", "ellip", "trap"])
+def test_mesh_metrics(cuda, npd, td, kind):
+    v = wing(kind, 7, 11, npd)
+    for alpha in (0.0, math.radians(7.0)):
+        col, nor, ar = O.mesh_metrics(alpha, [v], npd)
+        be = B.Backend(td)
+        c = torch.zeros((3,) + col[0].shape[1:], dtype=td, device="cuda")
+        n, a = torch.zeros_like(c), torch.zeros(ar[0].shape, dtype=td, device="cuda")
+        be.mesh_metrics(alpha, [T(v)], [c], [n], [a])
+        r = 2e-6 if npd == np.float32 else 1e-13
+        close(H(c), col[0], r, r, "colloc")
+        close(H(n), nor[0], r, r, "normals")
+        close(H(a), ar[0], r, r, "areas")
+
+
+def _steady_geometry(npd, surfaces, alpha=math.radians(4.0)):
+    verts = [s.copy() for s in surfaces]
+    wake = []
+    for v in verts:
+        w = np.zeros((4, 2, v.shape[2]), npd)
+        w[3] = 1
+        wake.append(w)
+    O.wake_shed(verts, wake, 0)
+    tr = O.translation(np.array([-100 * math.cos(alpha), 0, -100 * math.sin(alpha)], npd), npd)
+    for v, vi in zip(verts, surfaces):
+        O.displace_wing(tr, v, vi)
+    O.wake_shed(verts, wake, 1)
+    col, nor, ar = O.mesh_metrics(alpha, verts, npd)
+    return verts, wake, col, nor, ar
+
+
+@pytest.mark.parametrize("npd,td", DT)
+@pytest.mark.parametrize("case", ["single", "split", "ellip"])
+def test_lhs_assemble(cuda, npd, td, case):
+    if case == "single":
+        surf = [wing("trap", 5, 13, npd)]
+    elif case == "ellip":
+        surf = [wing("ellip", 8, 8, npd)]
+    else:
+        from tinyvlm_gb300 import mesh as M
+        a = M.rectangular(3, 4, 1.0, 2.0, 0.0).astype(npd)
+        b = M.rectangular(3, 5, 1.0, 2.5, 2.0).astype(npd)
+        M.quarter_chord(a)
+        M.quarter_chord(b)
+        surf = [a, b]
+    verts, wake, col, nor, ar = _steady_geometry(npd, surf)
+    n = sum(c.shape[1] * c.shape[2] for c in col)
+    for iteration in (0, 1):
+        ref = np.zeros((n, n), npd, order="F")
+        O.lhs_assemble(ref, col, nor, verts, wake, iteration)
+        be = B.Backend(td)
+        lhs = torch.zeros((n, n), dtype=td, device="cuda")
+        be.lhs_assemble(lhs, [T(c) for c in col], [T(x) for x in nor], [T(v) for v in verts], [T(w) for w in wake],
+                        iteration)
+        rt, at = TOL[npd]
+        close(H(lhs).T, ref, rt, at, "lhs it=%d" % iteration)
+
+
+@pytest.mark.parametrize("npd,td", DT)
+def test_rhs_velocities(cuda, npd, td):
+    v = [wing("rect", 4, 6, npd), wing("trap", 3, 5, npd)]
+    col, nor, _ = O.mesh_metrics(0.0, v, npd)
+    vel = [aero_inputs(x, seed=i, dtype=npd)[1] for i, x in enumerate(v)]
+    n = sum(c.shape[1] * c.shape[2] for c in col)
+    ref = np.linspace(-1, 1, n).astype(npd)
+    got = T(ref.copy())
+    O.rhs_assemble_velocities(ref, nor, vel)
+    B.Backend(td).rhs_assemble_velocities(got, [T(x) for x in nor], [T(x) for x in vel])
+    close(H(got), ref, 1e-6 if npd == np.float32 else 1e-14, 1e-7 if npd == np.float32 else 1e-15, "rhs")
+
+
+@pytest.mark.parametrize("npd,td", DT)
+@pytest.mark.parametrize("rows,iteration", [(12, 11), (12, 5), (40, 39)])
+def test_wake_influence(cuda, npd, td, rows, iteration):
+    surf = [wing("rect", 4, 10, npd), wing("trap", 3, 7, npd)]
+    col, nor, _ = O.mesh_metrics(0.0, surf, npd)
+    wakes = [synthetic_wake(s, rows, seed=i, dtype=npd) for i, s in enumerate(surf)]
+    rng = np.random.default_rng(5)
+    gw = [rng.standard_normal((rows - 1, s.shape[2] - 1)).astype(npd) for s in surf]
+    lifting = [True, True]
+    n = sum(c.shape[1] * c.shape[2] for c in col)
+    for lift in (lifting, [False, True]):
+        ref = np.zeros(n, npd)
+        O.rhs_assemble_wake_influence(ref, gw, col, nor, wakes, lift, iteration)
+        got = torch.zeros(n, dtype=td, device="cuda")
+        B.Backend(td).rhs_assemble_wake_influence(got, [T(g) for g in gw], [T(c) for c in col], [T(x) for x in nor],
+                                                  [T(w) for w in wakes], lift, iteration)
+        if npd == np.float32:
+            close(H(got), ref, 2e-4, 2e-5, "wake rhs")
+        else:
+            close(H(got), ref, 1e-10, 1e-12, "wake rhs")
+
+
+@pytest.mark.parametrize("npd,td", DT)
+def test_forces_and_coefficients(cuda, npd, td):
+    v = wing("trap", 6, 9, npd)
+    col, nor, ar = O.mesh_metrics(0.05, [v], npd)
+    g, vel = aero_inputs(v, dtype=npd)
+    gd = O.gamma_delta(g)
+    dg = (0.1 * g).astype(npd)
+    be = B.Backend(td)
+    f = torch.zeros((3,) + g.shape, dtype=td, device="cuda")
+    be.forces_steady(T(v), T(gd), T(vel), f)
+    fr = O.forces_steady(v, gd, vel)
+    r = 2e-6 if npd == np.float32 else 1e-14
+    close(H(f), fr, r, r, "forces_steady")
+    be.forces_unsteady(T(v), T(gd), T(dg), T(vel), T(ar[0]), T(nor[0]), f)
+    fr = O.forces_unsteady(v, gd, dg, vel, ar[0], nor[0])
+    close(H(f), fr, r, r, "forces_unsteady")
+    fs = O.freestream(1.0, 0.07, 0.0, npd)
+    la = O.lift_axis(fs)
+    area = O.asum(ar[0])
+    cl = be.coeff_cl(f, la, fs, 1.0, area)
+    rc = 1e-5 if npd == np.float32 else 1e-12
+    assert abs(cl - O.coeff_cl(fr, la, fs, 1.0, area)) <= rc * abs(O.coeff_cl(fr, la, fs, 1.0, area)) + 1e-6
+    mac = be.mesh_mac(T(v), T(ar[0]))
+    assert abs(mac - O.mesh_mac(v, ar[0])) <= rc * abs(O.mesh_mac(v, ar[0]))
+    ref_pt = np.array([0.25, 0.1, 0.0], npd)
+    cm = be.coeff_cm(f, T(v), ref_pt, fs, 1.0, area, mac)
+    close(cm, O.coeff_cm(fr, v, ref_pt, fs, 1.0, area, O.mesh_mac(v, ar[0])), rc, rc, "cm")
+    assert abs(be.sum(T(ar[0])) - area) <= rc * area
+
+
+@pytest.mark.parametrize("npd,td", DT)
+def test_gamma_wake_from_coeffs(cuda, npd, td):
+    ns, H_, ncols = 7, 3, 40
+    rng = np.random.default_rng(3)
+    co = np.asfortranarray(rng.standard_normal((ns, 2 * H_ + 1))).astype(npd)
+    ref = np.zeros((ncols, ns), npd)
+    O.gamma_wake_from_coeffs(ref, co, H_, 1.3, 2.1, 0.05, 25)
+    got = torch.zeros((ncols, ns), dtype=td, device="cuda")
+    coeffs_t = T(np.ascontiguousarray(co.T))  # column-major (ns, 2H+1) == row-major (2H+1, ns)
+    B.Backend(td).gamma_wake_from_coeffs(got, coeffs_t, H_, 1.3, 2.1, 0.05, 25)
+    close(H(got), ref, 1e-5 if npd == np.float32 else 1e-12, 1e-6 if npd == np.float32 else 1e-13, "gamma_wake")
+
+
+@pytest.mark.parametrize("npd,td", DT)
+def test_displace_and_shed(cuda, npd, td):
+    v = [wing("rect", 3, 4, npd), wing("trap", 2, 3, npd)]
+    rng = np.random.default_rng(2)
+    trs = [np.asfortranarray(np.eye(4) + 0.1 * rng.standard_normal((4, 4))).astype(npd) for _ in v]
+    for t in trs:
+        t[3, :] = [0, 0, 0, 1]
+    ref = [x.copy() for x in v]
+    for r, x, t in zip(ref, v, trs):
+        O.displace_wing(t, r, x)
+    be = B.Backend(td)
+    out = [torch.zeros_like(T(x)) for x in v]
+    be.displace_wing([T(np.ascontiguousarray(t.T)) for t in trs], out, [T(x) for x in v])
+    for o, r in zip(out, ref):
+        close(H(o), r, 1e-6 if npd == np.float32 else 1e-14, 1e-6 if npd == np.float32 else 1e-14, "displace")
+    wakes = [np.zeros((4, 5, x.shape[2]), npd) for x in v]
+    gw = [T(w) for w in wakes]
+    O.wake_shed(ref, wakes, 2)
+    be.wake_shed(out, gw, 2)
+    for a, b in zip(gw, wakes):
+        close(H(a), b, 1e-6, 1e-7, "shed")
+
+
+@pytest.mark.parametrize("npd,td", DT)
+def test_wake_rollup(cuda, npd, td):
+    surf = [wing("rect", 4, 8, npd)]
+    rows, it = 10, 7
+    wakes = [synthetic_wake(surf[0], rows, dtype=npd)]
+    rng = np.random.default_rng(9)
+    gwing = [rng.standard_normal((4, 8)).astype(npd)]
+    gwake = [rng.standard_normal((rows - 1, 8)).astype(npd)]
+    ref = [w.copy() for w in wakes]
+    O.wake_rollup(ref, surf, gwing, gwake, [True], 0.05, it)
+    got = [T(w) for w in wakes]
+    B.Backend(td).wake_rollup(got, [T(s) for s in surf], [T(g) for g in gwing], [T(g) for g in gwake], [True],
+                              0.05, it)
+    close(H(got[0]), ref[0], 1e-5 if npd == np.float32 else 1e-12, 1e-6 if npd == np.float32 else 1e-13, "rollup")
+
+
+@pytest.mark.parametrize("npd,td", DT)
+def test_trefftz(cuda, npd, td):
+    v = wing("ellip", 4, 12, npd)
+    verts, wake, col, nor, ar = _steady_geometry(npd, [v])
+    gw = np.linspace(0.1, 0.5, v.shape[2] - 1).astype(npd)[None, :]
+    fs = O.freestream(1.0, math.radians(4.0), 0.0, npd)
+    area = O.asum(ar[0])
+    ref = O.trefftz_cd(wake[0], gw) / (np.dot(fs, fs) * area)
+    got = B.Backend(td).trefftz_cd(T(wake[0]), T(gw), fs, area)
+    assert abs(got - ref) <= (1e-4 if npd == np.float32 else 1e-10) * abs(ref)
+
+
+@pytest.mark.parametrize("npd,td", DT)
+@pytest.mark.parametrize("n", [1, 5, 31, 32, 33, 64, 97, 200, 513])
+def test_lu(cuda, npd, td, n):
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n)) + n * 0.05 * np.eye(n)
+    b = rng.standard_normal((3, n))
+    be = B.Backend(td)
+    At = T(np.ascontiguousarray(A.T).astype(npd))  # column-major storage
+    X = T(b.astype(npd))
+    lu = be.create_lu_solver()
+    lu.init(At)
+    lu.factorize(At)
+    lu.solve(At, X)
+    ref = np.linalg.solve(A, b.T).T
+    tol = 1e-3 if npd == np.float32 else 1e-9
+    close(H(X), ref, tol, tol, "lu solve n=%d" % n)
+
+
+def test_lu_singular(cuda):
+    n = 8
+    A = np.ones((n, n), np.float32)
+    be = B.Backend(torch.float32)
+    At = T(A)
+    lu = be.create_lu_solver()
+    lu.init(At)
+    with pytest.raises(Exception):
+        lu.factorize(At)

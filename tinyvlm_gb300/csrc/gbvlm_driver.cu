@@ -1,0 +1,355 @@
+// Host drivers above the operator C ABI: the steady VLM simulation
+// (vlm/src/vlm.cpp:17-151) and the plot3d reader (vlm/src/vlm_mesh.cpp).
+// These are the "plain per-solve" paths: one operator call per reference
+// backend call, scalars read back synchronously, in float (the reference's
+// semantics) or double.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "gbvlm_internal.h"
+
+namespace gbvlm {
+
+template <class T>
+__global__ void k_fill3(T* v, int64_t np, T x, T y, T z) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    v[p] = x;
+    v[np + p] = y;
+    v[2 * np + p] = z;
+}
+
+template <class T>
+__global__ void k_cast(const float* in, T* out, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (T)in[i];
+}
+
+template <class T>
+struct Ops;
+#define OPS(T, sfx)                                                                                                  \
+    template <>                                                                                                      \
+    struct Ops<T> {                                                                                                  \
+        static int lhs(T* a, int64_t ld, int32_t ns, const gbvlm_dims* d, const T* const* c, const T* const* n,      \
+                       const T* const* vw, const T* const* vk, int32_t it, T sg, gbvlm_stream s) {                    \
+            return gbvlm_lhs_assemble_##sfx(a, ld, ns, d, c, n, vw, vk, it, sg, s);                                  \
+        }                                                                                                            \
+        static int rhsv(T* r, int32_t ns, const gbvlm_dims* d, const T* const* n, const T* const* v, gbvlm_stream s) { \
+            return gbvlm_rhs_assemble_velocities_##sfx(r, ns, d, n, v, s);                                          \
+        }                                                                                                            \
+        static int metrics(T a, int32_t ns, const gbvlm_dims* d, const T* const* v, T* const* c, T* const* n,        \
+                           T* const* ar, gbvlm_stream s) {                                                           \
+            return gbvlm_mesh_metrics_##sfx(a, ns, d, v, c, n, ar, s);                                              \
+        }                                                                                                            \
+        static int displace(int32_t ns, const gbvlm_dims* d, const T* const* t, T* const* v, const T* const* vi,     \
+                            gbvlm_stream s) {                                                                        \
+            return gbvlm_displace_wing_##sfx(ns, d, t, v, vi, s);                                                   \
+        }                                                                                                            \
+        static int shed(int32_t ns, const gbvlm_dims* d, const T* const* v, T* const* k, int32_t it, gbvlm_stream s) { \
+            return gbvlm_wake_shed_##sfx(ns, d, v, k, it, s);                                                       \
+        }                                                                                                            \
+        static int factor(gbvlm_lu h, T* a, int64_t n, gbvlm_stream s) { return gbvlm_lu_factor_##sfx(h, a, n, n, s); } \
+        static int solve(gbvlm_lu h, const T* a, int64_t n, T* x, gbvlm_stream s) {                                  \
+            return gbvlm_lu_solve_##sfx(h, a, n, n, x, n, 1, s);                                                     \
+        }                                                                                                            \
+        static int gupd(int64_t ns, int64_t nc, const T* x, T* g, T* gd, T* gw, gbvlm_stream s) {                    \
+            return gbvlm_gamma_update_##sfx(ns, nc, x, g, gd, gw, 0, nullptr, nullptr, (T)0, s);                     \
+        }                                                                                                            \
+        static int forces(int64_t ns, int64_t nc, const T* v, const T* gd, const T* vel, T* f, gbvlm_stream s) {     \
+            return gbvlm_forces_steady_##sfx(ns, nc, v, gd, vel, f, s);                                             \
+        }                                                                                                            \
+        static int sum(const T* x, int64_t n, T* o, gbvlm_stream s) { return gbvlm_sum_##sfx(x, n, o, s); }          \
+        static int cl(int64_t ns, int64_t nc, const T* f, const T* la, const T* fs, T rho, T area, T* o,             \
+                      gbvlm_stream s) {                                                                              \
+            return gbvlm_coeff_cl_##sfx(ns, nc, f, la, fs, rho, area, o, s);                                        \
+        }                                                                                                            \
+        static int cm(int64_t ns, int64_t nc, const T* f, const T* v, const T* r, const T* fs, T rho, T area, T mac, \
+                      T* o, gbvlm_stream s) {                                                                        \
+            return gbvlm_coeff_cm_##sfx(ns, nc, f, v, r, fs, rho, area, mac, o, s);                                 \
+        }                                                                                                            \
+        static int mac(int64_t ns, int64_t nc, const T* v, const T* a, T* o, gbvlm_stream s) {                       \
+            return gbvlm_mesh_mac_##sfx(ns, nc, v, a, o, s);                                                        \
+        }                                                                                                            \
+        static int cd(int64_t ns, int64_t nwv, const T* vk, const T* gw, const T* fs, T area, T sg, T* o,            \
+                      gbvlm_stream s) {                                                                              \
+            return gbvlm_trefftz_cd_##sfx(ns, nwv, vk, gw, fs, area, sg, o, s);                                     \
+        }                                                                                                            \
+    };
+OPS(float, f32)
+OPS(double, f64)
+
+// Per-precision simulation state of a steady VLM (vlm/src/vlm.cpp:60-95).
+struct VlmBase {
+    virtual ~VlmBase() = default;
+    virtual int run(double alpha, double beta, double u_inf, double rho, const double* ref_pt, gbvlm_coeffs* out,
+                    double* gamma_out, cudaStream_t st) = 0;
+};
+
+template <class T>
+struct VlmState : VlmBase {
+    int32_t nsurf = 0;
+    std::vector<gbvlm_dims> dims;
+    int64_t n = 0;
+    void* mem = nullptr;
+    std::vector<T*> verts_init, verts, wake, colloc, normals, areas, gamma, gdelta, gwake, vel, forces, transform;
+    T* lhs = nullptr;
+    T* rhs = nullptr;
+    gbvlm_lu lu = nullptr;
+    T sigma = 0;
+
+    ~VlmState() override {
+        if (lu) gbvlm_lu_destroy(lu);
+        if (mem) cudaFree(mem);
+    }
+
+    int init(int32_t ns_, const gbvlm_dims* d, const float* const* vinit_host) {
+        nsurf = ns_;
+        dims.assign(d, d + ns_);
+        size_t bytes = 0;
+        n = 0;
+        for (auto& x : dims) {
+            x.nwv = 2;  // single row of wake panels (vlm.cpp:73)
+            int64_t np = x.ns * x.nc, nv = (x.ns + 1) * (x.nc + 1);
+            n += np;
+            bytes += sizeof(T) * (2 * 4 * nv + 4 * (x.ns + 1) * 2 + 3 * 3 * np + 3 * np + 3 * np + x.ns + 16 + 3 * np);
+        }
+        bytes += sizeof(T) * (n * n + n) + 4096 * 8;
+        GB_CUDA(cudaMalloc(&mem, bytes));
+        GB_CUDA(cudaMemset(mem, 0, bytes));
+        char* p = (char*)mem;
+        auto take = [&](int64_t cnt) {
+            T* r = (T*)p;
+            p += ((sizeof(T) * cnt + 255) / 256) * 256;
+            return r;
+        };
+        lhs = take(n * n);
+        rhs = take(n);
+        for (auto& x : dims) {
+            int64_t np = x.ns * x.nc, nv = (x.ns + 1) * (x.nc + 1);
+            verts_init.push_back(take(4 * nv));
+            verts.push_back(take(4 * nv));
+            wake.push_back(take(4 * (x.ns + 1) * 2));
+            colloc.push_back(take(3 * np));
+            normals.push_back(take(3 * np));
+            areas.push_back(take(np));
+            gamma.push_back(take(np));
+            gdelta.push_back(take(np));
+            gwake.push_back(take(x.ns));
+            vel.push_back(take(3 * np));
+            forces.push_back(take(3 * np));
+            transform.push_back(take(16));
+        }
+        // upload initial vertices (float host) and set wake w = 1
+        for (int m = 0; m < nsurf; m++) {
+            int64_t nv = (dims[m].ns + 1) * (dims[m].nc + 1);
+            float* tmp = nullptr;
+            GB_CUDA(cudaMalloc(&tmp, sizeof(float) * 4 * nv));
+            GB_CUDA(cudaMemcpy(tmp, vinit_host[m], sizeof(float) * 4 * nv, cudaMemcpyHostToDevice));
+            k_cast<T><<<(unsigned)cdiv(4 * nv, 256), 256>>>(tmp, verts_init[m], 4 * nv);
+            GB_LAUNCH_CHECK();
+            GB_CUDA(cudaDeviceSynchronize());
+            cudaFree(tmp);
+            std::vector<T> ones(2 * (dims[m].ns + 1), (T)1);
+            GB_CUDA(cudaMemcpy(wake[m] + 3 * 2 * (dims[m].ns + 1), ones.data(), sizeof(T) * ones.size(),
+                               cudaMemcpyHostToDevice));
+        }
+        int rc = gbvlm_lu_create(&lu);
+        if (rc) return rc;
+        return gbvlm_lu_init(lu, n);
+    }
+
+    int run(double alpha_d, double beta_d, double u_inf_d, double rho_d, const double* ref_pt, gbvlm_coeffs* out,
+            double* gamma_out, cudaStream_t st) override {
+        gbvlm_stream s = (gbvlm_stream)st;
+        const T alpha = (T)alpha_d, beta = (T)beta_d, u = (T)u_inf_d, rho = (T)rho_d;
+        // FlowData (vlm_utils.cpp:5-19)
+        T fs[3] = {u * (T)cos(alpha) * (T)cos(beta), -(u * (T)cos(alpha) * (T)sin(beta)), u * (T)sin(alpha)};
+        T la[3] = {-fs[2], (T)0, fs[0]};
+        T ll = (T)sqrt(la[0] * la[0] + la[1] * la[1] + la[2] * la[2]);
+        la[0] /= ll; la[1] /= ll; la[2] /= ll;
+        GB_CUDA(cudaMemsetAsync(lhs, 0, sizeof(T) * n * n, st));
+        GB_CUDA(cudaMemsetAsync(rhs, 0, sizeof(T) * n, st));
+        for (int m = 0; m < nsurf; m++) {
+            int64_t nv = (dims[m].ns + 1) * (dims[m].nc + 1);
+            GB_CUDA(cudaMemcpyAsync(verts[m], verts_init[m], sizeof(T) * 4 * nv, cudaMemcpyDeviceToDevice, st));
+        }
+        // 100-chord wake (vlm.cpp:104-114)
+        T tr[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, (T)-100 * u * (T)cos(alpha), 0, (T)-100 * u * (T)sin(alpha), 1};
+        for (int m = 0; m < nsurf; m++) GB_CUDA(cudaMemcpyAsync(transform[m], tr, sizeof(tr), cudaMemcpyHostToDevice, st));
+        std::vector<const T*> cverts(verts.begin(), verts.end()), cinit(verts_init.begin(), verts_init.end()),
+            ctr(transform.begin(), transform.end()), ccol(colloc.begin(), colloc.end()),
+            cnor(normals.begin(), normals.end()), cwake(wake.begin(), wake.end()), cvel(vel.begin(), vel.end());
+        int rc;
+        if ((rc = Ops<T>::shed(nsurf, dims.data(), cverts.data(), wake.data(), 0, s))) return rc;
+        if ((rc = Ops<T>::displace(nsurf, dims.data(), ctr.data(), verts.data(), cinit.data(), s))) return rc;
+        if ((rc = Ops<T>::shed(nsurf, dims.data(), cverts.data(), wake.data(), 1, s))) return rc;
+        if ((rc = Ops<T>::metrics(alpha, nsurf, dims.data(), cverts.data(), colloc.data(), normals.data(), areas.data(), s)))
+            return rc;
+        if ((rc = Ops<T>::lhs(lhs, n, nsurf, dims.data(), ccol.data(), cnor.data(), cverts.data(), cwake.data(), 1, sigma, s)))
+            return rc;
+        for (int m = 0; m < nsurf; m++) {
+            int64_t np = dims[m].ns * dims[m].nc;
+            k_fill3<T><<<(unsigned)cdiv(np, 256), 256, 0, st>>>(vel[m], np, fs[0], fs[1], fs[2]);
+            GB_LAUNCH_CHECK();
+        }
+        if ((rc = Ops<T>::rhsv(rhs, nsurf, dims.data(), cnor.data(), cvel.data(), s))) return rc;
+        if ((rc = Ops<T>::factor(lu, lhs, n, s))) return rc;
+        if ((rc = Ops<T>::solve(lu, lhs, n, rhs, s))) return rc;
+        int64_t off = 0;
+        for (int m = 0; m < nsurf; m++) {
+            if ((rc = Ops<T>::gupd(dims[m].ns, dims[m].nc, rhs + off, gamma[m], gdelta[m], gwake[m], s))) return rc;
+            if ((rc = Ops<T>::forces(dims[m].ns, dims[m].nc, verts[m], gdelta[m], vel[m], forces[m], s))) return rc;
+            off += dims[m].ns * dims[m].nc;
+        }
+        // coefficient reductions (vlm_backend.cpp:72-139) + Trefftz drag
+        T ref[3] = {(T)(ref_pt ? ref_pt[0] : 0), (T)(ref_pt ? ref_pt[1] : 0), (T)(ref_pt ? ref_pt[2] : 0)};
+        T cl = 0, ta = 0, tm = 0, cdn = 0;
+        T cm[3] = {0, 0, 0};
+        for (int m = 0; m < nsurf; m++) {
+            int64_t ns = dims[m].ns, nc = dims[m].nc;
+            T area, clm, mac, cmm[3], cdm;
+            if ((rc = Ops<T>::sum(areas[m], ns * nc, &area, s))) return rc;
+            if ((rc = Ops<T>::cl(ns, nc, forces[m], la, fs, rho, area, &clm, s))) return rc;
+            if ((rc = Ops<T>::mac(ns, nc, verts[m], areas[m], &mac, s))) return rc;
+            if ((rc = Ops<T>::cm(ns, nc, forces[m], verts[m], ref, fs, rho, area, mac, cmm, s))) return rc;
+            if ((rc = Ops<T>::cd(ns, 2, wake[m], gwake[m], fs, area, sigma, &cdm, s))) return rc;
+            cl += clm * area;
+            cdn += cdm * area;
+            for (int k = 0; k < 3; k++) cm[k] += cmm[k] * area * mac;
+            ta += area;
+            tm += mac;
+        }
+        out->cl = (double)(cl / ta);
+        out->cdi = (double)(cdn / ta);
+        for (int k = 0; k < 3; k++) out->cm[k] = (double)(cm[k] / (ta * tm));
+        if (gamma_out) {
+            std::vector<T> h(n);
+            GB_CUDA(cudaMemcpyAsync(h.data(), rhs, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+            GB_CUDA(cudaStreamSynchronize(st));
+            for (int64_t i = 0; i < n; i++) gamma_out[i] = (double)h[i];
+        }
+        return GBVLM_OK;
+    }
+};
+
+}  // namespace gbvlm
+
+using namespace gbvlm;
+
+struct gbvlm_vlm_s {
+    VlmBase* impl = nullptr;
+};
+
+extern "C" {
+
+int gbvlm_vlm_create(gbvlm_vlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                     int32_t precision) {
+    GB_REQUIRE(out && dims && verts_init, "null argument");
+    GB_REQUIRE(nsurf >= 1 && nsurf <= GBVLM_MAX_SURFACES, "nsurf=%d outside [1, %d]", nsurf, GBVLM_MAX_SURFACES);
+    GB_REQUIRE(precision == 32 || precision == 64, "precision must be 32 or 64");
+    for (int m = 0; m < nsurf; m++) {
+        GB_REQUIRE(verts_init[m], "verts_init[%d] is null", m);
+        GB_REQUIRE(dims[m].ns >= 1 && dims[m].nc >= 1, "surface %d has bad sizes", m);
+    }
+    auto* h = new gbvlm_vlm_s();
+    int rc;
+    if (precision == 32) {
+        auto* s = new VlmState<float>();
+        h->impl = s;
+        rc = s->init(nsurf, dims, verts_init);
+    } else {
+        auto* s = new VlmState<double>();
+        h->impl = s;
+        rc = s->init(nsurf, dims, verts_init);
+    }
+    if (rc) {
+        delete h->impl;
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBVLM_OK;
+}
+
+int gbvlm_vlm_destroy(gbvlm_vlm h) {
+    if (!h) return GBVLM_OK;
+    delete h->impl;
+    delete h;
+    return GBVLM_OK;
+}
+
+int gbvlm_vlm_run(gbvlm_vlm h, double alpha, double beta, double u_inf, double rho, const double* ref_pt,
+                  gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream) {
+    GB_REQUIRE(h && h->impl && out, "null argument");
+    return h->impl->run(alpha, beta, u_inf, rho, ref_pt, out, gamma_out, to_cuda(stream));
+}
+
+int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts) {
+    GB_REQUIRE(path && dims, "null argument");
+    std::ifstream f(path);
+    if (!f.is_open()) {
+        set_error("Failed to open mesh file %s", path);
+        return GBVLM_ERR_IO;
+    }
+    long long blocks = 0, ni = 0, nj = 0, nk = 0;
+    f >> blocks;
+    if (blocks != 1) {
+        set_error("Only single block plot3d mesh is supported");
+        return GBVLM_ERR_IO;
+    }
+    f >> ni >> nj >> nk;
+    if (nk != 1 || ni < 2 || nj < 2 || !f) {
+        set_error("Only 2D plot3d mesh is supported");
+        return GBVLM_ERR_IO;
+    }
+    dims->nc = ni - 1;
+    dims->ns = nj - 1;
+    dims->nwv = 0;
+    if (!verts) return GBVLM_OK;
+    // reference tensor (nj, ni, 4): span index fastest (vlm_mesh.cpp:61-78)
+    const int64_t nv = ni * nj;
+    for (int k = 0; k < 3; k++) {
+        for (long long j = 0; j < nj; j++) {
+            for (long long i = 0; i < ni; i++) {
+                double x;
+                if (!(f >> x)) {
+                    set_error("plot3d file %s ended early", path);
+                    return GBVLM_ERR_IO;
+                }
+                verts[k * nv + j + i * nj] = (float)x;
+            }
+        }
+    }
+    for (int64_t q = 0; q < nv; q++) verts[3 * nv + q] = 1.0f;
+    const float first_y = verts[nv];
+    for (long long i = 1; i < ni; i++) {
+        if (verts[nv + i * nj] != first_y) {
+            set_error("Mesh vertices should be ordered in chordwise direction");
+            return GBVLM_ERR_IO;
+        }
+    }
+    if (quarter_chord) {
+        // vlm_mesh.cpp:16-32
+        for (long long i = 0; i + 1 < ni; i++)
+            for (long long j = 0; j < nj; j++)
+                for (int k = 0; k < 3; k++) {
+                    float* a = &verts[k * nv + j + i * nj];
+                    a[0] = 0.75f * a[0] + 0.25f * a[nj];
+                }
+        const long long i = ni - 2;
+        for (long long j = 0; j < nj; j++)
+            for (int k = 0; k < 3; k++) {
+                float* a = &verts[k * nv + j + i * nj];
+                a[nj] = (4.f / 3.f) * a[nj] - (1.f / 3.f) * a[0];
+            }
+    }
+    return GBVLM_OK;
+}
+
+}  // extern "C"

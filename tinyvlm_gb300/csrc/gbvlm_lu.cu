@@ -1,0 +1,652 @@
+// Dense LU with partial pivoting for one matrix or a ragged batch of
+// matrices ("variable-size batched" right-looking LU), plus multi-RHS
+// triangular solves and mixed-precision iterative refinement.
+//
+// Replaces vlm::LU (vlm/include/vlm_backend.hpp:99-119), i.e. LAPACKE
+// ?getrf/?getrs on the CPU backend (vlm_backend_cpu_lapack.cpp:40-94) and
+// cuSOLVER on the CUDA backend (vlm_backend_cuda_solvers.cu:39-102).
+//
+// Panel step k of every system with n > k runs in the same launches, so a
+// batch of uneven systems fills the GPU with the trailing updates of all of
+// them at once:
+//   panel  : one CTA per active system factors columns [k, k+nb) (pivot
+//            search = largest |a|, first row on ties, like LAPACK i?amax)
+//   swap   : the panel's row interchanges applied to the other columns
+//   trsm   : U12 = L11^-1 A12 (unit lower, L11 staged in shared memory)
+//   update : A22 -= L21 U12, 64x64 register-tiled tiles enumerated over all
+//            systems through a per-step prefix table
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "gbvlm_internal.h"
+#include "gbvlm_lu.h"
+
+namespace gbvlm {
+
+constexpr int PANEL_THREADS = 512;
+constexpr int TRSM_COLS = 128;
+constexpr int GT = 64;  // update tile edge
+constexpr int GK = LU_NB;
+
+template <class T>
+__device__ __forceinline__ T tabs(T x) { return x < (T)0 ? -x : x; }
+
+// ---------------------------------------------------------------------------
+// panel: CTA b handles system act[b]
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) k_panel(LuBatch<T> B, int64_t k, const int32_t* act) {
+    const int32_t sid = act[blockIdx.x];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    T* A = B.A[sid];
+    int32_t* ipiv = B.ipiv[sid];
+    const int nb = (int)min((int64_t)GK, n - k);
+    __shared__ T s_val[PANEL_THREADS / 32];
+    __shared__ int64_t s_idx[PANEL_THREADS / 32];
+    __shared__ int64_t s_piv;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int jj = 0; jj < nb; jj++) {
+        const int64_t col = k + jj;
+        T* c = A + col * ld;
+        T best = (T)-1;
+        int64_t bi = col;
+        for (int64_t r = col + tid; r < n; r += PANEL_THREADS) {
+            T v = tabs(c[r]);
+            if (v > best) { best = v; bi = r; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            T ov = __shfl_down_sync(0xffffffffu, best, o);
+            int64_t oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            T bv = s_val[0];
+            int64_t bix = s_idx[0];
+            for (int w = 1; w < PANEL_THREADS / 32; w++) {
+                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bix)) { bv = s_val[w]; bix = s_idx[w]; }
+            }
+            s_piv = bix;
+            ipiv[col] = (int32_t)bix;
+            if (c[bix] == (T)0 && B.info[sid] == 0) B.info[sid] = (int32_t)(col + 1);
+        }
+        __syncthreads();
+        const int64_t p = s_piv;
+        if (p != col) {
+            for (int t = tid; t < nb; t += PANEL_THREADS) {
+                T* a = A + (k + t) * ld;
+                T tmp = a[col];
+                a[col] = a[p];
+                a[p] = tmp;
+            }
+        }
+        __syncthreads();
+        const T d = c[col];
+        if (d != (T)0) {
+            for (int64_t r = col + 1 + tid; r < n; r += PANEL_THREADS) c[r] = c[r] / d;
+        }
+        __syncthreads();
+        for (int64_t r = col + 1 + tid; r < n; r += PANEL_THREADS) {
+            const T l = c[r];
+            for (int t = jj + 1; t < nb; t++) {
+                T* a = A + (k + t) * ld;
+                a[r] -= l * a[col];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// swap: one thread per column outside the panel, per system.  col table:
+// blocks enumerated through prefix pfx (over act).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_block(const int64_t* pfx, int cnt, int64_t b) {
+    int lo = 0, hi = cnt - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pfx[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <class T>
+__global__ void k_swap(LuBatch<T> B, int64_t k, const int32_t* act, const int64_t* pfx, int cnt) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t tot = pfx[cnt];
+    if (g >= tot) return;
+    const int a = find_block(pfx, cnt, g);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    const int nb = (int)min((int64_t)GK, n - k);
+    int64_t j = g - pfx[a];  // 0 .. n-nb-1
+    if (j >= k) j += nb;     // skip the panel columns
+    T* col = B.A[sid] + j * ld;
+    const int32_t* ip = B.ipiv[sid];
+    for (int t = 0; t < nb; t++) {
+        const int64_t r = k + t, p = ip[r];
+        if (p != r) {
+            T tmp = col[r];
+            col[r] = col[p];
+            col[p] = tmp;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// trsm: U12 = L11^-1 A12, one thread per column, TRSM_COLS columns per block
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(TRSM_COLS) k_trsm(LuBatch<T> B, int64_t k, const int32_t* act, const int64_t* pfx,
+                                                   int cnt) {
+    __shared__ T L[GK][GK + 1];
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    T* A = B.A[sid];
+    const int nb = (int)min((int64_t)GK, n - k);
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+        int r = t % nb, c = t / nb;
+        L[r][c] = A[(k + r) + (k + c) * ld];
+    }
+    __syncthreads();
+    const int64_t j = k + nb + (int64_t)(blockIdx.x - pfx[a]) * TRSM_COLS + threadIdx.x;
+    if (j >= n) return;
+    T x[GK];
+    T* col = A + j * ld + k;
+#pragma unroll
+    for (int r = 0; r < GK; r++) x[r] = r < nb ? col[r] : (T)0;
+#pragma unroll
+    for (int r = 1; r < GK; r++) {
+        if (r < nb) {
+            T s = x[r];
+#pragma unroll
+            for (int l = 0; l < r; l++) s -= L[r][l] * x[l];
+            x[r] = s;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < GK; r++)
+        if (r < nb) col[r] = x[r];
+}
+
+// ---------------------------------------------------------------------------
+// update: A22 -= L21 * U12 on 64x64 tiles, 256 threads, 4x4 per thread
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const int32_t* act, const int64_t* pfx,
+                                               int cnt) {
+    __shared__ T sA[GK][GT + 1];  // L21 tile: [kk][row]
+    __shared__ T sB[GK][GT + 1];  // U12 tile: [kk][col]
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    T* A = B.A[sid];
+    const int64_t m = n - k - GK;  // trailing size (systems here have n > k + GK)
+    const int64_t tiles = (m + GT - 1) / GT;
+    const int64_t t = blockIdx.x - pfx[a];
+    const int64_t r0 = k + GK + (t % tiles) * GT, c0 = k + GK + (t / tiles) * GT;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < GK * GT; e += 256) {
+        int kk = e / GT, rr = e % GT;
+        int64_t r = r0 + rr;
+        sA[kk][rr] = r < n ? A[r + (k + kk) * ld] : (T)0;
+        int cc = e / GK, k2 = e % GK;  // coalesced along kk for U12 (column-major rows k..k+GK)
+        int64_t c = c0 + cc;
+        sB[k2][cc] = c < n ? A[(k + k2) + c * ld] : (T)0;
+    }
+    __syncthreads();
+    const int tx = tid % 16, ty = tid / 16;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0;
+#pragma unroll 8
+    for (int kk = 0; kk < GK; kk++) {
+        T av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) av[i] = sA[kk][tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; j++) bv[j] = sB[kk][ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[i][j] += av[i] * bv[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int64_t c = c0 + ty + 16 * j;
+        if (c >= n) continue;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int64_t r = r0 + tx + 16 * i;
+            if (r < n) A[r + c * ld] -= acc[i][j];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves: one CTA per system, all its right-hand sides
+// ---------------------------------------------------------------------------
+constexpr int TS_THREADS = 256;
+constexpr int TS_MAXRHS = 8;
+
+template <class T>
+__global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rhs0, int32_t nrhs_blk) {
+    const int32_t sid = blockIdx.x;
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    const T* A = B.A[sid];
+    const int32_t nr = (int32_t)min((int64_t)nrhs_blk, (int64_t)B.nrhs[sid] - rhs0);
+    if (nr <= 0) return;
+    T* X = B.X[sid] + (int64_t)rhs0 * B.ldx[sid];
+    const int64_t ldx = B.ldx[sid];
+    const int32_t* ip = B.ipiv[sid];
+    __shared__ T xs[GK][TS_MAXRHS];
+    const int tid = threadIdx.x;
+    // row interchanges
+    if (tid < nr) {
+        T* x = X + tid * ldx;
+        for (int64_t r = 0; r < n; r++) {
+            int64_t p = ip[r];
+            if (p != r) { T t = x[r]; x[r] = x[p]; x[p] = t; }
+        }
+    }
+    __syncthreads();
+    // forward: L (unit lower)
+    for (int64_t k = 0; k < n; k += GK) {
+        const int nb = (int)min((int64_t)GK, n - k);
+        if (tid < nr) {
+            T* x = X + tid * ldx;
+            for (int r = 0; r < nb; r++) {
+                T s = x[k + r];
+                for (int l = 0; l < r; l++) s -= A[(k + r) + (k + l) * ld] * xs[l][tid];
+                xs[r][tid] = s;
+                x[k + r] = s;
+            }
+        }
+        __syncthreads();
+        for (int64_t r = k + nb + tid; r < n; r += TS_THREADS) {
+            T acc[TS_MAXRHS];
+#pragma unroll
+            for (int q = 0; q < TS_MAXRHS; q++) acc[q] = 0;
+            for (int l = 0; l < nb; l++) {
+                const T a = A[r + (k + l) * ld];
+#pragma unroll
+                for (int q = 0; q < TS_MAXRHS; q++) acc[q] += a * xs[l][q];
+            }
+            for (int q = 0; q < nr; q++) X[r + q * ldx] -= acc[q];
+        }
+        __syncthreads();
+    }
+    // backward: U
+    const int64_t nblk = (n + GK - 1) / GK;
+    for (int64_t bk = nblk - 1; bk >= 0; bk--) {
+        const int64_t k = bk * GK;
+        const int nb = (int)min((int64_t)GK, n - k);
+        if (tid < nr) {
+            T* x = X + tid * ldx;
+            for (int r = nb - 1; r >= 0; r--) {
+                T s = x[k + r];
+                for (int l = r + 1; l < nb; l++) s -= A[(k + r) + (k + l) * ld] * xs[l][tid];
+                s = s / A[(k + r) + (k + r) * ld];
+                xs[r][tid] = s;
+                x[k + r] = s;
+            }
+        }
+        __syncthreads();
+        for (int64_t r = tid; r < k; r += TS_THREADS) {
+            T acc[TS_MAXRHS];
+#pragma unroll
+            for (int q = 0; q < TS_MAXRHS; q++) acc[q] = 0;
+            for (int l = 0; l < nb; l++) {
+                const T a = A[r + (k + l) * ld];
+#pragma unroll
+                for (int q = 0; q < TS_MAXRHS; q++) acc[q] += a * xs[l][q];
+            }
+            for (int q = 0; q < nr; q++) X[r + q * ldx] -= acc[q];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host plan
+// ---------------------------------------------------------------------------
+template <class T>
+int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
+    for (size_t s = 0; s < plan.steps.size(); s++) {
+        const LuStep& S = plan.steps[s];
+        if (S.n_panel == 0) continue;
+        k_panel<T><<<S.n_panel, PANEL_THREADS, 0, st>>>(B, S.k, plan.d_act + S.act_off);
+        GB_LAUNCH_CHECK();
+        if (S.swap_total > 0) {
+            k_swap<T><<<(unsigned)cdiv(S.swap_total, 256), 256, 0, st>>>(B, S.k, plan.d_act + S.act_off,
+                                                                       plan.d_pfx + S.swap_pfx, S.n_panel);
+            GB_LAUNCH_CHECK();
+        }
+        if (S.trsm_blocks > 0) {
+            k_trsm<T><<<(unsigned)S.trsm_blocks, TRSM_COLS, 0, st>>>(B, S.k, plan.d_act + S.act_off,
+                                                                   plan.d_pfx + S.trsm_pfx, S.n_panel);
+            GB_LAUNCH_CHECK();
+        }
+        if (S.upd_blocks > 0) {
+            k_update<T><<<(unsigned)S.upd_blocks, 256, 0, st>>>(B, S.k, plan.d_act + S.act_off + S.upd_act_skip,
+                                                              plan.d_pfx + S.upd_pfx, S.n_upd);
+            GB_LAUNCH_CHECK();
+        }
+    }
+    return GBVLM_OK;
+}
+
+template <class T>
+int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, cudaStream_t st) {
+    for (int32_t r0 = 0; r0 < max_nrhs; r0 += TS_MAXRHS) {
+        k_trsolve<T><<<nsys, TS_THREADS, 0, st>>>(B, r0, TS_MAXRHS);
+        GB_LAUNCH_CHECK();
+    }
+    return GBVLM_OK;
+}
+
+template int lu_batch_factor<float>(const LuBatch<float>&, const LuPlan&, cudaStream_t);
+template int lu_batch_factor<double>(const LuBatch<double>&, const LuPlan&, cudaStream_t);
+template int lu_batch_solve<float>(const LuBatch<float>&, int32_t, int32_t, cudaStream_t);
+template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, cudaStream_t);
+
+// Build the per-step tables.  Systems must be sorted by n descending so the
+// active systems of every step form a prefix of the order.
+int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st) {
+    plan.release();
+    const int nsys = (int)n_sorted.size();
+    for (int i = 1; i < nsys; i++) GB_REQUIRE(n_sorted[i] <= n_sorted[i - 1], "lu plan: sizes not sorted");
+    std::vector<int32_t> act;
+    std::vector<int64_t> pfx;
+    const int64_t maxn = nsys ? n_sorted[0] : 0;
+    for (int64_t k = 0; k < maxn; k += GK) {
+        LuStep S;
+        S.k = k;
+        S.act_off = (int64_t)act.size();
+        int cnt = 0;
+        while (cnt < nsys && n_sorted[cnt] > k) cnt++;
+        for (int i = 0; i < cnt; i++) act.push_back(i);
+        S.n_panel = cnt;
+        // swap: columns outside the panel, n - nb each
+        S.swap_pfx = (int64_t)pfx.size();
+        int64_t acc = 0;
+        for (int i = 0; i < cnt; i++) {
+            pfx.push_back(acc);
+            acc += n_sorted[i] - std::min<int64_t>(GK, n_sorted[i] - k);
+        }
+        pfx.push_back(acc);
+        S.swap_total = acc;
+        // trsm: blocks of TRSM_COLS over columns k+nb .. n
+        S.trsm_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < cnt; i++) {
+            pfx.push_back(acc);
+            int64_t m = n_sorted[i] - k - std::min<int64_t>(GK, n_sorted[i] - k);
+            acc += m > 0 ? cdiv(m, TRSM_COLS) : 0;
+        }
+        pfx.push_back(acc);
+        S.trsm_blocks = acc;
+        // update: systems with n > k + GK (a prefix), tiles GT x GT
+        int cu = 0;
+        while (cu < cnt && n_sorted[cu] > k + GK) cu++;
+        S.n_upd = cu;
+        S.upd_act_skip = 0;
+        S.upd_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < cu; i++) {
+            pfx.push_back(acc);
+            int64_t t = cdiv(n_sorted[i] - k - GK, GT);
+            acc += t * t;
+        }
+        pfx.push_back(acc);
+        S.upd_blocks = acc;
+        plan.steps.push_back(S);
+    }
+    if (!act.empty()) {
+        GB_CUDA(cudaMalloc(&plan.d_act, act.size() * sizeof(int32_t)));
+        GB_CUDA(cudaMemcpyAsync(plan.d_act, act.data(), act.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    }
+    if (!pfx.empty()) {
+        GB_CUDA(cudaMalloc(&plan.d_pfx, pfx.size() * sizeof(int64_t)));
+        GB_CUDA(cudaMemcpyAsync(plan.d_pfx, pfx.data(), pfx.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    }
+    GB_CUDA(cudaStreamSynchronize(st));
+    return GBVLM_OK;
+}
+
+void LuPlan::release() {
+    if (d_act) cudaFree(d_act);
+    if (d_pfx) cudaFree(d_pfx);
+    d_act = nullptr;
+    d_pfx = nullptr;
+    steps.clear();
+}
+
+// ---------------------------------------------------------------------------
+// mixed-precision refinement helpers
+// ---------------------------------------------------------------------------
+// R = B - A X   (A float n x n col-major, X/B/R double), grid (row blocks, rhs)
+__global__ void k_residual(const float* A, int64_t n, int64_t ld, const double* X, int64_t ldx, const double* Bm,
+                           int64_t ldb, double* R, int64_t ldr) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (r >= n) return;
+    const double* x = X + q * ldx;
+    double s = 0, c = 0;
+    for (int64_t j = 0; j < n; j++) {
+        double p = (double)A[r + j * ld] * x[j];
+        double t = s + p;
+        c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
+        s = t;
+    }
+    R[r + q * ldr] = Bm[r + q * ldb] - (s + c);
+}
+
+__global__ void k_d2f(const double* in, int64_t n, int64_t ldi, float* out, int64_t ldo) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) out[r + blockIdx.y * ldo] = (float)in[r + blockIdx.y * ldi];
+}
+
+__global__ void k_axpy_f2d(const float* d, int64_t n, int64_t ldd, double* x, int64_t ldx, double* maxupd) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double v = (double)d[r + blockIdx.y * ldd];
+    x[r + blockIdx.y * ldx] += v;
+    if (maxupd) {
+        unsigned long long* p = (unsigned long long*)maxupd;
+        double a = fabs(v);
+        atomicMax(p, __double_as_longlong(a));  // non-negative doubles order like their bit patterns
+    }
+}
+
+
+template <class T>
+int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv, int32_t* info, T* X, int64_t ldx,
+                      int32_t nrhs, void** work, size_t* work_bytes, cudaStream_t st) {
+    struct Tab {
+        int64_t n, ld, ldx;
+        T* A;
+        int32_t* ipiv;
+        T* X;
+        int32_t nrhs;
+    } tab{n, ld, ldx, A, ipiv, X, nrhs};
+    if (*work_bytes < sizeof(Tab)) {
+        if (*work) cudaFree(*work);
+        *work = nullptr;
+        GB_CUDA(cudaMalloc(work, 256));
+        *work_bytes = 256;
+    }
+    // pageable source: the call returns once the table is staged, so the
+    // stack copy may go out of scope
+    GB_CUDA(cudaMemcpyAsync(*work, &tab, sizeof(Tab), cudaMemcpyHostToDevice, st));
+    Tab* d = (Tab*)*work;
+    B.n = &d->n;
+    B.ld = &d->ld;
+    B.ldx = &d->ldx;
+    B.A = &d->A;
+    B.ipiv = &d->ipiv;
+    B.X = &d->X;
+    B.nrhs = &d->nrhs;
+    B.info = info;
+    return GBVLM_OK;
+}
+template int make_single_batch<float>(LuBatch<float>&, int64_t, int64_t, float*, int32_t*, int32_t*, float*, int64_t,
+                                      int32_t, void**, size_t*, cudaStream_t);
+template int make_single_batch<double>(LuBatch<double>&, int64_t, int64_t, double*, int32_t*, int32_t*, double*,
+                                       int64_t, int32_t, void**, size_t*, cudaStream_t);
+
+}  // namespace gbvlm
+
+using namespace gbvlm;
+
+struct gbvlm_lu_s {
+    int64_t n = 0;
+    int32_t* d_ipiv = nullptr;
+    int32_t* d_info = nullptr;
+    LuPlan plan;
+    int64_t plan_n = -1;
+    void* work = nullptr;
+    size_t work_bytes = 0;
+};
+
+static int lu_ensure(gbvlm_lu h, int64_t n, cudaStream_t st) {
+    if (h->plan_n == n && h->d_ipiv) return GBVLM_OK;
+    if (h->d_ipiv) cudaFree(h->d_ipiv);
+    if (h->d_info) cudaFree(h->d_info);
+    h->d_ipiv = nullptr;
+    h->d_info = nullptr;
+    GB_CUDA(cudaMalloc(&h->d_ipiv, sizeof(int32_t) * (n > 0 ? n : 1)));
+    GB_CUDA(cudaMalloc(&h->d_info, sizeof(int32_t)));
+    std::vector<int64_t> ns(1, n);
+    int rc = lu_plan_build(h->plan, ns, st);
+    if (rc) return rc;
+    h->plan_n = n;
+    h->n = n;
+    return GBVLM_OK;
+}
+
+template <class T>
+static int lu_factor_one(gbvlm_lu h, T* A, int64_t n, int64_t ld, cudaStream_t st) {
+    GB_REQUIRE(h && A && n >= 1 && ld >= n, "bad LU arguments");
+    int rc = lu_ensure(h, n, st);
+    if (rc) return rc;
+    GB_CUDA(cudaMemsetAsync(h->d_info, 0, sizeof(int32_t), st));
+    LuBatch<T> B;
+    rc = make_single_batch<T>(B, n, ld, A, h->d_ipiv, h->d_info, nullptr, 0, 0, &h->work, &h->work_bytes, st);
+    if (rc) return rc;
+    rc = lu_batch_factor<T>(B, h->plan, st);
+    if (rc) return rc;
+    int32_t* hi = (int32_t*)host_scratch(sizeof(int32_t));
+    GB_CUDA(cudaMemcpyAsync(hi, h->d_info, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (*hi != 0) {
+        set_error("LU: exactly zero pivot at column %d", *hi);
+        return GBVLM_ERR_SINGULAR;
+    }
+    return GBVLM_OK;
+}
+
+template <class T>
+static int lu_solve_one(gbvlm_lu h, const T* A, int64_t n, int64_t ld, T* X, int64_t ldx, int64_t nrhs,
+                        cudaStream_t st) {
+    GB_REQUIRE(h && A && X && n >= 1 && ld >= n && ldx >= n && nrhs >= 1, "bad LU solve arguments");
+    GB_REQUIRE(h->plan_n == n, "LU solve before factorize for this size");
+    LuBatch<T> B;
+    int rc = make_single_batch<T>(B, n, ld, (T*)A, h->d_ipiv, h->d_info, X, ldx, (int32_t)nrhs, &h->work,
+                                  &h->work_bytes, st);
+    if (rc) return rc;
+    return lu_batch_solve<T>(B, 1, (int32_t)nrhs, st);
+}
+
+extern "C" {
+
+int gbvlm_lu_create(gbvlm_lu* out) {
+    GB_REQUIRE(out != nullptr, "out is null");
+    *out = new gbvlm_lu_s();
+    return GBVLM_OK;
+}
+
+int gbvlm_lu_destroy(gbvlm_lu h) {
+    if (!h) return GBVLM_OK;
+    if (h->d_ipiv) cudaFree(h->d_ipiv);
+    if (h->d_info) cudaFree(h->d_info);
+    if (h->work) cudaFree(h->work);
+    h->plan.release();
+    delete h;
+    return GBVLM_OK;
+}
+
+int gbvlm_lu_init(gbvlm_lu h, int64_t n) {
+    GB_REQUIRE(h && n >= 1, "bad LU init arguments");
+    return lu_ensure(h, n, 0);
+}
+
+int gbvlm_lu_factor_f32(gbvlm_lu h, float* A, int64_t n, int64_t ld, gbvlm_stream s) {
+    return lu_factor_one<float>(h, A, n, ld, to_cuda(s));
+}
+int gbvlm_lu_factor_f64(gbvlm_lu h, double* A, int64_t n, int64_t ld, gbvlm_stream s) {
+    return lu_factor_one<double>(h, A, n, ld, to_cuda(s));
+}
+int gbvlm_lu_solve_f32(gbvlm_lu h, const float* A, int64_t n, int64_t ld, float* X, int64_t ldx, int64_t nrhs,
+                       gbvlm_stream s) {
+    return lu_solve_one<float>(h, A, n, ld, X, ldx, nrhs, to_cuda(s));
+}
+int gbvlm_lu_solve_f64(gbvlm_lu h, const double* A, int64_t n, int64_t ld, double* X, int64_t ldx, int64_t nrhs,
+                       gbvlm_stream s) {
+    return lu_solve_one<double>(h, A, n, ld, X, ldx, nrhs, to_cuda(s));
+}
+
+int gbvlm_lu_solve_refined(gbvlm_lu h, const float* LU, const float* A, int64_t n, int64_t ld, const double* Bm,
+                           double* X, int64_t nrhs, int32_t iters, double* last_update, gbvlm_stream s) {
+    GB_REQUIRE(h && LU && A && Bm && X && n >= 1 && ld >= n && nrhs >= 1 && nrhs <= 65535 && iters >= 0,
+               "bad refined-solve arguments");
+    GB_REQUIRE(h->plan_n == n, "refined solve before factorize for this size");
+    cudaStream_t st = to_cuda(s);
+    // workspace: float n*nrhs + double n*nrhs + 1 double
+    size_t need = sizeof(float) * n * nrhs + sizeof(double) * (n * nrhs + 1);
+    void* ws = nullptr;
+    int rc = device_scratch(need, &ws, st);
+    if (rc) return rc;
+    float* xf = (float*)ws;
+    double* R = (double*)((char*)ws + ((sizeof(float) * n * nrhs + 7) / 8) * 8);
+    double* dmax = R + n * nrhs;
+    dim3 g((unsigned)cdiv(n, 256), (unsigned)nrhs);
+    // x0 = LU^-1 b in float
+    k_d2f<<<g, 256, 0, st>>>(Bm, n, n, xf, n);
+    GB_LAUNCH_CHECK();
+    rc = gbvlm_lu_solve_f32(h, LU, n, ld, xf, n, nrhs, s);
+    if (rc) return rc;
+    GB_CUDA(cudaMemsetAsync(X, 0, sizeof(double) * n * nrhs, st));
+    k_axpy_f2d<<<g, 256, 0, st>>>(xf, n, n, X, n, nullptr);
+    GB_LAUNCH_CHECK();
+    for (int it = 0; it < iters; it++) {
+        k_residual<<<g, 256, 0, st>>>(A, n, ld, X, n, Bm, n, R, n);
+        GB_LAUNCH_CHECK();
+        k_d2f<<<g, 256, 0, st>>>(R, n, n, xf, n);
+        GB_LAUNCH_CHECK();
+        rc = gbvlm_lu_solve_f32(h, LU, n, ld, xf, n, nrhs, s);
+        if (rc) return rc;
+        if (it == iters - 1 && last_update) GB_CUDA(cudaMemsetAsync(dmax, 0, sizeof(double), st));
+        k_axpy_f2d<<<g, 256, 0, st>>>(xf, n, n, X, n, (it == iters - 1 && last_update) ? dmax : nullptr);
+        GB_LAUNCH_CHECK();
+    }
+    if (last_update) {
+        if (iters == 0) {
+            *last_update = 0;
+        } else {
+            GB_CUDA(cudaMemcpyAsync(last_update, dmax, sizeof(double), cudaMemcpyDeviceToHost, st));
+            GB_CUDA(cudaStreamSynchronize(st));
+        }
+    }
+    return GBVLM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+// Device math shared by the gbvlm kernels: 3-vectors, the Biot-Savart
+// straight-segment law in reference order (for the per-operator parity
+// kernels) and the factored "relative-vector" form used by the tiled
+// assembly, wake and roll-up kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbvlm {
+
+// vlm/include/vlm_types.hpp:22-24 and vlm_backend_cpu_kernels.ispc:9-12
+constexpr float PI_F = 3.141593f;
+constexpr float EPS_F = 1.19209e-07f;
+constexpr float RCUT_SQ = 1e-10f;   // |r1 x r2|^2 cut-off (both precisions)
+constexpr float RCUT_NORM_F = 1e-5f; // |r1|, |r2| cut-off, float kernels
+constexpr double RCUT_NORM_D = 1e-10; // |r1|, |r2| cut-off, double kernels
+
+template <class T> struct V3 { T x, y, z; };
+
+template <class T> __host__ __device__ __forceinline__ V3<T> v3(T x, T y, T z) { return V3<T>{x, y, z}; }
+template <class T> __host__ __device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> __host__ __device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> __host__ __device__ __forceinline__ V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class T> __host__ __device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> __host__ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class T> __host__ __device__ __forceinline__ T len2(V3<T> a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+
+template <class T> __device__ __forceinline__ T dsqrt(T x);
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
+
+template <class T> struct Prec;
+template <> struct Prec<float> {
+    static constexpr float rcut_norm = RCUT_NORM_F;
+    __device__ static float fourpi() { return 4.0f * PI_F; }
+};
+template <> struct Prec<double> {
+    static constexpr double rcut_norm = RCUT_NORM_D;
+    // the reference's double kernel still forms 4*pi as the float product
+    __device__ static double fourpi() { return (double)(4.0f * PI_F); }
+};
+
+// Katz-Plotkin eq. 10.115 in the reference's evaluation order
+// (vlm_backend_cpu_kernels.ispc:69-89 float, :383-402 double).
+template <class T>
+__device__ __forceinline__ V3<T> biosavart_ref(V3<T> c, V3<T> a, V3<T> b, T sigma) {
+    V3<T> r0 = b - a, r1 = c - a, r2 = c - b;
+    V3<T> cr = cross(r1, r2);
+    T r1n = dsqrt(len2(r1)), r2n = dsqrt(len2(r2));
+    T sq = len2(cr);
+    if (sq < (T)RCUT_SQ || r1n < Prec<T>::rcut_norm || r2n < Prec<T>::rcut_norm) return {0, 0, 0};
+    T sm = sigma * sigma * len2(r0);
+    T coeff = (dot(r0, r1) * r2n - dot(r0, r2) * r1n) / (Prec<T>::fourpi() * dsqrt(sq * sq + sm * sm) * r1n * r2n);
+    return coeff * cr;
+}
+
+// Segment plus its y=0 image (ispc:91-102).
+template <class T>
+__device__ __forceinline__ void symmetry_ref(V3<T>& inf, V3<T> c, V3<T> a, V3<T> b, T sigma) {
+    V3<T> s = biosavart_ref(c, a, b, sigma);
+    inf.x += s.x; inf.y += s.y; inf.z += s.z;
+    c.y = -c.y;
+    V3<T> m = biosavart_ref(c, a, b, sigma);
+    inf.x += m.x; inf.y -= m.y; inf.z += m.z;
+}
+
+template <class T>
+__device__ __forceinline__ V3<T> ring_velocity_ref(V3<T> c, V3<T> v0, V3<T> v1, V3<T> v2, V3<T> v3_, T sigma) {
+    V3<T> inf{0, 0, 0};
+    symmetry_ref(inf, c, v0, v1, sigma);
+    symmetry_ref(inf, c, v1, v2, sigma);
+    symmetry_ref(inf, c, v2, v3_, sigma);
+    symmetry_ref(inf, c, v3_, v0, sigma);
+    return inf;
+}
+
+// ---------------------------------------------------------------------------
+// Factored form.  For an evaluation point p and a lattice vertex v the kernel
+// keeps r = p - v together with |r|^2 and |r|; a segment a->b then needs only
+// r_a, r_b:  r0 = b - a = r_a - r_b, so
+//   r0.r1 = |r_a|^2 - r_a.r_b,  r0.r2 = r_a.r_b - |r_b|^2,
+//   v(a->b) = (r_a x r_b) * (r0.r1 |r_b| - r0.r2 |r_a|) / (4 pi |r_a x r_b|^2 |r_a| |r_b|)
+// which is eq. 10.115 rearranged (same cut-offs).  Vertices are shared by
+// the rings around them and a segment by its two rings, so a ring costs two
+// vertex terms and three segment terms instead of eight segment terms.
+// ---------------------------------------------------------------------------
+template <class T> struct Rel { T x, y, z, n2, n; };
+
+template <class T> __device__ __forceinline__ T fast_len(T n2);
+template <> __device__ __forceinline__ float fast_len<float>(float n2) { return n2 * rsqrtf(n2 + 1e-37f); }
+template <> __device__ __forceinline__ double fast_len<double>(double n2) { return sqrt(n2); }
+
+template <class T> __device__ __forceinline__ T fast_div(T a, T b);
+template <> __device__ __forceinline__ float fast_div<float>(float a, float b) { return __fdividef(a, b); }
+template <> __device__ __forceinline__ double fast_div<double>(double a, double b) { return a / b; }
+
+template <class T>
+__device__ __forceinline__ Rel<T> make_rel(T x, T y, T z) {
+    Rel<T> r;
+    r.x = x; r.y = y; r.z = z;
+    r.n2 = x * x + y * y + z * z;
+    r.n = fast_len<T>(r.n2);
+    return r;
+}
+
+// 4*pi * (velocity of segment a->b) . nrm ; sigma2 = sigma^2 (0 = no core)
+template <class T, bool SIGMA>
+__device__ __forceinline__ T seg_normal(const Rel<T>& a, const Rel<T>& b, T nx, T ny, T nz, T sigma2) {
+    T cx = a.y * b.z - a.z * b.y;
+    T cy = a.z * b.x - a.x * b.z;
+    T cz = a.x * b.y - a.y * b.x;
+    T sq = cx * cx + cy * cy + cz * cz;
+    T ab = a.x * b.x + a.y * b.y + a.z * b.z;
+    T num = (a.n2 - ab) * b.n - (ab - b.n2) * a.n;
+    T cn = cx * nx + cy * ny + cz * nz;
+    T den;
+    if (SIGMA) {
+        T rx = a.x - b.x, ry = a.y - b.y, rz = a.z - b.z;
+        T sm = sigma2 * (rx * rx + ry * ry + rz * rz);
+        den = dsqrt<T>(sq * sq + sm * sm) * a.n * b.n;
+    } else {
+        den = sq * a.n * b.n;
+    }
+    bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
+    return cut ? (T)0 : fast_div<T>(num * cn, den);
+}
+
+// 4*pi * velocity vector of segment a->b (for wake roll-up)
+template <class T, bool SIGMA>
+__device__ __forceinline__ V3<T> seg_vec(const Rel<T>& a, const Rel<T>& b, T sigma2) {
+    T cx = a.y * b.z - a.z * b.y;
+    T cy = a.z * b.x - a.x * b.z;
+    T cz = a.x * b.y - a.y * b.x;
+    T sq = cx * cx + cy * cy + cz * cz;
+    T ab = a.x * b.x + a.y * b.y + a.z * b.z;
+    T num = (a.n2 - ab) * b.n - (ab - b.n2) * a.n;
+    T den;
+    if (SIGMA) {
+        T rx = a.x - b.x, ry = a.y - b.y, rz = a.z - b.z;
+        T sm = sigma2 * (rx * rx + ry * ry + rz * rz);
+        den = dsqrt<T>(sq * sq + sm * sm) * a.n * b.n;
+    } else {
+        den = sq * a.n * b.n;
+    }
+    bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
+    T k = cut ? (T)0 : fast_div<T>(num, den);
+    return V3<T>{k * cx, k * cy, k * cz};
+}
+
+// Double-float difference (p_hi + p_lo) - (v_hi + v_lo): the hi difference is
+// exact or rounded relative to the result, so r keeps float accuracy
+// relative to |r| even far from the origin.
+__device__ __forceinline__ float df_sub(float ph, float pl, float vh, float vl) {
+    return (ph - vh) + (pl - vl);
+}
+
+// Kahan-Babuska (Neumaier) compensated accumulation in double.
+struct CSum {
+    double s = 0.0, c = 0.0;
+    __device__ __forceinline__ void add(double x) {
+        double t = s + x;
+        c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return s + c; }
+};
+
+}  // namespace gbvlm

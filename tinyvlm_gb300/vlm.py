@@ -1,0 +1,85 @@
+"""Simulation drivers (vlm/include/vlm.hpp) over the gbvlm C ABI.
+
+``VLM(backend_name, meshes).run(FlowData)`` mirrors vlm/src/vlm.cpp:17-151:
+meshes are plot3d paths (read with the quarter-chord shift, like
+``Simulation``) or ``(4, nc+1, ns+1)`` vertex arrays already shifted.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import Coeffs, call, dims_array
+
+__all__ = ["FlowData", "AeroCoefficients", "VLM", "read_plot3d"]
+
+
+class FlowData:
+    """vlm/include/vlm_data.hpp:11-25 with vlm/src/vlm_utils.cpp:5-19."""
+
+    def __init__(self, alpha, beta=0.0, u_inf=1.0, rho=1.0):
+        self.alpha, self.beta, self.u_inf, self.rho = float(alpha), float(beta), float(u_inf), float(rho)
+        ca, sa, cb, sb = math.cos(alpha), math.sin(alpha), math.cos(beta), math.sin(beta)
+        self.freestream = np.array([u_inf * ca * cb, -u_inf * ca * sb, u_inf * sa])
+        la = np.array([-self.freestream[2], 0.0, self.freestream[0]])
+        self.lift_axis = la / np.linalg.norm(la)
+        self.stream_axis = self.freestream / np.linalg.norm(self.freestream)
+
+
+class AeroCoefficients:
+    def __init__(self, cl, cd, cm):
+        self.cl, self.cd, self.cm = cl, cd, cm
+
+    def __repr__(self):
+        return "AeroCoefficients(cl=%.8g, cd=%.8g, cm=%s)" % (self.cl, self.cd, list(self.cm))
+
+
+def read_plot3d(path, qc=True):
+    """plot3d reader of the C ABI (vlm/src/vlm_mesh.cpp); returns (4, nc+1, ns+1) float32."""
+    d = _lib.Dims()
+    call("gbvlm_read_plot3d", path.encode(), 1 if qc else 0, ctypes.cast(ctypes.pointer(d), ctypes.c_void_p), None)
+    v = np.zeros((4, d.nc + 1, d.ns + 1), np.float32)
+    call("gbvlm_read_plot3d", path.encode(), 1 if qc else 0, ctypes.cast(ctypes.pointer(d), ctypes.c_void_p),
+         ctypes.c_void_p(v.ctypes.data))
+    return v
+
+
+class VLM:
+    """Steady VLM on the GPU.  ``precision=32`` keeps the reference's float
+    semantics; ``precision=64`` is the plain per-solve double path."""
+
+    def __init__(self, backend_name, meshes, precision=32):
+        if backend_name not in ("gb300", "cuda", "cpu"):
+            raise RuntimeError("Unsupported backend: " + backend_name)
+        verts = [read_plot3d(m) if isinstance(m, str) else np.ascontiguousarray(m, np.float32) for m in meshes]
+        self.verts = verts
+        self.dims = [(v.shape[2] - 1, v.shape[1] - 1, 0) for v in verts]
+        self.n = sum(a * b for a, b, _ in self.dims)
+        d = dims_array(self.dims)
+        arr = (ctypes.c_void_p * len(verts))(*[v.ctypes.data for v in verts])
+        h = ctypes.c_void_p()
+        call("gbvlm_vlm_create", ctypes.cast(ctypes.pointer(h), ctypes.c_void_p), len(verts), d,
+             ctypes.cast(arr, _lib.PP), int(precision))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                _lib.lib().gbvlm_vlm_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def run(self, flow, ref_pt=(0.0, 0.0, 0.0), return_gamma=False, stream=None):
+        out = Coeffs()
+        rp = (ctypes.c_double * 3)(*ref_pt)
+        g = np.zeros(self.n, np.float64) if return_gamma else None
+        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        call("gbvlm_vlm_run", self.h, flow.alpha, flow.beta, flow.u_inf, flow.rho, ctypes.cast(rp, ctypes.c_void_p),
+             ctypes.cast(ctypes.pointer(out), ctypes.c_void_p),
+             ctypes.c_void_p(g.ctypes.data) if g is not None else None, s)
+        res = AeroCoefficients(out.cl, out.cdi, tuple(out.cm))
+        if return_gamma:
+            return res, g
+        return res
