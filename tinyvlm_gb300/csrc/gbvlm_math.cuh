@@ -78,15 +78,18 @@ __device__ __forceinline__ V3<T> ring_velocity_ref(V3<T> c, V3<T> v0, V3<T> v1, 
 
 // ---------------------------------------------------------------------------
 // Factored form.  For an evaluation point p and a lattice vertex v the kernel
-// keeps r = p - v together with |r|^2 and |r|; a segment a->b then needs only
-// r_a, r_b:  r0 = b - a = r_a - r_b, so
-//   r0.r1 = |r_a|^2 - r_a.r_b,  r0.r2 = r_a.r_b - |r_b|^2,
-//   v(a->b) = (r_a x r_b) * (r0.r1 |r_b| - r0.r2 |r_a|) / (4 pi |r_a x r_b|^2 |r_a| |r_b|)
-// which is eq. 10.115 rearranged (same cut-offs).  Vertices are shared by
-// the rings around them and a segment by its two rings, so a ring costs two
-// vertex terms and three segment terms instead of eight segment terms.
+// keeps r = p - v and |r|; a segment a->b then needs only r_a, r_b.  With
+// r0 = b - a = r_a - r_b, eq. 10.115's factor r0.(r_a/|r_a| - r_b/|r_b|)
+// equals (|r_a|+|r_b|)(|r_a||r_b| - r_a.r_b)/(|r_a||r_b|), and
+// |r_a x r_b|^2 = (|r_a||r_b| - r_a.r_b)(|r_a||r_b| + r_a.r_b), so
+//   v(a->b) = (r_a x r_b) (|r_a|+|r_b|) / (4 pi |r_a||r_b| (|r_a||r_b| + r_a.r_b))
+// which is the same law without the cancellation the textbook form suffers
+// for far or nearly collinear segments.  The cut-offs are the reference's.
+// Vertices are shared by the rings around them and a segment by its two
+// rings, so a ring costs two vertex terms and three segment terms instead of
+// eight segment evaluations.
 // ---------------------------------------------------------------------------
-template <class T> struct Rel { T x, y, z, n2, n; };
+template <class T> struct Rel { T x, y, z, n; };
 
 template <class T> __device__ __forceinline__ T fast_len(T n2);
 template <> __device__ __forceinline__ float fast_len<float>(float n2) { return n2 * rsqrtf(n2 + 1e-37f); }
@@ -100,52 +103,46 @@ template <class T>
 __device__ __forceinline__ Rel<T> make_rel(T x, T y, T z) {
     Rel<T> r;
     r.x = x; r.y = y; r.z = z;
-    r.n2 = x * x + y * y + z * z;
-    r.n = fast_len<T>(r.n2);
+    r.n = fast_len<T>(x * x + y * y + z * z);
     return r;
 }
 
-// 4*pi * (velocity of segment a->b) . nrm ; sigma2 = sigma^2 (0 = no core)
+// scalar k with v(a->b) = k * (r_a x r_b) / (4 pi); returns the cross product in c
+template <class T, bool SIGMA>
+__device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T sigma2, T& cx, T& cy, T& cz) {
+    cx = a.y * b.z - a.z * b.y;
+    cy = a.z * b.x - a.x * b.z;
+    cz = a.x * b.y - a.y * b.x;
+    const T sq = cx * cx + cy * cy + cz * cz;
+    const T ab = a.x * b.x + a.y * b.y + a.z * b.z;
+    const T nab = a.n * b.n;
+    const T sum = a.n + b.n;
+    const bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
+    T k;
+    if (SIGMA) {
+        // reference core smoothing sqrt(sq^2 + (sigma^2 |r0|^2)^2) in place of sq
+        const T rx = a.x - b.x, ry = a.y - b.y, rz = a.z - b.z;
+        const T sm = sigma2 * (rx * rx + ry * ry + rz * rz);
+        k = fast_div<T>(sum * sq, (nab + ab) * dsqrt<T>(sq * sq + sm * sm) * nab);
+    } else {
+        k = fast_div<T>(sum, nab * (nab + ab));
+    }
+    return cut ? (T)0 : k;
+}
+
+// 4*pi * (velocity of segment a->b) . nrm
 template <class T, bool SIGMA>
 __device__ __forceinline__ T seg_normal(const Rel<T>& a, const Rel<T>& b, T nx, T ny, T nz, T sigma2) {
-    T cx = a.y * b.z - a.z * b.y;
-    T cy = a.z * b.x - a.x * b.z;
-    T cz = a.x * b.y - a.y * b.x;
-    T sq = cx * cx + cy * cy + cz * cz;
-    T ab = a.x * b.x + a.y * b.y + a.z * b.z;
-    T num = (a.n2 - ab) * b.n - (ab - b.n2) * a.n;
-    T cn = cx * nx + cy * ny + cz * nz;
-    T den;
-    if (SIGMA) {
-        T rx = a.x - b.x, ry = a.y - b.y, rz = a.z - b.z;
-        T sm = sigma2 * (rx * rx + ry * ry + rz * rz);
-        den = dsqrt<T>(sq * sq + sm * sm) * a.n * b.n;
-    } else {
-        den = sq * a.n * b.n;
-    }
-    bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
-    return cut ? (T)0 : fast_div<T>(num * cn, den);
+    T cx, cy, cz;
+    const T k = seg_coeff<T, SIGMA>(a, b, sigma2, cx, cy, cz);
+    return k * (cx * nx + cy * ny + cz * nz);
 }
 
 // 4*pi * velocity vector of segment a->b (for wake roll-up)
 template <class T, bool SIGMA>
 __device__ __forceinline__ V3<T> seg_vec(const Rel<T>& a, const Rel<T>& b, T sigma2) {
-    T cx = a.y * b.z - a.z * b.y;
-    T cy = a.z * b.x - a.x * b.z;
-    T cz = a.x * b.y - a.y * b.x;
-    T sq = cx * cx + cy * cy + cz * cz;
-    T ab = a.x * b.x + a.y * b.y + a.z * b.z;
-    T num = (a.n2 - ab) * b.n - (ab - b.n2) * a.n;
-    T den;
-    if (SIGMA) {
-        T rx = a.x - b.x, ry = a.y - b.y, rz = a.z - b.z;
-        T sm = sigma2 * (rx * rx + ry * ry + rz * rz);
-        den = dsqrt<T>(sq * sq + sm * sm) * a.n * b.n;
-    } else {
-        den = sq * a.n * b.n;
-    }
-    bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
-    T k = cut ? (T)0 : fast_div<T>(num, den);
+    T cx, cy, cz;
+    const T k = seg_coeff<T, SIGMA>(a, b, sigma2, cx, cy, cz);
     return V3<T>{k * cx, k * cy, k * cz};
 }
 
