@@ -78,16 +78,18 @@ __device__ __forceinline__ V3<T> ring_velocity_ref(V3<T> c, V3<T> v0, V3<T> v1, 
 
 // ---------------------------------------------------------------------------
 // Factored form.  For an evaluation point p and a lattice vertex v the kernel
-// keeps r = p - v and |r|; a segment a->b then needs only r_a, r_b.  With
-// r0 = b - a = r_a - r_b, eq. 10.115's factor r0.(r_a/|r_a| - r_b/|r_b|)
-// equals (|r_a|+|r_b|)(|r_a||r_b| - r_a.r_b)/(|r_a||r_b|), and
-// |r_a x r_b|^2 = (|r_a||r_b| - r_a.r_b)(|r_a||r_b| + r_a.r_b), so
-//   v(a->b) = (r_a x r_b) (|r_a|+|r_b|) / (4 pi |r_a||r_b| (|r_a||r_b| + r_a.r_b))
-// which is the same law without the cancellation the textbook form suffers
-// for far or nearly collinear segments.  The cut-offs are the reference's.
-// Vertices are shared by the rings around them and a segment by its two
-// rings, so a ring costs two vertex terms and three segment terms instead of
-// eight segment evaluations.
+// keeps r = p - v and |r|; a segment A->B with a = p - A, b = p - B and the
+// segment vector r0 = B - A (taken from the vertex coordinates) gives
+// a x b = r0 x a, and eq. 10.115's factor r0.(a/|a| - b/|b|) / |a x b|^2
+// equals (|a|+|b|) / (|a||b| (|a||b| + a.b)).  When a.b < 0 the last factor
+// is rewritten with |a x b|^2 = (|a||b| - a.b)(|a||b| + a.b), so neither the
+// far field (a ~ b) nor points beside a long segment (a ~ -b) cancel:
+//   k = (|a|+|b|) / (|a||b| (|a||b| + a.b))          a.b >= 0
+//   k = (|a|+|b|) (|a||b| - a.b) / (|a||b| |a x b|^2)  a.b <  0
+//   v(A->B) = k (r0 x a) / (4 pi)
+// The cut-offs are the reference's.  Vertices are shared by the rings around
+// them and a segment by its two rings, so a ring costs two vertex terms and
+// three segment terms instead of eight segment evaluations.
 // ---------------------------------------------------------------------------
 template <class T> struct Rel { T x, y, z, n; };
 
@@ -107,42 +109,46 @@ __device__ __forceinline__ Rel<T> make_rel(T x, T y, T z) {
     return r;
 }
 
-// scalar k with v(a->b) = k * (r_a x r_b) / (4 pi); returns the cross product in c
+// scalar k with v(A->B) = k * (r0 x a) / (4 pi); the cross product is returned in c
 template <class T, bool SIGMA>
-__device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T sigma2, T& cx, T& cy, T& cz) {
-    cx = a.y * b.z - a.z * b.y;
-    cy = a.z * b.x - a.x * b.z;
-    cz = a.x * b.y - a.y * b.x;
+__device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T r0x, T r0y, T r0z, T sigma2, T& cx,
+                                       T& cy, T& cz) {
+    cx = r0y * a.z - r0z * a.y;
+    cy = r0z * a.x - r0x * a.z;
+    cz = r0x * a.y - r0y * a.x;
     const T sq = cx * cx + cy * cy + cz * cz;
     const T ab = a.x * b.x + a.y * b.y + a.z * b.z;
     const T nab = a.n * b.n;
     const T sum = a.n + b.n;
     const bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
-    T k;
+    const bool pos = ab >= (T)0;
+    T num = pos ? sum : sum * (nab - ab);
+    T den = pos ? nab * (nab + ab) : nab * sq;
     if (SIGMA) {
-        // reference core smoothing sqrt(sq^2 + (sigma^2 |r0|^2)^2) in place of sq
-        const T rx = a.x - b.x, ry = a.y - b.y, rz = a.z - b.z;
-        const T sm = sigma2 * (rx * rx + ry * ry + rz * rz);
-        k = fast_div<T>(sum * sq, (nab + ab) * dsqrt<T>(sq * sq + sm * sm) * nab);
-    } else {
-        k = fast_div<T>(sum, nab * (nab + ab));
+        // reference core smoothing: sq -> sqrt(sq^2 + (sigma^2 |r0|^2)^2)
+        const T sm = sigma2 * (r0x * r0x + r0y * r0y + r0z * r0z);
+        const T sc = dsqrt<T>(sq * sq + sm * sm);
+        num = num * sq;
+        den = den * sc;
     }
+    const T k = fast_div<T>(num, den);
     return cut ? (T)0 : k;
 }
 
-// 4*pi * (velocity of segment a->b) . nrm
+// 4*pi * (velocity of segment A->B) . nrm
 template <class T, bool SIGMA>
-__device__ __forceinline__ T seg_normal(const Rel<T>& a, const Rel<T>& b, T nx, T ny, T nz, T sigma2) {
+__device__ __forceinline__ T seg_normal(const Rel<T>& a, const Rel<T>& b, T r0x, T r0y, T r0z, T nx, T ny, T nz,
+                                        T sigma2) {
     T cx, cy, cz;
-    const T k = seg_coeff<T, SIGMA>(a, b, sigma2, cx, cy, cz);
+    const T k = seg_coeff<T, SIGMA>(a, b, r0x, r0y, r0z, sigma2, cx, cy, cz);
     return k * (cx * nx + cy * ny + cz * nz);
 }
 
-// 4*pi * velocity vector of segment a->b (for wake roll-up)
+// 4*pi * velocity vector of segment A->B (for wake roll-up)
 template <class T, bool SIGMA>
-__device__ __forceinline__ V3<T> seg_vec(const Rel<T>& a, const Rel<T>& b, T sigma2) {
+__device__ __forceinline__ V3<T> seg_vec(const Rel<T>& a, const Rel<T>& b, T r0x, T r0y, T r0z, T sigma2) {
     T cx, cy, cz;
-    const T k = seg_coeff<T, SIGMA>(a, b, sigma2, cx, cy, cz);
+    const T k = seg_coeff<T, SIGMA>(a, b, r0x, r0y, r0z, sigma2, cx, cy, cz);
     return V3<T>{k * cx, k * cy, k * cz};
 }
 

@@ -222,10 +222,66 @@ __device__ __forceinline__ T ring_normal_full(T px, T py, T pz, T nx, T ny, T nz
     T v = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        v += seg_normal<T, SIGMA>(a[k], a[(k + 1) & 3], nx, ny, nz, sigma2);
-        v += seg_normal<T, SIGMA>(b[k], b[(k + 1) & 3], nx, -ny, nz, sigma2);
+        const int e = (k + 1) & 3;
+        const T rx = q[e].x - q[k].x, ry = q[e].y - q[k].y, rz = q[e].z - q[k].z;
+        v += seg_normal<T, SIGMA>(a[k], a[e], rx, ry, rz, nx, ny, nz, sigma2);
+        v += seg_normal<T, SIGMA>(b[k], b[e], rx, ry, rz, nx, -ny, nz, sigma2);
     }
     return v;
+}
+
+// Walk the rings of one strip whose vertex lines sit in shared memory
+// (top/bot: 3 planes W apart), local vertices 0..nvs-1; calls
+// f(ring_index, 4*pi*(v.n + v_mirror.n_mirror)) for rings 0..nvs-2.
+template <class T, bool SIGMA, class F>
+__device__ __forceinline__ void strip_normal(const T* top, const T* bot, int W, int nvs, T px, T py, T pz, T nx, T ny,
+                                             T nz, T sg, F&& f) {
+    auto V = [&](const T* line, int sl) { return V3<T>{line[sl], line[W + sl], line[2 * W + sl]}; };
+    V3<T> v0 = V(top, 0), v3 = V(bot, 0);
+    Rel<T> A0 = make_rel<T>(px - v0.x, py - v0.y, pz - v0.z), A3 = make_rel<T>(px - v3.x, py - v3.y, pz - v3.z);
+    Rel<T> B0 = make_rel<T>(px - v0.x, -py - v0.y, pz - v0.z), B3 = make_rel<T>(px - v3.x, -py - v3.y, pz - v3.z);
+    T Ca = seg_normal<T, SIGMA>(A0, A3, v3.x - v0.x, v3.y - v0.y, v3.z - v0.z, nx, ny, nz, sg);
+    T Cb = seg_normal<T, SIGMA>(B0, B3, v3.x - v0.x, v3.y - v0.y, v3.z - v0.z, nx, -ny, nz, sg);
+    for (int k = 1; k < nvs; k++) {
+        const V3<T> v1 = V(top, k), v2 = V(bot, k);
+        const Rel<T> A1 = make_rel<T>(px - v1.x, py - v1.y, pz - v1.z), A2 = make_rel<T>(px - v2.x, py - v2.y, pz - v2.z);
+        const Rel<T> B1 = make_rel<T>(px - v1.x, -py - v1.y, pz - v1.z), B2 = make_rel<T>(px - v2.x, -py - v2.y, pz - v2.z);
+        const T cx = v2.x - v1.x, cy = v2.y - v1.y, cz = v2.z - v1.z;  // right chordwise segment
+        const T tx = v1.x - v0.x, ty = v1.y - v0.y, tz = v1.z - v0.z;  // top segment v0->v1
+        const T bx = v3.x - v2.x, by = v3.y - v2.y, bz = v3.z - v2.z;  // bottom segment v2->v3
+        const T Cra = seg_normal<T, SIGMA>(A1, A2, cx, cy, cz, nx, ny, nz, sg);
+        const T Crb = seg_normal<T, SIGMA>(B1, B2, cx, cy, cz, nx, -ny, nz, sg);
+        T val = seg_normal<T, SIGMA>(A0, A1, tx, ty, tz, nx, ny, nz, sg) + Cra +
+                seg_normal<T, SIGMA>(A2, A3, bx, by, bz, nx, ny, nz, sg) - Ca;
+        val += seg_normal<T, SIGMA>(B0, B1, tx, ty, tz, nx, -ny, nz, sg) + Crb +
+               seg_normal<T, SIGMA>(B2, B3, bx, by, bz, nx, -ny, nz, sg) - Cb;
+        f(k - 1, val);
+        A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb; v0 = v1; v3 = v2;
+    }
+}
+
+// Same walk returning 4*pi times the full velocity of each ring (direct + mirror).
+template <class T, bool SIGMA, class F>
+__device__ __forceinline__ void strip_vec(const T* top, const T* bot, int W, int nvs, T px, T py, T pz, T sg, F&& f) {
+    auto V = [&](const T* line, int sl) { return V3<T>{line[sl], line[W + sl], line[2 * W + sl]}; };
+    V3<T> v0 = V(top, 0), v3 = V(bot, 0);
+    Rel<T> A0 = make_rel<T>(px - v0.x, py - v0.y, pz - v0.z), A3 = make_rel<T>(px - v3.x, py - v3.y, pz - v3.z);
+    Rel<T> B0 = make_rel<T>(px - v0.x, -py - v0.y, pz - v0.z), B3 = make_rel<T>(px - v3.x, -py - v3.y, pz - v3.z);
+    V3<T> Ca = seg_vec<T, SIGMA>(A0, A3, v3.x - v0.x, v3.y - v0.y, v3.z - v0.z, sg);
+    V3<T> Cb = seg_vec<T, SIGMA>(B0, B3, v3.x - v0.x, v3.y - v0.y, v3.z - v0.z, sg);
+    for (int k = 1; k < nvs; k++) {
+        const V3<T> v1 = V(top, k), v2 = V(bot, k);
+        const Rel<T> A1 = make_rel<T>(px - v1.x, py - v1.y, pz - v1.z), A2 = make_rel<T>(px - v2.x, py - v2.y, pz - v2.z);
+        const Rel<T> B1 = make_rel<T>(px - v1.x, -py - v1.y, pz - v1.z), B2 = make_rel<T>(px - v2.x, -py - v2.y, pz - v2.z);
+        const T cx = v2.x - v1.x, cy = v2.y - v1.y, cz = v2.z - v1.z;
+        const T tx = v1.x - v0.x, ty = v1.y - v0.y, tz = v1.z - v0.z;
+        const T bx = v3.x - v2.x, by = v3.y - v2.y, bz = v3.z - v2.z;
+        const V3<T> Cra = seg_vec<T, SIGMA>(A1, A2, cx, cy, cz, sg), Crb = seg_vec<T, SIGMA>(B1, B2, cx, cy, cz, sg);
+        const V3<T> ra = seg_vec<T, SIGMA>(A0, A1, tx, ty, tz, sg) + Cra + seg_vec<T, SIGMA>(A2, A3, bx, by, bz, sg) - Ca;
+        const V3<T> rb = seg_vec<T, SIGMA>(B0, B1, tx, ty, tz, sg) + Crb + seg_vec<T, SIGMA>(B2, B3, bx, by, bz, sg) - Cb;
+        f(k - 1, V3<T>{ra.x + rb.x, ra.y - rb.y, ra.z + rb.z});
+        A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb; v0 = v1; v3 = v2;
+    }
 }
 
 template <class T, bool SIGMA>
@@ -251,21 +307,11 @@ __global__ void __launch_bounds__(LHS_THREADS) k_lhs_pair(LhsPair<T> a) {
     const T px = a.colloc[i], py = a.colloc[a.np_i + i], pz = a.colloc[2 * a.np_i + i];
     const T nx = a.normals[i], ny = a.normals[a.np_i + i], nz = a.normals[2 * a.np_i + i];
     const T sg = a.sigma2;
-    auto relA = [&](int r, int sl) { return make_rel<T>(px - sv[(r * 3) * W + sl], py - sv[(r * 3 + 1) * W + sl], pz - sv[(r * 3 + 2) * W + sl]); };
-    auto relB = [&](int r, int sl) { return make_rel<T>(px - sv[(r * 3) * W + sl], -py - sv[(r * 3 + 1) * W + sl], pz - sv[(r * 3 + 2) * W + sl]); };
-    Rel<T> A0 = relA(0, 0), A3 = relA(1, 0), B0 = relB(0, 0), B3 = relB(1, 0);
-    T Ca = seg_normal<T, SIGMA>(A0, A3, nx, ny, nz, sg);
-    T Cb = seg_normal<T, SIGMA>(B0, B3, nx, -ny, nz, sg);
     const bool te = (c == a.nc - 1) && a.iteration > 0;
     const int64_t wk_ld = (a.ns + 1) * a.nwv;
     T* out = a.lhs + (a.row_off + i) + (a.col_off + c * a.ns) * a.ld;
-    for (int64_t s = s0; s < s1; s++) {
-        const int k = (int)(s - s0) + 1;
-        Rel<T> A1 = relA(0, k), A2 = relA(1, k), B1 = relB(0, k), B2 = relB(1, k);
-        T Cra = seg_normal<T, SIGMA>(A1, A2, nx, ny, nz, sg);
-        T Crb = seg_normal<T, SIGMA>(B1, B2, nx, -ny, nz, sg);
-        T val = seg_normal<T, SIGMA>(A0, A1, nx, ny, nz, sg) + Cra + seg_normal<T, SIGMA>(A2, A3, nx, ny, nz, sg) - Ca;
-        val += seg_normal<T, SIGMA>(B0, B1, nx, -ny, nz, sg) + Crb + seg_normal<T, SIGMA>(B2, B3, nx, -ny, nz, sg) - Cb;
+    strip_normal<T, SIGMA>(sv, sv + 3 * W, W, nv, px, py, pz, nx, ny, nz, sg, [&](int kk, T val) {
+        const int64_t s = s0 + kk;
         if (te) {
             for (int32_t it = 0; it < a.iteration; it++) {
                 const int64_t r0 = a.nwv - 2 - it;
@@ -278,8 +324,7 @@ __global__ void __launch_bounds__(LHS_THREADS) k_lhs_pair(LhsPair<T> a) {
             }
         }
         out[s * a.ld] += val * inv_four_pi<T>();
-        A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb;
-    }
+    });
 }
 
 template <class T>
@@ -450,22 +495,9 @@ __global__ void __launch_bounds__(WK_THREADS) k_wake_influence(WakeArgs<T> w) {
                     __syncthreads();
                     if (active) {
                         for (int r = 0; r < nr; r++) {
-                            auto relA = [&](int rr, int sl) { return make_rel<T>(px - sv[(rr * 3) * W + sl], py - sv[(rr * 3 + 1) * W + sl], pz - sv[(rr * 3 + 2) * W + sl]); };
-                            auto relB = [&](int rr, int sl) { return make_rel<T>(px - sv[(rr * 3) * W + sl], -py - sv[(rr * 3 + 1) * W + sl], pz - sv[(rr * 3 + 2) * W + sl]); };
-                            Rel<T> A0 = relA(r, 0), A3 = relA(r + 1, 0), B0 = relB(r, 0), B3 = relB(r + 1, 0);
-                            T Ca = seg_normal<T, SIGMA>(A0, A3, nx, ny, nz, w.sigma2);
-                            T Cb = seg_normal<T, SIGMA>(B0, B3, nx, -ny, nz, w.sigma2);
-                            for (int k = 1; k < nvs; k++) {
-                                Rel<T> A1 = relA(r, k), A2 = relA(r + 1, k), B1 = relB(r, k), B2 = relB(r + 1, k);
-                                T Cra = seg_normal<T, SIGMA>(A1, A2, nx, ny, nz, w.sigma2);
-                                T Crb = seg_normal<T, SIGMA>(B1, B2, nx, -ny, nz, w.sigma2);
-                                T val = seg_normal<T, SIGMA>(A0, A1, nx, ny, nz, w.sigma2) + Cra +
-                                        seg_normal<T, SIGMA>(A2, A3, nx, ny, nz, w.sigma2) - Ca;
-                                val += seg_normal<T, SIGMA>(B0, B1, nx, -ny, nz, w.sigma2) + Crb +
-                                       seg_normal<T, SIGMA>(B2, B3, nx, -ny, nz, w.sigma2) - Cb;
-                                acc += sg[r * SC + k - 1] * val;
-                                A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb;
-                            }
+                            const T* gr = sg + r * SC;
+                            strip_normal<T, SIGMA>(sv + r * 3 * W, sv + (r + 1) * 3 * W, W, nvs, px, py, pz, nx, ny, nz,
+                                                   w.sigma2, [&](int kk, T val) { acc += gr[kk] * val; });
                         }
                     }
                 }
@@ -598,21 +630,14 @@ __device__ __forceinline__ void lattice_vel(T px, T py, T pz, const T* v, int64_
             }
             __syncthreads();
             for (int r = 0; r < nr; r++) {
-                auto relA = [&](int q, int sl) { return make_rel<T>(px - sv[(q * 3) * W + sl], py - sv[(q * 3 + 1) * W + sl], pz - sv[(q * 3 + 2) * W + sl]); };
-                auto relB = [&](int q, int sl) { return make_rel<T>(px - sv[(q * 3) * W + sl], -py - sv[(q * 3 + 1) * W + sl], pz - sv[(q * 3 + 2) * W + sl]); };
-                Rel<T> A0 = relA(r, 0), A3 = relA(r + 1, 0), B0 = relB(r, 0), B3 = relB(r + 1, 0);
-                V3<T> Ca = seg_vec<T, SIGMA>(A0, A3, sigma2), Cb = seg_vec<T, SIGMA>(B0, B3, sigma2);
-                for (int k = 1; k < nvs; k++) {
-                    Rel<T> A1 = relA(r, k), A2 = relA(r + 1, k), B1 = relB(r, k), B2 = relB(r + 1, k);
-                    V3<T> Cra = seg_vec<T, SIGMA>(A1, A2, sigma2), Crb = seg_vec<T, SIGMA>(B1, B2, sigma2);
-                    V3<T> ra = seg_vec<T, SIGMA>(A0, A1, sigma2) + Cra + seg_vec<T, SIGMA>(A2, A3, sigma2) - Ca;
-                    V3<T> rb = seg_vec<T, SIGMA>(B0, B1, sigma2) + Crb + seg_vec<T, SIGMA>(B2, B3, sigma2) - Cb;
-                    const T gm = sgm[r * SC + k - 1];
-                    vel.x += gm * (ra.x + rb.x);
-                    vel.y += gm * (ra.y - rb.y);
-                    vel.z += gm * (ra.z + rb.z);
-                    A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb;
-                }
+                const T* gr = sgm + r * SC;
+                strip_vec<T, SIGMA>(sv + r * 3 * W, sv + (r + 1) * 3 * W, W, nvs, px, py, pz, sigma2,
+                                    [&](int kk, V3<T> v) {
+                                        const T gm = gr[kk];
+                                        vel.x += gm * v.x;
+                                        vel.y += gm * v.y;
+                                        vel.z += gm * v.z;
+                                    });
             }
         }
     }
