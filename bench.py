@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Benchmark: batched uneven steady VLM solves on GB300.
+
+Workload (one step): 512 seeded trapezoidal half wings (nc ~ U{4..32},
+ns ~ U{4..64}, AR ~ U[4,12], taper ~ U[0.3,1], sweep ~ U[0,35] deg, numpy
+PCG64 seed 20261203) with 8 angles of attack each (U[-8,8] deg) = 4096
+solves; every solve yields gamma, CL, CDi and CM.  ``--mode shared`` (the
+default) builds one AIC per wing at alpha = 0 and solves the 8 angles as
+right-hand sides; ``--mode exact`` builds one AIC per wing and angle with
+the reference's alpha-dependent collocation points and wake.
+
+``value`` is solves/s with inputs resident on the device (the CUDA graph of
+one step replayed K times, timed with CUDA events on the launching stream;
+the AIC set is larger than L2, so no flush is needed).  ``e2e`` times the
+same through the public API with host buffers: H2D of the packed vertices
+and angles from pinned memory, the graph, and D2H of the coefficients and
+every gamma.  ``cpu_baseline`` times the CPU restatement of the reference
+backend (float, all host threads) on a bounded sample of the same cases.
+
+``--impl reference`` times only that CPU implementation and prints its own
+line.  Under torchrun each rank runs its own replica (replicas only: the
+path has no exchange step); rank 0 prints.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s + p99 latency, batched/served vs plain on 1 GB300 at CL err≤1e-5"
+SEED = 20261203
+FLOP_PER_INTERACTION = 558  # Biot-Savart ring-point interaction, counted from the reference kernel
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--mode", default="shared", choices=["shared", "exact"])
+    p.add_argument("--cases", type=int, default=512)
+    p.add_argument("--alphas", type=int, default=8)
+    p.add_argument("--refine", type=int, default=1)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--plain-solves", type=int, default=48)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    from tinyvlm_gb300 import mesh as M
+    return M.batch_cases(args.cases, seed=SEED, n_alpha=args.alphas)
+
+
+def config(args, cases):
+    n = [c.n for c in cases]
+    return {"workload": "batched steady VLM: %d trapezoidal half wings x %d alpha, %s AIC" %
+                        (len(cases), args.alphas, "shared" if args.mode == "shared" else "per-alpha"),
+            "cases": len(cases), "alphas_per_case": args.alphas, "mode": args.mode,
+            "panels_min": int(min(n)), "panels_max": int(max(n)), "panels_sum": int(sum(n)),
+            "seed": SEED, "refine_iters": args.refine,
+            "l2": "not flushed: the step's AIC set is larger than the 129 MB L2"}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle port of the reference backend, float, all threads
+# ---------------------------------------------------------------------------
+def cpu_sample(args, cases, seconds):
+    from oracle import oracle as O
+    O.lib()
+    threads = O.num_threads()
+    done, t0 = 0, time.perf_counter()
+    used = 0
+    # a fixed stride through the batch keeps the sample's size mix close to the whole batch
+    order = list(range(0, len(cases), 7)) + [i for i in range(len(cases)) if i % 7]
+    for i in order:
+        c = cases[i]
+        if args.mode == "shared":
+            O.vlm_shared([c.verts], c.alphas, dtype=np.float32)
+        else:
+            for a in c.alphas:
+                O.vlm_run([c.verts], a, dtype=np.float32)
+        done += len(c.alphas)
+        used += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    sample = "%d of %d cases (%d solves, %d panels max), %.1f s" % (
+        used, len(cases), done, max(cases[i].n for i in order[:used]), dt)
+    return done / dt, threads, sample
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(self.rows), "reasons": reasons}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cases = workload(args)
+    rate, threads, sample = cpu_sample(args, cases, args.cpu_seconds)
+    step_solves = sum(len(c.alphas) for c in cases)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * step_solves / rate,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config(args, cases),
+        "cpu_baseline": {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference backend (OpenMP for its Taskflow loops, LAPACK sgetrf/sgetrs "
+                "through scipy's OpenBLAS); the reference's ISPC build needs ispc/xmake/Taskflow, absent here"}))
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+
+    cases = workload(args)
+    bs = BatchSolver(cases, mode=args.mode, refine=args.refine)
+    verts_h = torch.from_numpy(pack_verts(cases)).pin_memory()
+    alphas = pack_alphas(cases)
+    verts_d = verts_h.to(dev)
+    stream = torch.cuda.current_stream(dev)
+    co_h = torch.zeros((bs.nsolve, 5), dtype=torch.float64).pin_memory().numpy()
+    g_h = torch.zeros(bs.gamma_floats, dtype=torch.float32).pin_memory().numpy()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up: captures the graph
+    bs.set_inputs(verts_d, alphas, ref_pt=(0.25, 0.0, 0.0), stream=stream)
+    for _ in range(max(args.warmup, 3)):
+        bs.run(stream=stream)
+    torch.cuda.synchronize()
+
+    # --- device-resident throughput -----------------------------------------
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            bs.run(stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = bs.nsolve * world / (ms / 1000.0)
+
+    # --- end to end through the public API with host buffers ----------------
+    lat = []
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s0 = time.perf_counter()
+        bs.set_inputs(verts_h, alphas, ref_pt=(0.25, 0.0, 0.0), stream=stream)
+        bs.run(want_gamma=True, stream=stream)
+        bs.results_into(co_h, g_h, stream=stream)
+        lat.append(1000.0 * (time.perf_counter() - s0))
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(1000.0 * (time.perf_counter() - t0) / args.steps)
+    e2e = bs.nsolve * world / (e2e_ms / 1000.0)
+    h2d = verts_h.numel() * 4 + alphas.nbytes
+    d2h = co_h.nbytes + g_h.nbytes
+
+    # --- per-stage CUDA-event profile (same stream) --------------------------
+    prof = bs.profile(stream=stream)
+    prof2 = bs.profile(stream=stream)
+    prof = {k: min(prof[k], prof2[k]) for k in prof}
+    co_ref, _ = bs.results(stream=stream)
+    plain = plain_path_rate(args, cases, dev, co_ref) if rank == 0 else None
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, threads, sample = cpu_sample(args, cases, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample}
+    if rank != 0:
+        return
+
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    # dominant stage -> roofline
+    stage = max(prof, key=prof.get)
+    roof = roofline(stage, prof, bs, peaks)
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded trapezoidal wings)",
+        "config": config(args, cases),
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "what": "per step (one batch of %d solves) through the public API" % bs.nsolve},
+        "gpu_launches": int(bs.launches()) * args.steps,
+        "clocks": clk.summary(),
+        "roofline": roof,
+        "stage_ms": prof,
+        "plain_fp64_gpu": plain,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out))
+
+
+def roofline(stage, prof, bs, peaks):
+    """Roofline entry for the dominant stage (algorithmic work / CUDA-event time)."""
+    t = prof[stage] / 1000.0
+    if stage == "assembly":
+        flops = FLOP_PER_INTERACTION * bs.interactions
+        # FP32 SIMT pipe: 152 SMs x 128 lanes x 2 flop/FMA x max SM clock
+        peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        return {"stage": stage, "kernel": "k_batch_assemble", "bound": "fp32", "achieved": flops / t / 1e12,
+                "peak": peak, "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak, "traffic": None,
+                "peak_source": "nominal FP32 FMA rate at the measured max SM clock (no FP32 figure in MEASURED_PEAKS.json)",
+                "work": "558 flop x %d ring-point interactions" % int(bs.interactions)}
+    if stage == "lu_factor":
+        flops = bs.lu_flops
+        peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        return {"stage": stage, "kernel": "k_panel/k_swap/k_trsm/k_update", "bound": "fp32",
+                "achieved": flops / t / 1e12, "peak": peak, "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak,
+                "traffic": None, "peak_source": "nominal FP32 FMA rate at the measured max SM clock",
+                "work": "sum of 2/3 n^3 over systems"}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    return {"stage": stage, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+            "traffic": None}
+
+
+def plain_path_rate(args, cases, dev, co):
+    """The plain per-solve double path on the GPU (one VLM::run per solve) on
+    a sample of the cases, and the batched path's CL/CM deviation from it."""
+    if args.plain_solves <= 0:
+        return None
+    import torch
+    from tinyvlm_gb300.vlm import VLM, FlowData
+    start = np.cumsum([0] + [len(c.alphas) for c in cases])
+    picks, total = [], 0
+    for i in range(0, len(cases), 7):
+        picks.append(i)
+        total += len(cases[i].alphas)
+        if total >= args.plain_solves:
+            break
+    sims = {i: VLM("gb300", [cases[i].verts], precision=64) for i in picks}
+    res = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in picks:
+        for q, a in enumerate(cases[i].alphas):
+            res.append((start[i] + q, sims[i].run(FlowData(a), ref_pt=(0.25, 0.0, 0.0))))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    cl_err = max(abs(co[k, 0] - r.cl) / max(abs(r.cl), 1e-3) for k, r in res)
+    cm_err = max(float(np.abs(co[k, 2:5] - np.array(r.cm)).max() / max(np.abs(r.cm).max(), 1e-6)) for k, r in res)
+    return {"value": len(res) / dt, "unit": "solves/s", "solves": len(res),
+            "what": "plain per-solve double GPU path (VLM::run semantics, one solve per call, double throughout)",
+            "batched_vs_plain": {"max_rel_err_cl": cl_err, "max_rel_err_cm": cm_err, "target": 1e-5}}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

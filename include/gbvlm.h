@@ -262,6 +262,51 @@ int gbvlm_vlm_destroy(gbvlm_vlm h);
 int gbvlm_vlm_run(gbvlm_vlm h, double alpha, double beta, double u_inf, double rho, const double* ref_pt,
                   gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched steady solves: many single-surface cases of uneven size, each with
+ * several angles of attack, in one CUDA graph.  No reference counterpart as
+ * one call: it runs, per case and angle, the operator sequence of
+ * VLM::run (vlm/src/vlm.cpp:97-151) -- geometry, lhs_assemble,
+ * rhs_assemble_velocities, LU factorize/solve, forces_steady, coeff_cl,
+ * coeff_cm -- plus the Trefftz CDi.  Geometry is formed in double, the AIC in
+ * float from double-float relative vectors, the LU in float, and
+ * `refine_iters` steps of refinement with a double residual recover double
+ * accuracy of the stored system; loads are summed in double.
+ *   GBVLM_BATCH_EXACT : one AIC per (case, alpha) with the reference's
+ *                       alpha-dependent collocation points and wake;
+ *   GBVLM_BATCH_SHARED: one AIC per case built at alpha = 0, each alpha a
+ *                       right-hand side V_inf(alpha) (the classical linear
+ *                       VLM; fewer factorizations).
+ * ------------------------------------------------------------------------- */
+enum { GBVLM_BATCH_EXACT = 0, GBVLM_BATCH_SHARED = 1 };
+typedef struct gbvlm_batch_s* gbvlm_batch;
+
+/* dims[c].ns/.nc: panels of case c; nalpha[c] in [1, 64] angles. */
+int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims, const int32_t* nalpha,
+                       int32_t mode, int32_t refine_iters);
+int gbvlm_batch_destroy(gbvlm_batch h);
+/* Sizes of the plan: solves (= sum nalpha), systems, gamma floats, Biot-Savart
+ * ring-point interactions and LU flops per run, device bytes held. */
+int gbvlm_batch_info(gbvlm_batch h, int64_t* nsolve, int64_t* nsys, int64_t* gamma_floats, double* interactions,
+                     double* lu_flops, int64_t* arena_bytes);
+/* Kernel launches one gbvlm_batch_run makes (after the first run). */
+int gbvlm_batch_launches(gbvlm_batch h, int64_t* out);
+/* verts: every case's (ns+1, nc+1, 4) float vertices (quarter-chord shifted)
+ * packed in case order, host (pageable or pinned) or device memory;
+ * alphas: host, sum(nalpha) radians in case order; ref_pt: host [3] moment
+ * reference in the wing frame (may be NULL = origin). */
+int gbvlm_batch_set_inputs(gbvlm_batch h, const float* verts, const double* alphas, double u_inf, double rho,
+                           const double* ref_pt, gbvlm_stream stream);
+/* Enqueue the whole solve (a CUDA graph captured on first use) on stream. */
+int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream);
+/* Run the stages once without the graph, each bracketed by CUDA events on
+ * `stream`; stage_ms[6] = geometry, assembly, rhs, LU factor, solve +
+ * refinement, loads (milliseconds).  Synchronous. */
+int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream);
+/* Synchronous read-back in case/alpha order: coeffs[5*k..] = cl, cdi, cm_x,
+ * cm_y, cm_z; gamma (optional, needs want_gamma) = each solve's n floats. */
+int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_stream stream);
+
 /* plot3d reader (vlm/src/vlm_mesh.cpp:34-123): dims first (verts == NULL),
  * then the vertices into a HOST float (ns+1, nc+1, 4) array. */
 int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts);

@@ -336,7 +336,7 @@ def vlm_run(verts_init, alpha, beta=0.0, u_inf=1.0, rho=1.0, dtype=np.float32, s
     CL follows VLM::run.  CDi is the Trefftz-plane drag of the (dead in the
     reference) kernel_trefftz_cd normalised as its commented caller does,
     area-weighted over surfaces like CL; CM is coeff_cm_multibody about
-    ``ref_pt``, which VLM::run leaves at zero.
+    ``ref_pt`` in the wing's own frame (VLM::run leaves CM at zero).
     """
     T = np.dtype(dtype).type
     verts_init = [np.ascontiguousarray(v, dtype) for v in verts_init]
@@ -381,7 +381,10 @@ def vlm_run(verts_init, alpha, beta=0.0, u_inf=1.0, rho=1.0, dtype=np.float32, s
         gwake.append(gw)
     forces = [forces_steady(v, d, u) for v, d, u in zip(verts, deltas, vel)]
     cl = coeff_cl_multibody(forces, areas, fs, T(rho))
-    cm = coeff_cm_multibody(forces, verts, areas, np.asarray(ref_pt, dtype), fs, T(rho))
+    # the wing sits displaced by the wake translation; the moment reference
+    # moves with it, so CM is the body-frame moment about ref_pt
+    ref_disp = np.asarray(ref_pt, dtype) + tr[0:3, 3]
+    cm = coeff_cm_multibody(forces, verts, areas, ref_disp, fs, T(rho))
     cdi_num, area_tot = T(0), T(0)
     for w, gw, a in zip(wake, gwake, areas):
         area = asum(a)
@@ -391,4 +394,50 @@ def vlm_run(verts_init, alpha, beta=0.0, u_inf=1.0, rho=1.0, dtype=np.float32, s
     if return_state:
         out.update(lhs=lhs, rhs=rhs, colloc=colloc, normals=normals, areas=areas, verts=verts, wake=wake,
                    forces=forces)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Shared-AIC steady sweep: one AIC per wing at alpha = 0 (collocation factor
+# 1/2, 100-chord wake along +x), every alpha a right-hand side.  Built from
+# the same operators as vlm_run; the reference's LU::solve takes several
+# right-hand sides (vlm_backend_cpu_lapack.cpp:52-64).
+# ---------------------------------------------------------------------------
+def vlm_shared(verts_init, alphas, u_inf=1.0, rho=1.0, dtype=np.float64, ref_pt=(0.0, 0.0, 0.0), sigma=0.0):
+    T = np.dtype(dtype).type
+    r0 = vlm_run(verts_init, 0.0, 0.0, u_inf, rho, dtype, sigma, ref_pt, return_state=True)
+    lhs, normals, areas, verts, wake = r0["lhs"], r0["normals"], r0["areas"], r0["verts"], r0["wake"]
+    ns, nc = dims(verts)
+    lu, piv = lu_factor(lhs.copy(order="F"))
+    tr = translation(np.array([T(-100.0) * T(u_inf), T(0), T(0)], dtype), dtype)
+    ref_disp = np.asarray(ref_pt, dtype) + tr[0:3, 3]
+    out = []
+    for al in alphas:
+        fs = freestream(u_inf, al, 0.0, dtype)
+        vel = []
+        for s, c in zip(ns, nc):
+            v = np.empty((3, c, s), dtype)
+            v[0], v[1], v[2] = fs[0], fs[1], fs[2]
+            vel.append(v)
+        rhs = np.zeros(sum(a * b for a, b in zip(ns, nc)), dtype)
+        rhs_assemble_velocities(rhs, normals, vel)
+        x = lu_solve(lu, piv, rhs)
+        gam, deltas, gwake, off = [], [], [], 0
+        for s, c in zip(ns, nc):
+            g = x[off:off + s * c].reshape(c, s).copy()
+            off += s * c
+            gam.append(g)
+            deltas.append(gamma_delta(g))
+            gw = np.zeros((1, s), dtype)
+            gw[0] = g[-1]
+            gwake.append(gw)
+        forces = [forces_steady(v, d, u) for v, d, u in zip(verts, deltas, vel)]
+        cl = coeff_cl_multibody(forces, areas, fs, T(rho))
+        cm = coeff_cm_multibody(forces, verts, areas, ref_disp, fs, T(rho))
+        cdn, at = T(0), T(0)
+        for w, gw, a in zip(wake, gwake, areas):
+            area = asum(a)
+            cdn += trefftz_cd(w, gw, sigma) / (np.dot(fs, fs) * area) * area
+            at += area
+        out.append(dict(cl=cl, cdi=T(cdn / at), cm=cm, gamma=gam))
     return out

@@ -1,0 +1,101 @@
+"""Batched steady solver (C ABI gbvlm_batch_*) against the double oracle.
+
+Target of the batched mixed-precision path: CL, CM and CDi within a relative
+1e-5 of the full double solve (geometry, assembly and LU in double).  Also
+checks the result of every case is the same alone and inside the batch."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tinyvlm_gb300 import mesh as M
+from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+from tinyvlm_gb300.vlm import VLM, FlowData
+
+pytestmark = pytest.mark.gpu
+REF = (0.25, 0.0, 0.0)
+TOL = 1e-5
+
+
+def _ref(mode, c):
+    v64 = c.verts.astype(np.float64)
+    if mode == "shared":
+        return O.vlm_shared([v64], c.alphas, ref_pt=REF)
+    return [O.vlm_run([v64], a, dtype=np.float64, ref_pt=REF) for a in c.alphas]
+
+
+def _check(co, gam, cases, mode):
+    k = 0
+    cl_all = [float(r["cl"]) for c in cases for r in _ref(mode, c)]
+    guard = 1e-3 * max(abs(x) for x in cl_all)
+    for c in cases:
+        for r in _ref(mode, c):
+            cl = float(r["cl"])
+            assert abs(co[k, 0] - cl) <= TOL * max(abs(cl), guard), ("CL", mode, k, co[k, 0], cl)
+            cms = max(np.abs(r["cm"]).max(), 1e-6)
+            assert np.abs(co[k, 2:5] - r["cm"]).max() <= TOL * cms, ("CM", mode, k, co[k, 2:5], r["cm"])
+            cd = float(r["cdi"])
+            assert abs(co[k, 1] - cd) <= TOL * max(abs(cd), 1e-6) + 1e-12, ("CDi", mode, k, co[k, 1], cd)
+            if gam is not None:
+                g = np.concatenate([x.ravel() for x in r["gamma"]])
+                assert np.linalg.norm(gam[k] - g) <= 1e-5 * np.linalg.norm(g) + 1e-7, ("gamma", mode, k)
+            k += 1
+
+
+@pytest.mark.parametrize("mode", ["shared", "exact"])
+@pytest.mark.parametrize("refine", [0, 1])
+def test_batch_matches_double_oracle(cuda, mode, refine):
+    cases = M.batch_cases(10, seed=11, n_alpha=3, nc_range=(4, 12), ns_range=(4, 24))
+    bs = BatchSolver(cases, mode=mode, refine=refine)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run(want_gamma=True)
+    co, gam = bs.results(gamma=True)
+    _check(co, gam, cases, mode)
+    # run again (graph replay) with new angles
+    for c in cases:
+        c.alphas = c.alphas[::-1].copy()
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run(want_gamma=False)
+    co2, _ = bs.results()
+    _check(co2, None, cases, mode)
+
+
+def test_batch_large_cases(cuda):
+    """Sizes up to the full workload's largest (32 x 64 = 2048 panels)."""
+    cases = M.batch_cases(4, seed=3, n_alpha=2, nc_range=(28, 32), ns_range=(56, 64))
+    bs = BatchSolver(cases, mode="shared", refine=1)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run()
+    co, _ = bs.results()
+    _check(co, None, cases, "shared")
+
+
+def test_alone_equals_in_mix(cuda):
+    cases = M.batch_cases(8, seed=5, n_alpha=2, nc_range=(4, 10), ns_range=(4, 20))
+    bs = BatchSolver(cases, mode="exact", refine=1)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run()
+    mix, _ = bs.results()
+    for i, c in enumerate(cases):
+        one = BatchSolver([c], mode="exact", refine=1)
+        one.set_inputs(pack_verts([c]), pack_alphas([c]), ref_pt=REF)
+        one.run()
+        alone, _ = one.results()
+        np.testing.assert_allclose(alone, mix[2 * i:2 * i + 2], rtol=1e-12, atol=1e-14)
+
+
+def test_batch_vs_plain_double_path(cuda):
+    """The batched mixed-precision path against the plain per-solve double GPU path."""
+    cases = M.batch_cases(3, seed=9, n_alpha=2, nc_range=(6, 10), ns_range=(8, 16))
+    bs = BatchSolver(cases, mode="exact", refine=1)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run()
+    co, _ = bs.results()
+    k = 0
+    for c in cases:
+        plain = VLM("gb300", [c.verts], precision=64)
+        for a in c.alphas:
+            r = plain.run(FlowData(a), ref_pt=REF)
+            assert abs(co[k, 0] - r.cl) <= TOL * max(abs(r.cl), 1e-3), (co[k, 0], r.cl)
+            k += 1

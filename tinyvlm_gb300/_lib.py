@@ -65,6 +65,14 @@ def _protos():
     t["gbvlm_vlm_destroy"] = [P]
     t["gbvlm_vlm_run"] = [P, F64, F64, F64, F64, P, P, P, P]
     t["gbvlm_read_plot3d"] = [ctypes.c_char_p, I32, P, P]
+    t["gbvlm_batch_create"] = [P, I32, P, P, I32, I32]
+    t["gbvlm_batch_destroy"] = [P]
+    t["gbvlm_batch_info"] = [P, P, P, P, P, P, P]
+    t["gbvlm_batch_set_inputs"] = [P, P, P, F64, F64, P, P]
+    t["gbvlm_batch_run"] = [P, I32, P]
+    t["gbvlm_batch_results"] = [P, P, P, P]
+    t["gbvlm_batch_profile"] = [P, P, P]
+    t["gbvlm_batch_launches"] = [P, P]
     return t
 
 

@@ -1,0 +1,911 @@
+// Batched steady VLM: many single-surface cases of uneven size, each with
+// several angles of attack, solved in one CUDA graph.
+//
+// Per system (one AIC):
+//   geometry  (double)  wake ring 100 u_inf chords along the freestream of
+//                       the system's geometry angle, collocation points with
+//                       the high-AoA factor, normals, areas
+//                       (vlm/src/vlm.cpp:97-116, vlm_backend_cpu.cpp:391-433);
+//                       positions stored as float hi/lo pairs
+//   assembly  (float)   AIC from relative vectors formed in double-float, so
+//                       input rounding does not enter (vlm_backend_cpu.cpp:84-148)
+//   factor    (float)   variable-size batched LU (gbvlm_lu.cu)
+//   solve     (float + double refinement) residual b - A x in double against
+//                       an unfactored copy of A
+//   loads     (double)  Joukowski forces, CL, CM (compensated sums), Trefftz
+//                       CDi (vlm_backend_cpu.cpp:276-362, ispc:273-323)
+//
+// Two ways to map angles to systems:
+//   GBVLM_BATCH_EXACT : one system per (case, alpha) with the reference's
+//                       alpha-dependent geometry (VLM::run semantics);
+//   GBVLM_BATCH_SHARED: one system per case, geometry at alpha = 0 (wake
+//                       along +x, collocation factor 1/2), every alpha a
+//                       right-hand side V_inf(alpha) of the same AIC.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "gbvlm_internal.h"
+#include "gbvlm_lu.h"
+#include "gbvlm_math.cuh"
+
+namespace gbvlm {
+
+// device description of one system (all pointers into the batch arena)
+struct SysDesc {
+    int64_t ns, nc, n;
+    int32_t case_id, nrhs;
+    int32_t rhs_off;        // first solve index of this system (alphas / outputs)
+    double alpha_geom;      // angle that shapes the geometry
+    const float* vinit;     // case vertices (4, nc+1, ns+1) float, quarter-chord shifted
+    float* vh;              // wing vertex hi (3 planes)
+    float* vl;              // wing vertex lo
+    float* wh;              // wake vertex hi (3 planes, 2 rows)
+    float* wl;
+    float* ch;              // colloc hi (3 planes)
+    float* cl_;             // colloc lo
+    float* nrm;             // normals float (3 planes)
+    double* area;           // panel areas
+    double* vd;             // wing vertices double (3 planes)
+    double* wd;             // wake vertices double (3 planes, 2 rows)
+    double* nrmd;           // normals double
+    float* A;               // AIC (factored in place)
+    float* A2;              // unfactored copy (refinement), may be null
+    int32_t* ipiv;
+    float* X;               // float rhs / solutions (n x nrhs)
+    double* B;              // double rhs (n x nrhs)
+    double* Xd;             // double solution
+    double* R;              // double residual
+    double sarea, smac;     // filled by geometry
+};
+
+struct BatchArgs {
+    SysDesc* sys;
+    int32_t nsys;
+    const double* alphas;   // per solve
+    double u_inf, rho, beta;
+    double ref[3];
+    double* out;            // per solve: cl, cdi, cmx, cmy, cmz
+    float* gamma_out;       // per solve, n floats at goff[solve] (may be null)
+    const int64_t* goff;
+};
+
+__device__ __forceinline__ void split_hl(double x, float& h, float& l) {
+    h = (float)x;
+    l = (float)(x - (double)h);
+}
+
+// ---------------------------------------------------------------------------
+// geometry: one block per system
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
+    SysDesc& S = a.sys[blockIdx.x];
+    const int64_t ns = S.ns, nc = S.nc, nv = (ns + 1) * (nc + 1), np = ns * nc;
+    const double al = S.alpha_geom;
+    for (int64_t v = threadIdx.x; v < nv; v += blockDim.x) {
+        for (int k = 0; k < 3; k++) {
+            double x = (double)S.vinit[k * nv + v];
+            S.vd[k * nv + v] = x;
+            split_hl(x, S.vh[k * nv + v], S.vl[k * nv + v]);
+        }
+    }
+    // wake: row 1 = trailing edge, row 0 = trailing edge + 100 u (cos a, 0, sin a)
+    const double dx = 100.0 * a.u_inf * cos(al), dz = 100.0 * a.u_inf * sin(al);
+    const int64_t wl = 2 * (ns + 1);
+    for (int64_t i = threadIdx.x; i <= ns; i += blockDim.x) {
+        const int64_t te = i + nc * (ns + 1);
+        double x = S.vinit[te], y = S.vinit[nv + te], z = S.vinit[2 * nv + te];
+        double w0[3] = {x + dx, y, z + dz}, w1[3] = {x, y, z};
+        for (int k = 0; k < 3; k++) {
+            S.wd[k * wl + i] = w0[k];
+            S.wd[k * wl + (ns + 1) + i] = w1[k];
+            split_hl(w0[k], S.wh[k * wl + i], S.wl[k * wl + i]);
+            split_hl(w1[k], S.wh[k * wl + (ns + 1) + i], S.wl[k * wl + (ns + 1) + i]);
+        }
+    }
+    __syncthreads();
+    const double factor = (al < (double)EPS_F) ? 0.5 : 0.5 * (al / (sin(al) + (double)EPS_F));
+    const double* v = S.vd;
+    for (int64_t p = threadIdx.x; p < np; p += blockDim.x) {
+        const int64_t i = p % ns, j = p / ns;
+        const int64_t ia = i + j * (ns + 1), ib = ia + 1, ic = ib + (ns + 1), id = ia + (ns + 1);
+        V3<double> v0{v[ia], v[nv + ia], v[2 * nv + ia]}, v1{v[ib], v[nv + ib], v[2 * nv + ib]};
+        V3<double> v2{v[ic], v[nv + ic], v[2 * nv + ic]}, v3_{v[id], v[nv + id], v[2 * nv + id]};
+        V3<double> nn = cross(v3_ - v1, v2 - v0);
+        double l = sqrt(len2(nn));
+        V3<double> n{nn.x / l, nn.y / l, nn.z / l};
+        S.nrmd[p] = n.x; S.nrmd[np + p] = n.y; S.nrmd[2 * np + p] = n.z;
+        S.nrm[p] = (float)n.x; S.nrm[np + p] = (float)n.y; S.nrm[2 * np + p] = (float)n.z;
+        V3<double> f = v3_ - v0, b = v2 - v0, e = v1 - v0;
+        S.area[p] = 0.5 * (sqrt(len2(cross(f, b))) + sqrt(len2(cross(b, e))));
+        V3<double> ch = 0.5 * (((v2 + v3_) - v0) - v1);
+        V3<double> cp = 0.5 * (v0 + v1) + factor * ch;
+        split_hl(cp.x, S.ch[p], S.cl_[p]);
+        split_hl(cp.y, S.ch[np + p], S.cl_[np + p]);
+        split_hl(cp.z, S.ch[2 * np + p], S.cl_[2 * np + p]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// assembly: tiles (system, 128-row block, chordwise ring row, span chunk)
+// ---------------------------------------------------------------------------
+constexpr int BA_THREADS = 128;
+constexpr int BA_SPAN = 128;  // rings per span chunk
+constexpr int BA_W = BA_SPAN + 1;
+
+struct HL {
+    float h, l;
+};
+
+// Walk a strip of rings with double-float positions (top/bot: hi planes at
+// topH[k*BA_W], lo planes at topL[k*BA_W]); f(ring, 4*pi*(v.n + v'.n')).
+template <class F>
+__device__ __forceinline__ void strip_hl(const float* topH, const float* topL, const float* botH, const float* botL,
+                                         int nvs, HL px, HL py, HL pz, float nx, float ny, float nz, F&& f) {
+    auto rel = [&](const float* H, const float* L, int sl, bool mir) {
+        const float y = mir ? df_sub(-py.h, -py.l, H[BA_W + sl], L[BA_W + sl]) : df_sub(py.h, py.l, H[BA_W + sl], L[BA_W + sl]);
+        return make_rel<float>(df_sub(px.h, px.l, H[sl], L[sl]), y, df_sub(pz.h, pz.l, H[2 * BA_W + sl], L[2 * BA_W + sl]));
+    };
+    auto sv = [&](const float* H1, const float* L1, int s1, const float* H0, const float* L0, int s0, float& x, float& y,
+                  float& z) {
+        x = df_sub(H1[s1], L1[s1], H0[s0], L0[s0]);
+        y = df_sub(H1[BA_W + s1], L1[BA_W + s1], H0[BA_W + s0], L0[BA_W + s0]);
+        z = df_sub(H1[2 * BA_W + s1], L1[2 * BA_W + s1], H0[2 * BA_W + s0], L0[2 * BA_W + s0]);
+    };
+    Rel<float> A0 = rel(topH, topL, 0, false), A3 = rel(botH, botL, 0, false);
+    Rel<float> B0 = rel(topH, topL, 0, true), B3 = rel(botH, botL, 0, true);
+    float lx, ly, lz;
+    sv(botH, botL, 0, topH, topL, 0, lx, ly, lz);
+    float Ca = seg_normal<float, false>(A0, A3, lx, ly, lz, nx, ny, nz, 0.f);
+    float Cb = seg_normal<float, false>(B0, B3, lx, ly, lz, nx, -ny, nz, 0.f);
+    for (int k = 1; k < nvs; k++) {
+        const Rel<float> A1 = rel(topH, topL, k, false), A2 = rel(botH, botL, k, false);
+        const Rel<float> B1 = rel(topH, topL, k, true), B2 = rel(botH, botL, k, true);
+        float cx, cy, cz, tx, ty, tz, bx, by, bz;
+        sv(botH, botL, k, topH, topL, k, cx, cy, cz);          // v1 -> v2
+        sv(topH, topL, k, topH, topL, k - 1, tx, ty, tz);      // v0 -> v1
+        sv(botH, botL, k - 1, botH, botL, k, bx, by, bz);      // v2 -> v3
+        const float Cra = seg_normal<float, false>(A1, A2, cx, cy, cz, nx, ny, nz, 0.f);
+        const float Crb = seg_normal<float, false>(B1, B2, cx, cy, cz, nx, -ny, nz, 0.f);
+        float val = seg_normal<float, false>(A0, A1, tx, ty, tz, nx, ny, nz, 0.f) + Cra +
+                    seg_normal<float, false>(A2, A3, bx, by, bz, nx, ny, nz, 0.f) - Ca;
+        val += seg_normal<float, false>(B0, B1, tx, ty, tz, nx, -ny, nz, 0.f) + Crb +
+               seg_normal<float, false>(B2, B3, bx, by, bz, nx, -ny, nz, 0.f) - Cb;
+        f(k - 1, val);
+        A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb;
+    }
+}
+
+__device__ __forceinline__ int find_sys(const int64_t* pfx, int cnt, int64_t b) {
+    int lo = 0, hi = cnt - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pfx[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, const int64_t* tpfx) {
+    __shared__ float sw[2][2][3 * BA_W];  // [row][hi/lo][plane*W + s]
+    const int si = find_sys(tpfx, a.nsys, blockIdx.x);
+    const SysDesc& S = a.sys[si];
+    const int64_t ns = S.ns, nc = S.nc, n = S.n;
+    const int64_t nchunk = (ns + BA_SPAN - 1) / BA_SPAN, nrb = (n + BA_THREADS - 1) / BA_THREADS;
+    int64_t t = blockIdx.x - tpfx[si];
+    const int64_t rb = t % nrb;
+    t /= nrb;
+    const int64_t z = t % nchunk, c = t / nchunk;
+    const int64_t s0 = z * BA_SPAN, s1 = min(s0 + (int64_t)BA_SPAN, ns);
+    const int nvs = (int)(s1 - s0 + 1);
+    const int64_t nv = (ns + 1) * (nc + 1);
+    for (int e = threadIdx.x; e < 2 * 3 * nvs; e += BA_THREADS) {
+        const int r = e / (3 * nvs), rem = e - r * 3 * nvs, k = rem / nvs, sl = rem - k * nvs;
+        const int64_t vi = k * nv + (s0 + sl) + (c + r) * (ns + 1);
+        sw[r][0][k * BA_W + sl] = S.vh[vi];
+        sw[r][1][k * BA_W + sl] = S.vl[vi];
+    }
+    __syncthreads();
+    const int64_t i = rb * BA_THREADS + threadIdx.x;
+    if (i >= n) return;
+    const HL px{S.ch[i], S.cl_[i]}, py{S.ch[n + i], S.cl_[n + i]}, pz{S.ch[2 * n + i], S.cl_[2 * n + i]};
+    const float nx = S.nrm[i], ny = S.nrm[n + i], nz = S.nrm[2 * n + i];
+    const float k4 = 1.0f / (4.0f * PI_F);
+    float* colA = S.A + i + (c * ns + s0) * n;
+    float* colB = S.A2 ? S.A2 + i + (c * ns + s0) * n : nullptr;
+    const bool te = (c == nc - 1);
+    if (!te) {
+        strip_hl(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz, [&](int kk, float v) {
+            const float val = v * k4;
+            colA[(int64_t)kk * n] = val;
+            if (colB) colB[(int64_t)kk * n] = val;
+        });
+        return;
+    }
+    // trailing-edge ring row: wing ring plus the wake ring behind it (Kutta
+    // condition, vlm_backend_cpu.cpp:121-139 with iteration = 1)
+    strip_hl(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz,
+             [&](int kk, float v) { colA[(int64_t)kk * n] = v; });
+    const int64_t wl = 2 * (ns + 1);
+    for (int64_t s = s0; s < s1; s++) {
+        // wake ring: v0=(s,far) v1=(s+1,far) v2=(s+1,TE) v3=(s,TE)
+        float Qh[4][3], Ql[4][3];
+        const int64_t idx[4] = {s, s + 1, (ns + 1) + s + 1, (ns + 1) + s};
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                Qh[q][k] = S.wh[k * wl + idx[q]];
+                Ql[q][k] = S.wl[k * wl + idx[q]];
+            }
+        float val = 0.f;
+#pragma unroll
+        for (int mir = 0; mir < 2; mir++) {
+            Rel<float> R[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float y = mir ? df_sub(-py.h, -py.l, Qh[q][1], Ql[q][1]) : df_sub(py.h, py.l, Qh[q][1], Ql[q][1]);
+                R[q] = make_rel<float>(df_sub(px.h, px.l, Qh[q][0], Ql[q][0]), y, df_sub(pz.h, pz.l, Qh[q][2], Ql[q][2]));
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int e = (q + 1) & 3;
+                const float rx = df_sub(Qh[e][0], Ql[e][0], Qh[q][0], Ql[q][0]);
+                const float ry = df_sub(Qh[e][1], Ql[e][1], Qh[q][1], Ql[q][1]);
+                const float rz = df_sub(Qh[e][2], Ql[e][2], Qh[q][2], Ql[q][2]);
+                val += seg_normal<float, false>(R[q], R[e], rx, ry, rz, nx, mir ? -ny : ny, nz, 0.f);
+            }
+        }
+        float* dst = colA + (s - s0) * n;
+        const float tot = (*dst + val) * k4;
+        *dst = tot;
+        if (colB) colB[(s - s0) * n] = tot;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// right-hand sides: b = -V_inf(alpha).n in double, float copy into X
+// grid: (blocks over max n, systems)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V3<double> freestream_d(double u, double al, double be) {
+    return {u * cos(al) * cos(be), -(u * cos(al) * sin(be)), u * sin(al)};
+}
+
+__global__ void k_batch_rhs(BatchArgs a) {
+    const SysDesc& S = a.sys[blockIdx.y];
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= S.n) return;
+    const double nx = S.nrmd[p], ny = S.nrmd[S.n + p], nz = S.nrmd[2 * S.n + p];
+    for (int q = 0; q < S.nrhs; q++) {
+        const V3<double> V = freestream_d(a.u_inf, a.alphas[S.rhs_off + q], a.beta);
+        const double b = -(V.x * nx + V.y * ny + V.z * nz);
+        S.B[p + q * S.n] = b;
+        S.X[p + q * S.n] = (float)b;
+        S.Xd[p + q * S.n] = 0.0;
+    }
+}
+
+// x (double) += x_float ; grid (blocks over n, systems)
+__global__ void k_batch_accum(BatchArgs a) {
+    const SysDesc& S = a.sys[blockIdx.y];
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= S.n) return;
+    for (int q = 0; q < S.nrhs; q++) S.Xd[p + q * S.n] += (double)S.X[p + q * S.n];
+}
+
+// R = B - A2 Xd in double; X = (float)R.  One thread per row, tiles (system, row block)
+constexpr int RS_THREADS = 128;
+constexpr int RS_MAXRHS = 8;
+__global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, const int64_t* rpfx) {
+    const int si = find_sys(rpfx, a.nsys, blockIdx.x);
+    const SysDesc& S = a.sys[si];
+    const int64_t r = (blockIdx.x - rpfx[si]) * RS_THREADS + threadIdx.x;
+    const int64_t n = S.n;
+    if (r >= n) return;
+    for (int q0 = 0; q0 < S.nrhs; q0 += RS_MAXRHS) {
+        const int nq = min(RS_MAXRHS, S.nrhs - q0);
+        double acc[RS_MAXRHS];
+#pragma unroll
+        for (int q = 0; q < RS_MAXRHS; q++) acc[q] = 0.0;
+        for (int64_t c = 0; c < n; c++) {
+            const double av = (double)S.A2[r + c * n];
+#pragma unroll
+            for (int q = 0; q < RS_MAXRHS; q++)
+                if (q < nq) acc[q] = fma(av, S.Xd[c + (q0 + q) * n], acc[q]);
+        }
+        for (int q = 0; q < nq; q++) {
+            const double res = S.B[r + (q0 + q) * n] - acc[q];
+            S.R[r + (q0 + q) * n] = res;
+            S.X[r + (q0 + q) * n] = (float)res;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// loads: one block per solve.  Forces F = rho dgamma (V x dl) on the bound
+// segment (vlm_backend_cpu.cpp:276-297), CL/CM (:323-362), Trefftz CDi
+// (ispc:273-323), sums compensated in double.
+// ---------------------------------------------------------------------------
+constexpr int LD_THREADS = 256;
+
+__device__ double block_sum_d(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double r = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) r += sh[k];
+    return r;
+}
+
+__device__ __forceinline__ V3<double> bs_d(V3<double> c, V3<double> a, V3<double> b) {
+    // double Biot-Savart (same law, reference cut-offs), unscaled by 1/4pi
+    V3<double> r1 = c - a, r2 = c - b, r0 = b - a;
+    V3<double> cr = cross(r1, r2);
+    double n1 = sqrt(len2(r1)), n2 = sqrt(len2(r2)), sq = len2(cr);
+    if (sq < 1e-10 || n1 < 1e-10 || n2 < 1e-10) return {0, 0, 0};
+    double k = (dot(r0, r1) * n2 - dot(r0, r2) * n1) / (sq * n1 * n2);
+    return k * cr;
+}
+
+__global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const int32_t* solve_sys, int32_t want_gamma) {
+    __shared__ double sh[32];
+    const int32_t sol = blockIdx.x;
+    const int32_t si = solve_sys[sol];
+    const SysDesc& S = a.sys[si];
+    const int q = sol - S.rhs_off;
+    const int64_t ns = S.ns, nc = S.nc, n = S.n, nv = (ns + 1) * (nc + 1);
+    const double al = a.alphas[sol];
+    const V3<double> V = freestream_d(a.u_inf, al, a.beta);
+    V3<double> L{-V.z, 0.0, V.x};
+    const double ll = sqrt(len2(L));
+    L = (1.0 / ll) * L;
+    const double* x = S.Xd + q * n;
+    const double* v = S.vd;
+    CSum cl, cmx, cmy, cmz, ar, mac;
+    for (int64_t p = threadIdx.x; p < n; p += LD_THREADS) {
+        const int64_t i = p % ns, j = p / ns;
+        const double g = x[p], gd = (j > 0) ? g - x[p - ns] : g;
+        const int64_t ia = i + j * (ns + 1), ib = ia + 1;
+        const V3<double> v0{v[ia], v[nv + ia], v[2 * nv + ia]}, v1{v[ib], v[nv + ib], v[2 * nv + ib]};
+        const V3<double> F = (a.rho * gd) * cross(V, v1 - v0);
+        cl.add(dot(F, L));
+        const V3<double> lev = 0.5 * (v0 + v1) - V3<double>{a.ref[0], a.ref[1], a.ref[2]};
+        const V3<double> m = cross(lev, F);
+        cmx.add(m.x);
+        cmy.add(m.y);
+        cmz.add(m.z);
+        ar.add(S.area[p]);
+        if (want_gamma && a.gamma_out) a.gamma_out[a.goff[sol] + p] = (float)g;
+    }
+    // MAC numerator over spanwise stations (vlm_backend_cpu.cpp:443-468)
+    const int64_t last = nc * (ns + 1);
+    for (int64_t i = threadIdx.x; i < ns; i += LD_THREADS) {
+        double c0 = sqrt((v[i] - v[last + i]) * (v[i] - v[last + i]) + (v[nv + i] - v[nv + last + i]) * (v[nv + i] - v[nv + last + i]) +
+                         (v[2 * nv + i] - v[2 * nv + last + i]) * (v[2 * nv + i] - v[2 * nv + last + i]));
+        double c1 = sqrt((v[i + 1] - v[last + i + 1]) * (v[i + 1] - v[last + i + 1]) +
+                         (v[nv + i + 1] - v[nv + last + i + 1]) * (v[nv + i + 1] - v[nv + last + i + 1]) +
+                         (v[2 * nv + i + 1] - v[2 * nv + last + i + 1]) * (v[2 * nv + i + 1] - v[2 * nv + last + i + 1]));
+        double w = sqrt((v[i + 1] - v[i]) * (v[i + 1] - v[i]) + (v[nv + i + 1] - v[nv + i]) * (v[nv + i + 1] - v[nv + i]) +
+                        (v[2 * nv + i + 1] - v[2 * nv + i]) * (v[2 * nv + i + 1] - v[2 * nv + i]));
+        mac.add(0.5 * (c0 * c0 + c1 * c1) * w);
+    }
+    // Trefftz drag over the wake ring row (trailing segments only)
+    CSum cd;
+    const double* w = S.wd;
+    const int64_t wl = 2 * (ns + 1);
+    auto WP = [&](int64_t idx) { return V3<double>{w[idx], w[wl + idx], w[2 * wl + idx]}; };
+    const double* gte = x + (nc - 1) * ns;  // trailing-edge gamma = wake gamma
+    for (int64_t j = threadIdx.x; j < ns; j += LD_THREADS) {
+        const V3<double> q0 = WP(j), q1 = WP(j + 1), q2 = WP((ns + 1) + j + 1), q3 = WP((ns + 1) + j);
+        const V3<double> c = 0.25 * (((q0 + q1) + q2) + q3);
+        V3<double> nn = cross(q3 - q1, q2 - q0);
+        nn = (1.0 / sqrt(len2(nn))) * nn;
+        V3<double> inf{0, 0, 0};
+        for (int64_t jj = 0; jj < ns; jj++) {
+            const V3<double> w0 = WP(jj), w1 = WP(jj + 1), w2 = WP((ns + 1) + jj + 1), w3 = WP((ns + 1) + jj);
+            V3<double> s{0, 0, 0};
+            V3<double> cm_{c.x, -c.y, c.z};
+            V3<double> t = bs_d(c, w1, w2) + bs_d(c, w3, w0);
+            V3<double> tm = bs_d(cm_, w1, w2) + bs_d(cm_, w3, w0);
+            s = V3<double>{t.x + tm.x, t.y - tm.y, t.z + tm.z};
+            inf = inf + gte[jj] * s;
+        }
+        const double iv = dot(inf, nn) / (4.0 * (double)PI_F);
+        cd.add(-gte[j] * iv * sqrt(len2(q1 - q0)));
+    }
+    const double s_cl = block_sum_d(cl.value(), sh), s_x = block_sum_d(cmx.value(), sh);
+    const double s_y = block_sum_d(cmy.value(), sh), s_z = block_sum_d(cmz.value(), sh);
+    const double s_ar = block_sum_d(ar.value(), sh), s_mac = block_sum_d(mac.value(), sh);
+    const double s_cd = block_sum_d(cd.value(), sh);
+    if (threadIdx.x == 0) {
+        const double v2 = len2(V);
+        const double macv = s_mac / s_ar;
+        double* o = a.out + 5 * (int64_t)sol;
+        o[0] = s_cl / (0.5 * a.rho * v2 * s_ar);
+        o[1] = s_cd / (v2 * s_ar);
+        const double d = 0.5 * a.rho * v2 * s_ar * macv;
+        o[2] = s_x / d;
+        o[3] = s_y / d;
+        o[4] = s_z / d;
+    }
+}
+
+}  // namespace gbvlm
+
+using namespace gbvlm;
+
+// ===========================================================================
+// host object
+// ===========================================================================
+struct gbvlm_batch_s {
+    int32_t ncases = 0, nsys = 0, nsolve = 0, mode = 0, refine = 1;
+    std::vector<gbvlm_dims> dims;
+    std::vector<int32_t> nalpha;
+    std::vector<int64_t> case_voff;   // float offsets of case vertices in the input buffer
+    std::vector<int64_t> solve_n;     // n per solve
+    std::vector<int64_t> goff;        // gamma offsets per solve
+    int64_t vin_floats = 0, gamma_floats = 0;
+    std::vector<SysDesc> sys;         // sorted by n descending
+    std::vector<int32_t> solve_sys;   // solve -> system (sorted index)
+    std::vector<int32_t> solve_order; // solve index in user order -> solve index in batch order
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    float* d_vin = nullptr;
+    double* d_alpha = nullptr;   // per solve (batch order)
+    double* d_out = nullptr;     // per solve x5 (batch order)
+    float* d_gamma = nullptr;
+    int64_t* d_goff = nullptr;
+    SysDesc* d_sys = nullptr;
+    int32_t* d_solve_sys = nullptr;
+    int64_t* d_tpfx = nullptr;   // assembly tiles
+    int64_t* d_rpfx = nullptr;   // residual tiles
+    int64_t assembly_tiles = 0, residual_tiles = 0;
+    int64_t maxn = 0;
+    LuPlan plan;
+    LuBatch<float> lub;
+    double u_inf = 1, rho = 1, beta = 0, ref[3] = {0, 0, 0};
+    int32_t want_gamma = 0;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    double interactions = 0, lu_flops = 0;
+    int64_t launches = 0;
+    ~gbvlm_batch_s() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+        if (arena) cudaFree(arena);
+        plan.release();
+    }
+};
+
+static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    int64_t nlaunch = 0;
+    for (const LuStep& S : h->plan.steps)
+        nlaunch += (S.n_panel > 0) + (S.swap_total > 0) + (S.trsm_blocks > 0) + (S.upd_blocks > 0);
+    int32_t mr = 0;
+    for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
+    const int64_t solves = (mr + 7) / 8;
+    h->launches = 3 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
+    BatchArgs a;
+    a.sys = h->d_sys;
+    a.nsys = h->nsys;
+    a.alphas = h->d_alpha;
+    a.u_inf = h->u_inf;
+    a.rho = h->rho;
+    a.beta = h->beta;
+    for (int k = 0; k < 3; k++) a.ref[k] = h->ref[k];
+    a.out = h->d_out;
+    a.gamma_out = h->d_gamma;
+    a.goff = h->d_goff;
+    mark(0);
+    k_batch_geom<<<h->nsys, 256, 0, st>>>(a);
+    GB_LAUNCH_CHECK();
+    mark(1);
+    k_batch_assemble<<<(unsigned)h->assembly_tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx);
+    GB_LAUNCH_CHECK();
+    mark(2);
+    dim3 g((unsigned)cdiv(h->maxn, 256), (unsigned)h->nsys);
+    k_batch_rhs<<<g, 256, 0, st>>>(a);
+    GB_LAUNCH_CHECK();
+    mark(3);
+    int rc = lu_batch_factor<float>(h->lub, h->plan, st);
+    if (rc) return rc;
+    mark(4);
+    int32_t maxrhs = 0;
+    for (auto& s : h->sys) maxrhs = std::max(maxrhs, s.nrhs);
+    rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, st);
+    if (rc) return rc;
+    k_batch_accum<<<g, 256, 0, st>>>(a);
+    GB_LAUNCH_CHECK();
+    for (int it = 0; it < h->refine; it++) {
+        k_batch_residual<<<(unsigned)h->residual_tiles, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+        GB_LAUNCH_CHECK();
+        rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, st);
+        if (rc) return rc;
+        k_batch_accum<<<g, 256, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+    }
+    mark(5);
+    k_batch_loads<<<h->nsolve, LD_THREADS, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+    GB_LAUNCH_CHECK();
+    mark(6);
+    return GBVLM_OK;
+}
+
+extern "C" {
+
+int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims, const int32_t* nalpha, int32_t mode,
+                       int32_t refine_iters) {
+    GB_REQUIRE(out && dims && nalpha && ncases >= 1, "bad batch arguments");
+    GB_REQUIRE(mode == GBVLM_BATCH_EXACT || mode == GBVLM_BATCH_SHARED, "unknown batch mode %d", mode);
+    GB_REQUIRE(refine_iters >= 0 && refine_iters <= 8, "refine_iters outside [0, 8]");
+    auto* h = new gbvlm_batch_s();
+    h->ncases = ncases;
+    h->mode = mode;
+    h->refine = refine_iters;
+    h->dims.assign(dims, dims + ncases);
+    h->nalpha.assign(nalpha, nalpha + ncases);
+    struct Proto {
+        int32_t case_id;
+        int64_t n;
+        int32_t nrhs;
+        int32_t first_user_solve;
+    };
+    std::vector<Proto> protos;
+    int32_t user_solve = 0;
+    for (int c = 0; c < ncases; c++) {
+        if (dims[c].ns < 1 || dims[c].nc < 1 || nalpha[c] < 1 || nalpha[c] > 64) {
+            delete h;
+            set_error("case %d: bad sizes (ns=%lld nc=%lld nalpha=%d)", c, (long long)dims[c].ns,
+                      (long long)dims[c].nc, nalpha[c]);
+            return GBVLM_ERR_ARG;
+        }
+        h->case_voff.push_back(h->vin_floats);
+        h->vin_floats += 4 * (dims[c].ns + 1) * (dims[c].nc + 1);
+        const int64_t n = dims[c].ns * dims[c].nc;
+        if (mode == GBVLM_BATCH_SHARED) {
+            protos.push_back({c, n, nalpha[c], user_solve});
+        } else {
+            for (int q = 0; q < nalpha[c]; q++) protos.push_back({c, n, 1, user_solve + q});
+        }
+        user_solve += nalpha[c];
+    }
+    h->nsolve = user_solve;
+    std::vector<int> order(protos.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return protos[x].n > protos[y].n; });
+    h->nsys = (int32_t)protos.size();
+    // arena layout
+    size_t bytes = 0;
+    auto reserve = [&](size_t b) {
+        size_t o = bytes;
+        bytes += (b + 255) / 256 * 256;
+        return o;
+    };
+    struct Off {
+        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, ipiv, X, B, Xd, R;
+    };
+    std::vector<Off> offs(h->nsys);
+    const size_t o_vin = reserve(sizeof(float) * h->vin_floats);
+    for (int k = 0; k < h->nsys; k++) {
+        const Proto& P = protos[order[k]];
+        const gbvlm_dims& d = dims[P.case_id];
+        const int64_t nv = (d.ns + 1) * (d.nc + 1), n = P.n, wv = 2 * (d.ns + 1);
+        Off& o = offs[k];
+        o.vh = reserve(sizeof(float) * 3 * nv);
+        o.vl = reserve(sizeof(float) * 3 * nv);
+        o.wh = reserve(sizeof(float) * 3 * wv);
+        o.wl = reserve(sizeof(float) * 3 * wv);
+        o.ch = reserve(sizeof(float) * 3 * n);
+        o.cl = reserve(sizeof(float) * 3 * n);
+        o.nrm = reserve(sizeof(float) * 3 * n);
+        o.area = reserve(sizeof(double) * n);
+        o.vd = reserve(sizeof(double) * 3 * nv);
+        o.wd = reserve(sizeof(double) * 3 * wv);
+        o.nrmd = reserve(sizeof(double) * 3 * n);
+        o.A = reserve(sizeof(float) * n * n);
+        o.A2 = refine_iters > 0 ? reserve(sizeof(float) * n * n) : (size_t)-1;
+        o.ipiv = reserve(sizeof(int32_t) * n);
+        o.X = reserve(sizeof(float) * n * P.nrhs);
+        o.B = reserve(sizeof(double) * n * P.nrhs);
+        o.Xd = reserve(sizeof(double) * n * P.nrhs);
+        o.R = reserve(sizeof(double) * n * P.nrhs);
+        h->interactions += (double)n * (double)n + (double)n * d.ns;
+        h->lu_flops += 2.0 / 3.0 * (double)n * n * n;
+    }
+    const size_t o_alpha = reserve(sizeof(double) * h->nsolve);
+    const size_t o_out = reserve(sizeof(double) * 5 * h->nsolve);
+    // gamma per solve in batch order
+    std::vector<int32_t> solve_sys;
+    std::vector<int64_t> goff;
+    int64_t gtot = 0;
+    for (int k = 0; k < h->nsys; k++) {
+        for (int q = 0; q < protos[order[k]].nrhs; q++) {
+            solve_sys.push_back(k);
+            goff.push_back(gtot);
+            gtot += protos[order[k]].n;
+        }
+    }
+    h->gamma_floats = gtot;
+    const size_t o_gamma = reserve(sizeof(float) * gtot);
+    const size_t o_goff = reserve(sizeof(int64_t) * goff.size());
+    const size_t o_sys = reserve(sizeof(SysDesc) * h->nsys);
+    const size_t o_ssys = reserve(sizeof(int32_t) * solve_sys.size());
+    // tile prefix tables
+    std::vector<int64_t> tpfx(h->nsys + 1, 0), rpfx(h->nsys + 1, 0);
+    for (int k = 0; k < h->nsys; k++) {
+        const gbvlm_dims& d = dims[protos[order[k]].case_id];
+        const int64_t n = protos[order[k]].n;
+        tpfx[k + 1] = tpfx[k] + cdiv(n, BA_THREADS) * cdiv(d.ns, BA_SPAN) * d.nc;
+        rpfx[k + 1] = rpfx[k] + cdiv(n, RS_THREADS);
+    }
+    h->assembly_tiles = tpfx[h->nsys];
+    h->residual_tiles = rpfx[h->nsys];
+    const size_t o_tpfx = reserve(sizeof(int64_t) * tpfx.size());
+    const size_t o_rpfx = reserve(sizeof(int64_t) * rpfx.size());
+    // LU tables
+    const size_t o_lun = reserve(sizeof(int64_t) * h->nsys);
+    const size_t o_luA = reserve(sizeof(float*) * h->nsys);
+    const size_t o_lup = reserve(sizeof(int32_t*) * h->nsys);
+    const size_t o_luinfo = reserve(sizeof(int32_t) * h->nsys);
+    const size_t o_luX = reserve(sizeof(float*) * h->nsys);
+    const size_t o_lurhs = reserve(sizeof(int32_t) * h->nsys);
+    cudaError_t e = cudaMalloc(&h->arena, bytes);
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "cudaMalloc(batch arena)", __FILE__, __LINE__);
+    }
+    h->arena_bytes = bytes;
+    char* base = (char*)h->arena;
+    h->d_vin = (float*)(base + o_vin);
+    h->d_alpha = (double*)(base + o_alpha);
+    h->d_out = (double*)(base + o_out);
+    h->d_gamma = (float*)(base + o_gamma);
+    h->d_goff = (int64_t*)(base + o_goff);
+    h->d_sys = (SysDesc*)(base + o_sys);
+    h->d_solve_sys = (int32_t*)(base + o_ssys);
+    h->d_tpfx = (int64_t*)(base + o_tpfx);
+    h->d_rpfx = (int64_t*)(base + o_rpfx);
+    // system descriptors
+    h->sys.resize(h->nsys);
+    std::vector<int64_t> lun(h->nsys);
+    std::vector<float*> luA(h->nsys), luX(h->nsys);
+    std::vector<int32_t*> lup(h->nsys);
+    std::vector<int32_t> lurhs(h->nsys);
+    int32_t rhs_off = 0;
+    h->solve_order.assign(h->nsolve, 0);
+    for (int k = 0; k < h->nsys; k++) {
+        const Proto& P = protos[order[k]];
+        const gbvlm_dims& d = dims[P.case_id];
+        const Off& o = offs[k];
+        SysDesc& S = h->sys[k];
+        memset(&S, 0, sizeof(S));
+        S.ns = d.ns;
+        S.nc = d.nc;
+        S.n = P.n;
+        S.case_id = P.case_id;
+        S.nrhs = P.nrhs;
+        S.rhs_off = rhs_off;
+        for (int q = 0; q < P.nrhs; q++) h->solve_order[P.first_user_solve + q] = rhs_off + q;
+        rhs_off += P.nrhs;
+        S.vinit = h->d_vin + h->case_voff[P.case_id];
+        S.vh = (float*)(base + o.vh);
+        S.vl = (float*)(base + o.vl);
+        S.wh = (float*)(base + o.wh);
+        S.wl = (float*)(base + o.wl);
+        S.ch = (float*)(base + o.ch);
+        S.cl_ = (float*)(base + o.cl);
+        S.nrm = (float*)(base + o.nrm);
+        S.area = (double*)(base + o.area);
+        S.vd = (double*)(base + o.vd);
+        S.wd = (double*)(base + o.wd);
+        S.nrmd = (double*)(base + o.nrmd);
+        S.A = (float*)(base + o.A);
+        S.A2 = o.A2 == (size_t)-1 ? nullptr : (float*)(base + o.A2);
+        S.ipiv = (int32_t*)(base + o.ipiv);
+        S.X = (float*)(base + o.X);
+        S.B = (double*)(base + o.B);
+        S.Xd = (double*)(base + o.Xd);
+        S.R = (double*)(base + o.R);
+        lun[k] = P.n;
+        luA[k] = S.A;
+        lup[k] = S.ipiv;
+        luX[k] = S.X;
+        lurhs[k] = P.nrhs;
+        h->maxn = std::max(h->maxn, P.n);
+    }
+    h->solve_sys = solve_sys;
+    h->goff = goff;
+    int rc = GBVLM_OK;
+    auto up = [&](void* dst, const void* src, size_t b) {
+        if (rc == GBVLM_OK && b) {
+            cudaError_t ee = cudaMemcpy(dst, src, b, cudaMemcpyHostToDevice);
+            if (ee != cudaSuccess) rc = cuda_fail(ee, "cudaMemcpy(batch tables)", __FILE__, __LINE__);
+        }
+    };
+    up(h->d_sys, h->sys.data(), sizeof(SysDesc) * h->nsys);
+    up(h->d_solve_sys, solve_sys.data(), sizeof(int32_t) * solve_sys.size());
+    up(h->d_goff, goff.data(), sizeof(int64_t) * goff.size());
+    up(h->d_tpfx, tpfx.data(), sizeof(int64_t) * tpfx.size());
+    up(h->d_rpfx, rpfx.data(), sizeof(int64_t) * rpfx.size());
+    up(base + o_lun, lun.data(), sizeof(int64_t) * h->nsys);
+    up(base + o_luA, luA.data(), sizeof(float*) * h->nsys);
+    up(base + o_lup, lup.data(), sizeof(int32_t*) * h->nsys);
+    up(base + o_luX, luX.data(), sizeof(float*) * h->nsys);
+    up(base + o_lurhs, lurhs.data(), sizeof(int32_t) * h->nsys);
+    if (rc == GBVLM_OK) {
+        cudaError_t ee = cudaMemset(base + o_luinfo, 0, sizeof(int32_t) * h->nsys);
+        if (ee != cudaSuccess) rc = cuda_fail(ee, "cudaMemset", __FILE__, __LINE__);
+    }
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    h->lub.n = (const int64_t*)(base + o_lun);
+    h->lub.ld = (const int64_t*)(base + o_lun);  // leading dimension = n
+    h->lub.A = (float* const*)(base + o_luA);
+    h->lub.ipiv = (int32_t* const*)(base + o_lup);
+    h->lub.info = (int32_t*)(base + o_luinfo);
+    h->lub.X = (float* const*)(base + o_luX);
+    h->lub.ldx = (const int64_t*)(base + o_lun);
+    h->lub.nrhs = (const int32_t*)(base + o_lurhs);
+    std::vector<int64_t> ns_sorted(lun.begin(), lun.end());
+    rc = lu_plan_build(h->plan, ns_sorted, 0);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBVLM_OK;
+}
+
+int gbvlm_batch_destroy(gbvlm_batch h) {
+    delete h;
+    return GBVLM_OK;
+}
+
+int gbvlm_batch_info(gbvlm_batch h, int64_t* nsolve, int64_t* nsys, int64_t* gamma_floats, double* interactions,
+                     double* lu_flops, int64_t* arena_bytes) {
+    GB_REQUIRE(h, "null batch");
+    if (nsolve) *nsolve = h->nsolve;
+    if (nsys) *nsys = h->nsys;
+    if (gamma_floats) *gamma_floats = h->gamma_floats;
+    if (interactions) *interactions = h->interactions;
+    if (lu_flops) *lu_flops = h->lu_flops;
+    if (arena_bytes) *arena_bytes = (int64_t)h->arena_bytes;
+    return GBVLM_OK;
+}
+
+int gbvlm_batch_launches(gbvlm_batch h, int64_t* out) {
+    GB_REQUIRE(h && out, "null argument");
+    GB_REQUIRE(h->exec != nullptr || h->launches > 0, "run the batch first");
+    *out = h->launches;
+    return GBVLM_OK;
+}
+
+int gbvlm_batch_set_inputs(gbvlm_batch h, const float* verts, const double* alphas, double u_inf, double rho,
+                           const double* ref_pt, gbvlm_stream stream) {
+    GB_REQUIRE(h && verts && alphas, "null argument");
+    GB_REQUIRE(u_inf > 0 && rho > 0, "u_inf and rho must be positive");
+    cudaStream_t st = to_cuda(stream);
+    // conditions baked into the graph: rebuild it if they change
+    const double r[3] = {ref_pt ? ref_pt[0] : 0, ref_pt ? ref_pt[1] : 0, ref_pt ? ref_pt[2] : 0};
+    if (u_inf != h->u_inf || rho != h->rho || r[0] != h->ref[0] || r[1] != h->ref[1] || r[2] != h->ref[2]) {
+        h->u_inf = u_inf;
+        h->rho = rho;
+        for (int k = 0; k < 3; k++) h->ref[k] = r[k];
+        if (h->exec) {
+            cudaGraphExecDestroy(h->exec);
+            h->exec = nullptr;
+        }
+    }
+    GB_CUDA(cudaMemcpyAsync(h->d_vin, verts, sizeof(float) * h->vin_floats, cudaMemcpyDefault, st));
+    // alphas in user order -> batch order; geometry angles live in the descriptors
+    std::vector<double> al(h->nsolve);
+    for (int32_t u = 0; u < h->nsolve; u++) al[h->solve_order[u]] = alphas[u];
+    bool geom_changed = false;
+    for (auto& S : h->sys) {
+        const double g = (h->mode == GBVLM_BATCH_EXACT) ? al[S.rhs_off] : 0.0;
+        if (g != S.alpha_geom) {
+            S.alpha_geom = g;
+            geom_changed = true;
+        }
+    }
+    if (geom_changed) {
+        GB_CUDA(cudaStreamSynchronize(st));
+        GB_CUDA(cudaMemcpy(h->d_sys, h->sys.data(), sizeof(SysDesc) * h->nsys, cudaMemcpyHostToDevice));
+    }
+    GB_CUDA(cudaMemcpyAsync(h->d_alpha, al.data(), sizeof(double) * h->nsolve, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaStreamSynchronize(st));  // `al` is a host temporary
+    return GBVLM_OK;
+}
+
+int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream) {
+    GB_REQUIRE(h, "null batch");
+    cudaStream_t st = to_cuda(stream);
+    if (want_gamma != h->want_gamma && h->exec) {
+        cudaGraphExecDestroy(h->exec);
+        h->exec = nullptr;
+    }
+    h->want_gamma = want_gamma ? 1 : 0;
+    if (!h->exec) {
+        if (!h->cap) GB_CUDA(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+        if (h->graph) {
+            cudaGraphDestroy(h->graph);
+            h->graph = nullptr;
+        }
+        GB_CUDA(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal));
+        int rc = batch_enqueue(h, h->cap);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(h->cap, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        GB_CUDA(e);
+        h->graph = g;
+        GB_CUDA(cudaGraphInstantiate(&h->exec, h->graph, 0));
+    }
+    GB_CUDA(cudaGraphLaunch(h->exec, st));
+    return GBVLM_OK;
+}
+
+int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream) {
+    GB_REQUIRE(h && stage_ms, "null argument");
+    cudaStream_t st = to_cuda(stream);
+    cudaEvent_t ev[7];
+    for (int k = 0; k < 7; k++) GB_CUDA(cudaEventCreate(&ev[k]));
+    int rc = batch_enqueue(h, st, ev);
+    if (rc == GBVLM_OK) {
+        cudaError_t e = cudaEventSynchronize(ev[6]);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__);
+        for (int k = 0; k < 6 && rc == GBVLM_OK; k++) {
+            e = cudaEventElapsedTime(&stage_ms[k], ev[k], ev[k + 1]);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventElapsedTime", __FILE__, __LINE__);
+        }
+    }
+    for (int k = 0; k < 7; k++) cudaEventDestroy(ev[k]);
+    return rc;
+}
+
+int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_stream stream) {
+    GB_REQUIRE(h && coeffs, "null argument");
+    cudaStream_t st = to_cuda(stream);
+    std::vector<double> tmp(5 * (size_t)h->nsolve);
+    GB_CUDA(cudaMemcpyAsync(tmp.data(), h->d_out, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, st));
+    std::vector<float> gt;
+    if (gamma) {
+        GB_REQUIRE(h->want_gamma, "gamma requested but the last run did not store it");
+        gt.resize(h->gamma_floats);
+        GB_CUDA(cudaMemcpyAsync(gt.data(), h->d_gamma, sizeof(float) * gt.size(), cudaMemcpyDeviceToHost, st));
+    }
+    GB_CUDA(cudaStreamSynchronize(st));
+    int32_t* info = (int32_t*)host_scratch(sizeof(int32_t) * h->nsys);
+    GB_CUDA(cudaMemcpy(info, h->lub.info, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < h->nsys; k++) {
+        if (info[k] != 0) {
+            set_error("batch system %d (case %d): exactly zero pivot at column %d", k, h->sys[k].case_id, info[k]);
+            return GBVLM_ERR_SINGULAR;
+        }
+    }
+    int64_t uoff = 0;
+    for (int32_t u = 0; u < h->nsolve; u++) {
+        const int32_t b = h->solve_order[u];
+        for (int k = 0; k < 5; k++) coeffs[5 * (int64_t)u + k] = tmp[5 * (int64_t)b + k];
+        if (gamma) {
+            const int64_t n = h->sys[h->solve_sys[b]].n;
+            memcpy(gamma + uoff, gt.data() + h->goff[b], sizeof(float) * n);
+            uoff += n;
+        }
+    }
+    return GBVLM_OK;
+}
+
+}  // extern "C"

@@ -208,7 +208,10 @@ struct VlmState : VlmBase {
             off += dims[m].ns * dims[m].nc;
         }
         // coefficient reductions (vlm_backend.cpp:72-139) + Trefftz drag
-        T ref[3] = {(T)(ref_pt ? ref_pt[0] : 0), (T)(ref_pt ? ref_pt[1] : 0), (T)(ref_pt ? ref_pt[2] : 0)};
+        // the wing sits displaced by the wake translation; move the moment
+        // reference with it so CM is the body-frame moment about ref_pt
+        T ref[3] = {(T)(ref_pt ? ref_pt[0] : 0) + tr[12], (T)(ref_pt ? ref_pt[1] : 0) + tr[13],
+                    (T)(ref_pt ? ref_pt[2] : 0) + tr[14]};
         T cl = 0, ta = 0, tm = 0, cdn = 0;
         T cm[3] = {0, 0, 0};
         for (int m = 0; m < nsurf; m++) {
