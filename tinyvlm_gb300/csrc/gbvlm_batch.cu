@@ -60,7 +60,7 @@ struct SysDesc {
     double* B;              // double rhs (n x nrhs)
     double* Xd;             // double solution
     double* R;              // double residual
-    double sarea, smac;     // filled by geometry
+    double* K;              // Trefftz influence (ns x ns) of unit wake gammas
 };
 
 struct BatchArgs {
@@ -93,13 +93,14 @@ __global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
             split_hl(x, S.vh[k * nv + v], S.vl[k * nv + v]);
         }
     }
-    // wake: row 1 = trailing edge, row 0 = trailing edge + 100 u (cos a, 0, sin a)
+    // wake (vlm.cpp:104-114 seen from the displaced wing): row 0 = trailing
+    // edge, row 1 = trailing edge + 100 u (cos a, 0, sin a)
     const double dx = 100.0 * a.u_inf * cos(al), dz = 100.0 * a.u_inf * sin(al);
     const int64_t wl = 2 * (ns + 1);
     for (int64_t i = threadIdx.x; i <= ns; i += blockDim.x) {
         const int64_t te = i + nc * (ns + 1);
         double x = S.vinit[te], y = S.vinit[nv + te], z = S.vinit[2 * nv + te];
-        double w0[3] = {x + dx, y, z + dz}, w1[3] = {x, y, z};
+        double w0[3] = {x, y, z}, w1[3] = {x + dx, y, z + dz};
         for (int k = 0; k < 3; k++) {
             S.wd[k * wl + i] = w0[k];
             S.wd[k * wl + (ns + 1) + i] = w1[k];
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
              [&](int kk, float v) { colA[(int64_t)kk * n] = v; });
     const int64_t wl = 2 * (ns + 1);
     for (int64_t s = s0; s < s1; s++) {
-        // wake ring: v0=(s,far) v1=(s+1,far) v2=(s+1,TE) v3=(s,TE)
+        // wake ring: v0=(s,TE) v1=(s+1,TE) v2=(s+1,far) v3=(s,far)
         float Qh[4][3], Ql[4][3];
         const int64_t idx[4] = {s, s + 1, (ns + 1) + s + 1, (ns + 1) + s};
 #pragma unroll
@@ -352,6 +353,30 @@ __device__ __forceinline__ V3<double> bs_d(V3<double> c, V3<double> a, V3<double
     return k * cr;
 }
 
+// Trefftz influence matrix of one system: K[j, jj] = -(induced velocity of
+// the trailing legs of wake ring jj with unit gamma, plus mirror, at the
+// centre of wake ring j) . n_j * |dl_j| / (4 pi); CDi = gamma^T K gamma / (|V|^2 S)
+// (ispc:273-323).  grid: (blocks over ns*ns, systems)
+__global__ void k_batch_trefftz_k(BatchArgs a) {
+    const SysDesc& S = a.sys[blockIdx.y];
+    const int64_t ns = S.ns, e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ns * ns) return;
+    const int64_t j = e % ns, jj = e / ns;
+    const double* w = S.wd;
+    const int64_t wl = 2 * (ns + 1);
+    auto WP = [&](int64_t idx) { return V3<double>{w[idx], w[wl + idx], w[2 * wl + idx]}; };
+    const V3<double> q0 = WP(j), q1 = WP(j + 1), q2 = WP((ns + 1) + j + 1), q3 = WP((ns + 1) + j);
+    const V3<double> c = 0.25 * (((q0 + q1) + q2) + q3);
+    V3<double> nn = cross(q3 - q1, q2 - q0);
+    nn = (1.0 / sqrt(len2(nn))) * nn;
+    const V3<double> w0 = WP(jj), w1 = WP(jj + 1), w2 = WP((ns + 1) + jj + 1), w3 = WP((ns + 1) + jj);
+    const V3<double> cm_{c.x, -c.y, c.z};
+    const V3<double> t = bs_d(c, w1, w2) + bs_d(c, w3, w0);
+    const V3<double> tm = bs_d(cm_, w1, w2) + bs_d(cm_, w3, w0);
+    const V3<double> sv{t.x + tm.x, t.y - tm.y, t.z + tm.z};
+    S.K[j + jj * ns] = -dot(sv, nn) / (4.0 * (double)PI_F) * sqrt(len2(q1 - q0));
+}
+
 __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const int32_t* solve_sys, int32_t want_gamma) {
     __shared__ double sh[32];
     const int32_t sol = blockIdx.x;
@@ -394,29 +419,12 @@ __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const i
                         (v[2 * nv + i + 1] - v[2 * nv + i]) * (v[2 * nv + i + 1] - v[2 * nv + i]));
         mac.add(0.5 * (c0 * c0 + c1 * c1) * w);
     }
-    // Trefftz drag over the wake ring row (trailing segments only)
+    // Trefftz drag: gamma_TE^T K gamma_TE (the wake carries the TE gamma)
     CSum cd;
-    const double* w = S.wd;
-    const int64_t wl = 2 * (ns + 1);
-    auto WP = [&](int64_t idx) { return V3<double>{w[idx], w[wl + idx], w[2 * wl + idx]}; };
-    const double* gte = x + (nc - 1) * ns;  // trailing-edge gamma = wake gamma
-    for (int64_t j = threadIdx.x; j < ns; j += LD_THREADS) {
-        const V3<double> q0 = WP(j), q1 = WP(j + 1), q2 = WP((ns + 1) + j + 1), q3 = WP((ns + 1) + j);
-        const V3<double> c = 0.25 * (((q0 + q1) + q2) + q3);
-        V3<double> nn = cross(q3 - q1, q2 - q0);
-        nn = (1.0 / sqrt(len2(nn))) * nn;
-        V3<double> inf{0, 0, 0};
-        for (int64_t jj = 0; jj < ns; jj++) {
-            const V3<double> w0 = WP(jj), w1 = WP(jj + 1), w2 = WP((ns + 1) + jj + 1), w3 = WP((ns + 1) + jj);
-            V3<double> s{0, 0, 0};
-            V3<double> cm_{c.x, -c.y, c.z};
-            V3<double> t = bs_d(c, w1, w2) + bs_d(c, w3, w0);
-            V3<double> tm = bs_d(cm_, w1, w2) + bs_d(cm_, w3, w0);
-            s = V3<double>{t.x + tm.x, t.y - tm.y, t.z + tm.z};
-            inf = inf + gte[jj] * s;
-        }
-        const double iv = dot(inf, nn) / (4.0 * (double)PI_F);
-        cd.add(-gte[j] * iv * sqrt(len2(q1 - q0)));
+    const double* gte = x + (nc - 1) * ns;
+    for (int64_t e = threadIdx.x; e < ns * ns; e += LD_THREADS) {
+        const int64_t j = e % ns, jj = e / ns;
+        cd.add(gte[j] * S.K[e] * gte[jj]);
     }
     const double s_cl = block_sum_d(cl.value(), sh), s_x = block_sum_d(cmx.value(), sh);
     const double s_y = block_sum_d(cmy.value(), sh), s_z = block_sum_d(cmz.value(), sh);
@@ -488,11 +496,12 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     int64_t nlaunch = 0;
     for (const LuStep& S : h->plan.steps)
-        nlaunch += (S.n_panel > 0) + (S.swap_total > 0) + (S.trsm_blocks > 0) + (S.upd_blocks > 0);
+        nlaunch += (S.n_tall_by_elem[0] > 0) + (S.n_panel > S.n_tall_by_elem[0]) + (S.swap_total > 0) +
+                   (S.trsm_blocks > 0) + (S.upd_blocks > 0);
     int32_t mr = 0;
     for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
     const int64_t solves = (mr + 7) / 8;
-    h->launches = 3 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
+    h->launches = 4 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
     BatchArgs a;
     a.sys = h->d_sys;
     a.nsys = h->nsys;
@@ -507,6 +516,13 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     mark(0);
     k_batch_geom<<<h->nsys, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
+    {
+        int64_t maxns = 1;
+        for (auto& S : h->sys) maxns = std::max(maxns, S.ns);
+        dim3 gk((unsigned)cdiv(maxns * maxns, 128), (unsigned)h->nsys);
+        k_batch_trefftz_k<<<gk, 128, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+    }
     mark(1);
     k_batch_assemble<<<(unsigned)h->assembly_tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx);
     GB_LAUNCH_CHECK();
@@ -590,7 +606,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         return o;
     };
     struct Off {
-        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, ipiv, X, B, Xd, R;
+        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, ipiv, X, B, Xd, R, K;
     };
     std::vector<Off> offs(h->nsys);
     const size_t o_vin = reserve(sizeof(float) * h->vin_floats);
@@ -617,6 +633,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         o.B = reserve(sizeof(double) * n * P.nrhs);
         o.Xd = reserve(sizeof(double) * n * P.nrhs);
         o.R = reserve(sizeof(double) * n * P.nrhs);
+        o.K = reserve(sizeof(double) * d.ns * d.ns);
         h->interactions += (double)n * (double)n + (double)n * d.ns;
         h->lu_flops += 2.0 / 3.0 * (double)n * n * n;
     }
@@ -714,6 +731,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         S.B = (double*)(base + o.B);
         S.Xd = (double*)(base + o.Xd);
         S.R = (double*)(base + o.R);
+        S.K = (double*)(base + o.K);
         lun[k] = P.n;
         luA[k] = S.A;
         lup[k] = S.ipiv;

@@ -102,6 +102,78 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(LuBatch<T> B, int64_t k
     }
 }
 
+// Same panel factorisation with the panel (rows k..n-1, nb columns) staged in
+// shared memory, column-major with leading dimension `rows`.  Used when the
+// panel fits (PANEL_SMEM_ROWS rows); the panel is read once and written once.
+constexpr int PANEL_SMEM_BYTES = 220 * 1024;
+
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) k_panel_smem(LuBatch<T> B, int64_t k, const int32_t* act) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* P = reinterpret_cast<T*>(smem_raw);
+    const int32_t sid = act[blockIdx.x];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    T* A = B.A[sid];
+    int32_t* ipiv = B.ipiv[sid];
+    const int nb = (int)min((int64_t)GK, n - k);
+    const int rows = (int)(n - k);
+    __shared__ T s_val[PANEL_THREADS / 32];
+    __shared__ int s_idx[PANEL_THREADS / 32];
+    __shared__ int s_piv;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int t = 0; t < nb; t++)
+        for (int r = tid; r < rows; r += PANEL_THREADS) P[t * rows + r] = A[(k + r) + (k + t) * ld];
+    __syncthreads();
+    for (int jj = 0; jj < nb; jj++) {
+        T* c = P + jj * rows;
+        T best = (T)-1;
+        int bi = jj;
+        for (int r = jj + tid; r < rows; r += PANEL_THREADS) {
+            T v = tabs(c[r]);
+            if (v > best) { best = v; bi = r; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            T ov = __shfl_down_sync(0xffffffffu, best, o);
+            int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            T bv = s_val[0];
+            int bix = s_idx[0];
+            for (int w = 1; w < PANEL_THREADS / 32; w++) {
+                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bix)) { bv = s_val[w]; bix = s_idx[w]; }
+            }
+            s_piv = bix;
+            ipiv[k + jj] = (int32_t)(k + bix);
+            if (c[bix] == (T)0 && B.info[sid] == 0) B.info[sid] = (int32_t)(k + jj + 1);
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (p != jj) {
+            for (int t = tid; t < nb; t += PANEL_THREADS) {
+                T tmp = P[t * rows + jj];
+                P[t * rows + jj] = P[t * rows + p];
+                P[t * rows + p] = tmp;
+            }
+        }
+        __syncthreads();
+        const T d = c[jj];
+        const T inv = (d != (T)0) ? (T)1 / d : (T)0;
+        for (int r = jj + 1 + tid; r < rows; r += PANEL_THREADS) {
+            const T l = (d != (T)0) ? c[r] / d : c[r];
+            c[r] = l;
+            for (int t = jj + 1; t < nb; t++) P[t * rows + r] -= l * P[t * rows + jj];
+        }
+        (void)inv;
+        __syncthreads();
+    }
+    for (int t = 0; t < nb; t++)
+        for (int r = tid; r < rows; r += PANEL_THREADS) A[(k + r) + (k + t) * ld] = P[t * rows + r];
+}
+
 // ---------------------------------------------------------------------------
 // swap: one thread per column outside the panel, per system.  col table:
 // blocks enumerated through prefix pfx (over act).
@@ -248,6 +320,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     const int64_t ldx = B.ldx[sid];
     const int32_t* ip = B.ipiv[sid];
     __shared__ T xs[GK][TS_MAXRHS];
+    __shared__ T dg[GK][GK + 1];
     const int tid = threadIdx.x;
     // row interchanges
     if (tid < nr) {
@@ -261,11 +334,16 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     // forward: L (unit lower)
     for (int64_t k = 0; k < n; k += GK) {
         const int nb = (int)min((int64_t)GK, n - k);
+        for (int e = tid; e < nb * nb; e += TS_THREADS) {
+            const int r = e % nb, c = e / nb;
+            dg[r][c] = A[(k + r) + (k + c) * ld];
+        }
+        __syncthreads();
         if (tid < nr) {
             T* x = X + tid * ldx;
             for (int r = 0; r < nb; r++) {
                 T s = x[k + r];
-                for (int l = 0; l < r; l++) s -= A[(k + r) + (k + l) * ld] * xs[l][tid];
+                for (int l = 0; l < r; l++) s -= dg[r][l] * xs[l][tid];
                 xs[r][tid] = s;
                 x[k + r] = s;
             }
@@ -289,12 +367,17 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     for (int64_t bk = nblk - 1; bk >= 0; bk--) {
         const int64_t k = bk * GK;
         const int nb = (int)min((int64_t)GK, n - k);
+        for (int e = tid; e < nb * nb; e += TS_THREADS) {
+            const int r = e % nb, c = e / nb;
+            dg[r][c] = A[(k + r) + (k + c) * ld];
+        }
+        __syncthreads();
         if (tid < nr) {
             T* x = X + tid * ldx;
             for (int r = nb - 1; r >= 0; r--) {
                 T s = x[k + r];
-                for (int l = r + 1; l < nb; l++) s -= A[(k + r) + (k + l) * ld] * xs[l][tid];
-                s = s / A[(k + r) + (k + r) * ld];
+                for (int l = r + 1; l < nb; l++) s -= dg[r][l] * xs[l][tid];
+                s = s / dg[r][r];
                 xs[r][tid] = s;
                 x[k + r] = s;
             }
@@ -323,8 +406,21 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
     for (size_t s = 0; s < plan.steps.size(); s++) {
         const LuStep& S = plan.steps[s];
         if (S.n_panel == 0) continue;
-        k_panel<T><<<S.n_panel, PANEL_THREADS, 0, st>>>(B, S.k, plan.d_act + S.act_off);
-        GB_LAUNCH_CHECK();
+        // systems are sorted by n descending: the ones whose panel is too tall
+        // for shared memory form a prefix of the active list
+        const int64_t max_rows = (PANEL_SMEM_BYTES / (int64_t)(GK * sizeof(T)));
+        const int n_glob = S.n_tall_by_elem[sizeof(T) == 4 ? 0 : 1];
+        (void)max_rows;
+        if (n_glob > 0) {
+            k_panel<T><<<n_glob, PANEL_THREADS, 0, st>>>(B, S.k, plan.d_act + S.act_off);
+            GB_LAUNCH_CHECK();
+        }
+        if (S.n_panel > n_glob) {
+            const int64_t rows = S.smem_rows[sizeof(T) == 4 ? 0 : 1];
+            const size_t smem = (size_t)rows * GK * sizeof(T);
+            k_panel_smem<T><<<S.n_panel - n_glob, PANEL_THREADS, smem, st>>>(B, S.k, plan.d_act + S.act_off + n_glob);
+            GB_LAUNCH_CHECK();
+        }
         if (S.swap_total > 0) {
             k_swap<T><<<(unsigned)cdiv(S.swap_total, 256), 256, 0, st>>>(B, S.k, plan.d_act + S.act_off,
                                                                        plan.d_pfx + S.swap_pfx, S.n_panel);
@@ -362,6 +458,8 @@ template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, cu
 // active systems of every step form a prefix of the order.
 int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st) {
     plan.release();
+    GB_CUDA(cudaFuncSetAttribute(k_panel_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(k_panel_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
     const int nsys = (int)n_sorted.size();
     for (int i = 1; i < nsys; i++) GB_REQUIRE(n_sorted[i] <= n_sorted[i - 1], "lu plan: sizes not sorted");
     std::vector<int32_t> act;
@@ -375,6 +473,14 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         while (cnt < nsys && n_sorted[cnt] > k) cnt++;
         for (int i = 0; i < cnt; i++) act.push_back(i);
         S.n_panel = cnt;
+        for (int e = 0; e < 2; e++) {
+            const int64_t es = e == 0 ? 4 : 8;
+            const int64_t lim = PANEL_SMEM_BYTES / (GK * es);
+            int tall = 0;
+            while (tall < cnt && n_sorted[tall] - k > lim) tall++;
+            S.n_tall_by_elem[e] = tall;
+            S.smem_rows[e] = tall < cnt ? n_sorted[tall] - k : 0;
+        }
         // swap: columns outside the panel, n - nb each
         S.swap_pfx = (int64_t)pfx.size();
         int64_t acc = 0;

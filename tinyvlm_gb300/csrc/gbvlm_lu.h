@@ -26,6 +26,8 @@ struct LuStep {
     int64_t k = 0;
     int64_t act_off = 0;
     int32_t n_panel = 0;
+    int32_t n_tall_by_elem[2] = {0, 0};  // active systems whose panel exceeds shared memory (float, double)
+    int64_t smem_rows[2] = {0, 0};       // tallest panel of the rest (float, double)
     int64_t swap_pfx = 0, swap_total = 0;
     int64_t trsm_pfx = 0, trsm_blocks = 0;
     int32_t n_upd = 0;
