@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--mode", default="shared", choices=["shared", "exact"])
     p.add_argument("--cases", type=int, default=512)
     p.add_argument("--alphas", type=int, default=8)
-    p.add_argument("--refine", type=int, default=1)
+    p.add_argument("--refine", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)

@@ -501,7 +501,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     int32_t mr = 0;
     for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
     const int64_t solves = (mr + 7) / 8;
-    h->launches = 4 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
+    h->launches = 5 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
     BatchArgs a;
     a.sys = h->d_sys;
     a.nsys = h->nsys;
@@ -536,14 +536,14 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     mark(4);
     int32_t maxrhs = 0;
     for (auto& s : h->sys) maxrhs = std::max(maxrhs, s.nrhs);
-    rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, st);
+    rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st);
     if (rc) return rc;
     k_batch_accum<<<g, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
     for (int it = 0; it < h->refine; it++) {
         k_batch_residual<<<(unsigned)h->residual_tiles, RS_THREADS, 0, st>>>(a, h->d_rpfx);
         GB_LAUNCH_CHECK();
-        rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, st);
+        rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st);
         if (rc) return rc;
         k_batch_accum<<<g, 256, 0, st>>>(a);
         GB_LAUNCH_CHECK();
@@ -606,7 +606,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         return o;
     };
     struct Off {
-        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, ipiv, X, B, Xd, R, K;
+        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, ipiv, perm, X, B, Xd, R, K;
     };
     std::vector<Off> offs(h->nsys);
     const size_t o_vin = reserve(sizeof(float) * h->vin_floats);
@@ -629,6 +629,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         o.A = reserve(sizeof(float) * n * n);
         o.A2 = refine_iters > 0 ? reserve(sizeof(float) * n * n) : (size_t)-1;
         o.ipiv = reserve(sizeof(int32_t) * n);
+        o.perm = reserve(sizeof(int32_t) * n);
         o.X = reserve(sizeof(float) * n * P.nrhs);
         o.B = reserve(sizeof(double) * n * P.nrhs);
         o.Xd = reserve(sizeof(double) * n * P.nrhs);
@@ -674,6 +675,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     const size_t o_luinfo = reserve(sizeof(int32_t) * h->nsys);
     const size_t o_luX = reserve(sizeof(float*) * h->nsys);
     const size_t o_lurhs = reserve(sizeof(int32_t) * h->nsys);
+    const size_t o_luperm = reserve(sizeof(int32_t*) * h->nsys);
     cudaError_t e = cudaMalloc(&h->arena, bytes);
     if (e != cudaSuccess) {
         delete h;
@@ -694,7 +696,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     h->sys.resize(h->nsys);
     std::vector<int64_t> lun(h->nsys);
     std::vector<float*> luA(h->nsys), luX(h->nsys);
-    std::vector<int32_t*> lup(h->nsys);
+    std::vector<int32_t*> lup(h->nsys), lperm(h->nsys);
     std::vector<int32_t> lurhs(h->nsys);
     int32_t rhs_off = 0;
     h->solve_order.assign(h->nsolve, 0);
@@ -735,6 +737,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         lun[k] = P.n;
         luA[k] = S.A;
         lup[k] = S.ipiv;
+        lperm[k] = (int32_t*)(base + o.perm);
         luX[k] = S.X;
         lurhs[k] = P.nrhs;
         h->maxn = std::max(h->maxn, P.n);
@@ -758,6 +761,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     up(base + o_lup, lup.data(), sizeof(int32_t*) * h->nsys);
     up(base + o_luX, luX.data(), sizeof(float*) * h->nsys);
     up(base + o_lurhs, lurhs.data(), sizeof(int32_t) * h->nsys);
+    up(base + o_luperm, lperm.data(), sizeof(int32_t*) * h->nsys);
     if (rc == GBVLM_OK) {
         cudaError_t ee = cudaMemset(base + o_luinfo, 0, sizeof(int32_t) * h->nsys);
         if (ee != cudaSuccess) rc = cuda_fail(ee, "cudaMemset", __FILE__, __LINE__);
@@ -774,6 +778,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     h->lub.X = (float* const*)(base + o_luX);
     h->lub.ldx = (const int64_t*)(base + o_lun);
     h->lub.nrhs = (const int32_t*)(base + o_lurhs);
+    h->lub.perm = (int32_t* const*)(base + o_luperm);
     std::vector<int64_t> ns_sorted(lun.begin(), lun.end());
     rc = lu_plan_build(h->plan, ns_sorted, 0);
     if (rc) {

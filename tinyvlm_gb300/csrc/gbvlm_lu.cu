@@ -30,6 +30,8 @@ constexpr int PANEL_THREADS = 512;
 constexpr int TRSM_COLS = 128;
 constexpr int GT = 64;  // update tile edge
 constexpr int GK = LU_NB;
+constexpr int PERM_SMEM = 12 * 1024;  // systems up to this size build the permutation in shared memory
+constexpr int TS_SMEM_BYTES = 200 * 1024;
 
 template <class T>
 __device__ __forceinline__ T tabs(T x) { return x < (T)0 ? -x : x; }
@@ -248,13 +250,19 @@ __global__ void __launch_bounds__(TRSM_COLS) k_trsm(LuBatch<T> B, int64_t k, con
 }
 
 // ---------------------------------------------------------------------------
-// update: A22 -= L21 * U12 on 64x64 tiles, 256 threads, 4x4 per thread
+// update: A22 -= L21 * U12 on 64x64 tiles, 256 threads, each a 4x4 block of
+// consecutive rows/columns read from shared memory as vectors
 // ---------------------------------------------------------------------------
+template <class T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4; };
+
 template <class T>
 __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const int32_t* act, const int64_t* pfx,
                                                int cnt) {
-    __shared__ T sA[GK][GT + 1];  // L21 tile: [kk][row]
-    __shared__ T sB[GK][GT + 1];  // U12 tile: [kk][col]
+    constexpr int SW = GT + 4;  // row stride keeps 16-byte alignment of every 4-run
+    __shared__ __align__(16) T sA[GK][SW];  // L21 tile: [kk][row]
+    __shared__ __align__(16) T sB[GK][SW];  // U12 tile: [kk][col]
     const int a = find_block(pfx, cnt, blockIdx.x);
     const int32_t sid = act[a];
     const int64_t n = B.n[sid], ld = B.ld[sid];
@@ -265,52 +273,94 @@ __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const i
     const int64_t r0 = k + GK + (t % tiles) * GT, c0 = k + GK + (t / tiles) * GT;
     const int tid = threadIdx.x;
     for (int e = tid; e < GK * GT; e += 256) {
-        int kk = e / GT, rr = e % GT;
-        int64_t r = r0 + rr;
+        const int kk = e / GT, rr = e % GT;
+        const int64_t r = r0 + rr;
         sA[kk][rr] = r < n ? A[r + (k + kk) * ld] : (T)0;
-        int cc = e / GK, k2 = e % GK;  // coalesced along kk for U12 (column-major rows k..k+GK)
-        int64_t c = c0 + cc;
+        const int cc = e / GK, k2 = e % GK;
+        const int64_t c = c0 + cc;
         sB[k2][cc] = c < n ? A[(k + k2) + c * ld] : (T)0;
     }
     __syncthreads();
-    const int tx = tid % 16, ty = tid / 16;
+    const int tx = tid & 15, ty = tid >> 4;
     T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j] = 0;
+    using V = typename Vec4<T>::type;
 #pragma unroll 8
     for (int kk = 0; kk < GK; kk++) {
-        T av[4], bv[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) av[i] = sA[kk][tx + 16 * i];
-#pragma unroll
-        for (int j = 0; j < 4; j++) bv[j] = sB[kk][ty + 16 * j];
+        const V av = *reinterpret_cast<const V*>(&sA[kk][4 * tx]);
+        const V bv = *reinterpret_cast<const V*>(&sB[kk][4 * ty]);
+        const T a4[4] = {av.x, av.y, av.z, av.w}, b4[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
         for (int i = 0; i < 4; i++)
 #pragma unroll
-            for (int j = 0; j < 4; j++) acc[i][j] += av[i] * bv[j];
+            for (int j = 0; j < 4; j++) acc[i][j] += a4[i] * b4[j];
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        const int64_t c = c0 + ty + 16 * j;
+        const int64_t c = c0 + 4 * ty + j;
         if (c >= n) continue;
+        T* col = A + c * ld;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int64_t r = r0 + tx + 16 * i;
-            if (r < n) A[r + c * ld] -= acc[i][j];
+            const int64_t r = r0 + 4 * tx + i;
+            if (r < n) col[r] -= acc[i][j];
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// triangular solves: one CTA per system, all its right-hand sides
+// row permutation of a finished factorisation: perm[r] = original row that
+// ends up in position r (the ipiv interchanges composed in order)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_perm(LuBatch<T> B) {
+    extern __shared__ int32_t sp[];
+    const int32_t sid = blockIdx.x;
+    const int64_t n = B.n[sid];
+    const int32_t* ip = B.ipiv[sid];
+    int32_t* pm = B.perm[sid];
+    if (n <= PERM_SMEM) {
+        for (int64_t r = threadIdx.x; r < n; r += blockDim.x) sp[r] = (int32_t)r;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int64_t r = 0; r < n; r++) {
+                const int32_t p = ip[r];
+                const int32_t t = sp[r];
+                sp[r] = sp[p];
+                sp[p] = t;
+            }
+        }
+        __syncthreads();
+        for (int64_t r = threadIdx.x; r < n; r += blockDim.x) pm[r] = sp[r];
+    } else {
+        for (int64_t r = threadIdx.x; r < n; r += blockDim.x) pm[r] = (int32_t)r;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int64_t r = 0; r < n; r++) {
+                const int32_t p = ip[r];
+                const int32_t t = pm[r];
+                pm[r] = pm[p];
+                pm[p] = t;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves, one CTA per system and block of up to TS_MAXRHS
+// right-hand sides held in shared memory (n * nrhs values).  The diagonal
+// blocks are solved one warp per right-hand side, a lane per row: after
+// row r is final, lanes below subtract L[l][r] x_r in parallel.
 // ---------------------------------------------------------------------------
 constexpr int TS_THREADS = 256;
 constexpr int TS_MAXRHS = 8;
 
 template <class T>
-__global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rhs0, int32_t nrhs_blk) {
+__global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rhs0, int32_t nrhs_blk, int use_smem) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int32_t sid = blockIdx.x;
     const int64_t n = B.n[sid], ld = B.ld[sid];
     const T* A = B.A[sid];
@@ -318,18 +368,34 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     if (nr <= 0) return;
     T* X = B.X[sid] + (int64_t)rhs0 * B.ldx[sid];
     const int64_t ldx = B.ldx[sid];
-    const int32_t* ip = B.ipiv[sid];
-    __shared__ T xs[GK][TS_MAXRHS];
+    const int32_t* pm = B.perm[sid];
     __shared__ T dg[GK][GK + 1];
-    const int tid = threadIdx.x;
-    // row interchanges
-    if (tid < nr) {
-        T* x = X + tid * ldx;
-        for (int64_t r = 0; r < n; r++) {
-            int64_t p = ip[r];
-            if (p != r) { T t = x[r]; x[r] = x[p]; x[p] = t; }
+    __shared__ T xs[GK][TS_MAXRHS];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // working copy of X: shared memory (n x TS_MAXRHS, row-major) or X itself after an in-place gather
+    T* W = reinterpret_cast<T*>(smem_raw);
+    const int64_t wld = use_smem ? 1 : ldx;     // stride between rows
+    const int64_t wcs = use_smem ? TS_MAXRHS : 1;  // unused when not smem
+    (void)wcs;
+    auto WX = [&](int64_t r, int q) -> T& { return use_smem ? W[r * TS_MAXRHS + q] : X[r + q * ldx]; };
+    if (use_smem) {
+        for (int64_t e = tid; e < n * nr; e += TS_THREADS) {
+            const int64_t r = e % n;
+            const int q = (int)(e / n);
+            W[r * TS_MAXRHS + q] = X[pm[r] + q * ldx];
+        }
+    } else {
+        // gather through the double-buffer-free route: rows are permuted one
+        // right-hand side at a time with the CTA's shared scratch as staging
+        T* stage = W;  // n entries (caller sized the shared memory for one column)
+        for (int q = 0; q < nr; q++) {
+            for (int64_t r = tid; r < n; r += TS_THREADS) stage[r] = X[pm[r] + q * ldx];
+            __syncthreads();
+            for (int64_t r = tid; r < n; r += TS_THREADS) X[r + q * ldx] = stage[r];
+            __syncthreads();
         }
     }
+    (void)wld;
     __syncthreads();
     // forward: L (unit lower)
     for (int64_t k = 0; k < n; k += GK) {
@@ -339,13 +405,15 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
             dg[r][c] = A[(k + r) + (k + c) * ld];
         }
         __syncthreads();
-        if (tid < nr) {
-            T* x = X + tid * ldx;
+        if (wid < nr) {
+            T x = lane < nb ? WX(k + lane, wid) : (T)0;
             for (int r = 0; r < nb; r++) {
-                T s = x[k + r];
-                for (int l = 0; l < r; l++) s -= dg[r][l] * xs[l][tid];
-                xs[r][tid] = s;
-                x[k + r] = s;
+                const T xr = __shfl_sync(0xffffffffu, x, r);
+                if (lane > r && lane < nb) x -= dg[lane][r] * xr;
+            }
+            if (lane < nb) {
+                xs[lane][wid] = x;
+                WX(k + lane, wid) = x;
             }
         }
         __syncthreads();
@@ -358,7 +426,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
 #pragma unroll
                 for (int q = 0; q < TS_MAXRHS; q++) acc[q] += a * xs[l][q];
             }
-            for (int q = 0; q < nr; q++) X[r + q * ldx] -= acc[q];
+            for (int q = 0; q < nr; q++) WX(r, q) -= acc[q];
         }
         __syncthreads();
     }
@@ -372,14 +440,17 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
             dg[r][c] = A[(k + r) + (k + c) * ld];
         }
         __syncthreads();
-        if (tid < nr) {
-            T* x = X + tid * ldx;
+        if (wid < nr) {
+            T x = lane < nb ? WX(k + lane, wid) : (T)0;
             for (int r = nb - 1; r >= 0; r--) {
-                T s = x[k + r];
-                for (int l = r + 1; l < nb; l++) s -= dg[r][l] * xs[l][tid];
-                s = s / dg[r][r];
-                xs[r][tid] = s;
-                x[k + r] = s;
+                T xr = __shfl_sync(0xffffffffu, x, r);
+                xr = xr / dg[r][r];
+                if (lane == r) x = xr;
+                if (lane < r) x -= dg[lane][r] * xr;
+            }
+            if (lane < nb) {
+                xs[lane][wid] = x;
+                WX(k + lane, wid) = x;
             }
         }
         __syncthreads();
@@ -392,9 +463,16 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
 #pragma unroll
                 for (int q = 0; q < TS_MAXRHS; q++) acc[q] += a * xs[l][q];
             }
-            for (int q = 0; q < nr; q++) X[r + q * ldx] -= acc[q];
+            for (int q = 0; q < nr; q++) WX(r, q) -= acc[q];
         }
         __syncthreads();
+    }
+    if (use_smem) {
+        for (int64_t e = tid; e < n * nr; e += TS_THREADS) {
+            const int64_t r = e % n;
+            const int q = (int)(e / n);
+            X[r + q * ldx] = W[r * TS_MAXRHS + q];
+        }
     }
 }
 
@@ -437,13 +515,25 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
             GB_LAUNCH_CHECK();
         }
     }
+    if (plan.nsys > 0) {
+        k_perm<T><<<plan.nsys, 256, sizeof(int32_t) * std::min<int64_t>(plan.maxn, PERM_SMEM), st>>>(B);
+        GB_LAUNCH_CHECK();
+    }
     return GBVLM_OK;
 }
 
 template <class T>
-int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, cudaStream_t st) {
+int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st) {
+    // X of the largest system in shared memory when it fits, else staged per column
+    const size_t full = sizeof(T) * (size_t)maxn * TS_MAXRHS;
+    const int use_smem = full <= (size_t)TS_SMEM_BYTES ? 1 : 0;
+    const size_t smem = use_smem ? full : sizeof(T) * (size_t)maxn;
+    if (smem > 48 * 1024) {
+        GB_REQUIRE(smem <= (size_t)TS_SMEM_BYTES || !use_smem, "triangular solve: n=%lld too large", (long long)maxn);
+    }
+    GB_REQUIRE(smem <= 227 * 1024, "triangular solve: n=%lld needs %zu bytes of shared memory", (long long)maxn, smem);
     for (int32_t r0 = 0; r0 < max_nrhs; r0 += TS_MAXRHS) {
-        k_trsolve<T><<<nsys, TS_THREADS, 0, st>>>(B, r0, TS_MAXRHS);
+        k_trsolve<T><<<nsys, TS_THREADS, smem, st>>>(B, r0, TS_MAXRHS, use_smem);
         GB_LAUNCH_CHECK();
     }
     return GBVLM_OK;
@@ -451,8 +541,8 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, cudaStre
 
 template int lu_batch_factor<float>(const LuBatch<float>&, const LuPlan&, cudaStream_t);
 template int lu_batch_factor<double>(const LuBatch<double>&, const LuPlan&, cudaStream_t);
-template int lu_batch_solve<float>(const LuBatch<float>&, int32_t, int32_t, cudaStream_t);
-template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, cudaStream_t);
+template int lu_batch_solve<float>(const LuBatch<float>&, int32_t, int32_t, int64_t, cudaStream_t);
+template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, int64_t, cudaStream_t);
 
 // Build the per-step tables.  Systems must be sorted by n descending so the
 // active systems of every step form a prefix of the order.
@@ -460,6 +550,12 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     plan.release();
     GB_CUDA(cudaFuncSetAttribute(k_panel_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_panel_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(k_trsolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GB_CUDA(cudaFuncSetAttribute(k_trsolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GB_CUDA(cudaFuncSetAttribute(k_perm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
+    GB_CUDA(cudaFuncSetAttribute(k_perm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
+    plan.nsys = (int32_t)n_sorted.size();
+    plan.maxn = n_sorted.empty() ? 0 : n_sorted[0];
     const int nsys = (int)n_sorted.size();
     for (int i = 1; i < nsys; i++) GB_REQUIRE(n_sorted[i] <= n_sorted[i - 1], "lu plan: sizes not sorted");
     std::vector<int32_t> act;
@@ -575,15 +671,16 @@ __global__ void k_axpy_f2d(const float* d, int64_t n, int64_t ldd, double* x, in
 
 
 template <class T>
-int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv, int32_t* info, T* X, int64_t ldx,
-                      int32_t nrhs, void** work, size_t* work_bytes, cudaStream_t st) {
+int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv, int32_t* perm, int32_t* info, T* X,
+                      int64_t ldx, int32_t nrhs, void** work, size_t* work_bytes, cudaStream_t st) {
     struct Tab {
         int64_t n, ld, ldx;
         T* A;
         int32_t* ipiv;
         T* X;
         int32_t nrhs;
-    } tab{n, ld, ldx, A, ipiv, X, nrhs};
+        int32_t* perm;
+    } tab{n, ld, ldx, A, ipiv, X, nrhs, perm};
     if (*work_bytes < sizeof(Tab)) {
         if (*work) cudaFree(*work);
         *work = nullptr;
@@ -601,13 +698,14 @@ int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv,
     B.ipiv = &d->ipiv;
     B.X = &d->X;
     B.nrhs = &d->nrhs;
+    B.perm = &d->perm;
     B.info = info;
     return GBVLM_OK;
 }
-template int make_single_batch<float>(LuBatch<float>&, int64_t, int64_t, float*, int32_t*, int32_t*, float*, int64_t,
-                                      int32_t, void**, size_t*, cudaStream_t);
-template int make_single_batch<double>(LuBatch<double>&, int64_t, int64_t, double*, int32_t*, int32_t*, double*,
-                                       int64_t, int32_t, void**, size_t*, cudaStream_t);
+template int make_single_batch<float>(LuBatch<float>&, int64_t, int64_t, float*, int32_t*, int32_t*, int32_t*, float*,
+                                      int64_t, int32_t, void**, size_t*, cudaStream_t);
+template int make_single_batch<double>(LuBatch<double>&, int64_t, int64_t, double*, int32_t*, int32_t*, int32_t*,
+                                       double*, int64_t, int32_t, void**, size_t*, cudaStream_t);
 
 }  // namespace gbvlm
 
@@ -615,6 +713,7 @@ using namespace gbvlm;
 
 struct gbvlm_lu_s {
     int64_t n = 0;
+    int32_t* d_perm = nullptr;
     int32_t* d_ipiv = nullptr;
     int32_t* d_info = nullptr;
     LuPlan plan;
@@ -627,9 +726,12 @@ static int lu_ensure(gbvlm_lu h, int64_t n, cudaStream_t st) {
     if (h->plan_n == n && h->d_ipiv) return GBVLM_OK;
     if (h->d_ipiv) cudaFree(h->d_ipiv);
     if (h->d_info) cudaFree(h->d_info);
+    if (h->d_perm) cudaFree(h->d_perm);
     h->d_ipiv = nullptr;
     h->d_info = nullptr;
+    h->d_perm = nullptr;
     GB_CUDA(cudaMalloc(&h->d_ipiv, sizeof(int32_t) * (n > 0 ? n : 1)));
+    GB_CUDA(cudaMalloc(&h->d_perm, sizeof(int32_t) * (n > 0 ? n : 1)));
     GB_CUDA(cudaMalloc(&h->d_info, sizeof(int32_t)));
     std::vector<int64_t> ns(1, n);
     int rc = lu_plan_build(h->plan, ns, st);
@@ -646,7 +748,7 @@ static int lu_factor_one(gbvlm_lu h, T* A, int64_t n, int64_t ld, cudaStream_t s
     if (rc) return rc;
     GB_CUDA(cudaMemsetAsync(h->d_info, 0, sizeof(int32_t), st));
     LuBatch<T> B;
-    rc = make_single_batch<T>(B, n, ld, A, h->d_ipiv, h->d_info, nullptr, 0, 0, &h->work, &h->work_bytes, st);
+    rc = make_single_batch<T>(B, n, ld, A, h->d_ipiv, h->d_perm, h->d_info, nullptr, 0, 0, &h->work, &h->work_bytes, st);
     if (rc) return rc;
     rc = lu_batch_factor<T>(B, h->plan, st);
     if (rc) return rc;
@@ -666,10 +768,10 @@ static int lu_solve_one(gbvlm_lu h, const T* A, int64_t n, int64_t ld, T* X, int
     GB_REQUIRE(h && A && X && n >= 1 && ld >= n && ldx >= n && nrhs >= 1, "bad LU solve arguments");
     GB_REQUIRE(h->plan_n == n, "LU solve before factorize for this size");
     LuBatch<T> B;
-    int rc = make_single_batch<T>(B, n, ld, (T*)A, h->d_ipiv, h->d_info, X, ldx, (int32_t)nrhs, &h->work,
-                                  &h->work_bytes, st);
+    int rc = make_single_batch<T>(B, n, ld, (T*)A, h->d_ipiv, h->d_perm, h->d_info, X, ldx, (int32_t)nrhs,
+                                  &h->work, &h->work_bytes, st);
     if (rc) return rc;
-    return lu_batch_solve<T>(B, 1, (int32_t)nrhs, st);
+    return lu_batch_solve<T>(B, 1, (int32_t)nrhs, n, st);
 }
 
 extern "C" {
@@ -684,6 +786,7 @@ int gbvlm_lu_destroy(gbvlm_lu h) {
     if (!h) return GBVLM_OK;
     if (h->d_ipiv) cudaFree(h->d_ipiv);
     if (h->d_info) cudaFree(h->d_info);
+    if (h->d_perm) cudaFree(h->d_perm);
     if (h->work) cudaFree(h->work);
     h->plan.release();
     delete h;

@@ -20,6 +20,7 @@ struct LuBatch {
     T* const* X;
     const int64_t* ldx;
     const int32_t* nrhs;
+    int32_t* const* perm;  // row permutation of the factorisation (perm[r] = original row), n per system
 };
 
 struct LuStep {
@@ -37,6 +38,8 @@ struct LuStep {
 
 struct LuPlan {
     std::vector<LuStep> steps;
+    int32_t nsys = 0;
+    int64_t maxn = 0;
     int32_t* d_act = nullptr;
     int64_t* d_pfx = nullptr;
     void release();
@@ -50,11 +53,11 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
 template <class T>
 int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st);
 template <class T>
-int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, cudaStream_t st);
+int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st);
 
 // Single-system tables packed in a small device buffer (*work, grown on demand).
 template <class T>
-int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv, int32_t* info, T* X, int64_t ldx,
-                      int32_t nrhs, void** work, size_t* work_bytes, cudaStream_t st);
+int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv, int32_t* perm, int32_t* info, T* X,
+                      int64_t ldx, int32_t nrhs, void** work, size_t* work_bytes, cudaStream_t st);
 
 }  // namespace gbvlm
