@@ -53,6 +53,11 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
+    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm"],
+                   help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
+                        "uvlm: 20x80 rectangular wing, 500 pitch-plunge steps")
+    p.add_argument("--uvlm-steps", type=int, default=500)
+    p.add_argument("--rollup", type=int, default=1)
     return p.parse_args()
 
 
@@ -336,10 +341,88 @@ def plain_path_rate(args, cases, dev, co):
     return out
 
 
+def run_large(args):
+    """128 x 128 elliptic wing (16,384 panels), 64 alphas in [-10, 10] deg on one AIC."""
+    import torch
+    from tinyvlm_gb300 import mesh as M
+    from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+    v = M.elliptic(128, 128).astype(np.float32)
+    M.quarter_chord(v)
+    case = M.Case(v, np.radians(np.linspace(-10.0, 10.0, 64)), {})
+    bs = BatchSolver([case], mode="shared", refine=args.refine)
+    stream = torch.cuda.current_stream()
+    bs.set_inputs(pack_verts([case]), pack_alphas([case]), ref_pt=(0.0, 0.0, 0.0), stream=stream)
+    bs.run(stream=stream)
+    torch.cuda.synchronize()
+    prof = bs.profile(stream=stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bs.run(stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    co, _ = bs.results(stream=stream)
+    lu = bs.lu_flops / (prof["lu_factor"] / 1000.0) / 1e12
+    asm = FLOP_PER_INTERACTION * bs.interactions / (prof["assembly"] / 1000.0) / 1e12
+    print(json.dumps({"workload": "large steady: elliptic 128x128 = 16384 panels, 64 alphas, one AIC",
+                      "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof,
+                      "lu_tflops": lu, "assembly_tflops_alg": asm, "cl_range": [float(co[:, 0].min()), float(co[:, 0].max())],
+                      "refine_iters": args.refine}))
+
+
+def run_uvlm(args):
+    """20 x 80 rectangular half wing (chord 1, semispan 4), heave 0.1 sin(kt), pitch 3 deg sin(kt + 90 deg)
+    about the quarter chord, k = 0.5, dt = 0.05, 500 steps; float (reference semantics)."""
+    import torch
+    from tinyvlm_gb300 import mesh as M
+    from tinyvlm_gb300.kinematics import Assembly, KinematicsTree, rotation_matrix, sin, translation_matrix
+    from tinyvlm_gb300.uvlm import UVLM, kinematics_arrays
+    v = M.rectangular(20, 80, 1.0, 4.0).astype(np.float32)
+    M.quarter_chord(v)
+    k = 0.5
+    tree = KinematicsTree()
+    fs = tree.add(lambda t: translation_matrix([-t, 0.0, 0.0]))
+    heave = tree.add(lambda t: translation_matrix([0.0, 0.0, 0.1 * sin(k * t)])).after(fs)
+    pitch = tree.add(lambda t: rotation_matrix([0.25, 0, 0], [0, 1, 0], math.radians(3.0) * sin(k * t + math.pi / 2))).after(heave)
+    asm = Assembly(fs)
+    asm.add("wing", pitch)
+    sim = UVLM("gb300", [v], precision=32)
+    out = {"workload": "UVLM pitch-plunge: rectangular 20x80 = 1600 panels, %d steps, rollup=%d" %
+                       (args.uvlm_steps, args.rollup)}
+    for roll in sorted({0, args.rollup}):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = sim.run(asm, t_steps=args.uvlm_steps, dt=0.05, rollup=bool(roll))
+        torch.cuda.synchronize()
+        out["gpu_s_rollup%d" % roll] = time.perf_counter() - t0
+        out["cl_last_rollup%d" % roll] = float(r["cl"][-2])
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        steps = 40
+        T, Td, fsv, ref = kinematics_arrays(asm, steps, 0.05)
+        t0 = time.perf_counter()
+        O.uvlm_run([v], [True], T, Td, fsv, ref, steps, 0.05, dtype=np.float32, rollup=False)
+        cpu = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.run(asm, t_steps=steps, dt=0.05, rollup=False)
+        torch.cuda.synchronize()
+        out["sample_first_steps"] = steps
+        out["cpu_s_sample"] = cpu
+        out["gpu_s_sample"] = time.perf_counter() - t0
+        out["cpu_threads"] = O.num_threads()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "large":
+        run_large(args)
+    elif args.workload == "uvlm":
+        run_uvlm(args)
     else:
         run_gpu(args)
 

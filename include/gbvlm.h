@@ -307,6 +307,63 @@ int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream);
  * cm_y, cm_z; gamma (optional, needs want_gamma) = each solve's n floats. */
 int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_stream stream);
 
+/* ---------------------------------------------------------------------------
+ * Unsteady VLM, UVLM::run (vlm/src/vlm.cpp:358-509), with the time loop on
+ * the device.  The caller evaluates each surface's kinematic transform and
+ * its time derivative at t_i = i*dt, i in [0, t_steps] (the reference does
+ * this with dual numbers, vlm/include/vlm_kinematics.hpp:215-239):
+ *   transforms[(i*nsurf + m)*16 ..]  4x4 column-major T_m(t_i)
+ *   dtransforms[...]                  dT_m/dt (t_i)
+ *   freestream[i*3 ..]                -V_body(t_i) (vlm.cpp:414)
+ *   ref_pt[i*3 ..]                    moment reference at t_i (may be NULL)
+ * Results per step i (i >= 1, as the reference skips i = 0): CL(t_i) and
+ * CM(t_i) (coeff_cl_multibody / coeff_cm_multibody, vlm.cpp:461-475).
+ * rollup != 0 adds the free-wake roll-up of kernel_rollup
+ * (vlm_backend_cpu_kernels.ispc:215-271) after each solve; the reference's
+ * wake is purely kinematic. */
+typedef struct gbvlm_uvlm_s* gbvlm_uvlm;
+int gbvlm_uvlm_create(gbvlm_uvlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                      const int32_t* lifting, int64_t t_steps, int32_t precision);
+int gbvlm_uvlm_destroy(gbvlm_uvlm h);
+int gbvlm_uvlm_set_kinematics(gbvlm_uvlm h, const double* transforms, const double* dtransforms,
+                              const double* freestream, const double* ref_pt);
+int gbvlm_uvlm_run(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_stream stream);
+/* cl: t_steps doubles, cm: 3*t_steps, gamma_last: n doubles of the last step (each may be NULL). Synchronous. */
+int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Harmonic-balance VLM (lib/libhbvlm3.cpp:262-552; 2-DOF lib/libhbvlm.cpp:230-468),
+ * double.  Exactly one surface is lifting; its wake carries the
+ * trailing-edge gamma rebuilt from Fourier coefficients.  The host supplies
+ * the kinematics (per-step wake transforms and per-instance transforms and
+ * rates, N = 2*harmonics + 1 instances) and the DFT matrix.
+ * ------------------------------------------------------------------------- */
+typedef struct gbvlm_hbvlm_s* gbvlm_hbvlm;
+/* HBVLM(backend, meshes): verts_init HOST double (ns+1, nc+1, 4) per surface, already scaled. */
+int gbvlm_hbvlm_create(gbvlm_hbvlm* out, int32_t nsurf, const gbvlm_dims* dims, const double* const* verts_init,
+                       const int32_t* lifting);
+int gbvlm_hbvlm_destroy(gbvlm_hbvlm h);
+/* libhbvlm3.cpp:266-347: metrics at the undisplaced pose, AIC (no wake) and
+ * its factors, wake pre-generation over max_t_steps steps
+ * (wake_transforms[(i*nsurf+m)*16]), then per instance q (t_steps[q],
+ * times[q], transforms/dtransforms[(q*nsurf+m)*16]) the geometry and -V.n
+ * right-hand side; dft is the (N x N) column-major DFT matrix. */
+int gbvlm_hbvlm_prepare(gbvlm_hbvlm h, int32_t harmonics, int64_t max_t_steps, const double* wake_transforms,
+                        const int64_t* t_steps, const double* times, const double* transforms,
+                        const double* dtransforms, const double* dft, gbvlm_stream stream);
+/* One fixed-point map x_in -> x_out (HOST, n x N column-major) (libhbvlm3.cpp:349-410). */
+int gbvlm_hbvlm_map(gbvlm_hbvlm h, const double* x_in, double* x_out, double omega, double dt, gbvlm_stream stream);
+/* anderson_acceleration (vlm/src/vlm_solvers.cpp:6-115) of the map from x (HOST, updated in place). */
+int gbvlm_hbvlm_solve(gbvlm_hbvlm h, double* x, double omega, double dt, int32_t max_iter, double tol, int32_t m,
+                      int32_t* iters, gbvlm_stream stream);
+/* Loads at N force instances (libhbvlm3.cpp:428-550): out (3 x N, row-major)
+ * = CL, CM_y about ref_a (multibody), CM_y of surface 1 about ref_b (if
+ * ref_b != NULL).  coupled_te: surface m's first chordwise gamma delta also
+ * subtracts surface m-1's trailing-edge gamma (wing + flap). */
+int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, const double* ddft,
+                      const double* transforms, const double* dtransforms, const double* freestream,
+                      const double* ref_a, const double* ref_b, int32_t coupled_te, double* out, gbvlm_stream stream);
+
 /* plot3d reader (vlm/src/vlm_mesh.cpp:34-123): dims first (verts == NULL),
  * then the vertices into a HOST float (ns+1, nc+1, 4) array. */
 int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts);

@@ -441,3 +441,72 @@ def vlm_shared(verts_init, alphas, u_inf=1.0, rho=1.0, dtype=np.float64, ref_pt=
             at += area
         out.append(dict(cl=cl, cdi=T(cdn / at), cm=cm, gamma=gam))
     return out
+
+
+# ---------------------------------------------------------------------------
+# UVLM driver, vlm/src/vlm.cpp:358-509, over precomputed per-step transforms
+# T[i, m] (16, column-major), Td[i, m], freestream fs[i], reference ref[i]
+# (the same arrays the GPU driver receives).
+# ---------------------------------------------------------------------------
+def uvlm_run(verts_init, lifting, T, Td, fs, ref, t_steps, dt, dtype=np.float64, rollup=False, sigma=0.0):
+    dt_ = np.dtype(dtype).type
+    verts_init = [np.ascontiguousarray(v, dtype) for v in verts_init]
+    ns, nc = dims(verts_init)
+    nsurf = len(verts_init)
+    n = sum(a * b for a, b in zip(ns, nc))
+    tr = lambda i, m: np.asfortranarray(np.asarray(T[i, m], dtype).reshape(4, 4).T)
+    vpos = [v.copy() for v in verts_init]
+    for m in range(nsurf):
+        displace_wing(tr(0, m), vpos[m], verts_init[m])
+    verts = [v.copy() for v in vpos]
+    colloc, normals, areas = mesh_metrics(0.0, verts, dtype)
+    colloc0 = [c.copy() for c in colloc]
+    wake = []
+    for s in ns:
+        w = np.zeros((4, t_steps, s + 1), dtype)
+        w[3] = 1
+        wake.append(w)
+    gwake = [np.zeros((t_steps - 1, s), dtype) for s in ns]
+    lhs = np.zeros((n, n), dtype, order="F")
+    lhs_assemble(lhs, colloc, normals, verts, wake, 0, sigma)
+    lu, piv = lu_factor(lhs)
+    gprev = [np.zeros((c, s), dtype) for s, c in zip(ns, nc)]
+    cl = np.zeros(t_steps)
+    cm = np.zeros((t_steps, 3))
+    gam = None
+    for i in range(t_steps - 1):
+        wake_shed(verts, wake, i)
+        vel = []
+        for m in range(nsurf):
+            d = np.asarray(Td[i, m], np.float64).reshape(4, 4).T.astype(dtype)
+            c = colloc0[m]
+            v = np.empty_like(c)
+            for r in range(3):
+                v[r] = -(d[r, 0] * c[0] + d[r, 1] * c[1] + d[r, 2] * c[2] + d[r, 3])
+            vel.append(v)
+        rhs = np.zeros(n, dtype)
+        rhs_assemble_velocities(rhs, normals, vel)
+        rhs_assemble_wake_influence(rhs, gwake, colloc, normals, wake, lifting, i, sigma)
+        x = lu_solve(lu, piv, rhs)
+        gam, deltas, gdts, off = [], [], [], 0
+        for m in range(nsurf):
+            g = x[off:off + ns[m] * nc[m]].reshape(nc[m], ns[m]).copy()
+            off += ns[m] * nc[m]
+            gam.append(g)
+            deltas.append(gamma_delta(g))
+            gwake[m][t_steps - 2 - i] = g[-1]
+            gdts.append(((g - gprev[m]) * dt_(1.0 / dt)).astype(dtype) if dtype == np.float64 else
+                        ((g - gprev[m]) * (dt_(1) / dt_(dt))).astype(dtype))
+        if i > 0:
+            forces = [forces_unsteady(verts[m], deltas[m], gdts[m], vel[m], areas[m], normals[m])
+                      for m in range(nsurf)]
+            f_s = np.asarray(fs[i], dtype)
+            cl[i] = coeff_cl_multibody(forces, areas, f_s, dt_(1))
+            cm[i] = coeff_cm_multibody(forces, verts, areas, np.asarray(ref[i], dtype), f_s, dt_(1))
+        if rollup and i > 0:
+            wake_rollup(wake, verts, gam, gwake, lifting, dt, i, sigma)
+        gprev = [g.copy() for g in gam]
+        for m in range(nsurf):
+            displace_wing(tr(i + 1, m), verts[m], vpos[m])
+        colloc, normals, areas = mesh_metrics(0.0, verts, dtype)
+    return dict(cl=cl, cm=cm, gamma=gam)

@@ -73,6 +73,17 @@ def _protos():
     t["gbvlm_batch_results"] = [P, P, P, P]
     t["gbvlm_batch_profile"] = [P, P, P]
     t["gbvlm_batch_launches"] = [P, P]
+    t["gbvlm_uvlm_create"] = [P, I32, P, PP, P, I64, I32]
+    t["gbvlm_uvlm_destroy"] = [P]
+    t["gbvlm_uvlm_set_kinematics"] = [P, P, P, P, P]
+    t["gbvlm_uvlm_run"] = [P, F64, I32, F64, P]
+    t["gbvlm_uvlm_results"] = [P, P, P, P, P]
+    t["gbvlm_hbvlm_create"] = [P, I32, P, PP, P]
+    t["gbvlm_hbvlm_destroy"] = [P]
+    t["gbvlm_hbvlm_prepare"] = [P, I32, I64, P, P, P, P, P, P, P]
+    t["gbvlm_hbvlm_map"] = [P, P, P, F64, F64, P]
+    t["gbvlm_hbvlm_solve"] = [P, P, F64, F64, I32, F64, I32, P, P]
+    t["gbvlm_hbvlm_loads"] = [P, P, P, P, P, P, P, P, P, I32, P, P]
     return t
 
 

@@ -1,0 +1,493 @@
+// Harmonic-balance VLM (lib/libhbvlm3.cpp:262-552 and lib/libhbvlm.cpp:230-468)
+// in double on the device.
+//
+// The circulation is expanded in 2H+1 Fourier coefficients per panel
+// (scaled orthonormal basis).  One fixed-point map (libhbvlm3.cpp:349-410):
+// for every time instance s, the lifting surface's wake gamma is rebuilt
+// from its trailing-edge coefficients and its influence (over the
+// pre-generated kinematic wake) is subtracted from the instance's
+// -V.n right-hand side; the (n x N) RHS is multiplied by the DFT matrix and
+// solved with the AIC factored once.  Anderson acceleration
+// (vlm/src/vlm_solvers.cpp:6-115, type II, history m, least squares by
+// Householder QR like LAPACK dgels) iterates the map to a fixed point.  The
+// instance geometry, normals and -V.n do not depend on gamma and are
+// computed once per run.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "gbvlm_internal.h"
+
+namespace gbvlm {
+
+__global__ void k_gather_te(const double* X, int64_t n, int64_t off, int64_t ns, int32_t N, double* te) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= ns * N) return;
+    const int64_t i = g % ns, h = g / ns;
+    te[i + h * ns] = X[off + i + h * n];
+}
+
+// Y (n x N) = R (n x N) . D (N x N), all column-major
+__global__ void k_rdft(const double* R, const double* D, int64_t n, int32_t N, double* Y) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= n * N) return;
+    const int64_t r = g % n, j = g / n;
+    double s = 0;
+    for (int32_t k = 0; k < N; k++) s += R[r + k * n] * D[k + j * N];
+    Y[g] = s;
+}
+
+// g = C . row_s(D) : g[p] = sum_j C[p + j n] D[s + j N]
+__global__ void k_dft_row(const double* C, const double* D, int64_t n, int32_t N, int32_t s, double* g) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double v = 0;
+    for (int32_t j = 0; j < N; j++) v += C[p + j * n] * D[s + j * N];
+    g[p] = v;
+}
+
+// chordwise delta of one surface; with `prev_te` the first chordwise row
+// also loses the previous surface's trailing-edge gamma (libhbvlm3.cpp:476-480)
+__global__ void k_delta(const double* g, int64_t ns, int64_t nc, const double* prev_te, double* d) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= ns * nc) return;
+    const int64_t i = p % ns, j = p / ns;
+    double v = g[p];
+    if (j > 0) v -= g[p - ns];
+    else if (prev_te) v -= prev_te[i];
+    d[p] = v;
+}
+
+template <class T>
+__global__ void k_vel_dual(const double* Td, const double* c0, double* vel, int64_t np) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const double x = c0[p], y = c0[np + p], z = c0[2 * np + p];
+    for (int r = 0; r < 3; r++) vel[r * np + p] = -(Td[r] * x + Td[r + 4] * y + Td[r + 8] * z + Td[r + 12]);
+}
+
+struct Inst {
+    int64_t t_steps = 0;
+    double t = 0;
+    std::vector<double*> colloc, normals;
+    double* rhs_vel = nullptr;
+    std::vector<double*> gwake;
+};
+
+struct HbState {
+    int32_t nsurf = 0, wake_surf = 0, N = 0;
+    std::vector<gbvlm_dims> dims;
+    std::vector<int32_t> lifting;
+    int64_t n = 0, max_t = 0;
+    std::vector<int64_t> poff;
+    std::vector<void*> allocs;
+    std::vector<double*> vinit, verts, wake, colloc_h, colloc, normals, areas, vel, forces, gdelta, gdt, gam, trans;
+    double *lhs = nullptr, *D = nullptr, *Xin = nullptr, *Xout = nullptr, *R = nullptr, *te = nullptr;
+    gbvlm_lu lu = nullptr;
+    std::vector<Inst> inst;
+
+    ~HbState() {
+        if (lu) gbvlm_lu_destroy(lu);
+        for (void* p : allocs) cudaFree(p);
+    }
+
+    int alloc(double** p, size_t cnt) {
+        GB_CUDA(cudaMalloc((void**)p, sizeof(double) * (cnt > 0 ? cnt : 1)));
+        GB_CUDA(cudaMemset(*p, 0, sizeof(double) * (cnt > 0 ? cnt : 1)));
+        allocs.push_back(*p);
+        return GBVLM_OK;
+    }
+    std::vector<const double*> C(const std::vector<double*>& v) const { return {v.begin(), v.end()}; }
+
+    int init(int32_t ns_, const gbvlm_dims* d, const double* const* vh, const int32_t* lift) {
+        nsurf = ns_;
+        dims.assign(d, d + ns_);
+        lifting.assign(lift, lift + ns_);
+        int nl = 0;
+        for (int m = 0; m < nsurf; m++)
+            if (lifting[m]) {
+                wake_surf = m;
+                nl++;
+            }
+        GB_REQUIRE(nl == 1, "harmonic balance needs exactly one lifting surface (its wake carries the TE gamma)");
+        poff.assign(nsurf + 1, 0);
+        int rc;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t np = dims[m].ns * dims[m].nc, nv = (dims[m].ns + 1) * (dims[m].nc + 1);
+            poff[m + 1] = poff[m] + np;
+            double* p;
+            if ((rc = alloc(&p, 4 * nv))) return rc;
+            vinit.push_back(p);
+            GB_CUDA(cudaMemcpy(p, vh[m], sizeof(double) * 4 * nv, cudaMemcpyHostToDevice));
+            if ((rc = alloc(&p, 4 * nv))) return rc;
+            verts.push_back(p);
+            for (auto* vec : {&colloc_h, &colloc, &normals, &vel, &forces}) {
+                if ((rc = alloc(&p, 3 * np))) return rc;
+                vec->push_back(p);
+            }
+            for (auto* vec : {&areas, &gdelta, &gdt, &gam}) {
+                if ((rc = alloc(&p, np))) return rc;
+                vec->push_back(p);
+            }
+            if ((rc = alloc(&p, 16))) return rc;
+            trans.push_back(p);
+        }
+        n = poff[nsurf];
+        if ((rc = alloc(&lhs, n * n))) return rc;
+        if ((rc = gbvlm_lu_create(&lu))) return rc;
+        return gbvlm_lu_init(lu, n);
+    }
+
+    int place(const double* Th, cudaStream_t st) {
+        for (int m = 0; m < nsurf; m++)
+            GB_CUDA(cudaMemcpyAsync(trans[m], Th + 16 * m, sizeof(double) * 16, cudaMemcpyHostToDevice, st));
+        return gbvlm_displace_wing_f64(nsurf, dims.data(), C(trans).data(), verts.data(), C(vinit).data(),
+                                       (gbvlm_stream)st);
+    }
+
+    // libhbvlm3.cpp:266-319: metrics at the undisplaced pose, AIC without wake, factor, wake pre-generation
+    int prepare(int32_t harmonics, int64_t max_t_steps, const double* wake_T, cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        N = 2 * harmonics + 1;
+        max_t = max_t_steps;
+        int rc;
+        for (auto& d : dims) d.nwv = max_t;
+        for (double* p : wake) cudaFree(p);
+        wake.clear();
+        for (int m = 0; m < nsurf; m++) {
+            double* p;
+            GB_CUDA(cudaMalloc((void**)&p, sizeof(double) * 4 * (dims[m].ns + 1) * max_t));
+            GB_CUDA(cudaMemset(p, 0, sizeof(double) * 4 * (dims[m].ns + 1) * max_t));
+            wake.push_back(p);
+        }
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t nv = (dims[m].ns + 1) * (dims[m].nc + 1);
+            GB_CUDA(cudaMemcpyAsync(verts[m], vinit[m], sizeof(double) * 4 * nv, cudaMemcpyDeviceToDevice, st));
+        }
+        if ((rc = gbvlm_mesh_metrics_f64(0.0, nsurf, dims.data(), C(verts).data(), colloc_h.data(), normals.data(),
+                                         areas.data(), s)))
+            return rc;
+        GB_CUDA(cudaMemsetAsync(lhs, 0, sizeof(double) * n * n, st));
+        if ((rc = gbvlm_lhs_assemble_f64(lhs, n, nsurf, dims.data(), C(colloc_h).data(), C(normals).data(),
+                                         C(verts).data(), nullptr, 0, 0.0, s)))
+            return rc;
+        if ((rc = gbvlm_lu_factor_f64(lu, lhs, n, n, s))) return rc;
+        for (int64_t i = 0; i < max_t; i++) {
+            if ((rc = place(wake_T + 16 * nsurf * i, st))) return rc;
+            if ((rc = gbvlm_wake_shed_f64(nsurf, dims.data(), C(verts).data(), wake.data(), (int32_t)i, s))) return rc;
+        }
+        GB_CUDA(cudaStreamSynchronize(st));
+        return GBVLM_OK;
+    }
+
+    // per-instance geometry, -V.n and wake-gamma buffers (libhbvlm3.cpp:363-393 without the gamma part)
+    int set_instances(const int64_t* t_steps, const double* times, const double* Th, const double* Tdh,
+                      const double* dft, cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        int rc;
+        for (auto& I : inst) {
+            for (double* p : I.colloc) cudaFree(p);
+            for (double* p : I.normals) cudaFree(p);
+            for (double* p : I.gwake) cudaFree(p);
+            if (I.rhs_vel) cudaFree(I.rhs_vel);
+        }
+        inst.assign(N, Inst());
+        if (!D && (rc = alloc(&D, N * N))) return rc;
+        if (!Xin) {
+            if ((rc = alloc(&Xin, n * N)) || (rc = alloc(&Xout, n * N)) || (rc = alloc(&R, n * N)) ||
+                (rc = alloc(&te, dims[wake_surf].ns * N)))
+                return rc;
+        }
+        GB_CUDA(cudaMemcpy(D, dft, sizeof(double) * N * N, cudaMemcpyHostToDevice));
+        std::vector<double*> tdm(nsurf);
+        for (int m = 0; m < nsurf; m++) {
+            GB_CUDA(cudaMalloc((void**)&tdm[m], sizeof(double) * 16));
+        }
+        for (int q = 0; q < N; q++) {
+            Inst& I = inst[q];
+            I.t_steps = t_steps[q];
+            I.t = times[q];
+            GB_REQUIRE(I.t_steps >= 0 && I.t_steps <= max_t - 1, "instance %d: t_steps %lld outside the wake", q,
+                       (long long)I.t_steps);
+            if ((rc = place(Th + 16 * nsurf * q, st))) return rc;
+            for (int m = 0; m < nsurf; m++) {
+                const int64_t np = dims[m].ns * dims[m].nc;
+                double *c, *nm, *gw;
+                GB_CUDA(cudaMalloc((void**)&c, sizeof(double) * 3 * np));
+                GB_CUDA(cudaMalloc((void**)&nm, sizeof(double) * 3 * np));
+                GB_CUDA(cudaMalloc((void**)&gw, sizeof(double) * dims[m].ns * (max_t - 1)));
+                GB_CUDA(cudaMemset(gw, 0, sizeof(double) * dims[m].ns * (max_t - 1)));
+                I.colloc.push_back(c);
+                I.normals.push_back(nm);
+                I.gwake.push_back(gw);
+            }
+            if ((rc = gbvlm_mesh_metrics_f64(0.0, nsurf, dims.data(), C(verts).data(), I.colloc.data(),
+                                             I.normals.data(), areas.data(), s)))
+                return rc;
+            for (int m = 0; m < nsurf; m++) {
+                const int64_t np = dims[m].ns * dims[m].nc;
+                GB_CUDA(cudaMemcpyAsync(tdm[m], Tdh + 16 * (nsurf * q + m), sizeof(double) * 16, cudaMemcpyHostToDevice, st));
+                k_vel_dual<double><<<(unsigned)cdiv(np, 128), 128, 0, st>>>(tdm[m], colloc_h[m], vel[m], np);
+                GB_LAUNCH_CHECK();
+            }
+            GB_CUDA(cudaMalloc((void**)&I.rhs_vel, sizeof(double) * n));
+            GB_CUDA(cudaMemsetAsync(I.rhs_vel, 0, sizeof(double) * n, st));
+            if ((rc = gbvlm_rhs_assemble_velocities_f64(I.rhs_vel, nsurf, dims.data(), C(I.normals).data(),
+                                                        C(vel).data(), s)))
+                return rc;
+            GB_CUDA(cudaStreamSynchronize(st));
+        }
+        for (double* p : tdm) cudaFree(p);
+        return GBVLM_OK;
+    }
+
+    // one fixed-point map on device buffers Xin -> Xout (libhbvlm3.cpp:349-410)
+    int map_dev(double omega, double dt, int32_t harmonics, cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        int rc;
+        const gbvlm_dims& W = dims[wake_surf];
+        const int64_t te_off = poff[wake_surf] + (W.nc - 1) * W.ns;
+        k_gather_te<<<(unsigned)cdiv(W.ns * N, 128), 128, 0, st>>>(Xin, n, te_off, W.ns, N, te);
+        GB_LAUNCH_CHECK();
+        for (int q = 0; q < N; q++) {
+            Inst& I = inst[q];
+            if ((rc = gbvlm_gamma_wake_from_coeffs_f64(I.gwake[wake_surf], W.ns, max_t - 1, te, harmonics, I.t, omega,
+                                                        dt, I.t_steps, s)))
+                return rc;
+            double* col = R + (int64_t)q * n;
+            GB_CUDA(cudaMemcpyAsync(col, I.rhs_vel, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            if ((rc = gbvlm_rhs_assemble_wake_influence_f64(col, nsurf, dims.data(), C(I.gwake).data(),
+                                                            C(I.colloc).data(), C(I.normals).data(), C(wake).data(),
+                                                            lifting.data(), (int32_t)I.t_steps, 0.0, s)))
+                return rc;
+        }
+        k_rdft<<<(unsigned)cdiv(n * N, 128), 128, 0, st>>>(R, D, n, N, Xout);
+        GB_LAUNCH_CHECK();
+        return gbvlm_lu_solve_f64(lu, lhs, n, n, Xout, n, N, s);
+    }
+};
+
+// Householder least squares min ||A x - b|| for a tall (rows x k) column-major A (k <= 16); A, b overwritten.
+static void lsq_qr(std::vector<double>& A, int64_t rows, int k, std::vector<double>& b, double* x) {
+    for (int j = 0; j < k; j++) {
+        double nrm = 0;
+        for (int64_t i = j; i < rows; i++) nrm += A[i + j * rows] * A[i + j * rows];
+        nrm = sqrt(nrm);
+        if (nrm == 0) continue;
+        const double a0 = A[j + j * rows];
+        const double alpha = a0 > 0 ? -nrm : nrm;
+        A[j + j * rows] = a0 - alpha;
+        double vv = 0;
+        for (int64_t i = j; i < rows; i++) vv += A[i + j * rows] * A[i + j * rows];
+        for (int c = j + 1; c < k; c++) {
+            double d = 0;
+            for (int64_t i = j; i < rows; i++) d += A[i + j * rows] * A[i + c * rows];
+            const double f = 2 * d / vv;
+            for (int64_t i = j; i < rows; i++) A[i + c * rows] -= f * A[i + j * rows];
+        }
+        double d = 0;
+        for (int64_t i = j; i < rows; i++) d += A[i + j * rows] * b[i];
+        const double f = 2 * d / vv;
+        for (int64_t i = j; i < rows; i++) b[i] -= f * A[i + j * rows];
+        A[j + j * rows] = alpha;  // R diagonal
+    }
+    for (int j = k - 1; j >= 0; j--) {
+        double s = b[j];
+        for (int c = j + 1; c < k; c++) s -= A[j + c * rows] * x[c];
+        x[j] = A[j + j * rows] != 0 ? s / A[j + j * rows] : 0;
+    }
+}
+
+}  // namespace gbvlm
+
+using namespace gbvlm;
+
+struct gbvlm_hbvlm_s {
+    HbState st;
+};
+
+extern "C" {
+
+int gbvlm_hbvlm_create(gbvlm_hbvlm* out, int32_t nsurf, const gbvlm_dims* dims, const double* const* verts_init,
+                       const int32_t* lifting) {
+    GB_REQUIRE(out && dims && verts_init && lifting, "null argument");
+    GB_REQUIRE(nsurf >= 1 && nsurf <= GBVLM_MAX_SURFACES, "nsurf=%d outside [1, %d]", nsurf, GBVLM_MAX_SURFACES);
+    auto* h = new gbvlm_hbvlm_s();
+    int rc = h->st.init(nsurf, dims, verts_init, lifting);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBVLM_OK;
+}
+
+int gbvlm_hbvlm_destroy(gbvlm_hbvlm h) {
+    delete h;
+    return GBVLM_OK;
+}
+
+int gbvlm_hbvlm_prepare(gbvlm_hbvlm h, int32_t harmonics, int64_t max_t_steps, const double* wake_transforms,
+                        const int64_t* t_steps, const double* times, const double* transforms,
+                        const double* dtransforms, const double* dft, gbvlm_stream stream) {
+    GB_REQUIRE(h && wake_transforms && t_steps && times && transforms && dtransforms && dft, "null argument");
+    GB_REQUIRE(harmonics >= 0 && harmonics <= 64 && max_t_steps >= 2, "bad sizes");
+    int rc = h->st.prepare(harmonics, max_t_steps, wake_transforms, to_cuda(stream));
+    if (rc) return rc;
+    return h->st.set_instances(t_steps, times, transforms, dtransforms, dft, to_cuda(stream));
+}
+
+int gbvlm_hbvlm_map(gbvlm_hbvlm h, const double* x_in, double* x_out, double omega, double dt, gbvlm_stream stream) {
+    GB_REQUIRE(h && x_in && x_out && h->st.N > 0, "map before prepare");
+    HbState& S = h->st;
+    cudaStream_t st = to_cuda(stream);
+    GB_CUDA(cudaMemcpyAsync(S.Xin, x_in, sizeof(double) * S.n * S.N, cudaMemcpyHostToDevice, st));
+    int rc = S.map_dev(omega, dt, (S.N - 1) / 2, st);
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(x_out, S.Xout, sizeof(double) * S.n * S.N, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    return GBVLM_OK;
+}
+
+int gbvlm_hbvlm_solve(gbvlm_hbvlm h, double* x, double omega, double dt, int32_t max_iter, double tol, int32_t m,
+                      int32_t* iters, gbvlm_stream stream) {
+    GB_REQUIRE(h && x && h->st.N > 0, "solve before prepare");
+    GB_REQUIRE(m >= 1 && m <= 16 && max_iter >= 2, "history m in [1, 16], max_iter >= 2");
+    HbState& S = h->st;
+    const int64_t L = S.n * S.N;
+    std::vector<double> xc(x, x + L), xn(L), gc(L), gn(L), X((size_t)L * m, 0.0), G((size_t)L * m, 0.0), Gk, rhs;
+    auto f = [&](const std::vector<double>& in, std::vector<double>& out) {
+        return gbvlm_hbvlm_map(h, in.data(), out.data(), omega, dt, stream);
+    };
+    // vlm_solvers.cpp:49-66
+    int rc;
+    if ((rc = f(xc, xn))) return rc;
+    for (int64_t i = 0; i < L; i++) gc[i] = xn[i] - xc[i];
+    for (int64_t i = 0; i < L; i++) X[i] = gc[i];
+    xc = xn;
+    if ((rc = f(xc, xn))) return rc;
+    for (int64_t i = 0; i < L; i++) {
+        gn[i] = xn[i] - xc[i];
+        G[i] = gn[i] - gc[i];
+    }
+    gc = gn;
+    int k = 1;
+    auto norm = [&](const std::vector<double>& v) {
+        double s = 0;
+        for (double a : v) s += a * a;
+        return sqrt(s);
+    };
+    while (k < max_iter && norm(gc) > tol) {
+        const int mk = std::min(m, k);
+        Gk.assign(G.begin(), G.begin() + (size_t)L * mk);
+        rhs = gc;
+        double gam[16];
+        lsq_qr(Gk, L, mk, rhs, gam);
+        for (int64_t i = 0; i < L; i++) {
+            double v = xc[i] + gc[i];
+            for (int j = 0; j < mk; j++) v -= (X[i + (size_t)L * j] + G[i + (size_t)L * j]) * gam[j];
+            xn[i] = v;
+        }
+        const int slot = k % m;
+        for (int64_t i = 0; i < L; i++) X[i + (size_t)L * slot] = xn[i] - xc[i];
+        xc = xn;
+        if ((rc = f(xc, xn))) return rc;
+        for (int64_t i = 0; i < L; i++) {
+            gn[i] = xn[i] - xc[i];
+            G[i + (size_t)L * slot] = gn[i] - gc[i];
+        }
+        gc = gn;
+        k++;
+    }
+    std::copy(xc.begin(), xc.end(), x);
+    if (iters) *iters = k;
+    return GBVLM_OK;
+}
+
+// libhbvlm3.cpp:428-550: loads at the force instances.  coeffs (n x N),
+// dft / ddft (N x N), per instance transforms/rates (N x nsurf x 16),
+// freestream (N x 3), ref_a / ref_b (N x 3; ref_b may be NULL).  out: 3 x N
+// row-major [cl; cm_y about ref_a (multibody); cm_y of surface 1 about ref_b].
+int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, const double* ddft,
+                      const double* transforms, const double* dtransforms, const double* freestream,
+                      const double* ref_a, const double* ref_b, int32_t coupled_te, double* out, gbvlm_stream stream) {
+    GB_REQUIRE(h && coeffs && dft && ddft && transforms && dtransforms && freestream && ref_a && out, "null argument");
+    HbState& S = h->st;
+    cudaStream_t st = to_cuda(stream);
+    gbvlm_stream s = stream;
+    const int N = S.N, ns = S.nsurf;
+    int rc = GBVLM_OK;
+    double *C, *Dd, *DDd, *td;
+    GB_CUDA(cudaMalloc((void**)&C, sizeof(double) * S.n * N));
+    GB_CUDA(cudaMalloc((void**)&Dd, sizeof(double) * N * N));
+    GB_CUDA(cudaMalloc((void**)&DDd, sizeof(double) * N * N));
+    GB_CUDA(cudaMalloc((void**)&td, sizeof(double) * 16 * ns));
+    GB_CUDA(cudaMemcpy(C, coeffs, sizeof(double) * S.n * N, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(Dd, dft, sizeof(double) * N * N, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(DDd, ddft, sizeof(double) * N * N, cudaMemcpyHostToDevice));
+    double* gfull;
+    double* dgfull;
+    GB_CUDA(cudaMalloc((void**)&gfull, sizeof(double) * S.n));
+    GB_CUDA(cudaMalloc((void**)&dgfull, sizeof(double) * S.n));
+    for (int q = 0; q < N && rc == 0; q++) {
+        rc = S.place(transforms + 16 * ns * q, st);
+        if (rc) break;
+        rc = gbvlm_mesh_metrics_f64(0.0, ns, S.dims.data(), S.C(S.verts).data(), S.colloc.data(), S.normals.data(),
+                                    S.areas.data(), s);
+        if (rc) break;
+        GB_CUDA(cudaMemcpyAsync(td, dtransforms + 16 * ns * q, sizeof(double) * 16 * ns, cudaMemcpyHostToDevice, st));
+        k_dft_row<<<(unsigned)cdiv(S.n, 128), 128, 0, st>>>(C, Dd, S.n, N, q, gfull);
+        k_dft_row<<<(unsigned)cdiv(S.n, 128), 128, 0, st>>>(C, DDd, S.n, N, q, dgfull);
+        for (int m = 0; m < ns; m++) {
+            const int64_t nsm = S.dims[m].ns, ncm = S.dims[m].nc, np = nsm * ncm;
+            k_vel_dual<double><<<(unsigned)cdiv(np, 128), 128, 0, st>>>(td + 16 * m, S.colloc_h[m], S.vel[m], np);
+            const double* prev = nullptr;
+            if (coupled_te && m > 0 && S.dims[m - 1].ns == nsm) prev = gfull + S.poff[m] - nsm;  // TE row of surface m-1
+            k_delta<<<(unsigned)cdiv(np, 128), 128, 0, st>>>(gfull + S.poff[m], nsm, ncm, prev, S.gdelta[m]);
+            rc = gbvlm_forces_unsteady_f64(nsm, ncm, S.verts[m], S.gdelta[m], dgfull + S.poff[m], S.vel[m],
+                                           S.areas[m], S.normals[m], S.forces[m], s);
+            if (rc) break;
+        }
+        if (rc) break;
+        const double* fs = freestream + 3 * q;
+        double la[3] = {-fs[2], 0.0, fs[0]};
+        const double ll = sqrt(la[0] * la[0] + la[2] * la[2]);
+        la[0] /= ll;
+        la[2] /= ll;
+        double cl = 0, ta = 0, tm = 0, cm = 0;
+        for (int m = 0; m < ns && rc == 0; m++) {
+            const int64_t nsm = S.dims[m].ns, ncm = S.dims[m].nc;
+            double area, clm, mac, cmm[3];
+            if ((rc = gbvlm_sum_f64(S.areas[m], nsm * ncm, &area, s))) break;
+            if ((rc = gbvlm_coeff_cl_f64(nsm, ncm, S.forces[m], la, fs, 1.0, area, &clm, s))) break;
+            if ((rc = gbvlm_mesh_mac_f64(nsm, ncm, S.verts[m], S.areas[m], &mac, s))) break;
+            if ((rc = gbvlm_coeff_cm_f64(nsm, ncm, S.forces[m], S.verts[m], ref_a + 3 * q, fs, 1.0, area, mac, cmm, s)))
+                break;
+            cl += clm * area;
+            ta += area;
+            tm += mac;
+            cm += cmm[1] * area * mac;
+            if (m == 1 && ref_b) {
+                double cmb[3];
+                if ((rc = gbvlm_coeff_cm_f64(nsm, ncm, S.forces[m], S.verts[m], ref_b + 3 * q, fs, 1.0, area, mac, cmb,
+                                             s)))
+                    break;
+                out[2 * N + q] = cmb[1];
+            }
+        }
+        out[q] = cl / ta;
+        out[N + q] = cm / (ta * tm);
+    }
+    cudaFree(C);
+    cudaFree(Dd);
+    cudaFree(DDd);
+    cudaFree(td);
+    cudaFree(gfull);
+    cudaFree(dgfull);
+    return rc;
+}
+
+}  // extern "C"

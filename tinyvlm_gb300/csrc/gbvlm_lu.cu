@@ -528,10 +528,8 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t 
     const size_t full = sizeof(T) * (size_t)maxn * TS_MAXRHS;
     const int use_smem = full <= (size_t)TS_SMEM_BYTES ? 1 : 0;
     const size_t smem = use_smem ? full : sizeof(T) * (size_t)maxn;
-    if (smem > 48 * 1024) {
-        GB_REQUIRE(smem <= (size_t)TS_SMEM_BYTES || !use_smem, "triangular solve: n=%lld too large", (long long)maxn);
-    }
-    GB_REQUIRE(smem <= 227 * 1024, "triangular solve: n=%lld needs %zu bytes of shared memory", (long long)maxn, smem);
+    GB_REQUIRE(smem <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld needs %zu bytes of shared memory",
+               (long long)maxn, smem);
     for (int32_t r0 = 0; r0 < max_nrhs; r0 += TS_MAXRHS) {
         k_trsolve<T><<<nsys, TS_THREADS, smem, st>>>(B, r0, TS_MAXRHS, use_smem);
         GB_LAUNCH_CHECK();
@@ -550,8 +548,8 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     plan.release();
     GB_CUDA(cudaFuncSetAttribute(k_panel_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_panel_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
-    GB_CUDA(cudaFuncSetAttribute(k_trsolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    GB_CUDA(cudaFuncSetAttribute(k_trsolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GB_CUDA(cudaFuncSetAttribute(k_trsolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(k_trsolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_perm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
     GB_CUDA(cudaFuncSetAttribute(k_perm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
     plan.nsys = (int32_t)n_sorted.size();
