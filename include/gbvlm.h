@@ -328,6 +328,12 @@ int gbvlm_uvlm_destroy(gbvlm_uvlm h);
 int gbvlm_uvlm_set_kinematics(gbvlm_uvlm h, const double* transforms, const double* dtransforms,
                               const double* freestream, const double* ref_pt);
 int gbvlm_uvlm_run(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_stream stream);
+/* Step-wise use (a resident case advanced one step per call): begin places
+ * the wing, assembles and factors the AIC; each step advances one time
+ * step and, if cl/cm are not NULL, reads that step's coefficients back
+ * (synchronous then).  At most t_steps-1 steps. */
+int gbvlm_uvlm_begin(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_stream stream);
+int gbvlm_uvlm_step(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, gbvlm_stream stream);
 /* cl: t_steps doubles, cm: 3*t_steps, gamma_last: n doubles of the last step (each may be NULL). Synchronous. */
 int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream);
 

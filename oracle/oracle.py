@@ -510,3 +510,134 @@ def uvlm_run(verts_init, lifting, T, Td, fs, ref, t_steps, dt, dtype=np.float64,
             displace_wing(tr(i + 1, m), verts[m], vpos[m])
         colloc, normals, areas = mesh_metrics(0.0, verts, dtype)
     return dict(cl=cl, cm=cm, gamma=gam)
+
+
+# ---------------------------------------------------------------------------
+# Anderson acceleration, vlm/src/vlm_solvers.cpp:6-115 (type II, history m;
+# least squares through LAPACK ?gels like the CPU LSQ, vlm_backend_cpu_lapack.cpp:123-205)
+# ---------------------------------------------------------------------------
+def anderson(x0, f, max_iter=100, tol=1e-6, m=3):
+    from scipy.linalg import lapack
+    x_curr = np.array(x0, np.float64)
+    n = x_curr.size
+    X = np.zeros((n, m))
+    G = np.zeros((n, m))
+    x_new = f(x_curr)
+    g_curr = x_new - x_curr
+    X[:, 0] = g_curr
+    x_curr = x_new
+    x_new = f(x_curr)
+    g_new = x_new - x_curr
+    G[:, 0] = g_new - g_curr
+    g_curr = g_new
+    k = 1
+    while k < max_iter and np.linalg.norm(g_curr) > tol:
+        mk = min(m, k)
+        A = np.asfortranarray(G[:, :mk].copy())
+        b = g_curr.copy().reshape(-1, 1)
+        _, sol, info = lapack.dgels(A, b)
+        gam = sol[:mk, 0]
+        x_new = x_curr + g_curr - X[:, :mk] @ gam - G[:, :mk] @ gam
+        X[:, k % m] = x_new - x_curr
+        x_curr = x_new
+        x_new = f(x_curr)
+        g_new = x_new - x_curr
+        G[:, k % m] = g_new - g_curr
+        g_curr = g_new
+        k += 1
+    return x_curr, k
+
+
+# ---------------------------------------------------------------------------
+# Harmonic-balance VLM, lib/libhbvlm3.cpp:262-552 (double), over the host
+# arrays the product's HBVLM module builds (kinematics, DFT, instances).
+# ---------------------------------------------------------------------------
+def hbvlm_run(verts, lifting, H, omega, dt, max_t, wake_T, inst, dft, ddft, force_inst, fs, ref_a, ref_b,
+              coupled_te, x0, tol, m=10, max_iter=100):
+    dtp = np.float64
+    verts_init = [np.ascontiguousarray(v, dtp) for v in verts]
+    ns, nc = dims(verts_init)
+    nsurf = len(verts_init)
+    N = 2 * H + 1
+    n = sum(a * b for a, b in zip(ns, nc))
+    poff = np.cumsum([0] + [a * b for a, b in zip(ns, nc)])
+    w = lifting.index(True)
+    tr = lambda A, i, mm: np.asfortranarray(np.asarray(A[i, mm]).reshape(4, 4).T)
+    vcur = [v.copy() for v in verts_init]
+    colloc_h, normals0, _ = mesh_metrics(0.0, vcur, dtp)
+    wake = []
+    for s in ns:
+        wk = np.zeros((4, max_t, s + 1), dtp)
+        wk[3] = 1
+        wake.append(wk)
+    lhs = np.zeros((n, n), dtp, order="F")
+    lhs_assemble(lhs, colloc_h, normals0, vcur, wake, 0)
+    lu, piv = lu_factor(lhs)
+    for i in range(max_t):
+        for mm in range(nsurf):
+            displace_wing(tr(wake_T, i, mm), vcur[mm], verts_init[mm])
+        wake_shed(vcur, wake, i)
+
+    def vel_of(Td, i, c0):
+        out = []
+        for mm in range(nsurf):
+            d = np.asarray(Td[i, mm]).reshape(4, 4).T
+            c = c0[mm]
+            v = np.empty_like(c)
+            for r in range(3):
+                v[r] = -(d[r, 0] * c[0] + d[r, 1] * c[1] + d[r, 2] * c[2] + d[r, 3])
+            out.append(v)
+        return out
+
+    ts, tm, T, Td = inst
+    geo = []
+    for s in range(N):
+        for mm in range(nsurf):
+            displace_wing(tr(T, s, mm), vcur[mm], verts_init[mm])
+        col, nor, _ = mesh_metrics(0.0, vcur, dtp)
+        rv = np.zeros(n, dtp)
+        rhs_assemble_velocities(rv, nor, vel_of(Td, s, colloc_h))
+        geo.append((col, nor, rv))
+
+    def fmap(xflat):
+        x = xflat.reshape(N, n).T  # column-major (n x N)
+        te = np.asfortranarray(x[poff[w] + (nc[w] - 1) * ns[w]:poff[w] + nc[w] * ns[w], :])
+        R = np.zeros((n, N), dtp, order="F")
+        for s in range(N):
+            col, nor, rv = geo[s]
+            gw = [np.zeros((max_t - 1, a), dtp) for a in ns]
+            gamma_wake_from_coeffs(gw[w], te, H, tm[s], omega, dt, int(ts[s]))
+            r = rv.copy()
+            rhs_assemble_wake_influence(r, gw, col, nor, wake, lifting, int(ts[s]))
+            R[:, s] = r
+        Y = R @ dft
+        Y = lu_solve(lu, piv, Y)
+        return np.asarray(Y).T.ravel()
+
+    xs, iters = anderson(np.asarray(x0, dtp).T.ravel() if np.ndim(x0) == 2 else x0, fmap, max_iter, tol, m)
+    X = xs.reshape(N, n).T
+    fts, ftm, fT, fTd = force_inst
+    out = np.zeros((3, N))
+    for s in range(N):
+        for mm in range(nsurf):
+            displace_wing(tr(fT, s, mm), vcur[mm], verts_init[mm])
+        col, nor, ar = mesh_metrics(0.0, vcur, dtp)
+        vel = vel_of(fTd, s, colloc_h)
+        g = X @ dft[s, :]
+        dg = X @ ddft[s, :]
+        forces = []
+        for mm in range(nsurf):
+            gm = g[poff[mm]:poff[mm + 1]].reshape(nc[mm], ns[mm])
+            dgm = dg[poff[mm]:poff[mm + 1]].reshape(nc[mm], ns[mm])
+            d = gamma_delta(gm)
+            if coupled_te and mm > 0:
+                prev = g[poff[mm - 1]:poff[mm]].reshape(nc[mm - 1], ns[mm - 1])[-1]
+                d[0] -= prev
+            forces.append(forces_unsteady(vcur[mm], np.ascontiguousarray(d), np.ascontiguousarray(dgm), vel[mm], ar[mm], nor[mm]))
+        f_s = np.asarray(fs[s], dtp)
+        out[0, s] = coeff_cl_multibody(forces, ar, f_s, 1.0)
+        out[1, s] = coeff_cm_multibody(forces, vcur, ar, np.asarray(ref_a[s]), f_s, 1.0)[1]
+        if ref_b is not None and nsurf > 1:
+            area = asum(ar[1])
+            out[2, s] = coeff_cm(forces[1], vcur[1], np.asarray(ref_b[s]), f_s, 1.0, area, mesh_mac(vcur[1], ar[1]))[1]
+    return X, out, iters

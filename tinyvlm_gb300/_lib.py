@@ -78,6 +78,8 @@ def _protos():
     t["gbvlm_uvlm_set_kinematics"] = [P, P, P, P, P]
     t["gbvlm_uvlm_run"] = [P, F64, I32, F64, P]
     t["gbvlm_uvlm_results"] = [P, P, P, P, P]
+    t["gbvlm_uvlm_begin"] = [P, F64, I32, F64, P]
+    t["gbvlm_uvlm_step"] = [P, P, P, P, P]
     t["gbvlm_hbvlm_create"] = [P, I32, P, PP, P]
     t["gbvlm_hbvlm_destroy"] = [P]
     t["gbvlm_hbvlm_prepare"] = [P, I32, I64, P, P, P, P, P, P, P]

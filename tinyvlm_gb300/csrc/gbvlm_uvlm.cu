@@ -165,6 +165,10 @@ struct UvlmBase {
     virtual ~UvlmBase() = default;
     virtual int set_kinematics(const double* T, const double* Td, const double* fs, const double* ref) = 0;
     virtual int run(double dt, int32_t rollup, double sigma, cudaStream_t st) = 0;
+    virtual int begin(double dt, int32_t rollup, double sigma, cudaStream_t st) = 0;
+    virtual int step(cudaStream_t st) = 0;
+    virtual int step_result(int64_t i, double* cl, double* cm, cudaStream_t st) = 0;
+    virtual int64_t last_step() const = 0;
     virtual int results(double* cl, double* cm, double* gamma_last, cudaStream_t st) = 0;
     int64_t t_steps = 0, n = 0;
 };
@@ -275,10 +279,28 @@ struct UvlmState : UvlmBase {
         return out;
     }
 
+    CoefArgs<T> ca;
+    T dt_ = 0, sigma_ = 0;
+    int32_t roll_ = 0;
+    int64_t next_step = 0;
+
+    static std::vector<const T*> C(const std::vector<T*>& v) { return std::vector<const T*>(v.begin(), v.end()); }
+
     int run(double dt_d, int32_t roll, double sigma_d, cudaStream_t st) override {
+        int rc = begin(dt_d, roll, sigma_d, st);
+        if (rc) return rc;
+        for (int64_t i = 0; i + 1 < t_steps; i++)
+            if ((rc = step(st))) return rc;
+        return GBVLM_OK;
+    }
+
+    int begin(double dt_d, int32_t roll, double sigma_d, cudaStream_t st) override {
         gbvlm_stream s = (gbvlm_stream)st;
         const T dt = (T)dt_d, sigma = (T)sigma_d;
-        auto C = [](const std::vector<T*>& v) { return std::vector<const T*>(v.begin(), v.end()); };
+        dt_ = dt;
+        sigma_ = sigma;
+        roll_ = roll;
+        next_step = 0;
         int rc;
         // t = 0 placement (vlm.cpp:368-376): verts_pos = T(0) verts_init; metrics; colloc at t = 0 kept
         auto t0 = tr_at(Tm, 0);
@@ -298,7 +320,6 @@ struct UvlmState : UvlmBase {
         if ((rc = Ops2<T>::lhs(lhs, n, nsurf, dims.data(), C(colloc).data(), C(normals).data(), C(verts).data(), sigma, s)))
             return rc;
         if ((rc = Ops2<T>::factor(lu, lhs, n, s))) return rc;
-        CoefArgs<T> ca;
         memset(&ca, 0, sizeof(ca));
         ca.n = nsurf;
         for (int m = 0; m < nsurf; m++) {
@@ -309,7 +330,18 @@ struct UvlmState : UvlmBase {
             ca.areas[m] = areas[m];
         }
         GB_CUDA(cudaMemsetAsync(res, 0, sizeof(double) * 4 * t_steps, st));
-        for (int64_t i = 0; i + 1 < t_steps; i++) {
+        return GBVLM_OK;
+    }
+
+    // one time step (vlm.cpp:410-508); steps run in order 0, 1, ..., t_steps-2
+    int step(cudaStream_t st) override {
+        gbvlm_stream s = (gbvlm_stream)st;
+        GB_REQUIRE(next_step + 1 < t_steps, "UVLM: all %lld steps done (wake capacity)", (long long)t_steps);
+        const int64_t i = next_step++;
+        const T dt = dt_, sigma = sigma_;
+        const int32_t roll = roll_;
+        int rc;
+        {
             if ((rc = Ops2<T>::shed(nsurf, dims.data(), C(verts).data(), wake.data(), (int32_t)i, s))) return rc;
             for (int m = 0; m < nsurf; m++) {
                 const int64_t np = dims[m].ns * dims[m].nc;
@@ -355,6 +387,18 @@ struct UvlmState : UvlmBase {
                                        s)))
                 return rc;
         }
+        return GBVLM_OK;
+    }
+
+    int64_t last_step() const override { return next_step - 1; }
+
+    int step_result(int64_t i, double* cl, double* cm, cudaStream_t st) override {
+        GB_REQUIRE(i >= 0 && i < t_steps, "step index outside the run");
+        double h[4];
+        GB_CUDA(cudaMemcpyAsync(h, res + 4 * i, sizeof(h), cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        if (cl) *cl = h[0];
+        if (cm) for (int k = 0; k < 3; k++) cm[k] = h[1 + k];
         return GBVLM_OK;
     }
 
@@ -435,6 +479,22 @@ int gbvlm_uvlm_set_kinematics(gbvlm_uvlm h, const double* transforms, const doub
 int gbvlm_uvlm_run(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_stream stream) {
     GB_REQUIRE(h && h->impl && dt > 0, "bad arguments");
     return h->impl->run(dt, rollup, sigma, to_cuda(stream));
+}
+
+int gbvlm_uvlm_begin(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_stream stream) {
+    GB_REQUIRE(h && h->impl && dt > 0, "bad arguments");
+    return h->impl->begin(dt, rollup, sigma, to_cuda(stream));
+}
+
+int gbvlm_uvlm_step(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, gbvlm_stream stream) {
+    GB_REQUIRE(h && h->impl, "null argument");
+    int rc = h->impl->step(to_cuda(stream));
+    if (rc) return rc;
+    auto* u = h->impl;
+    const int64_t i = u->last_step();
+    if (step_index) *step_index = i;
+    if (cl || cm) return u->step_result(i, cl, cm, to_cuda(stream));
+    return GBVLM_OK;
 }
 
 int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream) {

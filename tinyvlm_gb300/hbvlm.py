@@ -1,0 +1,249 @@
+"""Harmonic-balance VLM: the ``libhbvlm`` (2-DOF) and ``libhbvlm3`` (3-DOF
+wing + flap) Python modules of the reference, over the gbvlm C ABI.
+
+Mirrors lib/libhbvlm.cpp and lib/libhbvlm3.cpp: ``HBVLM(backend, mesh(es))``,
+``.init(harmonics, scaling)``, ``.run(omega, [U,] dyn_f, forces_t)`` with
+``forces_t`` filled in place.  The kinematics (heave / pitch / flap Fourier
+series) are evaluated here with dual numbers; the fixed-point map, Anderson
+acceleration and loads run in the library (double precision).  The
+circulation coefficients persist between ``run`` calls and seed the next
+fixed point, as in the reference.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import P, PP, call, dims_array
+from .kinematics import Assembly, KinematicsTree, cos, rotation_matrix, sin, translation_matrix
+from .vlm import read_plot3d
+
+PI_F = float(np.float32(3.141593))
+TWO_PI_F = float(np.float32(2.0) * np.float32(3.141593))  # 2.0f * PI_f as the reference forms it
+
+
+def dft_matrices(N, omega, period):
+    """Scaled orthonormal DFT and its time derivative (libhbvlm3.cpp:322-347), column-major (N x N)."""
+    s0 = 1.0 / math.sqrt(N)
+    s2 = math.sqrt(2.0 / N)
+    D = np.zeros((N, N))
+    DD = np.zeros((N, N))
+    D[:, 0] = s0
+    for j in range(1, N, 2):
+        k = (j + 1) / 2.0
+        for i in range(N):
+            tn = (i / N) * period
+            D[i, j] = math.cos(omega * tn * k) * s2
+            D[i, j + 1] = math.sin(omega * tn * k) * s2
+            DD[i, j] = -omega * k * math.sin(omega * tn * k) * s2
+            DD[i, j + 1] = omega * k * math.cos(omega * tn * k) * s2
+    return np.asfortranarray(D), np.asfortranarray(DD)
+
+
+def fourier(row, H, omega, t):
+    """r(row, 0) + sum_h cos(w t k) r(row, 2h+1) + sin(w t k) r(row, 2h+2) on a dual t."""
+    z = row[0] + 0.0 * t
+    for h in range(H):
+        k = float(h + 1)
+        z = z + cos(omega * t * k) * row[2 * h + 1] + sin(omega * t * k) * row[2 * h + 2]
+    return z
+
+
+def last_panel_chord(v):
+    d = v[:3, -1, 0].astype(np.float64) - v[:3, -2, 0].astype(np.float64)
+    return math.sqrt(float(d @ d))
+
+
+class HBEngine:
+    """gbvlm_hbvlm_* handle for a set of surfaces (exactly one lifting)."""
+
+    def __init__(self, verts, lifting):
+        self.verts = [np.ascontiguousarray(v, np.float64) for v in verts]
+        self.lifting = list(lifting)
+        self.n = sum((v.shape[1] - 1) * (v.shape[2] - 1) for v in self.verts)
+        d = dims_array([(v.shape[2] - 1, v.shape[1] - 1, 0) for v in self.verts])
+        arr = (ctypes.c_void_p * len(self.verts))(*[v.ctypes.data for v in self.verts])
+        lf = (ctypes.c_int32 * len(self.verts))(*[1 if x else 0 for x in self.lifting])
+        h = ctypes.c_void_p()
+        call("gbvlm_hbvlm_create", ctypes.cast(ctypes.pointer(h), P), len(self.verts), d, ctypes.cast(arr, PP),
+             ctypes.cast(lf, P))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                _lib.lib().gbvlm_hbvlm_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    @staticmethod
+    def _p(a):
+        return ctypes.c_void_p(a.ctypes.data)
+
+    def prepare(self, harmonics, max_t_steps, wake_T, t_steps, times, T, Td, dft):
+        self._keep = [np.ascontiguousarray(x) for x in (wake_T, T, Td, dft)] + \
+                     [np.ascontiguousarray(t_steps, np.int64), np.ascontiguousarray(times, np.float64)]
+        wT, T_, Td_, D_, ts, tm = self._keep
+        call("gbvlm_hbvlm_prepare", self.h, int(harmonics), int(max_t_steps), self._p(wT), self._p(ts), self._p(tm),
+             self._p(T_), self._p(Td_), self._p(D_), None)
+
+    def map(self, x, omega, dt):
+        x = np.asfortranarray(x, np.float64)
+        y = np.zeros_like(x, order="F")
+        call("gbvlm_hbvlm_map", self.h, self._p(x), self._p(y), float(omega), float(dt), None)
+        return y
+
+    def solve(self, x, omega, dt, max_iter, tol, m):
+        it = ctypes.c_int32()
+        call("gbvlm_hbvlm_solve", self.h, self._p(x), float(omega), float(dt), int(max_iter), float(tol), int(m),
+             ctypes.cast(ctypes.pointer(it), P), None)
+        return it.value
+
+    def loads(self, x, dft, ddft, T, Td, fs, ref_a, ref_b, coupled_te, N):
+        out = np.zeros(3 * N)
+        keep = [np.ascontiguousarray(a, np.float64) for a in (x, dft, ddft, T, Td, fs, ref_a)]
+        rb = np.ascontiguousarray(ref_b, np.float64) if ref_b is not None else None
+        call("gbvlm_hbvlm_loads", self.h, *[self._p(a) for a in keep], self._p(rb) if rb is not None else None,
+             1 if coupled_te else 0, self._p(out), None)
+        return out.reshape(3, N)
+
+
+def hb_arrays(assembly, N, dt, max_t_steps, t_start, period):
+    """Wake transforms per step, instance transforms/rates for the map and for the loads."""
+    nodes = assembly.surface_kinematics()
+    ns = len(nodes)
+    wake_T = np.zeros((max_t_steps, ns, 16))
+    for i in range(max_t_steps):
+        for m, nd in enumerate(nodes):
+            wake_T[i, m] = nd.transform(i * dt).T.ravel()
+
+    def inst(start):
+        ts = np.zeros(N, np.int64)
+        tm = np.zeros(N)
+        T = np.zeros((N, ns, 16))
+        Td = np.zeros((N, ns, 16))
+        for s in range(N):
+            tf = start + period * s / N
+            ts[s] = int(round(tf / dt))
+            tm[s] = ts[s] * dt
+            for m, nd in enumerate(nodes):
+                v, d = nd.transform_and_rate(tm[s])
+                T[s, m] = v.T.ravel()
+                Td[s, m] = d.T.ravel()
+        return ts, tm, T, Td
+
+    return wake_T, inst(t_start), inst(0.0)
+
+
+class _HBVLMBase:
+    qc = False
+    tol = 1e-12
+    dt_surface = 1
+
+    def __init__(self, backend_name, meshes, lifting):
+        if backend_name not in ("gb300", "cuda", "cpu"):
+            raise RuntimeError("Unsupported backend: " + backend_name)
+        self.verts_raw = [read_plot3d(m, qc=self.qc).astype(np.float64) if isinstance(m, str)
+                          else np.array(m, np.float64) for m in meshes]
+        self.lifting = lifting
+        self.m_harmonics = None
+
+    def init(self, harmonics, scaling):
+        """Scale the coordinates (libhbvlm3.cpp:176-187) and reset the coefficients."""
+        self.m_harmonics = int(harmonics)
+        self.m_coeffs = 2 * self.m_harmonics + 1
+        self.verts = []
+        for v in self.verts_raw:
+            w = v.copy()
+            w[:3] *= scaling
+            self.verts.append(w)
+        self.engine = HBEngine(self.verts, self.lifting)
+        self.gamma_coeffs = np.zeros((self.engine.n, self.m_coeffs), order="F")
+
+    def _run(self, t_start, omega, assembly, refs, forces_t, coupled_te):
+        N, H = self.m_coeffs, self.m_harmonics
+        period = TWO_PI_F / omega
+        interval = period / N
+        chord = last_panel_chord(self.verts[self.dt_surface])
+        if not interval > chord:
+            raise AssertionError("period interval %g must exceed the last panel chord %g" % (interval, chord))
+        dt = interval / math.ceil(interval / chord)
+        max_t = int((t_start + period + dt) / dt)
+        wake_T, (ts, tm, T, Td), (fts, ftm, fT, fTd) = hb_arrays(assembly, N, dt, max_t, t_start, period)
+        dft, ddft = dft_matrices(N, omega, period)
+        self.engine.prepare(H, max_t, wake_T, ts, tm, T, Td, dft)
+        self.iterations = self.engine.solve(self.gamma_coeffs, omega, dt, 100, self.tol, 10)
+        fs = np.array([-assembly.kinematics().linear_velocity(t, (0.0, 0.0, 0.0)) for t in ftm])
+        ref_a = np.array([(assembly.surface_kinematics()[0].transform(t) @ np.array([refs[0], 0, 0, 1.0]))[:3]
+                          for t in ftm])
+        ref_b = None
+        if len(refs) > 1:
+            ref_b = np.array([(assembly.surface_kinematics()[1].transform(t) @ np.array([refs[1], 0, 0, 1.0]))[:3]
+                              for t in ftm])
+        out = self.engine.loads(self.gamma_coeffs, dft, ddft, fT, fTd, fs, ref_a, ref_b, coupled_te, N)
+        rows = forces_t.shape[0]
+        forces_t[:, :] = out[:rows, :]
+        self._last = dict(dt=dt, max_t=max_t, period=period, wake_T=wake_T, inst=(ts, tm, T, Td),
+                          force_inst=(fts, ftm, fT, fTd), dft=dft, ddft=ddft, fs=fs, ref_a=ref_a, ref_b=ref_b)
+        return forces_t
+
+
+class HBVLM3(_HBVLMBase):
+    """libhbvlm3.HBVLM: wing (non-lifting) + flap (lifting), 3-DOF pitch/heave/flap."""
+    qc = False
+    tol = 1e-12
+    dt_surface = 1
+    VARS = dict(a=-0.5, b=0.127, c=0.5, omega_alpha=52.6506)
+
+    def __init__(self, backend_name, meshes):
+        if len(meshes) != 2:
+            raise AssertionError("libhbvlm3 expects two meshes (wing, flap)")
+        super().__init__(backend_name, meshes, [False, True])
+
+    def assembly(self, omega, U, dyn_f):
+        v = self.VARS
+        H = self.m_harmonics
+        r = np.asarray(dyn_f, np.float64)
+        tree = KinematicsTree()
+        fsn = tree.add(lambda t: translation_matrix([-(U / (v["b"] * v["omega_alpha"])) * t, 0.0, 0.0]))
+        heave = tree.add(lambda t: translation_matrix([0.0, 0.0, -fourier(r[0], H, omega, t)])).after(fsn)
+        pitch = tree.add(lambda t: rotation_matrix([1.0 + v["a"], 0, 0], [0, 1, 0], fourier(r[1], H, omega, t))).after(heave)
+        ctrl = tree.add(lambda t: rotation_matrix([1.0 + v["c"], 0, 0], [0, 1, 0], fourier(r[2], H, omega, t))).after(pitch)
+        asm = Assembly(fsn)
+        asm.add("wing", pitch, False)
+        asm.add("flap", ctrl, True)
+        return asm
+
+    def run(self, omega, U, dyn_f, forces_t):
+        t_final = 2.0 * TWO_PI_F / omega
+        asm = self.assembly(omega, U, dyn_f)
+        return self._run(t_final, omega, asm, (1.0 + self.VARS["a"], 1.0 + self.VARS["c"]), forces_t, True)
+
+
+class HBVLM2(_HBVLMBase):
+    """libhbvlm.HBVLM: one lifting surface, 2-DOF heave/pitch (lib/libhbvlm.cpp:470-515)."""
+    qc = True
+    tol = 1e-9
+    dt_surface = 0
+
+    def __init__(self, backend_name, mesh):
+        super().__init__(backend_name, [mesh], [True])
+
+    def assembly(self, omega, dyn_f):
+        H = self.m_harmonics
+        r = np.asarray(dyn_f, np.float64)
+        u_inf, a_h = 1.0, -0.5
+        tree = KinematicsTree()
+        fsn = tree.add(lambda t: translation_matrix([-u_inf * t, 0.0, 0.0]))
+        heave = tree.add(lambda t: translation_matrix([0.0, 0.0, -fourier(r[0], H, omega, t)])).after(fsn)
+        pitch = tree.add(lambda t: rotation_matrix([1.0 + a_h, 0, 0], [0, 1, 0], fourier(r[1], H, omega, t))).after(heave)
+        asm = Assembly(fsn)
+        asm.add("wing", pitch, True)
+        return asm
+
+    def run(self, omega, dyn_f, forces_t):
+        t_final = 3.0 * TWO_PI_F / omega
+        asm = self.assembly(omega, dyn_f)
+        return self._run(t_final, omega, asm, (0.5,), forces_t, False)
