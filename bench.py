@@ -53,10 +53,12 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
-    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm"],
+    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served"],
                    help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
                         "uvlm: 20x80 rectangular wing, 500 pitch-plunge steps")
     p.add_argument("--uvlm-steps", type=int, default=500)
+    p.add_argument("--rates", default="2,8,32", help="served: Poisson arrival rates (requests/s) to sweep")
+    p.add_argument("--requests", type=int, default=45, help="served: requests per rate")
     p.add_argument("--rollup", type=int, default=1)
     return p.parse_args()
 
@@ -415,6 +417,53 @@ def run_uvlm(args):
     print(json.dumps(out))
 
 
+def run_served(args):
+    """Poisson mixed stream in equal thirds: steady VLM on trapezoids of 256-16,384 panels (log-uniform),
+    single UVLM steps on a resident 20x80 wing with a 500-row (40,000-ring) wake, 2-DOF HBVLM residuals
+    (45 x 1 section, 5 harmonics = 11 instances); p50/p99 latency and throughput per arrival rate."""
+    import torch
+    from tinyvlm_gb300 import serve as S
+    rng = np.random.default_rng(SEED)
+    rates = [float(x) for x in args.rates.split(",")]
+    total = len(rates) * args.requests
+    uvlm = S.resident_uvlm(warm_steps=500, capacity=total + 8)
+    srv = S.Server(lanes=3, hbm_budget=48 << 30, max_batch=64, uvlm=uvlm, hbvlm=S.hbvlm_factory(45, 5)).start()
+    out = {"workload": "served mixed stream (steady 256-16384 panels / UVLM step on a 40,000-ring wake / "
+                       "HBVLM 2-DOF 45x1, H=5), Poisson arrivals", "lanes": 3, "rates": []}
+    rid = 0
+    for lam in rates:
+        reqs = []
+        t = time.perf_counter()
+        for _ in range(args.requests):
+            t += rng.exponential(1.0 / lam)
+            kind = ("steady", "uvlm", "hbvlm")[int(rng.integers(0, 3))]
+            payload = (S.steady_case(rng),) if kind == "steady" else (S.hbvlm_request(rng) if kind == "hbvlm" else None)
+            reqs.append((t, kind, payload))
+        done = []
+        for (ta, kind, payload) in reqs:
+            now = time.perf_counter()
+            if ta > now:
+                time.sleep(ta - now)
+            done.append(srv.submit(S.Request(rid, kind, payload, arrival=ta)))
+            rid += 1
+        for r in done:
+            r.done.wait()
+        lat = np.array([r.latency for r in done]) * 1000.0
+        span = max(r.finish for r in done) - min(r.arrival for r in done)
+        row = {"rate_req_s": lam, "completed": len(done), "errors": sum(r.error is not None for r in done),
+               "throughput_req_s": len(done) / span, "p50_ms": float(np.percentile(lat, 50)),
+               "p99_ms": float(np.percentile(lat, 99))}
+        for kind in ("steady", "uvlm", "hbvlm"):
+            lk = np.array([r.latency for r in done if r.kind == kind]) * 1000.0
+            if lk.size:
+                row[kind] = {"n": int(lk.size), "p50_ms": float(np.percentile(lk, 50)),
+                             "p99_ms": float(np.percentile(lk, 99))}
+        out["rates"].append(row)
+    srv.shutdown()
+    out["stats"] = dict(srv.stats)
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -423,6 +472,8 @@ def main():
         run_large(args)
     elif args.workload == "uvlm":
         run_uvlm(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_gpu(args)
 

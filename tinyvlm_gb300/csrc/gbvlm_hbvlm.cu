@@ -69,6 +69,25 @@ __global__ void k_vel_dual(const double* Td, const double* c0, double* vel, int6
     for (int r = 0; r < 3; r++) vel[r * np + p] = -(Td[r] * x + Td[r + 4] * y + Td[r + 8] * z + Td[r + 12]);
 }
 
+// wake pre-generation in one launch (libhbvlm3.cpp:307-319): wake row
+// nwv-1-i = T(i dt) applied to the trailing-edge vertices, every step i
+__global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, const double* vinit, int64_t ns, int64_t nc,
+                              int64_t max_t, double* wake) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t n1 = ns + 1;
+    if (g >= n1 * max_t) return;
+    const int64_t j = g % n1, i = g / n1;
+    const double* T = Tall + 16 * ((size_t)i * nsurf + m);
+    const int64_t nv = n1 * (nc + 1), te = j + nc * n1;
+    const double x[4] = {vinit[te], vinit[nv + te], vinit[2 * nv + te], vinit[3 * nv + te]};
+    const int64_t wl = n1 * max_t, row = max_t - 1 - i;
+    for (int c = 0; c < 4; c++) {
+        double acc = 0;
+        for (int k = 0; k < 4; k++) acc += x[k] * T[c + 4 * k];
+        wake[c * wl + j + row * n1] = acc;
+    }
+}
+
 struct Inst {
     int64_t t_steps = 0;
     double t = 0;
@@ -175,11 +194,17 @@ struct HbState {
                                          C(verts).data(), nullptr, 0, 0.0, s)))
             return rc;
         if ((rc = gbvlm_lu_factor_f64(lu, lhs, n, n, s))) return rc;
-        for (int64_t i = 0; i < max_t; i++) {
-            if ((rc = place(wake_T + 16 * nsurf * i, st))) return rc;
-            if ((rc = gbvlm_wake_shed_f64(nsurf, dims.data(), C(verts).data(), wake.data(), (int32_t)i, s))) return rc;
+        double* Tall = nullptr;
+        GB_CUDA(cudaMalloc((void**)&Tall, sizeof(double) * 16 * nsurf * max_t));
+        GB_CUDA(cudaMemcpyAsync(Tall, wake_T, sizeof(double) * 16 * nsurf * max_t, cudaMemcpyHostToDevice, st));
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t cnt = (dims[m].ns + 1) * max_t;
+            k_pregen_wake<<<(unsigned)cdiv(cnt, 128), 128, 0, st>>>(Tall, nsurf, m, vinit[m], dims[m].ns, dims[m].nc,
+                                                                     max_t, wake[m]);
+            GB_LAUNCH_CHECK();
         }
         GB_CUDA(cudaStreamSynchronize(st));
+        cudaFree(Tall);
         return GBVLM_OK;
     }
 

@@ -115,23 +115,20 @@ def hb_arrays(assembly, N, dt, max_t_steps, t_start, period):
     nodes = assembly.surface_kinematics()
     ns = len(nodes)
     wake_T = np.zeros((max_t_steps, ns, 16))
-    for i in range(max_t_steps):
-        for m, nd in enumerate(nodes):
-            wake_T[i, m] = nd.transform(i * dt).T.ravel()
+    tw = np.arange(max_t_steps) * dt
+    for m, nd in enumerate(nodes):
+        v, _ = nd.transform_series(tw)
+        wake_T[:, m] = v.transpose(0, 2, 1).reshape(-1, 16)
 
     def inst(start):
-        ts = np.zeros(N, np.int64)
-        tm = np.zeros(N)
+        ts = np.array([int(round((start + period * s / N) / dt)) for s in range(N)], np.int64)
+        tm = ts * dt
         T = np.zeros((N, ns, 16))
         Td = np.zeros((N, ns, 16))
-        for s in range(N):
-            tf = start + period * s / N
-            ts[s] = int(round(tf / dt))
-            tm[s] = ts[s] * dt
-            for m, nd in enumerate(nodes):
-                v, d = nd.transform_and_rate(tm[s])
-                T[s, m] = v.T.ravel()
-                Td[s, m] = d.T.ravel()
+        for m, nd in enumerate(nodes):
+            v, d = nd.transform_series(tm)
+            T[:, m] = v.transpose(0, 2, 1).reshape(-1, 16)
+            Td[:, m] = d.transpose(0, 2, 1).reshape(-1, 16)
         return ts, tm, T, Td
 
     return wake_T, inst(t_start), inst(0.0)
@@ -175,13 +172,14 @@ class _HBVLMBase:
         dft, ddft = dft_matrices(N, omega, period)
         self.engine.prepare(H, max_t, wake_T, ts, tm, T, Td, dft)
         self.iterations = self.engine.solve(self.gamma_coeffs, omega, dt, 100, self.tol, 10)
-        fs = np.array([-assembly.kinematics().linear_velocity(t, (0.0, 0.0, 0.0)) for t in ftm])
-        ref_a = np.array([(assembly.surface_kinematics()[0].transform(t) @ np.array([refs[0], 0, 0, 1.0]))[:3]
-                          for t in ftm])
+        _, da = assembly.kinematics().transform_series(ftm)
+        fs = -da[:, :3, 3]
+        v0, _ = assembly.surface_kinematics()[0].transform_series(ftm)
+        ref_a = (v0 @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
         ref_b = None
         if len(refs) > 1:
-            ref_b = np.array([(assembly.surface_kinematics()[1].transform(t) @ np.array([refs[1], 0, 0, 1.0]))[:3]
-                              for t in ftm])
+            v1, _ = assembly.surface_kinematics()[1].transform_series(ftm)
+            ref_b = (v1 @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
         out = self.engine.loads(self.gamma_coeffs, dft, ddft, fT, fTd, fs, ref_a, ref_b, coupled_te, N)
         rows = forces_t.shape[0]
         forces_t[:, :] = out[:rows, :]

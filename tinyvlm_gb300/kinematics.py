@@ -18,12 +18,13 @@ __all__ = ["Dual", "sin", "cos", "translation_matrix", "rotation_matrix", "Kinem
 
 
 class Dual:
-    """a + b eps with eps^2 = 0 (headeronly/tinyad.hpp fwd::Number)."""
+    """a + b eps with eps^2 = 0 (headeronly/tinyad.hpp fwd::Number).  val and
+    grad may be numpy arrays, so a whole time series evaluates at once."""
     __slots__ = ("val", "grad")
 
     def __init__(self, val, grad=0.0):
-        self.val = float(val)
-        self.grad = float(grad)
+        self.val = val
+        self.grad = grad
 
     @staticmethod
     def lift(x):
@@ -61,12 +62,12 @@ class Dual:
 
 def sin(x):
     x = Dual.lift(x)
-    return Dual(math.sin(x.val), math.cos(x.val) * x.grad)
+    return Dual(np.sin(x.val), np.cos(x.val) * x.grad)
 
 
 def cos(x):
     x = Dual.lift(x)
-    return Dual(math.cos(x.val), -math.sin(x.val) * x.grad)
+    return Dual(np.cos(x.val), -np.sin(x.val) * x.grad)
 
 
 def _I():
@@ -113,7 +114,7 @@ class KinematicNode:
         return self
 
     def transform_dual(self, t):
-        own = self.fn(Dual(t, 1.0))
+        own = self.fn(Dual(float(t), 1.0))
         return matmul(self.parent.transform_dual(t), own) if self.parent else own
 
     def transform(self, t):
@@ -122,8 +123,24 @@ class KinematicNode:
 
     def transform_and_rate(self, t):
         m = self.transform_dual(t)
-        return (np.array([[m[r][c].val for c in range(4)] for r in range(4)]),
-                np.array([[m[r][c].grad for c in range(4)] for r in range(4)]))
+        return (np.array([[m[r][c].val for c in range(4)] for r in range(4)], dtype=np.float64),
+                np.array([[m[r][c].grad for c in range(4)] for r in range(4)], dtype=np.float64))
+
+    def transform_series(self, ts):
+        """Transforms and rates at every time of ``ts``: two (len(ts), 4, 4) arrays."""
+        ts = np.asarray(ts, np.float64)
+        m = self.transform_dual_array(ts)
+        val = np.empty((ts.size, 4, 4))
+        grad = np.empty((ts.size, 4, 4))
+        for r in range(4):
+            for c in range(4):
+                val[:, r, c] = np.broadcast_to(m[r][c].val, ts.shape)
+                grad[:, r, c] = np.broadcast_to(m[r][c].grad, ts.shape)
+        return val, grad
+
+    def transform_dual_array(self, ts):
+        own = self.fn(Dual(ts, np.ones_like(ts)))
+        return matmul(self.parent.transform_dual_array(ts), own) if self.parent else own
 
     def linear_velocity(self, t, vertex):
         """d/dt of the transformed vertex (vlm_kinematics.hpp linear_velocity)."""

@@ -1,0 +1,295 @@
+"""Served mixed stream: continuous batching of steady VLM solves, UVLM
+single-step advances of a resident unsteady case, and harmonic-balance
+(HBVLM) residual evaluations on one GPU.
+
+Design
+------
+* ``lanes`` worker threads, each with its own CUDA stream; the library
+  calls release the GIL, so work of different lanes overlaps on the device.
+* One FIFO queue.  A lane that takes a steady request also takes every
+  other steady request already waiting (continuous batching) up to
+  ``max_batch`` cases and the free HBM budget, and solves them as one
+  batched graph (``tinyvlm_gb300.batch``); requests arriving meanwhile wait
+  for the next free lane.
+* Admission by HBM budget: each request reserves its device footprint
+  (AIC + work arrays for steady batches, the resident states are reserved
+  at start-up) before launch and releases it when done; a request that does
+  not fit waits at the head of the queue.
+* The UVLM case (wing, wake, AIC factors) and one HBVLM engine per lane
+  stay resident; a UVLM request advances the case by one time step (steps
+  are serialised, they depend on each other), an HBVLM request runs the
+  harmonic-balance fixed point for its own frequency and amplitudes.
+
+Every result carries its arrival, start and finish times; ``latency`` is
+finish - arrival.
+"""
+import collections
+import math
+import threading
+import time
+
+import numpy as np
+
+from . import mesh as M
+from .batch import BatchSolver, pack_alphas, pack_verts
+
+
+class Request:
+    __slots__ = ("rid", "kind", "payload", "arrival", "start", "finish", "result", "error", "done")
+
+    def __init__(self, rid, kind, payload, arrival=None):
+        self.rid, self.kind, self.payload = rid, kind, payload
+        self.arrival = time.perf_counter() if arrival is None else arrival
+        self.start = self.finish = None
+        self.result = self.error = None
+        self.done = threading.Event()
+
+    @property
+    def latency(self):
+        return None if self.finish is None else self.finish - self.arrival
+
+
+def steady_bytes(n, nalpha=1):
+    """Device footprint of one steady system in the batched engine (AIC plus per-panel and per-solve arrays)."""
+    return 4 * n * n + 200 * n + 64 * n * nalpha + 4096
+
+
+class Server:
+    def __init__(self, lanes=3, hbm_budget=32 << 30, max_batch=64, uvlm=None, hbvlm=None, mode="exact"):
+        import torch
+        self.torch = torch
+        self.lanes = lanes
+        self.budget = int(hbm_budget)
+        self.used = 0
+        self.max_batch = max_batch
+        self.mode = mode
+        self.q = collections.deque()
+        self.cv = threading.Condition()
+        self.stop = False
+        self.uvlm = uvlm          # resident unsteady case, or None
+        self.uvlm_cv = threading.Condition()
+        self.uvlm_next_ticket = 0  # issued at dequeue time: steps run in arrival order
+        self.uvlm_turn = 0
+        self.hbvlm_factory = hbvlm
+        self.threads = []
+        self.stats = collections.Counter()
+
+    # -- resident state -----------------------------------------------------
+    def reserve(self, nbytes, block=True):
+        with self.cv:
+            while self.used + nbytes > self.budget:
+                if not block:
+                    return False
+                self.cv.wait(0.01)
+            self.used += nbytes
+            return True
+
+    def release(self, nbytes):
+        with self.cv:
+            self.used -= nbytes
+            self.cv.notify_all()
+
+    # -- lifecycle ----------------------------------------------------------
+    def start(self):
+        for k in range(self.lanes):
+            t = threading.Thread(target=self._lane, args=(k,), daemon=True)
+            t.start()
+            self.threads.append(t)
+        return self
+
+    def shutdown(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        for t in self.threads:
+            t.join()
+
+    def submit(self, req):
+        with self.cv:
+            self.q.append(req)
+            self.cv.notify()
+        return req
+
+    # -- workers ------------------------------------------------------------
+    def _take(self):
+        with self.cv:
+            while not self.q and not self.stop:
+                self.cv.wait(0.05)
+            if not self.q:
+                return None
+            head = self.q.popleft()
+            group = [head]
+            if head.kind == "uvlm":
+                head.payload = self.uvlm_next_ticket
+                self.uvlm_next_ticket += 1
+            if head.kind == "steady":
+                need = steady_bytes(head.payload[0].n, len(head.payload[0].alphas))
+                keep = collections.deque()
+                while self.q and len(group) < self.max_batch:
+                    r = self.q.popleft()
+                    if r.kind == "steady":
+                        b = steady_bytes(r.payload[0].n, len(r.payload[0].alphas))
+                        if self.used + need + b <= self.budget:
+                            group.append(r)
+                            need += b
+                            continue
+                    keep.append(r)
+                self.q.extendleft(reversed(keep))
+            return group
+
+    def _lane(self, k):
+        torch = self.torch
+        stream = torch.cuda.Stream()
+        hb = self.hbvlm_factory() if self.hbvlm_factory else None
+        with torch.cuda.stream(stream):
+            while True:
+                group = self._take()
+                if group is None:
+                    return
+                t0 = time.perf_counter()
+                for r in group:
+                    r.start = t0
+                try:
+                    kind = group[0].kind
+                    if kind == "steady":
+                        self._steady(group, stream)
+                    elif kind == "uvlm":
+                        self._uvlm(group[0], stream)
+                    elif kind == "hbvlm":
+                        self._hbvlm(group[0], hb)
+                    else:
+                        raise ValueError("unknown request kind " + kind)
+                except Exception as e:  # the request fails, the lane keeps serving
+                    for r in group:
+                        r.error = e
+                t1 = time.perf_counter()
+                for r in group:
+                    r.finish = t1
+                    r.done.set()
+                self.stats[group[0].kind + "_groups"] += 1
+
+    def _steady(self, group, stream):
+        cases = [r.payload[0] for r in group]
+        need = sum(steady_bytes(c.n, len(c.alphas)) for c in cases)
+        if need > self.budget:
+            raise MemoryError("steady request needs %d bytes, above the %d-byte device budget" % (need, self.budget))
+        self.reserve(need)
+        try:
+            bs = BatchSolver(cases, mode=self.mode, refine=0)
+            bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=(0.25, 0.0, 0.0), stream=stream)
+            bs.run(want_gamma=False, stream=stream)
+            co, _ = bs.results(stream=stream)
+            del bs
+        finally:
+            self.release(need)
+        k = 0
+        for r, c in zip(group, cases):
+            r.result = co[k:k + len(c.alphas)].copy()
+            k += len(c.alphas)
+        self.stats["steady_solves"] += k
+
+    def _uvlm(self, req, stream):
+        import ctypes
+        from ._lib import P, call
+        ticket = req.payload
+        with self.uvlm_cv:
+            while self.uvlm_turn != ticket:
+                self.uvlm_cv.wait(0.01)
+        try:
+            sim = self.uvlm
+            step = ctypes.c_int64()
+            cl = ctypes.c_double()
+            cm = (ctypes.c_double * 3)()
+            call("gbvlm_uvlm_step", sim.h, ctypes.cast(ctypes.pointer(step), P), ctypes.cast(ctypes.pointer(cl), P),
+                 ctypes.cast(cm, P), ctypes.c_void_p(stream.cuda_stream))
+            req.result = (step.value, cl.value, tuple(cm))
+        finally:
+            with self.uvlm_cv:
+                self.uvlm_turn += 1
+                self.uvlm_cv.notify_all()
+
+    def _hbvlm(self, req, hb):
+        omega, dyn = req.payload
+        ft = np.zeros((2, dyn.shape[1]))
+        hb.gamma_coeffs[:] = 0.0  # each residual evaluation starts from rest, independent of order
+        hb.run(omega, dyn, ft)
+        req.result = ft
+
+
+# ---------------------------------------------------------------------------
+# workload helpers
+# ---------------------------------------------------------------------------
+def steady_case(rng, n_lo=256, n_hi=16384):
+    """Random trapezoid with a panel count log-uniform in [n_lo, n_hi]."""
+    n = int(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi))))
+    nc = int(np.clip(round(math.sqrt(n / 4.0)), 4, 64))
+    ns = int(np.clip(round(n / nc), 4, 512))
+    ar = float(rng.uniform(4, 12))
+    lam = float(rng.uniform(0.3, 1.0))
+    sw = float(rng.uniform(0, 35))
+    v = M.trapezoid(nc, ns, ar, lam, sw).astype(np.float32)
+    M.quarter_chord(v)
+    return M.Case(v, np.radians([rng.uniform(-8, 8)]), dict(nc=nc, ns=ns))
+
+
+def resident_uvlm(ns=80, nc=20, warm_steps=500, capacity=4096, rollup=False):
+    """The resident unsteady case: 20 x 80 pitch-plunge wing advanced
+    ``warm_steps`` steps (wake of warm_steps x ns rings); ``capacity`` bounds
+    the further steps it can serve."""
+    import ctypes
+    from . import _lib
+    from ._lib import P, PP, call, dims_array
+    from .kinematics import Assembly, KinematicsTree, rotation_matrix, sin, translation_matrix
+    from .uvlm import kinematics_arrays
+    v = M.rectangular(nc, ns, 1.0, 4.0).astype(np.float32)
+    M.quarter_chord(v)
+    k = 0.5
+    tree = KinematicsTree()
+    fs = tree.add(lambda t: translation_matrix([-t, 0.0, 0.0]))
+    heave = tree.add(lambda t: translation_matrix([0.0, 0.0, 0.1 * sin(k * t)])).after(fs)
+    pitch = tree.add(lambda t: rotation_matrix([0.25, 0, 0], [0, 1, 0], math.radians(3.0) * sin(k * t + math.pi / 2))).after(heave)
+    asm = Assembly(fs)
+    asm.add("wing", pitch)
+    t_steps = warm_steps + capacity + 2
+    T, Td, fsv, ref = kinematics_arrays(asm, t_steps, 0.05)
+
+    class Sim:
+        pass
+
+    sim = Sim()
+    sim.verts = v
+    d = dims_array([(ns, nc, 0)])
+    arr = (ctypes.c_void_p * 1)(v.ctypes.data)
+    lf = (ctypes.c_int32 * 1)(1)
+    h = ctypes.c_void_p()
+    call("gbvlm_uvlm_create", ctypes.cast(ctypes.pointer(h), P), 1, d, ctypes.cast(arr, PP), ctypes.cast(lf, P),
+         int(t_steps), 32)
+    sim.h = h
+    sim.keep = [np.ascontiguousarray(x) for x in (T, Td, fsv, ref)]
+    call("gbvlm_uvlm_set_kinematics", h, *[ctypes.c_void_p(x.ctypes.data) for x in sim.keep])
+    call("gbvlm_uvlm_begin", h, 0.05, 1 if rollup else 0, 0.0, None)
+    for _ in range(warm_steps):
+        call("gbvlm_uvlm_step", h, None, None, None, None)
+    return sim
+
+
+def hbvlm_factory(nc=45, harmonics=5):
+    """2-DOF pitch-heave section wing (nc chordwise x 1 spanwise)."""
+    from .hbvlm import HBVLM2
+
+    def make():
+        v = M.rectangular(nc, 1, 1.0, 40000.0)
+        hb = HBVLM2("gb300", v)
+        hb.init(harmonics, 1.0)
+        return hb
+
+    return make
+
+
+def hbvlm_request(rng, harmonics=5):
+    omega = float(rng.uniform(0.2, 0.6))
+    dyn = np.zeros((2, 2 * harmonics + 1))
+    dyn[0, 1:3] = rng.uniform(-0.02, 0.02, 2)
+    dyn[1, 0] = rng.uniform(-0.02, 0.02)
+    dyn[1, 1:3] = rng.uniform(-0.04, 0.04, 2)
+    return omega, dyn

@@ -23,19 +23,17 @@ __all__ = ["UVLM", "kinematics_arrays"]
 def kinematics_arrays(assembly, t_steps, dt):
     """Per-step transforms, their rates, freestream and moment reference."""
     nsurf = len(assembly.surface_kinematics())
+    ts = np.arange(t_steps + 1) * dt
     T = np.zeros((t_steps + 1, nsurf, 16))
     Td = np.zeros((t_steps + 1, nsurf, 16))
-    fs = np.zeros((t_steps + 1, 3))
-    ref = np.zeros((t_steps + 1, 3))
-    for i in range(t_steps + 1):
-        t = i * dt
-        for m, node in enumerate(assembly.surface_kinematics()):
-            v, d = node.transform_and_rate(t)
-            T[i, m] = v.T.ravel()
-            Td[i, m] = d.T.ravel()
-        fs[i] = -assembly.kinematics().linear_velocity(t, (0.0, 0.0, 0.0))
-        m0 = assembly.surface_kinematics()[0].transform(t)
-        ref[i] = (m0 @ np.array([0.5, 0.0, 0.0, 1.0]))[:3]
+    for m, node in enumerate(assembly.surface_kinematics()):
+        v, d = node.transform_series(ts)
+        T[:, m] = v.transpose(0, 2, 1).reshape(-1, 16)
+        Td[:, m] = d.transpose(0, 2, 1).reshape(-1, 16)
+    _, da = assembly.kinematics().transform_series(ts)
+    fs = -da[:, :3, 3]  # -(dT/dt) [0 0 0 1]: velocity of the assembly origin
+    v0, _ = assembly.surface_kinematics()[0].transform_series(ts)
+    ref = (v0 @ np.array([0.5, 0.0, 0.0, 1.0]))[:, :3]
     return T, Td, fs, ref
 
 
