@@ -29,9 +29,33 @@ def test_hbvlm3_matches_oracle(cuda):
     L = hb._last
     X, out, it = O.hbvlm_run(hb.verts, [False, True], 2, 1.0, L["dt"], L["max_t"], L["wake_T"], L["inst"], L["dft"],
                              L["ddft"], L["force_inst"], L["fs"], L["ref_a"], L["ref_b"], True, x0, 1e-12)
-    np.testing.assert_allclose(hb.gamma_coeffs, X, rtol=1e-8, atol=1e-10)
+    print("gpu iterations", hb.iterations, "oracle", it)
+    print("gpu forces", ft)
+    print("oracle forces", out)
+    print("gamma max diff", np.abs(hb.gamma_coeffs - X).max(), np.abs(X).max())
     np.testing.assert_allclose(ft, out, rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(hb.gamma_coeffs, X, rtol=1e-8, atol=1e-10)
     assert np.abs(ft).max() > 0
+
+
+def test_hbvlm_single_map_matches_oracle(cuda):
+    """One fixed-point map (no Anderson) from a nonzero state, both implementations."""
+    wing = section(9, 0.0, 0.1905)
+    flap = section(3, 0.1905, 0.254)
+    hb = HBVLM3("gb300", [wing, flap])
+    hb.init(2, 1.0 / 0.127)
+    dyn = np.array([[0.0, 0.01, 0.0, 0.0, 0.0], [0.02, 0.0, 0.03, 0.0, 0.0], [0.0, 0.01, 0.0, 0.005, 0.0]])
+    ft = np.zeros((3, 5))
+    hb.run(1.0, 10.0, dyn, ft)
+    L = hb._last
+    rng = np.random.default_rng(0)
+    x = np.asfortranarray(rng.standard_normal((hb.engine.n, 5)) * 0.01)
+    y = hb.engine.map(x, 1.0, L["dt"])
+    # oracle map through a 1-iteration Anderson is not available; rebuild it by running with max_iter=2
+    X1, _, _ = O.hbvlm_run(hb.verts, [False, True], 2, 1.0, L["dt"], L["max_t"], L["wake_T"], L["inst"], L["dft"],
+                           L["ddft"], L["force_inst"], L["fs"], L["ref_a"], L["ref_b"], True, x, 1e-30, max_iter=1)
+    print("map diff", np.abs(y - X1).max(), np.abs(X1).max())
+    np.testing.assert_allclose(y, X1, rtol=1e-9, atol=1e-12)
 
 
 def test_hbvlm2_matches_oracle(cuda):

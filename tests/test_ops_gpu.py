@@ -253,3 +253,22 @@ def test_lu_singular(cuda):
     lu.init(At)
     with pytest.raises(Exception):
         lu.factorize(At)
+
+
+@pytest.mark.parametrize("n,nrhs", [(2000, 3), (6500, 10)])
+def test_lu_large(cuda, n, nrhs):
+    """Tall panels (thread-block cluster path) and, at n = 6500, the multi-CTA
+    triangular solve; a diagonally weighted random matrix, float."""
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n)).astype(np.float32) + np.float32(0.05 * n) * np.eye(n, dtype=np.float32)
+    b = rng.standard_normal((nrhs, n)).astype(np.float32)
+    be = B.Backend(torch.float32)
+    At = T(np.ascontiguousarray(A.T))
+    X = T(b)
+    lu = be.create_lu_solver()
+    lu.init(At)
+    lu.factorize(At)
+    lu.solve(At, X)
+    x = H(X).astype(np.float64)
+    res = np.abs(A.astype(np.float64) @ x.T - b.T.astype(np.float64)).max()
+    assert res <= 1e-3 * np.abs(b).max() * 10, res

@@ -15,6 +15,7 @@
 //   trsm   : U12 = L11^-1 A12 (unit lower, L11 staged in shared memory)
 //   update : A22 -= L21 U12, 64x64 register-tiled tiles enumerated over all
 //            systems through a per-step prefix table
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -174,6 +175,108 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_smem(LuBatch<T> B, int6
     }
     for (int t = 0; t < nb; t++)
         for (int r = tid; r < rows; r += PANEL_THREADS) A[(k + r) + (k + t) * ld] = P[t * rows + r];
+}
+
+// Tall panels: a thread-block cluster of `csize` CTAs holds the panel in its
+// distributed shared memory, CTA q owning rows [q*slab, (q+1)*slab) of it.
+// Per column: local arg-max, cluster barrier, every CTA reads the csize
+// candidates over DSMEM and picks the same pivot (largest |a|, first row on
+// ties); the CTA owning the diagonal row swaps it with the pivot row across
+// the panel over DSMEM; after a second barrier every CTA copies the pivot row
+// and updates its own rows.  All remote accesses finish before the final
+// barrier, so no CTA exits while another still reads its shared memory.
+constexpr int PC_THREADS = 512;
+
+template <class T>
+__global__ void __launch_bounds__(PC_THREADS) k_panel_cluster(LuBatch<T> B, int64_t k, const int32_t* act, int slab) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int csize = (int)cl.num_blocks();
+    const int rank = (int)cl.block_rank();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* P = reinterpret_cast<T*>(smem_raw);  // [nb][slab]
+    __shared__ T cand_v;
+    __shared__ int cand_i;
+    __shared__ T prow[GK];
+    __shared__ T s_val[PC_THREADS / 32];
+    __shared__ int s_idx[PC_THREADS / 32];
+    __shared__ int s_piv;
+    const int32_t sid = act[blockIdx.x / csize];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    T* A = B.A[sid];
+    int32_t* ipiv = B.ipiv[sid];
+    const int nb = (int)min((int64_t)GK, n - k);
+    const int rows = (int)(n - k);
+    const int r0 = rank * slab, r1 = min(rows, r0 + slab);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int t = 0; t < nb; t++)
+        for (int r = r0 + tid; r < r1; r += PC_THREADS) P[t * slab + (r - r0)] = A[(k + r) + (k + t) * ld];
+    cl.sync();
+    for (int jj = 0; jj < nb; jj++) {
+        T best = (T)-1;
+        int bi = rows;
+        for (int r = max(r0, jj) + tid; r < r1; r += PC_THREADS) {
+            const T v = tabs(P[jj * slab + (r - r0)]);
+            if (v > best) { best = v; bi = r; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const T ov = __shfl_down_sync(0xffffffffu, best, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            T bv = s_val[0];
+            int bix = s_idx[0];
+            for (int w = 1; w < PC_THREADS / 32; w++)
+                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bix)) { bv = s_val[w]; bix = s_idx[w]; }
+            cand_v = bv;
+            cand_i = bix;
+        }
+        cl.sync();
+        if (tid == 0) {
+            T bv = (T)-1;
+            int bix = rows;
+            for (int q = 0; q < csize; q++) {
+                const T v = *cl.map_shared_rank(&cand_v, q);
+                const int i = *cl.map_shared_rank(&cand_i, q);
+                if (v > bv || (v == bv && i < bix)) { bv = v; bix = i; }
+            }
+            s_piv = bix;
+            if (rank == 0) {
+                ipiv[k + jj] = (int32_t)(k + bix);
+                if (bv == (T)0 && B.info[sid] == 0) B.info[sid] = (int32_t)(k + jj + 1);
+            }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        const int owner_j = jj / slab, owner_p = p / slab;
+        if (p != jj && rank == owner_j) {
+            T* Pp = cl.map_shared_rank(P, owner_p);
+            for (int t = tid; t < nb; t += PC_THREADS) {
+                const T a = P[t * slab + (jj - r0)];
+                const T b = Pp[t * slab + (p - owner_p * slab)];
+                P[t * slab + (jj - r0)] = b;
+                Pp[t * slab + (p - owner_p * slab)] = a;
+            }
+        }
+        cl.sync();
+        const T* Pj = cl.map_shared_rank(P, owner_j);
+        for (int t = tid; t < nb; t += PC_THREADS) prow[t] = Pj[t * slab + (jj - owner_j * slab)];
+        __syncthreads();
+        const T d = prow[jj];
+        for (int r = max(r0, jj + 1) + tid; r < r1; r += PC_THREADS) {
+            T l = P[jj * slab + (r - r0)];
+            if (d != (T)0) l = l / d;
+            P[jj * slab + (r - r0)] = l;
+            for (int t = jj + 1; t < nb; t++) P[t * slab + (r - r0)] -= l * prow[t];
+        }
+    }
+    cl.sync();
+    for (int t = 0; t < nb; t++)
+        for (int r = r0 + tid; r < r1; r += PC_THREADS) A[(k + r) + (k + t) * ld] = P[t * slab + (r - r0)];
 }
 
 // ---------------------------------------------------------------------------
@@ -477,6 +580,107 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
 }
 
 // ---------------------------------------------------------------------------
+// triangular solves of one large system (n too big for the per-CTA solve):
+// block-row sweeps, each block step = one CTA solving the 32 x 32 diagonal
+// block for every right-hand side + a grid updating all rows below (above)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_perm_apply(LuBatch<T> B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* stage = reinterpret_cast<T*>(smem_raw);
+    const int64_t n = B.n[0], ldx = B.ldx[0];
+    T* x = B.X[0] + (int64_t)blockIdx.x * ldx;
+    const int32_t* pm = B.perm[0];
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) stage[r] = x[pm[r]];
+    __syncthreads();
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) x[r] = stage[r];
+}
+
+// one warp per right-hand side, a lane per row of the diagonal block
+template <class T>
+__global__ void __launch_bounds__(256) k_trs_diag(LuBatch<T> B, int64_t k, int upper) {
+    __shared__ T dg[GK][GK + 1];
+    const int64_t n = B.n[0], ld = B.ld[0], ldx = B.ldx[0];
+    const T* A = B.A[0];
+    const int nb = (int)min((int64_t)GK, n - k);
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) dg[e % nb][e / nb] = A[(k + e % nb) + (k + e / nb) * ld];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    for (int q = threadIdx.x >> 5; q < B.nrhs[0]; q += nw) {
+        T* x = B.X[0] + (int64_t)q * ldx + k;
+        T v = lane < nb ? x[lane] : (T)0;
+        if (!upper) {
+            for (int r = 0; r < nb; r++) {
+                const T xr = __shfl_sync(0xffffffffu, v, r);
+                if (lane > r && lane < nb) v -= dg[lane][r] * xr;
+            }
+        } else {
+            for (int r = nb - 1; r >= 0; r--) {
+                T xr = __shfl_sync(0xffffffffu, v, r);
+                xr = xr / dg[r][r];
+                if (lane == r) v = xr;
+                if (lane < r) v -= dg[lane][r] * xr;
+            }
+        }
+        if (lane < nb) x[lane] = v;
+    }
+}
+
+// rows [lo, hi) -= A[rows, k:k+nb] x[k:k+nb, :]; grid (row blocks, rhs blocks of 8)
+template <class T>
+__global__ void __launch_bounds__(256) k_trs_update(LuBatch<T> B, int64_t k, int64_t lo, int64_t hi) {
+    __shared__ T xs[GK][8];
+    const int64_t n = B.n[0], ld = B.ld[0], ldx = B.ldx[0];
+    const T* A = B.A[0];
+    const int nb = (int)min((int64_t)GK, n - k);
+    const int q0 = blockIdx.y * 8;
+    const int nq = min(8, B.nrhs[0] - q0);
+    for (int e = threadIdx.x; e < nb * 8; e += blockDim.x) {
+        const int l = e % nb, q = e / nb;
+        xs[l][q] = q < nq ? B.X[0][(k + l) + (int64_t)(q0 + q) * ldx] : (T)0;
+    }
+    __syncthreads();
+    const int64_t r = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= hi) return;
+    T acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) acc[q] = 0;
+    for (int l = 0; l < nb; l++) {
+        const T a = A[r + (k + l) * ld];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] += a * xs[l][q];
+    }
+    for (int q = 0; q < nq; q++) B.X[0][r + (int64_t)(q0 + q) * ldx] -= acc[q];
+}
+
+template <class T>
+int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st) {
+    GB_REQUIRE(sizeof(T) * (size_t)n <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld too large", (long long)n);
+    k_perm_apply<T><<<nrhs, 256, sizeof(T) * n, st>>>(B);
+    GB_LAUNCH_CHECK();
+    const unsigned qb = (unsigned)cdiv(nrhs, 8);
+    for (int64_t k = 0; k < n; k += GK) {
+        k_trs_diag<T><<<1, 256, 0, st>>>(B, k, 0);
+        GB_LAUNCH_CHECK();
+        const int64_t lo = k + GK;
+        if (lo < n) {
+            k_trs_update<T><<<dim3((unsigned)cdiv(n - lo, 256), qb), 256, 0, st>>>(B, k, lo, n);
+            GB_LAUNCH_CHECK();
+        }
+    }
+    for (int64_t k = ((n - 1) / GK) * GK; k >= 0; k -= GK) {
+        k_trs_diag<T><<<1, 256, 0, st>>>(B, k, 1);
+        GB_LAUNCH_CHECK();
+        if (k > 0) {
+            k_trs_update<T><<<dim3((unsigned)cdiv(k, 256), qb), 256, 0, st>>>(B, k, 0, k);
+            GB_LAUNCH_CHECK();
+        }
+    }
+    return GBVLM_OK;
+}
+
+// ---------------------------------------------------------------------------
 // host plan
 // ---------------------------------------------------------------------------
 template <class T>
@@ -490,8 +694,29 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
         const int n_glob = S.n_tall_by_elem[sizeof(T) == 4 ? 0 : 1];
         (void)max_rows;
         if (n_glob > 0) {
-            k_panel<T><<<n_glob, PANEL_THREADS, 0, st>>>(B, S.k, plan.d_act + S.act_off);
-            GB_LAUNCH_CHECK();
+            // rows of the tallest panel spread over a cluster of CTAs
+            const int64_t rows_max = S.n_tall_rows[sizeof(T) == 4 ? 0 : 1];
+            const int csize = plan.cluster;
+            const int slab = (int)cdiv(rows_max, csize);
+            const size_t smem = (size_t)slab * GK * sizeof(T);
+            if (csize >= 2 && smem <= (size_t)PANEL_SMEM_BYTES) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3((unsigned)(n_glob * csize));
+                cfg.blockDim = dim3(PC_THREADS);
+                cfg.dynamicSmemBytes = smem;
+                cfg.stream = st;
+                cudaLaunchAttribute at[1];
+                at[0].id = cudaLaunchAttributeClusterDimension;
+                at[0].val.clusterDim.x = csize;
+                at[0].val.clusterDim.y = 1;
+                at[0].val.clusterDim.z = 1;
+                cfg.attrs = at;
+                cfg.numAttrs = 1;
+                GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_cluster<T>, B, S.k, plan.d_act + S.act_off, slab));
+            } else {
+                k_panel<T><<<n_glob, PANEL_THREADS, 0, st>>>(B, S.k, plan.d_act + S.act_off);
+                GB_LAUNCH_CHECK();
+            }
         }
         if (S.n_panel > n_glob) {
             const int64_t rows = S.smem_rows[sizeof(T) == 4 ? 0 : 1];
@@ -527,6 +752,7 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t 
     // X of the largest system in shared memory when it fits, else staged per column
     const size_t full = sizeof(T) * (size_t)maxn * TS_MAXRHS;
     const int use_smem = full <= (size_t)TS_SMEM_BYTES ? 1 : 0;
+    if (!use_smem && nsys == 1) return lu_large_solve<T>(B, maxn, max_nrhs, st);
     const size_t smem = use_smem ? full : sizeof(T) * (size_t)maxn;
     GB_REQUIRE(smem <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld needs %zu bytes of shared memory",
                (long long)maxn, smem);
@@ -551,9 +777,38 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     GB_CUDA(cudaFuncSetAttribute(k_trsolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_trsolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_perm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
+    GB_CUDA(cudaFuncSetAttribute(k_perm_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(k_perm_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_perm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
     plan.nsys = (int32_t)n_sorted.size();
     plan.maxn = n_sorted.empty() ? 0 : n_sorted[0];
+    // largest cluster the device schedules for the tall-panel kernel (16 needs the non-portable opt-in)
+    plan.cluster = 0;
+    {
+        cudaFuncSetAttribute(k_panel_cluster<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_cluster<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        GB_CUDA(cudaFuncSetAttribute(k_panel_cluster<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
+        GB_CUDA(cudaFuncSetAttribute(k_panel_cluster<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
+        for (int c : {16, 8, 4}) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(PC_THREADS);
+            cfg.dynamicSmemBytes = PANEL_SMEM_BYTES;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, k_panel_cluster<float>, &cfg) == cudaSuccess && nclusters > 0) {
+                plan.cluster = c;
+                break;
+            }
+            cudaGetLastError();
+        }
+    }
     const int nsys = (int)n_sorted.size();
     for (int i = 1; i < nsys; i++) GB_REQUIRE(n_sorted[i] <= n_sorted[i - 1], "lu plan: sizes not sorted");
     std::vector<int32_t> act;
@@ -573,6 +828,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             int tall = 0;
             while (tall < cnt && n_sorted[tall] - k > lim) tall++;
             S.n_tall_by_elem[e] = tall;
+            S.n_tall_rows[e] = tall > 0 ? n_sorted[0] - k : 0;
             S.smem_rows[e] = tall < cnt ? n_sorted[tall] - k : 0;
         }
         // swap: columns outside the panel, n - nb each

@@ -29,6 +29,7 @@ struct LuStep {
     int32_t n_panel = 0;
     int32_t n_tall_by_elem[2] = {0, 0};  // active systems whose panel exceeds shared memory (float, double)
     int64_t smem_rows[2] = {0, 0};       // tallest panel of the rest (float, double)
+    int64_t n_tall_rows[2] = {0, 0};     // tallest panel of the tall ones
     int64_t swap_pfx = 0, swap_total = 0;
     int64_t trsm_pfx = 0, trsm_blocks = 0;
     int32_t n_upd = 0;
@@ -40,6 +41,7 @@ struct LuPlan {
     std::vector<LuStep> steps;
     int32_t nsys = 0;
     int64_t maxn = 0;
+    int cluster = 0;  // CTAs per cluster for tall panels (0: one-CTA global-memory panel)
     int32_t* d_act = nullptr;
     int64_t* d_pfx = nullptr;
     void release();

@@ -49,12 +49,14 @@ void* host_scratch(size_t bytes) {
     return p;
 }
 
+// Scratch for partial sums and small reductions, one buffer per (thread,
+// device): calls from different host threads (each with its own stream) never
+// share one, and a grow only has to wait for the calling thread's stream.
 int device_scratch(size_t bytes, void** out, cudaStream_t s) {
-    static std::mutex mu;
-    static std::vector<std::pair<void*, size_t>> per_dev(64, {nullptr, 0});
+    static thread_local std::vector<std::pair<void*, size_t>> per_dev(64, {nullptr, 0});
     int dev = 0;
     GB_CUDA(cudaGetDevice(&dev));
-    std::lock_guard<std::mutex> lk(mu);
+    GB_REQUIRE(dev >= 0 && dev < 64, "device index %d out of range", dev);
     auto& slot = per_dev[dev];
     if (bytes > slot.second) {
         if (slot.first) {
