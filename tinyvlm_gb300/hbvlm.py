@@ -82,8 +82,13 @@ class HBEngine:
     def _p(a):
         return ctypes.c_void_p(a.ctypes.data)
 
+    @staticmethod
+    def _colmajor(m):
+        """Buffer holding the (N x N) matrix column-major (the C ABI's layout)."""
+        return np.ascontiguousarray(np.asarray(m, np.float64).T)
+
     def prepare(self, harmonics, max_t_steps, wake_T, t_steps, times, T, Td, dft):
-        self._keep = [np.ascontiguousarray(x) for x in (wake_T, T, Td, dft)] + \
+        self._keep = [np.ascontiguousarray(x) for x in (wake_T, T, Td)] + [self._colmajor(dft)] + \
                      [np.ascontiguousarray(t_steps, np.int64), np.ascontiguousarray(times, np.float64)]
         wT, T_, Td_, D_, ts, tm = self._keep
         call("gbvlm_hbvlm_prepare", self.h, int(harmonics), int(max_t_steps), self._p(wT), self._p(ts), self._p(tm),
@@ -103,7 +108,8 @@ class HBEngine:
 
     def loads(self, x, dft, ddft, T, Td, fs, ref_a, ref_b, coupled_te, N):
         out = np.zeros(3 * N)
-        keep = [np.ascontiguousarray(a, np.float64) for a in (x, dft, ddft, T, Td, fs, ref_a)]
+        keep = [np.asfortranarray(x, np.float64), self._colmajor(dft), self._colmajor(ddft)] + \
+               [np.ascontiguousarray(a, np.float64) for a in (T, Td, fs, ref_a)]
         rb = np.ascontiguousarray(ref_b, np.float64) if ref_b is not None else None
         call("gbvlm_hbvlm_loads", self.h, *[self._p(a) for a in keep], self._p(rb) if rb is not None else None,
              1 if coupled_te else 0, self._p(out), None)
