@@ -101,6 +101,22 @@ int gbvlm_rhs_assemble_wake_influence_f64(double* rhs, int32_t nsurf, const gbvl
                                           const int32_t* lifting, int32_t iteration, double sigma,
                                           gbvlm_stream stream);
 
+/* No counterpart in the reference.  Same as
+ * gbvlm_rhs_assemble_wake_influence_f32, for callers that cannot allocate
+ * device memory (inside a stream capture, in a latency path that must not
+ * take cudaMalloc's synchronisation, or under another owner's allocator):
+ * the split-K partial sums go to a fixed 4 MiB array in this library's
+ * device image instead of scratch grown with cudaMalloc.  At most 1,048,576
+ * collocation points (all surfaces); larger problems are rejected with
+ * GBVLM_ERR_ARG.  The first call on a device looks the array up with
+ * cudaGetSymbolAddress: make it before any stream capture.  Calls share the
+ * array, so calls whose kernels overlap on the GPU race. */
+int gbvlm_rhs_assemble_wake_influence_f32_noalloc(float* rhs, int32_t nsurf, const gbvlm_dims* dims,
+                                                  const float* const* gamma_wake, const float* const* colloc,
+                                                  const float* const* normals, const float* const* verts_wake,
+                                                  const int32_t* lifting, int32_t iteration, float sigma,
+                                                  gbvlm_stream stream);
+
 /* Backend::forces_steady (vlm_backend.hpp:34/48; vlm_backend_cpu.cpp:276-297), rho = 1. */
 int gbvlm_forces_steady_f32(int64_t ns, int64_t nc, const float* verts_wing, const float* gamma_delta,
                             const float* velocities, float* forces, gbvlm_stream stream);

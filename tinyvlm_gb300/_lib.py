@@ -57,6 +57,7 @@ def _protos():
         t["gbvlm_gamma_update_" + sfx] = [I64, I64, P, P, P, P, I64, P, P, R, P]
         t["gbvlm_lu_factor_" + sfx] = [P, P, I64, I64, P]
         t["gbvlm_lu_solve_" + sfx] = [P, P, I64, I64, P, I64, I64, P]
+    t["gbvlm_rhs_assemble_wake_influence_f32_noalloc"] = [P, I32, P, PP, PP, PP, PP, P, I32, F32, P]
     t["gbvlm_lu_create"] = [P]
     t["gbvlm_lu_destroy"] = [P]
     t["gbvlm_lu_init"] = [P, I64]

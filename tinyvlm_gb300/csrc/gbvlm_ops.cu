@@ -1212,3 +1212,77 @@ GB_BOTH(DEF_TREFFTZ)
 GB_BOTH(DEF_GUPDATE)
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free variant of the float wake-influence entry point.
+//
+// Some callers cannot call cudaMalloc: code that records into a CUDA stream
+// capture (an allocation there fails the capture or synchronises the
+// device), serving loops that must keep cudaMalloc's device-wide
+// synchronisation out of their latency path, and hosts whose device memory
+// belongs to another allocator.  For them the split-K partial sums of
+// gbvlm_rhs_assemble_wake_influence_f32 live in the fixed array below
+// instead of the library's grown-on-demand scratch buffer.
+//
+// The array is GBVLM_WAKE_SCRATCH_FLOATS floats (4 MiB) in this library's
+// device image, so every GPU that loads the library holds it until the
+// process exits.  Host code cannot hand the array's name to a kernel (on the
+// host it is only a stand-in symbol), so the first call on each device looks
+// up its device address with cudaGetSymbolAddress while that device is
+// current and caches it; make that first call before any stream capture.
+// All calls share the one array and every call overwrites the part it uses
+// (each partial is written before it is read), so no contents carry over;
+// calls whose kernels overlap on the GPU (different streams, no ordering
+// between them) race on the array and must not be issued.
+// ===========================================================================
+#define GBVLM_WAKE_SCRATCH_FLOATS (1 << 20)
+
+static __device__ __align__(256) float g_wake_scratch[GBVLM_WAKE_SCRATCH_FLOATS];
+
+static float* wake_scratch_address(int* rc) {
+    static std::mutex mu;
+    static float* addr[64] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *rc = cuda_fail(e, "cudaGetDevice", __FILE__, __LINE__);
+        return nullptr;
+    }
+    if (dev < 0 || dev >= 64) {
+        set_error("device index %d out of range", dev);
+        *rc = GBVLM_ERR_ARG;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_wake_scratch);
+        if (e != cudaSuccess) {
+            *rc = cuda_fail(e, "cudaGetSymbolAddress(g_wake_scratch)", __FILE__, __LINE__);
+            return nullptr;
+        }
+        addr[dev] = (float*)p;
+    }
+    *rc = GBVLM_OK;
+    return addr[dev];
+}
+
+extern "C" int gbvlm_rhs_assemble_wake_influence_f32_noalloc(
+    float* rhs, int32_t nsurf, const gbvlm_dims* dims, const float* const* gamma_wake, const float* const* colloc,
+    const float* const* normals, const float* const* verts_wake, const int32_t* lifting, int32_t iteration,
+    float sigma, gbvlm_stream stream) {
+    GB_REQUIRE(colloc && normals && dims, "null surface array");
+    GB_REQUIRE(nsurf >= 1 && nsurf <= GBVLM_MAX_SURFACES, "nsurf=%d outside [1, %d]", nsurf, GBVLM_MAX_SURFACES);
+    int64_t ntg = 0;
+    for (int m = 0; m < nsurf; m++) ntg += dims[m].ns * dims[m].nc;
+    GB_REQUIRE(ntg <= GBVLM_WAKE_SCRATCH_FLOATS,
+               "%lld collocation points exceed the %d-float fixed scratch of the allocation-free entry point",
+               (long long)ntg, GBVLM_WAKE_SCRATCH_FLOATS);
+    int rc = GBVLM_OK;
+    float* scratch = wake_scratch_address(&rc);
+    if (!scratch) return rc;
+    // wake_influence() sizes its split-K slices from the problem and rejects a
+    // partial-sum table larger than the scratch it is given
+    return wake_influence<float>(rhs, nsurf, dims, gamma_wake, colloc, normals, verts_wake, lifting, iteration, sigma,
+                                 5000, scratch, GBVLM_WAKE_SCRATCH_FLOATS, to_cuda(stream));
+}
