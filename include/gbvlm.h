@@ -319,6 +319,12 @@ int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream);
  * `stream`; stage_ms[6] = geometry, assembly, rhs, LU factor, solve +
  * refinement, loads (milliseconds).  Synchronous. */
 int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream);
+/* Measurement hook, no reference counterpart: run the solve once without the
+ * graph with CUDA events around every tensor-core trailing-update launch of
+ * the LU; out[4] = total milliseconds of those launches, their number, and
+ * their algorithmic flops (2 m^2 W) and bytes (8 m^2 + 8 m W) per solve of
+ * the batch (m = trailing size, W = outer block width).  Synchronous. */
+int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream);
 /* Synchronous read-back in case/alpha order: coeffs[5*k..] = cl, cdi, cm_x,
  * cm_y, cm_z; gamma (optional, needs want_gamma) = each solve's n floats. */
 int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_stream stream);

@@ -73,6 +73,7 @@ def _protos():
     t["gbvlm_batch_run"] = [P, I32, P]
     t["gbvlm_batch_results"] = [P, P, P, P]
     t["gbvlm_batch_profile"] = [P, P, P]
+    t["gbvlm_batch_update_profile"] = [P, P, P]
     t["gbvlm_batch_launches"] = [P, P]
     t["gbvlm_uvlm_create"] = [P, I32, P, PP, P, I64, I32]
     t["gbvlm_uvlm_destroy"] = [P]

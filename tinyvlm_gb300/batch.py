@@ -102,6 +102,13 @@ class BatchSolver:
         call("gbvlm_batch_profile", self.h, ctypes.cast(ms, P), self._s(stream))
         return dict(zip(STAGES, list(ms)))
 
+    def update_profile(self, stream=None):
+        """CUDA-event time of the LU's tensor-core trailing-update launches in
+        one eager run, with their algorithmic flops and bytes."""
+        out = (ctypes.c_double * 4)()
+        call("gbvlm_batch_update_profile", self.h, ctypes.cast(out, P), self._s(stream))
+        return {"ms": out[0], "launches": int(out[1]), "flops": out[2], "bytes": out[3]}
+
 
 def smoke_check():
     """Tiny batch through the C ABI checked against the oracle (used by smoke())."""

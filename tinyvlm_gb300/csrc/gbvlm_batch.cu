@@ -494,10 +494,7 @@ struct gbvlm_batch_s {
 
 static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
-    int64_t nlaunch = 0;
-    for (const LuStep& S : h->plan.steps)
-        nlaunch += (S.n_tall_by_elem[0] > 0) + (S.n_panel > S.n_tall_by_elem[0]) + (S.swap_total > 0) +
-                   (S.trsm_blocks > 0) + (S.upd_blocks > 0);
+    const int64_t nlaunch = lu_plan_launches(h->plan, 4);
     int32_t mr = 0;
     for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
     const int64_t solves = (mr + 7) / 8;
@@ -898,6 +895,33 @@ int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream) {
     return rc;
 }
 
+int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream) {
+    GB_REQUIRE(h && out, "null argument");
+    cudaStream_t st = to_cuda(stream);
+    std::vector<cudaEvent_t> ev;
+    h->plan.tc_events = &ev;
+    int rc = batch_enqueue(h, st);
+    h->plan.tc_events = nullptr;
+    double ms = 0;
+    if (rc == GBVLM_OK) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+        for (size_t k = 0; k + 1 < ev.size() && rc == GBVLM_OK; k += 2) {
+            float t = 0;
+            e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventElapsedTime", __FILE__, __LINE__);
+            ms += t;
+        }
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
+    out[0] = ms;
+    out[1] = (double)(ev.size() / 2);
+    out[2] = h->plan.tc_flops;
+    out[3] = h->plan.tc_bytes;
+    return GBVLM_OK;
+}
+
 int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_stream stream) {
     GB_REQUIRE(h && coeffs, "null argument");
     cudaStream_t st = to_cuda(stream);
@@ -910,6 +934,8 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
         GB_CUDA(cudaMemcpyAsync(gt.data(), h->d_gamma, sizeof(float) * gt.size(), cudaMemcpyDeviceToHost, st));
     }
     GB_CUDA(cudaStreamSynchronize(st));
+    int rc = lu_plan_check(h->plan, st);
+    if (rc) return rc;
     int32_t* info = (int32_t*)host_scratch(sizeof(int32_t) * h->nsys);
     GB_CUDA(cudaMemcpy(info, h->lub.info, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost));
     for (int k = 0; k < h->nsys; k++) {

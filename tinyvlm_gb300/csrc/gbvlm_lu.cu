@@ -17,17 +17,23 @@
 //            systems through a per-step prefix table
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
+#include <float.h>
+#include <limits.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "gbvlm_internal.h"
 #include "gbvlm_lu.h"
+#include "gbvlm_tc.cuh"
 
 namespace gbvlm {
 
 constexpr int PANEL_THREADS = 512;
+constexpr int PR_THREADS_F64 = 256;  // register panel, double: 32 doubles of panel per thread
 constexpr int TRSM_COLS = 128;
 constexpr int GT = 64;  // update tile edge
 constexpr int GK = LU_NB;
@@ -36,6 +42,29 @@ constexpr int TS_SMEM_BYTES = 200 * 1024;
 
 template <class T>
 __device__ __forceinline__ T tabs(T x) { return x < (T)0 ? -x : x; }
+
+// Element-wise copy of `total` elements (ld_(e) -> st_(e, v)) by `nthreads`
+// threads with U loads in flight per thread before the first store.  Written
+// as load-then-store per element, the compiler may not move a global load
+// above the previous store (it cannot prove they do not alias), which leaves
+// one memory round trip per element.
+template <int U, class LD, class ST>
+__device__ __forceinline__ void staged_copy(int64_t total, int tid, int nthreads, LD ld_, ST st_) {
+    using V = decltype(ld_((int64_t)0));
+    for (int64_t e0 = tid; e0 < total; e0 += (int64_t)nthreads * U) {
+        V v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t e = e0 + (int64_t)u * nthreads;
+            v[u] = e < total ? ld_(e) : V(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t e = e0 + (int64_t)u * nthreads;
+            if (e < total) st_(e, v[u]);
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------
 // panel: CTA b handles system act[b]
@@ -105,178 +134,196 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(LuBatch<T> B, int64_t k
     }
 }
 
-// Same panel factorisation with the panel (rows k..n-1, nb columns) staged in
-// shared memory, column-major with leading dimension `rows`.  Used when the
-// panel fits (PANEL_SMEM_ROWS rows); the panel is read once and written once.
-constexpr int PANEL_SMEM_BYTES = 220 * 1024;
+// Panel factorisation with the panel held in registers.  The panel (rows
+// k..n-1, nb <= GK columns) is split over `csize` CTAs of a thread-block
+// cluster (csize = 1: one CTA), CTA q owning rows [q*slab, (q+1)*slab) with
+// slab <= NT; thread t owns row q*slab + t and keeps its nb columns in
+// registers.
+//
+// Rows are never moved during the factorisation.  Each row carries its
+// logical position (LAPACK's row order after the interchanges so far); the
+// interchange jj <-> p only swaps two logical positions, and every row is
+// written to its final logical position at the end.  Rows whose logical
+// position is below jj are finished (pivot rows = rows of U).
+//
+// Per column jj, one CTA barrier (plus one cluster barrier when csize > 1):
+//   1. each warp reduces its candidates (largest |a|, smallest logical
+//      position on ties, like LAPACK i?amax) with redux.sync; the winning
+//      lane publishes its whole row in shared memory;
+//   2. barrier; every warp reduces the warp candidates of its CTA (and, in a
+//      cluster, the CTA candidates read over DSMEM) and loads the pivot row,
+//      lane t holding column t;
+//   3. each active row is scaled and updated with the pivot row taken from
+//      lane shuffles; the candidate for column jj+1 comes out of the same
+//      pass.
+// Candidate slots and published rows are double-buffered on jj, so a slot is
+// rewritten only after every reader has passed the next barrier.
+template <class T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4_16a; };
 
-template <class T>
-__global__ void __launch_bounds__(PANEL_THREADS) k_panel_smem(LuBatch<T> B, int64_t k, const int32_t* act) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* P = reinterpret_cast<T*>(smem_raw);
-    const int32_t sid = act[blockIdx.x];
-    const int64_t n = B.n[sid], ld = B.ld[sid];
-    T* A = B.A[sid];
-    int32_t* ipiv = B.ipiv[sid];
-    const int nb = (int)min((int64_t)GK, n - k);
-    const int rows = (int)(n - k);
-    __shared__ T s_val[PANEL_THREADS / 32];
-    __shared__ int s_idx[PANEL_THREADS / 32];
-    __shared__ int s_piv;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int t = 0; t < nb; t++)
-        for (int r = tid; r < rows; r += PANEL_THREADS) P[t * rows + r] = A[(k + r) + (k + t) * ld];
-    __syncthreads();
-    for (int jj = 0; jj < nb; jj++) {
-        T* c = P + jj * rows;
-        T best = (T)-1;
-        int bi = jj;
-        for (int r = jj + tid; r < rows; r += PANEL_THREADS) {
-            T v = tabs(c[r]);
-            if (v > best) { best = v; bi = r; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            T ov = __shfl_down_sync(0xffffffffu, best, o);
-            int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
-        __syncthreads();
-        if (tid == 0) {
-            T bv = s_val[0];
-            int bix = s_idx[0];
-            for (int w = 1; w < PANEL_THREADS / 32; w++) {
-                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bix)) { bv = s_val[w]; bix = s_idx[w]; }
-            }
-            s_piv = bix;
-            ipiv[k + jj] = (int32_t)(k + bix);
-            if (c[bix] == (T)0 && B.info[sid] == 0) B.info[sid] = (int32_t)(k + jj + 1);
-        }
-        __syncthreads();
-        const int p = s_piv;
-        if (p != jj) {
-            for (int t = tid; t < nb; t += PANEL_THREADS) {
-                T tmp = P[t * rows + jj];
-                P[t * rows + jj] = P[t * rows + p];
-                P[t * rows + p] = tmp;
-            }
-        }
-        __syncthreads();
-        const T d = c[jj];
-        const T inv = (d != (T)0) ? (T)1 / d : (T)0;
-        for (int r = jj + 1 + tid; r < rows; r += PANEL_THREADS) {
-            const T l = (d != (T)0) ? c[r] / d : c[r];
-            c[r] = l;
-            for (int t = jj + 1; t < nb; t++) P[t * rows + r] -= l * P[t * rows + jj];
-        }
-        (void)inv;
-        __syncthreads();
+// Pivot candidates as unsigned keys compared lexicographically, so a warp
+// picks its winner with redux.sync max: first the magnitude (IEEE bits of |a|
+// plus one, order-preserving for non-negative numbers; NaN -> 0 ranks below
+// every number; 0 -> no candidate), then the inverted logical position
+// (largest |a|, then smallest position, like LAPACK i?amax).
+template <class T> struct PivKey;
+template <> struct PivKey<float> {
+    uint32_t m, l;
+    __device__ __forceinline__ static PivKey make(float x, int lid) {
+        const float a = fabsf(x);
+        return {a == a ? __float_as_uint(a) + 1u : 0u, ~(uint32_t)lid};
     }
-    for (int t = 0; t < nb; t++)
-        for (int r = tid; r < rows; r += PANEL_THREADS) A[(k + r) + (k + t) * ld] = P[t * rows + r];
+    __device__ __forceinline__ static PivKey none() { return {0u, 0u}; }
+    // warp-wide maximum, every lane gets it
+    __device__ __forceinline__ PivKey warp_max() const {
+        const uint32_t mm = __reduce_max_sync(0xffffffffu, m);
+        const uint32_t ll = __reduce_max_sync(0xffffffffu, m == mm ? l : 0u);
+        return {mm, ll};
+    }
+    __device__ __forceinline__ bool operator==(const PivKey& o) const { return m == o.m && l == o.l; }
+    __device__ __forceinline__ int pos() const { return (int)~l; }
+};
+template <> struct PivKey<double> {
+    uint32_t m, m2, l;
+    __device__ __forceinline__ static PivKey make(double x, int lid) {
+        const double a = fabs(x);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+        return a == a ? PivKey{(uint32_t)(b >> 32) + 1u, (uint32_t)b, ~(uint32_t)lid} : PivKey{0u, 0u, ~(uint32_t)lid};
+    }
+    __device__ __forceinline__ static PivKey none() { return {0u, 0u, 0u}; }
+    __device__ __forceinline__ PivKey warp_max() const {
+        const uint32_t mm = __reduce_max_sync(0xffffffffu, m);
+        const uint32_t mm2 = __reduce_max_sync(0xffffffffu, m == mm ? m2 : 0u);
+        const uint32_t ll = __reduce_max_sync(0xffffffffu, (m == mm && m2 == mm2) ? l : 0u);
+        return {mm, mm2, ll};
+    }
+    __device__ __forceinline__ bool operator==(const PivKey& o) const { return m == o.m && m2 == o.m2 && l == o.l; }
+    __device__ __forceinline__ int pos() const { return (int)~l; }
+};
+
+// compile-time loop: f(integral_constant<int, I>) for I in [B, E)
+template <int B, int E, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
 }
 
-// Tall panels: a thread-block cluster of `csize` CTAs holds the panel in its
-// distributed shared memory, CTA q owning rows [q*slab, (q+1)*slab) of it.
-// Per column: local arg-max, cluster barrier, every CTA reads the csize
-// candidates over DSMEM and picks the same pivot (largest |a|, first row on
-// ties); the CTA owning the diagonal row swaps it with the pivot row across
-// the panel over DSMEM; after a second barrier every CTA copies the pivot row
-// and updates its own rows.  All remote accesses finish before the final
-// barrier, so no CTA exits while another still reads its shared memory.
-constexpr int PC_THREADS = 512;
-
-template <class T>
-__global__ void __launch_bounds__(PC_THREADS) k_panel_cluster(LuBatch<T> B, int64_t k, const int32_t* act, int slab) {
+template <class T, int NT, bool CLUSTER>
+__global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab) {
     namespace cg = cooperative_groups;
-    cg::cluster_group cl = cg::this_cluster();
-    const int csize = (int)cl.num_blocks();
-    const int rank = (int)cl.block_rank();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* P = reinterpret_cast<T*>(smem_raw);  // [nb][slab]
-    __shared__ T cand_v;
-    __shared__ int cand_i;
-    __shared__ T prow[GK];
-    __shared__ T s_val[PC_THREADS / 32];
-    __shared__ int s_idx[PC_THREADS / 32];
-    __shared__ int s_piv;
+    constexpr int NW = NT / 32;
+    using Key = PivKey<T>;
+    __shared__ __align__(16) T s_row[2][NW][GK];  // each warp's candidate row
+    __shared__ Key s_key[2][NW];
+    __shared__ Key c_key[2];  // this CTA's candidate (read by the cluster)
+    __shared__ int c_w[2];
+    int csize = 1, rank = 0;
+    if constexpr (CLUSTER) {
+        csize = (int)cg::this_cluster().num_blocks();
+        rank = (int)cg::this_cluster().block_rank();
+    }
     const int32_t sid = act[blockIdx.x / csize];
     const int64_t n = B.n[sid], ld = B.ld[sid];
     T* A = B.A[sid];
     int32_t* ipiv = B.ipiv[sid];
+    int zero_col = -1;  // first exactly zero pivot of this panel (thread 0 of rank 0)
     const int nb = (int)min((int64_t)GK, n - k);
     const int rows = (int)(n - k);
-    const int r0 = rank * slab, r1 = min(rows, r0 + slab);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int t = 0; t < nb; t++)
-        for (int r = r0 + tid; r < r1; r += PC_THREADS) P[t * slab + (r - r0)] = A[(k + r) + (k + t) * ld];
-    cl.sync();
-    for (int jj = 0; jj < nb; jj++) {
-        T best = (T)-1;
-        int bi = rows;
-        for (int r = max(r0, jj) + tid; r < r1; r += PC_THREADS) {
-            const T v = tabs(P[jj * slab + (r - r0)]);
-            if (v > best) { best = v; bi = r; }
-        }
+    const int r = rank * slab + tid;
+    int lid = (tid < slab && r < rows) ? r : -1;  // logical position of the own row, -1: no row
+
+    T x[GK];
+    {
+        const T* src = A + (k + r) + k * ld;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const T ov = __shfl_down_sync(0xffffffffu, best, o);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
-        __syncthreads();
-        if (tid == 0) {
-            T bv = s_val[0];
-            int bix = s_idx[0];
-            for (int w = 1; w < PC_THREADS / 32; w++)
-                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bix)) { bv = s_val[w]; bix = s_idx[w]; }
-            cand_v = bv;
-            cand_i = bix;
-        }
-        cl.sync();
-        if (tid == 0) {
-            T bv = (T)-1;
-            int bix = rows;
-            for (int q = 0; q < csize; q++) {
-                const T v = *cl.map_shared_rank(&cand_v, q);
-                const int i = *cl.map_shared_rank(&cand_i, q);
-                if (v > bv || (v == bv && i < bix)) { bv = v; bix = i; }
-            }
-            s_piv = bix;
-            if (rank == 0) {
-                ipiv[k + jj] = (int32_t)(k + bix);
-                if (bv == (T)0 && B.info[sid] == 0) B.info[sid] = (int32_t)(k + jj + 1);
-            }
-        }
-        __syncthreads();
-        const int p = s_piv;
-        const int owner_j = jj / slab, owner_p = p / slab;
-        if (p != jj && rank == owner_j) {
-            T* Pp = cl.map_shared_rank(P, owner_p);
-            for (int t = tid; t < nb; t += PC_THREADS) {
-                const T a = P[t * slab + (jj - r0)];
-                const T b = Pp[t * slab + (p - owner_p * slab)];
-                P[t * slab + (jj - r0)] = b;
-                Pp[t * slab + (p - owner_p * slab)] = a;
-            }
-        }
-        cl.sync();
-        const T* Pj = cl.map_shared_rank(P, owner_j);
-        for (int t = tid; t < nb; t += PC_THREADS) prow[t] = Pj[t * slab + (jj - owner_j * slab)];
-        __syncthreads();
-        const T d = prow[jj];
-        for (int r = max(r0, jj + 1) + tid; r < r1; r += PC_THREADS) {
-            T l = P[jj * slab + (r - r0)];
-            if (d != (T)0) l = l / d;
-            P[jj * slab + (r - r0)] = l;
-            for (int t = jj + 1; t < nb; t++) P[t * slab + (r - r0)] -= l * prow[t];
-        }
+        for (int t = 0; t < GK; t++) x[t] = (lid >= 0 && t < nb) ? src[t * ld] : (T)0;
     }
-    cl.sync();
-    for (int t = 0; t < nb; t++)
-        for (int r = r0 + tid; r < r1; r += PC_THREADS) A[(k + r) + (k + t) * ld] = P[t * slab + (r - r0)];
+    Key cand = lid >= 0 ? Key::make(x[0], lid) : Key::none();  // candidate for column 0
+
+    static_for<0, GK>([&](auto JJ) {
+        constexpr int jj = decltype(JJ)::value;
+        if (jj < nb) {
+            const int buf = jj & 1;
+            // 1. warp candidate; its owner publishes the row
+            {
+                const Key w = cand.warp_max();
+                if (lid >= 0 && cand == w) {
+                    using V2 = typename Vec4<T>::type;
+#pragma unroll
+                    for (int t = 0; t < GK; t += 4) {
+                        V2 v;
+                        v.x = x[t];
+                        v.y = x[t + 1];
+                        v.z = x[t + 2];
+                        v.w = x[t + 3];
+                        *reinterpret_cast<V2*>(&s_row[buf][wid][t]) = v;
+                    }
+                }
+                if (lane == 0) s_key[buf][wid] = w;
+            }
+            __syncthreads();
+            // 2. pivot: (p, row) known to every warp
+            T urow;  // lane t: column t of the pivot row
+            int p;
+            {
+                const Key mine = lane < NW ? s_key[buf][lane] : Key::none();
+                const Key best = mine.warp_max();
+                const int w = __ffs(__ballot_sync(0xffffffffu, lane < NW && mine == best)) - 1;
+                if constexpr (CLUSTER) {
+                    cg::cluster_group cl = cg::this_cluster();
+                    if (tid == 0) {
+                        c_key[buf] = best;
+                        c_w[buf] = w;
+                    }
+                    cl.sync();
+                    const Key ck = lane < csize ? *cl.map_shared_rank(&c_key[buf], lane) : Key::none();
+                    const Key cbest = ck.warp_max();
+                    const int q = __ffs(__ballot_sync(0xffffffffu, lane < csize && ck == cbest)) - 1;
+                    const int wq = *cl.map_shared_rank(&c_w[buf], q);
+                    p = cbest.pos();
+                    urow = *cl.map_shared_rank(&s_row[buf][wq][lane], q);
+                } else {
+                    p = best.pos();
+                    urow = s_row[buf][w][lane];
+                }
+            }
+            const T d = __shfl_sync(0xffffffffu, urow, jj);
+            if (tid == 0 && rank == 0) {
+                ipiv[k + jj] = (int32_t)(k + p);  // a store: nothing waits on it
+                if (d == (T)0 && zero_col < 0) zero_col = jj;
+            }
+            // 3. interchange of logical positions jj <-> p, then scale and update
+            if (lid == p) lid = jj;
+            else if (lid == jj) lid = p;
+            const bool active = lid > jj;
+            // scale by the reciprocal of the pivot (LAPACK ?getf2), dividing when it is subnormal
+            T lm = x[jj];
+            if (active) {
+                if (tabs(d) >= (sizeof(T) == 4 ? (T)FLT_MIN : (T)DBL_MIN)) lm = lm * ((T)1 / d);
+                else if (d != (T)0) lm = lm / d;
+                x[jj] = lm;
+            }
+#pragma unroll
+            for (int t = jj + 1; t < GK; t++) {
+                const T u = __shfl_sync(0xffffffffu, urow, t);
+                if (active) x[t] -= lm * u;
+            }
+            if constexpr (jj + 1 < GK) cand = active ? Key::make(x[jj + 1], lid) : Key::none();
+        }
+    });
+    if constexpr (CLUSTER) cg::this_cluster().sync();  // no CTA leaves while its rows may still be read
+    // panels of a system run in order, so the first zero pivot recorded is the first of the factorisation
+    if (zero_col >= 0) atomicCAS(&B.info[sid], 0, (int32_t)(k + zero_col + 1));
+    if (lid >= 0) {
+        T* dst = A + (k + lid) + k * ld;
+#pragma unroll
+        for (int t = 0; t < GK; t++)
+            if (t < nb) dst[t * ld] = x[t];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -315,25 +362,52 @@ __global__ void k_swap(LuBatch<T> B, int64_t k, const int32_t* act, const int64_
     }
 }
 
+// Interchanges of rows [r_lo, min(n, r_hi)) applied to the columns
+// [a_lo, min(n, a_hi)) and [min(n, b_lo), min(n, b_hi)) of every system, one
+// thread per column (two-level blocking: inner swaps stay inside the outer
+// panel, the outer block's swaps reach the other columns in one pass).
+template <class T>
+__global__ void k_swap2(LuBatch<T> B, const int32_t* act, const int64_t* pfx, int cnt, int64_t r_lo, int64_t r_hi,
+                        int64_t a_lo, int64_t a_hi, int64_t b_lo, int64_t b_hi) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= pfx[cnt]) return;
+    const int a = find_block(pfx, cnt, g);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    const int64_t na = max((int64_t)0, min(n, a_hi) - a_lo);
+    int64_t j = g - pfx[a];
+    j = j < na ? a_lo + j : min(n, b_lo) + (j - na);
+    T* col = B.A[sid] + j * ld;
+    const int32_t* ip = B.ipiv[sid];
+    const int64_t rh = min(n, r_hi);
+    for (int64_t r = r_lo; r < rh; r++) {
+        const int64_t p = ip[r];
+        if (p != r) {
+            const T tmp = col[r];
+            col[r] = col[p];
+            col[p] = tmp;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // trsm: U12 = L11^-1 A12, one thread per column, TRSM_COLS columns per block
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(TRSM_COLS) k_trsm(LuBatch<T> B, int64_t k, const int32_t* act, const int64_t* pfx,
-                                                   int cnt) {
+                                                   int cnt, int64_t c_hi) {
     __shared__ T L[GK][GK + 1];
     const int a = find_block(pfx, cnt, blockIdx.x);
     const int32_t sid = act[a];
     const int64_t n = B.n[sid], ld = B.ld[sid];
     T* A = B.A[sid];
     const int nb = (int)min((int64_t)GK, n - k);
-    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
-        int r = t % nb, c = t / nb;
-        L[r][c] = A[(k + r) + (k + c) * ld];
-    }
+    staged_copy<8>(
+        nb * nb, threadIdx.x, blockDim.x, [&](int64_t t) { return A[(k + t % nb) + (k + t / nb) * ld]; },
+        [&](int64_t t, T v) { L[t % nb][t / nb] = v; });
     __syncthreads();
     const int64_t j = k + nb + (int64_t)(blockIdx.x - pfx[a]) * TRSM_COLS + threadIdx.x;
-    if (j >= n) return;
+    if (j >= min(n, c_hi)) return;
     T x[GK];
     T* col = A + j * ld + k;
 #pragma unroll
@@ -353,16 +427,113 @@ __global__ void __launch_bounds__(TRSM_COLS) k_trsm(LuBatch<T> B, int64_t k, con
 }
 
 // ---------------------------------------------------------------------------
+// two-level blocking, end of an outer block [k0, k0 + WW): U12 = L11^-1 A12
+// for the columns right of the block, L11 the WW x WW unit lower triangle.
+// One CTA per TW_COLS columns: L11 and the columns in shared memory, solved
+// in 32-row blocks:
+//   * diagonal block: a warp per column, a lane per row holding its row of
+//     the 32 x 32 block in registers, four columns in flight per warp;
+//   * rows below: thread (column j, row group g) keeps the 32 solved values
+//     of column j in registers and sweeps rows g, g+4, ... with the L rows
+//     read as float4 broadcasts.
+// ---------------------------------------------------------------------------
+constexpr int TW_COLS = 64;
+constexpr int TW_LS = LU_OUTER + 4;  // L row stride (float4-aligned rows)
+constexpr int TW_XS = TW_COLS + 1;   // X row stride (odd: conflict-free columns)
+
+template <int WW>
+constexpr size_t trsm_wide_smem() { return sizeof(float) * ((size_t)WW * TW_LS + (size_t)WW * TW_XS); }
+
+template <int WW>
+__global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t k0, const int32_t* act,
+                                                     const int64_t* pfx, int cnt) {
+    static_assert(WW == LU_OUTER, "row stride sized for the outer block");
+    extern __shared__ __align__(16) float tw_smem[];
+    float* L = tw_smem;            // L[r * TW_LS + c]
+    float* X = L + WW * TW_LS;     // X[r * TW_XS + j]
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    float* A = B.A[sid];
+    const int64_t c0 = k0 + WW + (int64_t)(blockIdx.x - pfx[a]) * TW_COLS;  // systems here have n > k0 + WW
+    const int ncols = (int)min((int64_t)TW_COLS, n - c0);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const float* Ab = A + k0 + k0 * ld;
+    staged_copy<16>(
+        WW * WW, tid, 256, [&](int64_t e) { return Ab[(int)(e & (WW - 1)) + (e >> 7) * ld]; },
+        [&](int64_t e, float v) { L[(int)(e & (WW - 1)) * TW_LS + (int)(e >> 7)] = v; });
+    const float* Xb = A + k0 + c0 * ld;
+    staged_copy<16>(
+        WW * TW_COLS, tid, 256,
+        [&](int64_t e) { return (int)(e >> 7) < ncols ? Xb[(int)(e & (WW - 1)) + (e >> 7) * ld] : 0.f; },
+        [&](int64_t e, float v) { X[(int)(e & (WW - 1)) * TW_XS + (int)(e >> 7)] = v; });
+    __syncthreads();
+#pragma unroll 1
+    for (int b = 0; b < WW / 32; b++) {
+        const int rb = 32 * b;
+        // diagonal block
+        {
+            float lrow[32];
+#pragma unroll
+            for (int l = 0; l < 32; l++) lrow[l] = L[(rb + lane) * TW_LS + rb + l];
+#pragma unroll 1
+            for (int j0 = 4 * wid; j0 < TW_COLS; j0 += 32) {
+                float x[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) x[c] = X[(rb + lane) * TW_XS + j0 + c];
+#pragma unroll
+                for (int l = 0; l < 32; l++) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const float xl = __shfl_sync(0xffffffffu, x[c], l);
+                        if (lane > l) x[c] -= lrow[l] * xl;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 4; c++) X[(rb + lane) * TW_XS + j0 + c] = x[c];
+            }
+        }
+        __syncthreads();
+        // rows below the block
+        if (rb + 32 < WW) {
+            const int j = tid & (TW_COLS - 1), g = tid >> 6;
+            float xb[32];
+#pragma unroll
+            for (int l = 0; l < 32; l++) xb[l] = X[(rb + l) * TW_XS + j];
+#pragma unroll 1
+            for (int r = rb + 32 + g; r < WW; r += 4) {
+                const float4* lr = reinterpret_cast<const float4*>(L + r * TW_LS + rb);
+                float acc = 0.f;
+#pragma unroll
+                for (int m = 0; m < 8; m++) {
+                    const float4 v = lr[m];
+                    acc += v.x * xb[4 * m] + v.y * xb[4 * m + 1] + v.z * xb[4 * m + 2] + v.w * xb[4 * m + 3];
+                }
+                X[r * TW_XS + j] -= acc;
+            }
+        }
+        __syncthreads();
+    }
+    float* Xo = A + k0 + c0 * ld;
+    for (int e = tid; e < WW * TW_COLS; e += 256) {
+        const int r = e & (WW - 1), j = e >> 7;
+        if (j < ncols) Xo[r + (int64_t)j * ld] = X[r * TW_XS + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // update: A22 -= L21 * U12 on 64x64 tiles, 256 threads, each a 4x4 block of
 // consecutive rows/columns read from shared memory as vectors
 // ---------------------------------------------------------------------------
-template <class T> struct Vec4;
-template <> struct Vec4<float> { using type = float4; };
-template <> struct Vec4<double> { using type = double4; };
 
+// mode 0: the whole trailing matrix, rows and columns [k+GK, n).
+// mode 1 (two-level blocking, outer block ending at column kend): only the
+// outer panel's columns [k+GK, min(n, kend)) over rows [k+GK, n); the columns
+// right of the block wait for the block's swaps, U12 solve and tensor-core
+// update.
 template <class T>
 __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const int32_t* act, const int64_t* pfx,
-                                               int cnt) {
+                                               int cnt, int64_t kend, int mode) {
     constexpr int SW = GT + 4;  // row stride keeps 16-byte alignment of every 4-run
     __shared__ __align__(16) T sA[GK][SW];  // L21 tile: [kk][row]
     __shared__ __align__(16) T sB[GK][SW];  // U12 tile: [kk][col]
@@ -370,18 +541,37 @@ __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const i
     const int32_t sid = act[a];
     const int64_t n = B.n[sid], ld = B.ld[sid];
     T* A = B.A[sid];
-    const int64_t m = n - k - GK;  // trailing size (systems here have n > k + GK)
-    const int64_t tiles = (m + GT - 1) / GT;
+    const int64_t lo = k + GK;  // systems here have n > k + GK
     const int64_t t = blockIdx.x - pfx[a];
-    const int64_t r0 = k + GK + (t % tiles) * GT, c0 = k + GK + (t / tiles) * GT;
+    int64_t r0, c0, row_hi = n, col_hi = n;
+    if (mode == 0) {
+        const int64_t tiles = (n - lo + GT - 1) / GT;
+        r0 = lo + (t % tiles) * GT;
+        c0 = lo + (t / tiles) * GT;
+    } else {
+        const int64_t ke = min(n, kend);
+        const int64_t tr = (n - lo + GT - 1) / GT;
+        r0 = lo + (t % tr) * GT;
+        c0 = lo + (t / tr) * GT;
+        col_hi = ke;
+    }
     const int tid = threadIdx.x;
-    for (int e = tid; e < GK * GT; e += 256) {
-        const int kk = e / GT, rr = e % GT;
-        const int64_t r = r0 + rr;
-        sA[kk][rr] = r < n ? A[r + (k + kk) * ld] : (T)0;
-        const int cc = e / GK, k2 = e % GK;
-        const int64_t c = c0 + cc;
-        sB[k2][cc] = c < n ? A[(k + k2) + c * ld] : (T)0;
+    {
+        constexpr int PER = GK * GT / 256;  // elements of each tile per thread
+        T va[PER], vb[PER];
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int e = tid + u * 256;
+            const int64_t r = r0 + e % GT, c = c0 + e / GK;
+            va[u] = r < row_hi ? A[r + (k + e / GT) * ld] : (T)0;
+            vb[u] = c < col_hi ? A[(k + e % GK) + c * ld] : (T)0;
+        }
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int e = tid + u * 256;
+            sA[e / GT][e % GT] = va[u];
+            sB[e % GK][e / GK] = vb[u];
+        }
     }
     __syncthreads();
     const int tx = tid & 15, ty = tid >> 4;
@@ -401,17 +591,50 @@ __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const i
 #pragma unroll
             for (int j = 0; j < 4; j++) acc[i][j] += a4[i] * b4[j];
     }
+    // all 16 loads of the output block before its stores
+    T cur[4][4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         const int64_t c = c0 + 4 * ty + j;
-        if (c >= n) continue;
-        T* col = A + c * ld;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int64_t r = r0 + 4 * tx + i;
-            if (r < n) col[r] -= acc[i][j];
+            cur[i][j] = (c < col_hi && r < row_hi) ? A[r + c * ld] : (T)0;
         }
     }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int64_t c = c0 + 4 * ty + j;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int64_t r = r0 + 4 * tx + i;
+            if (c < col_hi && r < row_hi) A[r + c * ld] = cur[i][j] - acc[i][j];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// update on the tensor cores: the same A22 -= L21 U12 on 128 x 128 tiles
+// (gbvlm_tc.cuh), tiles enumerated over all systems through a prefix table
+// ---------------------------------------------------------------------------
+template <int PASSES>
+__global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, int64_t k0, int w, const int32_t* act,
+                                                             const int64_t* pfx, int cnt, int* err) {
+    // outer update of the block [k0, k0 + w): rows and columns [k0 + w, n), K = w
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tslot;
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    float* A = B.A[sid];
+    const int64_t lo = k0 + w;  // systems here have n > k0 + w
+    const int64_t tiles = (n - lo + tc::BM - 1) / tc::BM;
+    const int64_t t = blockIdx.x - pfx[a];
+    const int64_t r0 = lo + (t % tiles) * tc::BM, c0 = lo + (t / tiles) * tc::BN;
+    tc::update_tile<PASSES>(A + r0 + k0 * ld, A + k0 + c0 * ld, A + r0 + c0 * ld, ld,
+                            (int)min((int64_t)tc::BM, n - r0), (int)min((int64_t)tc::BN, n - c0), w, tc_smem, bar,
+                            &tslot, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -461,6 +684,30 @@ __global__ void k_perm(LuBatch<T> B) {
 constexpr int TS_THREADS = 256;
 constexpr int TS_MAXRHS = 8;
 
+// acc[q] = sum_l a[l * ld] * xs[l][q] over the nb <= GK columns of a block row;
+// a full block issues all GK loads before the first use
+template <class T>
+__device__ __forceinline__ void trs_row_dot(const T* a, int64_t ld, int nb, const T (*xs)[TS_MAXRHS],
+                                            T (&acc)[TS_MAXRHS]) {
+#pragma unroll
+    for (int q = 0; q < TS_MAXRHS; q++) acc[q] = 0;
+    if (nb == GK) {
+        T v[GK];
+#pragma unroll
+        for (int l = 0; l < GK; l++) v[l] = a[l * ld];
+#pragma unroll
+        for (int l = 0; l < GK; l++)
+#pragma unroll
+            for (int q = 0; q < TS_MAXRHS; q++) acc[q] += v[l] * xs[l][q];
+    } else {
+        for (int l = 0; l < nb; l++) {
+            const T v = a[l * ld];
+#pragma unroll
+            for (int q = 0; q < TS_MAXRHS; q++) acc[q] += v * xs[l][q];
+        }
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rhs0, int32_t nrhs_blk, int use_smem) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -482,11 +729,9 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     (void)wcs;
     auto WX = [&](int64_t r, int q) -> T& { return use_smem ? W[r * TS_MAXRHS + q] : X[r + q * ldx]; };
     if (use_smem) {
-        for (int64_t e = tid; e < n * nr; e += TS_THREADS) {
-            const int64_t r = e % n;
-            const int q = (int)(e / n);
-            W[r * TS_MAXRHS + q] = X[pm[r] + q * ldx];
-        }
+        staged_copy<8>(
+            n * nr, tid, TS_THREADS, [&](int64_t e) { return X[pm[e % n] + (e / n) * ldx]; },
+            [&](int64_t e, T v) { W[(e % n) * TS_MAXRHS + e / n] = v; });
     } else {
         // gather through the double-buffer-free route: rows are permuted one
         // right-hand side at a time with the CTA's shared scratch as staging
@@ -503,10 +748,9 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     // forward: L (unit lower)
     for (int64_t k = 0; k < n; k += GK) {
         const int nb = (int)min((int64_t)GK, n - k);
-        for (int e = tid; e < nb * nb; e += TS_THREADS) {
-            const int r = e % nb, c = e / nb;
-            dg[r][c] = A[(k + r) + (k + c) * ld];
-        }
+        staged_copy<4>(
+            nb * nb, tid, TS_THREADS, [&](int64_t e) { return A[(k + e % nb) + (k + e / nb) * ld]; },
+            [&](int64_t e, T v) { dg[e % nb][e / nb] = v; });
         __syncthreads();
         if (wid < nr) {
             T x = lane < nb ? WX(k + lane, wid) : (T)0;
@@ -522,14 +766,10 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
         __syncthreads();
         for (int64_t r = k + nb + tid; r < n; r += TS_THREADS) {
             T acc[TS_MAXRHS];
+            trs_row_dot(A + r + k * ld, ld, nb, xs, acc);
 #pragma unroll
-            for (int q = 0; q < TS_MAXRHS; q++) acc[q] = 0;
-            for (int l = 0; l < nb; l++) {
-                const T a = A[r + (k + l) * ld];
-#pragma unroll
-                for (int q = 0; q < TS_MAXRHS; q++) acc[q] += a * xs[l][q];
-            }
-            for (int q = 0; q < nr; q++) WX(r, q) -= acc[q];
+            for (int q = 0; q < TS_MAXRHS; q++)
+                if (q < nr) WX(r, q) -= acc[q];
         }
         __syncthreads();
     }
@@ -538,10 +778,9 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
     for (int64_t bk = nblk - 1; bk >= 0; bk--) {
         const int64_t k = bk * GK;
         const int nb = (int)min((int64_t)GK, n - k);
-        for (int e = tid; e < nb * nb; e += TS_THREADS) {
-            const int r = e % nb, c = e / nb;
-            dg[r][c] = A[(k + r) + (k + c) * ld];
-        }
+        staged_copy<4>(
+            nb * nb, tid, TS_THREADS, [&](int64_t e) { return A[(k + e % nb) + (k + e / nb) * ld]; },
+            [&](int64_t e, T v) { dg[e % nb][e / nb] = v; });
         __syncthreads();
         if (wid < nr) {
             T x = lane < nb ? WX(k + lane, wid) : (T)0;
@@ -559,14 +798,10 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
         __syncthreads();
         for (int64_t r = tid; r < k; r += TS_THREADS) {
             T acc[TS_MAXRHS];
+            trs_row_dot(A + r + k * ld, ld, nb, xs, acc);
 #pragma unroll
-            for (int q = 0; q < TS_MAXRHS; q++) acc[q] = 0;
-            for (int l = 0; l < nb; l++) {
-                const T a = A[r + (k + l) * ld];
-#pragma unroll
-                for (int q = 0; q < TS_MAXRHS; q++) acc[q] += a * xs[l][q];
-            }
-            for (int q = 0; q < nr; q++) WX(r, q) -= acc[q];
+            for (int q = 0; q < TS_MAXRHS; q++)
+                if (q < nr) WX(r, q) -= acc[q];
         }
         __syncthreads();
     }
@@ -603,7 +838,9 @@ __global__ void __launch_bounds__(256) k_trs_diag(LuBatch<T> B, int64_t k, int u
     const int64_t n = B.n[0], ld = B.ld[0], ldx = B.ldx[0];
     const T* A = B.A[0];
     const int nb = (int)min((int64_t)GK, n - k);
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) dg[e % nb][e / nb] = A[(k + e % nb) + (k + e / nb) * ld];
+    staged_copy<4>(
+        nb * nb, threadIdx.x, blockDim.x, [&](int64_t e) { return A[(k + e % nb) + (k + e / nb) * ld]; },
+        [&](int64_t e, T v) { dg[e % nb][e / nb] = v; });
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
@@ -681,6 +918,51 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
 }
 
 // ---------------------------------------------------------------------------
+// panel launch: register panel with the thread count of the group
+// ---------------------------------------------------------------------------
+template <class T, int NT>
+static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
+    if (g.csize == 1) {
+        k_panel_reg<T, NT, false><<<g.count, NT, 0, st>>>(B, k, act, g.slab);
+        GB_LAUNCH_CHECK();
+        return GBVLM_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(g.count * g.csize));
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = g.csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true>, B, k, act, g.slab));
+    return GBVLM_OK;
+}
+
+template <class T>
+static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
+    if (g.csize == 0) {
+        k_panel<T><<<g.count, PANEL_THREADS, 0, st>>>(B, k, act);
+        GB_LAUNCH_CHECK();
+        return GBVLM_OK;
+    }
+    if constexpr (sizeof(T) == 4) {
+        switch (g.nt) {
+            case 128: return launch_panel_nt<T, 128>(B, k, act, g, st);
+            case 256: return launch_panel_nt<T, 256>(B, k, act, g, st);
+            case 512: return launch_panel_nt<T, 512>(B, k, act, g, st);
+            default: return launch_panel_nt<T, 1024>(B, k, act, g, st);
+        }
+    } else {
+        return launch_panel_nt<T, PR_THREADS_F64>(B, k, act, g, st);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host plan
 // ---------------------------------------------------------------------------
 template <class T>
@@ -688,56 +970,74 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
     for (size_t s = 0; s < plan.steps.size(); s++) {
         const LuStep& S = plan.steps[s];
         if (S.n_panel == 0) continue;
-        // systems are sorted by n descending: the ones whose panel is too tall
-        // for shared memory form a prefix of the active list
-        const int64_t max_rows = (PANEL_SMEM_BYTES / (int64_t)(GK * sizeof(T)));
-        const int n_glob = S.n_tall_by_elem[sizeof(T) == 4 ? 0 : 1];
-        (void)max_rows;
-        if (n_glob > 0) {
-            // rows of the tallest panel spread over a cluster of CTAs
-            const int64_t rows_max = S.n_tall_rows[sizeof(T) == 4 ? 0 : 1];
-            const int csize = plan.cluster;
-            const int slab = (int)cdiv(rows_max, csize);
-            const size_t smem = (size_t)slab * GK * sizeof(T);
-            if (csize >= 2 && smem <= (size_t)PANEL_SMEM_BYTES) {
-                cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3((unsigned)(n_glob * csize));
-                cfg.blockDim = dim3(PC_THREADS);
-                cfg.dynamicSmemBytes = smem;
-                cfg.stream = st;
-                cudaLaunchAttribute at[1];
-                at[0].id = cudaLaunchAttributeClusterDimension;
-                at[0].val.clusterDim.x = csize;
-                at[0].val.clusterDim.y = 1;
-                at[0].val.clusterDim.z = 1;
-                cfg.attrs = at;
-                cfg.numAttrs = 1;
-                GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_cluster<T>, B, S.k, plan.d_act + S.act_off, slab));
-            } else {
-                k_panel<T><<<n_glob, PANEL_THREADS, 0, st>>>(B, S.k, plan.d_act + S.act_off);
+        for (const PanelGroup& g : S.panels[sizeof(T) == 4 ? 0 : 1]) {
+            const int rc = launch_panel<T>(B, S.k, plan.d_act + S.act_off + g.first, g, st);
+            if (rc) return rc;
+        }
+        const bool two_level = sizeof(T) == 4 && plan.W > GK;
+        const int32_t* act = plan.d_act + S.act_off;
+        if (!two_level) {
+            if (S.swap_total > 0) {
+                k_swap<T><<<(unsigned)cdiv(S.swap_total, 256), 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.swap_pfx,
+                                                                           S.n_panel);
                 GB_LAUNCH_CHECK();
             }
+            if (S.trsm_blocks > 0) {
+                k_trsm<T><<<(unsigned)S.trsm_blocks, TRSM_COLS, 0, st>>>(B, S.k, act, plan.d_pfx + S.trsm_pfx, S.n_panel,
+                                                                       INT64_MAX);
+                GB_LAUNCH_CHECK();
+            }
+            if (S.upd_blocks > 0) {
+                k_update<T><<<(unsigned)S.upd_blocks, 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.upd_pfx, S.n_upd, 0, 0);
+                GB_LAUNCH_CHECK();
+            }
+            continue;
         }
-        if (S.n_panel > n_glob) {
-            const int64_t rows = S.smem_rows[sizeof(T) == 4 ? 0 : 1];
-            const size_t smem = (size_t)rows * GK * sizeof(T);
-            k_panel_smem<T><<<S.n_panel - n_glob, PANEL_THREADS, smem, st>>>(B, S.k, plan.d_act + S.act_off + n_glob);
+        // two-level blocking, outer block [k0, kend)
+        const int64_t k0 = S.kend - plan.W;
+        if (S.iswap_total > 0) {
+            k_swap2<T><<<(unsigned)cdiv(S.iswap_total, 256), 256, 0, st>>>(B, act, plan.d_pfx + S.iswap_pfx, S.n_panel,
+                                                                        S.k, S.k + GK, k0, S.k, S.k + GK, S.kend);
             GB_LAUNCH_CHECK();
         }
-        if (S.swap_total > 0) {
-            k_swap<T><<<(unsigned)cdiv(S.swap_total, 256), 256, 0, st>>>(B, S.k, plan.d_act + S.act_off,
-                                                                       plan.d_pfx + S.swap_pfx, S.n_panel);
+        if (S.itrsm_blocks > 0) {
+            k_trsm<T><<<(unsigned)S.itrsm_blocks, TRSM_COLS, 0, st>>>(B, S.k, act, plan.d_pfx + S.itrsm_pfx, S.n_panel,
+                                                                    S.kend);
             GB_LAUNCH_CHECK();
         }
-        if (S.trsm_blocks > 0) {
-            k_trsm<T><<<(unsigned)S.trsm_blocks, TRSM_COLS, 0, st>>>(B, S.k, plan.d_act + S.act_off,
-                                                                   plan.d_pfx + S.trsm_pfx, S.n_panel);
+        if (S.in_blocks > 0) {
+            k_update<T><<<(unsigned)S.in_blocks, 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.in_pfx, S.n_in, S.kend, 1);
             GB_LAUNCH_CHECK();
         }
-        if (S.upd_blocks > 0) {
-            k_update<T><<<(unsigned)S.upd_blocks, 256, 0, st>>>(B, S.k, plan.d_act + S.act_off + S.upd_act_skip,
-                                                              plan.d_pfx + S.upd_pfx, S.n_upd);
+        if (S.bswap_total > 0) {
+            k_swap2<T><<<(unsigned)cdiv(S.bswap_total, 256), 256, 0, st>>>(
+                B, act + S.bswap_first, plan.d_pfx + S.bswap_pfx, S.n_panel - S.bswap_first, k0, S.kend, 0, k0, S.kend,
+                INT64_MAX);
             GB_LAUNCH_CHECK();
+        }
+        if constexpr (sizeof(T) == 4) {
+            if (S.tc_blocks > 0) {
+                k_trsm_wide<LU_OUTER><<<(unsigned)S.btrsm_blocks, 256, trsm_wide_smem<LU_OUTER>(), st>>>(
+                    B, k0, act, plan.d_pfx + S.btrsm_pfx, S.n_tc);
+                GB_LAUNCH_CHECK();
+                const int64_t* pfx = plan.d_pfx + S.tc_pfx;
+                if (plan.tc_events) {
+                    cudaEvent_t e0, e1;
+                    GB_CUDA(cudaEventCreate(&e0));
+                    GB_CUDA(cudaEventCreate(&e1));
+                    plan.tc_events->push_back(e0);
+                    plan.tc_events->push_back(e1);
+                    GB_CUDA(cudaEventRecord(e0, st));
+                }
+                if (plan.tc_passes == 1)
+                    k_update_tc<1><<<(unsigned)S.tc_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(B, k0, plan.W, act, pfx,
+                                                                                             S.n_tc, plan.d_err);
+                else
+                    k_update_tc<3><<<(unsigned)S.tc_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(B, k0, plan.W, act, pfx,
+                                                                                             S.n_tc, plan.d_err);
+                GB_LAUNCH_CHECK();
+                if (plan.tc_events) GB_CUDA(cudaEventRecord(plan.tc_events->back(), st));
+            }
         }
     }
     if (plan.nsys > 0) {
@@ -772,8 +1072,6 @@ template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, in
 // active systems of every step form a prefix of the order.
 int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st) {
     plan.release();
-    GB_CUDA(cudaFuncSetAttribute(k_panel_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
-    GB_CUDA(cudaFuncSetAttribute(k_panel_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_trsolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_trsolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_perm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
@@ -782,18 +1080,42 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     GB_CUDA(cudaFuncSetAttribute(k_perm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
     plan.nsys = (int32_t)n_sorted.size();
     plan.maxn = n_sorted.empty() ? 0 : n_sorted[0];
-    // largest cluster the device schedules for the tall-panel kernel (16 needs the non-portable opt-in)
-    plan.cluster = 0;
+    plan.tc_flops = plan.tc_bytes = 0;
+    plan.tc_launches = 0;
+    // trailing update of the float factorisation: tensor cores (3xTF32) on
+    // devices with tcgen05, or as GBVLM_LU_TC asks (0: CUDA cores, 1: TF32, 3: 3xTF32)
     {
-        cudaFuncSetAttribute(k_panel_cluster<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaFuncSetAttribute(k_panel_cluster<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        GB_CUDA(cudaFuncSetAttribute(k_panel_cluster<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
-        GB_CUDA(cudaFuncSetAttribute(k_panel_cluster<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM_BYTES));
-        for (int c : {16, 8, 4}) {
+        int dev = 0, major = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+        plan.tc_passes = major >= 10 ? 3 : 0;
+        if (const char* e = getenv("GBVLM_LU_TC")) {
+            const int v = atoi(e);
+            plan.tc_passes = (v == 1 || v == 3) && major >= 10 ? v : 0;
+        }
+        plan.W = plan.tc_passes ? LU_OUTER : GK;
+        if (plan.tc_passes) {
+            GB_CUDA(cudaFuncSetAttribute(k_update_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trsm_wide_smem<LU_OUTER>()));
+        }
+        GB_CUDA(cudaMalloc(&plan.d_err, sizeof(int)));
+        GB_CUDA(cudaMemsetAsync(plan.d_err, 0, sizeof(int), st));
+    }
+    // largest cluster the device schedules for the register panel (16 needs the non-portable opt-in)
+    plan.cluster = 1;
+    {
+        cudaFuncSetAttribute(k_panel_reg<float, 1024, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 512, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 256, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 128, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<double, PR_THREADS_F64, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        for (int c : {16, 8, 4, 2}) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(c);
-            cfg.blockDim = dim3(PC_THREADS);
-            cfg.dynamicSmemBytes = PANEL_SMEM_BYTES;
+            cfg.blockDim = dim3(1024);
+            cfg.dynamicSmemBytes = 0;
             cudaLaunchAttribute at[1];
             at[0].id = cudaLaunchAttributeClusterDimension;
             at[0].val.clusterDim.x = c;
@@ -801,8 +1123,11 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             at[0].val.clusterDim.z = 1;
             cfg.attrs = at;
             cfg.numAttrs = 1;
-            int nclusters = 0;
-            if (cudaOccupancyMaxActiveClusters(&nclusters, k_panel_cluster<float>, &cfg) == cudaSuccess && nclusters > 0) {
+            int n2 = 0, n1 = 0;
+            const bool ok2 = cudaOccupancyMaxActiveClusters(&n2, k_panel_reg<float, 1024, true>, &cfg) == cudaSuccess;
+            cfg.blockDim = dim3(PR_THREADS_F64);
+            const bool ok1 = cudaOccupancyMaxActiveClusters(&n1, k_panel_reg<double, PR_THREADS_F64, true>, &cfg) == cudaSuccess;
+            if (ok2 && ok1 && n2 > 0 && n1 > 0) {
                 plan.cluster = c;
                 break;
             }
@@ -823,13 +1148,31 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         for (int i = 0; i < cnt; i++) act.push_back(i);
         S.n_panel = cnt;
         for (int e = 0; e < 2; e++) {
-            const int64_t es = e == 0 ? 4 : 8;
-            const int64_t lim = PANEL_SMEM_BYTES / (GK * es);
-            int tall = 0;
-            while (tall < cnt && n_sorted[tall] - k > lim) tall++;
-            S.n_tall_by_elem[e] = tall;
-            S.n_tall_rows[e] = tall > 0 ? n_sorted[0] - k : 0;
-            S.smem_rows[e] = tall < cnt ? n_sorted[tall] - k : 0;
+            // rows per CTA = threads per CTA (one row per thread; 32 doubles per thread cap the f64 CTA at 256)
+            const int64_t slab_max = e == 0 ? 1024 : PR_THREADS_F64;
+            S.panels[e].clear();
+            int i = 0;
+            while (i < cnt) {
+                const int64_t rows = n_sorted[i] - k;
+                int cs = 1;
+                while ((int64_t)cs * slab_max < rows) cs *= 2;
+                PanelGroup g;
+                g.first = i;
+                int j = i;
+                if (cs > plan.cluster) {
+                    g.csize = 0;  // too tall for the largest cluster
+                    while (j < cnt && n_sorted[j] - k > (int64_t)plan.cluster * slab_max) j++;
+                } else {
+                    g.csize = cs;
+                    g.slab = (int)cdiv(rows, cs);
+                    g.nt = e == 0 ? 128 : PR_THREADS_F64;
+                    while (g.nt < g.slab) g.nt *= 2;
+                    while (j < cnt && n_sorted[j] - k > (int64_t)(cs / 2) * slab_max) j++;
+                }
+                g.count = j - i;
+                S.panels[e].push_back(g);
+                i = j;
+            }
         }
         // swap: columns outside the panel, n - nb each
         S.swap_pfx = (int64_t)pfx.size();
@@ -864,6 +1207,82 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         }
         pfx.push_back(acc);
         S.upd_blocks = acc;
+        // two-level blocking (float, tensor cores): outer block [k0, kend) of W columns
+        S.kend = (k / plan.W + 1) * plan.W;
+        const int64_t k0 = S.kend - plan.W;
+        // inner swap: columns [k0, k) and [k + GK, kend) of the outer panel
+        S.iswap_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < cnt; i++) {
+            pfx.push_back(acc);
+            const int64_t n = n_sorted[i];
+            acc += (k - k0) + std::max<int64_t>(0, std::min(n, S.kend) - std::min(n, k + GK));
+        }
+        pfx.push_back(acc);
+        S.iswap_total = acc;
+        // inner trsm: columns [k + nb, min(n, kend))
+        S.itrsm_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < cnt; i++) {
+            pfx.push_back(acc);
+            const int64_t m = std::min(n_sorted[i], S.kend) - k - std::min<int64_t>(GK, n_sorted[i] - k);
+            acc += m > 0 ? cdiv(m, TRSM_COLS) : 0;
+        }
+        pfx.push_back(acc);
+        S.itrsm_blocks = acc;
+        // inner update: rows [k + GK, n) x columns [k + GK, min(n, kend))
+        S.in_pfx = (int64_t)pfx.size();
+        acc = 0;
+        int ci = 0;
+        for (int i = 0; i < cu; i++) {
+            const int64_t ke = std::min<int64_t>(n_sorted[i], S.kend);
+            if (ke <= k + GK) break;  // a suffix of the sorted systems
+            pfx.push_back(acc);
+            acc += cdiv(n_sorted[i] - k - GK, GT) * cdiv(ke - k - GK, GT);
+            ci++;
+        }
+        pfx.push_back(acc);
+        S.n_in = ci;
+        S.in_blocks = acc;
+        // end of the outer block for the systems whose last step in it is this one:
+        // all active systems at the block's last step, else those with n <= k + GK
+        const bool block_end = k + GK == S.kend;
+        S.bswap_first = block_end ? 0 : cu;
+        S.bswap_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = S.bswap_first; i < cnt; i++) {
+            pfx.push_back(acc);
+            const int64_t n = n_sorted[i];
+            acc += k0 + (n - std::min(n, S.kend));
+        }
+        pfx.push_back(acc);
+        S.bswap_total = acc;
+        // U12 solve and tensor-core update: systems with n > kend, at the block's last step
+        ci = 0;
+        if (block_end)
+            while (ci < nsys && n_sorted[ci] > S.kend) ci++;
+        S.n_tc = ci;
+        S.btrsm_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < ci; i++) {
+            pfx.push_back(acc);
+            acc += cdiv(n_sorted[i] - S.kend, TW_COLS);
+        }
+        pfx.push_back(acc);
+        S.btrsm_blocks = acc;
+        S.tc_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < ci; i++) {
+            pfx.push_back(acc);
+            const int64_t m = n_sorted[i] - S.kend;
+            const int64_t t = cdiv(m, tc::BM);
+            acc += t * t;
+            plan.tc_flops += 2.0 * (double)m * (double)m * plan.W;
+            plan.tc_bytes += 8.0 * (double)m * (double)m + 8.0 * (double)m * plan.W;
+        }
+        pfx.push_back(acc);
+        S.tc_blocks = acc;
+        plan.tc_launches += acc > 0;
         plan.steps.push_back(S);
     }
     if (!act.empty()) {
@@ -878,11 +1297,42 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     return GBVLM_OK;
 }
 
+int lu_plan_check(const LuPlan& plan, cudaStream_t st) {
+    if (!plan.d_err) return GBVLM_OK;
+    int* h = (int*)host_scratch(sizeof(int));
+    GB_CUDA(cudaMemcpyAsync(h, plan.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (*h != 0) {
+        set_error("LU: a tensor-core update tile timed out waiting for its MMAs");
+        return GBVLM_ERR_CUDA;
+    }
+    return GBVLM_OK;
+}
+
+int64_t lu_plan_launches(const LuPlan& plan, int es) {
+    const int e = es == 4 ? 0 : 1;
+    const bool two_level = es == 4 && plan.W > GK;
+    int64_t n = 0;
+    for (const LuStep& S : plan.steps) {
+        if (S.n_panel == 0) continue;
+        n += (int64_t)S.panels[e].size();
+        if (!two_level) {
+            n += (S.swap_total > 0) + (S.trsm_blocks > 0) + (S.upd_blocks > 0);
+        } else {
+            n += (S.iswap_total > 0) + (S.itrsm_blocks > 0) + (S.in_blocks > 0) + (S.bswap_total > 0) +
+                 2 * (S.tc_blocks > 0);
+        }
+    }
+    return n + (plan.nsys > 0);  // + the permutation kernel
+}
+
 void LuPlan::release() {
     if (d_act) cudaFree(d_act);
     if (d_pfx) cudaFree(d_pfx);
+    if (d_err) cudaFree(d_err);
     d_act = nullptr;
     d_pfx = nullptr;
+    d_err = nullptr;
     steps.clear();
 }
 
@@ -1013,7 +1463,7 @@ static int lu_factor_one(gbvlm_lu h, T* A, int64_t n, int64_t ld, cudaStream_t s
         set_error("LU: exactly zero pivot at column %d", *hi);
         return GBVLM_ERR_SINGULAR;
     }
-    return GBVLM_OK;
+    return lu_plan_check(h->plan, st);
 }
 
 template <class T>

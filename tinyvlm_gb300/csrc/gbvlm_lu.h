@@ -7,7 +7,8 @@
 
 namespace gbvlm {
 
-constexpr int LU_NB = 32;  // panel width
+constexpr int LU_NB = 32;      // panel width
+constexpr int LU_OUTER = 128;  // outer block width with tensor-core updates
 
 // Device tables, one entry per system (systems sorted by n descending).
 template <class T>
@@ -23,27 +24,56 @@ struct LuBatch {
     int32_t* const* perm;  // row permutation of the factorisation (perm[r] = original row), n per system
 };
 
+// One panel launch: active systems [first, first + count) of a step, each
+// factored by a cluster of `csize` CTAs of `nt` threads owning `slab` rows
+// apiece, one row per thread in registers (csize 0: the global-memory
+// fallback).
+struct PanelGroup {
+    int32_t first = 0, count = 0;
+    int32_t csize = 1, slab = 0, nt = 0;
+};
+
 struct LuStep {
     int64_t k = 0;
     int64_t act_off = 0;
     int32_t n_panel = 0;
-    int32_t n_tall_by_elem[2] = {0, 0};  // active systems whose panel exceeds shared memory (float, double)
-    int64_t smem_rows[2] = {0, 0};       // tallest panel of the rest (float, double)
-    int64_t n_tall_rows[2] = {0, 0};     // tallest panel of the tall ones
+    std::vector<PanelGroup> panels[2];  // panel launches (float, double)
     int64_t swap_pfx = 0, swap_total = 0;
     int64_t trsm_pfx = 0, trsm_blocks = 0;
     int32_t n_upd = 0;
     int64_t upd_act_skip = 0;
-    int64_t upd_pfx = 0, upd_blocks = 0;
+    int64_t upd_pfx = 0, upd_blocks = 0;  // whole trailing update (one-level blocking)
+    // two-level blocking: outer block [kend - LuPlan::W, kend)
+    int64_t kend = 0;
+    int64_t iswap_pfx = 0, iswap_total = 0;   // inner swaps, outer-panel columns
+    int64_t itrsm_pfx = 0, itrsm_blocks = 0;  // inner U rows, outer-panel columns
+    int32_t n_in = 0;                         // systems with an inner update (a prefix)
+    int64_t in_pfx = 0, in_blocks = 0;        // inner update of the outer panel, 64 x 64 tiles
+    int32_t bswap_first = 0;                  // systems [bswap_first, n_panel) end the outer block here
+    int64_t bswap_pfx = 0, bswap_total = 0;   // the block's swaps on the columns outside it
+    int32_t n_tc = 0;                         // systems with n > kend at the block's last step (a prefix)
+    int64_t btrsm_pfx = 0, btrsm_blocks = 0;  // U12 = L11^-1 A12, 32 columns per CTA
+    int64_t tc_pfx = 0, tc_blocks = 0;        // outer update, 128 x 128 tensor-core tiles
 };
 
 struct LuPlan {
     std::vector<LuStep> steps;
     int32_t nsys = 0;
     int64_t maxn = 0;
-    int cluster = 0;  // CTAs per cluster for tall panels (0: one-CTA global-memory panel)
+    int cluster = 1;  // largest cluster the register panel can be launched with
+    int tc_passes = 0;  // float trailing update: 0 CUDA cores, 1 TF32, 3 3xTF32 tensor cores
+    int W = LU_NB;      // outer block width of the float factorisation
     int32_t* d_act = nullptr;
     int64_t* d_pfx = nullptr;
+    int* d_err = nullptr;  // set by a tensor-core tile whose bounded wait ran out
+    // algorithmic work of the outer (tensor-core) updates of one factorisation:
+    // 2 m^2 W flops and 8 m^2 + 8 m W bytes (C read and written, L21 and U12
+    // read once) per system and outer block, m = n - kend
+    double tc_flops = 0, tc_bytes = 0;
+    int64_t tc_launches = 0;
+    // when set, lu_batch_factor records an event before and after every
+    // tensor-core update launch (profiling; not used inside graphs)
+    std::vector<cudaEvent_t>* tc_events = nullptr;
     void release();
     ~LuPlan() { release(); }
     LuPlan() = default;
@@ -52,6 +82,10 @@ struct LuPlan {
 };
 
 int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st);
+// GBVLM_OK, or an error if a tensor-core update gave up waiting (synchronises st)
+int lu_plan_check(const LuPlan& plan, cudaStream_t st);
+// number of kernel launches lu_batch_factor makes for element size es (4 or 8)
+int64_t lu_plan_launches(const LuPlan& plan, int es);
 template <class T>
 int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st);
 template <class T>

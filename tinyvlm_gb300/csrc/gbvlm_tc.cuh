@@ -1,0 +1,290 @@
+// Tensor-core (tcgen05, TF32) trailing update of the blocked LU:
+//
+//     C[r, c] -= sum_kk L[r, kk] * U[kk, c]
+//
+// over 128 x 128 output tiles, for every active system of a step.  L, U and
+// C live in the system's column-major matrix (leading dimension ld).
+//
+// Precision: each fp32 operand x is split as hi = tf32(x) (round to nearest)
+// and lo = x - hi; the product is accumulated in fp32 in tensor memory as
+// hi*hi + hi*lo + lo*hi ("3xTF32"), which keeps the update at fp32 accuracy
+// (the dropped lo*lo term is ~2^-22 relative).  PASSES = 1 keeps hi*hi only
+// (plain TF32).
+//
+// Per CTA (256 threads, one output tile, two CTAs per SM):
+//   * operands are staged in shared memory per 32-wide K chunk, in the
+//     K-major, 128-byte-swizzled layout the MMA reads: row r of a chunk is
+//     128 bytes (32 tf32), its 16-byte pieces permuted by XOR with r % 8,
+//     8-row groups 1024 bytes apart.  With STAGES = 2 threads fill chunk
+//     c+1 while the tensor core works on chunk c; with one stage the other
+//     CTA on the SM fills that time;
+//   * one thread issues tcgen05.mma (M = 128, N = 128, K = 8 per
+//     instruction) into a 128-column fp32 accumulator in tensor memory and
+//     commits each chunk to that stage's mbarrier;
+//   * epilogue: warp w reads accumulator lanes 32(w%4)..+31 (tile rows),
+//     columns 64(w/4)..+63, with tcgen05.ld and subtracts them from C, a warp
+//     covering 32 consecutive rows of one column per store.
+// Every wait on an mbarrier is bounded in time; a CTA that runs out sets the
+// error word, skips its epilogue and still frees its tensor memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbvlm {
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int THREADS = 256;
+constexpr int CHUNK_BYTES = BM * BK * 4;        // one operand chunk, 16 KB
+constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;    // A hi, A lo, B hi, B lo
+constexpr int STAGES = 1;                       // one stage: two CTAs share an SM and hide each other's latency
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + alignment slack
+constexpr int TMEM_COLS = BN;
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// wait for the phase of the given parity to complete; false after WAIT_NS
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > WAIT_NS) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// D (tensor memory) (+)= A (smem) * B (smem)^T, kind::tf32
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// arrive on the mbarrier once every MMA issued so far by this thread is done
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 32 consecutive accumulator columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart; `saddr` is the chunk's (1024-aligned) address plus the
+// byte offset of the K step inside the 128-byte row
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                     // leading-dimension offset (not used by swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;           // stride-dimension offset
+    d |= (uint64_t)1 << 46;                     // descriptor version
+    d |= (uint64_t)2 << 61;                     // 128-byte swizzle
+    return d;
+}
+
+// instruction descriptor: fp32 accumulator, tf32 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// byte offset of element (row, kk) in a 128-row x 32-column swizzled chunk
+__device__ __forceinline__ uint32_t sw128_off(int row, int kk) {
+    return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((kk >> 2) ^ (row & 7)) & 7) << 4) + ((kk & 3) << 2));
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+__device__ __forceinline__ void st_shared_f32(uint32_t addr, float a) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(a) : "memory");
+}
+
+// One 128 x 128 tile: C(r0.., c0..) -= L(r0.., 0..K) * U(0..K, c0..).
+//   L(r, kk) = Lp[r + kk * ld], U(kk, c) = Up[kk + c * ld], C(r, c) = Cp[r + c * ld];
+//   rows r < m_rows and columns c < n_cols exist (tile-relative bounds).
+template <int PASSES>
+__device__ __forceinline__ void update_tile(const float* Lp, const float* Up, float* Cp, int64_t ld, int m_rows,
+                                            int n_cols, int K, unsigned char* smem_raw, uint64_t* bar, uint32_t* tslot,
+                                            int* err) {
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    if (wid == 0) {
+        tmem_alloc(tslot, TMEM_COLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < STAGES; i++) mbar_init(&bar[i], 1);
+        fence_mbar_init();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t idesc = idesc_tf32(BM, BN);
+    const int nchunks = (K + BK - 1) / BK;
+    bool ok = true;
+    int committed = -1;  // last chunk whose MMAs were committed
+    for (int c = 0; c < nchunks; c++) {
+        const int s = c % STAGES;
+        // stage s is free once the MMAs of chunk c - STAGES are done
+        const bool free_ = c < STAGES || mbar_wait(&bar[s], ((c - STAGES) / STAGES) & 1);
+        const uint32_t a_hi = base + s * STAGE_BYTES, a_lo = a_hi + CHUNK_BYTES;
+        const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+        const int kc = c * BK;
+        if (free_) {
+            // A chunk: thread = tile row (tid % 128), 16 K values of its half (coalesced across the warp per K)
+            {
+                const int row = tid & (BM - 1), kh = (tid >> 7) * 16;
+                float v[16];
+                const bool rv = row < m_rows;
+#pragma unroll
+                for (int kk = 0; kk < 16; kk++)
+                    v[kk] = (rv && kc + kh + kk < K) ? Lp[row + (int64_t)(kc + kh + kk) * ld] : 0.f;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint32_t off = sw128_off(row, kh + 4 * j);
+                    const float h0 = tf32_hi(v[4 * j]), h1 = tf32_hi(v[4 * j + 1]);
+                    const float h2 = tf32_hi(v[4 * j + 2]), h3 = tf32_hi(v[4 * j + 3]);
+                    st_shared_v4(a_hi + off, h0, h1, h2, h3);
+                    if (PASSES > 1)
+                        st_shared_v4(a_lo + off, v[4 * j] - h0, v[4 * j + 1] - h1, v[4 * j + 2] - h2,
+                                     v[4 * j + 3] - h3);
+                }
+            }
+            // B chunk: warp w covers tile columns 16w..16w+15, lane = K index (coalesced along the column)
+            {
+                float v[16];
+                const bool kv = kc + lane < K;
+#pragma unroll
+                for (int cc = 0; cc < 16; cc++) {
+                    const int col = 16 * wid + cc;
+                    v[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ld] : 0.f;
+                }
+#pragma unroll
+                for (int cc = 0; cc < 16; cc++) {
+                    const uint32_t off = sw128_off(16 * wid + cc, lane);
+                    const float h = tf32_hi(v[cc]);
+                    st_shared_f32(b_hi + off, h);
+                    if (PASSES > 1) st_shared_f32(b_lo + off, v[cc] - h);
+                }
+            }
+        }
+        fence_async_smem();  // generic-proxy stores visible to the tensor core
+        fence_before_sync();
+        ok = __syncthreads_and(free_) != 0;  // uniform over the CTA
+        if (!ok) break;
+        if (tid == 0) {
+            fence_after_sync();
+#pragma unroll
+            for (int ks = 0; ks < BK / 8; ks++) {
+                const uint64_t ah = sw128_desc(a_hi + ks * 32), bh = sw128_desc(b_hi + ks * 32);
+                mma_tf32(tmem, ah, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                if (PASSES > 1) {
+                    const uint64_t al = sw128_desc(a_lo + ks * 32), bl = sw128_desc(b_lo + ks * 32);
+                    mma_tf32(tmem, ah, bl, idesc, 1u);
+                    mma_tf32(tmem, al, bh, idesc, 1u);
+                }
+            }
+            mma_commit(&bar[s]);
+        }
+        committed = c;
+    }
+    // every committed MMA done (the last commit covers all earlier ones)
+    bool done = committed < 0 || mbar_wait(&bar[committed % STAGES], (committed / STAGES) & 1);
+    done = __syncthreads_and(done) != 0;
+    fence_after_sync();
+    if (ok && done) {
+        const int row = 32 * (wid & 3) + lane;
+        const bool rv = row < m_rows;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int cb = 64 * (wid >> 2) + 32 * q;
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)cb, v);
+            if (rv) {
+                // all 32 loads before the stores: a load may not pass a store to the same array
+                float c[32];
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int col = cb + j;
+                    c[j] = col < n_cols ? Cp[row + (int64_t)col * ld] : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int col = cb + j;
+                    if (col < n_cols) Cp[row + (int64_t)col * ld] = c[j] - v[j];
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (wid == 0) tmem_dealloc(tmem, TMEM_COLS);
+}
+
+}  // namespace tc
+}  // namespace gbvlm
