@@ -49,7 +49,8 @@ def parse():
     p.add_argument("--mode", default="shared", choices=["shared", "exact"])
     p.add_argument("--cases", type=int, default=512)
     p.add_argument("--alphas", type=int, default=8)
-    p.add_argument("--refine", type=int, default=0)
+    p.add_argument("--refine", type=int, default=1,
+                   help="refinement sweeps (double residual); 1 keeps every solve of the batch within CL/CM 1e-5")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
@@ -60,6 +61,7 @@ def parse():
     p.add_argument("--rates", default="2,8,32", help="served: Poisson arrival rates (requests/s) to sweep")
     p.add_argument("--requests", type=int, default=45, help="served: requests per rate")
     p.add_argument("--rollup", type=int, default=1)
+    p.add_argument("--large-n", type=int, default=128, help="large: chordwise = spanwise panels of the elliptic wing")
     return p.parse_args()
 
 
@@ -267,9 +269,7 @@ def run_gpu(args):
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
         peaks = json.load(open(pk))
-    # dominant stage -> roofline
-    stage = max(prof, key=prof.get)
-    roof = roofline(stage, prof, bs, peaks)
+    roof = roofline(bs, stream, peaks, ms)
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -288,27 +288,36 @@ def run_gpu(args):
     print(json.dumps(out))
 
 
-def roofline(stage, prof, bs, peaks):
-    """Roofline entry for the dominant stage (algorithmic work / CUDA-event time)."""
-    t = prof[stage] / 1000.0
-    if stage == "assembly":
-        flops = FLOP_PER_INTERACTION * bs.interactions
-        # FP32 SIMT pipe: 152 SMs x 128 lanes x 2 flop/FMA x max SM clock
-        peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-        return {"stage": stage, "kernel": "k_batch_assemble", "bound": "fp32", "achieved": flops / t / 1e12,
-                "peak": peak, "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak, "traffic": None,
-                "peak_source": "nominal FP32 FMA rate at the measured max SM clock (no FP32 figure in MEASURED_PEAKS.json)",
-                "work": "558 flop x %d ring-point interactions" % int(bs.interactions)}
-    if stage == "lu_factor":
-        flops = bs.lu_flops
-        peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-        return {"stage": stage, "kernel": "k_panel/k_swap/k_trsm/k_update", "bound": "fp32",
-                "achieved": flops / t / 1e12, "peak": peak, "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak,
-                "traffic": None, "peak_source": "nominal FP32 FMA rate at the measured max SM clock",
-                "work": "sum of 2/3 n^3 over systems"}
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    return {"stage": stage, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
-            "traffic": None}
+# DRAM bytes per algorithmic byte of the tensor-core trailing update, from
+# one ncu capture of k_update_tc on the 64-case batch (dram__bytes_read.sum +
+# dram__bytes_write.sum over the launch's algorithmic bytes; the operands are
+# re-read from L2, not DRAM).  Summary and command: profiles/k_update_tc_batch64.md
+TC_TRAFFIC_PER_ALG_BYTE = 0.747  # 140.4 MB DRAM / 187.9 MB algorithmic (outer block 128..256 of the 64-case batch)
+
+
+def roofline(bs, stream, peaks, ms_step):
+    """Roofline entry of the LU's tensor-core trailing update (k_update_tc),
+    the largest kernel of the batched step: algorithmic bytes per launch
+    (C read and written, L21 and U12 read once) over its CUDA-event time per
+    launch, against the measured HBM copy bandwidth (the update is
+    bandwidth-bound: 2W/8 = 32 flop per byte at W = 128)."""
+    up = bs.update_profile(stream=stream)
+    if up["launches"] == 0 or up["ms"] <= 0:
+        return None
+    hbm = peaks.get("hbm_gbs")
+    src = "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    if hbm is None:
+        hbm, src = 6800.0, "fallback 6.8 TB/s (of fallback)"
+    t = up["ms"] / 1000.0 / up["launches"]
+    per_launch = up["bytes"] / up["launches"]
+    achieved = per_launch / t / 1e9
+    traffic = per_launch * TC_TRAFFIC_PER_ALG_BYTE if TC_TRAFFIC_PER_ALG_BYTE else None
+    return {"kernel": "k_update_tc (LU trailing update, tcgen05 kind::tf32, 3xTF32)", "bound": "hbm",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+            "peak_source": src, "launches": up["launches"], "ms_total": up["ms"],
+            "share_of_step": up["ms"] / ms_step,
+            "tflops_alg": up["flops"] / (up["ms"] / 1000.0) / 1e12,
+            "work": "per outer block and system: 8 m^2 + 8 m W bytes, 2 m^2 W flops (m = n - kend, W = 128)"}
 
 
 def plain_path_rate(args, cases, dev, co):
@@ -348,7 +357,7 @@ def run_large(args):
     import torch
     from tinyvlm_gb300 import mesh as M
     from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
-    v = M.elliptic(128, 128).astype(np.float32)
+    v = M.elliptic(args.large_n, args.large_n).astype(np.float32)
     M.quarter_chord(v)
     case = M.Case(v, np.radians(np.linspace(-10.0, 10.0, 64)), {})
     bs = BatchSolver([case], mode="shared", refine=args.refine)
@@ -367,7 +376,8 @@ def run_large(args):
     co, _ = bs.results(stream=stream)
     lu = bs.lu_flops / (prof["lu_factor"] / 1000.0) / 1e12
     asm = FLOP_PER_INTERACTION * bs.interactions / (prof["assembly"] / 1000.0) / 1e12
-    print(json.dumps({"workload": "large steady: elliptic 128x128 = 16384 panels, 64 alphas, one AIC",
+    print(json.dumps({"workload": "large steady: elliptic %dx%d = %d panels, 64 alphas, one AIC" %
+                                  (args.large_n, args.large_n, args.large_n ** 2),
                       "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof,
                       "lu_tflops": lu, "assembly_tflops_alg": asm, "cl_range": [float(co[:, 0].min()), float(co[:, 0].max())],
                       "refine_iters": args.refine}))

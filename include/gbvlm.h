@@ -315,13 +315,17 @@ int gbvlm_batch_set_inputs(gbvlm_batch h, const float* verts, const double* alph
                            const double* ref_pt, gbvlm_stream stream);
 /* Enqueue the whole solve (a CUDA graph captured on first use) on stream. */
 int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream);
+/* The same solve launched kernel by kernel, without capturing a graph: for a
+ * batch solved once (a served request), where capture and instantiation would
+ * cost more than the launches they save. */
+int gbvlm_batch_run_eager(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream);
 /* Run the stages once without the graph, each bracketed by CUDA events on
  * `stream`; stage_ms[6] = geometry, assembly, rhs, LU factor, solve +
  * refinement, loads (milliseconds).  Synchronous. */
 int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream);
 /* Measurement hook, no reference counterpart: run the solve once without the
- * graph with CUDA events around every tensor-core trailing-update launch of
- * the LU; out[4] = total milliseconds of those launches, their number, and
+ * graph (the LU's size groups one after another) with CUDA events around
+ * every tensor-core trailing-update launch of the LU; out[4] = total milliseconds of those launches, their number, and
  * their algorithmic flops (2 m^2 W) and bytes (8 m^2 + 8 m W) per solve of
  * the batch (m = trailing size, W = outer block width).  Synchronous. */
 int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream);

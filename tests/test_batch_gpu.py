@@ -99,3 +99,27 @@ def test_batch_vs_plain_double_path(cuda):
             r = plain.run(FlowData(a), ref_pt=REF)
             assert abs(co[k, 0] - r.cl) <= TOL * max(abs(r.cl), 1e-3), (co[k, 0], r.cl)
             k += 1
+
+
+def test_eager_equals_graph_across_size_groups(cuda):
+    """Systems from all three LU size groups (n > 1024, 384 < n <= 1024,
+    n <= 384, factored on separate graph branches): the captured graph and
+    the kernel-by-kernel launch give identical results, and a large system
+    alone equals the same system inside the mixed batch."""
+    big = M.batch_cases(2, seed=11, n_alpha=2, nc_range=(28, 32), ns_range=(48, 64))
+    mid = M.batch_cases(3, seed=12, n_alpha=2, nc_range=(16, 20), ns_range=(30, 40))
+    small = M.batch_cases(4, seed=13, n_alpha=2, nc_range=(4, 8), ns_range=(4, 20))
+    cases = big + mid + small
+    assert max(c.n for c in cases) > 1024 and min(c.n for c in cases) <= 384
+    bs = BatchSolver(cases, mode="shared", refine=0)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run()
+    graph, _ = bs.results()
+    bs.run(graph=False)
+    eager, _ = bs.results()
+    np.testing.assert_array_equal(graph, eager)
+    one = BatchSolver([big[0]], mode="shared", refine=0)
+    one.set_inputs(pack_verts([big[0]]), pack_alphas([big[0]]), ref_pt=REF)
+    one.run(graph=False)
+    alone, _ = one.results()
+    np.testing.assert_allclose(alone, graph[0:2], rtol=1e-12, atol=1e-14)

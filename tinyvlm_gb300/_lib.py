@@ -71,6 +71,7 @@ def _protos():
     t["gbvlm_batch_info"] = [P, P, P, P, P, P, P]
     t["gbvlm_batch_set_inputs"] = [P, P, P, F64, F64, P, P]
     t["gbvlm_batch_run"] = [P, I32, P]
+    t["gbvlm_batch_run_eager"] = [P, I32, P]
     t["gbvlm_batch_results"] = [P, P, P, P]
     t["gbvlm_batch_profile"] = [P, P, P]
     t["gbvlm_batch_update_profile"] = [P, P, P]

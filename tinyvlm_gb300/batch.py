@@ -68,8 +68,10 @@ class BatchSolver:
     def _s(stream):
         return ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
 
-    def run(self, want_gamma=False, stream=None):
-        call("gbvlm_batch_run", self.h, 1 if want_gamma else 0, self._s(stream))
+    def run(self, want_gamma=False, stream=None, graph=True):
+        """Enqueue the solve; graph=False launches it kernel by kernel (a batch solved once)."""
+        call("gbvlm_batch_run" if graph else "gbvlm_batch_run_eager", self.h, 1 if want_gamma else 0,
+             self._s(stream))
 
     def results(self, gamma=False, stream=None):
         co = np.zeros((self.nsolve, 5), np.float64)

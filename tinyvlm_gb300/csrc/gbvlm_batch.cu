@@ -297,30 +297,70 @@ __global__ void k_batch_accum(BatchArgs a) {
     for (int q = 0; q < S.nrhs; q++) S.Xd[p + q * S.n] += (double)S.X[p + q * S.n];
 }
 
-// R = B - A2 Xd in double; X = (float)R.  One thread per row, tiles (system, row block)
+// R = B - A2 Xd; X = (float)R.  One thread per row, tiles (system, row
+// block).  The products of the float matrix A2 with the double solution Xd
+// are accumulated in double-float arithmetic on the fp32 units (Xd split as
+// hi + lo floats, each product a*hi exact through an FMA, running sums
+// (sh, sl) kept with a compensated addition): about 2^-44 relative per term,
+// where the fp64 units of this part run at a small fraction of the fp32 rate.
 constexpr int RS_THREADS = 128;
 constexpr int RS_MAXRHS = 8;
+constexpr int RS_CB = 32;  // columns of Xd staged per step
+
+// (sh, sl) += a * (xh + xl)
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    const float pe = __fmaf_rn(a, xh, -p);  // a*xh - p exactly
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));  // sh + p - s exactly
+    sh = s;
+    sl = __fmaf_rn(a, xl, __fadd_rn(sl, __fadd_rn(e, pe)));
+}
+
 __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, const int64_t* rpfx) {
+    __shared__ float xh[RS_CB][RS_MAXRHS], xl[RS_CB][RS_MAXRHS];
     const int si = find_sys(rpfx, a.nsys, blockIdx.x);
     const SysDesc& S = a.sys[si];
     const int64_t r = (blockIdx.x - rpfx[si]) * RS_THREADS + threadIdx.x;
     const int64_t n = S.n;
-    if (r >= n) return;
+    const bool rv = r < n;
+    const float* arow = S.A2 + (rv ? r : 0);
     for (int q0 = 0; q0 < S.nrhs; q0 += RS_MAXRHS) {
         const int nq = min(RS_MAXRHS, S.nrhs - q0);
-        double acc[RS_MAXRHS];
+        float sh[RS_MAXRHS], sl[RS_MAXRHS];
 #pragma unroll
-        for (int q = 0; q < RS_MAXRHS; q++) acc[q] = 0.0;
-        for (int64_t c = 0; c < n; c++) {
-            const double av = (double)S.A2[r + c * n];
+        for (int q = 0; q < RS_MAXRHS; q++) sh[q] = sl[q] = 0.f;
+        for (int64_t c0 = 0; c0 < n; c0 += RS_CB) {
+            __syncthreads();
+            for (int e = threadIdx.x; e < RS_CB * RS_MAXRHS; e += RS_THREADS) {
+                const int cc = e / RS_MAXRHS, q = e % RS_MAXRHS;
+                const double v = (c0 + cc < n && q < nq) ? S.Xd[(c0 + cc) + (q0 + q) * n] : 0.0;
+                const float h = (float)v;
+                xh[cc][q] = h;
+                xl[cc][q] = (float)(v - (double)h);
+            }
+            __syncthreads();
+            if (rv) {
+                const int cn = (int)min((int64_t)RS_CB, n - c0);
+                float av[RS_CB];
 #pragma unroll
-            for (int q = 0; q < RS_MAXRHS; q++)
-                if (q < nq) acc[q] = fma(av, S.Xd[c + (q0 + q) * n], acc[q]);
+                for (int cc = 0; cc < RS_CB; cc++) av[cc] = cc < cn ? arow[(c0 + cc) * n] : 0.f;
+#pragma unroll
+                for (int cc = 0; cc < RS_CB; cc++)
+#pragma unroll
+                    for (int q = 0; q < RS_MAXRHS; q++) df_mac(sh[q], sl[q], av[cc], xh[cc][q], xl[cc][q]);
+            }
         }
-        for (int q = 0; q < nq; q++) {
-            const double res = S.B[r + (q0 + q) * n] - acc[q];
-            S.R[r + (q0 + q) * n] = res;
-            S.X[r + (q0 + q) * n] = (float)res;
+        if (rv) {
+#pragma unroll
+            for (int q = 0; q < RS_MAXRHS; q++) {
+                if (q < nq) {
+                    const double res = S.B[r + (q0 + q) * n] - ((double)sh[q] + (double)sl[q]);
+                    S.R[r + (q0 + q) * n] = res;
+                    S.X[r + (q0 + q) * n] = (float)res;
+                }
+            }
         }
     }
 }
@@ -474,7 +514,14 @@ struct gbvlm_batch_s {
     int64_t* d_rpfx = nullptr;   // residual tiles
     int64_t assembly_tiles = 0, residual_tiles = 0;
     int64_t maxn = 0;
-    LuPlan plan;
+    // the sorted systems in size groups, each factored by its own plan on its
+    // own stream (graph branch), so the long step chain of the largest
+    // systems runs beside the shorter chains of the others
+    static constexpr int MAX_GROUPS = 3;
+    int ngroups = 0;
+    LuPlan plans[MAX_GROUPS];
+    cudaStream_t side[MAX_GROUPS] = {};
+    cudaEvent_t fork = nullptr, join[MAX_GROUPS] = {};
     LuBatch<float> lub;
     double u_inf = 1, rho = 1, beta = 0, ref[3] = {0, 0, 0};
     int32_t want_gamma = 0;
@@ -488,13 +535,23 @@ struct gbvlm_batch_s {
         if (graph) cudaGraphDestroy(graph);
         if (cap) cudaStreamDestroy(cap);
         if (arena) cudaFree(arena);
-        plan.release();
+        for (int g = 0; g < MAX_GROUPS; g++) {
+            plans[g].release();
+            if (side[g]) cudaStreamDestroy(side[g]);
+            if (join[g]) cudaEventDestroy(join[g]);
+        }
+        if (fork) cudaEventDestroy(fork);
     }
 };
 
-static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+constexpr int MAX_GROUPS_B = 2;  // size-group boundaries (gbvlm_batch_s::MAX_GROUPS - 1)
+
+// serial_lu: factor the size groups one after another on `st` (kernel timing
+// without the groups' launches overlapping)
+static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullptr, bool serial_lu = false) {
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
-    const int64_t nlaunch = lu_plan_launches(h->plan, 4);
+    int64_t nlaunch = 0;
+    for (int g = 0; g < h->ngroups; g++) nlaunch += lu_plan_launches(h->plans[g], 4);
     int32_t mr = 0;
     for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
     const int64_t solves = (mr + 7) / 8;
@@ -528,19 +585,35 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     k_batch_rhs<<<g, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
     mark(3);
-    int rc = lu_batch_factor<float>(h->lub, h->plan, st);
-    if (rc) return rc;
+    // group 0 (the largest systems) on a high-priority side stream, the
+    // others beside it; the main stream waits for all of them
+    if (serial_lu) {
+        for (int g = 0; g < h->ngroups; g++) {
+            int rc = lu_batch_factor<float>(h->lub, h->plans[g], st);
+            if (rc) return rc;
+        }
+    } else {
+        GB_CUDA(cudaEventRecord(h->fork, st));
+        for (int g = 0; g < h->ngroups; g++) {
+            GB_CUDA(cudaStreamWaitEvent(h->side[g], h->fork, 0));
+            int rc = lu_batch_factor<float>(h->lub, h->plans[g], h->side[g]);
+            if (rc) return rc;
+            GB_CUDA(cudaEventRecord(h->join[g], h->side[g]));
+        }
+        for (int g = 0; g < h->ngroups; g++) GB_CUDA(cudaStreamWaitEvent(st, h->join[g], 0));
+    }
+    int rc = GBVLM_OK;
     mark(4);
     int32_t maxrhs = 0;
     for (auto& s : h->sys) maxrhs = std::max(maxrhs, s.nrhs);
-    rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st);
+    rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st, h->plans[0].tc_passes ? h->plans[0].d_err : nullptr);
     if (rc) return rc;
     k_batch_accum<<<g, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
     for (int it = 0; it < h->refine; it++) {
         k_batch_residual<<<(unsigned)h->residual_tiles, RS_THREADS, 0, st>>>(a, h->d_rpfx);
         GB_LAUNCH_CHECK();
-        rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st);
+        rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st, h->plans[0].tc_passes ? h->plans[0].d_err : nullptr);
         if (rc) return rc;
         k_batch_accum<<<g, 256, 0, st>>>(a);
         GB_LAUNCH_CHECK();
@@ -776,8 +849,32 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     h->lub.ldx = (const int64_t*)(base + o_lun);
     h->lub.nrhs = (const int32_t*)(base + o_lurhs);
     h->lub.perm = (int32_t* const*)(base + o_luperm);
-    std::vector<int64_t> ns_sorted(lun.begin(), lun.end());
-    rc = lu_plan_build(h->plan, ns_sorted, 0);
+    // size groups: n > 1024, 384 < n <= 1024, n <= 384 (empty groups dropped)
+    {
+        const int64_t bounds[MAX_GROUPS_B] = {1024, 384};
+        int i0 = 0;
+        int greatest = 0, least = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        for (int g = 0; g <= MAX_GROUPS_B && rc == GBVLM_OK; g++) {
+            int i1 = i0;
+            while (i1 < h->nsys && (g == MAX_GROUPS_B || lun[i1] > bounds[g])) i1++;
+            if (i1 == i0) continue;
+            const int gi = h->ngroups++;
+            std::vector<int64_t> ns(lun.begin() + i0, lun.begin() + i1);
+            rc = lu_plan_build(h->plans[gi], ns, 0, i0);
+            if (rc == GBVLM_OK) {
+                cudaError_t ee = cudaStreamCreateWithPriority(&h->side[gi], cudaStreamNonBlocking,
+                                                              gi == 0 ? greatest : least);
+                if (ee == cudaSuccess) ee = cudaEventCreateWithFlags(&h->join[gi], cudaEventDisableTiming);
+                if (ee != cudaSuccess) rc = cuda_fail(ee, "batch streams", __FILE__, __LINE__);
+            }
+            i0 = i1;
+        }
+        if (rc == GBVLM_OK) {
+            cudaError_t ee = cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+            if (ee != cudaSuccess) rc = cuda_fail(ee, "batch streams", __FILE__, __LINE__);
+        }
+    }
     if (rc) {
         delete h;
         return rc;
@@ -847,6 +944,16 @@ int gbvlm_batch_set_inputs(gbvlm_batch h, const float* verts, const double* alph
     return GBVLM_OK;
 }
 
+int gbvlm_batch_run_eager(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream) {
+    GB_REQUIRE(h, "null batch");
+    h->want_gamma = want_gamma ? 1 : 0;
+    if (h->exec) {  // a captured graph bakes want_gamma in
+        cudaGraphExecDestroy(h->exec);
+        h->exec = nullptr;
+    }
+    return batch_enqueue(h, to_cuda(stream));
+}
+
 int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream) {
     GB_REQUIRE(h, "null batch");
     cudaStream_t st = to_cuda(stream);
@@ -871,7 +978,7 @@ int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream) {
         }
         GB_CUDA(e);
         h->graph = g;
-        GB_CUDA(cudaGraphInstantiate(&h->exec, h->graph, 0));
+        GB_CUDA(cudaGraphInstantiate(&h->exec, h->graph, cudaGraphInstantiateFlagUseNodePriority));
     }
     GB_CUDA(cudaGraphLaunch(h->exec, st));
     return GBVLM_OK;
@@ -899,9 +1006,9 @@ int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream) 
     GB_REQUIRE(h && out, "null argument");
     cudaStream_t st = to_cuda(stream);
     std::vector<cudaEvent_t> ev;
-    h->plan.tc_events = &ev;
-    int rc = batch_enqueue(h, st);
-    h->plan.tc_events = nullptr;
+    for (int g = 0; g < h->ngroups; g++) h->plans[g].tc_events = &ev;
+    int rc = batch_enqueue(h, st, nullptr, true);
+    for (int g = 0; g < h->ngroups; g++) h->plans[g].tc_events = nullptr;
     double ms = 0;
     if (rc == GBVLM_OK) {
         cudaError_t e = cudaStreamSynchronize(st);
@@ -917,8 +1024,11 @@ int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream) 
     if (rc) return rc;
     out[0] = ms;
     out[1] = (double)(ev.size() / 2);
-    out[2] = h->plan.tc_flops;
-    out[3] = h->plan.tc_bytes;
+    out[2] = out[3] = 0;
+    for (int g = 0; g < h->ngroups; g++) {
+        out[2] += h->plans[g].tc_flops;
+        out[3] += h->plans[g].tc_bytes;
+    }
     return GBVLM_OK;
 }
 
@@ -934,8 +1044,10 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
         GB_CUDA(cudaMemcpyAsync(gt.data(), h->d_gamma, sizeof(float) * gt.size(), cudaMemcpyDeviceToHost, st));
     }
     GB_CUDA(cudaStreamSynchronize(st));
-    int rc = lu_plan_check(h->plan, st);
-    if (rc) return rc;
+    for (int g = 0; g < h->ngroups; g++) {
+        int rc = lu_plan_check(h->plans[g], st);
+        if (rc) return rc;
+    }
     int32_t* info = (int32_t*)host_scratch(sizeof(int32_t) * h->nsys);
     GB_CUDA(cudaMemcpy(info, h->lub.info, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost));
     for (int k = 0; k < h->nsys; k++) {

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -34,6 +35,7 @@ namespace gbvlm {
 
 constexpr int PANEL_THREADS = 512;
 constexpr int PR_THREADS_F64 = 256;  // register panel, double: 32 doubles of panel per thread
+constexpr int PR_MAX_CLUSTER = 16;   // largest cluster of the register panel
 constexpr int TRSM_COLS = 128;
 constexpr int GT = 64;  // update tile edge
 constexpr int GK = LU_NB;
@@ -146,7 +148,8 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(LuBatch<T> B, int64_t k
 // written to its final logical position at the end.  Rows whose logical
 // position is below jj are finished (pivot rows = rows of U).
 //
-// Per column jj, one CTA barrier (plus one cluster barrier when csize > 1):
+// Per column jj, one CTA barrier (plus one cluster barrier when csize > 1,
+// before which every CTA has pushed its candidate into all the others):
 //   1. each warp reduces its candidates (largest |a|, smallest logical
 //      position on ties, like LAPACK i?amax) with redux.sync; the winning
 //      lane publishes its whole row in shared memory;
@@ -211,15 +214,71 @@ __device__ __forceinline__ void static_for(F&& f) {
     }
 }
 
+// Shared state of the register panel (dynamic shared memory, so the
+// out-of-line pivot exchange below addresses the same buffers).
+template <class T, int NT, bool CLUSTER>
+struct PanelSmem {
+    static constexpr int NW = NT / 32;
+    static constexpr int CM = CLUSTER ? PR_MAX_CLUSTER : 1;
+    T s_row[2][NW][GK];  // each warp's candidate row
+    T c_row[2][CM][GK];  // candidate rows pushed by the CTAs of the cluster
+    PivKey<T> s_key[2][NW];
+    PivKey<T> c_key[2][CM];
+};
+
+template <class T>
+struct PivotOut {
+    T urow;  // lane t: column t of the pivot row
+    int p;   // logical position of the pivot row
+};
+
+// Steps 2 of a column: barrier, CTA-wide (and cluster-wide) winner, pivot row
+// to the lanes.  Kept out of line: called once per column from the
+// unrolled column loop, it is the same code for all 32 columns.
+template <class T, int NT, bool CLUSTER>
+__device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank) {
+    namespace cg = cooperative_groups;
+    using Key = PivKey<T>;
+    using SM = PanelSmem<T, NT, CLUSTER>;
+    extern __shared__ __align__(16) unsigned char pr_smem[];
+    SM& sm = *reinterpret_cast<SM*>(pr_smem);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    const Key mine = lane < SM::NW ? sm.s_key[buf][lane] : Key::none();
+    const Key best = mine.warp_max();
+    const int w = __ffs(__ballot_sync(0xffffffffu, lane < SM::NW && mine == best)) - 1;
+    PivotOut<T> o;
+    if constexpr (CLUSTER) {
+        // warp 0 pushes this CTA's candidate (key and row) into every CTA of the
+        // cluster; after the cluster barrier all reads are local
+        cg::cluster_group cl = cg::this_cluster();
+        if (wid == 0) {
+            const T v = sm.s_row[buf][w][lane];
+            for (int q = 0; q < csize; q++) {
+                *cl.map_shared_rank(&sm.c_row[buf][rank][lane], q) = v;
+                if (lane == 0) *cl.map_shared_rank(&sm.c_key[buf][rank], q) = best;
+            }
+        }
+        cl.sync();
+        const Key ck = lane < csize ? sm.c_key[buf][lane] : Key::none();
+        const Key cbest = ck.warp_max();
+        const int q = __ffs(__ballot_sync(0xffffffffu, lane < csize && ck == cbest)) - 1;
+        o.p = cbest.pos();
+        o.urow = sm.c_row[buf][q][lane];
+    } else {
+        o.p = best.pos();
+        o.urow = sm.s_row[buf][w][lane];
+    }
+    return o;
+}
+
 template <class T, int NT, bool CLUSTER>
 __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab) {
     namespace cg = cooperative_groups;
-    constexpr int NW = NT / 32;
     using Key = PivKey<T>;
-    __shared__ __align__(16) T s_row[2][NW][GK];  // each warp's candidate row
-    __shared__ Key s_key[2][NW];
-    __shared__ Key c_key[2];  // this CTA's candidate (read by the cluster)
-    __shared__ int c_w[2];
+    using SM = PanelSmem<T, NT, CLUSTER>;
+    extern __shared__ __align__(16) unsigned char pr_smem[];
+    SM& sm = *reinterpret_cast<SM*>(pr_smem);
     int csize = 1, rank = 0;
     if constexpr (CLUSTER) {
         csize = (int)cg::this_cluster().num_blocks();
@@ -260,37 +319,15 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
                         v.y = x[t + 1];
                         v.z = x[t + 2];
                         v.w = x[t + 3];
-                        *reinterpret_cast<V2*>(&s_row[buf][wid][t]) = v;
+                        *reinterpret_cast<V2*>(&sm.s_row[buf][wid][t]) = v;
                     }
                 }
-                if (lane == 0) s_key[buf][wid] = w;
+                if (lane == 0) sm.s_key[buf][wid] = w;
             }
-            __syncthreads();
             // 2. pivot: (p, row) known to every warp
-            T urow;  // lane t: column t of the pivot row
-            int p;
-            {
-                const Key mine = lane < NW ? s_key[buf][lane] : Key::none();
-                const Key best = mine.warp_max();
-                const int w = __ffs(__ballot_sync(0xffffffffu, lane < NW && mine == best)) - 1;
-                if constexpr (CLUSTER) {
-                    cg::cluster_group cl = cg::this_cluster();
-                    if (tid == 0) {
-                        c_key[buf] = best;
-                        c_w[buf] = w;
-                    }
-                    cl.sync();
-                    const Key ck = lane < csize ? *cl.map_shared_rank(&c_key[buf], lane) : Key::none();
-                    const Key cbest = ck.warp_max();
-                    const int q = __ffs(__ballot_sync(0xffffffffu, lane < csize && ck == cbest)) - 1;
-                    const int wq = *cl.map_shared_rank(&c_w[buf], q);
-                    p = cbest.pos();
-                    urow = *cl.map_shared_rank(&s_row[buf][wq][lane], q);
-                } else {
-                    p = best.pos();
-                    urow = s_row[buf][w][lane];
-                }
-            }
+            const PivotOut<T> po = panel_exchange<T, NT, CLUSTER>(buf, csize, rank);
+            const T urow = po.urow;
+            const int p = po.p;
             const T d = __shfl_sync(0xffffffffu, urow, jj);
             if (tid == 0 && rank == 0) {
                 ipiv[k + jj] = (int32_t)(k + p);  // a store: nothing waits on it
@@ -632,7 +669,7 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, 
     const int64_t tiles = (n - lo + tc::BM - 1) / tc::BM;
     const int64_t t = blockIdx.x - pfx[a];
     const int64_t r0 = lo + (t % tiles) * tc::BM, c0 = lo + (t / tiles) * tc::BN;
-    tc::update_tile<PASSES>(A + r0 + k0 * ld, A + k0 + c0 * ld, A + r0 + c0 * ld, ld,
+    tc::update_tile<PASSES>(A + r0 + k0 * ld, ld, A + k0 + c0 * ld, ld, A + r0 + c0 * ld, ld,
                             (int)min((int64_t)tc::BM, n - r0), (int)min((int64_t)tc::BN, n - c0), w, tc_smem, bar,
                             &tslot, err);
 }
@@ -642,9 +679,9 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, 
 // ends up in position r (the ipiv interchanges composed in order)
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_perm(LuBatch<T> B) {
+__global__ void k_perm(LuBatch<T> B, int32_t base) {
     extern __shared__ int32_t sp[];
-    const int32_t sid = blockIdx.x;
+    const int32_t sid = base + blockIdx.x;
     const int64_t n = B.n[sid];
     const int32_t* ip = B.ipiv[sid];
     int32_t* pm = B.perm[sid];
@@ -891,11 +928,156 @@ __global__ void __launch_bounds__(256) k_trs_update(LuBatch<T> B, int64_t k, int
     for (int q = 0; q < nq; q++) B.X[0][r + (int64_t)(q0 + q) * ldx] -= acc[q];
 }
 
+// ---------------------------------------------------------------------------
+// single large float system on the tensor cores: triangular solves in
+// 128-row blocks.  Per block: the diagonal triangle (unit lower forward,
+// upper with its diagonal backward) solved in shared memory for up to 64
+// right-hand sides per CTA, then the rows below (forward) or above (backward)
+// updated with the block's solution by the 3xTF32 tcgen05 tile routine.
+// ---------------------------------------------------------------------------
+constexpr int TB = LU_OUTER;
+constexpr int TB_COLS = 64;
+constexpr int TB_LS = TB + 4, TB_XS = TB_COLS + 1;
+constexpr size_t trs_block_smem() { return sizeof(float) * ((size_t)TB * TB_LS + (size_t)TB * TB_XS); }
+
+template <bool UPPER>
+__global__ void __launch_bounds__(256, 2) k_trs_block(LuBatch<float> B, int64_t k) {
+    extern __shared__ __align__(16) float tb_smem[];
+    float* L = tb_smem;          // triangle, L[r * TB_LS + c], padded to 128 with the identity
+    float* X = L + TB * TB_LS;   // X[r * TB_XS + j]
+    const int64_t n = B.n[0], ld = B.ld[0], ldx = B.ldx[0];
+    const float* A = B.A[0] + k + k * ld;
+    const int j0 = blockIdx.x * TB_COLS;
+    const int ncols = min(TB_COLS, B.nrhs[0] - j0);
+    const int bw = (int)min((int64_t)TB, n - k);
+    float* Xg = B.X[0] + k + (int64_t)j0 * ldx;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    staged_copy<16>(
+        TB * TB, tid, 256,
+        [&](int64_t e) {
+            const int r = (int)(e & (TB - 1)), c = (int)(e >> 7);
+            return (r < bw && c < bw) ? A[r + (int64_t)c * ld] : (r == c ? 1.f : 0.f);
+        },
+        [&](int64_t e, float v) { L[(int)(e & (TB - 1)) * TB_LS + (int)(e >> 7)] = v; });
+    staged_copy<16>(
+        TB * TB_COLS, tid, 256,
+        [&](int64_t e) {
+            const int r = (int)(e & (TB - 1)), j = (int)(e >> 7);
+            return (r < bw && j < ncols) ? Xg[r + (int64_t)j * ldx] : 0.f;
+        },
+        [&](int64_t e, float v) { X[(int)(e & (TB - 1)) * TB_XS + (int)(e >> 7)] = v; });
+    __syncthreads();
+#pragma unroll 1
+    for (int bi = 0; bi < TB / 32; bi++) {
+        const int rb = 32 * (UPPER ? TB / 32 - 1 - bi : bi);
+        // diagonal 32 x 32: a warp per column, a lane per row, four columns in flight
+        {
+            float lrow[32];
+#pragma unroll
+            for (int l = 0; l < 32; l++) lrow[l] = L[(rb + lane) * TB_LS + rb + l];
+#pragma unroll 1
+            for (int jc = 4 * wid; jc < TB_COLS; jc += 32) {
+                float x[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) x[c] = X[(rb + lane) * TB_XS + jc + c];
+                if (!UPPER) {
+#pragma unroll
+                    for (int l = 0; l < 32; l++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const float xl = __shfl_sync(0xffffffffu, x[c], l);
+                            if (lane > l) x[c] -= lrow[l] * xl;
+                        }
+                } else {
+#pragma unroll
+                    for (int l = 31; l >= 0; l--) {
+                        const float dl = __shfl_sync(0xffffffffu, lrow[l], l);
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const float xl = __shfl_sync(0xffffffffu, x[c], l) / dl;
+                            if (lane == l) x[c] = xl;
+                            else if (lane < l) x[c] -= lrow[l] * xl;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 4; c++) X[(rb + lane) * TB_XS + jc + c] = x[c];
+            }
+        }
+        __syncthreads();
+        // the other rows of the block: below (forward) or above (backward)
+        const int r_lo = UPPER ? 0 : rb + 32, r_hi = UPPER ? rb : TB;
+        if (r_hi > r_lo) {
+            const int j = tid & (TB_COLS - 1), g = tid >> 6;
+            float xb[32];
+#pragma unroll
+            for (int l = 0; l < 32; l++) xb[l] = X[(rb + l) * TB_XS + j];
+#pragma unroll 1
+            for (int r = r_lo + g; r < r_hi; r += 4) {
+                const float4* lr = reinterpret_cast<const float4*>(L + r * TB_LS + rb);
+                float acc = 0.f;
+#pragma unroll
+                for (int m = 0; m < 8; m++) {
+                    const float4 v = lr[m];
+                    acc += v.x * xb[4 * m] + v.y * xb[4 * m + 1] + v.z * xb[4 * m + 2] + v.w * xb[4 * m + 3];
+                }
+                X[r * TB_XS + j] -= acc;
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < TB * TB_COLS; e += 256) {
+        const int r = e & (TB - 1), j = e >> 7;
+        if (r < bw && j < ncols) Xg[r + (int64_t)j * ldx] = X[r * TB_XS + j];
+    }
+}
+
+// rows [k + bw, n) (forward) or [0, k) (backward) of X -= A[rows, k:k+bw] X[k:k+bw, :]
+template <bool UPPER>
+__global__ void __launch_bounds__(tc::THREADS, 2) k_trs_tc(LuBatch<float> B, int64_t k, int* err) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tslot;
+    const int64_t n = B.n[0], ld = B.ld[0], ldx = B.ldx[0];
+    const int nrhs = B.nrhs[0];
+    const int bw = (int)min((int64_t)TB, n - k);
+    const int64_t lo = UPPER ? 0 : k + bw, hi = UPPER ? k : n;
+    const int64_t r0 = lo + (int64_t)blockIdx.x * tc::BM, c0 = (int64_t)blockIdx.y * tc::BN;
+    const float* A = B.A[0];
+    float* X = B.X[0];
+    tc::update_tile<3>(A + r0 + k * ld, ld, X + k + c0 * ldx, ldx, X + r0 + c0 * ldx, ldx,
+                       (int)min((int64_t)tc::BM, hi - r0), (int)min((int64_t)tc::BN, (int64_t)nrhs - c0), bw, tc_smem,
+                       bar, &tslot, err);
+}
+
 template <class T>
-int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st) {
+int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st, int* err) {
     GB_REQUIRE(sizeof(T) * (size_t)n <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld too large", (long long)n);
     k_perm_apply<T><<<nrhs, 256, sizeof(T) * n, st>>>(B);
     GB_LAUNCH_CHECK();
+    if constexpr (sizeof(T) == 4) {
+        if (err) {  // tensor cores available: 128-row blocks
+            const unsigned cb = (unsigned)cdiv(nrhs, TB_COLS), ct = (unsigned)cdiv(nrhs, tc::BN);
+            for (int64_t k = 0; k < n; k += TB) {
+                k_trs_block<false><<<cb, 256, trs_block_smem(), st>>>(B, k);
+                GB_LAUNCH_CHECK();
+                if (k + TB < n) {
+                    k_trs_tc<false><<<dim3((unsigned)cdiv(n - k - TB, tc::BM), ct), tc::THREADS, tc::SMEM_BYTES, st>>>(
+                        B, k, err);
+                    GB_LAUNCH_CHECK();
+                }
+            }
+            for (int64_t k = ((n - 1) / TB) * TB; k >= 0; k -= TB) {
+                k_trs_block<true><<<cb, 256, trs_block_smem(), st>>>(B, k);
+                GB_LAUNCH_CHECK();
+                if (k > 0) {
+                    k_trs_tc<true><<<dim3((unsigned)cdiv(k, tc::BM), ct), tc::THREADS, tc::SMEM_BYTES, st>>>(B, k, err);
+                    GB_LAUNCH_CHECK();
+                }
+            }
+            return GBVLM_OK;
+        }
+    }
     const unsigned qb = (unsigned)cdiv(nrhs, 8);
     for (int64_t k = 0; k < n; k += GK) {
         k_trs_diag<T><<<1, 256, 0, st>>>(B, k, 0);
@@ -923,14 +1105,14 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
 template <class T, int NT>
 static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
     if (g.csize == 1) {
-        k_panel_reg<T, NT, false><<<g.count, NT, 0, st>>>(B, k, act, g.slab);
+        k_panel_reg<T, NT, false><<<g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(B, k, act, g.slab);
         GB_LAUNCH_CHECK();
         return GBVLM_OK;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(g.count * g.csize));
     cfg.blockDim = dim3(NT);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = sizeof(PanelSmem<T, NT, true>);
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1041,18 +1223,18 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
         }
     }
     if (plan.nsys > 0) {
-        k_perm<T><<<plan.nsys, 256, sizeof(int32_t) * std::min<int64_t>(plan.maxn, PERM_SMEM), st>>>(B);
+        k_perm<T><<<plan.nsys, 256, sizeof(int32_t) * std::min<int64_t>(plan.maxn, PERM_SMEM), st>>>(B, plan.base);
         GB_LAUNCH_CHECK();
     }
     return GBVLM_OK;
 }
 
 template <class T>
-int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st) {
+int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st, int* err) {
     // X of the largest system in shared memory when it fits, else staged per column
     const size_t full = sizeof(T) * (size_t)maxn * TS_MAXRHS;
     const int use_smem = full <= (size_t)TS_SMEM_BYTES ? 1 : 0;
-    if (!use_smem && nsys == 1) return lu_large_solve<T>(B, maxn, max_nrhs, st);
+    if (!use_smem && nsys == 1) return lu_large_solve<T>(B, maxn, max_nrhs, st, err);
     const size_t smem = use_smem ? full : sizeof(T) * (size_t)maxn;
     GB_REQUIRE(smem <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld needs %zu bytes of shared memory",
                (long long)maxn, smem);
@@ -1065,13 +1247,14 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t 
 
 template int lu_batch_factor<float>(const LuBatch<float>&, const LuPlan&, cudaStream_t);
 template int lu_batch_factor<double>(const LuBatch<double>&, const LuPlan&, cudaStream_t);
-template int lu_batch_solve<float>(const LuBatch<float>&, int32_t, int32_t, int64_t, cudaStream_t);
-template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, int64_t, cudaStream_t);
+template int lu_batch_solve<float>(const LuBatch<float>&, int32_t, int32_t, int64_t, cudaStream_t, int*);
+template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, int64_t, cudaStream_t, int*);
 
 // Build the per-step tables.  Systems must be sorted by n descending so the
 // active systems of every step form a prefix of the order.
-int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st) {
+int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st, int32_t base) {
     plan.release();
+    plan.base = base;
     GB_CUDA(cudaFuncSetAttribute(k_trsolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_trsolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, TS_SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(k_perm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM * 4));
@@ -1099,13 +1282,25 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             GB_CUDA(cudaFuncSetAttribute(k_update_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsm_wide_smem<LU_OUTER>()));
+            GB_CUDA(cudaFuncSetAttribute(k_trs_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trs_block_smem()));
+            GB_CUDA(cudaFuncSetAttribute(k_trs_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trs_block_smem()));
+            GB_CUDA(cudaFuncSetAttribute(k_trs_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_trs_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
         }
         GB_CUDA(cudaMalloc(&plan.d_err, sizeof(int)));
         GB_CUDA(cudaMemsetAsync(plan.d_err, 0, sizeof(int), st));
     }
-    // largest cluster the device schedules for the register panel (16 needs the non-portable opt-in)
-    plan.cluster = 1;
-    {
+    // largest cluster the device schedules for the register panel (16 needs the
+    // non-portable opt-in), probed once per device
+    static std::mutex probe_mu;
+    static int probed[64];
+    int dev_id = 0;
+    GB_CUDA(cudaGetDevice(&dev_id));
+    std::lock_guard<std::mutex> probe_lock(probe_mu);
+    plan.cluster = dev_id < 64 && probed[dev_id] ? probed[dev_id] : 1;
+    if (dev_id >= 64 || !probed[dev_id]) {
         cudaFuncSetAttribute(k_panel_reg<float, 1024, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaFuncSetAttribute(k_panel_reg<float, 512, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaFuncSetAttribute(k_panel_reg<float, 256, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1115,7 +1310,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(c);
             cfg.blockDim = dim3(1024);
-            cfg.dynamicSmemBytes = 0;
+            cfg.dynamicSmemBytes = sizeof(PanelSmem<float, 1024, true>);
             cudaLaunchAttribute at[1];
             at[0].id = cudaLaunchAttributeClusterDimension;
             at[0].val.clusterDim.x = c;
@@ -1126,6 +1321,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             int n2 = 0, n1 = 0;
             const bool ok2 = cudaOccupancyMaxActiveClusters(&n2, k_panel_reg<float, 1024, true>, &cfg) == cudaSuccess;
             cfg.blockDim = dim3(PR_THREADS_F64);
+            cfg.dynamicSmemBytes = sizeof(PanelSmem<double, PR_THREADS_F64, true>);
             const bool ok1 = cudaOccupancyMaxActiveClusters(&n1, k_panel_reg<double, PR_THREADS_F64, true>, &cfg) == cudaSuccess;
             if (ok2 && ok1 && n2 > 0 && n1 > 0) {
                 plan.cluster = c;
@@ -1133,6 +1329,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             }
             cudaGetLastError();
         }
+        if (dev_id < 64) probed[dev_id] = plan.cluster;
     }
     const int nsys = (int)n_sorted.size();
     for (int i = 1; i < nsys; i++) GB_REQUIRE(n_sorted[i] <= n_sorted[i - 1], "lu plan: sizes not sorted");
@@ -1145,7 +1342,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         S.act_off = (int64_t)act.size();
         int cnt = 0;
         while (cnt < nsys && n_sorted[cnt] > k) cnt++;
-        for (int i = 0; i < cnt; i++) act.push_back(i);
+        for (int i = 0; i < cnt; i++) act.push_back(base + i);
         S.n_panel = cnt;
         for (int e = 0; e < 2; e++) {
             // rows per CTA = threads per CTA (one row per thread; 32 doubles per thread cap the f64 CTA at 256)
@@ -1475,7 +1672,7 @@ static int lu_solve_one(gbvlm_lu h, const T* A, int64_t n, int64_t ld, T* X, int
     int rc = make_single_batch<T>(B, n, ld, (T*)A, h->d_ipiv, h->d_perm, h->d_info, X, ldx, (int32_t)nrhs,
                                   &h->work, &h->work_bytes, st);
     if (rc) return rc;
-    return lu_batch_solve<T>(B, 1, (int32_t)nrhs, n, st);
+    return lu_batch_solve<T>(B, 1, (int32_t)nrhs, n, st, h->plan.tc_passes ? h->plan.d_err : nullptr);
 }
 
 extern "C" {

@@ -59,6 +59,7 @@ struct LuStep {
 struct LuPlan {
     std::vector<LuStep> steps;
     int32_t nsys = 0;
+    int32_t base = 0;  // the plan's systems are [base, base + nsys) of the batch tables
     int64_t maxn = 0;
     int cluster = 1;  // largest cluster the register panel can be launched with
     int tc_passes = 0;  // float trailing update: 0 CUDA cores, 1 TF32, 3 3xTF32 tensor cores
@@ -81,15 +82,18 @@ struct LuPlan {
     LuPlan& operator=(const LuPlan&) = delete;
 };
 
-int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st);
+// n_sorted: sizes of systems [base, base + n_sorted.size()) of the batch, descending
+int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream_t st, int32_t base = 0);
 // GBVLM_OK, or an error if a tensor-core update gave up waiting (synchronises st)
 int lu_plan_check(const LuPlan& plan, cudaStream_t st);
 // number of kernel launches lu_batch_factor makes for element size es (4 or 8)
 int64_t lu_plan_launches(const LuPlan& plan, int es);
 template <class T>
 int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st);
+// err: the tensor-core error word of a plan with tensor cores (a single large
+// float system then solves in 128-row blocks on the tensor cores), or null
 template <class T>
-int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st);
+int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st, int* err);
 
 // Single-system tables packed in a small device buffer (*work, grown on demand).
 template <class T>

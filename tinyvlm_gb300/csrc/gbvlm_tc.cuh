@@ -161,12 +161,12 @@ __device__ __forceinline__ void st_shared_f32(uint32_t addr, float a) {
 }
 
 // One 128 x 128 tile: C(r0.., c0..) -= L(r0.., 0..K) * U(0..K, c0..).
-//   L(r, kk) = Lp[r + kk * ld], U(kk, c) = Up[kk + c * ld], C(r, c) = Cp[r + c * ld];
+//   L(r, kk) = Lp[r + kk * ldl], U(kk, c) = Up[kk + c * ldu], C(r, c) = Cp[r + c * ldc];
 //   rows r < m_rows and columns c < n_cols exist (tile-relative bounds).
 template <int PASSES>
-__device__ __forceinline__ void update_tile(const float* Lp, const float* Up, float* Cp, int64_t ld, int m_rows,
-                                            int n_cols, int K, unsigned char* smem_raw, uint64_t* bar, uint32_t* tslot,
-                                            int* err) {
+__device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const float* Up, int64_t ldu, float* Cp,
+                                            int64_t ldc, int m_rows, int n_cols, int K, unsigned char* smem_raw,
+                                            uint64_t* bar, uint32_t* tslot, int* err) {
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
@@ -201,7 +201,7 @@ __device__ __forceinline__ void update_tile(const float* Lp, const float* Up, fl
                 const bool rv = row < m_rows;
 #pragma unroll
                 for (int kk = 0; kk < 16; kk++)
-                    v[kk] = (rv && kc + kh + kk < K) ? Lp[row + (int64_t)(kc + kh + kk) * ld] : 0.f;
+                    v[kk] = (rv && kc + kh + kk < K) ? Lp[row + (int64_t)(kc + kh + kk) * ldl] : 0.f;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const uint32_t off = sw128_off(row, kh + 4 * j);
@@ -220,7 +220,7 @@ __device__ __forceinline__ void update_tile(const float* Lp, const float* Up, fl
 #pragma unroll
                 for (int cc = 0; cc < 16; cc++) {
                     const int col = 16 * wid + cc;
-                    v[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ld] : 0.f;
+                    v[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ldu] : 0.f;
                 }
 #pragma unroll
                 for (int cc = 0; cc < 16; cc++) {
@@ -269,12 +269,12 @@ __device__ __forceinline__ void update_tile(const float* Lp, const float* Up, fl
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const int col = cb + j;
-                    c[j] = col < n_cols ? Cp[row + (int64_t)col * ld] : 0.f;
+                    c[j] = col < n_cols ? Cp[row + (int64_t)col * ldc] : 0.f;
                 }
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const int col = cb + j;
-                    if (col < n_cols) Cp[row + (int64_t)col * ld] = c[j] - v[j];
+                    if (col < n_cols) Cp[row + (int64_t)col * ldc] = c[j] - v[j];
                 }
             }
         }

@@ -177,7 +177,7 @@ class Server:
         try:
             bs = BatchSolver(cases, mode=self.mode, refine=0)
             bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=(0.25, 0.0, 0.0), stream=stream)
-            bs.run(want_gamma=False, stream=stream)
+            bs.run(want_gamma=False, stream=stream, graph=False)  # solved once: no graph capture
             co, _ = bs.results(stream=stream)
             del bs
         finally:
