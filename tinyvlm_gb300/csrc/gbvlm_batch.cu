@@ -589,14 +589,14 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     // others beside it; the main stream waits for all of them
     if (serial_lu) {
         for (int g = 0; g < h->ngroups; g++) {
-            int rc = lu_batch_factor<float>(h->lub, h->plans[g], st);
+            int rc = lu_batch_factor<float>(h->lub, h->plans[g], st, false);
             if (rc) return rc;
         }
     } else {
         GB_CUDA(cudaEventRecord(h->fork, st));
         for (int g = 0; g < h->ngroups; g++) {
             GB_CUDA(cudaStreamWaitEvent(h->side[g], h->fork, 0));
-            int rc = lu_batch_factor<float>(h->lub, h->plans[g], h->side[g]);
+            int rc = lu_batch_factor<float>(h->lub, h->plans[g], h->side[g], true);
             if (rc) return rc;
             GB_CUDA(cudaEventRecord(h->join[g], h->side[g]));
         }

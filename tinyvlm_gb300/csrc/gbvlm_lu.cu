@@ -656,8 +656,10 @@ __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const i
 // ---------------------------------------------------------------------------
 template <int PASSES>
 __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, int64_t k0, int w, const int32_t* act,
-                                                             const int64_t* pfx, int cnt, int* err) {
-    // outer update of the block [k0, k0 + w): rows and columns [k0 + w, n), K = w
+                                                             const int64_t* pfx, int cnt, int* err, int part) {
+    // outer update of the block [k0, k0 + w): rows and columns [k0 + w, n), K = w.
+    // part 0: all tiles; part 1: the first column of tiles (the next outer
+    // panel, BN = w); part 2: the other columns of tiles
     extern __shared__ __align__(16) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tslot;
@@ -667,7 +669,7 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, 
     float* A = B.A[sid];
     const int64_t lo = k0 + w;  // systems here have n > k0 + w
     const int64_t tiles = (n - lo + tc::BM - 1) / tc::BM;
-    const int64_t t = blockIdx.x - pfx[a];
+    const int64_t t = blockIdx.x - pfx[a] + (part == 2 ? tiles : 0);
     const int64_t r0 = lo + (t % tiles) * tc::BM, c0 = lo + (t / tiles) * tc::BN;
     tc::update_tile<PASSES>(A + r0 + k0 * ld, ld, A + k0 + c0 * ld, ld, A + r0 + c0 * ld, ld,
                             (int)min((int64_t)tc::BM, n - r0), (int)min((int64_t)tc::BN, n - c0), w, tc_smem, bar,
@@ -718,7 +720,7 @@ __global__ void k_perm(LuBatch<T> B, int32_t base) {
 // blocks are solved one warp per right-hand side, a lane per row: after
 // row r is final, lanes below subtract L[l][r] x_r in parallel.
 // ---------------------------------------------------------------------------
-constexpr int TS_THREADS = 256;
+constexpr int TS_THREADS = 512;
 constexpr int TS_MAXRHS = 8;
 
 // acc[q] = sum_l a[l * ld] * xs[l][q] over the nb <= GK columns of a block row;
@@ -1148,7 +1150,9 @@ static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, cons
 // host plan
 // ---------------------------------------------------------------------------
 template <class T>
-int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
+int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bool lookahead) {
+    lookahead = lookahead && plan.la_stream != nullptr && plan.tc_events == nullptr;
+    bool pending = false;  // a lookahead update in flight on plan.la_stream
     for (size_t s = 0; s < plan.steps.size(); s++) {
         const LuStep& S = plan.steps[s];
         if (S.n_panel == 0) continue;
@@ -1191,6 +1195,13 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
             k_update<T><<<(unsigned)S.in_blocks, 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.in_pfx, S.n_in, S.kend, 1);
             GB_LAUNCH_CHECK();
         }
+        if (pending && ((S.bswap_first == 0 && S.bswap_total > 0) || S.tc_blocks > 0)) {
+            // at the block's last step its swaps (and U12 solve) reach the columns the
+            // lookahead update is still working on; systems that end the block earlier
+            // have n <= kend of the previous block + W and no lookahead tiles
+            GB_CUDA(cudaStreamWaitEvent(st, plan.la_join, 0));
+            pending = false;
+        }
         if (S.bswap_total > 0) {
             k_swap2<T><<<(unsigned)cdiv(S.bswap_total, 256), 256, 0, st>>>(
                 B, act + S.bswap_first, plan.d_pfx + S.bswap_pfx, S.n_panel - S.bswap_first, k0, S.kend, 0, k0, S.kend,
@@ -1202,7 +1213,6 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
                 k_trsm_wide<LU_OUTER><<<(unsigned)S.btrsm_blocks, 256, trsm_wide_smem<LU_OUTER>(), st>>>(
                     B, k0, act, plan.d_pfx + S.btrsm_pfx, S.n_tc);
                 GB_LAUNCH_CHECK();
-                const int64_t* pfx = plan.d_pfx + S.tc_pfx;
                 if (plan.tc_events) {
                     cudaEvent_t e0, e1;
                     GB_CUDA(cudaEventCreate(&e0));
@@ -1211,17 +1221,38 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st) {
                     plan.tc_events->push_back(e1);
                     GB_CUDA(cudaEventRecord(e0, st));
                 }
-                if (plan.tc_passes == 1)
-                    k_update_tc<1><<<(unsigned)S.tc_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(B, k0, plan.W, act, pfx,
-                                                                                             S.n_tc, plan.d_err);
-                else
-                    k_update_tc<3><<<(unsigned)S.tc_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(B, k0, plan.W, act, pfx,
-                                                                                             S.n_tc, plan.d_err);
-                GB_LAUNCH_CHECK();
+                auto tc_launch = [&](int64_t blocks, int64_t pfx_off, int part, cudaStream_t s_) {
+                    const int64_t* pfx = plan.d_pfx + pfx_off;
+                    if (plan.tc_passes == 1)
+                        k_update_tc<1><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx,
+                                                                                           S.n_tc, plan.d_err, part);
+                    else
+                        k_update_tc<3><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx,
+                                                                                           S.n_tc, plan.d_err, part);
+                };
+                if (!lookahead) {
+                    tc_launch(S.tc_blocks, S.tc_pfx, 0, st);
+                    GB_LAUNCH_CHECK();
+                } else {
+                    // lookahead: the next outer panel's columns first; the rest of the
+                    // trailing matrix on the side stream while the next block's inner
+                    // steps (confined to that panel) run here
+                    tc_launch(S.tcn_blocks, S.tcn_pfx, 1, st);
+                    GB_LAUNCH_CHECK();
+                    if (S.tcr_blocks > 0) {
+                        GB_CUDA(cudaEventRecord(plan.la_fork, st));
+                        GB_CUDA(cudaStreamWaitEvent(plan.la_stream, plan.la_fork, 0));
+                        tc_launch(S.tcr_blocks, S.tcr_pfx, 2, plan.la_stream);
+                        GB_LAUNCH_CHECK();
+                        GB_CUDA(cudaEventRecord(plan.la_join, plan.la_stream));
+                        pending = true;
+                    }
+                }
                 if (plan.tc_events) GB_CUDA(cudaEventRecord(plan.tc_events->back(), st));
             }
         }
     }
+    if (pending) GB_CUDA(cudaStreamWaitEvent(st, plan.la_join, 0));
     if (plan.nsys > 0) {
         k_perm<T><<<plan.nsys, 256, sizeof(int32_t) * std::min<int64_t>(plan.maxn, PERM_SMEM), st>>>(B, plan.base);
         GB_LAUNCH_CHECK();
@@ -1245,8 +1276,8 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t 
     return GBVLM_OK;
 }
 
-template int lu_batch_factor<float>(const LuBatch<float>&, const LuPlan&, cudaStream_t);
-template int lu_batch_factor<double>(const LuBatch<double>&, const LuPlan&, cudaStream_t);
+template int lu_batch_factor<float>(const LuBatch<float>&, const LuPlan&, cudaStream_t, bool);
+template int lu_batch_factor<double>(const LuBatch<double>&, const LuPlan&, cudaStream_t, bool);
 template int lu_batch_solve<float>(const LuBatch<float>&, int32_t, int32_t, int64_t, cudaStream_t, int*);
 template int lu_batch_solve<double>(const LuBatch<double>&, int32_t, int32_t, int64_t, cudaStream_t, int*);
 
@@ -1291,6 +1322,13 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         }
         GB_CUDA(cudaMalloc(&plan.d_err, sizeof(int)));
         GB_CUDA(cudaMemsetAsync(plan.d_err, 0, sizeof(int), st));
+        if (plan.tc_passes) {  // lookahead stream (lowest priority) and its events
+            int least = 0, greatest = 0;
+            GB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            GB_CUDA(cudaStreamCreateWithPriority(&plan.la_stream, cudaStreamNonBlocking, least));
+            GB_CUDA(cudaEventCreateWithFlags(&plan.la_fork, cudaEventDisableTiming));
+            GB_CUDA(cudaEventCreateWithFlags(&plan.la_join, cudaEventDisableTiming));
+        }
     }
     // largest cluster the device schedules for the register panel (16 needs the
     // non-portable opt-in), probed once per device
@@ -1480,6 +1518,24 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         pfx.push_back(acc);
         S.tc_blocks = acc;
         plan.tc_launches += acc > 0;
+        // the same update split for lookahead: first column of tiles / the rest
+        S.tcn_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < ci; i++) {
+            pfx.push_back(acc);
+            acc += cdiv(n_sorted[i] - S.kend, tc::BM);
+        }
+        pfx.push_back(acc);
+        S.tcn_blocks = acc;
+        S.tcr_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < ci; i++) {
+            pfx.push_back(acc);
+            const int64_t t = cdiv(n_sorted[i] - S.kend, tc::BM);
+            acc += t * (t - 1);
+        }
+        pfx.push_back(acc);
+        S.tcr_blocks = acc;
         plan.steps.push_back(S);
     }
     if (!act.empty()) {
@@ -1517,7 +1573,7 @@ int64_t lu_plan_launches(const LuPlan& plan, int es) {
             n += (S.swap_total > 0) + (S.trsm_blocks > 0) + (S.upd_blocks > 0);
         } else {
             n += (S.iswap_total > 0) + (S.itrsm_blocks > 0) + (S.in_blocks > 0) + (S.bswap_total > 0) +
-                 2 * (S.tc_blocks > 0);
+                 2 * (S.tc_blocks > 0) + (S.tc_blocks > 0 && plan.la_stream && S.tcr_blocks > 0);
         }
     }
     return n + (plan.nsys > 0);  // + the permutation kernel
@@ -1527,9 +1583,14 @@ void LuPlan::release() {
     if (d_act) cudaFree(d_act);
     if (d_pfx) cudaFree(d_pfx);
     if (d_err) cudaFree(d_err);
+    if (la_stream) cudaStreamDestroy(la_stream);
+    if (la_fork) cudaEventDestroy(la_fork);
+    if (la_join) cudaEventDestroy(la_join);
     d_act = nullptr;
     d_pfx = nullptr;
     d_err = nullptr;
+    la_stream = nullptr;
+    la_fork = la_join = nullptr;
     steps.clear();
 }
 
@@ -1651,7 +1712,7 @@ static int lu_factor_one(gbvlm_lu h, T* A, int64_t n, int64_t ld, cudaStream_t s
     LuBatch<T> B;
     rc = make_single_batch<T>(B, n, ld, A, h->d_ipiv, h->d_perm, h->d_info, nullptr, 0, 0, &h->work, &h->work_bytes, st);
     if (rc) return rc;
-    rc = lu_batch_factor<T>(B, h->plan, st);
+    rc = lu_batch_factor<T>(B, h->plan, st, true);
     if (rc) return rc;
     int32_t* hi = (int32_t*)host_scratch(sizeof(int32_t));
     GB_CUDA(cudaMemcpyAsync(hi, h->d_info, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

@@ -54,6 +54,8 @@ struct LuStep {
     int32_t n_tc = 0;                         // systems with n > kend at the block's last step (a prefix)
     int64_t btrsm_pfx = 0, btrsm_blocks = 0;  // U12 = L11^-1 A12, 32 columns per CTA
     int64_t tc_pfx = 0, tc_blocks = 0;        // outer update, 128 x 128 tensor-core tiles
+    int64_t tcn_pfx = 0, tcn_blocks = 0;      // its first column of tiles (the next outer panel)
+    int64_t tcr_pfx = 0, tcr_blocks = 0;      // its other columns of tiles (lookahead)
 };
 
 struct LuPlan {
@@ -75,6 +77,10 @@ struct LuPlan {
     // when set, lu_batch_factor records an event before and after every
     // tensor-core update launch (profiling; not used inside graphs)
     std::vector<cudaEvent_t>* tc_events = nullptr;
+    // lookahead: the part of an outer update right of the next outer panel
+    // runs on la_stream while the next block's inner steps run
+    cudaStream_t la_stream = nullptr;
+    cudaEvent_t la_fork = nullptr, la_join = nullptr;
     void release();
     ~LuPlan() { release(); }
     LuPlan() = default;
@@ -88,8 +94,10 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
 int lu_plan_check(const LuPlan& plan, cudaStream_t st);
 // number of kernel launches lu_batch_factor makes for element size es (4 or 8)
 int64_t lu_plan_launches(const LuPlan& plan, int es);
+// lookahead: overlap each outer update's right part with the next block's
+// inner steps (float, tensor-core plans; ignored while timing launches)
 template <class T>
-int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st);
+int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bool lookahead);
 // err: the tensor-core error word of a plan with tensor cores (a single large
 // float system then solves in 128-row blocks on the tensor cores), or null
 template <class T>
