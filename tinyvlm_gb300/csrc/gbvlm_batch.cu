@@ -304,7 +304,7 @@ __global__ void k_batch_accum(BatchArgs a) {
 // (sh, sl) kept with a compensated addition): about 2^-44 relative per term,
 // where the fp64 units of this part run at a small fraction of the fp32 rate.
 constexpr int RS_THREADS = 128;
-constexpr int RS_MAXRHS = 8;
+constexpr int RS_MAXRHS = 8;  // (the inner loop reads them as two float4)
 constexpr int RS_CB = 32;  // columns of Xd staged per step
 
 // (sh, sl) += a * (xh + xl)
@@ -319,14 +319,16 @@ __device__ __forceinline__ void df_mac(float& sh, float& sl, float a, float xh, 
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, const int64_t* rpfx) {
-    __shared__ float xh[RS_CB][RS_MAXRHS], xl[RS_CB][RS_MAXRHS];
+    __shared__ __align__(16) float xh[RS_CB][RS_MAXRHS];
+    __shared__ __align__(16) float xl[RS_CB][RS_MAXRHS];
     const int si = find_sys(rpfx, a.nsys, blockIdx.x);
     const SysDesc& S = a.sys[si];
     const int64_t r = (blockIdx.x - rpfx[si]) * RS_THREADS + threadIdx.x;
     const int64_t n = S.n;
     const bool rv = r < n;
     const float* arow = S.A2 + (rv ? r : 0);
-    for (int q0 = 0; q0 < S.nrhs; q0 += RS_MAXRHS) {
+    // grid.y: blocks of RS_MAXRHS right-hand sides
+    for (int q0 = blockIdx.y * RS_MAXRHS; q0 < S.nrhs; q0 += RS_MAXRHS * gridDim.y) {
         const int nq = min(RS_MAXRHS, S.nrhs - q0);
         float sh[RS_MAXRHS], sl[RS_MAXRHS];
 #pragma unroll
@@ -347,9 +349,17 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 #pragma unroll
                 for (int cc = 0; cc < RS_CB; cc++) av[cc] = cc < cn ? arow[(c0 + cc) * n] : 0.f;
 #pragma unroll
-                for (int cc = 0; cc < RS_CB; cc++)
+                for (int cc = 0; cc < RS_CB; cc++) {
+                    // the 8 hi and 8 lo values of column cc as four 16-byte broadcasts
+                    const float4 h0 = *reinterpret_cast<const float4*>(&xh[cc][0]);
+                    const float4 h1 = *reinterpret_cast<const float4*>(&xh[cc][4]);
+                    const float4 l0 = *reinterpret_cast<const float4*>(&xl[cc][0]);
+                    const float4 l1 = *reinterpret_cast<const float4*>(&xl[cc][4]);
+                    const float hh[RS_MAXRHS] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+                    const float ll[RS_MAXRHS] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
 #pragma unroll
-                    for (int q = 0; q < RS_MAXRHS; q++) df_mac(sh[q], sl[q], av[cc], xh[cc][q], xl[cc][q]);
+                    for (int q = 0; q < RS_MAXRHS; q++) df_mac(sh[q], sl[q], av[cc], hh[q], ll[q]);
+                }
             }
         }
         if (rv) {
@@ -611,7 +621,8 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     k_batch_accum<<<g, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
     for (int it = 0; it < h->refine; it++) {
-        k_batch_residual<<<(unsigned)h->residual_tiles, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+        k_batch_residual<<<dim3((unsigned)h->residual_tiles, (unsigned)cdiv(maxrhs, RS_MAXRHS)), RS_THREADS, 0, st>>>(
+            a, h->d_rpfx);
         GB_LAUNCH_CHECK();
         rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st, h->plans[0].tc_passes ? h->plans[0].d_err : nullptr);
         if (rc) return rc;

@@ -186,6 +186,9 @@ template <> struct PivKey<float> {
     }
     __device__ __forceinline__ bool operator==(const PivKey& o) const { return m == o.m && l == o.l; }
     __device__ __forceinline__ int pos() const { return (int)~l; }
+    __device__ __forceinline__ static PivKey kmax(const PivKey& a, const PivKey& b) {
+        return (a.m > b.m || (a.m == b.m && a.l > b.l)) ? a : b;
+    }
 };
 template <> struct PivKey<double> {
     uint32_t m, m2, l;
@@ -203,6 +206,9 @@ template <> struct PivKey<double> {
     }
     __device__ __forceinline__ bool operator==(const PivKey& o) const { return m == o.m && m2 == o.m2 && l == o.l; }
     __device__ __forceinline__ int pos() const { return (int)~l; }
+    __device__ __forceinline__ static PivKey kmax(const PivKey& a, const PivKey& b) {
+        return (a.m > b.m || (a.m == b.m && (a.m2 > b.m2 || (a.m2 == b.m2 && a.l > b.l)))) ? a : b;
+    }
 };
 
 // compile-time loop: f(integral_constant<int, I>) for I in [B, E)
@@ -272,7 +278,7 @@ __device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank)
     return o;
 }
 
-template <class T, int NT, bool CLUSTER>
+template <class T, int NT, bool CLUSTER, int RPT>
 __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab) {
     namespace cg = cooperative_groups;
     using Key = PivKey<T>;
@@ -292,16 +298,22 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
     const int nb = (int)min((int64_t)GK, n - k);
     const int rows = (int)(n - k);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int r = rank * slab + tid;
-    int lid = (tid < slab && r < rows) ? r : -1;  // logical position of the own row, -1: no row
 
-    T x[GK];
-    {
+    // own rows: slab-relative tid, tid + NT, ...; lid = logical position, -1: no row
+    int lid[RPT];
+    T x[RPT][GK];
+#pragma unroll
+    for (int i = 0; i < RPT; i++) {
+        const int rr = tid + i * NT, r = rank * slab + rr;
+        lid[i] = (rr < slab && r < rows) ? r : -1;
         const T* src = A + (k + r) + k * ld;
 #pragma unroll
-        for (int t = 0; t < GK; t++) x[t] = (lid >= 0 && t < nb) ? src[t * ld] : (T)0;
+        for (int t = 0; t < GK; t++) x[i][t] = (lid[i] >= 0 && t < nb) ? src[t * ld] : (T)0;
     }
-    Key cand = lid >= 0 ? Key::make(x[0], lid) : Key::none();  // candidate for column 0
+    Key cand = Key::none();  // best candidate of the own rows for the current column
+#pragma unroll
+    for (int i = 0; i < RPT; i++)
+        if (lid[i] >= 0) cand = Key::kmax(cand, Key::make(x[i][0], lid[i]));
 
     static_for<0, GK>([&](auto JJ) {
         constexpr int jj = decltype(JJ)::value;
@@ -310,17 +322,21 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
             // 1. warp candidate; its owner publishes the row
             {
                 const Key w = cand.warp_max();
-                if (lid >= 0 && cand == w) {
-                    using V2 = typename Vec4<T>::type;
+                if (cand == w) {
 #pragma unroll
-                    for (int t = 0; t < GK; t += 4) {
-                        V2 v;
-                        v.x = x[t];
-                        v.y = x[t + 1];
-                        v.z = x[t + 2];
-                        v.w = x[t + 3];
-                        *reinterpret_cast<V2*>(&sm.s_row[buf][wid][t]) = v;
-                    }
+                    for (int i = 0; i < RPT; i++)
+                        if (lid[i] >= 0 && lid[i] == w.pos()) {
+                            using V2 = typename Vec4<T>::type;
+#pragma unroll
+                            for (int t = 0; t < GK; t += 4) {
+                                V2 v;
+                                v.x = x[i][t];
+                                v.y = x[i][t + 1];
+                                v.z = x[i][t + 2];
+                                v.w = x[i][t + 3];
+                                *reinterpret_cast<V2*>(&sm.s_row[buf][wid][t]) = v;
+                            }
+                        }
                 }
                 if (lane == 0) sm.s_key[buf][wid] = w;
             }
@@ -333,34 +349,50 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
                 ipiv[k + jj] = (int32_t)(k + p);  // a store: nothing waits on it
                 if (d == (T)0 && zero_col < 0) zero_col = jj;
             }
-            // 3. interchange of logical positions jj <-> p, then scale and update
-            if (lid == p) lid = jj;
-            else if (lid == jj) lid = p;
-            const bool active = lid > jj;
-            // scale by the reciprocal of the pivot (LAPACK ?getf2), dividing when it is subnormal
-            T lm = x[jj];
-            if (active) {
-                if (tabs(d) >= (sizeof(T) == 4 ? (T)FLT_MIN : (T)DBL_MIN)) lm = lm * ((T)1 / d);
-                else if (d != (T)0) lm = lm / d;
-                x[jj] = lm;
+            // 3. interchange of logical positions jj <-> p, then scale and update;
+            // scaling by the reciprocal of the pivot (LAPACK ?getf2), dividing when it is subnormal
+            const bool big = tabs(d) >= (sizeof(T) == 4 ? (T)FLT_MIN : (T)DBL_MIN);
+            const T rd = big ? (T)1 / d : (T)0;
+            T lm[RPT];
+            bool active[RPT];
+#pragma unroll
+            for (int i = 0; i < RPT; i++) {
+                if (lid[i] == p) lid[i] = jj;
+                else if (lid[i] == jj) lid[i] = p;
+                active[i] = lid[i] > jj;
+                lm[i] = x[i][jj];
+                if (active[i]) {
+                    if (big) lm[i] = lm[i] * rd;
+                    else if (d != (T)0) lm[i] = lm[i] / d;
+                    x[i][jj] = lm[i];
+                }
             }
 #pragma unroll
             for (int t = jj + 1; t < GK; t++) {
                 const T u = __shfl_sync(0xffffffffu, urow, t);
-                if (active) x[t] -= lm * u;
+#pragma unroll
+                for (int i = 0; i < RPT; i++)
+                    if (active[i]) x[i][t] -= lm[i] * u;
             }
-            if constexpr (jj + 1 < GK) cand = active ? Key::make(x[jj + 1], lid) : Key::none();
+            if constexpr (jj + 1 < GK) {
+                cand = Key::none();
+#pragma unroll
+                for (int i = 0; i < RPT; i++)
+                    if (active[i]) cand = Key::kmax(cand, Key::make(x[i][jj + 1], lid[i]));
+            }
         }
     });
     if constexpr (CLUSTER) cg::this_cluster().sync();  // no CTA leaves while its rows may still be read
     // panels of a system run in order, so the first zero pivot recorded is the first of the factorisation
     if (zero_col >= 0) atomicCAS(&B.info[sid], 0, (int32_t)(k + zero_col + 1));
-    if (lid >= 0) {
-        T* dst = A + (k + lid) + k * ld;
 #pragma unroll
-        for (int t = 0; t < GK; t++)
-            if (t < nb) dst[t * ld] = x[t];
-    }
+    for (int i = 0; i < RPT; i++)
+        if (lid[i] >= 0) {
+            T* dst = A + (k + lid[i]) + k * ld;
+#pragma unroll
+            for (int t = 0; t < GK; t++)
+                if (t < nb) dst[t * ld] = x[i][t];
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -991,12 +1023,17 @@ __global__ void __launch_bounds__(256, 2) k_trs_block(LuBatch<float> B, int64_t 
                             if (lane > l) x[c] -= lrow[l] * xl;
                         }
                 } else {
+                    // each lane's reciprocal of its own diagonal entry, computed once
+                    float dinv = 0.f;
+#pragma unroll
+                    for (int l = 0; l < 32; l++)
+                        if (lane == l) dinv = 1.f / lrow[l];
 #pragma unroll
                     for (int l = 31; l >= 0; l--) {
-                        const float dl = __shfl_sync(0xffffffffu, lrow[l], l);
+                        const float rl = __shfl_sync(0xffffffffu, dinv, l);
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const float xl = __shfl_sync(0xffffffffu, x[c], l) / dl;
+                            const float xl = __shfl_sync(0xffffffffu, x[c], l) * rl;
                             if (lane == l) x[c] = xl;
                             else if (lane < l) x[c] -= lrow[l] * xl;
                         }
@@ -1104,10 +1141,10 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
 // ---------------------------------------------------------------------------
 // panel launch: register panel with the thread count of the group
 // ---------------------------------------------------------------------------
-template <class T, int NT>
+template <class T, int NT, int RPT>
 static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
     if (g.csize == 1) {
-        k_panel_reg<T, NT, false><<<g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(B, k, act, g.slab);
+        k_panel_reg<T, NT, false, RPT><<<g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(B, k, act, g.slab);
         GB_LAUNCH_CHECK();
         return GBVLM_OK;
     }
@@ -1123,7 +1160,7 @@ static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, c
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true>, B, k, act, g.slab));
+    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true, RPT>, B, k, act, g.slab));
     return GBVLM_OK;
 }
 
@@ -1134,15 +1171,16 @@ static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, cons
         GB_LAUNCH_CHECK();
         return GBVLM_OK;
     }
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (sizeof(T) == 4) {  // one row per thread (two per thread measured slower: longer
+                                     // per-thread chains, fewer warps to hide them)
         switch (g.nt) {
-            case 128: return launch_panel_nt<T, 128>(B, k, act, g, st);
-            case 256: return launch_panel_nt<T, 256>(B, k, act, g, st);
-            case 512: return launch_panel_nt<T, 512>(B, k, act, g, st);
-            default: return launch_panel_nt<T, 1024>(B, k, act, g, st);
+            case 128: return launch_panel_nt<T, 128, 1>(B, k, act, g, st);
+            case 256: return launch_panel_nt<T, 256, 1>(B, k, act, g, st);
+            case 512: return launch_panel_nt<T, 512, 1>(B, k, act, g, st);
+            default: return launch_panel_nt<T, 1024, 1>(B, k, act, g, st);
         }
     } else {
-        return launch_panel_nt<T, PR_THREADS_F64>(B, k, act, g, st);
+        return launch_panel_nt<T, PR_THREADS_F64, 1>(B, k, act, g, st);
     }
 }
 
@@ -1339,11 +1377,11 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     std::lock_guard<std::mutex> probe_lock(probe_mu);
     plan.cluster = dev_id < 64 && probed[dev_id] ? probed[dev_id] : 1;
     if (dev_id >= 64 || !probed[dev_id]) {
-        cudaFuncSetAttribute(k_panel_reg<float, 1024, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaFuncSetAttribute(k_panel_reg<float, 512, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaFuncSetAttribute(k_panel_reg<float, 256, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaFuncSetAttribute(k_panel_reg<float, 128, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaFuncSetAttribute(k_panel_reg<double, PR_THREADS_F64, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 1024, true, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 512, true, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 256, true, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<float, 128, true, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_panel_reg<double, PR_THREADS_F64, true, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         for (int c : {16, 8, 4, 2}) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(c);
@@ -1357,10 +1395,11 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             cfg.attrs = at;
             cfg.numAttrs = 1;
             int n2 = 0, n1 = 0;
-            const bool ok2 = cudaOccupancyMaxActiveClusters(&n2, k_panel_reg<float, 1024, true>, &cfg) == cudaSuccess;
+            const bool ok2 = cudaOccupancyMaxActiveClusters(&n2, k_panel_reg<float, 1024, true, 1>, &cfg) == cudaSuccess;
             cfg.blockDim = dim3(PR_THREADS_F64);
             cfg.dynamicSmemBytes = sizeof(PanelSmem<double, PR_THREADS_F64, true>);
-            const bool ok1 = cudaOccupancyMaxActiveClusters(&n1, k_panel_reg<double, PR_THREADS_F64, true>, &cfg) == cudaSuccess;
+            const bool ok1 =
+                cudaOccupancyMaxActiveClusters(&n1, k_panel_reg<double, PR_THREADS_F64, true, 1>, &cfg) == cudaSuccess;
             if (ok2 && ok1 && n2 > 0 && n1 > 0) {
                 plan.cluster = c;
                 break;
@@ -1383,7 +1422,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         for (int i = 0; i < cnt; i++) act.push_back(base + i);
         S.n_panel = cnt;
         for (int e = 0; e < 2; e++) {
-            // rows per CTA = threads per CTA (one row per thread; 32 doubles per thread cap the f64 CTA at 256)
+            // rows per CTA = threads (one row per thread in registers): float up to 1024, double 256
             const int64_t slab_max = e == 0 ? 1024 : PR_THREADS_F64;
             S.panels[e].clear();
             int i = 0;
