@@ -500,8 +500,8 @@ __global__ void __launch_bounds__(TRSM_COLS) k_trsm(LuBatch<T> B, int64_t k, con
 // for the columns right of the block, L11 the WW x WW unit lower triangle.
 // One CTA per TW_COLS columns: L11 and the columns in shared memory, solved
 // in 32-row blocks:
-//   * diagonal block: a warp per column, a lane per row holding its row of
-//     the 32 x 32 block in registers, four columns in flight per warp;
+//   * diagonal block: a lane per row holding its row of the 32 x 32 block
+//     in registers, eight columns in flight per warp (8 warps x 8 columns);
 //   * rows below: thread (column j, row group g) keeps the 32 solved values
 //     of column j in registers and sweeps rows g, g+4, ... with the L rows
 //     read as float4 broadcasts.
@@ -517,6 +517,7 @@ template <int WW>
 __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t k0, const int32_t* act,
                                                      const int64_t* pfx, int cnt) {
     static_assert(WW == LU_OUTER, "row stride sized for the outer block");
+    static_assert(TW_COLS == 8 * 8, "eight warps of eight columns");
     extern __shared__ __align__(16) float tw_smem[];
     float* L = tw_smem;            // L[r * TW_LS + c]
     float* X = L + WW * TW_LS;     // X[r * TW_XS + j]
@@ -545,22 +546,21 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
             float lrow[32];
 #pragma unroll
             for (int l = 0; l < 32; l++) lrow[l] = L[(rb + lane) * TW_LS + rb + l];
-#pragma unroll 1
-            for (int j0 = 4 * wid; j0 < TW_COLS; j0 += 32) {
-                float x[4];
+            // warp w: columns 8w..8w+7, all eight in flight
+            const int j0 = 8 * wid;
+            float x[8];
 #pragma unroll
-                for (int c = 0; c < 4; c++) x[c] = X[(rb + lane) * TW_XS + j0 + c];
+            for (int c = 0; c < 8; c++) x[c] = X[(rb + lane) * TW_XS + j0 + c];
 #pragma unroll
-                for (int l = 0; l < 32; l++) {
+            for (int l = 0; l < 32; l++) {
 #pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const float xl = __shfl_sync(0xffffffffu, x[c], l);
-                        if (lane > l) x[c] -= lrow[l] * xl;
-                    }
+                for (int c = 0; c < 8; c++) {
+                    const float xl = __shfl_sync(0xffffffffu, x[c], l);
+                    if (lane > l) x[c] -= lrow[l] * xl;
                 }
-#pragma unroll
-                for (int c = 0; c < 4; c++) X[(rb + lane) * TW_XS + j0 + c] = x[c];
             }
+#pragma unroll
+            for (int c = 0; c < 8; c++) X[(rb + lane) * TW_XS + j0 + c] = x[c];
         }
         __syncthreads();
         // rows below the block
@@ -706,6 +706,37 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, 
     tc::update_tile<PASSES>(A + r0 + k0 * ld, ld, A + k0 + c0 * ld, ld, A + r0 + c0 * ld, ld,
                             (int)min((int64_t)tc::BM, n - r0), (int)min((int64_t)tc::BN, n - c0), w, tc_smem, bar,
                             &tslot, err);
+}
+
+// persistent warp-specialised form of k_update_tc (gbvlm_tc.cuh): one CTA per
+// SM over the same tile list; tile blk of the launch is prefix block blk
+template <int PASSES>
+__global__ void __launch_bounds__(tc::P_THREADS, 1) k_update_tcp(LuBatch<float> B, int64_t k0, int w, const int32_t* act,
+                                                                const int64_t* pfx, int cnt, int* err, int part,
+                                                                int64_t ntiles) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    auto job = [&](int64_t blk) {
+        const int a = find_block(pfx, cnt, blk);
+        const int32_t sid = act[a];
+        const int64_t n = B.n[sid], ld = B.ld[sid];
+        float* A = B.A[sid];
+        const int64_t lo = k0 + w;
+        const int64_t tiles = (n - lo + tc::BM - 1) / tc::BM;
+        const int64_t t = blk - pfx[a] + (part == 2 ? tiles : 0);
+        const int64_t r0 = lo + (t % tiles) * tc::BM, c0 = lo + (t / tiles) * tc::BN;
+        tc::TileJob J;
+        J.Lp = A + r0 + k0 * ld;
+        J.ldl = ld;
+        J.Up = A + k0 + c0 * ld;
+        J.ldu = ld;
+        J.Cp = A + r0 + c0 * ld;
+        J.ldc = ld;
+        J.m_rows = (int)min((int64_t)tc::BM, n - r0);
+        J.n_cols = (int)min((int64_t)tc::BN, n - c0);
+        J.K = w;
+        return J;
+    };
+    tc::update_persistent<PASSES>(ntiles, job, tc_smem, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1089,6 +1120,56 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_trs_tc(LuBatch<float> B, int
                        bar, &tslot, err);
 }
 
+// persistent form of k_trs_tc: tile blk = (row tile blk % nrt, right-hand-side tile blk / nrt)
+template <bool UPPER>
+__global__ void __launch_bounds__(tc::P_THREADS, 1) k_trs_tcp(LuBatch<float> B, int64_t k, int* err, int64_t nrt,
+                                                             int64_t ntiles) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    const int64_t n = B.n[0], ld = B.ld[0], ldx = B.ldx[0];
+    const int nrhs = B.nrhs[0];
+    const int bw = (int)min((int64_t)TB, n - k);
+    const int64_t lo = UPPER ? 0 : k + bw, hi = UPPER ? k : n;
+    const float* A = B.A[0];
+    float* X = B.X[0];
+    auto job = [&](int64_t blk) {
+        const int64_t r0 = lo + (blk % nrt) * tc::BM, c0 = (blk / nrt) * tc::BN;
+        tc::TileJob J;
+        J.Lp = A + r0 + k * ld;
+        J.ldl = ld;
+        J.Up = X + k + c0 * ldx;
+        J.ldu = ldx;
+        J.Cp = X + r0 + c0 * ldx;
+        J.ldc = ldx;
+        J.m_rows = (int)min((int64_t)tc::BM, hi - r0);
+        J.n_cols = (int)min((int64_t)tc::BN, (int64_t)nrhs - c0);
+        J.K = bw;
+        return J;
+    };
+    tc::update_persistent<3>(ntiles, job, tc_smem, err);
+}
+
+static int tc_num_sms() {
+    static int sms[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && sms[dev]) return sms[dev];
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (v <= 0) v = 1;
+    if (dev < 64) sms[dev] = v;
+    return v;
+}
+
+// GBVLM_TC_PERSISTENT=1 selects the persistent warp-specialised update
+static bool tc_persistent() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("GBVLM_TC_PERSISTENT");
+        mode = (e && atoi(e) == 1) ? 1 : 0;
+    }
+    return mode == 1;
+}
+
 template <class T>
 int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st, int* err) {
     GB_REQUIRE(sizeof(T) * (size_t)n <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld too large", (long long)n);
@@ -1101,8 +1182,14 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
                 k_trs_block<false><<<cb, 256, trs_block_smem(), st>>>(B, k);
                 GB_LAUNCH_CHECK();
                 if (k + TB < n) {
-                    k_trs_tc<false><<<dim3((unsigned)cdiv(n - k - TB, tc::BM), ct), tc::THREADS, tc::SMEM_BYTES, st>>>(
-                        B, k, err);
+                    const int64_t nrt = cdiv(n - k - TB, tc::BM);
+                    if (tc_persistent()) {
+                        const int64_t nt = nrt * ct;
+                        k_trs_tcp<false><<<(unsigned)std::min<int64_t>(nt, tc_num_sms()), tc::P_THREADS, tc::P_SMEM_BYTES,
+                                           st>>>(B, k, err, nrt, nt);
+                    } else {
+                        k_trs_tc<false><<<dim3((unsigned)nrt, ct), tc::THREADS, tc::SMEM_BYTES, st>>>(B, k, err);
+                    }
                     GB_LAUNCH_CHECK();
                 }
             }
@@ -1110,7 +1197,14 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
                 k_trs_block<true><<<cb, 256, trs_block_smem(), st>>>(B, k);
                 GB_LAUNCH_CHECK();
                 if (k > 0) {
-                    k_trs_tc<true><<<dim3((unsigned)cdiv(k, tc::BM), ct), tc::THREADS, tc::SMEM_BYTES, st>>>(B, k, err);
+                    const int64_t nrt = cdiv(k, tc::BM);
+                    if (tc_persistent()) {
+                        const int64_t nt = nrt * ct;
+                        k_trs_tcp<true><<<(unsigned)std::min<int64_t>(nt, tc_num_sms()), tc::P_THREADS, tc::P_SMEM_BYTES,
+                                          st>>>(B, k, err, nrt, nt);
+                    } else {
+                        k_trs_tc<true><<<dim3((unsigned)nrt, ct), tc::THREADS, tc::SMEM_BYTES, st>>>(B, k, err);
+                    }
                     GB_LAUNCH_CHECK();
                 }
             }
@@ -1261,6 +1355,16 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
                 }
                 auto tc_launch = [&](int64_t blocks, int64_t pfx_off, int part, cudaStream_t s_) {
                     const int64_t* pfx = plan.d_pfx + pfx_off;
+                    if (tc_persistent()) {
+                        const unsigned grid = (unsigned)std::min<int64_t>(blocks, tc_num_sms());
+                        if (plan.tc_passes == 1)
+                            k_update_tcp<1><<<grid, tc::P_THREADS, tc::P_SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx, S.n_tc,
+                                                                                        plan.d_err, part, blocks);
+                        else
+                            k_update_tcp<3><<<grid, tc::P_THREADS, tc::P_SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx, S.n_tc,
+                                                                                        plan.d_err, part, blocks);
+                        return;
+                    }
                     if (plan.tc_passes == 1)
                         k_update_tc<1><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx,
                                                                                            S.n_tc, plan.d_err, part);
@@ -1357,6 +1461,10 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
                                          (int)trs_block_smem()));
             GB_CUDA(cudaFuncSetAttribute(k_trs_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
             GB_CUDA(cudaFuncSetAttribute(k_trs_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tcp<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::P_SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tcp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::P_SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_trs_tcp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::P_SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_trs_tcp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::P_SMEM_BYTES));
         }
         GB_CUDA(cudaMalloc(&plan.d_err, sizeof(int)));
         GB_CUDA(cudaMemsetAsync(plan.d_err, 0, sizeof(int), st));

@@ -288,3 +288,251 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
 
 }  // namespace tc
 }  // namespace gbvlm
+
+namespace gbvlm {
+
+// ===========================================================================
+// Persistent, warp-specialised form of the same update.  One CTA per SM walks
+// the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; its warps split the work
+//   warps 0-7   producers in two groups of four: group g fills stage g for
+//               the chunks g, g+2, ... (hi/lo split into shared memory)
+//   warp 8      one thread issues the MMAs of a tile into one of two
+//               accumulators in tensor memory (tfull/tempty per accumulator)
+//   warps 9-12  epilogue: the tile's C is copied to shared memory with
+//               cp.async while the MMAs run; then C - acc is stored and the
+//               accumulator released
+// so operand loads, MMAs and the C read-modify-write overlap, with the C
+// reads in flight as asynchronous copies.  Every wait is bounded; a role that
+// gives up raises a shared abort flag that ends the others' waits, the MMA
+// thread drains its MMAs, and the CTA frees its tensor memory and sets the
+// error word.
+// ===========================================================================
+namespace tc {
+
+constexpr int PSTAGES = 2;  // one per producer group
+constexpr int P_GROUP_WARPS = 4;
+constexpr int P_PROD_WARPS = PSTAGES * P_GROUP_WARPS, P_EPI_WARPS = 4;
+constexpr int P_MMA_WARP = P_PROD_WARPS;
+constexpr int P_THREADS = (P_PROD_WARPS + 1 + P_EPI_WARPS) * 32;
+constexpr int C_TILE_BYTES = BM * BN * 4;  // C staged column-major, [col][row]
+constexpr int P_SMEM_BYTES = PSTAGES * STAGE_BYTES + C_TILE_BYTES + 1024;
+constexpr int P_TMEM_COLS = 2 * BN;
+
+// C(r, c) -= sum_kk L(r, kk) U(kk, c) for r < m_rows, c < n_cols (tile-relative)
+struct TileJob {
+    const float* Lp;
+    int64_t ldl;
+    const float* Up;
+    int64_t ldu;
+    float* Cp;
+    int64_t ldc;
+    int m_rows, n_cols, K;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ float ld_shared_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
+// bounded wait that also ends when another role has aborted
+__device__ __forceinline__ bool pwait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (global_ns() - t0 > WAIT_NS) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+template <int PASSES, class JobOf>
+__device__ __forceinline__ void update_persistent(int64_t ntiles, JobOf job_of, unsigned char* smem_raw, int* err) {
+    __shared__ __align__(8) uint64_t full[PSTAGES], empty[PSTAGES], tfull[2], tempty[2], drain;
+    __shared__ uint32_t tslot;
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    const uint32_t cbuf = base + PSTAGES * STAGE_BYTES;
+    if (wid == 0) {
+        tmem_alloc(&tslot, P_TMEM_COLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < PSTAGES; i++) {
+            mbar_init(&full[i], P_GROUP_WARPS * 32);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], P_EPI_WARPS * 32);
+        }
+        mbar_init(&drain, 1);
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = tslot;
+    constexpr uint32_t idesc = idesc_tf32(BM, BN);
+
+    if (wid < P_PROD_WARPS) {
+        // ---- producers: group pg fills stage pg for the chunks pg, pg+2, ... ----
+        const int pg = wid / P_GROUP_WARPS, pw = wid % P_GROUP_WARPS, ptid = tid % (P_GROUP_WARPS * 32);
+        const uint32_t a_hi = base + pg * STAGE_BYTES, a_lo = a_hi + CHUNK_BYTES;
+        const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+        int g = 0;    // chunk counter over all tiles
+        int use = 0;  // this group's uses of its stage
+        bool ok = true;
+        for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            const TileJob J = job_of(t);
+            const int nch = (J.K + BK - 1) / BK;
+            for (int c = 0; c < nch; c++, g++) {
+                if (g % PSTAGES != pg) continue;
+                if (!pwait(&empty[pg], (use & 1) ^ 1, &abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                use++;
+                const int kc = c * BK;
+                // A chunk: thread = tile row, its 32 K values (coalesced across the warp per K)
+                {
+                    float va[BK];
+                    const bool rv = ptid < J.m_rows;
+#pragma unroll
+                    for (int kk = 0; kk < BK; kk++)
+                        va[kk] = (rv && kc + kk < J.K) ? J.Lp[ptid + (int64_t)(kc + kk) * J.ldl] : 0.f;
+#pragma unroll
+                    for (int j = 0; j < BK / 4; j++) {
+                        const uint32_t off = sw128_off(ptid, 4 * j);
+                        const float h0 = tf32_hi(va[4 * j]), h1 = tf32_hi(va[4 * j + 1]);
+                        const float h2 = tf32_hi(va[4 * j + 2]), h3 = tf32_hi(va[4 * j + 3]);
+                        st_shared_v4(a_hi + off, h0, h1, h2, h3);
+                        if (PASSES > 1)
+                            st_shared_v4(a_lo + off, va[4 * j] - h0, va[4 * j + 1] - h1, va[4 * j + 2] - h2,
+                                         va[4 * j + 3] - h3);
+                    }
+                }
+                // B chunk: warp pw covers tile columns 32pw..32pw+31, lane = K index
+                {
+                    float vb[32];
+                    const bool kv = kc + lane < J.K;
+#pragma unroll
+                    for (int cc = 0; cc < 32; cc++) {
+                        const int col = 32 * pw + cc;
+                        vb[cc] = (kv && col < J.n_cols) ? J.Up[(kc + lane) + (int64_t)col * J.ldu] : 0.f;
+                    }
+#pragma unroll
+                    for (int cc = 0; cc < 32; cc++) {
+                        const uint32_t off = sw128_off(32 * pw + cc, lane);
+                        const float h = tf32_hi(vb[cc]);
+                        st_shared_f32(b_hi + off, h);
+                        if (PASSES > 1) st_shared_f32(b_lo + off, vb[cc] - h);
+                    }
+                }
+                fence_async_smem();  // generic-proxy stores visible to the tensor core
+                mbar_arrive(&full[pg]);
+            }
+        }
+    } else if (wid == P_MMA_WARP) {
+        // ---- MMA issuer ------------------------------------------------------
+        if (lane == 0) {
+            int g = 0, li = 0;
+            int uses[PSTAGES] = {};
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, li++) {
+                const TileJob J = job_of(t);
+                const int nch = (J.K + BK - 1) / BK;
+                const int acc = li & 1;
+                if (!pwait(&tempty[acc], ((li >> 1) & 1) ^ 1, &abort_flag)) break;
+                fence_after_sync();
+                const uint32_t d = tmem + (uint32_t)(acc * BN);
+                for (int c = 0; c < nch; c++, g++) {
+                    const int s = g % PSTAGES;
+                    if (!pwait(&full[s], uses[s] & 1, &abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    uses[s]++;
+                    fence_after_sync();
+                    const uint32_t a_hi = base + s * STAGE_BYTES, a_lo = a_hi + CHUNK_BYTES;
+                    const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+#pragma unroll
+                    for (int ks = 0; ks < BK / 8; ks++) {
+                        const uint64_t ah = sw128_desc(a_hi + ks * 32), bh = sw128_desc(b_hi + ks * 32);
+                        mma_tf32(d, ah, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                        if (PASSES > 1) {
+                            const uint64_t al = sw128_desc(a_lo + ks * 32), bl = sw128_desc(b_lo + ks * 32);
+                            mma_tf32(d, ah, bl, idesc, 1u);
+                            mma_tf32(d, al, bh, idesc, 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (ok) mma_commit(&tfull[acc]);
+            }
+            // every MMA issued by this thread done before the CTA tears down
+            mma_commit(&drain);
+            if (!mbar_wait(&drain, 0)) abort_flag = 1;
+        }
+    } else {
+        // ---- epilogue: thread = tile row (warp w owns tensor-memory lanes 32(w%4)..) ----
+        const int quarter = wid & 3;
+        const int row = 32 * quarter + lane;
+        int li = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
+            const TileJob J = job_of(t);
+            const int acc = li & 1;
+            const bool rv = row < J.m_rows;
+            float* crow = J.Cp + row;
+            // this thread's row of C into shared memory while the MMAs run (each
+            // thread reads back only what it copied: no barrier needed)
+            if (rv)
+                for (int col = 0; col < J.n_cols; col++)
+                    cp_async4(cbuf + (uint32_t)((col * BM + row) * 4), crow + (int64_t)col * J.ldc);
+            cp_async_wait_all();
+            if (!pwait(&tfull[acc], (li >> 1) & 1, &abort_flag)) break;
+            fence_after_sync();
+#pragma unroll 1
+            for (int q = 0; q < BN / 32; q++) {
+                const int cb = 32 * q;
+                float v[32];
+                tmem_ld32(tmem + (uint32_t)(acc * BN) + ((uint32_t)(32 * quarter) << 16) + (uint32_t)cb, v);
+                if (rv) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        if (cb + j < J.n_cols)
+                            crow[(int64_t)(cb + j) * J.ldc] =
+                                ld_shared_f32(cbuf + (uint32_t)(((cb + j) * BM + row) * 4)) - v[j];
+                }
+            }
+            fence_before_sync();
+            mbar_arrive(&tempty[acc]);
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (tid == 0 && abort_flag) atomicExch(err, 1);
+    if (wid == 0) tmem_dealloc(tmem, P_TMEM_COLS);
+}
+
+}  // namespace tc
+}  // namespace gbvlm
