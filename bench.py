@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
-    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served"],
+    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof"],
                    help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
                         "uvlm: 20x80 rectangular wing, 500 pitch-plunge steps")
     p.add_argument("--uvlm-steps", type=int, default=500)
@@ -427,6 +427,39 @@ def run_uvlm(args):
     print(json.dumps(out))
 
 
+def run_aero2dof(args):
+    """Coupled pitch-plunge UVLM (the reference's tests/uvlm_2dof.cpp run): wing + flap pair (chord 1, span
+    40,000, 2 x 2 panels each), the reference's parameters, t_final 1000 (2000 steps of dt 0.5); float
+    aerodynamics, double Newmark structure, Newton loop per step on the device.  The CPU leg runs the
+    oracle's restatement of the same loop (double) on the first steps."""
+    import torch
+    from tinyvlm_gb300 import mesh as M
+    from tinyvlm_gb300.aeroelastic import UVLM_2DOF, reference_vars
+    v = M.rectangular(4, 2, 1.0, 40000.0).astype(np.float32)
+    M.quarter_chord(v)
+    surfaces = [np.ascontiguousarray(v[:, :3, :]), np.ascontiguousarray(v[:, 2:, :])]
+    vars = reference_vars()
+    sim = UVLM_2DOF(surfaces, [0, 1])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = sim.run(vars, 1000.0)
+    torch.cuda.synchronize()
+    gpu = time.perf_counter() - t0
+    n = len(r["iters"])
+    out = {"workload": "coupled 2-DOF pitch-plunge UVLM, wing + flap 2x2 + 2x2 panels, U_a = 7, %d steps" % n,
+           "gpu_s": gpu, "ms_per_step": 1000.0 * gpu / n, "newton_iters_mean": float(np.mean(r["iters"])),
+           "pitch_amplitude_last_quarter_rad": float(np.abs(r["u"][-n // 4:, 1]).max()),
+           "plunge_amplitude_last_quarter": float(np.abs(r["u"][-n // 4:, 0]).max())}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        steps = 200
+        t0 = time.perf_counter()
+        O.aero2dof_run(surfaces, [0, 1], vars, 1000.0, steps=steps)
+        out["cpu_ms_per_step_first%d" % steps] = 1000.0 * (time.perf_counter() - t0) / steps
+        out["cpu_note"] = "oracle restatement (numpy driver over the C operators), one thread for these sizes"
+    print(json.dumps(out))
+
+
 def run_served(args):
     """Poisson mixed stream in equal thirds: steady VLM on trapezoids of 256-16,384 panels (log-uniform),
     single UVLM steps on a resident 20x80 wing with a 500-row (40,000-ring) wake, 2-DOF HBVLM residuals
@@ -482,6 +515,8 @@ def main():
         run_large(args)
     elif args.workload == "uvlm":
         run_uvlm(args)
+    elif args.workload == "aero2dof":
+        run_aero2dof(args)
     elif args.workload == "served":
         run_served(args)
     else:

@@ -364,6 +364,56 @@ int gbvlm_uvlm_step(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, g
 int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream);
 
 /* ---------------------------------------------------------------------------
+ * Structural integrator: Newmark-beta in incremental form (class NewmarkBeta,
+ * vlm/include/vlm_integrator.hpp:7-41, vlm/src/vlm_integrator.cpp:5-68), in
+ * double on the device (the reference's is float).  Matrices are (ndof, ndof)
+ * column-major, vectors ndof long, all DEVICE double; ndof <= 16.
+ * ------------------------------------------------------------------------- */
+typedef struct gbvlm_newmark_s* gbvlm_newmark;
+/* NewmarkBeta(backend, beta = 0.25, gamma = 0.5) (vlm_integrator.hpp:9-15). */
+int gbvlm_newmark_create(gbvlm_newmark* out, double beta, double gamma);
+int gbvlm_newmark_destroy(gbvlm_newmark h);
+/* NewmarkBeta::init (vlm_integrator.cpp:5-26): K_eff = K + M/(beta dt^2) +
+ * gamma C/(beta dt), LU-factored on the device.  Synchronous (returns
+ * GBVLM_ERR_SINGULAR for a singular K_eff). */
+int gbvlm_newmark_init(gbvlm_newmark h, int32_t ndof, const double* M, const double* C, const double* K, double dt,
+                       gbvlm_stream stream);
+/* NewmarkBeta::step (vlm_integrator.cpp:28-68): du, dv, da of one step from
+ * v_i, a_i and the load increment delta_F; coefficients from this dt, K_eff
+ * from init.  Asynchronous; outputs must not alias inputs. */
+int gbvlm_newmark_step(gbvlm_newmark h, const double* M, const double* C, const double* v_i, const double* a_i,
+                       double* du, double* dv, double* da, const double* delta_F, double dt, gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Coupled aeroelastic 2-DOF (pitch-plunge) UVLM: class UVLM_2DOF of the
+ * reference's tests/uvlm_2dof.cpp:52-808 (COUPLED branch).  Aerodynamics in
+ * float as the reference; the structure (Newmark-beta, Newton loop on the load
+ * increment per time step) in double on the device.  The moving surfaces
+ * follow freestream(-t) . heave(-h) . pitch(alpha about x = 1 + a_h); the
+ * time step is the chord of the last surface's last chordwise panel
+ * (nondimensional), t_steps = t_final / dt.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    double b, k_a, rho, a_h, omega, zeta_a, zeta_h, x_a, mu, r_a, U_a; /* UVLM_2DOF_Vars, uvlm_2dof.cpp:23-39 */
+} gbvlm_2dof_vars;
+typedef struct gbvlm_aero2dof_s* gbvlm_aero2dof;
+/* Set-up of UVLM_2DOF::run (uvlm_2dof.cpp:437-515): verts_init HOST float
+ * (ns+1, nc+1, 4) per surface in dimensional units; returns t_steps and dt.
+ * Synchronous. */
+int gbvlm_aero2dof_create(gbvlm_aero2dof* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                          const int32_t* lifting, const gbvlm_2dof_vars* vars, double t_final, int64_t* t_steps,
+                          double* dt, gbvlm_stream stream);
+int gbvlm_aero2dof_destroy(gbvlm_aero2dof h);
+/* Advance `steps` time steps (uvlm_2dof.cpp:588-808), at most t_steps-2 in
+ * all; each Newton loop stops when |du_prev - du| <= FLT_EPSILON or after
+ * max_iter + 1 iterations (the reference uses 50).  Synchronous. */
+int gbvlm_aero2dof_run(gbvlm_aero2dof h, int64_t steps, int32_t max_iter, gbvlm_stream stream);
+/* HOST outputs for steps 0..steps_done: u, v, a, F ((steps_done+1) x 2 each,
+ * row-major: h, alpha), iters (steps_done Newton counts); each may be NULL. */
+int gbvlm_aero2dof_results(gbvlm_aero2dof h, int64_t* steps_done, double* u, double* v, double* a, double* F,
+                           int32_t* iters, gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
  * Harmonic-balance VLM (lib/libhbvlm3.cpp:262-552; 2-DOF lib/libhbvlm.cpp:230-468),
  * double.  Exactly one surface is lifting; its wake carries the
  * trailing-edge gamma rebuilt from Fourier coefficients.  The host supplies

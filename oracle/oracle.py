@@ -641,3 +641,227 @@ def hbvlm_run(verts, lifting, H, omega, dt, max_t, wake_T, inst, dft, ddft, forc
             area = asum(ar[1])
             out[2, s] = coeff_cm(forces[1], vcur[1], np.asarray(ref_b[s]), f_s, 1.0, area, mesh_mac(vcur[1], ar[1]))[1]
     return X, out, iters
+
+
+# ---------------------------------------------------------------------------
+# structural integrator (vlm/include/vlm_integrator.hpp:7-41,
+# vlm/src/vlm_integrator.cpp:5-68), double
+# ---------------------------------------------------------------------------
+def newmark_keff(M, C, K, dt, beta=0.25, gamma=0.5):
+    """NewmarkBeta::init (vlm_integrator.cpp:5-26): K + M/(beta dt^2) + gamma C/(beta dt)."""
+    x1 = gamma / (beta * dt)
+    x0 = 1.0 / (beta * dt * dt)
+    return np.asarray(K, np.float64) + x0 * np.asarray(M, np.float64) + x1 * np.asarray(C, np.float64)
+
+
+def newmark_step(M, C, K_eff, v_i, a_i, delta_F, dt, beta=0.25, gamma=0.5):
+    """NewmarkBeta::step (vlm_integrator.cpp:28-68): (du, dv, da)."""
+    x1 = gamma / (beta * dt)
+    x0 = 1.0 / (beta * dt * dt)
+    xd0 = 1.0 / (beta * dt)
+    xd1 = gamma / beta
+    xdd0 = 1.0 / (2.0 * beta)
+    xdd1 = -dt * (1.0 - gamma / (2.0 * beta))
+    F = np.asarray(delta_F, np.float64) + M @ (xd0 * v_i + xdd0 * a_i) + C @ (xd1 * v_i + xdd1 * a_i)
+    du = np.linalg.solve(K_eff, F)
+    dv = x1 * du - xd1 * v_i - xdd1 * a_i
+    da = x0 * du - xd0 * v_i - xdd0 * a_i
+    return du, dv, da
+
+
+def newmark_linear(M, C, K, u0, v0, dt, steps, beta=0.25, gamma=0.5):
+    """Free response of M u'' + C u' + K u = 0 by the incremental steps, as
+    the reference's tests/newmark.cpp:108-158 drives them: a_0 from
+    M a = -C v_0 - K u_0, then u, v, a += du, dv, da.  Returns (u, v, a),
+    each (steps + 1, ndof)."""
+    M, C, K = (np.asarray(x, np.float64) for x in (M, C, K))
+    n = M.shape[0]
+    u = np.zeros((steps + 1, n))
+    v = np.zeros((steps + 1, n))
+    a = np.zeros((steps + 1, n))
+    u[0], v[0] = u0, v0
+    a[0] = np.linalg.solve(M, -C @ v[0] - K @ u[0])
+    Ke = newmark_keff(M, C, K, dt, beta, gamma)
+    for i in range(steps):
+        du, dv, da = newmark_step(M, C, Ke, v[i], a[i], np.zeros(n), dt, beta, gamma)
+        u[i + 1], v[i + 1], a[i + 1] = u[i] + du, v[i] + dv, a[i] + da
+    return u, v, a
+
+
+# ---------------------------------------------------------------------------
+# Coupled aeroelastic 2-DOF (pitch-plunge) UVLM: tests/uvlm_2dof.cpp:437-808
+# (COUPLED branch).  Structure in double (Newmark-beta, Newton loop per time
+# step on the load increment); aerodynamics in `dtype`.
+# ---------------------------------------------------------------------------
+def torsional_cubic(alpha, b0=0.0, b1=0.1, b2=0.0, b3=40.0):
+    """Cubic pitch stiffness (tests/uvlm_2dof.cpp:238-241)."""
+    return b0 + b1 * alpha + b2 * alpha * alpha + b3 * alpha * alpha * alpha
+
+
+def _rot_y(point_x, angle):
+    """rotation_matrix({point_x, 0, 0}, {0, 1, 0}, angle) (vlm_kinematics.hpp:184-201) and d/d(angle)."""
+    c, s = math.cos(angle), math.sin(angle)
+    R = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+    dR = np.array([[-s, 0, c], [0, 0, 0], [-c, 0, -s]])
+    p = np.array([point_x, 0.0, 0.0])
+    T = np.eye(4)
+    T[:3, :3] = R
+    T[:3, 3] = p - R @ p
+    dT = np.zeros((4, 4))
+    dT[:3, :3] = dR
+    dT[:3, 3] = -dR @ p
+    return T, dT
+
+
+def aero2dof_pose(t_next, h, alpha, hdot, adot, a_h):
+    """Dual transform fs(t + dt) . heave . pitch at tau = 0 of the Newton
+    iterate (tests/uvlm_2dof.cpp:653-681): value and time derivative (4x4)."""
+    Tf = np.eye(4)
+    Tf[0, 3] = -t_next
+    dTf = np.zeros((4, 4))
+    dTf[0, 3] = -1.0
+    Th = np.eye(4)
+    Th[2, 3] = -h
+    dTh = np.zeros((4, 4))
+    dTh[2, 3] = -hdot
+    Tp, dTp_da = _rot_y(1.0 + a_h, alpha)
+    dTp = dTp_da * adot
+    T = Tf @ Th @ Tp
+    dT = dTf @ Th @ Tp + Tf @ dTh @ Tp + Tf @ Th @ dTp
+    return T, dT
+
+
+def aero2dof_run(verts_init, lifting, vars, t_final, dtype=np.float64, max_iter=50, steps=None, sigma=0.0):
+    """UVLM_2DOF::run (tests/uvlm_2dof.cpp:437-808).  verts_init: surfaces in
+    dimensional units (quarter-chord shifted), vars: dict of UVLM_2DOF_Vars
+    (b, k_a, rho, a_h, omega, zeta_a, zeta_h, x_a, mu, r_a, U_a).  Returns
+    dict t, u, v, a, F ((t_steps, 2) each, rows 0 .. last step done), iters
+    per step and dt."""
+    dt_ = np.dtype(dtype).type
+    b = vars["b"]
+    vin = []
+    for v in verts_init:  # nondimensionalize_verts (:428-435)
+        w = np.array(v, np.float64)
+        w[:3] /= b
+        vin.append(np.ascontiguousarray(w, dtype))
+    ns, nc = dims(vin)
+    nsurf = len(vin)
+    n = sum(x * y for x, y in zip(ns, nc))
+    a_h, mu, r_a, Ua, om, rho = vars["a_h"], vars["mu"], vars["r_a"], vars["U_a"], vars["omega"], vars["rho"]
+    # initial pose: 3 deg pitch about the elastic axis (:453-467)
+    T0, _ = _rot_y(1.0 + a_h, math.radians(3.0))
+    verts = [np.empty_like(v) for v in vin]
+    for m in range(nsurf):
+        displace_wing(np.asfortranarray(T0.astype(dtype)), verts[m], vin[m])
+    colloc, normals, areas = mesh_metrics(0.0, verts, dtype)
+    colloc_h = [c.copy() for c in colloc]
+    # time step = the last chordwise panel's chord of the last surface (:473-480)
+    last = vin[-1]
+    d = last[:3, -1, 0].astype(np.float32) - last[:3, -2, 0].astype(np.float32)
+    dt_nd = float(np.float32(np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]))))
+    t_steps = int(np.float32(t_final) / np.float32(dt_nd))
+    wake = []
+    for s in ns:
+        w = np.zeros((4, t_steps, s + 1), dtype)
+        w[3] = 1
+        wake.append(w)
+    gwake = [np.zeros((t_steps - 1, s), dtype) for s in ns]
+    # structure (:352-416): K = 0, linear stiffness in the load
+    M = np.array([[1.0, vars["x_a"]], [vars["x_a"] / r_a ** 2, 1.0]])
+    C = np.array([[2.0 * vars["zeta_h"] * (om / Ua), 0.0], [0.0, 2.0 * vars["zeta_a"] / Ua]])
+    K = np.zeros((2, 2))
+    Ke = newmark_keff(M, C, K, dt_nd)
+    u = np.zeros((t_steps, 2))
+    v = np.zeros((t_steps, 2))
+    a = np.zeros((t_steps, 2))
+    F = np.zeros((t_steps, 2))
+    u[0, 1] = math.radians(3.0)
+    rhs0 = np.array([-(om / Ua) ** 2 * u[0, 0], -1.0 / (Ua * Ua) * torsional_cubic(u[0, 1])])
+    a[0] = np.linalg.solve(M, rhs0 - C @ v[0] - K @ u[0])
+    # AIC at the initial pose, no wake, factored once (:504-506)
+    lhs = np.zeros((n, n), dtype, order="F")
+    lhs_assemble(lhs, colloc, normals, verts, wake, 0, sigma)
+    lu, piv = lu_factor(lhs)
+
+    def aero(T, dT, it):
+        for m in range(nsurf):
+            displace_wing(np.asfortranarray(T.astype(dtype)), verts[m], vin[m])
+        col, nor, are = mesh_metrics(0.0, verts, dtype)
+        wake_shed(verts, wake, it)
+        vel = []
+        for m in range(nsurf):
+            c = colloc_h[m]
+            dd = dT.astype(dtype)
+            ve = np.empty_like(c)
+            for r in range(3):
+                ve[r] = -(dd[r, 0] * c[0] + dd[r, 1] * c[1] + dd[r, 2] * c[2] + dd[r, 3])
+            vel.append(ve)
+        rhs = np.zeros(n, dtype)
+        rhs_assemble_velocities(rhs, nor, vel)
+        rhs_assemble_wake_influence(rhs, gwake, col, nor, wake, lifting, it, sigma)
+        x = lu_solve(lu, piv, rhs)
+        gam, off = [], 0
+        for m in range(nsurf):
+            gam.append(x[off:off + ns[m] * nc[m]].reshape(nc[m], ns[m]).copy())
+            off += ns[m] * nc[m]
+        deltas = []
+        for m in range(nsurf):
+            g = gam[m]
+            dl = g.copy()
+            gwake[m][t_steps - 2 - it] = g[-1]  # shed the trailing-edge gamma
+            if m == 1:  # the reference's wing-flap coupling of the flap's first row (:578-584)
+                dl[0] -= gam[0][-1]
+            dl[1:] -= g[:-1]
+            deltas.append(dl)
+        return col, nor, are, vel, gam, deltas
+
+    # t = 0 (:507-515): the initial pose already in place, freestream velocity (1, 0, 0)
+    wake_shed(verts, wake, 0)
+    vel = []
+    for m in range(nsurf):
+        c = colloc_h[m]
+        ve = np.empty_like(c)
+        ve[0], ve[1], ve[2] = dt_(1), dt_(0), dt_(0)
+        vel.append(ve)
+    rhs = np.zeros(n, dtype)
+    rhs_assemble_velocities(rhs, normals, vel)
+    x = lu_solve(lu, piv, rhs)
+    gam, off = [], 0
+    for m in range(nsurf):
+        gam.append(x[off:off + ns[m] * nc[m]].reshape(nc[m], ns[m]).copy())
+        off += ns[m] * nc[m]
+        gwake[m][t_steps - 2] = gam[m][-1]
+    nsteps = t_steps - 2 if steps is None else min(steps, t_steps - 2)
+    iters = np.zeros(nsteps, np.int32)
+    eps = float(np.finfo(np.float32).eps)
+    fs = np.array([1.0, 0.0, 0.0], dtype)  # -d/dt of the freestream translation (-t, 0, 0)
+    for i in range(nsteps):
+        t_nd = float(np.float32(i) * np.float32(dt_nd))
+        gprev = [g.copy() for g in gam]
+        dF = np.zeros(2)
+        du = np.zeros(2)
+        du_k = np.ones(2)
+        it = 0
+        while np.linalg.norm(du_k) > eps:
+            du_k = du.copy()
+            du, dv, da = newmark_step(M, C, Ke, v[i], a[i], dF, dt_nd)
+            u[i + 1], v[i + 1], a[i + 1] = u[i] + du, v[i] + dv, a[i] + da
+            T, dT = aero2dof_pose(t_nd + dt_nd, u[i + 1, 0], u[i + 1, 1], v[i + 1, 0], v[i + 1, 1], a_h)
+            ref = (T @ np.array([1.0 + a_h, 0.0, 0.0, 1.0]))[:3]
+            col, nor, are, vel, gam, deltas = aero(T, dT, i + 1)
+            gdts = [((g - gp) * dt_(1.0 / dt_nd)).astype(dtype) for g, gp in zip(gam, gprev)]
+            forces = [forces_unsteady(verts[m], deltas[m], gdts[m], vel[m], are[m], nor[m]) for m in range(nsurf)]
+            cl = float(coeff_cl_multibody(forces, are, fs, dt_(rho)))
+            cm = coeff_cm_multibody(forces, verts, are, ref.astype(dtype), fs, dt_(rho))
+            F[i + 1, 0] = -cl / (float(PI_F) * mu)
+            F[i + 1, 1] = (2.0 * float(cm[1])) / (float(PI_F) * mu * r_a ** 2)
+            dF[0] = F[i + 1, 0] - F[i, 0] - (om / Ua) ** 2 * du[0]
+            dF[1] = F[i + 1, 1] - F[i, 1] - 1.0 / (Ua * Ua) * (torsional_cubic(u[i + 1, 1]) - torsional_cubic(u[i, 1]))
+            du_k = du_k - du
+            it += 1
+            if it > max_iter:
+                break
+        iters[i] = it
+    t = np.arange(nsteps + 1) * dt_nd
+    return dict(t=t, u=u[:nsteps + 1], v=v[:nsteps + 1], a=a[:nsteps + 1], F=F[:nsteps + 1], iters=iters, dt=dt_nd,
+                t_steps=t_steps)

@@ -83,6 +83,14 @@ def _protos():
     t["gbvlm_uvlm_results"] = [P, P, P, P, P]
     t["gbvlm_uvlm_begin"] = [P, F64, I32, F64, P]
     t["gbvlm_uvlm_step"] = [P, P, P, P, P]
+    t["gbvlm_newmark_create"] = [P, F64, F64]
+    t["gbvlm_newmark_destroy"] = [P]
+    t["gbvlm_newmark_init"] = [P, I32, P, P, P, F64, P]
+    t["gbvlm_newmark_step"] = [P, P, P, P, P, P, P, P, P, F64, P]
+    t["gbvlm_aero2dof_create"] = [P, I32, P, PP, P, P, F64, P, P, P]
+    t["gbvlm_aero2dof_destroy"] = [P]
+    t["gbvlm_aero2dof_run"] = [P, I64, I32, P]
+    t["gbvlm_aero2dof_results"] = [P, P, P, P, P, P, P, P]
     t["gbvlm_hbvlm_create"] = [P, I32, P, PP, P]
     t["gbvlm_hbvlm_destroy"] = [P]
     t["gbvlm_hbvlm_prepare"] = [P, I32, I64, P, P, P, P, P, P, P]

@@ -13,6 +13,7 @@
 //   wake roll-up (the reference's kernel_rollup, whose caller it disables);
 //   move to t + dt and recompute the panel metrics.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <string.h>
 
 #include <vector>
@@ -426,6 +427,370 @@ struct UvlmState : UvlmBase {
     }
 };
 
+// ===========================================================================
+// Coupled aeroelastic 2-DOF (pitch-plunge) UVLM, tests/uvlm_2dof.cpp:437-808
+// (COUPLED branch).  Aerodynamics in float as the reference; structure in
+// double on the device (Newmark-beta, gbvlm_struct.cu).  Per time step i a
+// Newton loop on the load increment: Newmark step -> state at i+1 -> pose
+// fs(t+dt).heave.pitch (value and time derivative) -> displaced wing,
+// metrics, wake shed, panel velocities, RHS with the wake, solve with the
+// AIC factored at t = 0 -> gamma, wing-flap delta coupling, forces, CL/CM ->
+// loads F(i+1) and their increment -> converged when |du_prev - du| <= eps.
+// Each iteration is a fixed chain of launches; the host reads one flag per
+// iteration to end the loop.
+// ===========================================================================
+struct A2Dev {
+    double M[4], C[4], K[4];
+    double du[2], dv[2], da[2], dF[2], du_prev[2];
+    double coef[4];  // CL, CM x, y, z of the iterate
+    float T[16], dT[16], ref[3], fs[3];
+    int converged;
+};
+
+// state at i+1 from the Newmark increments, the pose and the moment point
+__global__ void k_a2_pose(A2Dev* d, double* u, double* v, double* a, int64_t i, double t_next, double a_h,
+                          int32_t nsurf, float* T_all, float* dT_all) {
+    if (threadIdx.x != 0) return;
+    double* u1 = u + 2 * (i + 1);
+    double* v1 = v + 2 * (i + 1);
+    double* a1 = a + 2 * (i + 1);
+    for (int k = 0; k < 2; k++) {
+        u1[k] = u[2 * i + k] + d->du[k];
+        v1[k] = v[2 * i + k] + d->dv[k];
+        a1[k] = a[2 * i + k] + d->da[k];
+    }
+    const double h = u1[0], al = u1[1], hd = v1[0], ad = v1[1];
+    const double px = 1.0 + a_h;
+    // pitch: rotation about y through (px, 0, 0) (vlm_kinematics.hpp:184-201), and d/dt = dR/dalpha * alpha'
+    const double c = cos(al), sn = sin(al);
+    double P[16] = {c, 0, -sn, 0, 0, 1, 0, 0, sn, 0, c, 0, px - c * px, 0, sn * px, 1};   // column-major
+    double dP[16] = {-sn * ad, 0, -c * ad, 0, 0, 0, 0, 0, c * ad, 0, -sn * ad, 0, sn * px * ad, 0, c * px * ad, 0};
+    // heave: translation (0, 0, -h), d/dt (0, 0, -h'); freestream: translation (-t, 0, 0), d/dt (-1, 0, 0)
+    double H[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, -h, 1};
+    double dH[16] = {0};
+    dH[14] = -hd;
+    double Fm[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, -t_next, 0, 0, 1};
+    double dFm[16] = {0};
+    dFm[12] = -1.0;
+    auto mul = [](const double* A, const double* B, double* R) {
+        for (int cc = 0; cc < 4; cc++)
+            for (int r = 0; r < 4; r++) {
+                double s_ = 0;
+                for (int k = 0; k < 4; k++) s_ += A[r + 4 * k] * B[k + 4 * cc];
+                R[r + 4 * cc] = s_;
+            }
+    };
+    double HP[16], dHP[16], t1[16], t2[16], TT[16], dTT[16];
+    mul(H, P, HP);
+    mul(dH, P, t1);
+    mul(H, dP, t2);
+    for (int q = 0; q < 16; q++) dHP[q] = t1[q] + t2[q];
+    mul(Fm, HP, TT);
+    mul(dFm, HP, t1);
+    mul(Fm, dHP, t2);
+    for (int q = 0; q < 16; q++) dTT[q] = t1[q] + t2[q];
+    for (int q = 0; q < 16; q++) {
+        d->T[q] = (float)TT[q];
+        d->dT[q] = (float)dTT[q];
+    }
+    for (int r = 0; r < 3; r++) d->ref[r] = (float)(TT[r] * px + TT[r + 12]);
+    for (int m = 0; m < nsurf; m++)
+        for (int q = 0; q < 16; q++) {
+            T_all[16 * m + q] = (float)TT[q];
+            dT_all[16 * m + q] = (float)dTT[q];
+        }
+}
+
+// the reference's wing-flap coupling: the flap's first chordwise row of
+// gamma_delta also subtracts the wing's trailing-edge gamma (uvlm_2dof.cpp:578-584)
+__global__ void k_a2_flap(float* gdelta1, const float* gamma0, int64_t ns, int64_t nc0) {
+    const int64_t s_ = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s_ < ns) gdelta1[s_] -= gamma0[s_ + (nc0 - 1) * ns];
+}
+
+__host__ __device__ inline double torsional_cubic(double al) { return 0.1 * al + 40.0 * al * al * al; }
+
+// loads of the iterate (uvlm_2dof.cpp:728-744) and the Newton test
+__global__ void k_a2_loads(A2Dev* d, double* u, double* F, int64_t i, double mu, double r_a, double om, double Ua,
+                           double eps) {
+    if (threadIdx.x != 0) return;
+    const double pi_f = (double)3.141593f;
+    F[2 * (i + 1)] = -d->coef[0] / (pi_f * mu);
+    F[2 * (i + 1) + 1] = (2.0 * d->coef[2]) / (pi_f * mu * r_a * r_a);
+    d->dF[0] = F[2 * (i + 1)] - F[2 * i] - (om / Ua) * (om / Ua) * d->du[0];
+    d->dF[1] = F[2 * (i + 1) + 1] - F[2 * i + 1] -
+               1.0 / (Ua * Ua) * (torsional_cubic(u[2 * (i + 1) + 1]) - torsional_cubic(u[2 * i + 1]));
+    const double k0 = d->du_prev[0] - d->du[0], k1 = d->du_prev[1] - d->du[1];
+    d->converged = sqrt(k0 * k0 + k1 * k1) <= eps ? 1 : 0;
+}
+
+struct Aero2Dof {
+    int32_t nsurf = 0;
+    std::vector<gbvlm_dims> dims;
+    std::vector<int32_t> lifting;
+    gbvlm_2dof_vars vars{};
+    double dt = 0;
+    int64_t t_steps = 0, n = 0, done = 0;  // steps advanced
+    void* mem = nullptr;
+    std::vector<float*> vinit, verts, wake, colloc, colloch, normals, areas, gamma, gprev, gdelta, gdt, gwake, vel,
+        forces;
+    float *lhs = nullptr, *rhs = nullptr, *T_all = nullptr, *dT_all = nullptr;
+    double *u = nullptr, *v = nullptr, *a = nullptr, *F = nullptr;
+    A2Dev* dev = nullptr;
+    gbvlm_lu lu = nullptr;
+    gbvlm_newmark nm = nullptr;
+    std::vector<int32_t> iters;
+    CoefArgs<float> ca;
+
+    ~Aero2Dof() {
+        if (lu) gbvlm_lu_destroy(lu);
+        if (nm) gbvlm_newmark_destroy(nm);
+        if (mem) cudaFree(mem);
+    }
+
+    static std::vector<const float*> C(const std::vector<float*>& x) { return std::vector<const float*>(x.begin(), x.end()); }
+
+    int init(int32_t ns_, const gbvlm_dims* d, const float* const* vh, const int32_t* lift, const gbvlm_2dof_vars& vr,
+             double t_final, cudaStream_t st) {
+        nsurf = ns_;
+        vars = vr;
+        dims.assign(d, d + ns_);
+        lifting.assign(lift, lift + ns_);
+        // nondimensional vertices (uvlm_2dof.cpp:428-435) and the time step: the chord of the last
+        // chordwise panel of the last surface at the first spanwise station (:473-480), in float
+        std::vector<std::vector<float>> vnd(nsurf);
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t nv = (dims[m].ns + 1) * (dims[m].nc + 1);
+            vnd[m].assign(vh[m], vh[m] + 4 * nv);
+            for (int64_t q = 0; q < 3 * nv; q++) vnd[m][q] = (float)(vnd[m][q] / (float)vars.b);
+        }
+        {
+            const gbvlm_dims& L = dims[nsurf - 1];
+            const int64_t nv = (L.ns + 1) * (L.nc + 1), lastj = L.nc * (L.ns + 1), prevj = (L.nc - 1) * (L.ns + 1);
+            const std::vector<float>& w = vnd[nsurf - 1];
+            const float dx = w[lastj] - w[prevj], dy = w[nv + lastj] - w[nv + prevj];
+            const float dz = w[2 * nv + lastj] - w[2 * nv + prevj];
+            const float dtf = sqrtf(dx * dx + dy * dy + dz * dz);
+            dt = (double)dtf;
+            t_steps = (int64_t)((float)t_final / dtf);
+        }
+        GB_REQUIRE(t_steps >= 3, "aeroelastic 2-DOF: t_final %.3g gives %lld steps of %.3g", t_final,
+                   (long long)t_steps, dt);
+        size_t bytes = 0;
+        auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+        n = 0;
+        for (auto& x : dims) {
+            x.nwv = t_steps;
+            const int64_t np = x.ns * x.nc, nv = (x.ns + 1) * (x.nc + 1);
+            n += np;
+            bytes += al(4 * 4 * nv) * 2 + al(4 * 4 * (x.ns + 1) * t_steps) + al(4 * 3 * np) * 5 + al(4 * np) * 5 +
+                     al(4 * x.ns * (t_steps - 1));
+        }
+        bytes += al(4 * n * n) + al(4 * n) + 2 * al(4 * 16 * nsurf) + 4 * al(8 * 2 * t_steps) + al(sizeof(A2Dev));
+        GB_CUDA(cudaMalloc(&mem, bytes));
+        GB_CUDA(cudaMemset(mem, 0, bytes));
+        char* p = (char*)mem;
+        auto take = [&](size_t b) {
+            void* r = p;
+            p += al(b);
+            return r;
+        };
+        lhs = (float*)take(4 * n * n);
+        rhs = (float*)take(4 * n);
+        T_all = (float*)take(4 * 16 * nsurf);
+        dT_all = (float*)take(4 * 16 * nsurf);
+        u = (double*)take(8 * 2 * t_steps);
+        v = (double*)take(8 * 2 * t_steps);
+        a = (double*)take(8 * 2 * t_steps);
+        F = (double*)take(8 * 2 * t_steps);
+        dev = (A2Dev*)take(sizeof(A2Dev));
+        for (auto& x : dims) {
+            const int64_t np = x.ns * x.nc, nv = (x.ns + 1) * (x.nc + 1);
+            vinit.push_back((float*)take(4 * 4 * nv));
+            verts.push_back((float*)take(4 * 4 * nv));
+            wake.push_back((float*)take(4 * 4 * (x.ns + 1) * t_steps));
+            colloc.push_back((float*)take(4 * 3 * np));
+            colloch.push_back((float*)take(4 * 3 * np));
+            normals.push_back((float*)take(4 * 3 * np));
+            vel.push_back((float*)take(4 * 3 * np));
+            forces.push_back((float*)take(4 * 3 * np));
+            areas.push_back((float*)take(4 * np));
+            gamma.push_back((float*)take(4 * np));
+            gprev.push_back((float*)take(4 * np));
+            gdelta.push_back((float*)take(4 * np));
+            gdt.push_back((float*)take(4 * np));
+            gwake.push_back((float*)take(4 * x.ns * (t_steps - 1)));
+        }
+        for (int m = 0; m < nsurf; m++) {
+            GB_CUDA(cudaMemcpy(vinit[m], vnd[m].data(), 4 * vnd[m].size(), cudaMemcpyHostToDevice));
+            std::vector<float> ones((dims[m].ns + 1) * t_steps, 1.f);  // wake w plane
+            GB_CUDA(cudaMemcpy(wake[m] + 3 * (dims[m].ns + 1) * t_steps, ones.data(), 4 * ones.size(),
+                               cudaMemcpyHostToDevice));
+        }
+        // structure (uvlm_2dof.cpp:352-416): K = 0, the linear stiffness is in the load
+        A2Dev h{};
+        const double xa = vars.x_a, ra = vars.r_a, om = vars.omega, Ua = vars.U_a;
+        h.M[0] = 1.0;
+        h.M[1] = xa / (ra * ra);
+        h.M[2] = xa;
+        h.M[3] = 1.0;
+        h.C[0] = 2.0 * vars.zeta_h * (om / Ua);
+        h.C[3] = 2.0 * vars.zeta_a / Ua;
+        h.fs[0] = 1.f;  // -d/dt of the freestream translation (-t, 0, 0)
+        GB_CUDA(cudaMemcpy(dev, &h, sizeof(h), cudaMemcpyHostToDevice));
+        {
+            const double u0[2] = {0.0, 3.0 * M_PI / 180.0}, v0[2] = {0.0, 0.0};
+            const double r0[2] = {-(om / Ua) * (om / Ua) * u0[0], -1.0 / (Ua * Ua) * torsional_cubic(u0[1])};
+            // M a0 = r0 - C v0 - K u0 (2 x 2, column-major M)
+            const double det = h.M[0] * h.M[3] - h.M[2] * h.M[1];
+            const double a0[2] = {(h.M[3] * r0[0] - h.M[2] * r0[1]) / det, (-h.M[1] * r0[0] + h.M[0] * r0[1]) / det};
+            GB_CUDA(cudaMemcpy(u, u0, sizeof(u0), cudaMemcpyHostToDevice));
+            GB_CUDA(cudaMemcpy(v, v0, sizeof(v0), cudaMemcpyHostToDevice));
+            GB_CUDA(cudaMemcpy(a, a0, sizeof(a0), cudaMemcpyHostToDevice));
+        }
+        int rc = gbvlm_newmark_create(&nm, 0.25, 0.5);
+        if (rc) return rc;
+        if ((rc = gbvlm_newmark_init(nm, 2, dev->M, dev->C, dev->K, dt, (gbvlm_stream)st))) return rc;
+        if ((rc = gbvlm_lu_create(&lu))) return rc;
+        if ((rc = gbvlm_lu_init(lu, n))) return rc;
+        memset(&ca, 0, sizeof(ca));
+        ca.n = nsurf;
+        for (int m = 0; m < nsurf; m++) {
+            ca.ns[m] = dims[m].ns;
+            ca.nc[m] = dims[m].nc;
+            ca.forces[m] = forces[m];
+            ca.verts[m] = verts[m];
+            ca.areas[m] = areas[m];
+        }
+        return start(st);
+    }
+
+    // initial pose, AIC factored once, the t = 0 solve (uvlm_2dof.cpp:453-515)
+    int start(cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        const double px = 1.0 + vars.a_h, th = 3.0 * M_PI / 180.0, c = cos(th), sn = sin(th);
+        float T0[16] = {(float)c, 0, (float)-sn, 0, 0, 1, 0, 0, (float)sn, 0, (float)c, 0,
+                        (float)(px - c * px), 0, (float)(sn * px), 1};
+        float dT0[16] = {0};
+        dT0[12] = -1.f;
+        std::vector<float> ta(16 * nsurf), tb(16 * nsurf);
+        for (int m = 0; m < nsurf; m++)
+            for (int q = 0; q < 16; q++) {
+                ta[16 * m + q] = T0[q];
+                tb[16 * m + q] = dT0[q];
+            }
+        GB_CUDA(cudaMemcpyAsync(T_all, ta.data(), 4 * ta.size(), cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(dT_all, tb.data(), 4 * tb.size(), cudaMemcpyHostToDevice, st));
+        std::vector<const float*> tr(nsurf);
+        for (int m = 0; m < nsurf; m++) tr[m] = T_all + 16 * m;
+        int rc;
+        if ((rc = Ops2<float>::displace(nsurf, dims.data(), tr.data(), verts.data(), C(vinit).data(), s))) return rc;
+        if ((rc = Ops2<float>::metrics(nsurf, dims.data(), C(verts).data(), colloc.data(), normals.data(),
+                                       areas.data(), s)))
+            return rc;
+        for (int m = 0; m < nsurf; m++)
+            GB_CUDA(cudaMemcpyAsync(colloch[m], colloc[m], 4 * 3 * dims[m].ns * dims[m].nc, cudaMemcpyDeviceToDevice,
+                                    st));
+        GB_CUDA(cudaMemsetAsync(lhs, 0, 4 * n * n, st));
+        if ((rc = Ops2<float>::lhs(lhs, n, nsurf, dims.data(), C(colloc).data(), C(normals).data(), C(verts).data(),
+                                   0.f, s)))
+            return rc;
+        if ((rc = Ops2<float>::factor(lu, lhs, n, s))) return rc;
+        if ((rc = Ops2<float>::shed(nsurf, dims.data(), C(verts).data(), wake.data(), 0, s))) return rc;
+        if ((rc = aero_solve(0, st))) return rc;
+        done = 0;
+        iters.clear();
+        return GBVLM_OK;
+    }
+
+    // velocities, RHS, solve and circulation of the current pose (wake rows 0..it)
+    int aero_solve(int64_t it, cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        int rc;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t np = dims[m].ns * dims[m].nc;
+            k_dual_velocity<float><<<(unsigned)cdiv(np, 256), 256, 0, st>>>(dT_all + 16 * m, colloch[m], vel[m], np);
+            GB_LAUNCH_CHECK();
+        }
+        GB_CUDA(cudaMemsetAsync(rhs, 0, 4 * n, st));
+        if ((rc = Ops2<float>::rhsv(rhs, nsurf, dims.data(), C(normals).data(), C(vel).data(), s))) return rc;
+        if ((rc = Ops2<float>::wake(rhs, nsurf, dims.data(), C(gwake).data(), C(colloc).data(), C(normals).data(),
+                                    C(wake).data(), lifting.data(), (int32_t)it, 0.f, s)))
+            return rc;
+        if ((rc = Ops2<float>::solve(lu, lhs, n, rhs, s))) return rc;
+        int64_t off = 0;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t ns = dims[m].ns, nc = dims[m].nc;
+            if ((rc = Ops2<float>::gupd(ns, nc, rhs + off, gamma[m], gdelta[m], gwake[m], t_steps - 2 - it, gprev[m],
+                                        gdt[m], (float)dt, s)))
+                return rc;
+            off += ns * nc;
+        }
+        if (nsurf > 1 && dims[1].ns == dims[0].ns) {
+            k_a2_flap<<<(unsigned)cdiv(dims[1].ns, 128), 128, 0, st>>>(gdelta[1], gamma[0], dims[0].ns, dims[0].nc);
+            GB_LAUNCH_CHECK();
+        }
+        return GBVLM_OK;
+    }
+
+    // one Newton iteration of time step i (uvlm_2dof.cpp:639-751)
+    int iterate(int64_t i, cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        int rc;
+        GB_CUDA(cudaMemcpyAsync(dev->du_prev, dev->du, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st));
+        if ((rc = gbvlm_newmark_step(nm, dev->M, dev->C, v + 2 * i, a + 2 * i, dev->du, dev->dv, dev->da, dev->dF, dt,
+                                     s)))
+            return rc;
+        const float tn = (float)i * (float)dt + (float)dt;
+        k_a2_pose<<<1, 32, 0, st>>>(dev, u, v, a, i, (double)tn, vars.a_h, nsurf, T_all, dT_all);
+        GB_LAUNCH_CHECK();
+        std::vector<const float*> tr(nsurf);
+        for (int m = 0; m < nsurf; m++) tr[m] = T_all + 16 * m;
+        if ((rc = Ops2<float>::displace(nsurf, dims.data(), tr.data(), verts.data(), C(vinit).data(), s))) return rc;
+        if ((rc = Ops2<float>::metrics(nsurf, dims.data(), C(verts).data(), colloc.data(), normals.data(),
+                                       areas.data(), s)))
+            return rc;
+        if ((rc = Ops2<float>::shed(nsurf, dims.data(), C(verts).data(), wake.data(), (int32_t)(i + 1), s))) return rc;
+        if ((rc = aero_solve(i + 1, st))) return rc;
+        for (int m = 0; m < nsurf; m++)
+            if ((rc = Ops2<float>::forces(dims[m].ns, dims[m].nc, verts[m], gdelta[m], gdt[m], vel[m], areas[m],
+                                          normals[m], forces[m], s)))
+                return rc;
+        k_step_coeffs<float><<<1, 512, 0, st>>>(ca, dev->fs, dev->ref, 0, vars.rho, dev->coef);
+        GB_LAUNCH_CHECK();
+        k_a2_loads<<<1, 32, 0, st>>>(dev, u, F, i, vars.mu, vars.r_a, vars.omega, vars.U_a,
+                                     (double)1.1920928955078125e-07);
+        GB_LAUNCH_CHECK();
+        return GBVLM_OK;
+    }
+
+    int run(int64_t steps, int32_t max_iter, cudaStream_t st) {
+        GB_REQUIRE(done + steps <= t_steps - 2, "aeroelastic 2-DOF: %lld steps requested, %lld left",
+                   (long long)steps, (long long)(t_steps - 2 - done));
+        int* hflag = (int*)host_scratch(sizeof(int));
+        for (int64_t k = 0; k < steps; k++) {
+            const int64_t i = done;
+            for (int m = 0; m < nsurf; m++)
+                GB_CUDA(cudaMemcpyAsync(gprev[m], gamma[m], 4 * dims[m].ns * dims[m].nc, cudaMemcpyDeviceToDevice,
+                                        st));
+            GB_CUDA(cudaMemsetAsync(dev->dF, 0, sizeof(double) * 2, st));
+            GB_CUDA(cudaMemsetAsync(dev->du, 0, sizeof(double) * 2, st));
+            int it = 0;
+            while (true) {
+                int rc = iterate(i, st);
+                if (rc) return rc;
+                it++;
+                GB_CUDA(cudaMemcpyAsync(hflag, &dev->converged, sizeof(int), cudaMemcpyDeviceToHost, st));
+                GB_CUDA(cudaStreamSynchronize(st));
+                if (*hflag || it > max_iter) break;
+            }
+            iters.push_back(it);
+            done++;
+        }
+        return GBVLM_OK;
+    }
+};
+
 }  // namespace gbvlm
 
 using namespace gbvlm;
@@ -500,6 +865,53 @@ int gbvlm_uvlm_step(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, g
 int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream) {
     GB_REQUIRE(h && h->impl, "null argument");
     return h->impl->results(cl, cm, gamma_last, to_cuda(stream));
+}
+
+int gbvlm_aero2dof_create(gbvlm_aero2dof* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                          const int32_t* lifting, const gbvlm_2dof_vars* vars, double t_final, int64_t* t_steps,
+                          double* dt, gbvlm_stream stream) {
+    GB_REQUIRE(out && dims && verts_init && lifting && vars, "null argument");
+    GB_REQUIRE(nsurf >= 1 && nsurf <= GBVLM_MAX_SURFACES, "nsurf=%d outside [1, %d]", nsurf, GBVLM_MAX_SURFACES);
+    GB_REQUIRE(vars->b > 0 && vars->mu > 0 && vars->r_a > 0 && vars->U_a > 0, "aeroelastic 2-DOF: bad parameters");
+    for (int m = 0; m < nsurf; m++) GB_REQUIRE(verts_init[m] && dims[m].ns >= 1 && dims[m].nc >= 1, "surface %d", m);
+    GB_REQUIRE(dims[nsurf - 1].nc >= 2, "aeroelastic 2-DOF: the last surface needs two chordwise panels (time step)");
+    auto* h = new Aero2Dof();
+    int rc = h->init(nsurf, dims, verts_init, lifting, *vars, t_final, to_cuda(stream));
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    if (t_steps) *t_steps = h->t_steps;
+    if (dt) *dt = h->dt;
+    *out = (gbvlm_aero2dof)h;
+    return GBVLM_OK;
+}
+
+int gbvlm_aero2dof_destroy(gbvlm_aero2dof h) {
+    delete (Aero2Dof*)h;
+    return GBVLM_OK;
+}
+
+int gbvlm_aero2dof_run(gbvlm_aero2dof h, int64_t steps, int32_t max_iter, gbvlm_stream stream) {
+    GB_REQUIRE(h && steps >= 0 && max_iter >= 1, "bad arguments");
+    return ((Aero2Dof*)h)->run(steps, max_iter, to_cuda(stream));
+}
+
+int gbvlm_aero2dof_results(gbvlm_aero2dof h, int64_t* steps_done, double* u, double* v, double* a, double* F,
+                           int32_t* iters, gbvlm_stream stream) {
+    GB_REQUIRE(h, "null argument");
+    Aero2Dof* s = (Aero2Dof*)h;
+    cudaStream_t st = to_cuda(stream);
+    const size_t nb = sizeof(double) * 2 * (size_t)(s->done + 1);
+    if (u) GB_CUDA(cudaMemcpyAsync(u, s->u, nb, cudaMemcpyDeviceToHost, st));
+    if (v) GB_CUDA(cudaMemcpyAsync(v, s->v, nb, cudaMemcpyDeviceToHost, st));
+    if (a) GB_CUDA(cudaMemcpyAsync(a, s->a, nb, cudaMemcpyDeviceToHost, st));
+    if (F) GB_CUDA(cudaMemcpyAsync(F, s->F, nb, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (steps_done) *steps_done = s->done;
+    if (iters)
+        for (int64_t k = 0; k < s->done; k++) iters[k] = s->iters[k];
+    return GBVLM_OK;
 }
 
 }  // extern "C"
