@@ -23,6 +23,7 @@
 //                       right-hand side V_inf(alpha) of the same AIC.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -533,6 +534,8 @@ struct gbvlm_batch_s {
     cudaStream_t side[MAX_GROUPS] = {};
     cudaEvent_t fork = nullptr, join[MAX_GROUPS] = {};
     LuBatch<float> lub;
+    TrsFlow flow;  // triangular solves of all systems (unless GBVLM_TRS_FLOW=0: one CTA per system)
+    bool use_flow = true;
     double u_inf = 1, rho = 1, beta = 0, ref[3] = {0, 0, 0};
     int32_t want_gamma = 0;
     cudaStream_t cap = nullptr;
@@ -616,7 +619,12 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     mark(4);
     int32_t maxrhs = 0;
     for (auto& s : h->sys) maxrhs = std::max(maxrhs, s.nrhs);
-    rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st, h->plans[0].tc_passes ? h->plans[0].d_err : nullptr);
+    auto solve = [&]() {
+        return h->use_flow ? trs_flow_solve(h->lub, h->flow, maxrhs, st)
+                           : lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st,
+                                                   h->plans[0].tc_passes ? h->plans[0].d_err : nullptr);
+    };
+    rc = solve();
     if (rc) return rc;
     k_batch_accum<<<g, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
@@ -624,7 +632,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         k_batch_residual<<<dim3((unsigned)h->residual_tiles, (unsigned)cdiv(maxrhs, RS_MAXRHS)), RS_THREADS, 0, st>>>(
             a, h->d_rpfx);
         GB_LAUNCH_CHECK();
-        rc = lu_batch_solve<float>(h->lub, h->nsys, maxrhs, h->maxn, st, h->plans[0].tc_passes ? h->plans[0].d_err : nullptr);
+        rc = solve();
         if (rc) return rc;
         k_batch_accum<<<g, 256, 0, st>>>(a);
         GB_LAUNCH_CHECK();
@@ -886,6 +894,11 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
             if (ee != cudaSuccess) rc = cuda_fail(ee, "batch streams", __FILE__, __LINE__);
         }
     }
+    if (rc == GBVLM_OK) {
+        const char* fe = getenv("GBVLM_TRS_FLOW");
+        h->use_flow = !(fe && fe[0] == '0');
+        if (h->use_flow) rc = trs_flow_build(h->flow, lun, 0);
+    }
     if (rc) {
         delete h;
         return rc;
@@ -1057,6 +1070,10 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
     GB_CUDA(cudaStreamSynchronize(st));
     for (int g = 0; g < h->ngroups; g++) {
         int rc = lu_plan_check(h->plans[g], st);
+        if (rc) return rc;
+    }
+    if (h->use_flow) {
+        int rc = trs_flow_check(h->flow, st);
         if (rc) return rc;
     }
     int32_t* info = (int32_t*)host_scratch(sizeof(int32_t) * h->nsys);

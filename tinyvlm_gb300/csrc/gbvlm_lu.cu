@@ -917,6 +917,265 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
 }
 
 // ---------------------------------------------------------------------------
+// dataflow triangular solves of a float batch: one persistent launch runs
+// the forward (L, unit lower) and backward (U) sweeps of every system in
+// blocks of FL_B rows.  Work items are (system, block) pairs handed out in a
+// fixed order by an atomic counter: all forward items by block level, then
+// all backward items by distance from the last block.  Item (s, i) of the
+// forward sweep accumulates b_i - sum_{j<i} L_ij y_j as y_j become final,
+// then solves its diagonal block; the backward sweep likewise with U and
+// x_j, j > i.  A system's finished blocks are counted (forward and backward
+// separately, each finishing in order), and an item waits only on items
+// handed out before it, which are held by running CTAs, so the launch cannot
+// deadlock whatever the number of resident CTAs.  Every wait is bounded
+// (tc::WAIT_NS) and ends early once any CTA has recorded an error.
+//
+// One item: 256 threads; thread t holds rows t%64 and t%64+64 of the block
+// and columns 32*(t/64) .. +31 of each off-diagonal FL_B x FL_B block (64
+// loads issued before waiting for that block's x); the four column quarters
+// are summed in shared memory at the end.  The diagonal block (the triangle
+// the sweep needs) is copied to shared memory with cp.async while the
+// off-diagonal blocks stream; it is solved one warp per right-hand side in
+// 32-row steps.
+// ---------------------------------------------------------------------------
+constexpr int FL_B = 128;
+constexpr int FL_THREADS = 256;
+constexpr int FL_R = 8;  // right-hand sides per launch
+constexpr int FL_LD = FL_B + 1;
+constexpr int FL_SMEM = (FL_B * FL_LD + 4 * FL_B * FL_R) * 4;  // diagonal block + quarter sums (x staging aliased)
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// 4-byte cp.async; src_bytes 0 fills the destination with zero and reads nothing
+__device__ __forceinline__ void cp_async4_zfill(uint32_t dst, const float* src, bool load) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(load ? 4 : 0) : "memory");
+}
+
+// all threads: true once *cnt > need; false if the launch has failed or the
+// wait ran out (which records the failure)
+__device__ __forceinline__ bool flow_wait(const int* cnt, int need, int* err, int* s_ok) {
+    if (threadIdx.x == 0) {
+        bool ok = ld_acquire_gpu(cnt) > need;
+        if (!ok) {
+            const uint64_t t0 = tc::global_ns();
+            while (true) {
+                __nanosleep(100);
+                if (ld_acquire_gpu(cnt) > need) {
+                    ok = true;
+                    break;
+                }
+                if (*(volatile int*)err) break;
+                if (tc::global_ns() - t0 > tc::WAIT_NS) {
+                    atomicCAS(err, 0, 1);
+                    break;
+                }
+            }
+        }
+        *s_ok = ok;
+    }
+    __syncthreads();
+    const bool ok = *(volatile int*)s_ok != 0;
+    __syncthreads();  // every thread has read the flag before thread 0 can write the next one
+    return ok;
+}
+
+// ctl: [0] dispatch counter, [1] error word, [2, 2 + nsys) forward blocks
+// finished per system, [2 + nsys, 2 + 2 nsys) backward blocks finished
+__global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, const int2* items, int nfwd, int nitems,
+                                                            int nsys, int* ctl, float* const* Yp, int32_t rhs0) {
+    extern __shared__ __align__(16) float fsm[];
+    float* Ld = fsm;                  // [FL_B][FL_LD] diagonal block
+    float* xs = fsm + FL_B * FL_LD;   // [2][FL_B][FL_R] x of an off-diagonal block (two buffers)
+    float* red = xs;                  // [4][FL_B][FL_R] column-quarter sums, then [FL_B][FL_R] the block's values
+    __shared__ int s_item, s_ok;
+    int* err = ctl + 1;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int r = tid & 63, cq = tid >> 6;
+    while (true) {
+        __syncthreads();  // the previous item is done with shared memory
+        if (tid == 0) s_item = *(volatile int*)err ? nitems : atomicAdd(ctl, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) return;
+        const bool fwd = it < nfwd;
+        const int2 w = items[it];
+        const int s = w.x, bi = w.y;
+        const int nr = min(FL_R, B.nrhs[s] - rhs0);
+        if (nr <= 0) continue;  // no right-hand side of this launch: no item of the system waits
+        const int64_t n = B.n[s], ld = B.ld[s], ldx = B.ldx[s];
+        const int nblk = (int)((n + FL_B - 1) / FL_B);
+        const int64_t R0 = (int64_t)bi * FL_B;
+        const int nb = (int)min((int64_t)FL_B, n - R0);
+        const float* A = B.A[s];
+        float* Y = Yp[s];  // n x FL_R, row-major: y (forward), then x (backward)
+        float* X = B.X[s] + (int64_t)rhs0 * ldx;
+        int* done = ctl + 2 + (fwd ? 0 : nsys) + s;
+        // diagonal block: the strict lower triangle (forward) or the upper one
+        // with the diagonal (backward), zero elsewhere
+        for (int e = tid; e < FL_B * FL_B; e += FL_THREADS) {
+            const int rr = e & (FL_B - 1), cc = e >> 7;
+            const bool need = rr < nb && cc < nb && (fwd ? cc < rr : cc >= rr);
+            cp_async4_zfill(tc::smem_u32(Ld + rr * FL_LD + cc), need ? A + (R0 + rr) + (R0 + cc) * ld : A, need);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        float acc[2][FL_R];
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+#pragma unroll
+            for (int q = 0; q < FL_R; q++) acc[h][q] = 0.f;
+        if (fwd) {
+            if (cq == 0) {  // b = P x: rows of X through the factorisation's permutation
+                const int32_t* pm = B.perm[s];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int row = r + 64 * h;
+                    if (row < nb) {
+                        const int64_t p = pm[R0 + row];
+#pragma unroll
+                        for (int q = 0; q < FL_R; q++)
+                            if (q < nr) acc[h][q] = X[p + q * ldx];
+                    }
+                }
+            }
+        } else {
+            if (!flow_wait(ctl + 2 + s, bi, err, &s_ok)) break;  // y_i
+            if (cq == 0) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int row = r + 64 * h;
+                    if (row < nb) {
+                        const float4* y4 = reinterpret_cast<const float4*>(Y + (R0 + row) * FL_R);
+                        const float4 a = __ldcg(y4), b = __ldcg(y4 + 1);
+                        acc[h][0] = a.x, acc[h][1] = a.y, acc[h][2] = a.z, acc[h][3] = a.w;
+                        acc[h][4] = b.x, acc[h][5] = b.y, acc[h][6] = b.z, acc[h][7] = b.w;
+                    }
+                }
+            }
+        }
+        // off-diagonal blocks, in the order their x become final
+        const int nj = fwd ? bi : nblk - 1 - bi;
+        bool ok = true;
+        for (int t = 0; t < nj; t++) {
+            const int bj = fwd ? t : nblk - 1 - t;
+            const int64_t C0 = (int64_t)bj * FL_B;
+            const int ncol = (int)min((int64_t)FL_B, n - C0);
+            const float* a0 = A + (R0 + r) + (C0 + cq * 32) * ld;
+            float v[2][32];
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                const bool cok = cq * 32 + c < ncol;
+                v[0][c] = (cok && r < nb) ? a0[c * ld] : 0.f;
+                v[1][c] = (cok && r + 64 < nb) ? a0[64 + c * ld] : 0.f;
+            }
+            if (!flow_wait(done, fwd ? bj : nblk - 1 - bj, err, &s_ok)) {
+                ok = false;
+                break;
+            }
+            float* xb = xs + (t & 1) * FL_B * FL_R;
+            reinterpret_cast<float4*>(xb)[tid] =
+                tid < 2 * ncol ? __ldcg(reinterpret_cast<const float4*>(Y + C0 * FL_R) + tid) : make_float4(0, 0, 0, 0);
+            __syncthreads();
+            const float4* x4 = reinterpret_cast<const float4*>(xb) + cq * 64;
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                const float4 xa = x4[2 * c], xb4 = x4[2 * c + 1];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    acc[h][0] -= v[h][c] * xa.x;
+                    acc[h][1] -= v[h][c] * xa.y;
+                    acc[h][2] -= v[h][c] * xa.z;
+                    acc[h][3] -= v[h][c] * xa.w;
+                    acc[h][4] -= v[h][c] * xb4.x;
+                    acc[h][5] -= v[h][c] * xb4.y;
+                    acc[h][6] -= v[h][c] * xb4.z;
+                    acc[h][7] -= v[h][c] * xb4.w;
+                }
+            }
+        }
+        if (!ok) break;
+        __syncthreads();  // x staging (aliased by the sums) no longer read
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float4* d = reinterpret_cast<float4*>(red + (cq * FL_B + r + 64 * h) * FL_R);
+            d[0] = make_float4(acc[h][0], acc[h][1], acc[h][2], acc[h][3]);
+            d[1] = make_float4(acc[h][4], acc[h][5], acc[h][6], acc[h][7]);
+        }
+        __syncthreads();
+        for (int e = tid; e < FL_B * FL_R; e += FL_THREADS)
+            red[e] = red[e] + red[e + FL_B * FL_R] + red[e + 2 * FL_B * FL_R] + red[e + 3 * FL_B * FL_R];
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        // diagonal block: warp q solves right-hand side q, a lane per row of
+        // a 32-row step, then updates the block's remaining rows
+        if (wid < nr) {
+            const int q = wid;
+            const int nsb = (nb + 31) >> 5;
+            if (fwd) {
+                for (int sb = 0; sb < nsb; sb++) {
+                    const int row = sb * 32 + lane;
+                    const float* lrow = Ld + row * FL_LD + sb * 32;
+                    float x = red[row * FL_R + q];
+#pragma unroll
+                    for (int c = 0; c < 32; c++) {
+                        const float xc = __shfl_sync(0xffffffffu, x, c);
+                        if (lane > c) x -= lrow[c] * xc;
+                    }
+                    red[row * FL_R + q] = x;
+                    for (int g = sb + 1; g < nsb; g++) {
+                        const float* l2 = Ld + (g * 32 + lane) * FL_LD + sb * 32;
+                        float d = 0.f;
+#pragma unroll
+                        for (int c = 0; c < 32; c++) d += l2[c] * __shfl_sync(0xffffffffu, x, c);
+                        red[(g * 32 + lane) * FL_R + q] -= d;
+                    }
+                }
+            } else {
+                for (int sb = nsb - 1; sb >= 0; sb--) {
+                    const int row = sb * 32 + lane;
+                    const int cmax = min(32, nb - sb * 32);
+                    const float* urow = Ld + row * FL_LD + sb * 32;
+                    float x = red[row * FL_R + q];
+                    for (int c = cmax - 1; c >= 0; c--) {
+                        if (lane == c) x = x / urow[c];
+                        const float xc = __shfl_sync(0xffffffffu, x, c);
+                        if (lane < c) x -= urow[c] * xc;
+                    }
+                    if (lane >= cmax) x = 0.f;
+                    red[row * FL_R + q] = x;
+                    for (int g = 0; g < sb; g++) {
+                        const float* u2 = Ld + (g * 32 + lane) * FL_LD + sb * 32;
+                        float d = 0.f;
+#pragma unroll
+                        for (int c = 0; c < 32; c++) d += u2[c] * __shfl_sync(0xffffffffu, x, c);
+                        red[(g * 32 + lane) * FL_R + q] -= d;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < 2 * nb)
+            __stcg(reinterpret_cast<float4*>(Y + R0 * FL_R) + tid, reinterpret_cast<const float4*>(red)[tid]);
+        if (!fwd)
+            for (int e = tid; e < FL_B * FL_R; e += FL_THREADS) {
+                const int row = e & (FL_B - 1), q = e >> 7;
+                if (row < nb && q < nr) X[R0 + row + q * ldx] = red[row * FL_R + q];
+            }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_release_gpu(done, fwd ? bi + 1 : nblk - bi);
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");  // leaving early: no copy into shared memory in flight
+}
+
+// ---------------------------------------------------------------------------
 // triangular solves of one large system (n too big for the per-CTA solve):
 // block-row sweeps, each block step = one CTA solving the 32 x 32 diagonal
 // block for every right-hand side + a grid updating all rows below (above)
@@ -1724,6 +1983,90 @@ int64_t lu_plan_launches(const LuPlan& plan, int es) {
         }
     }
     return n + (plan.nsys > 0);  // + the permutation kernel
+}
+
+int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st) {
+    f.release();
+    f.nsys = (int32_t)n_sorted.size();
+    if (f.nsys == 0) return GBVLM_OK;
+    std::vector<int32_t> nblk(f.nsys);
+    int32_t maxblk = 0;
+    int64_t rows = 0;
+    for (int32_t s = 0; s < f.nsys; s++) {
+        GB_REQUIRE(s == 0 || n_sorted[s] <= n_sorted[s - 1], "dataflow solve: systems must be sorted by size");
+        nblk[s] = (int32_t)((n_sorted[s] + FL_B - 1) / FL_B);
+        maxblk = std::max(maxblk, nblk[s]);
+        rows += n_sorted[s];
+    }
+    // forward items by block level, backward items by distance from the last
+    // block; within a level the largest systems (longest chains) first
+    std::vector<int2> items;
+    for (int32_t i = 0; i < maxblk; i++)
+        for (int32_t s = 0; s < f.nsys && nblk[s] > i; s++) items.push_back(make_int2(s, i));
+    f.nfwd = (int32_t)items.size();
+    for (int32_t d = 0; d < maxblk; d++)
+        for (int32_t s = 0; s < f.nsys && nblk[s] > d; s++) items.push_back(make_int2(s, nblk[s] - 1 - d));
+    f.nitems = (int32_t)items.size();
+    GB_CUDA(cudaFuncSetAttribute(k_trs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, FL_SMEM));
+    int dev = 0, sms = 0, per_sm = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trs_flow, FL_THREADS, FL_SMEM));
+    GB_REQUIRE(per_sm > 0, "dataflow solve: kernel does not fit on an SM");
+    f.grid = (int32_t)std::min<int64_t>((int64_t)sms * per_sm, f.nitems);
+    std::vector<float*> yp(f.nsys);
+    GB_CUDA(cudaMalloc(&f.d_items, sizeof(int2) * items.size()));
+    GB_CUDA(cudaMalloc(&f.d_ctl, sizeof(int32_t) * (2 + 2 * (size_t)f.nsys)));
+    GB_CUDA(cudaMalloc(&f.d_y, sizeof(float) * FL_R * (size_t)rows));
+    GB_CUDA(cudaMalloc(&f.d_yp, sizeof(float*) * f.nsys));
+    int64_t off = 0;
+    for (int32_t s = 0; s < f.nsys; s++) {
+        yp[s] = f.d_y + off;
+        off += FL_R * n_sorted[s];
+    }
+    GB_CUDA(cudaMemcpyAsync(f.d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(f.d_yp, yp.data(), sizeof(float*) * yp.size(), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemsetAsync(f.d_ctl, 0, sizeof(int32_t) * (2 + 2 * (size_t)f.nsys), st));
+    GB_CUDA(cudaStreamSynchronize(st));  // the host tables above are about to go out of scope
+    return GBVLM_OK;
+}
+
+int64_t trs_flow_launches(int32_t max_nrhs) { return (max_nrhs + FL_R - 1) / FL_R; }
+
+int trs_flow_solve(const LuBatch<float>& B, const TrsFlow& f, int32_t max_nrhs, cudaStream_t st) {
+    if (f.nitems == 0) return GBVLM_OK;
+    for (int32_t r0 = 0; r0 < max_nrhs; r0 += FL_R) {
+        // the counter and progress words restart; the error word is kept
+        GB_CUDA(cudaMemsetAsync(f.d_ctl, 0, sizeof(int32_t), st));
+        GB_CUDA(cudaMemsetAsync(f.d_ctl + 2, 0, sizeof(int32_t) * 2 * (size_t)f.nsys, st));
+        k_trs_flow<<<f.grid, FL_THREADS, FL_SMEM, st>>>(B, f.d_items, f.nfwd, f.nitems, f.nsys, f.d_ctl, f.d_yp, r0);
+        GB_LAUNCH_CHECK();
+    }
+    return GBVLM_OK;
+}
+
+int trs_flow_check(const TrsFlow& f, cudaStream_t st) {
+    if (!f.d_ctl) return GBVLM_OK;
+    int* h = (int*)host_scratch(sizeof(int));
+    GB_CUDA(cudaMemcpyAsync(h, f.d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (*h != 0) {
+        set_error("triangular solve: a block timed out waiting for the blocks it depends on");
+        return GBVLM_ERR_CUDA;
+    }
+    return GBVLM_OK;
+}
+
+void TrsFlow::release() {
+    if (d_items) cudaFree(d_items);
+    if (d_ctl) cudaFree(d_ctl);
+    if (d_y) cudaFree(d_y);
+    if (d_yp) cudaFree(d_yp);
+    d_items = nullptr;
+    d_ctl = nullptr;
+    d_y = nullptr;
+    d_yp = nullptr;
+    nsys = nfwd = nitems = grid = 0;
 }
 
 void LuPlan::release() {

@@ -103,6 +103,28 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
 template <class T>
 int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t maxn, cudaStream_t st, int* err);
 
+// Dataflow triangular solves of a float batch (k_trs_flow): one persistent
+// launch per 8 right-hand sides runs the forward and backward sweeps of every
+// system in 128-row blocks, items handed out in dependency order.
+struct TrsFlow {
+    int32_t nsys = 0, nfwd = 0, nitems = 0, grid = 0;
+    int2* d_items = nullptr;   // (system, block) in dispatch order
+    int32_t* d_ctl = nullptr;  // counter, error word, per-system forward and backward progress
+    float* d_y = nullptr;      // per system n x 8 row-major
+    float** d_yp = nullptr;    // per-system pointers into d_y
+    void release();
+    ~TrsFlow() { release(); }
+    TrsFlow() = default;
+    TrsFlow(const TrsFlow&) = delete;
+    TrsFlow& operator=(const TrsFlow&) = delete;
+};
+// n_sorted: sizes of all systems of the batch, in batch order
+int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st);
+int trs_flow_solve(const LuBatch<float>& B, const TrsFlow& f, int32_t max_nrhs, cudaStream_t st);
+int64_t trs_flow_launches(int32_t max_nrhs);
+// GBVLM_OK, or an error if a wait of the last solve ran out (synchronises st)
+int trs_flow_check(const TrsFlow& f, cudaStream_t st);
+
 // Single-system tables packed in a small device buffer (*work, grown on demand).
 template <class T>
 int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv, int32_t* perm, int32_t* info, T* X,
