@@ -895,8 +895,12 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         }
     }
     if (rc == GBVLM_OK) {
+        // a single large system solves faster in 128-row blocks on the tensor
+        // cores with every right-hand side at once (its dataflow chain would be
+        // the whole solve); up to that size a system gives the same bits alone
+        // and inside any batch
         const char* fe = getenv("GBVLM_TRS_FLOW");
-        h->use_flow = !(fe && fe[0] == '0');
+        h->use_flow = !(fe && fe[0] == '0') && (h->nsys > 1 || h->maxn <= 4096);
         if (h->use_flow) rc = trs_flow_build(h->flow, lun, 0);
     }
     if (rc) {

@@ -154,11 +154,11 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel(LuBatch<T> B, int64_t k
 //      position on ties, like LAPACK i?amax) with redux.sync; the winning
 //      lane publishes its whole row in shared memory;
 //   2. barrier; every warp reduces the warp candidates of its CTA (and, in a
-//      cluster, the CTA candidates read over DSMEM) and loads the pivot row,
-//      lane t holding column t;
-//   3. each active row is scaled and updated with the pivot row taken from
-//      lane shuffles; the candidate for column jj+1 comes out of the same
-//      pass.
+//      cluster, the CTA candidates read over DSMEM) and finds the pivot
+//      row in shared memory;
+//   3. each active row is scaled and updated with the pivot row read as
+//      16-byte broadcasts (the same address in every lane); the candidate
+//      for column jj+1 comes out of the same pass.
 // Candidate slots and published rows are double-buffered on jj, so a slot is
 // rewritten only after every reader has passed the next barrier.
 template <class T> struct Vec4;
@@ -234,12 +234,34 @@ struct PanelSmem {
 
 template <class T>
 struct PivotOut {
-    T urow;  // lane t: column t of the pivot row
-    int p;   // logical position of the pivot row
+    uint32_t row;  // shared-memory address of the pivot row (32 values, 16-byte aligned)
+    int p;         // logical position of the pivot row
 };
 
-// Steps 2 of a column: barrier, CTA-wide (and cluster-wide) winner, pivot row
-// to the lanes.  Kept out of line: called once per column from the
+// pivot-row reads: the same address in every lane (a broadcast)
+__device__ __forceinline__ void lds4(uint32_t a, float (&v)[4]) {
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "r"(a));
+}
+__device__ __forceinline__ void lds4(uint32_t a, double (&v)[4]) {
+    asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "r"(a));
+    asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v[2]), "=d"(v[3]) : "r"(a + 16));
+}
+__device__ __forceinline__ float lds1(uint32_t a, float) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ double lds1(uint32_t a, double) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(a));
+    return v;
+}
+// reciprocal rounded to nearest, the value of 1 / d in IEEE arithmetic
+__device__ __forceinline__ float rcp_rn(float d) { return __frcp_rn(d); }
+__device__ __forceinline__ double rcp_rn(double d) { return __drcp_rn(d); }
+
+// Steps 2 of a column: barrier, CTA-wide (and cluster-wide) winner, the
+// pivot row's shared-memory address.  Kept out of line: called once per column from the
 // unrolled column loop, it is the same code for all 32 columns.
 template <class T, int NT, bool CLUSTER>
 __device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank) {
@@ -270,10 +292,10 @@ __device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank)
         const Key cbest = ck.warp_max();
         const int q = __ffs(__ballot_sync(0xffffffffu, lane < csize && ck == cbest)) - 1;
         o.p = cbest.pos();
-        o.urow = sm.c_row[buf][q][lane];
+        o.row = (uint32_t)__cvta_generic_to_shared(&sm.c_row[buf][q][0]);
     } else {
         o.p = best.pos();
-        o.urow = sm.s_row[buf][w][lane];
+        o.row = (uint32_t)__cvta_generic_to_shared(&sm.s_row[buf][w][0]);
     }
     return o;
 }
@@ -342,9 +364,8 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
             }
             // 2. pivot: (p, row) known to every warp
             const PivotOut<T> po = panel_exchange<T, NT, CLUSTER>(buf, csize, rank);
-            const T urow = po.urow;
             const int p = po.p;
-            const T d = __shfl_sync(0xffffffffu, urow, jj);
+            const T d = lds1(po.row + jj * (uint32_t)sizeof(T), T(0));
             if (tid == 0 && rank == 0) {
                 ipiv[k + jj] = (int32_t)(k + p);  // a store: nothing waits on it
                 if (d == (T)0 && zero_col < 0) zero_col = jj;
@@ -352,7 +373,7 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
             // 3. interchange of logical positions jj <-> p, then scale and update;
             // scaling by the reciprocal of the pivot (LAPACK ?getf2), dividing when it is subnormal
             const bool big = tabs(d) >= (sizeof(T) == 4 ? (T)FLT_MIN : (T)DBL_MIN);
-            const T rd = big ? (T)1 / d : (T)0;
+            const T rd = big ? rcp_rn(d) : (T)0;
             T lm[RPT];
             bool active[RPT];
 #pragma unroll
@@ -367,12 +388,18 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
                     x[i][jj] = lm[i];
                 }
             }
+            // the pivot row's columns jj+1.. as 16-byte broadcasts from shared memory
 #pragma unroll
-            for (int t = jj + 1; t < GK; t++) {
-                const T u = __shfl_sync(0xffffffffu, urow, t);
+            for (int tg = (jj + 1) & ~3; tg < GK; tg += 4) {
+                T u[4];
+                lds4(po.row + tg * (uint32_t)sizeof(T), u);
 #pragma unroll
-                for (int i = 0; i < RPT; i++)
-                    if (active[i]) x[i][t] -= lm[i] * u;
+                for (int e = 0; e < 4; e++)
+                    if (tg + e > jj) {
+#pragma unroll
+                        for (int i = 0; i < RPT; i++)
+                            if (active[i]) x[i][tg + e] -= lm[i] * u[e];
+                    }
             }
             if constexpr (jj + 1 < GK) {
                 cand = Key::none();
@@ -1524,8 +1551,8 @@ static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, cons
         GB_LAUNCH_CHECK();
         return GBVLM_OK;
     }
-    if constexpr (sizeof(T) == 4) {  // one row per thread (two per thread measured slower: longer
-                                     // per-thread chains, fewer warps to hide them)
+    if constexpr (sizeof(T) == 4) {  // one row per thread (two per thread, half the warps, measured
+                                     // slower with both shuffled and shared-memory pivot rows)
         switch (g.nt) {
             case 128: return launch_panel_nt<T, 128, 1>(B, k, act, g, st);
             case 256: return launch_panel_nt<T, 256, 1>(B, k, act, g, st);
