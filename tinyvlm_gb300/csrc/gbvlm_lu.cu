@@ -968,8 +968,8 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
 constexpr int FL_B = 128;
 constexpr int FL_THREADS = 256;
 constexpr int FL_R = 8;  // right-hand sides per launch
-constexpr int FL_LD = FL_B + 1;
-constexpr int FL_SMEM = (FL_B * FL_LD + 4 * FL_B * FL_R) * 4;  // diagonal block + quarter sums (x staging aliased)
+constexpr int FL_LD = FL_B + 4;  // rows 16-byte aligned: a lane reads its row as float4, conflict-free
+constexpr int FL_SMEM = (FL_B * FL_LD + 5 * FL_B * FL_R) * 4;  // diagonal block + quarter sums (x staging aliased) + the block's values
 
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
     int v;
@@ -1012,6 +1012,61 @@ __device__ __forceinline__ bool flow_wait(const int* cnt, int need, int* err, in
     return ok;
 }
 
+// One warp inverts the 32-row triangle sb of the diagonal block in place,
+// lane j computing column j by substitution on the unit vector e_j: the
+// strict lower part of L^-1 (unit lower, forward sweep) or the upper part
+// with the diagonal of U^-1 (backward sweep).  Rows at or past nb are left
+// zero.
+__device__ __noinline__ void flow_invert_lower(float* T, int lane) {
+    float t[32];
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        float d0 = 0.f, d1 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 32; c++)
+            if (c < r) {
+                if (c & 1) d1 += T[r * FL_LD + c] * t[c];
+                else d0 += T[r * FL_LD + c] * t[c];
+            }
+        t[r] = r < lane ? 0.f : (r == lane ? 1.f : -(d0 + d1));
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; r++)
+        if (r > lane) T[r * FL_LD + lane] = t[r];
+}
+
+__device__ __noinline__ void flow_invert_upper(float* T, int cmax, int lane) {
+    float t[32];
+#pragma unroll
+    for (int r = 31; r >= 0; r--) {
+        float d0 = 0.f, d1 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 32; c++)
+            if (c > r) {
+                if (c & 1) d1 += T[r * FL_LD + c] * t[c];
+                else d0 += T[r * FL_LD + c] * t[c];
+            }
+        const float rd = r < cmax ? __frcp_rn(T[r * FL_LD + r]) : 0.f;
+        t[r] = r > lane ? 0.f : (r == lane ? rd : -(d0 + d1) * rd);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; r++)
+        if (r <= lane) T[r * FL_LD + lane] = lane < cmax ? t[r] : 0.f;
+}
+
+// One warp inverts the 32-row triangle sb of the diagonal block in place,
+// lane j computing column j by substitution on the unit vector e_j: the
+// strict lower part of L^-1 (unit lower, forward sweep) or the upper part
+// with the diagonal of U^-1 (backward sweep).  Rows at or past nb are left
+// zero.
+__device__ __forceinline__ void flow_invert_tri(float* Ld, int sb, int nb, bool fwd, int lane) {
+    float* T = Ld + sb * 32 * FL_LD + sb * 32;  // T[r * FL_LD + c]
+    if (fwd) flow_invert_lower(T, lane);
+    else flow_invert_upper(T, min(32, nb - sb * 32), lane);
+}
+
 // ctl: [0] dispatch counter, [1] error word, [2, 2 + nsys) forward blocks
 // finished per system, [2 + nsys, 2 + 2 nsys) backward blocks finished
 __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, const int2* items, int nfwd, int nitems,
@@ -1019,7 +1074,8 @@ __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, co
     extern __shared__ __align__(16) float fsm[];
     float* Ld = fsm;                  // [FL_B][FL_LD] diagonal block
     float* xs = fsm + FL_B * FL_LD;   // [2][FL_B][FL_R] x of an off-diagonal block (two buffers)
-    float* red = xs;                  // [4][FL_B][FL_R] column-quarter sums, then [FL_B][FL_R] the block's values
+    float* red = xs;                  // [4][FL_B][FL_R] column-quarter sums
+    float* xT = red + 4 * FL_B * FL_R;  // [FL_R][FL_B] the block's values, a right-hand side per row
     __shared__ int s_item, s_ok;
     int* err = ctl + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -1085,6 +1141,12 @@ __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, co
                 }
             }
         }
+        // the diagonal block's 32-row triangles inverted in place (warp sb:
+        // triangle sb) while the item may still wait for other blocks
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        if (wid < 4 && wid * 32 < nb) flow_invert_tri(Ld, wid, nb, fwd, lane);
+        __syncthreads();
         // off-diagonal blocks, in the order their x become final
         const int nj = fwd ? bi : nblk - 1 - bi;
         bool ok = true;
@@ -1134,70 +1196,73 @@ __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, co
             d[1] = make_float4(acc[h][4], acc[h][5], acc[h][6], acc[h][7]);
         }
         __syncthreads();
-        for (int e = tid; e < FL_B * FL_R; e += FL_THREADS)
-            red[e] = red[e] + red[e + FL_B * FL_R] + red[e + 2 * FL_B * FL_R] + red[e + 3 * FL_B * FL_R];
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        for (int e = tid; e < FL_B * FL_R; e += FL_THREADS)  // e = row * FL_R + q
+            xT[(e & (FL_R - 1)) * FL_B + (e >> 3)] =
+                red[e] + red[e + FL_B * FL_R] + red[e + 2 * FL_B * FL_R] + red[e + 3 * FL_B * FL_R];
         __syncthreads();
-        // diagonal block: warp q solves right-hand side q, a lane per row of
-        // a 32-row step, then updates the block's remaining rows
+        // diagonal block: warp q solves right-hand side q, 32 rows at a time
+        // (a lane per row): the 32 values times the lane's row of the
+        // inverted triangle, then the block's remaining rows updated with the
+        // 32 results.  Rows of the tile and the 32 values are read as float4
+        // (the values as broadcasts); rows past nb hold zeros throughout.
         if (wid < nr) {
-            const int q = wid;
+            float* xq = xT + wid * FL_B;
             const int nsb = (nb + 31) >> 5;
+            auto dot32 = [&](const float* arow, const float* vals) {
+                const float4* a4 = reinterpret_cast<const float4*>(arow);
+                const float4* v4 = reinterpret_cast<const float4*>(vals);
+                float e0 = 0.f, e1 = 0.f, e2 = 0.f, e3 = 0.f;
+#pragma unroll
+                for (int m = 0; m < 8; m++) {
+                    const float4 av = a4[m], vv = v4[m];
+                    e0 += av.x * vv.x;
+                    e1 += av.y * vv.y;
+                    e2 += av.z * vv.z;
+                    e3 += av.w * vv.w;
+                }
+                return (e0 + e1) + (e2 + e3);
+            };
             if (fwd) {
                 for (int sb = 0; sb < nsb; sb++) {
                     const int row = sb * 32 + lane;
-                    const float* lrow = Ld + row * FL_LD + sb * 32;
-                    float x = red[row * FL_R + q];
-#pragma unroll
-                    for (int c = 0; c < 32; c++) {
-                        const float xc = __shfl_sync(0xffffffffu, x, c);
-                        if (lane > c) x -= lrow[c] * xc;
-                    }
-                    red[row * FL_R + q] = x;
-                    for (int g = sb + 1; g < nsb; g++) {
-                        const float* l2 = Ld + (g * 32 + lane) * FL_LD + sb * 32;
-                        float d = 0.f;
-#pragma unroll
-                        for (int c = 0; c < 32; c++) d += l2[c] * __shfl_sync(0xffffffffu, x, c);
-                        red[(g * 32 + lane) * FL_R + q] -= d;
-                    }
+                    // row of L^-1: zero on and above the diagonal (its unit diagonal implied)
+                    const float x = xq[row] + dot32(Ld + row * FL_LD + sb * 32, xq + sb * 32);
+                    __syncwarp();
+                    xq[row] = x;
+                    __syncwarp();
+                    for (int g = sb + 1; g < nsb; g++)
+                        xq[g * 32 + lane] -= dot32(Ld + (g * 32 + lane) * FL_LD + sb * 32, xq + sb * 32);
+                    __syncwarp();  // the next step reads rows other lanes updated
                 }
             } else {
                 for (int sb = nsb - 1; sb >= 0; sb--) {
                     const int row = sb * 32 + lane;
-                    const int cmax = min(32, nb - sb * 32);
-                    const float* urow = Ld + row * FL_LD + sb * 32;
-                    float x = red[row * FL_R + q];
-                    for (int c = cmax - 1; c >= 0; c--) {
-                        if (lane == c) x = x / urow[c];
-                        const float xc = __shfl_sync(0xffffffffu, x, c);
-                        if (lane < c) x -= urow[c] * xc;
-                    }
-                    if (lane >= cmax) x = 0.f;
-                    red[row * FL_R + q] = x;
-                    for (int g = 0; g < sb; g++) {
-                        const float* u2 = Ld + (g * 32 + lane) * FL_LD + sb * 32;
-                        float d = 0.f;
-#pragma unroll
-                        for (int c = 0; c < 32; c++) d += u2[c] * __shfl_sync(0xffffffffu, x, c);
-                        red[(g * 32 + lane) * FL_R + q] -= d;
-                    }
+                    // row of U^-1: zero below the diagonal
+                    float x = dot32(Ld + row * FL_LD + sb * 32, xq + sb * 32);
+                    if (lane >= min(32, nb - sb * 32)) x = 0.f;
+                    __syncwarp();
+                    xq[row] = x;
+                    __syncwarp();
+                    for (int g = 0; g < sb; g++)
+                        xq[g * 32 + lane] -= dot32(Ld + (g * 32 + lane) * FL_LD + sb * 32, xq + sb * 32);
+                    __syncwarp();  // the next step reads rows other lanes updated
                 }
             }
         }
         __syncthreads();
-        if (tid < 2 * nb)
-            __stcg(reinterpret_cast<float4*>(Y + R0 * FL_R) + tid, reinterpret_cast<const float4*>(red)[tid]);
+        if (tid < 2 * nb) {
+            const int row = tid >> 1, q0 = (tid & 1) * 4;
+            __stcg(reinterpret_cast<float4*>(Y + R0 * FL_R) + tid,
+                   make_float4(xT[q0 * FL_B + row], xT[(q0 + 1) * FL_B + row], xT[(q0 + 2) * FL_B + row],
+                               xT[(q0 + 3) * FL_B + row]));
+        }
         if (!fwd)
             for (int e = tid; e < FL_B * FL_R; e += FL_THREADS) {
                 const int row = e & (FL_B - 1), q = e >> 7;
-                if (row < nb && q < nr) X[R0 + row + q * ldx] = red[row * FL_R + q];
+                if (row < nb && q < nr) X[R0 + row + q * ldx] = xT[q * FL_B + row];
             }
         __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            st_release_gpu(done, fwd ? bi + 1 : nblk - bi);
-        }
+        if (tid == 0) st_release_gpu(done, fwd ? bi + 1 : nblk - bi);  // after the barrier: publishes the CTA's writes
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");  // leaving early: no copy into shared memory in flight
 }
