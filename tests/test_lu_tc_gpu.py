@@ -3,7 +3,8 @@ same matrices: the tensor-core trailing update (3xTF32, the default) must keep
 the solution error at the level of a plain fp32 factorisation; the CUDA-core
 path (GBVLM_LU_TC=0) likewise; plain TF32 (GBVLM_LU_TC=1) only to TF32
 accuracy.  Sizes cover one and several 128-column outer blocks, ragged
-edges, and panels split over a thread-block cluster."""
+edges, panels split over a thread-block cluster, and a system taller than
+4096 rows."""
 import os
 
 import numpy as np
@@ -52,7 +53,7 @@ def _lapack_err(A, b, x_true):
     return np.abs(x.T.astype(np.float64) - x_true).max() / np.abs(x_true).max()
 
 
-@pytest.mark.parametrize("n", [129, 256, 300, 1000, 1100, 2500])
+@pytest.mark.parametrize("n", [129, 256, 300, 1000, 1100, 2500, 4500])
 @pytest.mark.parametrize("boost", [0.0, 2.0])
 def test_lu_float_accuracy(cuda, n, boost):
     A, b = _matrix(n, 1000 + n, boost)
@@ -71,3 +72,28 @@ def test_lu_tf32(cuda, n):
     x = _solve(A, b, "1")
     err = np.abs(x - x_true).max() / np.abs(x_true).max()
     assert err <= 5e-2, err  # tf32 operands: ~1e-3 relative per product
+
+
+def test_batch_with_tall_system(cuda):
+    """A 4608-unknown wing (8-CTA cluster panels for its first steps) in a
+    batch with small ones: every solve within the batched path's bar of the double
+    oracle."""
+    from oracle import oracle as O
+    from tinyvlm_gb300 import mesh as M
+    from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+    rng = np.random.default_rng(5)
+    cases = []
+    for nc, ns in [(48, 96), (8, 30), (4, 12)]:
+        v = M.trapezoid(nc, ns, 8.0, 0.5, 15.0)
+        M.quarter_chord(v)
+        cases.append(M.Case(v.astype(np.float32), np.radians(rng.uniform(-6, 6, size=3)), {}))
+    bs = BatchSolver(cases, mode="shared", refine=1)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=(0.25, 0.0, 0.0))
+    bs.run()
+    co, _ = bs.results()
+    k = 0
+    for c in cases:
+        for r in O.vlm_shared([c.verts.astype(np.float64)], c.alphas, ref_pt=(0.25, 0.0, 0.0)):
+            cl = float(r["cl"])
+            assert abs(co[k, 0] - cl) <= 1e-5 * max(abs(cl), 1e-3), (c.n, k, co[k, 0], cl)
+            k += 1

@@ -765,6 +765,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     const size_t o_luX = reserve(sizeof(float*) * h->nsys);
     const size_t o_lurhs = reserve(sizeof(int32_t) * h->nsys);
     const size_t o_luperm = reserve(sizeof(int32_t*) * h->nsys);
+    const size_t o_lumv = reserve(sizeof(int32_t) * 64 * h->nsys);
     cudaError_t e = cudaMalloc(&h->arena, bytes);
     if (e != cudaSuccess) {
         delete h;
@@ -868,6 +869,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     h->lub.ldx = (const int64_t*)(base + o_lun);
     h->lub.nrhs = (const int32_t*)(base + o_lurhs);
     h->lub.perm = (int32_t* const*)(base + o_luperm);
+    h->lub.mv = (int32_t*)(base + o_lumv);
     // size groups: n > 1024, 384 < n <= 1024, n <= 384 (empty groups dropped)
     {
         const int64_t bounds[MAX_GROUPS_B] = {1024, 384};

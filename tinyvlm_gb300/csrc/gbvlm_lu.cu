@@ -412,6 +412,16 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
     if constexpr (CLUSTER) cg::this_cluster().sync();  // no CTA leaves while its rows may still be read
     // panels of a system run in order, so the first zero pivot recorded is the first of the factorisation
     if (zero_col >= 0) atomicCAS(&B.info[sid], 0, (int32_t)(k + zero_col + 1));
+    if (B.mv) {  // the panel's row moves, for the other columns of the outer block
+        int32_t* mv = B.mv + (int64_t)sid * 64;
+#pragma unroll
+        for (int i = 0; i < RPT; i++)
+            if (lid[i] >= 0) {
+                const int r = rank * slab + tid + i * NT;
+                if (lid[i] < GK) mv[lid[i]] = r;
+                if (r < GK) mv[GK + r] = lid[i];
+            }
+    }
 #pragma unroll
     for (int i = 0; i < RPT; i++)
         if (lid[i] >= 0) {
@@ -615,6 +625,68 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
         const int r = e & (WW - 1), j = e >> 7;
         if (j < ncols) Xo[r + (int64_t)j * ld] = X[r * TW_XS + j];
     }
+}
+
+// ---------------------------------------------------------------------------
+// inner step of the two-level float factorisation, after the panel of
+// columns [k, k + nb) inside the outer block [k0, kend): for the outer
+// block's other columns, the panel's row moves (from the move lists the
+// panel wrote: LAPACK's sequential interchanges composed) and the U rows
+// U12 = L11^-1 A12 right of the panel; the update of the rows below follows
+// in 64 x 64 tiles (k_update).  A CTA owns IN_COLS columns of one system:
+// warp c, lane t holds column c, row t of the 32 moved rows; all moved values
+// are read before any is written (a pivot row's old place receives a
+// displaced top row), and the U rows are solved by shuffles down the warp.
+// (Updating the rows below here as well, a thread per row, measured slower:
+// it costs more SM time than the tiles.)
+// ---------------------------------------------------------------------------
+constexpr int IN_COLS = 16;
+constexpr int IN_THREADS = 512;  // IN_COLS warps of 32 rows
+
+__global__ void __launch_bounds__(IN_THREADS) k_inner(LuBatch<float> B, int64_t k, int64_t k0, int64_t kend,
+                                                     const int32_t* act, const int64_t* pfx, int cnt) {
+    __shared__ float L11[GK][GK + 1];
+    __shared__ int32_t msrc[GK], mdst[GK];
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    float* A = B.A[sid];
+    const int nb = (int)min((int64_t)GK, n - k);  // rows k .. k + nb - 1 and their pivots move
+    // chunks: the columns left of the panel [k0, k), then right of it [k + nb, min(n, kend))
+    const int64_t nleft = k - k0;
+    const int64_t cidx = (int64_t)(blockIdx.x - pfx[a]) * IN_COLS;
+    const bool right = cidx >= nleft;
+    const int64_t c0 = right ? k + nb + (cidx - nleft) : k0 + cidx;
+    const int cw = (int)min((int64_t)IN_COLS, (right ? min(n, kend) : k) - c0);
+    const int tid = threadIdx.x, t = tid & 31, c = tid >> 5;
+    if (tid < GK) {
+        const int32_t* mv = B.mv + (int64_t)sid * 64;
+        msrc[tid] = tid < nb ? mv[tid] : tid;
+        mdst[tid] = tid < nb ? mv[GK + tid] : tid;
+    }
+    if (right)
+        for (int e = tid; e < GK * GK; e += IN_THREADS) {
+            const int rr = e & (GK - 1), cc = e >> 5;
+            L11[rr][cc] = rr < nb && cc < nb ? A[(k + rr) + (k + cc) * ld] : 0.f;
+        }
+    __syncthreads();
+    const bool live = c < cw && t < nb;
+    float* col = A + (c0 + c) * ld;
+    float top = 0.f, out = 0.f;
+    if (live) {
+        top = col[k + msrc[t]];  // the row that ends at k + t
+        out = col[k + t];        // the row that starts at k + t
+    }
+    __syncthreads();  // every moved value read before any is written
+    if (live && mdst[t] >= GK) col[k + mdst[t]] = out;
+    if (right) {
+#pragma unroll
+        for (int r = 0; r < GK; r++) {
+            const float xr = __shfl_sync(0xffffffffu, top, r);
+            if (t > r) top -= L11[t][r] * xr;
+        }
+    }
+    if (live) col[k + t] = top;
 }
 
 // ---------------------------------------------------------------------------
@@ -1617,7 +1689,8 @@ static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, cons
         return GBVLM_OK;
     }
     if constexpr (sizeof(T) == 4) {  // one row per thread (two per thread, half the warps, measured
-                                     // slower with both shuffled and shared-memory pivot rows)
+                                     // slower with both shuffled and shared-memory pivot rows, and for
+                                     // the cluster panels alone)
         switch (g.nt) {
             case 128: return launch_panel_nt<T, 128, 1>(B, k, act, g, st);
             case 256: return launch_panel_nt<T, 256, 1>(B, k, act, g, st);
@@ -1664,19 +1737,17 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
         }
         // two-level blocking, outer block [k0, kend)
         const int64_t k0 = S.kend - plan.W;
-        if (S.iswap_total > 0) {
-            k_swap2<T><<<(unsigned)cdiv(S.iswap_total, 256), 256, 0, st>>>(B, act, plan.d_pfx + S.iswap_pfx, S.n_panel,
-                                                                        S.k, S.k + GK, k0, S.k, S.k + GK, S.kend);
-            GB_LAUNCH_CHECK();
-        }
-        if (S.itrsm_blocks > 0) {
-            k_trsm<T><<<(unsigned)S.itrsm_blocks, TRSM_COLS, 0, st>>>(B, S.k, act, plan.d_pfx + S.itrsm_pfx, S.n_panel,
-                                                                    S.kend);
-            GB_LAUNCH_CHECK();
-        }
-        if (S.in_blocks > 0) {
-            k_update<T><<<(unsigned)S.in_blocks, 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.in_pfx, S.n_in, S.kend, 1);
-            GB_LAUNCH_CHECK();
+        // the panel's row moves and U rows in one launch, then the inner update in tiles
+        if constexpr (sizeof(T) == 4) {
+            if (S.ik_blocks > 0) {
+                k_inner<<<(unsigned)S.ik_blocks, IN_THREADS, 0, st>>>(B, S.k, k0, S.kend, act, plan.d_pfx + S.ik_pfx,
+                                                                      S.n_panel);
+                GB_LAUNCH_CHECK();
+            }
+            if (S.in_blocks > 0) {
+                k_update<T><<<(unsigned)S.in_blocks, 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.in_pfx, S.n_in, S.kend, 1);
+                GB_LAUNCH_CHECK();
+            }
         }
         if (pending && ((S.bswap_first == 0 && S.bswap_total > 0) || S.tc_blocks > 0)) {
             // at the block's last step its swaps (and U12 solve) reach the columns the
@@ -1943,26 +2014,6 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         // two-level blocking (float, tensor cores): outer block [k0, kend) of W columns
         S.kend = (k / plan.W + 1) * plan.W;
         const int64_t k0 = S.kend - plan.W;
-        // inner swap: columns [k0, k) and [k + GK, kend) of the outer panel
-        S.iswap_pfx = (int64_t)pfx.size();
-        acc = 0;
-        for (int i = 0; i < cnt; i++) {
-            pfx.push_back(acc);
-            const int64_t n = n_sorted[i];
-            acc += (k - k0) + std::max<int64_t>(0, std::min(n, S.kend) - std::min(n, k + GK));
-        }
-        pfx.push_back(acc);
-        S.iswap_total = acc;
-        // inner trsm: columns [k + nb, min(n, kend))
-        S.itrsm_pfx = (int64_t)pfx.size();
-        acc = 0;
-        for (int i = 0; i < cnt; i++) {
-            pfx.push_back(acc);
-            const int64_t m = std::min(n_sorted[i], S.kend) - k - std::min<int64_t>(GK, n_sorted[i] - k);
-            acc += m > 0 ? cdiv(m, TRSM_COLS) : 0;
-        }
-        pfx.push_back(acc);
-        S.itrsm_blocks = acc;
         // inner update: rows [k + GK, n) x columns [k + GK, min(n, kend))
         S.in_pfx = (int64_t)pfx.size();
         acc = 0;
@@ -1977,6 +2028,16 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         pfx.push_back(acc);
         S.n_in = ci;
         S.in_blocks = acc;
+        // k_inner: IN_COLS-column chunks of [k0, k) and [k + nb, min(n, kend))
+        S.ik_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < cnt; i++) {
+            pfx.push_back(acc);
+            const int64_t n = n_sorted[i], nbk = std::min<int64_t>(GK, n - k);
+            acc += (k - k0) / IN_COLS + cdiv(std::max<int64_t>(0, std::min(n, S.kend) - (k + nbk)), IN_COLS);
+        }
+        pfx.push_back(acc);
+        S.ik_blocks = acc;
         // end of the outer block for the systems whose last step in it is this one:
         // all active systems at the block's last step, else those with n <= k + GK
         const bool block_end = k + GK == S.kend;
@@ -2070,7 +2131,7 @@ int64_t lu_plan_launches(const LuPlan& plan, int es) {
         if (!two_level) {
             n += (S.swap_total > 0) + (S.trsm_blocks > 0) + (S.upd_blocks > 0);
         } else {
-            n += (S.iswap_total > 0) + (S.itrsm_blocks > 0) + (S.in_blocks > 0) + (S.bswap_total > 0) +
+            n += (S.ik_blocks > 0) + (S.in_blocks > 0) + (S.bswap_total > 0) +
                  2 * (S.tc_blocks > 0) + (S.tc_blocks > 0 && plan.la_stream && S.tcr_blocks > 0);
         }
     }
@@ -2225,11 +2286,13 @@ int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv,
         int32_t nrhs;
         int32_t* perm;
     } tab{n, ld, ldx, A, ipiv, X, nrhs, perm};
-    if (*work_bytes < sizeof(Tab)) {
+    constexpr size_t MV_OFF = 256;  // the panel's move lists after the table
+    static_assert(sizeof(Tab) <= MV_OFF, "table larger than its slot");
+    if (*work_bytes < MV_OFF + 64 * sizeof(int32_t)) {
         if (*work) cudaFree(*work);
         *work = nullptr;
-        GB_CUDA(cudaMalloc(work, 256));
-        *work_bytes = 256;
+        GB_CUDA(cudaMalloc(work, MV_OFF + 64 * sizeof(int32_t)));
+        *work_bytes = MV_OFF + 64 * sizeof(int32_t);
     }
     // pageable source: the call returns once the table is staged, so the
     // stack copy may go out of scope
@@ -2244,6 +2307,7 @@ int make_single_batch(LuBatch<T>& B, int64_t n, int64_t ld, T* A, int32_t* ipiv,
     B.nrhs = &d->nrhs;
     B.perm = &d->perm;
     B.info = info;
+    B.mv = (int32_t*)((char*)*work + MV_OFF);
     return GBVLM_OK;
 }
 template int make_single_batch<float>(LuBatch<float>&, int64_t, int64_t, float*, int32_t*, int32_t*, int32_t*, float*,

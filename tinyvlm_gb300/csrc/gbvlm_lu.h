@@ -22,6 +22,11 @@ struct LuBatch {
     const int64_t* ldx;
     const int32_t* nrhs;
     int32_t* const* perm;  // row permutation of the factorisation (perm[r] = original row), n per system
+    // float two-level factorisation: the row moves of the last 32-column panel,
+    // 64 entries per system at sid * 64: [t] = offset below k of the row that
+    // ends at position k + t, [32 + r] = final offset of the row that started
+    // at k + r (null: not recorded)
+    int32_t* mv = nullptr;
 };
 
 // One panel launch: active systems [first, first + count) of a step, each
@@ -45,10 +50,9 @@ struct LuStep {
     int64_t upd_pfx = 0, upd_blocks = 0;  // whole trailing update (one-level blocking)
     // two-level blocking: outer block [kend - LuPlan::W, kend)
     int64_t kend = 0;
-    int64_t iswap_pfx = 0, iswap_total = 0;   // inner swaps, outer-panel columns
-    int64_t itrsm_pfx = 0, itrsm_blocks = 0;  // inner U rows, outer-panel columns
     int32_t n_in = 0;                         // systems with an inner update (a prefix)
     int64_t in_pfx = 0, in_blocks = 0;        // inner update of the outer panel, 64 x 64 tiles
+    int64_t ik_pfx = 0, ik_blocks = 0;        // k_inner: row moves and U rows, 16-column chunks of the outer panel
     int32_t bswap_first = 0;                  // systems [bswap_first, n_panel) end the outer block here
     int64_t bswap_pfx = 0, bswap_total = 0;   // the block's swaps on the columns outside it
     int32_t n_tc = 0;                         // systems with n > kend at the block's last step (a prefix)

@@ -186,50 +186,49 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     const int nchunks = (K + BK - 1) / BK;
     bool ok = true;
     int committed = -1;  // last chunk whose MMAs were committed
+    // operand chunks pass through registers: chunk c + 1 is loaded from global
+    // memory while the MMAs of chunk c run (one shared-memory stage)
+    const int arow = tid & (BM - 1), akh = (tid >> 7) * 16;
+    float va[16], vb[16];
+    auto load_chunk = [&](int c) {
+        const int kc = c * BK;
+        const bool rv = arow < m_rows;  // A: thread = tile row, 16 K values of its half
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++)
+            va[kk] = (rv && kc + akh + kk < K) ? Lp[arow + (int64_t)(kc + akh + kk) * ldl] : 0.f;
+        const bool kv = kc + lane < K;  // B: warp w, tile columns 16w..16w+15, lane = K index
+#pragma unroll
+        for (int cc = 0; cc < 16; cc++) {
+            const int col = 16 * wid + cc;
+            vb[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ldu] : 0.f;
+        }
+    };
+    if (nchunks > 0) load_chunk(0);
     for (int c = 0; c < nchunks; c++) {
         const int s = c % STAGES;
         // stage s is free once the MMAs of chunk c - STAGES are done
         const bool free_ = c < STAGES || mbar_wait(&bar[s], ((c - STAGES) / STAGES) & 1);
         const uint32_t a_hi = base + s * STAGE_BYTES, a_lo = a_hi + CHUNK_BYTES;
         const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
-        const int kc = c * BK;
         if (free_) {
-            // A chunk: thread = tile row (tid % 128), 16 K values of its half (coalesced across the warp per K)
-            {
-                const int row = tid & (BM - 1), kh = (tid >> 7) * 16;
-                float v[16];
-                const bool rv = row < m_rows;
 #pragma unroll
-                for (int kk = 0; kk < 16; kk++)
-                    v[kk] = (rv && kc + kh + kk < K) ? Lp[row + (int64_t)(kc + kh + kk) * ldl] : 0.f;
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const uint32_t off = sw128_off(row, kh + 4 * j);
-                    const float h0 = tf32_hi(v[4 * j]), h1 = tf32_hi(v[4 * j + 1]);
-                    const float h2 = tf32_hi(v[4 * j + 2]), h3 = tf32_hi(v[4 * j + 3]);
-                    st_shared_v4(a_hi + off, h0, h1, h2, h3);
-                    if (PASSES > 1)
-                        st_shared_v4(a_lo + off, v[4 * j] - h0, v[4 * j + 1] - h1, v[4 * j + 2] - h2,
-                                     v[4 * j + 3] - h3);
-                }
+            for (int j = 0; j < 4; j++) {
+                const uint32_t off = sw128_off(arow, akh + 4 * j);
+                const float h0 = tf32_hi(va[4 * j]), h1 = tf32_hi(va[4 * j + 1]);
+                const float h2 = tf32_hi(va[4 * j + 2]), h3 = tf32_hi(va[4 * j + 3]);
+                st_shared_v4(a_hi + off, h0, h1, h2, h3);
+                if (PASSES > 1)
+                    st_shared_v4(a_lo + off, va[4 * j] - h0, va[4 * j + 1] - h1, va[4 * j + 2] - h2,
+                                 va[4 * j + 3] - h3);
             }
-            // B chunk: warp w covers tile columns 16w..16w+15, lane = K index (coalesced along the column)
-            {
-                float v[16];
-                const bool kv = kc + lane < K;
 #pragma unroll
-                for (int cc = 0; cc < 16; cc++) {
-                    const int col = 16 * wid + cc;
-                    v[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ldu] : 0.f;
-                }
-#pragma unroll
-                for (int cc = 0; cc < 16; cc++) {
-                    const uint32_t off = sw128_off(16 * wid + cc, lane);
-                    const float h = tf32_hi(v[cc]);
-                    st_shared_f32(b_hi + off, h);
-                    if (PASSES > 1) st_shared_f32(b_lo + off, v[cc] - h);
-                }
+            for (int cc = 0; cc < 16; cc++) {
+                const uint32_t off = sw128_off(16 * wid + cc, lane);
+                const float h = tf32_hi(vb[cc]);
+                st_shared_f32(b_hi + off, h);
+                if (PASSES > 1) st_shared_f32(b_lo + off, vb[cc] - h);
             }
+            if (c + 1 < nchunks) load_chunk(c + 1);
         }
         fence_async_smem();  // generic-proxy stores visible to the tensor core
         fence_before_sync();
@@ -251,30 +250,37 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
         }
         committed = c;
     }
+    // the first half of this thread's C in flight while the last MMAs finish
+    const int erow = 32 * (wid & 3) + lane;
+    const bool erv = erow < m_rows;
+    float cpre[32];
+    {
+        const int cb = 64 * (wid >> 2);
+#pragma unroll
+        for (int j = 0; j < 32; j++) cpre[j] = (ok && erv && cb + j < n_cols) ? Cp[erow + (int64_t)(cb + j) * ldc] : 0.f;
+    }
     // every committed MMA done (the last commit covers all earlier ones)
     bool done = committed < 0 || mbar_wait(&bar[committed % STAGES], (committed / STAGES) & 1);
     done = __syncthreads_and(done) != 0;
     fence_after_sync();
     if (ok && done) {
-        const int row = 32 * (wid & 3) + lane;
-        const bool rv = row < m_rows;
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             const int cb = 64 * (wid >> 2) + 32 * q;
             float v[32];
             tmem_ld32(tmem + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)cb, v);
-            if (rv) {
+            if (erv) {
                 // all 32 loads before the stores: a load may not pass a store to the same array
                 float c[32];
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const int col = cb + j;
-                    c[j] = col < n_cols ? Cp[row + (int64_t)col * ldc] : 0.f;
+                    c[j] = q == 0 ? cpre[j] : (col < n_cols ? Cp[erow + (int64_t)col * ldc] : 0.f);
                 }
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const int col = cb + j;
-                    if (col < n_cols) Cp[row + (int64_t)col * ldc] = c[j] - v[j];
+                    if (col < n_cols) Cp[erow + (int64_t)col * ldc] = c[j] - v[j];
                 }
             }
         }
