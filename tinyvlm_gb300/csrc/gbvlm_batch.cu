@@ -379,7 +379,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 // ---------------------------------------------------------------------------
 // loads: one block per solve.  Forces F = rho dgamma (V x dl) on the bound
 // segment (vlm_backend_cpu.cpp:276-297), CL/CM (:323-362), Trefftz CDi
-// (ispc:273-323), sums compensated in double.
+// (ispc:273-323).  The geometry differences are formed in double, the force
+// and moment terms in float (this part's fp64 rate is a small fraction of its
+// fp32 rate) and summed in double.
 // ---------------------------------------------------------------------------
 constexpr int LD_THREADS = 256;
 
@@ -442,24 +444,34 @@ __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const i
     L = (1.0 / ll) * L;
     const double* x = S.Xd + q * n;
     const double* v = S.vd;
-    CSum cl, cmx, cmy, cmz, ar, mac;
+    // per panel: the bound-vortex vector and lever arm formed in double and
+    // rounded to float, the Joukowski force and its moment in float, sums in
+    // double (float terms: ~1e-7 relative each; plain double sums of at most
+    // a few thousand terms per thread keep ~1e-13 relative)
+    const float Vx = (float)V.x, Vy = (float)V.y, Vz = (float)V.z;
+    const float Lx = (float)L.x, Lz = (float)L.z;
+    double cl = 0, cmx = 0, cmy = 0, cmz = 0, ar = 0;
     for (int64_t p = threadIdx.x; p < n; p += LD_THREADS) {
         const int64_t i = p % ns, j = p / ns;
         const double g = x[p], gd = (j > 0) ? g - x[p - ns] : g;
         const int64_t ia = i + j * (ns + 1), ib = ia + 1;
-        const V3<double> v0{v[ia], v[nv + ia], v[2 * nv + ia]}, v1{v[ib], v[nv + ib], v[2 * nv + ib]};
-        const V3<double> F = (a.rho * gd) * cross(V, v1 - v0);
-        cl.add(dot(F, L));
-        const V3<double> lev = 0.5 * (v0 + v1) - V3<double>{a.ref[0], a.ref[1], a.ref[2]};
-        const V3<double> m = cross(lev, F);
-        cmx.add(m.x);
-        cmy.add(m.y);
-        cmz.add(m.z);
-        ar.add(S.area[p]);
+        const double ax = v[ia], ay = v[nv + ia], az = v[2 * nv + ia];
+        const double bx = v[ib], by = v[nv + ib], bz = v[2 * nv + ib];
+        const float dx = (float)(bx - ax), dy = (float)(by - ay), dz = (float)(bz - az);
+        const float mx = (float)(0.5 * (ax + bx) - a.ref[0]), my = (float)(0.5 * (ay + by) - a.ref[1]),
+                    mz = (float)(0.5 * (az + bz) - a.ref[2]);
+        const float rg = (float)(a.rho * gd);
+        const float Fx = rg * (Vy * dz - Vz * dy), Fy = rg * (Vz * dx - Vx * dz), Fz = rg * (Vx * dy - Vy * dx);
+        cl += (double)(Fx * Lx + Fz * Lz);  // L has no y component
+        cmx += (double)(my * Fz - mz * Fy);
+        cmy += (double)(mz * Fx - mx * Fz);
+        cmz += (double)(mx * Fy - my * Fx);
+        ar += S.area[p];
         if (want_gamma && a.gamma_out) a.gamma_out[a.goff[sol] + p] = (float)g;
     }
     // MAC numerator over spanwise stations (vlm_backend_cpu.cpp:443-468)
     const int64_t last = nc * (ns + 1);
+    double mac = 0;
     for (int64_t i = threadIdx.x; i < ns; i += LD_THREADS) {
         double c0 = sqrt((v[i] - v[last + i]) * (v[i] - v[last + i]) + (v[nv + i] - v[nv + last + i]) * (v[nv + i] - v[nv + last + i]) +
                          (v[2 * nv + i] - v[2 * nv + last + i]) * (v[2 * nv + i] - v[2 * nv + last + i]));
@@ -468,19 +480,19 @@ __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const i
                          (v[2 * nv + i + 1] - v[2 * nv + last + i + 1]) * (v[2 * nv + i + 1] - v[2 * nv + last + i + 1]));
         double w = sqrt((v[i + 1] - v[i]) * (v[i + 1] - v[i]) + (v[nv + i + 1] - v[nv + i]) * (v[nv + i + 1] - v[nv + i]) +
                         (v[2 * nv + i + 1] - v[2 * nv + i]) * (v[2 * nv + i + 1] - v[2 * nv + i]));
-        mac.add(0.5 * (c0 * c0 + c1 * c1) * w);
+        mac += 0.5 * (c0 * c0 + c1 * c1) * w;
     }
     // Trefftz drag: gamma_TE^T K gamma_TE (the wake carries the TE gamma)
-    CSum cd;
+    double cd = 0;
     const double* gte = x + (nc - 1) * ns;
     for (int64_t e = threadIdx.x; e < ns * ns; e += LD_THREADS) {
         const int64_t j = e % ns, jj = e / ns;
-        cd.add(gte[j] * S.K[e] * gte[jj]);
+        cd += gte[j] * S.K[e] * gte[jj];
     }
-    const double s_cl = block_sum_d(cl.value(), sh), s_x = block_sum_d(cmx.value(), sh);
-    const double s_y = block_sum_d(cmy.value(), sh), s_z = block_sum_d(cmz.value(), sh);
-    const double s_ar = block_sum_d(ar.value(), sh), s_mac = block_sum_d(mac.value(), sh);
-    const double s_cd = block_sum_d(cd.value(), sh);
+    const double s_cl = block_sum_d(cl, sh), s_x = block_sum_d(cmx, sh);
+    const double s_y = block_sum_d(cmy, sh), s_z = block_sum_d(cmz, sh);
+    const double s_ar = block_sum_d(ar, sh), s_mac = block_sum_d(mac, sh);
+    const double s_cd = block_sum_d(cd, sh);
     if (threadIdx.x == 0) {
         const double v2 = len2(V);
         const double macv = s_mac / s_ar;
