@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
-    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof"],
+    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof", "nlvlm"],
                    help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
                         "uvlm: 20x80 rectangular wing, 500 pitch-plunge steps")
     p.add_argument("--uvlm-steps", type=int, default=500)
@@ -460,6 +460,49 @@ def run_aero2dof(args):
     print(json.dumps(out))
 
 
+def run_nlvlm(args):
+    """Nonlinear VLM (the reference's tests/nlvlm_curves.cpp case): the 5 x 200 "infinite" rectangle at
+    alpha = 19 deg, strip angles corrected toward three tabulated lift curves (100 points, 0-20 deg); float,
+    the iteration loop on the device with one error read per iteration.  The CPU leg runs the oracle's
+    restatement of the same loop."""
+    import math
+    import torch
+    from tinyvlm_gb300 import mesh as M
+    from tinyvlm_gb300.vlm import NLVLM, Database, FlowData, WingProfile
+
+    def spallart(cl0, a0, a1, cla0, cla1):
+        return lambda a: cla0 * a + 0.5 * (cl0 - cla1 * a) * (1.0 + math.erf((a - a0) / a1))
+    curves = {"spallart1": spallart(1.2, 0.28, 0.02, 2 * math.pi, 2 * math.pi),
+              "spallart2": spallart(0.72, 0.28, 0.04, 2 * math.pi, 1.5 * math.pi),
+              "polar": lambda a: 2 * math.pi * a}
+    v = M.rectangular(5, 200, 1.0, 40000.0).astype(np.float32)
+    M.quarter_chord(v)
+    alpha = math.radians(19.0)
+    db_a = np.linspace(0.0, math.radians(20.0), 100).astype(np.float32)
+    sim = NLVLM("gb300", [v])
+    out = {"workload": "NLVLM, 5x200 rectangle (1000 panels), alpha 19 deg, three lift curves", "runs": {}}
+    for name, f in curves.items():
+        db = Database()
+        db.profiles.append(WingProfile(db_a, np.array([f(float(a)) for a in db_a], np.float32)))
+        sim.run(FlowData(alpha), db)  # warm-up
+        torch.cuda.synchronize()
+        reps = 20
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            res = sim.run(FlowData(alpha), db)
+        torch.cuda.synchronize()
+        ms = 1000.0 * (time.perf_counter() - t0) / reps
+        row = {"gpu_ms_per_run": ms, "iters": sim.iters, "cl": res.cl, "cl_rel_err_vs_curve": abs(res.cl - f(alpha)) / f(alpha)}
+        if not args.no_cpu_baseline:
+            from oracle import oracle as O
+            t0 = time.perf_counter()
+            O.nlvlm_run([v], alpha, db_a, db.profiles[0].CL)
+            row["cpu_ms_per_run"] = 1000.0 * (time.perf_counter() - t0)
+        out["runs"][name] = row
+    out["note"] = "per run: AIC assembly and factorisation, then the iterations; the CPU leg is the oracle (numpy driver over the C operators)"
+    print(json.dumps(out))
+
+
 def run_served(args):
     """Poisson mixed stream in equal thirds: steady VLM on trapezoids of 256-16,384 panels (log-uniform),
     single UVLM steps on a resident 20x80 wing with a 500-row (40,000-ring) wake, 2-DOF HBVLM residuals
@@ -517,6 +560,8 @@ def main():
         run_uvlm(args)
     elif args.workload == "aero2dof":
         run_aero2dof(args)
+    elif args.workload == "nlvlm":
+        run_nlvlm(args)
     elif args.workload == "served":
         run_served(args)
     else:

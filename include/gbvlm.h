@@ -450,6 +450,26 @@ int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, co
  * then the vertices into a HOST float (ns+1, nc+1, 4) array. */
 int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts);
 
+/* ---------------------------------------------------------------------------
+ * Nonlinear VLM: NLVLM::run (vlm/include/vlm.hpp:87-115, vlm/src/vlm.cpp:
+ * 153-295), the strip-wise correction of the angle of attack toward a 2D
+ * lift polar.  The polar is (db_alpha[i], db_cl[i]), n_db >= 4 points with
+ * increasing angles, interpolated as tiny::AkimaInterpolator does
+ * (Database2D::interpolate_CL, vlm_data.hpp:85-90: one profile).  The
+ * reference's defaults are tol = 1e-5 and max_iter = 100 (vlm.hpp:90-91).
+ * Returns the final CL (strips reset to alpha, as the reference does), the
+ * iterations run, the last L1 correction per panel, and optionally the strip
+ * angles before the reset (sum of ns floats over the surfaces, host memory).
+ * Synchronous.
+ * ------------------------------------------------------------------------- */
+typedef struct gbvlm_nlvlm_s* gbvlm_nlvlm;
+int gbvlm_nlvlm_create(gbvlm_nlvlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                       int32_t precision);
+int gbvlm_nlvlm_destroy(gbvlm_nlvlm h);
+int gbvlm_nlvlm_run(gbvlm_nlvlm h, double alpha, double beta, double u_inf, double rho, const float* db_alpha,
+                    const float* db_cl, int32_t n_db, double tol, int32_t max_iter, double* cl, int32_t* iters,
+                    double* err, float* strip_alpha, gbvlm_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

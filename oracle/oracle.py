@@ -865,3 +865,138 @@ def aero2dof_run(verts_init, lifting, vars, t_final, dtype=np.float64, max_iter=
     t = np.arange(nsteps + 1) * dt_nd
     return dict(t=t, u=u[:nsteps + 1], v=v[:nsteps + 1], a=a[:nsteps + 1], F=F[:nsteps + 1], iters=iters, dt=dt_nd,
                 t_steps=t_steps)
+
+
+# ---------------------------------------------------------------------------
+# Nonlinear VLM (strip-wise viscous correction, van Dam's method)
+# ---------------------------------------------------------------------------
+def akima_table(x, y, dtype=np.float32):
+    """Slopes m (per segment) and spline coefficients s (per point) of
+    tiny::AkimaInterpolator (headeronly/tinyinterpolate.hpp:29-54)."""
+    T = np.dtype(dtype).type
+    x = np.asarray(x, dtype)
+    y = np.asarray(y, dtype)
+    n = len(x)
+    m = np.array([(y[i + 1] - y[i]) / (x[i + 1] - x[i]) for i in range(n - 1)], dtype)
+    s = np.zeros(n, dtype)
+    s[0] = m[0]
+    s[1] = T(0.5) * (m[0] + m[1])
+    for i in range(2, n - 2):
+        d1 = abs(m[i + 1] - m[i])
+        d2 = abs(m[i - 1] - m[i - 2])
+        s[i] = (d1 * m[i - 1] + d2 * m[i]) / (d1 + d2) if d1 + d2 > T(0) else T(0.5) * (m[i] + m[i - 1])
+    s[n - 2] = T(0.5) * (m[n - 3] + m[n - 2])
+    s[n - 1] = m[n - 2]
+    return x, y, m, s
+
+
+def akima_eval(tab, xq):
+    """tiny::AkimaInterpolator::operator() (tinyinterpolate.hpp:56-73):
+    cubic on the interval holding xq (std::lower_bound), linear with the end
+    segment's slope outside the table."""
+    x, y, m, s = tab
+    T = x.dtype.type
+    xq = T(xq)
+    idx = int(np.searchsorted(x, xq, side="left"))
+    if idx == 0:
+        return T(y[0] - m[0] * (x[0] - xq))
+    if idx == len(x):
+        return T(y[-1] + m[-1] * (xq - x[-1]))
+    i = idx - 1
+    dx = x[i + 1] - x[i]
+    dxx = xq - x[i]
+    a, b = y[i], s[i]
+    c = (T(3) * m[i] - T(2) * s[i] - s[i + 1]) / dx
+    d = (s[i] + s[i + 1] - T(2) * m[i]) / (dx * dx)
+    return T(a + b * dxx + c * dxx * dxx + d * dxx * dxx * dxx)
+
+
+def nlvlm_run(verts_init, alpha, db_alpha, db_cl, beta=0.0, u_inf=1.0, rho=1.0, dtype=np.float32, tol=1e-5,
+              max_iter=100):
+    """NLVLM::run (vlm/src/vlm.cpp:198-295, defaults vlm.hpp:90-91).
+
+    The wing and its single 100-chord wake row as in VLM::run, one AIC
+    factored once.  Each iteration: panel velocities from the strip angles
+    (vlm.cpp:186-196: beta = 0 there), RHS, solve, gamma deltas, steady
+    forces; per spanwise strip its CL about the strip's own lift axis, the
+    effective angle CL/(2 pi) - alpha_strip + alpha, and the correction
+    (CL_polar(effective) - CL)/(2 pi) added to the strip angle; the L1 sum of
+    the corrections divided by the panel count ends the loop below `tol`.
+    The final CL resets the strip angles to alpha (:281-285) and is
+    coeff_cl_multibody of the last circulation.  The polar is the Akima
+    interpolant of (db_alpha, db_cl) (Database2D::interpolate_CL,
+    vlm_data.hpp:85-90: the first profile, no blending in y).
+
+    Returns dict(cl, iters, err, strip_alpha (list per surface, before the
+    reset), gamma)."""
+    T = np.dtype(dtype).type
+    tab = akima_table(db_alpha, db_cl, dtype)
+    verts_init = [np.ascontiguousarray(v, dtype) for v in verts_init]
+    verts = [v.copy() for v in verts_init]
+    ns, nc = dims(verts)
+    n = sum(a * b for a, b in zip(ns, nc))
+    wake = []
+    for s in ns:
+        w = np.zeros((4, 2, s + 1), dtype)
+        w[3] = 1
+        wake.append(w)
+    a32 = T(alpha)
+    tr = translation(np.array([T(-100.0) * T(u_inf) * np.cos(a32), T(0), T(-100.0) * T(u_inf) * np.sin(a32)], dtype),
+                     dtype)
+    wake_shed(verts, wake, 0)
+    for v, vi in zip(verts, verts_init):
+        displace_wing(tr, v, vi)
+    wake_shed(verts, wake, 1)
+    colloc, normals, areas = mesh_metrics(alpha, verts, dtype)
+    lhs = np.zeros((n, n), dtype, order="F")
+    lhs_assemble(lhs, colloc, normals, verts, wake, 1, 0.0)
+    lu, piv = lu_factor(lhs)
+    strips = [np.full(s, a32, dtype) for s in ns]
+    two_pi = T(np.float32(2.0) * np.float32(3.141593))  # 2 PI_f, the reference's float pi (vlm_types.hpp:22)
+
+    def velocities():
+        out = []
+        for st, s, c in zip(strips, ns, nc):
+            v = np.empty((3, c, s), dtype)
+            for i in range(s):
+                f = freestream(u_inf, st[i], 0.0, dtype)
+                v[:, :, i] = f[:, None]
+            out.append(v)
+        return out
+
+    err, it = 1.0, 0
+    deltas, gam = None, None
+    while it < max_iter and err > tol:
+        err = 0.0
+        vel = velocities()
+        rhs = np.zeros(n, dtype)
+        rhs_assemble_velocities(rhs, normals, vel)
+        x = lu_solve(lu, piv, rhs)
+        gam, deltas = [], []
+        off = 0
+        for s, c in zip(ns, nc):
+            g = x[off:off + s * c].reshape(c, s).copy()
+            off += s * c
+            gam.append(g)
+            deltas.append(gamma_delta(g))
+        forces = [forces_steady(v, d, u) for v, d, u in zip(verts, deltas, vel)]
+        for st, f, a in zip(strips, forces, areas):
+            for i in range(len(st)):
+                fi = np.ascontiguousarray(f[:, :, i:i + 1])
+                area = asum(np.ascontiguousarray(a[:, i:i + 1]))
+                fs_i = freestream(u_inf, st[i], beta, dtype)
+                cl_i = coeff_cl(fi, lift_axis(fs_i), fs_i, T(rho), area)
+                eff = T(cl_i / two_pi - st[i] + a32)
+                corr = T((akima_eval(tab, eff) - cl_i) / two_pi)
+                st[i] = T(st[i] + corr)
+                err += abs(float(corr))
+        err /= float(n)
+        it += 1
+    strip_out = [st.copy() for st in strips]
+    for st in strips:
+        st[:] = a32
+    vel = velocities()
+    forces = [forces_steady(v, d, u) for v, d, u in zip(verts, deltas, vel)]
+    fs = freestream(u_inf, alpha, beta, dtype)
+    cl = coeff_cl_multibody(forces, areas, fs, T(rho))
+    return dict(cl=cl, iters=it, err=err, strip_alpha=strip_out, gamma=gam)

@@ -1,5 +1,6 @@
 // Host drivers above the operator C ABI: the steady VLM simulation
-// (vlm/src/vlm.cpp:17-151) and the plot3d reader (vlm/src/vlm_mesh.cpp).
+// (vlm/src/vlm.cpp:17-151), the nonlinear VLM (vlm.cpp:153-295) and the
+// plot3d reader (vlm/src/vlm_mesh.cpp).
 // These are the "plain per-solve" paths: one operator call per reference
 // backend call, scalars read back synchronously, in float (the reference's
 // semantics) or double.
@@ -241,12 +242,268 @@ struct VlmState : VlmBase {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Nonlinear VLM (vlm/src/vlm.cpp:153-295): strip-wise correction of the
+// angle of attack toward a 2D lift polar (van Dam's method).  The AIC of the
+// wing with its 100-chord wake row is factored once; each iteration runs on
+// the device (panel velocities from the strip angles, RHS, solve, gamma
+// deltas, forces, strip correction) and the host reads one error per
+// surface to decide whether to continue, as the reference's loop does.
+// ---------------------------------------------------------------------------
+
+// Akima interpolant (headeronly/tinyinterpolate.hpp:26-73): lower_bound on
+// x, the cubic of that interval, the end segment's line outside the table
+template <class T>
+__device__ T akima_at(const T* x, const T* y, const T* m, const T* s, int n, T xq) {
+    int lo = 0, hi = n;  // first index with x[i] >= xq
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (x[mid] < xq) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo == 0) return y[0] - m[0] * (x[0] - xq);
+    if (lo == n) return y[n - 1] + m[n - 2] * (xq - x[n - 1]);
+    const int i = lo - 1;
+    const T dx = x[i + 1] - x[i], dxx = xq - x[i];
+    const T c = ((T)3 * m[i] - (T)2 * s[i] - s[i + 1]) / dx;
+    const T d = (s[i] + s[i + 1] - (T)2 * m[i]) / (dx * dx);
+    return y[i] + s[i] * dxx + c * dxx * dxx + d * dxx * dxx * dxx;
+}
+
+// panel velocities of a surface from its strip angles (vlm.cpp:186-196:
+// freestream(u_inf, alpha_strip, 0), one value per spanwise strip)
+template <class T>
+__global__ void k_strip_vel(T* vel, const T* strip, int64_t ns, int64_t nc, T u) {
+    const int64_t np = ns * nc, p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const T a = strip[p % ns];
+    vel[p] = u * cos(a);
+    vel[np + p] = (T)0;
+    vel[2 * np + p] = u * sin(a);
+}
+
+// one CTA per surface: for every spanwise strip its CL about the strip's own
+// lift axis, the effective angle and the correction toward the polar
+// (vlm.cpp:257-276); err_out = the surface's sum of |correction|
+template <class T>
+__global__ void __launch_bounds__(256) k_strip_correct(T* strip, const T* forces, const T* areas, int64_t ns, int64_t nc,
+                                                       T alpha, T beta, T u, T rho, const T* tx, const T* ty,
+                                                       const T* tm, const T* ts, int ntab, double* err_out) {
+    __shared__ double red[256];
+    const int64_t np = ns * nc;
+    const T two_pi = (T)(2.0f * 3.141593f);  // 2 PI_f with the reference's float pi (vlm_types.hpp:22)
+    double e = 0;
+    for (int64_t i = threadIdx.x; i < ns; i += blockDim.x) {
+        const T a = strip[i];
+        // FlowData of the strip (vlm_utils.cpp:5-19): freestream and lift axis
+        const T fx = u * cos(a) * cos(beta), fy = -(u * cos(a) * sin(beta)), fz = u * sin(a);
+        T lx = -fz, lz = fx;
+        const T ll = sqrt(lx * lx + lz * lz);
+        lx /= ll;
+        lz /= ll;
+        T fl = 0, area = 0;
+        for (int64_t j = 0; j < nc; j++) {
+            const int64_t p = i + j * ns;
+            fl += forces[p] * lx + forces[2 * np + p] * lz;  // the lift axis has no y component
+            area += areas[p];
+        }
+        const T cl = fl / ((T)0.5 * rho * (fx * fx + fy * fy + fz * fz) * area);
+        const T eff = cl / two_pi - a + alpha;
+        const T corr = (akima_at<T>(tx, ty, tm, ts, ntab, eff) - cl) / two_pi;
+        strip[i] = a + corr;
+        e += fabs((double)corr);
+    }
+    red[threadIdx.x] = e;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *err_out = red[0];
+}
+
+struct NlvlmBase {
+    virtual ~NlvlmBase() = default;
+    virtual int run(double alpha, double beta, double u_inf, double rho, const float* db_alpha, const float* db_cl,
+                    int32_t ndb, double tol, int32_t max_iter, double* cl, int32_t* iters, double* err,
+                    float* strip_out, cudaStream_t st) = 0;
+};
+
+template <class T>
+struct NlvlmState : NlvlmBase {
+    VlmState<T> w;  // wing, wake, AIC and per-panel buffers of the steady simulation
+    void* mem = nullptr;
+    std::vector<T*> strip;
+    double* d_err = nullptr;
+    T* tab = nullptr;  // x, y, m, s of the polar
+    int32_t tab_cap = 0;
+
+    ~NlvlmState() override {
+        if (mem) cudaFree(mem);
+        if (tab) cudaFree(tab);
+    }
+
+    int init(int32_t ns_, const gbvlm_dims* d, const float* const* vinit) {
+        int rc = w.init(ns_, d, vinit);
+        if (rc) return rc;
+        int64_t strips = 0;
+        for (auto& x : w.dims) strips += x.ns;
+        GB_CUDA(cudaMalloc(&mem, sizeof(T) * strips + sizeof(double) * w.nsurf + 256));
+        d_err = (double*)mem;
+        T* p = (T*)((char*)mem + ((sizeof(double) * w.nsurf + 255) / 256) * 256);
+        for (auto& x : w.dims) {
+            strip.push_back(p);
+            p += x.ns;
+        }
+        return GBVLM_OK;
+    }
+
+    int run(double alpha_d, double beta_d, double u_inf_d, double rho_d, const float* db_alpha, const float* db_cl,
+            int32_t ndb, double tol, int32_t max_iter, double* cl_out, int32_t* iters_out, double* err_out,
+            float* strip_out, cudaStream_t st) override {
+        gbvlm_stream s = (gbvlm_stream)st;
+        const int32_t nsurf = w.nsurf;
+        const T alpha = (T)alpha_d, beta = (T)beta_d, u = (T)u_inf_d, rho = (T)rho_d;
+        // the polar's Akima coefficients (tinyinterpolate.hpp:29-54), as the reference builds them on the host
+        std::vector<T> tx(ndb), ty(ndb), tm(ndb - 1), ts(ndb);
+        for (int i = 0; i < ndb; i++) {
+            tx[i] = (T)db_alpha[i];
+            ty[i] = (T)db_cl[i];
+            GB_REQUIRE(i == 0 || tx[i] > tx[i - 1], "NLVLM: polar angles must increase");
+        }
+        for (int i = 0; i + 1 < ndb; i++) tm[i] = (ty[i + 1] - ty[i]) / (tx[i + 1] - tx[i]);
+        ts[0] = tm[0];
+        ts[1] = (T)0.5 * (tm[0] + tm[1]);
+        for (int i = 2; i < ndb - 2; i++) {
+            const T d1 = std::abs(tm[i + 1] - tm[i]), d2 = std::abs(tm[i - 1] - tm[i - 2]);
+            ts[i] = d1 + d2 > (T)0 ? (d1 * tm[i - 1] + d2 * tm[i]) / (d1 + d2) : (T)0.5 * (tm[i] + tm[i - 1]);
+        }
+        ts[ndb - 2] = (T)0.5 * (tm[ndb - 3] + tm[ndb - 2]);
+        ts[ndb - 1] = tm[ndb - 2];
+        if (tab_cap < ndb) {
+            if (tab) cudaFree(tab);
+            tab = nullptr;
+            GB_CUDA(cudaMalloc(&tab, sizeof(T) * 4 * ndb));
+            tab_cap = ndb;
+        }
+        T* dx = tab;
+        T* dy = tab + ndb;
+        T* dm = tab + 2 * ndb;
+        T* dsp = tab + 3 * ndb;
+        GB_CUDA(cudaMemcpyAsync(dx, tx.data(), sizeof(T) * ndb, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(dy, ty.data(), sizeof(T) * ndb, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(dm, tm.data(), sizeof(T) * (ndb - 1), cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(dsp, ts.data(), sizeof(T) * ndb, cudaMemcpyHostToDevice, st));
+        // the wing with its 100-chord wake row and the factored AIC (vlm.cpp:201-217)
+        GB_CUDA(cudaMemsetAsync(w.lhs, 0, sizeof(T) * w.n * w.n, st));
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t nv = (w.dims[m].ns + 1) * (w.dims[m].nc + 1);
+            GB_CUDA(cudaMemcpyAsync(w.verts[m], w.verts_init[m], sizeof(T) * 4 * nv, cudaMemcpyDeviceToDevice, st));
+        }
+        T tr[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, (T)-100 * u * (T)cos(alpha), 0, (T)-100 * u * (T)sin(alpha), 1};
+        for (int m = 0; m < nsurf; m++)
+            GB_CUDA(cudaMemcpyAsync(w.transform[m], tr, sizeof(tr), cudaMemcpyHostToDevice, st));
+        std::vector<const T*> cverts(w.verts.begin(), w.verts.end()), cinit(w.verts_init.begin(), w.verts_init.end()),
+            ctr(w.transform.begin(), w.transform.end()), ccol(w.colloc.begin(), w.colloc.end()),
+            cnor(w.normals.begin(), w.normals.end()), cwake(w.wake.begin(), w.wake.end()),
+            cvel(w.vel.begin(), w.vel.end());
+        int rc;
+        if ((rc = Ops<T>::shed(nsurf, w.dims.data(), cverts.data(), w.wake.data(), 0, s))) return rc;
+        if ((rc = Ops<T>::displace(nsurf, w.dims.data(), ctr.data(), w.verts.data(), cinit.data(), s))) return rc;
+        if ((rc = Ops<T>::shed(nsurf, w.dims.data(), cverts.data(), w.wake.data(), 1, s))) return rc;
+        if ((rc = Ops<T>::metrics(alpha, nsurf, w.dims.data(), cverts.data(), w.colloc.data(), w.normals.data(),
+                                  w.areas.data(), s)))
+            return rc;
+        if ((rc = Ops<T>::lhs(w.lhs, w.n, nsurf, w.dims.data(), ccol.data(), cnor.data(), cverts.data(),
+                              cwake.data(), 1, (T)0, s)))
+            return rc;
+        if ((rc = Ops<T>::factor(w.lu, w.lhs, w.n, s))) return rc;
+        for (int m = 0; m < nsurf; m++) {
+            std::vector<T> a0(w.dims[m].ns, alpha);
+            GB_CUDA(cudaMemcpyAsync(strip[m], a0.data(), sizeof(T) * a0.size(), cudaMemcpyHostToDevice, st));
+            GB_CUDA(cudaStreamSynchronize(st));  // a0 goes out of scope
+        }
+        auto velocities = [&]() -> int {
+            for (int m = 0; m < nsurf; m++) {
+                const int64_t np = w.dims[m].ns * w.dims[m].nc;
+                k_strip_vel<T><<<(unsigned)cdiv(np, 256), 256, 0, st>>>(w.vel[m], strip[m], w.dims[m].ns,
+                                                                        w.dims[m].nc, u);
+                GB_LAUNCH_CHECK();
+            }
+            return GBVLM_OK;
+        };
+        std::vector<double> herr(nsurf);
+        double err = 1.0;
+        int32_t it = 0;
+        for (; it < max_iter && err > tol; it++) {
+            if ((rc = velocities())) return rc;
+            GB_CUDA(cudaMemsetAsync(w.rhs, 0, sizeof(T) * w.n, st));
+            if ((rc = Ops<T>::rhsv(w.rhs, nsurf, w.dims.data(), cnor.data(), cvel.data(), s))) return rc;
+            if ((rc = Ops<T>::solve(w.lu, w.lhs, w.n, w.rhs, s))) return rc;
+            int64_t off = 0;
+            for (int m = 0; m < nsurf; m++) {
+                const int64_t ns = w.dims[m].ns, nc = w.dims[m].nc;
+                if ((rc = Ops<T>::gupd(ns, nc, w.rhs + off, w.gamma[m], w.gdelta[m], w.gwake[m], s))) return rc;
+                if ((rc = Ops<T>::forces(ns, nc, w.verts[m], w.gdelta[m], w.vel[m], w.forces[m], s))) return rc;
+                k_strip_correct<T><<<1, 256, 0, st>>>(strip[m], w.forces[m], w.areas[m], ns, nc, alpha, beta, u, rho,
+                                                      dx, dy, dm, dsp, ndb, d_err + m);
+                GB_LAUNCH_CHECK();
+                off += ns * nc;
+            }
+            GB_CUDA(cudaMemcpyAsync(herr.data(), d_err, sizeof(double) * nsurf, cudaMemcpyDeviceToHost, st));
+            GB_CUDA(cudaStreamSynchronize(st));
+            err = 0;
+            for (int m = 0; m < nsurf; m++) err += herr[m];
+            err /= (double)w.n;  // per panel, as the reference normalises
+        }
+        if (strip_out) {
+            int64_t o = 0;
+            for (int m = 0; m < nsurf; m++) {
+                std::vector<T> h(w.dims[m].ns);
+                GB_CUDA(cudaMemcpyAsync(h.data(), strip[m], sizeof(T) * h.size(), cudaMemcpyDeviceToHost, st));
+                GB_CUDA(cudaStreamSynchronize(st));
+                for (auto v : h) strip_out[o++] = (float)v;
+            }
+        }
+        // final loads with the strips back at alpha (vlm.cpp:281-291)
+        for (int m = 0; m < nsurf; m++) {
+            std::vector<T> a0(w.dims[m].ns, alpha);
+            GB_CUDA(cudaMemcpyAsync(strip[m], a0.data(), sizeof(T) * a0.size(), cudaMemcpyHostToDevice, st));
+            GB_CUDA(cudaStreamSynchronize(st));
+        }
+        if ((rc = velocities())) return rc;
+        T fs[3] = {u * (T)cos(alpha) * (T)cos(beta), -(u * (T)cos(alpha) * (T)sin(beta)), u * (T)sin(alpha)};
+        T la[3] = {-fs[2], (T)0, fs[0]};
+        const T ll = (T)sqrt(la[0] * la[0] + la[2] * la[2]);
+        la[0] /= ll;
+        la[2] /= ll;
+        T cl = 0, ta = 0;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t ns = w.dims[m].ns, nc = w.dims[m].nc;
+            if ((rc = Ops<T>::forces(ns, nc, w.verts[m], w.gdelta[m], w.vel[m], w.forces[m], s))) return rc;
+            T area, clm;
+            if ((rc = Ops<T>::sum(w.areas[m], ns * nc, &area, s))) return rc;
+            if ((rc = Ops<T>::cl(ns, nc, w.forces[m], la, fs, rho, area, &clm, s))) return rc;
+            cl += clm * area;
+            ta += area;
+        }
+        *cl_out = (double)(cl / ta);
+        if (iters_out) *iters_out = it;
+        if (err_out) *err_out = err;
+        return GBVLM_OK;
+    }
+};
+
 }  // namespace gbvlm
 
 using namespace gbvlm;
 
 struct gbvlm_vlm_s {
     VlmBase* impl = nullptr;
+};
+
+struct gbvlm_nlvlm_s {
+    NlvlmBase* impl = nullptr;
 };
 
 extern "C" {
@@ -291,6 +548,52 @@ int gbvlm_vlm_run(gbvlm_vlm h, double alpha, double beta, double u_inf, double r
                   gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream) {
     GB_REQUIRE(h && h->impl && out, "null argument");
     return h->impl->run(alpha, beta, u_inf, rho, ref_pt, out, gamma_out, to_cuda(stream));
+}
+
+int gbvlm_nlvlm_create(gbvlm_nlvlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
+                       int32_t precision) {
+    GB_REQUIRE(out && dims && verts_init, "null argument");
+    GB_REQUIRE(nsurf >= 1 && nsurf <= GBVLM_MAX_SURFACES, "nsurf=%d outside [1, %d]", nsurf, GBVLM_MAX_SURFACES);
+    GB_REQUIRE(precision == 32 || precision == 64, "precision must be 32 or 64");
+    for (int m = 0; m < nsurf; m++) {
+        GB_REQUIRE(verts_init[m], "verts_init[%d] is null", m);
+        GB_REQUIRE(dims[m].ns >= 1 && dims[m].nc >= 1, "surface %d has bad sizes", m);
+    }
+    auto* h = new gbvlm_nlvlm_s();
+    int rc;
+    if (precision == 32) {
+        auto* st = new NlvlmState<float>();
+        h->impl = st;
+        rc = st->init(nsurf, dims, verts_init);
+    } else {
+        auto* st = new NlvlmState<double>();
+        h->impl = st;
+        rc = st->init(nsurf, dims, verts_init);
+    }
+    if (rc) {
+        delete h->impl;
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBVLM_OK;
+}
+
+int gbvlm_nlvlm_destroy(gbvlm_nlvlm h) {
+    if (!h) return GBVLM_OK;
+    delete h->impl;
+    delete h;
+    return GBVLM_OK;
+}
+
+int gbvlm_nlvlm_run(gbvlm_nlvlm h, double alpha, double beta, double u_inf, double rho, const float* db_alpha,
+                    const float* db_cl, int32_t n_db, double tol, int32_t max_iter, double* cl, int32_t* iters,
+                    double* err, float* strip_alpha, gbvlm_stream stream) {
+    GB_REQUIRE(h && h->impl && db_alpha && db_cl && cl, "null argument");
+    GB_REQUIRE(n_db >= 4, "NLVLM: the polar needs at least 4 points (Akima), got %d", n_db);
+    GB_REQUIRE(max_iter >= 0, "NLVLM: max_iter must be non-negative");
+    return h->impl->run(alpha, beta, u_inf, rho, db_alpha, db_cl, n_db, tol, max_iter, cl, iters, err, strip_alpha,
+                        to_cuda(stream));
 }
 
 int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts) {
