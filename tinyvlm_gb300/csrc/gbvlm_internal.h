@@ -36,4 +36,34 @@ void* host_scratch(size_t bytes);
 // Per-device small device buffer for reductions (grown on demand).
 int device_scratch(size_t bytes, void** out, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Launch-only forms of a few operators for code captured into a CUDA graph
+// and replayed at every time step: the step-dependent argument (wake rows,
+// wake column, state index) is read from device memory, and nothing is
+// allocated or copied from the host.
+// ---------------------------------------------------------------------------
+// float single-system LU solve of one right-hand side: the device tables are
+// staged once by lu_solve_prepare_f32 (after the factorisation of A)
+int lu_solve_prepare_f32(gbvlm_lu h, const float* A, int64_t n, float* X, void** tables, cudaStream_t st);
+int lu_solve_prepared_f32(gbvlm_lu h, void* tables, int64_t n, cudaStream_t st);
+void lu_solve_tables_free(void* tables);
+// rhs -= wake influence with *it_dev active ring rows per lifting wake
+// (it_dev <= it_max); scratch of WAKE_DEV_MAX_SLICES x (total panels) floats
+constexpr int64_t WAKE_DEV_MAX_SLICES = 608;
+int wake_influence_dev_f32(float* rhs, int32_t nsurf, const gbvlm_dims* dims, const float* const* gamma_wake,
+                           const float* const* colloc, const float* const* normals, const float* const* verts_wake,
+                           const int32_t* lifting, const int64_t* it_dev, int32_t it_max, float* scratch,
+                           cudaStream_t st);
+// wake row nwv - 1 - *it_dev <- the wing's trailing-edge row
+int wake_shed_dev_f32(int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_wing, float* const* verts_wake,
+                      const int64_t* it_dev, cudaStream_t st);
+// gbvlm_gamma_update_f32 with the wake column col_base - *it_dev
+int gamma_update_dev_f32(int64_t ns, int64_t nc, const float* x, float* gamma, float* gamma_delta, float* gamma_wake,
+                         int64_t col_base, const int64_t* it_dev, const float* gamma_prev, float* dgamma_dt, float dt,
+                         cudaStream_t st);
+// gbvlm_newmark_step with v_i = v + ndof * (*i_dev), a_i = a + ndof * (*i_dev)
+int newmark_step_dev(gbvlm_newmark h, const double* M, const double* C, const double* v, const double* a,
+                     const int64_t* i_dev, double* du, double* dv, double* da, const double* delta_F, double dt,
+                     cudaStream_t st);
+
 }  // namespace gbvlm

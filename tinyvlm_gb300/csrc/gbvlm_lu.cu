@@ -2382,6 +2382,43 @@ static int lu_solve_one(gbvlm_lu h, const T* A, int64_t n, int64_t ld, T* X, int
     return lu_batch_solve<T>(B, 1, (int32_t)nrhs, n, st, h->plan.tc_passes ? h->plan.d_err : nullptr);
 }
 
+namespace gbvlm {
+
+struct LuSolveTables {
+    LuBatch<float> B;
+    void* work = nullptr;
+    size_t work_bytes = 0;
+};
+
+int lu_solve_prepare_f32(gbvlm_lu h, const float* A, int64_t n, float* X, void** tables, cudaStream_t st) {
+    GB_REQUIRE(h && A && X && tables && n >= 1, "null argument");
+    GB_REQUIRE(h->plan_n == n, "LU solve before factorize for this size");
+    auto* t = new LuSolveTables();
+    int rc = make_single_batch<float>(t->B, n, n, (float*)A, h->d_ipiv, h->d_perm, h->d_info, X, n, 1, &t->work,
+                                      &t->work_bytes, st);
+    if (rc) {
+        lu_solve_tables_free(t);
+        return rc;
+    }
+    *tables = t;
+    return GBVLM_OK;
+}
+
+int lu_solve_prepared_f32(gbvlm_lu h, void* tables, int64_t n, cudaStream_t st) {
+    GB_REQUIRE(h && tables, "null argument");
+    const LuSolveTables* t = (const LuSolveTables*)tables;
+    return lu_batch_solve<float>(t->B, 1, 1, n, st, h->plan.tc_passes ? h->plan.d_err : nullptr);
+}
+
+void lu_solve_tables_free(void* tables) {
+    auto* t = (LuSolveTables*)tables;
+    if (!t) return;
+    if (t->work) cudaFree(t->work);
+    delete t;
+}
+
+}  // namespace gbvlm
+
 extern "C" {
 
 int gbvlm_lu_create(gbvlm_lu* out) {

@@ -432,15 +432,17 @@ struct WakeArgs {
     int64_t rows_per_slice;
     T* partial;          // [slices][n_targets]
     int32_t sc;          // spanwise rings staged per chunk (<= WK_MAXSPAN)
+    const int64_t* it_dev;  // if set: the iteration, read on the device (the grid covers up to `iteration`)
 };
 
 // number of active ring rows of surface m and the first one
 template <class T>
 __device__ __forceinline__ void wake_rows(const WakeArgs<T>& w, int m, int64_t& first, int64_t& count) {
     const int64_t v_m = w.s.nwv[m];
-    first = v_m - w.iteration - 1;
+    const int64_t it = w.it_dev ? *w.it_dev : w.iteration;
+    first = v_m - it - 1;
     int64_t end = v_m - 1;
-    if (w.window > 0 && w.iteration > w.window) end = v_m - 1 - w.iteration + w.window;
+    if (w.window > 0 && it > w.window) end = v_m - 1 - it + w.window;
     count = end - first;
     if (count < 0) count = 0;
 }
@@ -462,8 +464,18 @@ __global__ void __launch_bounds__(WK_THREADS) k_wake_influence(WakeArgs<T> w) {
         nx = w.s.b[m][p]; ny = w.s.b[m][np + p]; nz = w.s.b[m][2 * np + p];
     }
     // this block's global row range [R0, R1) over the concatenation of lifting wakes
+    int64_t total_rows = w.total_rows;
+    if (w.it_dev) {  // rows of the current iteration; slices past them contribute zero
+        total_rows = 0;
+        for (int m = 0; m < w.s.n; m++)
+            if (w.s.flag[m]) {
+                int64_t f_, c_;
+                wake_rows(w, m, f_, c_);
+                total_rows += c_;
+            }
+    }
     const int64_t R0 = (int64_t)blockIdx.y * w.rows_per_slice;
-    const int64_t R1 = min(R0 + w.rows_per_slice, w.total_rows);
+    const int64_t R1 = min(R0 + w.rows_per_slice, total_rows);
     T acc = 0;
     int64_t base = 0;
     for (int m = 0; m < w.s.n && base < R1; m++) {
@@ -523,13 +535,14 @@ template <class T>
 static int wake_influence(T* rhs, int32_t nsurf, const gbvlm_dims* dims, const T* const* gamma_wake,
                           const T* const* colloc, const T* const* normals, const T* const* verts_wake,
                           const int32_t* lifting, int32_t iteration, T sigma, int32_t window, T* scratch,
-                          size_t scratch_elems, cudaStream_t st) {
+                          size_t scratch_elems, cudaStream_t st, const int64_t* it_dev = nullptr) {
     WakeArgs<T> w;
     int rc = make_surfs(w.s, nsurf, dims);
     if (rc) return rc;
     GB_REQUIRE(rhs != nullptr, "rhs is null");
     GB_REQUIRE(lifting != nullptr, "lifting is null");
     GB_REQUIRE(iteration >= 0, "iteration < 0");
+    w.it_dev = it_dev;
     w.iteration = iteration;
     w.window = window;
     w.sigma2 = sigma * sigma;
@@ -561,6 +574,7 @@ static int wake_influence(T* rhs, int32_t nsurf, const gbvlm_dims* dims, const T
     if (rps < WK_ROWS) rps = WK_ROWS;
     slices = cdiv(total, rps);
     if (scratch == nullptr) {
+        GB_REQUIRE(it_dev == nullptr, "the device-iteration form needs its own scratch");
         void* p = nullptr;
         rc = device_scratch(sizeof(T) * slices * ntg, &p, st);
         if (rc) return rc;
@@ -937,6 +951,41 @@ __global__ void k_gamma_update(int64_t ns, int64_t nc, const T* x, T* g, T* gd, 
     if (dgdt) dgdt[p] = (v - gp[p]) * inv_dt;
 }
 
+// the same two with the iteration read on the device (graph replay)
+template <class T>
+__global__ void k_wake_shed_dev(Surfs<T> s, const int64_t* it_dev) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int m = 0;
+    int64_t base = 0;
+    while (m < s.n) {
+        int64_t cnt = 4 * (s.ns[m] + 1);
+        if (g < base + cnt) break;
+        base += cnt;
+        m++;
+    }
+    if (m >= s.n) return;
+    const int64_t it = *it_dev;
+    if (it < 0 || it >= s.nwv[m]) return;
+    int64_t r = g - base, n = s.ns[m] + 1;
+    int64_t k = r / n, i = r % n;
+    int64_t vld = n * (s.nc[m] + 1), kld = n * s.nwv[m];
+    s.o0[m][k * kld + i + (s.nwv[m] - 1 - it) * n] = s.a[m][k * vld + i + s.nc[m] * n];
+}
+
+template <class T>
+__global__ void k_gamma_update_dev(int64_t ns, int64_t nc, const T* x, T* g, T* gd, T* gw, int64_t col_base,
+                                   const int64_t* it_dev, const T* gp, T* dgdt, T inv_dt, int64_t ncols) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= ns * nc) return;
+    int64_t i = p % ns, j = p / ns;
+    T v = x[p];
+    g[p] = v;
+    gd[p] = (j > 0) ? v - x[p - ns] : v;
+    const int64_t wcol = col_base - *it_dev;
+    if (gw && j == nc - 1 && wcol >= 0 && wcol < ncols) gw[i + wcol * ns] = v;
+    if (dgdt) dgdt[p] = (v - gp[p]) * inv_dt;
+}
+
 // ---------------------------------------------------------------------------
 // Trefftz-plane drag (ispc:273-323): one block per spanwise ring
 // ---------------------------------------------------------------------------
@@ -1040,6 +1089,54 @@ int gbvlm_rhs_assemble_wake_influence_f32(float* rhs, int32_t nsurf, const gbvlm
     return wake_influence<float>(rhs, nsurf, dims, gamma_wake, colloc, normals, verts_wake, lifting, iteration, sigma,
                                  5000, nullptr, 0, to_cuda(stream));
 }
+}  // extern "C"
+
+namespace gbvlm {
+
+int wake_influence_dev_f32(float* rhs, int32_t nsurf, const gbvlm_dims* dims, const float* const* gamma_wake,
+                           const float* const* colloc, const float* const* normals, const float* const* verts_wake,
+                           const int32_t* lifting, const int64_t* it_dev, int32_t it_max, float* scratch,
+                           cudaStream_t st) {
+    GB_REQUIRE(colloc && normals && it_dev && scratch, "null argument");
+    int64_t ntg = 0;
+    for (int m = 0; m < nsurf; m++) ntg += dims[m].ns * dims[m].nc;
+    return wake_influence<float>(rhs, nsurf, dims, gamma_wake, colloc, normals, verts_wake, lifting, it_max, 0.f, 5000,
+                                 scratch, (size_t)(WAKE_DEV_MAX_SLICES * ntg), st, it_dev);
+}
+
+int wake_shed_dev_f32(int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_wing, float* const* verts_wake,
+                      const int64_t* it_dev, cudaStream_t st) {
+    Surfs<float> s;
+    int rc = make_surfs(s, nsurf, dims);
+    if (rc) return rc;
+    int64_t total = 0;
+    for (int m = 0; m < nsurf; m++) {
+        GB_REQUIRE(verts_wing[m] && verts_wake[m], "null pointer surface %d", m);
+        s.a[m] = verts_wing[m];
+        s.o0[m] = verts_wake[m];
+        total += 4 * (dims[m].ns + 1);
+    }
+    k_wake_shed_dev<float><<<(unsigned)cdiv(total, 256), 256, 0, st>>>(s, it_dev);
+    GB_LAUNCH_CHECK();
+    return GBVLM_OK;
+}
+
+int gamma_update_dev_f32(int64_t ns, int64_t nc, const float* x, float* gamma, float* gamma_delta, float* gamma_wake,
+                         int64_t col_base, const int64_t* it_dev, const float* gamma_prev, float* dgamma_dt, float dt,
+                         cudaStream_t st) {
+    GB_REQUIRE(ns >= 1 && nc >= 1 && x && gamma && gamma_delta && it_dev, "bad arguments");
+    GB_REQUIRE(!dgamma_dt || (gamma_prev && dt != 0.f), "dgamma_dt needs gamma_prev and dt != 0");
+    k_gamma_update_dev<float><<<(unsigned)cdiv(ns * nc, 256), 256, 0, st>>>(
+        ns, nc, x, gamma, gamma_delta, gamma_wake, col_base, it_dev, gamma_prev, dgamma_dt, dgamma_dt ? 1.f / dt : 0.f,
+        col_base + 1);
+    GB_LAUNCH_CHECK();
+    return GBVLM_OK;
+}
+
+}  // namespace gbvlm
+
+extern "C" {
+
 int gbvlm_rhs_assemble_wake_influence_f64(double* rhs, int32_t nsurf, const gbvlm_dims* dims,
                                           const double* const* gamma_wake, const double* const* colloc,
                                           const double* const* normals, const double* const* verts_wake,

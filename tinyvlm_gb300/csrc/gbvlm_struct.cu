@@ -118,6 +118,15 @@ __global__ void k_newmark_step(int nd, const NewmarkDev* dev, NewmarkCoef k, con
     newmark_step_dev(nd, dev, k, M, C, v, a, dF, du, dv, da);
 }
 
+// the step with the state of step *i_dev (graph replay)
+__global__ void k_newmark_step_dev(int nd, const NewmarkDev* dev, NewmarkCoef k, const double* M, const double* C,
+                                   const double* v, const double* a, const int64_t* i_dev, const double* dF,
+                                   double* du, double* dv, double* da) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int64_t i = *i_dev;
+    newmark_step_dev(nd, dev, k, M, C, v + nd * i, a + nd * i, dF, du, dv, da);
+}
+
 }  // namespace gbvlm
 
 using namespace gbvlm;
@@ -185,3 +194,19 @@ int gbvlm_newmark_step(gbvlm_newmark h, const double* M, const double* C, const 
 }
 
 }  // extern "C"
+
+namespace gbvlm {
+
+int newmark_step_dev(gbvlm_newmark h, const double* M, const double* C, const double* v, const double* a,
+                     const int64_t* i_dev, double* du, double* dv, double* da, const double* delta_F, double dt,
+                     cudaStream_t st) {
+    GB_REQUIRE(h && M && C && v && a && i_dev && du && dv && da && delta_F, "null argument");
+    GB_REQUIRE(h->nd > 0, "Newmark: step before init");
+    GB_REQUIRE(dt > 0, "Newmark: dt must be positive");
+    const NewmarkCoef k = newmark_coef(h->beta, h->gamma, dt);
+    k_newmark_step_dev<<<1, 32, 0, st>>>(h->nd, h->dev, k, M, C, v, a, i_dev, delta_F, du, dv, da);
+    GB_LAUNCH_CHECK();
+    return GBVLM_OK;
+}
+
+}  // namespace gbvlm

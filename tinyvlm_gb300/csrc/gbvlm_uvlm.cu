@@ -445,12 +445,17 @@ struct A2Dev {
     double coef[4];  // CL, CM x, y, z of the iterate
     float T[16], dT[16], ref[3], fs[3];
     int converged;
+    int32_t iter, max_iter;  // Newton iterations of the current step, and their limit
+    int64_t step;            // the step being advanced: state i -> i + 1
+    int64_t wit;             // wake rows of that step's solve (step + 1)
 };
 
 // state at i+1 from the Newmark increments, the pose and the moment point
-__global__ void k_a2_pose(A2Dev* d, double* u, double* v, double* a, int64_t i, double t_next, double a_h,
-                          int32_t nsurf, float* T_all, float* dT_all) {
+__global__ void k_a2_pose(A2Dev* d, double* u, double* v, double* a, float dtf, double a_h, int32_t nsurf,
+                          float* T_all, float* dT_all) {
     if (threadIdx.x != 0) return;
+    const int64_t i = d->step;
+    const double t_next = (double)((float)i * dtf + dtf);
     double* u1 = u + 2 * (i + 1);
     double* v1 = v + 2 * (i + 1);
     double* a1 = a + 2 * (i + 1);
@@ -510,10 +515,13 @@ __global__ void k_a2_flap(float* gdelta1, const float* gamma0, int64_t ns, int64
 
 __host__ __device__ inline double torsional_cubic(double al) { return 0.1 * al + 40.0 * al * al * al; }
 
-// loads of the iterate (uvlm_2dof.cpp:728-744) and the Newton test
-__global__ void k_a2_loads(A2Dev* d, double* u, double* F, int64_t i, double mu, double r_a, double om, double Ua,
-                           double eps) {
+// loads of the iterate (uvlm_2dof.cpp:728-744) and the Newton test; the
+// loop of the time step's graph continues while the test fails and at most
+// max_iter iterations have run (the reference's loop, :639-807)
+__global__ void k_a2_loads(A2Dev* d, double* u, double* F, double mu, double r_a, double om, double Ua, double eps,
+                           cudaGraphConditionalHandle loop) {
     if (threadIdx.x != 0) return;
+    const int64_t i = d->step;
     const double pi_f = (double)3.141593f;
     F[2 * (i + 1)] = -d->coef[0] / (pi_f * mu);
     F[2 * (i + 1) + 1] = (2.0 * d->coef[2]) / (pi_f * mu * r_a * r_a);
@@ -522,6 +530,39 @@ __global__ void k_a2_loads(A2Dev* d, double* u, double* F, int64_t i, double mu,
                1.0 / (Ua * Ua) * (torsional_cubic(u[2 * (i + 1) + 1]) - torsional_cubic(u[2 * i + 1]));
     const double k0 = d->du_prev[0] - d->du[0], k1 = d->du_prev[1] - d->du[1];
     d->converged = sqrt(k0 * k0 + k1 * k1) <= eps ? 1 : 0;
+    d->iter += 1;
+    cudaGraphSetConditional(loop, (!d->converged && d->iter <= d->max_iter) ? 1u : 0u);
+}
+
+// start of a time step: the previous circulation kept, increments and the
+// iteration count cleared
+struct A2Copy {
+    int32_t n;
+    const float* src[GBVLM_MAX_SURFACES];
+    float* dst[GBVLM_MAX_SURFACES];
+    int64_t cnt[GBVLM_MAX_SURFACES];
+};
+__global__ void k_a2_step_begin(A2Dev* d, A2Copy c) {
+    for (int m = 0; m < c.n; m++)
+        for (int64_t e = threadIdx.x; e < c.cnt[m]; e += blockDim.x) c.dst[m][e] = c.src[m][e];
+    if (threadIdx.x == 0) {
+        d->dF[0] = d->dF[1] = 0.0;
+        d->du[0] = d->du[1] = 0.0;
+        d->iter = 0;
+    }
+}
+// end of a time step: its iteration count recorded, the next step's indices
+__global__ void k_a2_step_end(A2Dev* d, int32_t* iters) {
+    if (threadIdx.x != 0) return;
+    iters[d->step] = d->iter;
+    d->step += 1;
+    d->wit = d->step + 1;
+}
+__global__ void k_a2_set(A2Dev* d, int64_t step, int32_t max_iter) {
+    if (threadIdx.x != 0) return;
+    d->step = step;
+    d->wit = step + 1;
+    d->max_iter = max_iter;
 }
 
 struct Aero2Dof {
@@ -541,8 +582,22 @@ struct Aero2Dof {
     gbvlm_newmark nm = nullptr;
     std::vector<int32_t> iters;
     CoefArgs<float> ca;
+    // one time step as a CUDA graph: the Newton iterations in a conditional
+    // while node, replayed step after step without host round trips
+    void* aux = nullptr;             // iteration counts per step, wake-influence scratch
+    int32_t* iters_dev = nullptr;
+    float* wscratch = nullptr;
+    void* lut = nullptr;             // the staged LU solve of the factored AIC
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
 
     ~Aero2Dof() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+        if (lut) lu_solve_tables_free(lut);
+        if (aux) cudaFree(aux);
         if (lu) gbvlm_lu_destroy(lu);
         if (nm) gbvlm_newmark_destroy(nm);
         if (mem) cudaFree(mem);
@@ -604,6 +659,12 @@ struct Aero2Dof {
         a = (double*)take(8 * 2 * t_steps);
         F = (double*)take(8 * 2 * t_steps);
         dev = (A2Dev*)take(sizeof(A2Dev));
+        {
+            const size_t ib = (sizeof(int32_t) * t_steps + 255) / 256 * 256;
+            GB_CUDA(cudaMalloc(&aux, ib + sizeof(float) * WAKE_DEV_MAX_SLICES * n));
+            iters_dev = (int32_t*)aux;
+            wscratch = (float*)((char*)aux + ib);
+        }
         for (auto& x : dims) {
             const int64_t np = x.ns * x.nc, nv = (x.ns + 1) * (x.nc + 1);
             vinit.push_back((float*)take(4 * 4 * nv));
@@ -696,6 +757,7 @@ struct Aero2Dof {
                                    0.f, s)))
             return rc;
         if ((rc = Ops2<float>::factor(lu, lhs, n, s))) return rc;
+        if (!lut && (rc = lu_solve_prepare_f32(lu, lhs, n, rhs, &lut, st))) return rc;
         if ((rc = Ops2<float>::shed(nsurf, dims.data(), C(verts).data(), wake.data(), 0, s))) return rc;
         if ((rc = aero_solve(0, st))) return rc;
         done = 0;
@@ -733,16 +795,16 @@ struct Aero2Dof {
         return GBVLM_OK;
     }
 
-    // one Newton iteration of time step i (uvlm_2dof.cpp:639-751)
-    int iterate(int64_t i, cudaStream_t st) {
+    // one Newton iteration of the step dev->step (uvlm_2dof.cpp:639-751), with
+    // every step-dependent index read on the device: captured into the body
+    // of the step graph's while node
+    int iterate_dev(cudaStream_t st, cudaGraphConditionalHandle loop) {
         gbvlm_stream s = (gbvlm_stream)st;
         int rc;
         GB_CUDA(cudaMemcpyAsync(dev->du_prev, dev->du, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st));
-        if ((rc = gbvlm_newmark_step(nm, dev->M, dev->C, v + 2 * i, a + 2 * i, dev->du, dev->dv, dev->da, dev->dF, dt,
-                                     s)))
+        if ((rc = newmark_step_dev(nm, dev->M, dev->C, v, a, &dev->step, dev->du, dev->dv, dev->da, dev->dF, dt, st)))
             return rc;
-        const float tn = (float)i * (float)dt + (float)dt;
-        k_a2_pose<<<1, 32, 0, st>>>(dev, u, v, a, i, (double)tn, vars.a_h, nsurf, T_all, dT_all);
+        k_a2_pose<<<1, 32, 0, st>>>(dev, u, v, a, (float)dt, vars.a_h, nsurf, T_all, dT_all);
         GB_LAUNCH_CHECK();
         std::vector<const float*> tr(nsurf);
         for (int m = 0; m < nsurf; m++) tr[m] = T_all + 16 * m;
@@ -750,43 +812,110 @@ struct Aero2Dof {
         if ((rc = Ops2<float>::metrics(nsurf, dims.data(), C(verts).data(), colloc.data(), normals.data(),
                                        areas.data(), s)))
             return rc;
-        if ((rc = Ops2<float>::shed(nsurf, dims.data(), C(verts).data(), wake.data(), (int32_t)(i + 1), s))) return rc;
-        if ((rc = aero_solve(i + 1, st))) return rc;
+        if ((rc = wake_shed_dev_f32(nsurf, dims.data(), C(verts).data(), wake.data(), &dev->wit, st))) return rc;
+        // velocities, RHS, solve and circulation of the pose (wake rows 0..step+1)
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t np = dims[m].ns * dims[m].nc;
+            k_dual_velocity<float><<<(unsigned)cdiv(np, 256), 256, 0, st>>>(dT_all + 16 * m, colloch[m], vel[m], np);
+            GB_LAUNCH_CHECK();
+        }
+        GB_CUDA(cudaMemsetAsync(rhs, 0, 4 * n, st));
+        if ((rc = Ops2<float>::rhsv(rhs, nsurf, dims.data(), C(normals).data(), C(vel).data(), s))) return rc;
+        if ((rc = wake_influence_dev_f32(rhs, nsurf, dims.data(), C(gwake).data(), C(colloc).data(),
+                                         C(normals).data(), C(wake).data(), lifting.data(), &dev->wit,
+                                         (int32_t)(t_steps - 2), wscratch, st)))
+            return rc;
+        if ((rc = lu_solve_prepared_f32(lu, lut, n, st))) return rc;
+        int64_t off = 0;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t ns = dims[m].ns, nc = dims[m].nc;
+            if ((rc = gamma_update_dev_f32(ns, nc, rhs + off, gamma[m], gdelta[m], gwake[m], t_steps - 2, &dev->wit,
+                                           gprev[m], gdt[m], (float)dt, st)))
+                return rc;
+            off += ns * nc;
+        }
+        if (nsurf > 1 && dims[1].ns == dims[0].ns) {
+            k_a2_flap<<<(unsigned)cdiv(dims[1].ns, 128), 128, 0, st>>>(gdelta[1], gamma[0], dims[0].ns, dims[0].nc);
+            GB_LAUNCH_CHECK();
+        }
         for (int m = 0; m < nsurf; m++)
             if ((rc = Ops2<float>::forces(dims[m].ns, dims[m].nc, verts[m], gdelta[m], gdt[m], vel[m], areas[m],
                                           normals[m], forces[m], s)))
                 return rc;
         k_step_coeffs<float><<<1, 512, 0, st>>>(ca, dev->fs, dev->ref, 0, vars.rho, dev->coef);
         GB_LAUNCH_CHECK();
-        k_a2_loads<<<1, 32, 0, st>>>(dev, u, F, i, vars.mu, vars.r_a, vars.omega, vars.U_a,
-                                     (double)1.1920928955078125e-07);
+        k_a2_loads<<<1, 32, 0, st>>>(dev, u, F, vars.mu, vars.r_a, vars.omega, vars.U_a,
+                                     (double)1.1920928955078125e-07, loop);
         GB_LAUNCH_CHECK();
+        return GBVLM_OK;
+    }
+
+    // the step graph: begin (previous circulation, cleared increments) ->
+    // while (Newton test fails and iterations <= max_iter) { iteration } -> end
+    int build_graph() {
+        if (exec) return GBVLM_OK;
+        GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        GB_CUDA(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle loop;
+        GB_CUDA(cudaGraphConditionalHandleCreate(&loop, graph, 1, cudaGraphCondAssignDefault));
+        A2Copy cp{};
+        cp.n = nsurf;
+        for (int m = 0; m < nsurf; m++) {
+            cp.src[m] = gamma[m];
+            cp.dst[m] = gprev[m];
+            cp.cnt[m] = dims[m].ns * dims[m].nc;
+        }
+        cudaGraphNode_t nb, nw, ne;
+        {
+            void* args[] = {&dev, &cp};
+            cudaKernelNodeParams kp = {};
+            kp.func = (void*)k_a2_step_begin;
+            kp.gridDim = dim3(1);
+            kp.blockDim = dim3(256);
+            kp.kernelParams = args;
+            GB_CUDA(cudaGraphAddKernelNode(&nb, graph, nullptr, 0, &kp));
+        }
+        cudaGraphNodeParams wp = {};
+        wp.type = cudaGraphNodeTypeConditional;
+        wp.conditional.handle = loop;
+        wp.conditional.type = cudaGraphCondTypeWhile;
+        wp.conditional.size = 1;
+        GB_CUDA(cudaGraphAddNode(&nw, graph, &nb, nullptr, 1, &wp));
+        cudaGraph_t body = wp.conditional.phGraph_out[0];
+        GB_CUDA(cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        int rc = iterate_dev(cap, loop);
+        cudaGraph_t got = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(cap, &got);
+        if (rc) return rc;
+        GB_CUDA(e);
+        {
+            void* args[] = {&dev, &iters_dev};
+            cudaKernelNodeParams kp = {};
+            kp.func = (void*)k_a2_step_end;
+            kp.gridDim = dim3(1);
+            kp.blockDim = dim3(32);
+            kp.kernelParams = args;
+            GB_CUDA(cudaGraphAddKernelNode(&ne, graph, &nw, 1, &kp));
+        }
+        GB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
         return GBVLM_OK;
     }
 
     int run(int64_t steps, int32_t max_iter, cudaStream_t st) {
         GB_REQUIRE(done + steps <= t_steps - 2, "aeroelastic 2-DOF: %lld steps requested, %lld left",
                    (long long)steps, (long long)(t_steps - 2 - done));
-        int* hflag = (int*)host_scratch(sizeof(int));
-        for (int64_t k = 0; k < steps; k++) {
-            const int64_t i = done;
-            for (int m = 0; m < nsurf; m++)
-                GB_CUDA(cudaMemcpyAsync(gprev[m], gamma[m], 4 * dims[m].ns * dims[m].nc, cudaMemcpyDeviceToDevice,
-                                        st));
-            GB_CUDA(cudaMemsetAsync(dev->dF, 0, sizeof(double) * 2, st));
-            GB_CUDA(cudaMemsetAsync(dev->du, 0, sizeof(double) * 2, st));
-            int it = 0;
-            while (true) {
-                int rc = iterate(i, st);
-                if (rc) return rc;
-                it++;
-                GB_CUDA(cudaMemcpyAsync(hflag, &dev->converged, sizeof(int), cudaMemcpyDeviceToHost, st));
-                GB_CUDA(cudaStreamSynchronize(st));
-                if (*hflag || it > max_iter) break;
-            }
-            iters.push_back(it);
-            done++;
-        }
+        GB_REQUIRE(max_iter >= 0, "aeroelastic 2-DOF: max_iter must be non-negative");
+        if (steps <= 0) return GBVLM_OK;
+        int rc = build_graph();
+        if (rc) return rc;
+        k_a2_set<<<1, 32, 0, st>>>(dev, done, max_iter);
+        GB_LAUNCH_CHECK();
+        for (int64_t k = 0; k < steps; k++) GB_CUDA(cudaGraphLaunch(exec, st));
+        std::vector<int32_t> h(steps);
+        GB_CUDA(cudaMemcpyAsync(h.data(), iters_dev + done, sizeof(int32_t) * steps, cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        iters.insert(iters.end(), h.begin(), h.end());
+        done += steps;
         return GBVLM_OK;
     }
 };
