@@ -70,9 +70,10 @@ struct BatchArgs {
     const double* alphas;   // per solve
     double u_inf, rho, beta;
     double ref[3];
-    double* out;            // per solve: cl, cdi, cmx, cmy, cmz
-    float* gamma_out;       // per solve, n floats at goff[solve] (may be null)
+    double* out;            // per solve in the caller's order: cl, cdi, cmx, cmy, cmz
+    float* gamma_out;       // per solve, n floats at goff[solve] (the caller's order; may be null)
     const int64_t* goff;
+    const int32_t* uidx;    // batch solve -> the caller's solve index
 };
 
 __device__ __forceinline__ void split_hl(double x, float& h, float& l) {
@@ -496,7 +497,7 @@ __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const i
     if (threadIdx.x == 0) {
         const double v2 = len2(V);
         const double macv = s_mac / s_ar;
-        double* o = a.out + 5 * (int64_t)sol;
+        double* o = a.out + 5 * (int64_t)a.uidx[sol];
         o[0] = s_cl / (0.5 * a.rho * v2 * s_ar);
         o[1] = s_cd / (v2 * s_ar);
         const double d = 0.5 * a.rho * v2 * s_ar * macv;
@@ -528,9 +529,11 @@ struct gbvlm_batch_s {
     size_t arena_bytes = 0;
     float* d_vin = nullptr;
     double* d_alpha = nullptr;   // per solve (batch order)
-    double* d_out = nullptr;     // per solve x5 (batch order)
+    double* d_out = nullptr;     // per solve x5 (the caller's order)
     float* d_gamma = nullptr;
     int64_t* d_goff = nullptr;
+    int32_t* d_uidx = nullptr;   // batch solve -> the caller's solve
+    void* status = nullptr;      // pinned: error words and pivot flags read back with the results
     SysDesc* d_sys = nullptr;
     int32_t* d_solve_sys = nullptr;
     int64_t* d_tpfx = nullptr;   // assembly tiles
@@ -560,6 +563,7 @@ struct gbvlm_batch_s {
         if (graph) cudaGraphDestroy(graph);
         if (cap) cudaStreamDestroy(cap);
         if (arena) cudaFree(arena);
+        if (status) cudaFreeHost(status);
         for (int g = 0; g < MAX_GROUPS; g++) {
             plans[g].release();
             if (side[g]) cudaStreamDestroy(side[g]);
@@ -592,6 +596,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     a.out = h->d_out;
     a.gamma_out = h->d_gamma;
     a.goff = h->d_goff;
+    a.uidx = h->d_uidx;
     mark(0);
     k_batch_geom<<<h->nsys, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
@@ -757,6 +762,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     const size_t o_goff = reserve(sizeof(int64_t) * goff.size());
     const size_t o_sys = reserve(sizeof(SysDesc) * h->nsys);
     const size_t o_ssys = reserve(sizeof(int32_t) * solve_sys.size());
+    const size_t o_uidx = reserve(sizeof(int32_t) * solve_sys.size());
     // tile prefix tables
     std::vector<int64_t> tpfx(h->nsys + 1, 0), rpfx(h->nsys + 1, 0);
     for (int k = 0; k < h->nsys; k++) {
@@ -792,6 +798,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     h->d_goff = (int64_t*)(base + o_goff);
     h->d_sys = (SysDesc*)(base + o_sys);
     h->d_solve_sys = (int32_t*)(base + o_ssys);
+    h->d_uidx = (int32_t*)(base + o_uidx);
     h->d_tpfx = (int64_t*)(base + o_tpfx);
     h->d_rpfx = (int64_t*)(base + o_rpfx);
     // system descriptors
@@ -844,6 +851,18 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         lurhs[k] = P.nrhs;
         h->maxn = std::max(h->maxn, P.n);
     }
+    // outputs in the caller's order: circulations packed by the caller's solve
+    // index, so the results copy straight into the caller's buffers
+    std::vector<int32_t> uidx(h->nsolve);
+    {
+        int64_t uoff = 0;
+        for (int32_t u = 0; u < h->nsolve; u++) {
+            const int32_t b = h->solve_order[u];
+            uidx[b] = u;
+            goff[b] = uoff;
+            uoff += h->sys[solve_sys[b]].n;
+        }
+    }
     h->solve_sys = solve_sys;
     h->goff = goff;
     int rc = GBVLM_OK;
@@ -856,6 +875,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     up(h->d_sys, h->sys.data(), sizeof(SysDesc) * h->nsys);
     up(h->d_solve_sys, solve_sys.data(), sizeof(int32_t) * solve_sys.size());
     up(h->d_goff, goff.data(), sizeof(int64_t) * goff.size());
+    up(h->d_uidx, uidx.data(), sizeof(int32_t) * uidx.size());
     up(h->d_tpfx, tpfx.data(), sizeof(int64_t) * tpfx.size());
     up(h->d_rpfx, rpfx.data(), sizeof(int64_t) * rpfx.size());
     up(base + o_lun, lun.data(), sizeof(int64_t) * h->nsys);
@@ -1076,40 +1096,40 @@ int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream) 
 
 int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_stream stream) {
     GB_REQUIRE(h && coeffs, "null argument");
+    GB_REQUIRE(!gamma || h->want_gamma, "gamma requested but the last run did not store it");
     cudaStream_t st = to_cuda(stream);
-    std::vector<double> tmp(5 * (size_t)h->nsolve);
-    GB_CUDA(cudaMemcpyAsync(tmp.data(), h->d_out, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, st));
-    std::vector<float> gt;
-    if (gamma) {
-        GB_REQUIRE(h->want_gamma, "gamma requested but the last run did not store it");
-        gt.resize(h->gamma_floats);
-        GB_CUDA(cudaMemcpyAsync(gt.data(), h->d_gamma, sizeof(float) * gt.size(), cudaMemcpyDeviceToHost, st));
-    }
+    constexpr int G = gbvlm_batch_s::MAX_GROUPS;
+    // outputs are already in the caller's order: straight into the caller's buffers
+    GB_CUDA(cudaMemcpyAsync(coeffs, h->d_out, sizeof(double) * 5 * h->nsolve, cudaMemcpyDeviceToHost, st));
+    if (gamma)
+        GB_CUDA(cudaMemcpyAsync(gamma, h->d_gamma, sizeof(float) * h->gamma_floats, cudaMemcpyDeviceToHost, st));
+    // status words (bounded-wait errors of the LU plans and the triangular
+    // solve, pivot flags) with the same synchronisation
+    const size_t sbytes = sizeof(int32_t) * (G + 1 + (size_t)h->nsys);
+    if (!h->status) GB_CUDA(cudaMallocHost(&h->status, sbytes));
+    int32_t* hs = (int32_t*)h->status;
+    memset(hs, 0, sizeof(int32_t) * (G + 1));
+    for (int g = 0; g < h->ngroups; g++)
+        if (h->plans[g].d_err)
+            GB_CUDA(cudaMemcpyAsync(hs + g, h->plans[g].d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    if (h->use_flow && h->flow.d_ctl)
+        GB_CUDA(cudaMemcpyAsync(hs + G, h->flow.d_ctl + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(hs + G + 1, h->lub.info, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
-    for (int g = 0; g < h->ngroups; g++) {
-        int rc = lu_plan_check(h->plans[g], st);
-        if (rc) return rc;
-    }
-    if (h->use_flow) {
-        int rc = trs_flow_check(h->flow, st);
-        if (rc) return rc;
-    }
-    int32_t* info = (int32_t*)host_scratch(sizeof(int32_t) * h->nsys);
-    GB_CUDA(cudaMemcpy(info, h->lub.info, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost));
-    for (int k = 0; k < h->nsys; k++) {
-        if (info[k] != 0) {
-            set_error("batch system %d (case %d): exactly zero pivot at column %d", k, h->sys[k].case_id, info[k]);
-            return GBVLM_ERR_SINGULAR;
+    for (int g = 0; g < h->ngroups; g++)
+        if (hs[g]) {
+            set_error("LU: a tensor-core update tile timed out waiting for its MMAs");
+            return GBVLM_ERR_CUDA;
         }
+    if (hs[G]) {
+        set_error("triangular solve: a block timed out waiting for the blocks it depends on");
+        return GBVLM_ERR_CUDA;
     }
-    int64_t uoff = 0;
-    for (int32_t u = 0; u < h->nsolve; u++) {
-        const int32_t b = h->solve_order[u];
-        for (int k = 0; k < 5; k++) coeffs[5 * (int64_t)u + k] = tmp[5 * (int64_t)b + k];
-        if (gamma) {
-            const int64_t n = h->sys[h->solve_sys[b]].n;
-            memcpy(gamma + uoff, gt.data() + h->goff[b], sizeof(float) * n);
-            uoff += n;
+    for (int k = 0; k < h->nsys; k++) {
+        if (hs[G + 1 + k] != 0) {
+            set_error("batch system %d (case %d): exactly zero pivot at column %d", k, h->sys[k].case_id,
+                      hs[G + 1 + k]);
+            return GBVLM_ERR_SINGULAR;
         }
     }
     return GBVLM_OK;
