@@ -9,7 +9,9 @@
 // -V.n right-hand side; the (n x N) RHS is multiplied by the DFT matrix and
 // solved with the AIC factored once.  Anderson acceleration
 // (vlm/src/vlm_solvers.cpp:6-115, type II, history m, least squares by
-// Householder QR like LAPACK dgels) iterates the map to a fixed point.  The
+// Householder QR like LAPACK dgels) iterates the map to a fixed point, on
+// the device: iterate, residuals and histories stay in device memory and
+// the host reads one residual norm per iteration.  The
 // instance geometry, normals and -V.n do not depend on gamma and are
 // computed once per run.
 #include <cuda_runtime.h>
@@ -295,34 +297,133 @@ struct HbState {
     }
 };
 
-// Householder least squares min ||A x - b|| for a tall (rows x k) column-major A (k <= 16); A, b overwritten.
-static void lsq_qr(std::vector<double>& A, int64_t rows, int k, std::vector<double>& b, double* x) {
-    for (int j = 0; j < k; j++) {
-        double nrm = 0;
-        for (int64_t i = j; i < rows; i++) nrm += A[i + j * rows] * A[i + j * rows];
-        nrm = sqrt(nrm);
-        if (nrm == 0) continue;
-        const double a0 = A[j + j * rows];
-        const double alpha = a0 > 0 ? -nrm : nrm;
-        A[j + j * rows] = a0 - alpha;
-        double vv = 0;
-        for (int64_t i = j; i < rows; i++) vv += A[i + j * rows] * A[i + j * rows];
-        for (int c = j + 1; c < k; c++) {
-            double d = 0;
-            for (int64_t i = j; i < rows; i++) d += A[i + j * rows] * A[i + c * rows];
-            const double f = 2 * d / vv;
-            for (int64_t i = j; i < rows; i++) A[i + c * rows] -= f * A[i + j * rows];
+// ---------------------------------------------------------------------------
+// Anderson acceleration on the device (vlm/src/vlm_solvers.cpp:6-115): the
+// iterate, residuals and the m-column histories X (iterate steps) and G
+// (residual steps) stay in device memory; one CTA solves the small least
+// squares min |G[:, :mk] gam - g| by Householder QR (reflector columns in
+// a work copy of G, the right-hand side reflected alongside, then back
+// substitution) and forms the next iterate; the host reads one norm per
+// iteration.  Columns are L = n * N long (a few hundred to a few thousand).
+// ---------------------------------------------------------------------------
+constexpr int AA_THREADS = 512;
+
+__device__ double aa_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();  // sh free (previous sum read)
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double r = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) r += sh[k];
+    return r;
+}
+
+// sum over one warp, every lane gets it
+__device__ __forceinline__ double aa_wsum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// x_new = x + g - sum_j (X_j + G_j) gam_j with gam the least-squares
+// coefficients of G[:, :mk]; X[:, slot] = x_new - x; x = x_new (in place).
+// The CTA copies G[:, :mk] and g into shared memory (or, when they do not
+// fit, into the global work buffers Wg, bg) and runs the Householder QR
+// there: for each column j, warp 0 forms the reflector (its norm, the new
+// pivot, v^T v = 2 |a| (|a| + |a_j|)), then the warps reflect the later
+// columns and the right-hand side in parallel, one column per warp at a
+// time.  fp64 runs at a small fraction of the fp32 rate on this part, so the
+// work is spread over all four schedulers' fp64 units.
+constexpr int AA_STEP_THREADS = 256;
+
+__global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, int mk, int slot, double* X,
+                                                                   const double* G, double* Wg, double* bg,
+                                                                   const double* g, double* x, int use_smem) {
+    extern __shared__ double aa_sm[];
+    __shared__ double gam[16], diag[16];
+    __shared__ double s_nrm, s_rvv;
+    double* W = use_smem ? aa_sm : Wg;
+    double* b = use_smem ? aa_sm + L * mk : bg;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    for (int64_t e = tid; e < L * mk; e += blockDim.x) W[e] = G[e];
+    for (int64_t i = tid; i < L; i += blockDim.x) b[i] = g[i];
+    // dot products over rows j..L-1, four partial sums per lane, warp-reduced
+    auto dot = [&](const double* u, const double* w, int j) {
+        double t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+        int64_t i = j + lane;
+        for (; i + 96 < L; i += 128) {
+            t0 += u[i] * w[i];
+            t1 += u[i + 32] * w[i + 32];
+            t2 += u[i + 64] * w[i + 64];
+            t3 += u[i + 96] * w[i + 96];
         }
-        double d = 0;
-        for (int64_t i = j; i < rows; i++) d += A[i + j * rows] * b[i];
-        const double f = 2 * d / vv;
-        for (int64_t i = j; i < rows; i++) b[i] -= f * A[i + j * rows];
-        A[j + j * rows] = alpha;  // R diagonal
+        for (; i < L; i += 32) t0 += u[i] * w[i];
+        return aa_wsum((t0 + t1) + (t2 + t3));
+    };
+    __syncthreads();
+    for (int j = 0; j < mk; j++) {
+        double* wj = W + (int64_t)j * L;
+        if (wid == 0) {
+            const double nrm = sqrt(dot(wj, wj, j));
+            if (lane == 0) {
+                s_nrm = nrm;
+                diag[j] = 0;
+                if (nrm != 0) {
+                    const double a0 = wj[j];
+                    const double alpha = a0 > 0 ? -nrm : nrm;
+                    wj[j] = a0 - alpha;
+                    diag[j] = alpha;
+                    s_rvv = 1.0 / (2.0 * nrm * (nrm + fabs(a0)));
+                }
+            }
+        }
+        __syncthreads();
+        if (s_nrm != 0) {  // uniform
+            const double rvv = s_rvv;
+            for (int t = wid; t < mk - j; t += nw) {  // the later columns, then the right-hand side
+                double* wc = t < mk - j - 1 ? W + (int64_t)(j + 1 + t) * L : b;
+                const double f = 2.0 * dot(wj, wc, j) * rvv;
+                for (int64_t i = j + lane; i < L; i += 32) wc[i] -= f * wj[i];
+            }
+        }
+        __syncthreads();
     }
-    for (int j = k - 1; j >= 0; j--) {
-        double s = b[j];
-        for (int c = j + 1; c < k; c++) s -= A[j + c * rows] * x[c];
-        x[j] = A[j + j * rows] != 0 ? s / A[j + j * rows] : 0;
+    if (tid == 0)
+        for (int j = mk - 1; j >= 0; j--) {
+            double sj = b[j];
+            for (int c = j + 1; c < mk; c++) sj -= W[j + (int64_t)c * L] * gam[c];
+            gam[j] = diag[j] != 0 ? sj / diag[j] : 0;
+        }
+    __syncthreads();
+    for (int64_t i = tid; i < L; i += blockDim.x) {
+        double v = x[i] + g[i];
+        for (int j = 0; j < mk; j++) v -= (X[i + (int64_t)L * j] + G[i + (int64_t)L * j]) * gam[j];
+        X[i + (int64_t)L * slot] = v - x[i];
+        x[i] = v;
+    }
+}
+
+// after a map: g_new = f(x) - x; G[:, slot] = g_new - g (slot < 0: none);
+// g = g_new; *norm = |g|
+__global__ void __launch_bounds__(AA_THREADS) k_anderson_post(int64_t L, int slot, const double* fx, const double* x,
+                                                              double* g, double* G, double* norm) {
+    __shared__ double sh[32];
+    double t = 0;
+    for (int64_t i = threadIdx.x; i < L; i += blockDim.x) {
+        const double gn = fx[i] - x[i];
+        if (slot >= 0) G[i + (int64_t)L * slot] = gn - g[i];
+        g[i] = gn;
+        t += gn * gn;
+    }
+    const double s2 = aa_sum(t, sh);
+    if (threadIdx.x == 0) *norm = sqrt(s2);
+}
+
+// the first step (vlm_solvers.cpp:49-66): X[:, 0] = g, x = f(x)
+__global__ void k_anderson_first(int64_t L, const double* fx, double* x, const double* g, double* X) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L; i += (int64_t)gridDim.x * blockDim.x) {
+        X[i] = g[i];
+        x[i] = fx[i];
     }
 }
 
@@ -382,52 +483,59 @@ int gbvlm_hbvlm_solve(gbvlm_hbvlm h, double* x, double omega, double dt, int32_t
     GB_REQUIRE(h && x && h->st.N > 0, "solve before prepare");
     GB_REQUIRE(m >= 1 && m <= 16 && max_iter >= 2, "history m in [1, 16], max_iter >= 2");
     HbState& S = h->st;
+    cudaStream_t st = to_cuda(stream);
     const int64_t L = S.n * S.N;
-    std::vector<double> xc(x, x + L), xn(L), gc(L), gn(L), X((size_t)L * m, 0.0), G((size_t)L * m, 0.0), Gk, rhs;
-    auto f = [&](const std::vector<double>& in, std::vector<double>& out) {
-        return gbvlm_hbvlm_map(h, in.data(), out.data(), omega, dt, stream);
+    const int32_t H = (S.N - 1) / 2;
+    // device state: the iterate lives in the map's input S.Xin; g, the
+    // histories X and G, the QR work copy of G and its right-hand side
+    double* buf = nullptr;
+    GB_CUDA(cudaMalloc((void**)&buf, sizeof(double) * ((size_t)L * (3 * m + 2) + 1)));
+    double *g = buf, *X = g + L, *G = X + (size_t)L * m, *W = G + (size_t)L * m, *b = W + (size_t)L * m,
+           *dnorm = b + L;
+    double* hn = (double*)host_scratch(sizeof(double));
+    int rc = GBVLM_OK;
+    auto fail = [&](int r) {
+        cudaFree(buf);
+        return r;
     };
-    // vlm_solvers.cpp:49-66
-    int rc;
-    if ((rc = f(xc, xn))) return rc;
-    for (int64_t i = 0; i < L; i++) gc[i] = xn[i] - xc[i];
-    for (int64_t i = 0; i < L; i++) X[i] = gc[i];
-    xc = xn;
-    if ((rc = f(xc, xn))) return rc;
-    for (int64_t i = 0; i < L; i++) {
-        gn[i] = xn[i] - xc[i];
-        G[i] = gn[i] - gc[i];
-    }
-    gc = gn;
+    auto map = [&]() { return S.map_dev(omega, dt, H, st); };  // S.Xin -> S.Xout
+    const unsigned g1 = (unsigned)std::min<int64_t>(cdiv(L, 256), 1024);
+    if (cudaMemcpyAsync(S.Xin, x, sizeof(double) * L, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__));
+    if (cudaMemsetAsync(X, 0, sizeof(double) * (size_t)L * m * 2, st) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__));
+    // vlm_solvers.cpp:49-66: g0 = f(x0) - x0; X0 = g0; x1 = f(x0); g1 = f(x1) - x1; G0 = g1 - g0
+    if ((rc = map())) return fail(rc);
+    k_anderson_post<<<1, AA_THREADS, 0, st>>>(L, -1, S.Xout, S.Xin, g, G, dnorm);
+    k_anderson_first<<<g1, 256, 0, st>>>(L, S.Xout, S.Xin, g, X);
+    if ((rc = map())) return fail(rc);
+    k_anderson_post<<<1, AA_THREADS, 0, st>>>(L, 0, S.Xout, S.Xin, g, G, dnorm);
+    if (cudaGetLastError() != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "Anderson", __FILE__, __LINE__));
+    // the QR's columns in shared memory when m of them and g fit
+    const size_t smem = sizeof(double) * (size_t)L * (m + 1);
+    const int use_smem = smem <= 200 * 1024 ? 1 : 0;
+    if (use_smem && cudaFuncSetAttribute(k_anderson_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                        cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__));
     int k = 1;
-    auto norm = [&](const std::vector<double>& v) {
-        double s = 0;
-        for (double a : v) s += a * a;
-        return sqrt(s);
-    };
-    while (k < max_iter && norm(gc) > tol) {
-        const int mk = std::min(m, k);
-        Gk.assign(G.begin(), G.begin() + (size_t)L * mk);
-        rhs = gc;
-        double gam[16];
-        lsq_qr(Gk, L, mk, rhs, gam);
-        for (int64_t i = 0; i < L; i++) {
-            double v = xc[i] + gc[i];
-            for (int j = 0; j < mk; j++) v -= (X[i + (size_t)L * j] + G[i + (size_t)L * j]) * gam[j];
-            xn[i] = v;
-        }
-        const int slot = k % m;
-        for (int64_t i = 0; i < L; i++) X[i + (size_t)L * slot] = xn[i] - xc[i];
-        xc = xn;
-        if ((rc = f(xc, xn))) return rc;
-        for (int64_t i = 0; i < L; i++) {
-            gn[i] = xn[i] - xc[i];
-            G[i + (size_t)L * slot] = gn[i] - gc[i];
-        }
-        gc = gn;
+    while (k < max_iter) {
+        if (cudaMemcpyAsync(hn, dnorm, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "Anderson norm", __FILE__, __LINE__));
+        if (!(*hn > tol)) break;
+        const int mk = std::min(m, k), slot = k % m;
+        k_anderson_step<<<1, AA_STEP_THREADS, use_smem ? smem : 0, st>>>(L, mk, slot, X, G, W, b, g, S.Xin,
+                                                                          use_smem);
+        if ((rc = map())) return fail(rc);
+        k_anderson_post<<<1, AA_THREADS, 0, st>>>(L, slot, S.Xout, S.Xin, g, G, dnorm);
+        if (cudaGetLastError() != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "Anderson", __FILE__, __LINE__));
         k++;
     }
-    std::copy(xc.begin(), xc.end(), x);
+    if (cudaMemcpyAsync(x, S.Xin, sizeof(double) * L, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__));
+    cudaFree(buf);
     if (iters) *iters = k;
     return GBVLM_OK;
 }
