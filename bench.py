@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
-    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof", "nlvlm"],
+    p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof", "nlvlm", "hbvlm"],
                    help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
                         "uvlm: 20x80 rectangular wing, 500 pitch-plunge steps")
     p.add_argument("--uvlm-steps", type=int, default=500)
@@ -503,6 +503,33 @@ def run_nlvlm(args):
     print(json.dumps(out))
 
 
+def run_hbvlm(args):
+    """HBVLM 2-DOF residual solves (the served workload's third kind): section wing 45 x 1, 5 harmonics (11 time
+    instances, 495 unknowns), Anderson acceleration with history 10 on the device; six seeded requests, each
+    solved from rest.  Reports ms per solve and Anderson iterations."""
+    import torch
+    from tinyvlm_gb300 import serve as S
+    make = S.hbvlm_factory()
+    hb = make()
+    rng = np.random.default_rng(SEED)
+    reqs = [S.hbvlm_request(rng) for _ in range(6)]
+    ft = np.zeros((2, 11))
+    for om, dyn in reqs[:2]:  # warm-up
+        hb.gamma_coeffs[:] = 0.0
+        hb.run(om, dyn, ft)
+    torch.cuda.synchronize()
+    ms, its = [], []
+    for om, dyn in reqs:
+        hb.gamma_coeffs[:] = 0.0
+        t0 = time.perf_counter()
+        hb.run(om, dyn, ft)
+        torch.cuda.synchronize()
+        ms.append(1000.0 * (time.perf_counter() - t0))
+        its.append(int(hb.iterations))
+    print(json.dumps({"workload": "HBVLM 2-DOF section 45x1, H = 5, Anderson m = 10 on the device, 6 seeded requests",
+                      "ms_per_solve": ms, "median_ms": float(np.median(ms)), "anderson_iters": its}))
+
+
 def run_served(args):
     """Poisson mixed stream in equal thirds: steady VLM on trapezoids of 256-16,384 panels (log-uniform),
     single UVLM steps on a resident 20x80 wing with a 500-row (40,000-ring) wake, 2-DOF HBVLM residuals
@@ -562,6 +589,8 @@ def main():
         run_aero2dof(args)
     elif args.workload == "nlvlm":
         run_nlvlm(args)
+    elif args.workload == "hbvlm":
+        run_hbvlm(args)
     elif args.workload == "served":
         run_served(args)
     else:
