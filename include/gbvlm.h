@@ -450,6 +450,14 @@ int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, co
  * then the vertices into a HOST float (ns+1, nc+1, 4) array. */
 int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims, float* verts);
 
+/* Test hook with no counterpart in the reference: runs the batched
+ * dataflow triangular solve on an identity system of n unknowns (two to four
+ * 128-row blocks) with the first block withheld, so the second block's wait
+ * for it must run out (after 2 s).  Returns GBVLM_ERR_CUDA with the solve's
+ * timeout message when the bounded wait works; the CUDA context stays
+ * usable. */
+int gbvlm_test_flow_wait_timeout(int32_t n, gbvlm_stream stream);
+
 /* ---------------------------------------------------------------------------
  * Nonlinear VLM: NLVLM::run (vlm/include/vlm.hpp:87-115, vlm/src/vlm.cpp:
  * 153-295), the strip-wise correction of the angle of attack toward a 2D

@@ -1,0 +1,31 @@
+"""Failure path of the bounded waits: the dataflow triangular solve's wait
+for a block that never finishes runs out (2 s), the launch reports it as an
+error with its message, and the CUDA context stays usable (a batch solve
+afterwards gives the right answer).  No fault, trap or hang: the wait is a
+polled counter with a time limit."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tinyvlm_gb300 import _lib
+from tinyvlm_gb300 import mesh as M
+from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+
+pytestmark = pytest.mark.gpu
+
+
+def test_wait_runs_out_and_context_survives(cuda):
+    L = _lib.lib()
+    rc = L.gbvlm_test_flow_wait_timeout(256, None)
+    assert rc == 2, rc  # GBVLM_ERR_CUDA
+    assert b"timed out" in L.gbvlm_last_error()
+    cases = M.batch_cases(3, seed=4, n_alpha=2, nc_range=(4, 8), ns_range=(8, 16))
+    bs = BatchSolver(cases, mode="shared", refine=1)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=(0.25, 0.0, 0.0))
+    bs.run()
+    co, _ = bs.results()
+    k = 0
+    for c in cases:
+        for r in O.vlm_shared([c.verts.astype(np.float64)], c.alphas, ref_pt=(0.25, 0.0, 0.0)):
+            assert abs(co[k, 0] - float(r["cl"])) <= 1e-5 * max(abs(float(r["cl"])), 1e-3)
+            k += 1

@@ -2421,6 +2421,46 @@ void lu_solve_tables_free(void* tables) {
 
 extern "C" {
 
+int gbvlm_test_flow_wait_timeout(int32_t n, gbvlm_stream stream) {
+    GB_REQUIRE(n > FL_B && n <= 4 * FL_B, "n must span 2 to 4 blocks of %d rows", FL_B);
+    cudaStream_t st = to_cuda(stream);
+    // an identity system of n unknowns; only the forward item of its second
+    // block is handed out, so that item's wait for the first block never ends
+    float *A = nullptr, *X = nullptr;
+    int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
+    void* work = nullptr;
+    size_t work_bytes = 0;
+    TrsFlow f;
+    auto run = [&]() -> int {
+        GB_CUDA(cudaMalloc(&A, sizeof(float) * n * n));
+        GB_CUDA(cudaMalloc(&X, sizeof(float) * n));
+        GB_CUDA(cudaMalloc(&ipiv, sizeof(int32_t) * n));
+        GB_CUDA(cudaMalloc(&perm, sizeof(int32_t) * n));
+        GB_CUDA(cudaMalloc(&info, sizeof(int32_t)));
+        std::vector<float> a((size_t)n * n, 0.f);
+        std::vector<int32_t> id(n);
+        for (int32_t i = 0; i < n; i++) {
+            a[(size_t)i * n + i] = 1.f;
+            id[i] = i;
+        }
+        GB_CUDA(cudaMemcpy(A, a.data(), sizeof(float) * a.size(), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(perm, id.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemset(X, 0, sizeof(float) * n));
+        LuBatch<float> B;
+        if (int rc = make_single_batch<float>(B, n, n, A, ipiv, perm, info, X, n, 1, &work, &work_bytes, st)) return rc;
+        if (int rc = trs_flow_build(f, std::vector<int64_t>{n}, st)) return rc;
+        GB_CUDA(cudaMemsetAsync(f.d_ctl, 0, sizeof(int32_t) * 4, st));
+        k_trs_flow<<<1, FL_THREADS, FL_SMEM, st>>>(B, f.d_items + 1, 1, 1, 1, f.d_ctl, f.d_yp, 0);
+        GB_LAUNCH_CHECK();
+        return trs_flow_check(f, st);
+    };
+    const int rc = run();
+    cudaStreamSynchronize(st);
+    for (void* p : {(void*)A, (void*)X, (void*)ipiv, (void*)perm, (void*)info, work})
+        if (p) cudaFree(p);
+    return rc;
+}
+
 int gbvlm_lu_create(gbvlm_lu* out) {
     GB_REQUIRE(out != nullptr, "out is null");
     *out = new gbvlm_lu_s();
