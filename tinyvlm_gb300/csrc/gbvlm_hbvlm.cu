@@ -16,12 +16,14 @@
 // computed once per run.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
 #include <vector>
 
 #include "gbvlm_internal.h"
+#include "gbvlm_math.cuh"
 
 namespace gbvlm {
 
@@ -90,6 +92,167 @@ __global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, cons
     }
 }
 
+// ---------------------------------------------------------------------------
+// The map's wake term as a precomputed linear operator.  The wake geometry
+// (pre-generated once) and each instance's collocation points and normals do
+// not change while Anderson iterates, and the wake gamma is linear in the
+// trailing-edge Fourier coefficients te (i, c): gamma(j, i) = sum_c te(i, c)
+// basis(j, c), with basis(j, 0) = 1/sqrt(N) and cos / sin (w k (t - (j -
+// start + 1) dt)) sqrt(2/N) for harmonic k.  So the influence of instance q's
+// wake on target p is sum_{i,c} Mq(p, i, c) te(i, c) with
+//   Mq(p, i, c) = sum_j ring(p, j, i) basis_q(j, c),
+// ring(p, j, i) = 4 pi (v . n) of the unit ring (row j, span i) and its mirror.
+// The double Biot-Savart sums (the map's whole cost, and fp64 is a small
+// fraction of the fp32 rate on this part) then run once per solve instead of
+// once per map; each map reduces to the small contraction k_hb_rhs.
+// ---------------------------------------------------------------------------
+constexpr int WOP_THREADS = 128;
+constexpr int WOP_NMAX = 32;  // Fourier coefficients a thread accumulates (harmonics <= 15)
+
+struct WopInst {
+    const double* colloc[GBVLM_MAX_SURFACES];
+    const double* normals[GBVLM_MAX_SURFACES];
+    const double* rhs_vel;  // -V.n of the instance (n)
+    double* basis;          // (it x N) row-major
+    int64_t it;             // active wake rows
+    double t;               // instance time
+};
+
+struct WopArgs {
+    const WopInst* inst;
+    int32_t nsurf, N, H;
+    int64_t poff[GBVLM_MAX_SURFACES + 1];
+    const double* wake;  // lifting wake vertices, 4 planes of (ns+1) x nwv
+    int64_t wns, nwv;
+    int64_t rows_per_slice;
+    double* partial;  // [slice][instance][n * wns][N]
+};
+
+// basis_q(j, c) for the active rows of every instance (grid y: instance),
+// the same phases as k_gamma_wake in the operator library
+__global__ void k_hb_basis(WopArgs a, double omega, double dt) {
+    const WopInst& I = a.inst[blockIdx.y];
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // j - start
+    if (r >= I.it) return;
+    const int32_t U = a.N;
+    const double s0 = 1.0 / sqrt((double)U), s2 = sqrt(2.0 / (double)U);
+    double* b = I.basis + r * U;
+    b[0] = s0;
+    for (int32_t h = 0; h < a.H; h++) {
+        const double wk = omega * (double)(h + 1);
+        const double ph = wk * (I.t - (double)(r + 1) * dt);
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        b[2 * h + 1] = cs * s2;
+        b[2 * h + 2] = sn * s2;
+    }
+}
+
+// one thread per (target p, wake span i) of instance blockIdx.y over the
+// rows of slice blockIdx.z: the ring values along the rows, each line's
+// spanwise segment shared by the two rings it bounds
+__global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
+    const WopInst& I = a.inst[blockIdx.y];
+    const int64_t n = a.poff[a.nsurf], npairs = n * a.wns;
+    const int64_t g = blockIdx.x * (int64_t)WOP_THREADS + threadIdx.x;
+    if (g >= npairs) return;
+    const int64_t p = g / a.wns, i = g - p * a.wns;
+    int m = 0;
+    while (p >= a.poff[m + 1]) m++;
+    const int64_t pl = p - a.poff[m], np = a.poff[m + 1] - a.poff[m];
+    const double px = I.colloc[m][pl], py = I.colloc[m][np + pl], pz = I.colloc[m][2 * np + pl];
+    const double nx = I.normals[m][pl], ny = I.normals[m][np + pl], nz = I.normals[m][2 * np + pl];
+    const int64_t start = a.nwv - 1 - I.it;
+    const int64_t j0 = start + (int64_t)blockIdx.z * a.rows_per_slice;
+    const int64_t j1 = min(j0 + a.rows_per_slice, a.nwv - 1);
+    double acc[WOP_NMAX];
+#pragma unroll
+    for (int c = 0; c < WOP_NMAX; c++) acc[c] = 0.0;
+    if (j0 < j1) {
+        const int64_t n1 = a.wns + 1, wl = n1 * a.nwv;
+        auto V = [&](int64_t row, int64_t k) {
+            const int64_t o = k + row * n1;
+            return V3<double>{a.wake[o], a.wake[wl + o], a.wake[2 * wl + o]};
+        };
+        // line j: v0 = (j, i), v1 = (j, i + 1)
+        V3<double> v0 = V(j0, i), v1 = V(j0, i + 1);
+        Rel<double> A0 = make_rel<double>(px - v0.x, py - v0.y, pz - v0.z);
+        Rel<double> A1 = make_rel<double>(px - v1.x, py - v1.y, pz - v1.z);
+        Rel<double> B0 = make_rel<double>(px - v0.x, -py - v0.y, pz - v0.z);
+        Rel<double> B1 = make_rel<double>(px - v1.x, -py - v1.y, pz - v1.z);
+        double Ta = seg_normal<double, false>(A0, A1, v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, nx, ny, nz, 0.0);
+        double Tb = seg_normal<double, false>(B0, B1, v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, nx, -ny, nz, 0.0);
+        for (int64_t j = j0; j < j1; j++) {
+            // line j + 1: v3 = (j + 1, i), v2 = (j + 1, i + 1)
+            const V3<double> v3 = V(j + 1, i), v2 = V(j + 1, i + 1);
+            const Rel<double> A3 = make_rel<double>(px - v3.x, py - v3.y, pz - v3.z);
+            const Rel<double> A2 = make_rel<double>(px - v2.x, py - v2.y, pz - v2.z);
+            const Rel<double> B3 = make_rel<double>(px - v3.x, -py - v3.y, pz - v3.z);
+            const Rel<double> B2 = make_rel<double>(px - v2.x, -py - v2.y, pz - v2.z);
+            const double rx = v2.x - v1.x, ry = v2.y - v1.y, rz = v2.z - v1.z;  // v1 -> v2
+            const double lx = v0.x - v3.x, ly = v0.y - v3.y, lz = v0.z - v3.z;  // v3 -> v0
+            const double bx = v2.x - v3.x, by = v2.y - v3.y, bz = v2.z - v3.z;  // v3 -> v2: the next ring's top
+            const double Na = seg_normal<double, false>(A3, A2, bx, by, bz, nx, ny, nz, 0.0);
+            const double Nb = seg_normal<double, false>(B3, B2, bx, by, bz, nx, -ny, nz, 0.0);
+            double val = Ta + seg_normal<double, false>(A1, A2, rx, ry, rz, nx, ny, nz, 0.0) - Na +
+                         seg_normal<double, false>(A3, A0, lx, ly, lz, nx, ny, nz, 0.0);
+            val += Tb + seg_normal<double, false>(B1, B2, rx, ry, rz, nx, -ny, nz, 0.0) - Nb +
+                   seg_normal<double, false>(B3, B0, lx, ly, lz, nx, -ny, nz, 0.0);
+            const double* br = I.basis + (j - start) * a.N;
+#pragma unroll
+            for (int c = 0; c < WOP_NMAX; c++)
+                if (c < a.N) acc[c] += val * br[c];
+            v0 = v3, v1 = v2;
+            A0 = A3, A1 = A2, B0 = B3, B1 = B2;
+            Ta = Na, Tb = Nb;
+        }
+    }
+    double* out = a.partial + (((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * npairs + g) * a.N;
+#pragma unroll
+    for (int c = 0; c < WOP_NMAX; c++)
+        if (c < a.N) out[c] = acc[c];
+}
+
+// M = sum over slices of the partial operators, in slice order
+__global__ void k_wake_operator_sum(const double* partial, int64_t slices, int64_t len, double* M) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= len) return;
+    double s = 0;
+    for (int64_t k = 0; k < slices; k++) s += partial[k * len + e];
+    M[e] = s;
+}
+
+// One map's right-hand sides and their DFT, one block per target p:
+// R(p, q) = -V.n_q(p) - sum_{i,c} Mq(p, i, c) te(i, c) / (4 pi), with te
+// read from the iterate X (n x N) at the lifting surface's trailing-edge
+// row; then Y(p, k) = sum_q R(p, q) D(q, k).
+constexpr int HBR_THREADS = 128;
+__global__ void __launch_bounds__(HBR_THREADS) k_hb_rhs(const WopInst* inst, const double* M, const double* X,
+                                                        int64_t n, int64_t te_off, int64_t wns, int32_t N,
+                                                        const double* D, double* Y) {
+    __shared__ double R[WOP_NMAX];
+    const int64_t p = blockIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t K = wns * N;
+    const double inv4pi = 1.0 / (double)(4.0f * PI_F);
+    for (int q = wid; q < N; q += HBR_THREADS / 32) {
+        const double* mq = M + ((int64_t)q * n + p) * K;
+        double s = 0;
+        for (int64_t e = lane; e < K; e += 32) {
+            const int64_t i = e / N, c = e - i * N;
+            s += mq[e] * X[te_off + i + c * n];
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) R[q] = inst[q].rhs_vel[p] - s * inv4pi;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < N; k += HBR_THREADS) {
+        double y = 0;
+        for (int q = 0; q < N; q++) y += R[q] * D[q + (int64_t)k * N];
+        Y[p + (int64_t)k * n] = y;
+    }
+}
+
 struct Inst {
     int64_t t_steps = 0;
     double t = 0;
@@ -109,10 +272,76 @@ struct HbState {
     double *lhs = nullptr, *D = nullptr, *Xin = nullptr, *Xout = nullptr, *R = nullptr, *te = nullptr;
     gbvlm_lu lu = nullptr;
     std::vector<Inst> inst;
+    // the wake operator (k_wake_operator): instance table, basis rows,
+    // partial sums and the operators, built at the first map of a solve
+    WopInst* d_wop = nullptr;
+    double *wop_basis = nullptr, *wop_part = nullptr, *wop_M = nullptr;
+    size_t wop_part_cap = 0, wop_M_cap = 0;
+    bool wop_valid = false;
+    double wop_omega = 0, wop_dt = 0;
 
     ~HbState() {
         if (lu) gbvlm_lu_destroy(lu);
         for (void* p : allocs) cudaFree(p);
+        for (void* p : {(void*)d_wop, (void*)wop_basis, (void*)wop_part, (void*)wop_M})
+            if (p) cudaFree(p);
+    }
+
+    // the wake term through the precomputed operator unless the harmonics
+    // exceed what a thread accumulates (or GBVLM_HB_DIRECT=1 asks for the
+    // per-map Biot-Savart sums)
+    bool use_wop() const {
+        if (N > WOP_NMAX) return false;
+        const char* e = getenv("GBVLM_HB_DIRECT");
+        return !(e && e[0] == '1');
+    }
+
+    static int grow(double** p, size_t* cap, size_t cnt) {
+        if (*cap >= cnt) return GBVLM_OK;
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        *cap = 0;
+        GB_CUDA(cudaMalloc((void**)p, sizeof(double) * cnt));
+        *cap = cnt;
+        return GBVLM_OK;
+    }
+
+    // basis rows, ring values contracted with them per slice of wake rows,
+    // and the slice sums (for the map's omega and dt)
+    int build_wop(double omega, double dt, cudaStream_t st) {
+        const gbvlm_dims& W = dims[wake_surf];
+        int64_t max_it = 1;
+        for (const Inst& I : inst) max_it = std::max(max_it, I.t_steps);
+        WopArgs a;
+        a.inst = d_wop;
+        a.nsurf = nsurf;
+        a.N = N;
+        a.H = (N - 1) / 2;
+        for (int m = 0; m <= nsurf; m++) a.poff[m] = poff[m];
+        a.wake = wake[wake_surf];
+        a.wns = W.ns;
+        a.nwv = max_t;
+        const int64_t npairs = n * W.ns, xb = cdiv(npairs, WOP_THREADS);
+        // about four waves of 152 SMs, at least 32 rows per slice
+        int64_t slices = std::max<int64_t>(1, cdiv(4 * 152, xb * N));
+        const int64_t rps = std::max<int64_t>(32, cdiv(max_it, slices));
+        slices = std::max<int64_t>(1, cdiv(max_it, rps));
+        a.rows_per_slice = rps;
+        const int64_t len = (int64_t)N * npairs * N;
+        int rc;
+        if ((rc = grow(&wop_part, &wop_part_cap, (size_t)(slices * len)))) return rc;
+        if ((rc = grow(&wop_M, &wop_M_cap, (size_t)len))) return rc;
+        a.partial = wop_part;
+        k_hb_basis<<<dim3((unsigned)cdiv(max_it, 128), (unsigned)N), 128, 0, st>>>(a, omega, dt);
+        GB_LAUNCH_CHECK();
+        k_wake_operator<<<dim3((unsigned)xb, (unsigned)N, (unsigned)slices), WOP_THREADS, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+        k_wake_operator_sum<<<(unsigned)cdiv(len, 256), 256, 0, st>>>(wop_part, slices, len, wop_M);
+        GB_LAUNCH_CHECK();
+        wop_valid = true;
+        wop_omega = omega;
+        wop_dt = dt;
+        return GBVLM_OK;
     }
 
     int alloc(double** p, size_t cnt) {
@@ -207,6 +436,7 @@ struct HbState {
         }
         GB_CUDA(cudaStreamSynchronize(st));
         cudaFree(Tall);
+        wop_valid = false;
         return GBVLM_OK;
     }
 
@@ -268,6 +498,30 @@ struct HbState {
             GB_CUDA(cudaStreamSynchronize(st));
         }
         for (double* p : tdm) cudaFree(p);
+        // the operator's instance table and basis rows
+        wop_valid = false;
+        int64_t rows = 0;
+        for (const Inst& I : inst) rows += std::max<int64_t>(I.t_steps, 1);
+        if (wop_basis) cudaFree(wop_basis);
+        wop_basis = nullptr;
+        GB_CUDA(cudaMalloc((void**)&wop_basis, sizeof(double) * rows * N));
+        if (!d_wop) GB_CUDA(cudaMalloc((void**)&d_wop, sizeof(WopInst) * (2 * 64 + 1)));
+        std::vector<WopInst> tab(N);
+        int64_t off = 0;
+        for (int q = 0; q < N; q++) {
+            WopInst& w = tab[q];
+            memset(&w, 0, sizeof(w));
+            for (int m = 0; m < nsurf; m++) {
+                w.colloc[m] = inst[q].colloc[m];
+                w.normals[m] = inst[q].normals[m];
+            }
+            w.rhs_vel = inst[q].rhs_vel;
+            w.basis = wop_basis + off * N;
+            w.it = inst[q].t_steps;
+            w.t = inst[q].t;
+            off += std::max<int64_t>(inst[q].t_steps, 1);
+        }
+        GB_CUDA(cudaMemcpy(d_wop, tab.data(), sizeof(WopInst) * N, cudaMemcpyHostToDevice));
         return GBVLM_OK;
     }
 
@@ -277,6 +531,12 @@ struct HbState {
         int rc;
         const gbvlm_dims& W = dims[wake_surf];
         const int64_t te_off = poff[wake_surf] + (W.nc - 1) * W.ns;
+        if (use_wop()) {
+            if ((!wop_valid || omega != wop_omega || dt != wop_dt) && (rc = build_wop(omega, dt, st))) return rc;
+            k_hb_rhs<<<(unsigned)n, HBR_THREADS, 0, st>>>(d_wop, wop_M, Xin, n, te_off, W.ns, N, D, Xout);
+            GB_LAUNCH_CHECK();
+            return gbvlm_lu_solve_f64(lu, lhs, n, n, Xout, n, N, s);
+        }
         k_gather_te<<<(unsigned)cdiv(W.ns * N, 128), 128, 0, st>>>(Xin, n, te_off, W.ns, N, te);
         GB_LAUNCH_CHECK();
         for (int q = 0; q < N; q++) {
