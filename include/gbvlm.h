@@ -438,6 +438,29 @@ int gbvlm_hbvlm_map(gbvlm_hbvlm h, const double* x_in, double* x_out, double ome
 /* anderson_acceleration (vlm/src/vlm_solvers.cpp:6-115) of the map from x (HOST, updated in place). */
 int gbvlm_hbvlm_solve(gbvlm_hbvlm h, double* x, double omega, double dt, int32_t max_iter, double tol, int32_t m,
                       int32_t* iters, gbvlm_stream stream);
+/* K independent parameter sets on the same meshes (for instance the
+ * columns of a finite-difference Jacobian, scripts/continuation.py:192-195
+ * through scripts/finite_diff.py:26-48), solved together: the AIC factors
+ * are shared, every map of every set runs in the same launches and one
+ * solve, and each set runs its own Anderson iteration (stopping on its own
+ * test).  Per set c: max_t_steps[c] and wake_transforms[c] (max_t_steps[c]
+ * x nsurf x 16); t_steps, times, transforms, dtransforms and dft are the
+ * single-set arrays concatenated over the K sets.  The single-set calls
+ * above are these with K = 1. */
+int gbvlm_hbvlm_prepare_batch(gbvlm_hbvlm h, int32_t K, int32_t harmonics, const int64_t* max_t_steps,
+                              const double* const* wake_transforms, const int64_t* t_steps, const double* times,
+                              const double* transforms, const double* dtransforms, const double* dft,
+                              gbvlm_stream stream);
+/* x: HOST K x (n x N) column-major iterates, updated in place; omega, dt,
+ * iters: K each. */
+int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* omega, const double* dt,
+                            int32_t max_iter, double tol, int32_t m, int32_t* iters, gbvlm_stream stream);
+/* gbvlm_hbvlm_loads for K sets: every array the single-set arrays
+ * concatenated over the sets (ref_b may be NULL); out: K x 3 x N. */
+int gbvlm_hbvlm_loads_batch(gbvlm_hbvlm h, int32_t K, const double* coeffs, const double* dft, const double* ddft,
+                            const double* transforms, const double* dtransforms, const double* freestream,
+                            const double* ref_a, const double* ref_b, int32_t coupled_te, double* out,
+                            gbvlm_stream stream);
 /* Loads at N force instances (libhbvlm3.cpp:428-550): out (3 x N, row-major)
  * = CL, CM_y about ref_a (multibody), CM_y of surface 1 about ref_b (if
  * ref_b != NULL).  coupled_te: surface m's first chordwise gamma delta also

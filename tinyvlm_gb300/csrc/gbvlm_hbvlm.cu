@@ -109,31 +109,35 @@ __global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, cons
 constexpr int WOP_THREADS = 128;
 constexpr int WOP_NMAX = 32;  // Fourier coefficients a thread accumulates (harmonics <= 15)
 
+// one instance of one parameter set (column)
 struct WopInst {
     const double* colloc[GBVLM_MAX_SURFACES];
     const double* normals[GBVLM_MAX_SURFACES];
     const double* rhs_vel;  // -V.n of the instance (n)
+    const double* wake;     // the column's lifting wake vertices, 4 planes of (wns+1) x nwv
     double* basis;          // (it x N) row-major
     int64_t it;             // active wake rows
+    int64_t nwv;            // the column's wake vertex rows
+    int64_t rps;            // wake rows per slice of k_wake_operator
     double t;               // instance time
+    double omega, dt;       // the column's map parameters
 };
 
 struct WopArgs {
     const WopInst* inst;
     int32_t nsurf, N, H;
     int64_t poff[GBVLM_MAX_SURFACES + 1];
-    const double* wake;  // lifting wake vertices, 4 planes of (ns+1) x nwv
-    int64_t wns, nwv;
-    int64_t rows_per_slice;
+    int64_t wns;
     double* partial;  // [slice][instance][n * wns][N]
 };
 
 // basis_q(j, c) for the active rows of every instance (grid y: instance),
 // the same phases as k_gamma_wake in the operator library
-__global__ void k_hb_basis(WopArgs a, double omega, double dt) {
+__global__ void k_hb_basis(WopArgs a) {
     const WopInst& I = a.inst[blockIdx.y];
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // j - start
     if (r >= I.it) return;
+    const double omega = I.omega, dt = I.dt;
     const int32_t U = a.N;
     const double s0 = 1.0 / sqrt((double)U), s2 = sqrt(2.0 / (double)U);
     double* b = I.basis + r * U;
@@ -162,17 +166,17 @@ __global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
     const int64_t pl = p - a.poff[m], np = a.poff[m + 1] - a.poff[m];
     const double px = I.colloc[m][pl], py = I.colloc[m][np + pl], pz = I.colloc[m][2 * np + pl];
     const double nx = I.normals[m][pl], ny = I.normals[m][np + pl], nz = I.normals[m][2 * np + pl];
-    const int64_t start = a.nwv - 1 - I.it;
-    const int64_t j0 = start + (int64_t)blockIdx.z * a.rows_per_slice;
-    const int64_t j1 = min(j0 + a.rows_per_slice, a.nwv - 1);
+    const int64_t start = I.nwv - 1 - I.it;
+    const int64_t j0 = start + (int64_t)blockIdx.z * I.rps;
+    const int64_t j1 = min(j0 + I.rps, I.nwv - 1);
     double acc[WOP_NMAX];
 #pragma unroll
     for (int c = 0; c < WOP_NMAX; c++) acc[c] = 0.0;
     if (j0 < j1) {
-        const int64_t n1 = a.wns + 1, wl = n1 * a.nwv;
+        const int64_t n1 = a.wns + 1, wl = n1 * I.nwv;
         auto V = [&](int64_t row, int64_t k) {
             const int64_t o = k + row * n1;
-            return V3<double>{a.wake[o], a.wake[wl + o], a.wake[2 * wl + o]};
+            return V3<double>{I.wake[o], I.wake[wl + o], I.wake[2 * wl + o]};
         };
         // line j: v0 = (j, i), v1 = (j, i + 1)
         V3<double> v0 = V(j0, i), v1 = V(j0, i + 1);
@@ -222,16 +226,21 @@ __global__ void k_wake_operator_sum(const double* partial, int64_t slices, int64
     M[e] = s;
 }
 
-// One map's right-hand sides and their DFT, one block per target p:
-// R(p, q) = -V.n_q(p) - sum_{i,c} Mq(p, i, c) te(i, c) / (4 pi), with te
-// read from the iterate X (n x N) at the lifting surface's trailing-edge
-// row; then Y(p, k) = sum_q R(p, q) D(q, k).
+// One map's right-hand sides and their DFT, one block per target p and
+// column blockIdx.y: R(p, q) = -V.n_q(p) - sum_{i,c} Mq(p, i, c) te(i, c) /
+// (4 pi), with te read from the column's iterate X (n x N) at the lifting
+// surface's trailing-edge row; then Y(p, k) = sum_q R(p, q) D(q, k).
 constexpr int HBR_THREADS = 128;
 __global__ void __launch_bounds__(HBR_THREADS) k_hb_rhs(const WopInst* inst, const double* M, const double* X,
                                                         int64_t n, int64_t te_off, int64_t wns, int32_t N,
                                                         const double* D, double* Y) {
     __shared__ double R[WOP_NMAX];
-    const int64_t p = blockIdx.x;
+    const int64_t p = blockIdx.x, col = blockIdx.y;
+    inst += col * N;
+    M += col * (int64_t)N * n * wns * N;
+    X += col * n * N;
+    D += col * (int64_t)N * N;
+    Y += col * n * N;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t K = wns * N;
     const double inv4pi = 1.0 / (double)(4.0f * PI_F);
@@ -253,95 +262,71 @@ __global__ void __launch_bounds__(HBR_THREADS) k_hb_rhs(const WopInst* inst, con
     }
 }
 
+// device buffer of doubles, grown on demand
+struct DBuf {
+    double* p = nullptr;
+    size_t cap = 0;
+    int grow(size_t cnt) {
+        cnt = std::max<size_t>(cnt, 1);
+        if (cap >= cnt) return GBVLM_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        GB_CUDA(cudaMalloc((void**)&p, sizeof(double) * cnt));
+        cap = cnt;
+        return GBVLM_OK;
+    }
+    ~DBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+// one time instance of one column; pointers into the batch buffers
 struct Inst {
     int64_t t_steps = 0;
     double t = 0;
-    std::vector<double*> colloc, normals;
+    std::vector<double*> colloc, normals, gwake;
     double* rhs_vel = nullptr;
-    std::vector<double*> gwake;
+};
+
+// one parameter set (for instance a finite-difference Jacobian column):
+// its wake, its instances and its map parameters
+struct HbCol {
+    int64_t max_t = 0;
+    std::vector<gbvlm_dims> dims;  // nwv = max_t
+    std::vector<double*> wake;     // per surface; only the lifting surface's is built
+    std::vector<Inst> inst;        // N
 };
 
 struct HbState {
-    int32_t nsurf = 0, wake_surf = 0, N = 0;
+    int32_t nsurf = 0, wake_surf = 0, N = 0, K = 0;
     std::vector<gbvlm_dims> dims;
     std::vector<int32_t> lifting;
-    int64_t n = 0, max_t = 0;
+    int64_t n = 0;
     std::vector<int64_t> poff;
     std::vector<void*> allocs;
-    std::vector<double*> vinit, verts, wake, colloc_h, colloc, normals, areas, vel, forces, gdelta, gdt, gam, trans;
-    double *lhs = nullptr, *D = nullptr, *Xin = nullptr, *Xout = nullptr, *R = nullptr, *te = nullptr;
+    std::vector<double*> vinit, verts, colloc_h, colloc, normals, areas, vel, forces, gdelta, gdt, gam, trans;
+    double* lhs = nullptr;
     gbvlm_lu lu = nullptr;
-    std::vector<Inst> inst;
-    // the wake operator (k_wake_operator): instance table, basis rows,
-    // partial sums and the operators, built at the first map of a solve
+    bool aic_ready = false;
+    std::vector<HbCol> cols;
+    // batch buffers: per instance colloc, normals (3n each) and -V.n (n);
+    // the lifting wake's gammas for the per-map sums; wakes; transforms and
+    // rates of every instance; iterate, map output and right-hand sides
+    // (K x n x N); DFT matrices (K x N x N); trailing-edge coefficients
+    DBuf inst_buf, gwake_buf, wake_buf, tw_buf, tdev, tddev, Xin, Xout, R, D, te;
+    // the wake operator (k_wake_operator): instance table (host copy and
+    // device), basis rows, partial sums and the operators
+    std::vector<WopInst> wtab;
     WopInst* d_wop = nullptr;
-    double *wop_basis = nullptr, *wop_part = nullptr, *wop_M = nullptr;
-    size_t wop_part_cap = 0, wop_M_cap = 0;
+    size_t d_wop_cap = 0;
+    DBuf wop_basis, wop_part, wop_M;
     bool wop_valid = false;
-    double wop_omega = 0, wop_dt = 0;
 
     ~HbState() {
         if (lu) gbvlm_lu_destroy(lu);
         for (void* p : allocs) cudaFree(p);
-        for (void* p : {(void*)d_wop, (void*)wop_basis, (void*)wop_part, (void*)wop_M})
-            if (p) cudaFree(p);
-    }
-
-    // the wake term through the precomputed operator unless the harmonics
-    // exceed what a thread accumulates (or GBVLM_HB_DIRECT=1 asks for the
-    // per-map Biot-Savart sums)
-    bool use_wop() const {
-        if (N > WOP_NMAX) return false;
-        const char* e = getenv("GBVLM_HB_DIRECT");
-        return !(e && e[0] == '1');
-    }
-
-    static int grow(double** p, size_t* cap, size_t cnt) {
-        if (*cap >= cnt) return GBVLM_OK;
-        if (*p) cudaFree(*p);
-        *p = nullptr;
-        *cap = 0;
-        GB_CUDA(cudaMalloc((void**)p, sizeof(double) * cnt));
-        *cap = cnt;
-        return GBVLM_OK;
-    }
-
-    // basis rows, ring values contracted with them per slice of wake rows,
-    // and the slice sums (for the map's omega and dt)
-    int build_wop(double omega, double dt, cudaStream_t st) {
-        const gbvlm_dims& W = dims[wake_surf];
-        int64_t max_it = 1;
-        for (const Inst& I : inst) max_it = std::max(max_it, I.t_steps);
-        WopArgs a;
-        a.inst = d_wop;
-        a.nsurf = nsurf;
-        a.N = N;
-        a.H = (N - 1) / 2;
-        for (int m = 0; m <= nsurf; m++) a.poff[m] = poff[m];
-        a.wake = wake[wake_surf];
-        a.wns = W.ns;
-        a.nwv = max_t;
-        const int64_t npairs = n * W.ns, xb = cdiv(npairs, WOP_THREADS);
-        // about four waves of 152 SMs, at least 32 rows per slice
-        int64_t slices = std::max<int64_t>(1, cdiv(4 * 152, xb * N));
-        const int64_t rps = std::max<int64_t>(32, cdiv(max_it, slices));
-        slices = std::max<int64_t>(1, cdiv(max_it, rps));
-        a.rows_per_slice = rps;
-        const int64_t len = (int64_t)N * npairs * N;
-        int rc;
-        if ((rc = grow(&wop_part, &wop_part_cap, (size_t)(slices * len)))) return rc;
-        if ((rc = grow(&wop_M, &wop_M_cap, (size_t)len))) return rc;
-        a.partial = wop_part;
-        k_hb_basis<<<dim3((unsigned)cdiv(max_it, 128), (unsigned)N), 128, 0, st>>>(a, omega, dt);
-        GB_LAUNCH_CHECK();
-        k_wake_operator<<<dim3((unsigned)xb, (unsigned)N, (unsigned)slices), WOP_THREADS, 0, st>>>(a);
-        GB_LAUNCH_CHECK();
-        k_wake_operator_sum<<<(unsigned)cdiv(len, 256), 256, 0, st>>>(wop_part, slices, len, wop_M);
-        GB_LAUNCH_CHECK();
-        wop_valid = true;
-        wop_omega = omega;
-        wop_dt = dt;
-        return GBVLM_OK;
+        if (d_wop) cudaFree(d_wop);
     }
 
     int alloc(double** p, size_t cnt) {
@@ -398,21 +383,13 @@ struct HbState {
                                        (gbvlm_stream)st);
     }
 
-    // libhbvlm3.cpp:266-319: metrics at the undisplaced pose, AIC without wake, factor, wake pre-generation
-    int prepare(int32_t harmonics, int64_t max_t_steps, const double* wake_T, cudaStream_t st) {
+    // libhbvlm3.cpp:266-300: metrics at the undisplaced pose, the AIC
+    // without wake and its factors.  The meshes are fixed once created, so
+    // this runs at the first prepare only.
+    int aic(cudaStream_t st) {
+        if (aic_ready) return GBVLM_OK;
         gbvlm_stream s = (gbvlm_stream)st;
-        N = 2 * harmonics + 1;
-        max_t = max_t_steps;
         int rc;
-        for (auto& d : dims) d.nwv = max_t;
-        for (double* p : wake) cudaFree(p);
-        wake.clear();
-        for (int m = 0; m < nsurf; m++) {
-            double* p;
-            GB_CUDA(cudaMalloc((void**)&p, sizeof(double) * 4 * (dims[m].ns + 1) * max_t));
-            GB_CUDA(cudaMemset(p, 0, sizeof(double) * 4 * (dims[m].ns + 1) * max_t));
-            wake.push_back(p);
-        }
         for (int m = 0; m < nsurf; m++) {
             const int64_t nv = (dims[m].ns + 1) * (dims[m].nc + 1);
             GB_CUDA(cudaMemcpyAsync(verts[m], vinit[m], sizeof(double) * 4 * nv, cudaMemcpyDeviceToDevice, st));
@@ -425,135 +402,233 @@ struct HbState {
                                          C(verts).data(), nullptr, 0, 0.0, s)))
             return rc;
         if ((rc = gbvlm_lu_factor_f64(lu, lhs, n, n, s))) return rc;
-        double* Tall = nullptr;
-        GB_CUDA(cudaMalloc((void**)&Tall, sizeof(double) * 16 * nsurf * max_t));
-        GB_CUDA(cudaMemcpyAsync(Tall, wake_T, sizeof(double) * 16 * nsurf * max_t, cudaMemcpyHostToDevice, st));
-        for (int m = 0; m < nsurf; m++) {
-            const int64_t cnt = (dims[m].ns + 1) * max_t;
-            k_pregen_wake<<<(unsigned)cdiv(cnt, 128), 128, 0, st>>>(Tall, nsurf, m, vinit[m], dims[m].ns, dims[m].nc,
-                                                                     max_t, wake[m]);
+        aic_ready = true;
+        return GBVLM_OK;
+    }
+
+    // K parameter sets (libhbvlm3.cpp:307-319 and 363-393 without the gamma
+    // part, per set): the lifting wake pre-generated over max_t[c] steps,
+    // then per instance the displaced geometry and -V.n.  Nothing here
+    // synchronises per instance: every transform is uploaded once.
+    int prepare(int32_t K_, int32_t harmonics, const int64_t* max_t, const double* const* wake_T,
+                const int64_t* t_steps, const double* times, const double* Th, const double* Tdh, const double* dft,
+                cudaStream_t st) {
+        gbvlm_stream s = (gbvlm_stream)st;
+        int rc;
+        if ((rc = aic(st))) return rc;
+        K = K_;
+        N = 2 * harmonics + 1;
+        wop_valid = false;
+        const gbvlm_dims& W = dims[wake_surf];
+        const int64_t wn1 = W.ns + 1;
+        cols.assign(K, HbCol());
+        int64_t wake_tot = 0, tw_tot = 0, gw_tot = 0;
+        for (int c = 0; c < K; c++) {
+            GB_REQUIRE(max_t[c] >= 2, "column %d: max_t_steps %lld < 2", c, (long long)max_t[c]);
+            GB_REQUIRE(wake_T[c] != nullptr, "column %d: wake transforms are null", c);
+            wake_tot += 4 * wn1 * max_t[c];
+            tw_tot += 16 * nsurf * max_t[c];
+            gw_tot += (int64_t)N * W.ns * (max_t[c] - 1);
+        }
+        const int64_t ninst = (int64_t)K * N;
+        if ((rc = wake_buf.grow(wake_tot)) || (rc = tw_buf.grow(tw_tot)) || (rc = gwake_buf.grow(gw_tot)) ||
+            (rc = inst_buf.grow(ninst * 7 * n)) || (rc = tdev.grow(ninst * nsurf * 16)) ||
+            (rc = tddev.grow(ninst * nsurf * 16)) || (rc = D.grow(ninst * N)) || (rc = Xin.grow(ninst * n)) ||
+            (rc = Xout.grow(ninst * n)) || (rc = R.grow(ninst * n)) || (rc = te.grow(ninst * W.ns)))
+            return rc;
+        // wakes (only the lifting surface's: the others shed none)
+        int64_t wo = 0, two = 0;
+        for (int c = 0; c < K; c++) {
+            HbCol& col = cols[c];
+            col.max_t = max_t[c];
+            col.dims = dims;
+            for (auto& d : col.dims) d.nwv = col.max_t;
+            col.wake.assign(nsurf, nullptr);
+            col.wake[wake_surf] = wake_buf.p + wo;
+            double* Tall = tw_buf.p + two;
+            GB_CUDA(cudaMemcpyAsync(Tall, wake_T[c], sizeof(double) * 16 * nsurf * col.max_t, cudaMemcpyHostToDevice,
+                                    st));
+            const int64_t cnt = wn1 * col.max_t;
+            k_pregen_wake<<<(unsigned)cdiv(cnt, 128), 128, 0, st>>>(Tall, nsurf, wake_surf, vinit[wake_surf], W.ns,
+                                                                     W.nc, col.max_t, col.wake[wake_surf]);
             GB_LAUNCH_CHECK();
+            wo += 4 * wn1 * col.max_t;
+            two += 16 * nsurf * col.max_t;
         }
-        GB_CUDA(cudaStreamSynchronize(st));
-        cudaFree(Tall);
-        wop_valid = false;
-        return GBVLM_OK;
-    }
-
-    // per-instance geometry, -V.n and wake-gamma buffers (libhbvlm3.cpp:363-393 without the gamma part)
-    int set_instances(const int64_t* t_steps, const double* times, const double* Th, const double* Tdh,
-                      const double* dft, cudaStream_t st) {
-        gbvlm_stream s = (gbvlm_stream)st;
-        int rc;
-        for (auto& I : inst) {
-            for (double* p : I.colloc) cudaFree(p);
-            for (double* p : I.normals) cudaFree(p);
-            for (double* p : I.gwake) cudaFree(p);
-            if (I.rhs_vel) cudaFree(I.rhs_vel);
-        }
-        inst.assign(N, Inst());
-        if (!D && (rc = alloc(&D, N * N))) return rc;
-        if (!Xin) {
-            if ((rc = alloc(&Xin, n * N)) || (rc = alloc(&Xout, n * N)) || (rc = alloc(&R, n * N)) ||
-                (rc = alloc(&te, dims[wake_surf].ns * N)))
-                return rc;
-        }
-        GB_CUDA(cudaMemcpy(D, dft, sizeof(double) * N * N, cudaMemcpyHostToDevice));
-        std::vector<double*> tdm(nsurf);
-        for (int m = 0; m < nsurf; m++) {
-            GB_CUDA(cudaMalloc((void**)&tdm[m], sizeof(double) * 16));
-        }
-        for (int q = 0; q < N; q++) {
-            Inst& I = inst[q];
-            I.t_steps = t_steps[q];
-            I.t = times[q];
-            GB_REQUIRE(I.t_steps >= 0 && I.t_steps <= max_t - 1, "instance %d: t_steps %lld outside the wake", q,
-                       (long long)I.t_steps);
-            if ((rc = place(Th + 16 * nsurf * q, st))) return rc;
-            for (int m = 0; m < nsurf; m++) {
-                const int64_t np = dims[m].ns * dims[m].nc;
-                double *c, *nm, *gw;
-                GB_CUDA(cudaMalloc((void**)&c, sizeof(double) * 3 * np));
-                GB_CUDA(cudaMalloc((void**)&nm, sizeof(double) * 3 * np));
-                GB_CUDA(cudaMalloc((void**)&gw, sizeof(double) * dims[m].ns * (max_t - 1)));
-                GB_CUDA(cudaMemset(gw, 0, sizeof(double) * dims[m].ns * (max_t - 1)));
-                I.colloc.push_back(c);
-                I.normals.push_back(nm);
-                I.gwake.push_back(gw);
+        // instances
+        GB_CUDA(cudaMemcpyAsync(tdev.p, Th, sizeof(double) * ninst * nsurf * 16, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(tddev.p, Tdh, sizeof(double) * ninst * nsurf * 16, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(D.p, dft, sizeof(double) * ninst * N, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemsetAsync(inst_buf.p, 0, sizeof(double) * ninst * 7 * n, st));
+        GB_CUDA(cudaMemsetAsync(gwake_buf.p, 0, sizeof(double) * std::max<int64_t>(gw_tot, 1), st));
+        std::vector<const double*> tp(nsurf);
+        int64_t gwo = 0;
+        for (int c = 0; c < K; c++) {
+            HbCol& col = cols[c];
+            col.inst.assign(N, Inst());
+            for (int q = 0; q < N; q++) {
+                const int64_t e = (int64_t)c * N + q;
+                Inst& I = col.inst[q];
+                I.t_steps = t_steps[e];
+                I.t = times[e];
+                GB_REQUIRE(I.t_steps >= 0 && I.t_steps <= col.max_t - 1,
+                           "column %d instance %d: t_steps %lld outside the wake", c, q, (long long)I.t_steps);
+                double* base = inst_buf.p + e * 7 * n;
+                I.colloc.resize(nsurf);
+                I.normals.resize(nsurf);
+                I.gwake.assign(nsurf, nullptr);
+                for (int m = 0; m < nsurf; m++) {
+                    I.colloc[m] = base + 3 * poff[m];
+                    I.normals[m] = base + 3 * n + 3 * poff[m];
+                    tp[m] = tdev.p + 16 * (e * nsurf + m);
+                }
+                I.rhs_vel = base + 6 * n;
+                I.gwake[wake_surf] = gwake_buf.p + gwo;
+                gwo += W.ns * (col.max_t - 1);
+                if ((rc = gbvlm_displace_wing_f64(nsurf, dims.data(), tp.data(), verts.data(), C(vinit).data(), s)))
+                    return rc;
+                if ((rc = gbvlm_mesh_metrics_f64(0.0, nsurf, dims.data(), C(verts).data(), I.colloc.data(),
+                                                 I.normals.data(), areas.data(), s)))
+                    return rc;
+                for (int m = 0; m < nsurf; m++) {
+                    const int64_t np = dims[m].ns * dims[m].nc;
+                    k_vel_dual<double><<<(unsigned)cdiv(np, 128), 128, 0, st>>>(tddev.p + 16 * (e * nsurf + m),
+                                                                                 colloc_h[m], vel[m], np);
+                    GB_LAUNCH_CHECK();
+                }
+                if ((rc = gbvlm_rhs_assemble_velocities_f64(I.rhs_vel, nsurf, dims.data(), C(I.normals).data(),
+                                                            C(vel).data(), s)))
+                    return rc;
             }
-            if ((rc = gbvlm_mesh_metrics_f64(0.0, nsurf, dims.data(), C(verts).data(), I.colloc.data(),
-                                             I.normals.data(), areas.data(), s)))
-                return rc;
-            for (int m = 0; m < nsurf; m++) {
-                const int64_t np = dims[m].ns * dims[m].nc;
-                GB_CUDA(cudaMemcpyAsync(tdm[m], Tdh + 16 * (nsurf * q + m), sizeof(double) * 16, cudaMemcpyHostToDevice, st));
-                k_vel_dual<double><<<(unsigned)cdiv(np, 128), 128, 0, st>>>(tdm[m], colloc_h[m], vel[m], np);
-                GB_LAUNCH_CHECK();
-            }
-            GB_CUDA(cudaMalloc((void**)&I.rhs_vel, sizeof(double) * n));
-            GB_CUDA(cudaMemsetAsync(I.rhs_vel, 0, sizeof(double) * n, st));
-            if ((rc = gbvlm_rhs_assemble_velocities_f64(I.rhs_vel, nsurf, dims.data(), C(I.normals).data(),
-                                                        C(vel).data(), s)))
-                return rc;
-            GB_CUDA(cudaStreamSynchronize(st));
         }
-        for (double* p : tdm) cudaFree(p);
         // the operator's instance table and basis rows
-        wop_valid = false;
         int64_t rows = 0;
-        for (const Inst& I : inst) rows += std::max<int64_t>(I.t_steps, 1);
-        if (wop_basis) cudaFree(wop_basis);
-        wop_basis = nullptr;
-        GB_CUDA(cudaMalloc((void**)&wop_basis, sizeof(double) * rows * N));
-        if (!d_wop) GB_CUDA(cudaMalloc((void**)&d_wop, sizeof(WopInst) * (2 * 64 + 1)));
-        std::vector<WopInst> tab(N);
-        int64_t off = 0;
-        for (int q = 0; q < N; q++) {
-            WopInst& w = tab[q];
-            memset(&w, 0, sizeof(w));
-            for (int m = 0; m < nsurf; m++) {
-                w.colloc[m] = inst[q].colloc[m];
-                w.normals[m] = inst[q].normals[m];
-            }
-            w.rhs_vel = inst[q].rhs_vel;
-            w.basis = wop_basis + off * N;
-            w.it = inst[q].t_steps;
-            w.t = inst[q].t;
-            off += std::max<int64_t>(inst[q].t_steps, 1);
+        for (const HbCol& col : cols)
+            for (const Inst& I : col.inst) rows += std::max<int64_t>(I.t_steps, 1);
+        if ((rc = wop_basis.grow(rows * N))) return rc;
+        if (d_wop_cap < (size_t)ninst) {
+            if (d_wop) cudaFree(d_wop);
+            d_wop = nullptr;
+            d_wop_cap = 0;
+            GB_CUDA(cudaMalloc((void**)&d_wop, sizeof(WopInst) * ninst));
+            d_wop_cap = ninst;
         }
-        GB_CUDA(cudaMemcpy(d_wop, tab.data(), sizeof(WopInst) * N, cudaMemcpyHostToDevice));
+        wtab.assign(ninst, WopInst());
+        int64_t off = 0;
+        for (int c = 0; c < K; c++)
+            for (int q = 0; q < N; q++) {
+                const Inst& I = cols[c].inst[q];
+                WopInst& w = wtab[(int64_t)c * N + q];
+                memset(&w, 0, sizeof(w));
+                for (int m = 0; m < nsurf; m++) {
+                    w.colloc[m] = I.colloc[m];
+                    w.normals[m] = I.normals[m];
+                }
+                w.rhs_vel = I.rhs_vel;
+                w.wake = cols[c].wake[wake_surf];
+                w.basis = wop_basis.p + off * N;
+                w.it = I.t_steps;
+                w.nwv = cols[c].max_t;
+                w.t = I.t;
+                off += std::max<int64_t>(I.t_steps, 1);
+            }
+        GB_CUDA(cudaStreamSynchronize(st));
         return GBVLM_OK;
     }
 
-    // one fixed-point map on device buffers Xin -> Xout (libhbvlm3.cpp:349-410)
-    int map_dev(double omega, double dt, int32_t harmonics, cudaStream_t st) {
+    // the wake term through the precomputed operator unless the harmonics
+    // exceed what a thread accumulates (or GBVLM_HB_DIRECT=1 asks for the
+    // per-map Biot-Savart sums)
+    bool use_wop() const {
+        if (N > WOP_NMAX) return false;
+        const char* e = getenv("GBVLM_HB_DIRECT");
+        return !(e && e[0] == '1');
+    }
+
+    // basis rows, ring values contracted with them per slice of wake rows,
+    // and the slice sums, for every instance of every column (each with its
+    // column's omega and dt)
+    int build_wop(const double* omega, const double* dt, cudaStream_t st) {
+        const gbvlm_dims& W = dims[wake_surf];
+        const int64_t ninst = (int64_t)K * N;
+        const int64_t npairs = n * W.ns, xb = cdiv(npairs, WOP_THREADS);
+        // each instance's rows in about four waves' worth of slices of one
+        // instance (at least 32 rows each): its partial sums, and so its
+        // result, do not depend on the other sets of the batch
+        const int64_t slices = std::max<int64_t>(1, cdiv(4 * 152, xb));
+        int64_t max_it = 1;
+        for (int64_t e = 0; e < ninst; e++) {
+            wtab[e].omega = omega[e / N];
+            wtab[e].dt = dt[e / N];
+            wtab[e].rps = std::max<int64_t>(32, cdiv(wtab[e].it, slices));
+            max_it = std::max(max_it, wtab[e].it);
+        }
+        const int64_t zs = std::min(slices, cdiv(max_it, 32));
+        GB_CUDA(cudaMemcpyAsync(d_wop, wtab.data(), sizeof(WopInst) * ninst, cudaMemcpyHostToDevice, st));
+        WopArgs a;
+        a.inst = d_wop;
+        a.nsurf = nsurf;
+        a.N = N;
+        a.H = (N - 1) / 2;
+        for (int m = 0; m <= nsurf; m++) a.poff[m] = poff[m];
+        a.wns = W.ns;
+        const int64_t len = ninst * npairs * N;
+        int rc;
+        if ((rc = wop_part.grow((size_t)(zs * len))) || (rc = wop_M.grow((size_t)len))) return rc;
+        a.partial = wop_part.p;
+        k_hb_basis<<<dim3((unsigned)cdiv(max_it, 128), (unsigned)ninst), 128, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+        k_wake_operator<<<dim3((unsigned)xb, (unsigned)ninst, (unsigned)zs), WOP_THREADS, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+        k_wake_operator_sum<<<(unsigned)cdiv(len, 256), 256, 0, st>>>(wop_part.p, zs, len, wop_M.p);
+        GB_LAUNCH_CHECK();
+        wop_valid = true;
+        return GBVLM_OK;
+    }
+
+    // one fixed-point map of every column on device buffers Xin -> Xout
+    // (libhbvlm3.cpp:349-410); omega and dt per column
+    int map_dev(const double* omega, const double* dt, cudaStream_t st) {
         gbvlm_stream s = (gbvlm_stream)st;
         int rc;
+        const int32_t harmonics = (N - 1) / 2;
         const gbvlm_dims& W = dims[wake_surf];
         const int64_t te_off = poff[wake_surf] + (W.nc - 1) * W.ns;
         if (use_wop()) {
-            if ((!wop_valid || omega != wop_omega || dt != wop_dt) && (rc = build_wop(omega, dt, st))) return rc;
-            k_hb_rhs<<<(unsigned)n, HBR_THREADS, 0, st>>>(d_wop, wop_M, Xin, n, te_off, W.ns, N, D, Xout);
+            bool same = wop_valid;
+            for (int c = 0; c < K && same; c++)
+                same = wtab[(int64_t)c * N].omega == omega[c] && wtab[(int64_t)c * N].dt == dt[c];
+            if (!same && (rc = build_wop(omega, dt, st))) return rc;
+            k_hb_rhs<<<dim3((unsigned)n, (unsigned)K), HBR_THREADS, 0, st>>>(d_wop, wop_M.p, Xin.p, n, te_off, W.ns,
+                                                                             N, D.p, Xout.p);
             GB_LAUNCH_CHECK();
-            return gbvlm_lu_solve_f64(lu, lhs, n, n, Xout, n, N, s);
+        } else {
+            for (int c = 0; c < K; c++) {
+                HbCol& col = cols[c];
+                const double* Xc = Xin.p + (int64_t)c * n * N;
+                double* tec = te.p + (int64_t)c * W.ns * N;
+                double* Rc = R.p + (int64_t)c * n * N;
+                k_gather_te<<<(unsigned)cdiv(W.ns * N, 128), 128, 0, st>>>(Xc, n, te_off, W.ns, N, tec);
+                GB_LAUNCH_CHECK();
+                for (int q = 0; q < N; q++) {
+                    Inst& I = col.inst[q];
+                    if ((rc = gbvlm_gamma_wake_from_coeffs_f64(I.gwake[wake_surf], W.ns, col.max_t - 1, tec,
+                                                                harmonics, I.t, omega[c], dt[c], I.t_steps, s)))
+                        return rc;
+                    double* rcol = Rc + (int64_t)q * n;
+                    GB_CUDA(cudaMemcpyAsync(rcol, I.rhs_vel, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+                    if ((rc = gbvlm_rhs_assemble_wake_influence_f64(rcol, nsurf, col.dims.data(), C(I.gwake).data(),
+                                                                    C(I.colloc).data(), C(I.normals).data(),
+                                                                    C(col.wake).data(), lifting.data(),
+                                                                    (int32_t)I.t_steps, 0.0, s)))
+                        return rc;
+                }
+                k_rdft<<<(unsigned)cdiv(n * N, 128), 128, 0, st>>>(Rc, D.p + (int64_t)c * N * N, n, N,
+                                                                   Xout.p + (int64_t)c * n * N);
+                GB_LAUNCH_CHECK();
+            }
         }
-        k_gather_te<<<(unsigned)cdiv(W.ns * N, 128), 128, 0, st>>>(Xin, n, te_off, W.ns, N, te);
-        GB_LAUNCH_CHECK();
-        for (int q = 0; q < N; q++) {
-            Inst& I = inst[q];
-            if ((rc = gbvlm_gamma_wake_from_coeffs_f64(I.gwake[wake_surf], W.ns, max_t - 1, te, harmonics, I.t, omega,
-                                                        dt, I.t_steps, s)))
-                return rc;
-            double* col = R + (int64_t)q * n;
-            GB_CUDA(cudaMemcpyAsync(col, I.rhs_vel, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-            if ((rc = gbvlm_rhs_assemble_wake_influence_f64(col, nsurf, dims.data(), C(I.gwake).data(),
-                                                            C(I.colloc).data(), C(I.normals).data(), C(wake).data(),
-                                                            lifting.data(), (int32_t)I.t_steps, 0.0, s)))
-                return rc;
-        }
-        k_rdft<<<(unsigned)cdiv(n * N, 128), 128, 0, st>>>(R, D, n, N, Xout);
-        GB_LAUNCH_CHECK();
-        return gbvlm_lu_solve_f64(lu, lhs, n, n, Xout, n, N, s);
+        return gbvlm_lu_solve_f64(lu, lhs, n, n, Xout.p, n, (int64_t)K * N, s);
     }
 };
 
@@ -596,12 +671,30 @@ __device__ __forceinline__ double aa_wsum(double v) {
 // work is spread over all four schedulers' fp64 units.
 constexpr int AA_STEP_THREADS = 256;
 
-__global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, int mk, int slot, double* X,
-                                                                   const double* G, double* Wg, double* bg,
-                                                                   const double* g, double* x, int use_smem) {
+// Per column c = blockIdx.x (its state at buf + c * stride: g (L), the
+// histories X and G (L x m each), the QR work copy W (L x m) and its
+// right-hand side b (L)); columns with act[c] == 0 are left as they are.
+struct AaCol {
+    double *g, *X, *G, *W, *b;
+};
+__device__ __forceinline__ AaCol aa_col(double* buf, int64_t L, int m) {
+    double* g = buf + (int64_t)blockIdx.x * L * (3 * m + 2);
+    return AaCol{g, g + L, g + L + L * m, g + L + 2 * L * m, g + L + 3 * L * m};
+}
+
+__global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, int m, int mk, int slot, double* buf,
+                                                                   double* xall, const int* act, int use_smem) {
+    if (!act[blockIdx.x]) return;
     extern __shared__ double aa_sm[];
     __shared__ double gam[16], diag[16];
     __shared__ double s_nrm, s_rvv;
+    const AaCol cs = aa_col(buf, L, m);
+    double* X = cs.X;
+    const double* G = cs.G;
+    const double* g = cs.g;
+    double* x = xall + (int64_t)blockIdx.x * L;
+    double* Wg = cs.W;
+    double* bg = cs.b;
     double* W = use_smem ? aa_sm : Wg;
     double* b = use_smem ? aa_sm + L * mk : bg;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
@@ -665,9 +758,16 @@ __global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, in
 
 // after a map: g_new = f(x) - x; G[:, slot] = g_new - g (slot < 0: none);
 // g = g_new; *norm = |g|
-__global__ void __launch_bounds__(AA_THREADS) k_anderson_post(int64_t L, int slot, const double* fx, const double* x,
-                                                              double* g, double* G, double* norm) {
+__global__ void __launch_bounds__(AA_THREADS) k_anderson_post(int64_t L, int m, int slot, const double* fxall,
+                                                              const double* xall, double* buf, double* norm,
+                                                              const int* act) {
+    if (!act[blockIdx.x]) return;
     __shared__ double sh[32];
+    const AaCol cs = aa_col(buf, L, m);
+    double* g = cs.g;
+    double* G = cs.G;
+    const double* fx = fxall + (int64_t)blockIdx.x * L;
+    const double* x = xall + (int64_t)blockIdx.x * L;
     double t = 0;
     for (int64_t i = threadIdx.x; i < L; i += blockDim.x) {
         const double gn = fx[i] - x[i];
@@ -676,15 +776,44 @@ __global__ void __launch_bounds__(AA_THREADS) k_anderson_post(int64_t L, int slo
         t += gn * gn;
     }
     const double s2 = aa_sum(t, sh);
-    if (threadIdx.x == 0) *norm = sqrt(s2);
+    if (threadIdx.x == 0) norm[blockIdx.x] = sqrt(s2);
 }
 
-// the first step (vlm_solvers.cpp:49-66): X[:, 0] = g, x = f(x)
-__global__ void k_anderson_first(int64_t L, const double* fx, double* x, const double* g, double* X) {
+// the first step (vlm_solvers.cpp:49-66): X[:, 0] = g, x = f(x); grid y: column
+__global__ void k_anderson_first(int64_t L, int m, const double* fxall, double* xall, double* buf) {
+    const int64_t c = blockIdx.y;
+    const double* g = buf + c * L * (3 * m + 2);
+    double* X = const_cast<double*>(g) + L;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L; i += (int64_t)gridDim.x * blockDim.x) {
         X[i] = g[i];
-        x[i] = fx[i];
+        xall[c * L + i] = fxall[c * L + i];
     }
+}
+
+// the loop's test (vlm_solvers.cpp:68-70) per column: a column whose
+// residual norm is no longer above tol stops at iteration k; ctl[0] = the
+// number still iterating
+__global__ void k_anderson_check(int K, const double* norm, double tol, int k, int* act, int* iters, int* ctl) {
+    int live = 0;
+    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+        if (act[c] && !(norm[c] > tol)) {
+            act[c] = 0;
+            iters[c] = k;
+        }
+        live += act[c];
+    }
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if (threadIdx.x == 0) ctl[0] = live;
+}
+
+// columns still iterating after max_iter steps report max_iter
+__global__ void k_anderson_finish(int K, int k, const int* act, int* iters) {
+    for (int c = threadIdx.x; c < K; c += blockDim.x)
+        if (act[c]) iters[c] = k;
+}
+
+__global__ void k_fill_i32(int* p, int n, int v) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
 }
 
 }  // namespace gbvlm
@@ -719,58 +848,83 @@ int gbvlm_hbvlm_destroy(gbvlm_hbvlm h) {
 int gbvlm_hbvlm_prepare(gbvlm_hbvlm h, int32_t harmonics, int64_t max_t_steps, const double* wake_transforms,
                         const int64_t* t_steps, const double* times, const double* transforms,
                         const double* dtransforms, const double* dft, gbvlm_stream stream) {
-    GB_REQUIRE(h && wake_transforms && t_steps && times && transforms && dtransforms && dft, "null argument");
-    GB_REQUIRE(harmonics >= 0 && harmonics <= 64 && max_t_steps >= 2, "bad sizes");
-    int rc = h->st.prepare(harmonics, max_t_steps, wake_transforms, to_cuda(stream));
-    if (rc) return rc;
-    return h->st.set_instances(t_steps, times, transforms, dtransforms, dft, to_cuda(stream));
+    return gbvlm_hbvlm_prepare_batch(h, 1, harmonics, &max_t_steps, &wake_transforms, t_steps, times, transforms,
+                                     dtransforms, dft, stream);
+}
+
+int gbvlm_hbvlm_prepare_batch(gbvlm_hbvlm h, int32_t K, int32_t harmonics, const int64_t* max_t_steps,
+                              const double* const* wake_transforms, const int64_t* t_steps, const double* times,
+                              const double* transforms, const double* dtransforms, const double* dft,
+                              gbvlm_stream stream) {
+    GB_REQUIRE(h && max_t_steps && wake_transforms && t_steps && times && transforms && dtransforms && dft,
+               "null argument");
+    GB_REQUIRE(harmonics >= 0 && harmonics <= 64, "harmonics %d outside [0, 64]", harmonics);
+    GB_REQUIRE(K >= 1 && (int64_t)K * (2 * harmonics + 1) <= 65535, "K=%d: K (2H+1) must be in [1, 65535]", K);
+    return h->st.prepare(K, harmonics, max_t_steps, wake_transforms, t_steps, times, transforms, dtransforms, dft,
+                         to_cuda(stream));
 }
 
 int gbvlm_hbvlm_map(gbvlm_hbvlm h, const double* x_in, double* x_out, double omega, double dt, gbvlm_stream stream) {
     GB_REQUIRE(h && x_in && x_out && h->st.N > 0, "map before prepare");
     HbState& S = h->st;
+    GB_REQUIRE(S.K == 1, "map needs a single parameter set (prepared K=%d)", S.K);
     cudaStream_t st = to_cuda(stream);
-    GB_CUDA(cudaMemcpyAsync(S.Xin, x_in, sizeof(double) * S.n * S.N, cudaMemcpyHostToDevice, st));
-    int rc = S.map_dev(omega, dt, (S.N - 1) / 2, st);
+    GB_CUDA(cudaMemcpyAsync(S.Xin.p, x_in, sizeof(double) * S.n * S.N, cudaMemcpyHostToDevice, st));
+    int rc = S.map_dev(&omega, &dt, st);
     if (rc) return rc;
-    GB_CUDA(cudaMemcpyAsync(x_out, S.Xout, sizeof(double) * S.n * S.N, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(x_out, S.Xout.p, sizeof(double) * S.n * S.N, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     return GBVLM_OK;
 }
 
 int gbvlm_hbvlm_solve(gbvlm_hbvlm h, double* x, double omega, double dt, int32_t max_iter, double tol, int32_t m,
                       int32_t* iters, gbvlm_stream stream) {
-    GB_REQUIRE(h && x && h->st.N > 0, "solve before prepare");
+    GB_REQUIRE(h && h->st.K == 1, "solve needs a single parameter set");
+    return gbvlm_hbvlm_solve_batch(h, 1, x, &omega, &dt, max_iter, tol, m, iters, stream);
+}
+
+int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* omega, const double* dt,
+                            int32_t max_iter, double tol, int32_t m, int32_t* iters, gbvlm_stream stream) {
+    GB_REQUIRE(h && x && omega && dt && h->st.N > 0, "solve before prepare");
+    GB_REQUIRE(K == h->st.K, "K=%d differs from the prepared %d parameter sets", K, h->st.K);
     GB_REQUIRE(m >= 1 && m <= 16 && max_iter >= 2, "history m in [1, 16], max_iter >= 2");
     HbState& S = h->st;
     cudaStream_t st = to_cuda(stream);
     const int64_t L = S.n * S.N;
-    const int32_t H = (S.N - 1) / 2;
-    // device state: the iterate lives in the map's input S.Xin; g, the
-    // histories X and G, the QR work copy of G and its right-hand side
+    // device state: the iterates live in the map's input S.Xin; per column
+    // g, the histories X and G, the QR work copy of G and its right-hand
+    // side; then the residual norms and the loop's flags
+    const size_t per = (size_t)L * (3 * m + 2);
     double* buf = nullptr;
-    GB_CUDA(cudaMalloc((void**)&buf, sizeof(double) * ((size_t)L * (3 * m + 2) + 1)));
-    double *g = buf, *X = g + L, *G = X + (size_t)L * m, *W = G + (size_t)L * m, *b = W + (size_t)L * m,
-           *dnorm = b + L;
-    double* hn = (double*)host_scratch(sizeof(double));
+    GB_CUDA(cudaMalloc((void**)&buf, sizeof(double) * (per * K + K) + sizeof(int) * (2 * K + 1)));
+    double* dnorm = buf + per * K;
+    int* act = (int*)(dnorm + K);
+    int* d_iters = act + K;
+    int* ctl = d_iters + K;
+    int* hctl = (int*)host_scratch(sizeof(int));
     int rc = GBVLM_OK;
     auto fail = [&](int r) {
         cudaFree(buf);
         return r;
     };
-    auto map = [&]() { return S.map_dev(omega, dt, H, st); };  // S.Xin -> S.Xout
+    auto check = [&](const char* what) {
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? GBVLM_OK : cuda_fail(e, what, __FILE__, __LINE__);
+    };
+    auto map = [&]() { return S.map_dev(omega, dt, st); };  // S.Xin -> S.Xout, every column
     const unsigned g1 = (unsigned)std::min<int64_t>(cdiv(L, 256), 1024);
-    if (cudaMemcpyAsync(S.Xin, x, sizeof(double) * L, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return fail(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__));
-    if (cudaMemsetAsync(X, 0, sizeof(double) * (size_t)L * m * 2, st) != cudaSuccess)
-        return fail(cuda_fail(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__));
+    if (cudaMemcpyAsync(S.Xin.p, x, sizeof(double) * L * K, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(buf, 0, sizeof(double) * per * K, st) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "Anderson setup", __FILE__, __LINE__));
+    k_fill_i32<<<1, 256, 0, st>>>(act, K, 1);
+    k_fill_i32<<<1, 256, 0, st>>>(d_iters, K, 0);
     // vlm_solvers.cpp:49-66: g0 = f(x0) - x0; X0 = g0; x1 = f(x0); g1 = f(x1) - x1; G0 = g1 - g0
     if ((rc = map())) return fail(rc);
-    k_anderson_post<<<1, AA_THREADS, 0, st>>>(L, -1, S.Xout, S.Xin, g, G, dnorm);
-    k_anderson_first<<<g1, 256, 0, st>>>(L, S.Xout, S.Xin, g, X);
-    if ((rc = map())) return fail(rc);
-    k_anderson_post<<<1, AA_THREADS, 0, st>>>(L, 0, S.Xout, S.Xin, g, G, dnorm);
-    if (cudaGetLastError() != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "Anderson", __FILE__, __LINE__));
+    k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, -1, S.Xout.p, S.Xin.p, buf, dnorm, act);
+    k_anderson_first<<<dim3(g1, K), 256, 0, st>>>(L, m, S.Xout.p, S.Xin.p, buf);
+    if ((rc = check("Anderson")) || (rc = map())) return fail(rc);
+    k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, 0, S.Xout.p, S.Xin.p, buf, dnorm, act);
+    if ((rc = check("Anderson"))) return fail(rc);
     // the QR's columns in shared memory when m of them and g fit
     const size_t smem = sizeof(double) * (size_t)L * (m + 1);
     const int use_smem = smem <= 200 * 1024 ? 1 : 0;
@@ -779,24 +933,28 @@ int gbvlm_hbvlm_solve(gbvlm_hbvlm h, double* x, double omega, double dt, int32_t
         return fail(cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__));
     int k = 1;
     while (k < max_iter) {
-        if (cudaMemcpyAsync(hn, dnorm, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        k_anderson_check<<<1, 32, 0, st>>>(K, dnorm, tol, k, act, d_iters, ctl);
+        if (cudaMemcpyAsync(hctl, ctl, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
             return fail(cuda_fail(cudaGetLastError(), "Anderson norm", __FILE__, __LINE__));
-        if (!(*hn > tol)) break;
+        if (*hctl == 0) break;
         const int mk = std::min(m, k), slot = k % m;
-        k_anderson_step<<<1, AA_STEP_THREADS, use_smem ? smem : 0, st>>>(L, mk, slot, X, G, W, b, g, S.Xin,
+        k_anderson_step<<<K, AA_STEP_THREADS, use_smem ? smem : 0, st>>>(L, m, mk, slot, buf, S.Xin.p, act,
                                                                           use_smem);
-        if ((rc = map())) return fail(rc);
-        k_anderson_post<<<1, AA_THREADS, 0, st>>>(L, slot, S.Xout, S.Xin, g, G, dnorm);
-        if (cudaGetLastError() != cudaSuccess)
-            return fail(cuda_fail(cudaGetLastError(), "Anderson", __FILE__, __LINE__));
+        if ((rc = check("Anderson")) || (rc = map())) return fail(rc);
+        k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, slot, S.Xout.p, S.Xin.p, buf, dnorm, act);
+        if ((rc = check("Anderson"))) return fail(rc);
         k++;
     }
-    if (cudaMemcpyAsync(x, S.Xin, sizeof(double) * L, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+    k_anderson_finish<<<1, 256, 0, st>>>(K, k, act, d_iters);
+    std::vector<int> hit(K);
+    if (cudaMemcpyAsync(x, S.Xin.p, sizeof(double) * L * K, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(hit.data(), d_iters, sizeof(int) * K, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return fail(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__));
     cudaFree(buf);
-    if (iters) *iters = k;
+    if (iters)
+        for (int c = 0; c < K; c++) iters[c] = hit[c];
     return GBVLM_OK;
 }
 
@@ -881,6 +1039,23 @@ int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, co
     cudaFree(gfull);
     cudaFree(dgfull);
     return rc;
+}
+
+int gbvlm_hbvlm_loads_batch(gbvlm_hbvlm h, int32_t K, const double* coeffs, const double* dft, const double* ddft,
+                            const double* transforms, const double* dtransforms, const double* freestream,
+                            const double* ref_a, const double* ref_b, int32_t coupled_te, double* out,
+                            gbvlm_stream stream) {
+    GB_REQUIRE(h && coeffs && dft && ddft && transforms && dtransforms && freestream && ref_a && out, "null argument");
+    const HbState& S = h->st;
+    GB_REQUIRE(K >= 1 && S.N > 0, "loads before prepare");
+    const int64_t N = S.N, ln = S.n * N, lt = N * S.nsurf * 16;
+    for (int32_t c = 0; c < K; c++) {
+        int rc = gbvlm_hbvlm_loads(h, coeffs + c * ln, dft + c * N * N, ddft + c * N * N, transforms + c * lt,
+                                   dtransforms + c * lt, freestream + c * N * 3, ref_a + c * N * 3,
+                                   ref_b ? ref_b + c * N * 3 : nullptr, coupled_te, out + c * 3 * N, stream);
+        if (rc) return rc;
+    }
+    return GBVLM_OK;
 }
 
 }  // extern "C"

@@ -106,6 +106,45 @@ class HBEngine:
              ctypes.cast(ctypes.pointer(it), P), None)
         return it.value
 
+    def prepare_batch(self, harmonics, max_ts, wake_Ts, t_steps, times, T, Td, dfts):
+        """K parameter sets: per-set wake arrays (lists), the rest stacked over the sets."""
+        K = len(max_ts)
+        wk = [np.ascontiguousarray(w, np.float64) for w in wake_Ts]
+        keep = wk + [np.ascontiguousarray(np.asarray(max_ts, np.int64)),
+                     np.ascontiguousarray(np.asarray(t_steps, np.int64)),
+                     np.ascontiguousarray(np.asarray(times, np.float64)),
+                     np.ascontiguousarray(np.asarray(T, np.float64)), np.ascontiguousarray(np.asarray(Td, np.float64)),
+                     np.ascontiguousarray(np.stack([self._colmajor(d) for d in dfts]))]
+        self._keep = keep
+        mt, ts, tm, T_, Td_, D_ = keep[K:]
+        wp = (ctypes.c_void_p * K)(*[w.ctypes.data for w in wk])
+        call("gbvlm_hbvlm_prepare_batch", self.h, K, int(harmonics), self._p(mt), ctypes.cast(wp, PP), self._p(ts),
+             self._p(tm), self._p(T_), self._p(Td_), self._p(D_), None)
+
+    def solve_batch(self, xs, omegas, dts, max_iter, tol, m):
+        """xs: (K, n, N) iterates, updated in place (C-contiguous over sets, each set column-major)."""
+        K = xs.shape[0]
+        buf = np.ascontiguousarray(np.transpose(xs, (0, 2, 1)))  # (K, N, n): each set n x N column-major
+        om = np.ascontiguousarray(omegas, np.float64)
+        dt = np.ascontiguousarray(dts, np.float64)
+        its = np.zeros(K, np.int32)
+        call("gbvlm_hbvlm_solve_batch", self.h, K, self._p(buf), self._p(om), self._p(dt), int(max_iter), float(tol),
+             int(m), self._p(its), None)
+        xs[:] = np.transpose(buf, (0, 2, 1))
+        return its
+
+    def loads_batch(self, xs, dfts, ddfts, T, Td, fs, ref_a, ref_b, coupled_te, N):
+        K = xs.shape[0]
+        out = np.zeros((K, 3, N))
+        keep = [np.ascontiguousarray(np.transpose(xs, (0, 2, 1))),
+                np.ascontiguousarray(np.stack([self._colmajor(d) for d in dfts])),
+                np.ascontiguousarray(np.stack([self._colmajor(d) for d in ddfts]))] + \
+               [np.ascontiguousarray(a, np.float64) for a in (T, Td, fs, ref_a)]
+        rb = np.ascontiguousarray(ref_b, np.float64) if ref_b is not None else None
+        call("gbvlm_hbvlm_loads_batch", self.h, K, *[self._p(a) for a in keep],
+             self._p(rb) if rb is not None else None, 1 if coupled_te else 0, self._p(out), None)
+        return out
+
     def loads(self, x, dft, ddft, T, Td, fs, ref_a, ref_b, coupled_te, N):
         out = np.zeros(3 * N)
         keep = [np.asfortranarray(x, np.float64), self._colmajor(dft), self._colmajor(ddft)] + \
@@ -194,6 +233,52 @@ class _HBVLMBase:
         return forces_t
 
 
+    def _run_batch(self, t_starts, omegas, assemblies, refs, forces_list, coupled_te):
+        """Every parameter set starts from the current coefficients; afterwards
+        they hold the last set's fixed point, as after the same runs in sequence."""
+        N, H = self.m_coeffs, self.m_harmonics
+        chord = last_panel_chord(self.verts[self.dt_surface])
+        K = len(omegas)
+        cols = []
+        for t_start, omega, asm in zip(t_starts, omegas, assemblies):
+            period = TWO_PI_F / omega
+            interval = period / N
+            if not interval > chord:
+                raise AssertionError("period interval %g must exceed the last panel chord %g" % (interval, chord))
+            dt = interval / math.ceil(interval / chord)
+            max_t = int((t_start + period + dt) / dt)
+            wake_T, inst, finst = hb_arrays(asm, N, dt, max_t, t_start, period)
+            dft, ddft = dft_matrices(N, omega, period)
+            _, da = asm.kinematics().transform_series(finst[1])
+            fs = -da[:, :3, 3]
+            v0, _ = asm.surface_kinematics()[0].transform_series(finst[1])
+            ref_a = (v0 @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
+            ref_b = None
+            if len(refs) > 1:
+                v1, _ = asm.surface_kinematics()[1].transform_series(finst[1])
+                ref_b = (v1 @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
+            cols.append(dict(dt=dt, max_t=max_t, wake_T=wake_T, inst=inst, finst=finst, dft=dft, ddft=ddft, fs=fs,
+                             ref_a=ref_a, ref_b=ref_b))
+        self.engine.prepare_batch(H, [c["max_t"] for c in cols], [c["wake_T"] for c in cols],
+                                  np.concatenate([c["inst"][0] for c in cols]),
+                                  np.concatenate([c["inst"][1] for c in cols]),
+                                  np.concatenate([c["inst"][2] for c in cols]),
+                                  np.concatenate([c["inst"][3] for c in cols]), [c["dft"] for c in cols])
+        xs = np.repeat(self.gamma_coeffs[None], K, axis=0)
+        self.iterations = self.engine.solve_batch(xs, omegas, [c["dt"] for c in cols], 100, self.tol, 10)
+        ref_b = np.concatenate([c["ref_b"] for c in cols]) if len(refs) > 1 else None
+        out = self.engine.loads_batch(xs, [c["dft"] for c in cols], [c["ddft"] for c in cols],
+                                      np.concatenate([c["finst"][2] for c in cols]),
+                                      np.concatenate([c["finst"][3] for c in cols]),
+                                      np.concatenate([c["fs"] for c in cols]), np.concatenate([c["ref_a"] for c in cols]),
+                                      ref_b, coupled_te, N)
+        for f, o in zip(forces_list, out):
+            f[:, :] = o[:f.shape[0], :]
+        self.gamma_coeffs[:] = xs[-1]
+        self._last_batch = cols
+        return forces_list
+
+
 class HBVLM3(_HBVLMBase):
     """libhbvlm3.HBVLM: wing (non-lifting) + flap (lifting), 3-DOF pitch/heave/flap."""
     qc = False
@@ -225,6 +310,12 @@ class HBVLM3(_HBVLMBase):
         asm = self.assembly(omega, U, dyn_f)
         return self._run(t_final, omega, asm, (1.0 + self.VARS["a"], 1.0 + self.VARS["c"]), forces_t, True)
 
+    def run_batch(self, omegas, Us, dyn_fs, forces_list):
+        """``run`` for K parameter sets solved together (one device solve)."""
+        asms = [self.assembly(om, U, d) for om, U, d in zip(omegas, Us, dyn_fs)]
+        return self._run_batch([2.0 * TWO_PI_F / om for om in omegas], list(omegas), asms,
+                               (1.0 + self.VARS["a"], 1.0 + self.VARS["c"]), forces_list, True)
+
 
 class HBVLM2(_HBVLMBase):
     """libhbvlm.HBVLM: one lifting surface, 2-DOF heave/pitch (lib/libhbvlm.cpp:470-515)."""
@@ -251,3 +342,9 @@ class HBVLM2(_HBVLMBase):
         t_final = 3.0 * TWO_PI_F / omega
         asm = self.assembly(omega, dyn_f)
         return self._run(t_final, omega, asm, (0.5,), forces_t, False)
+
+    def run_batch(self, omegas, dyn_fs, forces_list):
+        """``run`` for K parameter sets solved together (one device solve)."""
+        asms = [self.assembly(om, d) for om, d in zip(omegas, dyn_fs)]
+        return self._run_batch([3.0 * TWO_PI_F / om for om in omegas], list(omegas), asms, (0.5,), forces_list,
+                               False)
