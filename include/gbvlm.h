@@ -463,7 +463,7 @@ int gbvlm_hbvlm_loads_batch(gbvlm_hbvlm h, int32_t K, const double* coeffs, cons
                             gbvlm_stream stream);
 /* Loads at N force instances (libhbvlm3.cpp:428-550): out (3 x N, row-major)
  * = CL, CM_y about ref_a (multibody), CM_y of surface 1 about ref_b (if
- * ref_b != NULL).  coupled_te: surface m's first chordwise gamma delta also
+ * ref_b != NULL, else 0).  coupled_te: surface m's first chordwise gamma delta also
  * subtracts surface m-1's trailing-edge gamma (wing + flap). */
 int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, const double* ddft,
                       const double* transforms, const double* dtransforms, const double* freestream,

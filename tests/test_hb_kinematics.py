@@ -1,0 +1,52 @@
+"""The closed-form kinematics of the HBVLM modules against the kinematics
+tree (Dual evaluation of the chain the modules build, libhbvlm3.cpp:559-641
+and libhbvlm.cpp:470-515), for several parameter sets."""
+import numpy as np
+
+from tinyvlm_gb300 import hbvlm as HB
+
+
+def _sets(rng, K, H, nd, with_U):
+    sets = []
+    for _ in range(K):
+        d = rng.uniform(-0.05, 0.05, (nd, 2 * H + 1))
+        S = dict(omega=float(rng.uniform(0.3, 1.2)), dyn=d)
+        if with_U:
+            S["U"] = float(rng.uniform(5.0, 12.0))
+        sets.append(S)
+    return sets
+
+
+def _check(obj, sets, tree_nodes):
+    rng = np.random.default_rng(1)
+    times = [np.sort(rng.uniform(0.0, 40.0, 37 + 5 * k)) for k in range(len(sets))]
+    worst = 0.0
+    for k, S in enumerate(sets):
+        series = obj._series(S, times[k])
+        sl = slice(0, times[k].size)
+        for m, node in enumerate(tree_nodes(S)):
+            v, g = node.transform_series(times[k])
+            worst = max(worst, np.abs(series[m][0][sl] - v).max(), np.abs(series[m][1][sl] - g).max())
+            np.testing.assert_allclose(series[m][0][sl], v, rtol=0, atol=1e-14)
+            np.testing.assert_allclose(series[m][1][sl], g, rtol=0, atol=1e-13)
+    return worst
+
+
+def test_hbvlm2_chain():
+    obj = HB.HBVLM2.__new__(HB.HBVLM2)
+    obj.m_harmonics = 3
+    sets = _sets(np.random.default_rng(0), 4, 3, 2, False)
+    w = _check(obj, sets, lambda S: obj.assembly(S["omega"], S["dyn"]).surface_kinematics())
+    print("max difference", w)
+
+
+def test_hbvlm3_chain_wing_and_flap():
+    obj = HB.HBVLM3.__new__(HB.HBVLM3)
+    obj.m_harmonics = 2
+    sets = _sets(np.random.default_rng(2), 3, 2, 3, True)
+    w = _check(obj, sets, lambda S: obj.assembly(S["omega"], S["U"], S["dyn"]).surface_kinematics())
+    print("max difference", w)
+    # the free stream rate the loads use
+    S = sets[0]
+    _, da = obj.assembly(S["omega"], S["U"], S["dyn"]).kinematics().transform_series(np.array([0.0, 1.0]))
+    np.testing.assert_array_equal(-da[:, 0, 3], obj._sigma(S))

@@ -44,27 +44,6 @@ __global__ void k_rdft(const double* R, const double* D, int64_t n, int32_t N, d
     Y[g] = s;
 }
 
-// g = C . row_s(D) : g[p] = sum_j C[p + j n] D[s + j N]
-__global__ void k_dft_row(const double* C, const double* D, int64_t n, int32_t N, int32_t s, double* g) {
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    double v = 0;
-    for (int32_t j = 0; j < N; j++) v += C[p + j * n] * D[s + j * N];
-    g[p] = v;
-}
-
-// chordwise delta of one surface; with `prev_te` the first chordwise row
-// also loses the previous surface's trailing-edge gamma (libhbvlm3.cpp:476-480)
-__global__ void k_delta(const double* g, int64_t ns, int64_t nc, const double* prev_te, double* d) {
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= ns * nc) return;
-    const int64_t i = p % ns, j = p / ns;
-    double v = g[p];
-    if (j > 0) v -= g[p - ns];
-    else if (prev_te) v -= prev_te[i];
-    d[p] = v;
-}
-
 template <class T>
 __global__ void k_vel_dual(const double* Td, const double* c0, double* vel, int64_t np) {
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -262,6 +241,146 @@ __global__ void __launch_bounds__(HBR_THREADS) k_hb_rhs(const WopInst* inst, con
     }
 }
 
+// ---------------------------------------------------------------------------
+// Loads at the force instances (libhbvlm3.cpp:428-550) for every instance of
+// every parameter set in one launch, one 512-thread block per (set,
+// instance).  Per panel, as the operator library's kernels compute it: the
+// displaced vertices (k_displace), normal and area (k_mesh_metrics), the
+// circulation and its rate from the Fourier coefficients (one DFT row), the
+// chordwise gamma delta (the wing's trailing edge subtracted from the flap's
+// first row when coupled), -(dT/dt) at the undisplaced collocation point, and
+// the unsteady Joukowski force (k_forces).  The sums per surface (area, CL,
+// the mean aerodynamic chord and CM_y about each reference point) are
+// compensated and strided over the block exactly as k_reduce sums them, and
+// combined over the surfaces as the host does for one instance.
+// ---------------------------------------------------------------------------
+constexpr int HBL_THREADS = 512;
+
+struct LoadsArgs {
+    int32_t nsurf, N, coupled;
+    int64_t n;
+    int64_t ns[GBVLM_MAX_SURFACES], nc[GBVLM_MAX_SURFACES], poff[GBVLM_MAX_SURFACES + 1];
+    const double* vinit[GBVLM_MAX_SURFACES];
+    const double* colloc_h[GBVLM_MAX_SURFACES];
+    const double *C, *D, *DD, *T, *Td, *fs, *ref_a, *ref_b;
+    double* out;  // per set 3 x N
+};
+
+__device__ __forceinline__ double hbl_block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double r = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) r += sh[k];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(HBL_THREADS) k_hb_loads(LoadsArgs a) {
+    __shared__ double sh[32];
+    const int64_t e = blockIdx.x, c = e / a.N, q = e - c * a.N;
+    const int N = a.N, tid = threadIdx.x;
+    const double* Cc = a.C + c * a.n * N;
+    const double* Dr = a.D + c * (int64_t)N * N + q;   // row q: Dr[j * N]
+    const double* DDr = a.DD + c * (int64_t)N * N + q;
+    const double* fs = a.fs + 3 * e;
+    auto gam = [&](const double* row, int64_t p) {
+        double v = 0;
+        for (int j = 0; j < N; j++) v += Cc[p + (int64_t)j * a.n] * row[(int64_t)j * N];
+        return v;
+    };
+    double la[3] = {-fs[2], 0.0, fs[0]};
+    const double ll = sqrt(la[0] * la[0] + la[2] * la[2]);
+    la[0] /= ll;
+    la[2] /= ll;
+    const double v2 = fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2];
+    const double* ra = a.ref_a + 3 * e;
+    const double* rb = a.ref_b ? a.ref_b + 3 * e : nullptr;
+    double cl = 0, ta = 0, tm = 0, cm = 0, cmb_out = 0;
+    for (int m = 0; m < a.nsurf; m++) {
+        const int64_t ns = a.ns[m], nc = a.nc[m], np = ns * nc, nv = (ns + 1) * (nc + 1), po = a.poff[m];
+        const double* vin = a.vinit[m];
+        const double* tr = a.T + 16 * (e * a.nsurf + m);
+        const double* td = a.Td + 16 * (e * a.nsurf + m);
+        auto vert = [&](int64_t r) {
+            const double x[4] = {vin[r], vin[nv + r], vin[2 * nv + r], vin[3 * nv + r]};
+            double o[3];
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                double acc = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc += x[k] * tr[cc + 4 * k];
+                o[cc] = acc;
+            }
+            return V3<double>{o[0], o[1], o[2]};
+        };
+        const bool prev = a.coupled && m > 0 && a.ns[m - 1] == ns;
+        const bool with_b = m == 1 && rb != nullptr;
+        CSum s_area, s_cl, s_cm, s_cmb, s_mac0, s_mac1;
+        for (int64_t p = tid; p < np; p += HBL_THREADS) {
+            const int64_t i = p % ns, j = p / ns;
+            const int64_t ia = i + j * (ns + 1), ib = ia + 1, ic = ib + (ns + 1), id = ia + (ns + 1);
+            const V3<double> v0 = vert(ia), v1 = vert(ib), v2p = vert(ic), v3 = vert(id);
+            const V3<double> nn = cross(v3 - v1, v2p - v0);
+            const double l = sqrt(len2(nn));
+            const V3<double> nor{nn.x / l, nn.y / l, nn.z / l};
+            const V3<double> f = v3 - v0, bb = v2p - v0, ee = v1 - v0;
+            const double ar = 0.5 * (sqrt(len2(cross(f, bb))) + sqrt(len2(cross(bb, ee))));
+            const double gp = gam(Dr, po + p);
+            double gd = gp;
+            if (j > 0) gd -= gam(Dr, po + p - ns);
+            else if (prev) gd -= gam(Dr, po - ns + i);
+            const double dg = gam(DDr, po + p);
+            const double* ch = a.colloc_h[m];
+            const double x = ch[p], y = ch[np + p], z = ch[2 * np + p];
+            double vel[3];
+            for (int r = 0; r < 3; r++) vel[r] = -(td[r] * x + td[r + 4] * y + td[r + 8] * z + td[r + 12]);
+            const V3<double> V{vel[0], vel[1], vel[2]};
+            V3<double> F = (1.0 * gd) * cross(V, v1 - v0);
+            F = F + (1.0 * dg * ar) * nor;
+            s_area.add(ar);
+            s_mac1.add(ar);
+            s_cl.add(F.x * la[0] + F.y * la[1] + F.z * la[2]);
+            const double lx = 0.5 * (v0.x + v1.x) - ra[0], lz = 0.5 * (v0.z + v1.z) - ra[2];
+            s_cm.add(lz * F.x - lx * F.z);
+            if (with_b) {
+                const double bx = 0.5 * (v0.x + v1.x) - rb[0], bz = 0.5 * (v0.z + v1.z) - rb[2];
+                s_cmb.add(bz * F.x - bx * F.z);
+            }
+        }
+        const int64_t last = nc * (ns + 1);
+        for (int64_t i = tid; i < ns; i += HBL_THREADS) {
+            const V3<double> l0 = vert(i), l1 = vert(i + 1), t0 = vert(last + i), t1 = vert(last + i + 1);
+            const V3<double> d0 = l0 - t0, d1 = l1 - t1, d3 = l1 - l0;
+            const double c0 = sqrt(len2(d0)), c1 = sqrt(len2(d1));
+            s_mac0.add(0.5 * (c0 * c0 + c1 * c1) * sqrt(len2(d3)));
+        }
+        const double area = hbl_block_sum(s_area.value(), sh);
+        const double rcl = hbl_block_sum(s_cl.value(), sh);
+        const double mac0 = hbl_block_sum(s_mac0.value(), sh), mac1 = hbl_block_sum(s_mac1.value(), sh);
+        const double rcm = hbl_block_sum(s_cm.value(), sh);
+        const double rcmb = with_b ? hbl_block_sum(s_cmb.value(), sh) : 0.0;
+        if (tid == 0) {
+            const double clm = rcl / (0.5 * 1.0 * v2 * area);
+            const double mac = mac0 / mac1;
+            const double d = 0.5 * 1.0 * v2 * area * mac;
+            cl += clm * area;
+            ta += area;
+            tm += mac;
+            cm += (rcm / d) * area * mac;
+            if (with_b) cmb_out = rcmb / d;
+        }
+    }
+    if (tid == 0) {
+        double* o = a.out + c * 3 * N;
+        o[q] = cl / ta;
+        o[N + q] = cm / (ta * tm);
+        o[2 * N + q] = cmb_out;
+    }
+}
+
 // device buffer of doubles, grown on demand
 struct DBuf {
     double* p = nullptr;
@@ -305,7 +424,7 @@ struct HbState {
     int64_t n = 0;
     std::vector<int64_t> poff;
     std::vector<void*> allocs;
-    std::vector<double*> vinit, verts, colloc_h, colloc, normals, areas, vel, forces, gdelta, gdt, gam, trans;
+    std::vector<double*> vinit, verts, colloc_h, normals, areas, vel;
     double* lhs = nullptr;
     gbvlm_lu lu = nullptr;
     bool aic_ready = false;
@@ -322,6 +441,8 @@ struct HbState {
     size_t d_wop_cap = 0;
     DBuf wop_basis, wop_part, wop_M;
     bool wop_valid = false;
+    // inputs and outputs of k_hb_loads
+    DBuf ld_C, ld_D, ld_DD, ld_T, ld_Td, ld_fs, ld_ra, ld_rb, ld_out;
 
     ~HbState() {
         if (lu) gbvlm_lu_destroy(lu);
@@ -359,28 +480,17 @@ struct HbState {
             GB_CUDA(cudaMemcpy(p, vh[m], sizeof(double) * 4 * nv, cudaMemcpyHostToDevice));
             if ((rc = alloc(&p, 4 * nv))) return rc;
             verts.push_back(p);
-            for (auto* vec : {&colloc_h, &colloc, &normals, &vel, &forces}) {
+            for (auto* vec : {&colloc_h, &normals, &vel}) {
                 if ((rc = alloc(&p, 3 * np))) return rc;
                 vec->push_back(p);
             }
-            for (auto* vec : {&areas, &gdelta, &gdt, &gam}) {
-                if ((rc = alloc(&p, np))) return rc;
-                vec->push_back(p);
-            }
-            if ((rc = alloc(&p, 16))) return rc;
-            trans.push_back(p);
+            if ((rc = alloc(&p, np))) return rc;
+            areas.push_back(p);
         }
         n = poff[nsurf];
         if ((rc = alloc(&lhs, n * n))) return rc;
         if ((rc = gbvlm_lu_create(&lu))) return rc;
         return gbvlm_lu_init(lu, n);
-    }
-
-    int place(const double* Th, cudaStream_t st) {
-        for (int m = 0; m < nsurf; m++)
-            GB_CUDA(cudaMemcpyAsync(trans[m], Th + 16 * m, sizeof(double) * 16, cudaMemcpyHostToDevice, st));
-        return gbvlm_displace_wing_f64(nsurf, dims.data(), C(trans).data(), verts.data(), C(vinit).data(),
-                                       (gbvlm_stream)st);
     }
 
     // libhbvlm3.cpp:266-300: metrics at the undisplaced pose, the AIC
@@ -965,80 +1075,8 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
 int gbvlm_hbvlm_loads(gbvlm_hbvlm h, const double* coeffs, const double* dft, const double* ddft,
                       const double* transforms, const double* dtransforms, const double* freestream,
                       const double* ref_a, const double* ref_b, int32_t coupled_te, double* out, gbvlm_stream stream) {
-    GB_REQUIRE(h && coeffs && dft && ddft && transforms && dtransforms && freestream && ref_a && out, "null argument");
-    HbState& S = h->st;
-    cudaStream_t st = to_cuda(stream);
-    gbvlm_stream s = stream;
-    const int N = S.N, ns = S.nsurf;
-    int rc = GBVLM_OK;
-    double *C, *Dd, *DDd, *td;
-    GB_CUDA(cudaMalloc((void**)&C, sizeof(double) * S.n * N));
-    GB_CUDA(cudaMalloc((void**)&Dd, sizeof(double) * N * N));
-    GB_CUDA(cudaMalloc((void**)&DDd, sizeof(double) * N * N));
-    GB_CUDA(cudaMalloc((void**)&td, sizeof(double) * 16 * ns));
-    GB_CUDA(cudaMemcpy(C, coeffs, sizeof(double) * S.n * N, cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(Dd, dft, sizeof(double) * N * N, cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(DDd, ddft, sizeof(double) * N * N, cudaMemcpyHostToDevice));
-    double* gfull;
-    double* dgfull;
-    GB_CUDA(cudaMalloc((void**)&gfull, sizeof(double) * S.n));
-    GB_CUDA(cudaMalloc((void**)&dgfull, sizeof(double) * S.n));
-    for (int q = 0; q < N && rc == 0; q++) {
-        rc = S.place(transforms + 16 * ns * q, st);
-        if (rc) break;
-        rc = gbvlm_mesh_metrics_f64(0.0, ns, S.dims.data(), S.C(S.verts).data(), S.colloc.data(), S.normals.data(),
-                                    S.areas.data(), s);
-        if (rc) break;
-        GB_CUDA(cudaMemcpyAsync(td, dtransforms + 16 * ns * q, sizeof(double) * 16 * ns, cudaMemcpyHostToDevice, st));
-        k_dft_row<<<(unsigned)cdiv(S.n, 128), 128, 0, st>>>(C, Dd, S.n, N, q, gfull);
-        k_dft_row<<<(unsigned)cdiv(S.n, 128), 128, 0, st>>>(C, DDd, S.n, N, q, dgfull);
-        for (int m = 0; m < ns; m++) {
-            const int64_t nsm = S.dims[m].ns, ncm = S.dims[m].nc, np = nsm * ncm;
-            k_vel_dual<double><<<(unsigned)cdiv(np, 128), 128, 0, st>>>(td + 16 * m, S.colloc_h[m], S.vel[m], np);
-            const double* prev = nullptr;
-            if (coupled_te && m > 0 && S.dims[m - 1].ns == nsm) prev = gfull + S.poff[m] - nsm;  // TE row of surface m-1
-            k_delta<<<(unsigned)cdiv(np, 128), 128, 0, st>>>(gfull + S.poff[m], nsm, ncm, prev, S.gdelta[m]);
-            rc = gbvlm_forces_unsteady_f64(nsm, ncm, S.verts[m], S.gdelta[m], dgfull + S.poff[m], S.vel[m],
-                                           S.areas[m], S.normals[m], S.forces[m], s);
-            if (rc) break;
-        }
-        if (rc) break;
-        const double* fs = freestream + 3 * q;
-        double la[3] = {-fs[2], 0.0, fs[0]};
-        const double ll = sqrt(la[0] * la[0] + la[2] * la[2]);
-        la[0] /= ll;
-        la[2] /= ll;
-        double cl = 0, ta = 0, tm = 0, cm = 0;
-        for (int m = 0; m < ns && rc == 0; m++) {
-            const int64_t nsm = S.dims[m].ns, ncm = S.dims[m].nc;
-            double area, clm, mac, cmm[3];
-            if ((rc = gbvlm_sum_f64(S.areas[m], nsm * ncm, &area, s))) break;
-            if ((rc = gbvlm_coeff_cl_f64(nsm, ncm, S.forces[m], la, fs, 1.0, area, &clm, s))) break;
-            if ((rc = gbvlm_mesh_mac_f64(nsm, ncm, S.verts[m], S.areas[m], &mac, s))) break;
-            if ((rc = gbvlm_coeff_cm_f64(nsm, ncm, S.forces[m], S.verts[m], ref_a + 3 * q, fs, 1.0, area, mac, cmm, s)))
-                break;
-            cl += clm * area;
-            ta += area;
-            tm += mac;
-            cm += cmm[1] * area * mac;
-            if (m == 1 && ref_b) {
-                double cmb[3];
-                if ((rc = gbvlm_coeff_cm_f64(nsm, ncm, S.forces[m], S.verts[m], ref_b + 3 * q, fs, 1.0, area, mac, cmb,
-                                             s)))
-                    break;
-                out[2 * N + q] = cmb[1];
-            }
-        }
-        out[q] = cl / ta;
-        out[N + q] = cm / (ta * tm);
-    }
-    cudaFree(C);
-    cudaFree(Dd);
-    cudaFree(DDd);
-    cudaFree(td);
-    cudaFree(gfull);
-    cudaFree(dgfull);
-    return rc;
+    return gbvlm_hbvlm_loads_batch(h, 1, coeffs, dft, ddft, transforms, dtransforms, freestream, ref_a, ref_b,
+                                   coupled_te, out, stream);
 }
 
 int gbvlm_hbvlm_loads_batch(gbvlm_hbvlm h, int32_t K, const double* coeffs, const double* dft, const double* ddft,
@@ -1046,15 +1084,51 @@ int gbvlm_hbvlm_loads_batch(gbvlm_hbvlm h, int32_t K, const double* coeffs, cons
                             const double* ref_a, const double* ref_b, int32_t coupled_te, double* out,
                             gbvlm_stream stream) {
     GB_REQUIRE(h && coeffs && dft && ddft && transforms && dtransforms && freestream && ref_a && out, "null argument");
-    const HbState& S = h->st;
-    GB_REQUIRE(K >= 1 && S.N > 0, "loads before prepare");
-    const int64_t N = S.N, ln = S.n * N, lt = N * S.nsurf * 16;
-    for (int32_t c = 0; c < K; c++) {
-        int rc = gbvlm_hbvlm_loads(h, coeffs + c * ln, dft + c * N * N, ddft + c * N * N, transforms + c * lt,
-                                   dtransforms + c * lt, freestream + c * N * 3, ref_a + c * N * 3,
-                                   ref_b ? ref_b + c * N * 3 : nullptr, coupled_te, out + c * 3 * N, stream);
-        if (rc) return rc;
+    HbState& S = h->st;
+    GB_REQUIRE(S.N > 0 && S.aic_ready, "loads before prepare");
+    GB_REQUIRE(K >= 1 && (int64_t)K * S.N <= 2147483647, "bad K=%d", K);
+    cudaStream_t st = to_cuda(stream);
+    const int64_t N = S.N, ninst = (int64_t)K * N, nt = ninst * S.nsurf * 16;
+    int rc;
+    if ((rc = S.ld_C.grow(ninst * S.n)) || (rc = S.ld_D.grow(ninst * N)) || (rc = S.ld_DD.grow(ninst * N)) ||
+        (rc = S.ld_T.grow(nt)) || (rc = S.ld_Td.grow(nt)) || (rc = S.ld_fs.grow(ninst * 3)) ||
+        (rc = S.ld_ra.grow(ninst * 3)) || (rc = S.ld_rb.grow(ninst * 3)) || (rc = S.ld_out.grow(ninst * 3)))
+        return rc;
+    GB_CUDA(cudaMemcpyAsync(S.ld_C.p, coeffs, sizeof(double) * ninst * S.n, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S.ld_D.p, dft, sizeof(double) * ninst * N, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S.ld_DD.p, ddft, sizeof(double) * ninst * N, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S.ld_T.p, transforms, sizeof(double) * nt, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S.ld_Td.p, dtransforms, sizeof(double) * nt, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S.ld_fs.p, freestream, sizeof(double) * ninst * 3, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S.ld_ra.p, ref_a, sizeof(double) * ninst * 3, cudaMemcpyHostToDevice, st));
+    if (ref_b) GB_CUDA(cudaMemcpyAsync(S.ld_rb.p, ref_b, sizeof(double) * ninst * 3, cudaMemcpyHostToDevice, st));
+    LoadsArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nsurf = S.nsurf;
+    a.N = (int32_t)N;
+    a.coupled = coupled_te ? 1 : 0;
+    a.n = S.n;
+    for (int m = 0; m < S.nsurf; m++) {
+        a.ns[m] = S.dims[m].ns;
+        a.nc[m] = S.dims[m].nc;
+        a.poff[m] = S.poff[m];
+        a.vinit[m] = S.vinit[m];
+        a.colloc_h[m] = S.colloc_h[m];
     }
+    a.poff[S.nsurf] = S.poff[S.nsurf];
+    a.C = S.ld_C.p;
+    a.D = S.ld_D.p;
+    a.DD = S.ld_DD.p;
+    a.T = S.ld_T.p;
+    a.Td = S.ld_Td.p;
+    a.fs = S.ld_fs.p;
+    a.ref_a = S.ld_ra.p;
+    a.ref_b = ref_b ? S.ld_rb.p : nullptr;
+    a.out = S.ld_out.p;
+    k_hb_loads<<<(unsigned)ninst, HBL_THREADS, 0, st>>>(a);
+    GB_LAUNCH_CHECK();
+    GB_CUDA(cudaMemcpyAsync(out, S.ld_out.p, sizeof(double) * ninst * 3, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
     return GBVLM_OK;
 }
 

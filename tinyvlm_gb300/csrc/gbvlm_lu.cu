@@ -913,6 +913,7 @@ template <class T>
 __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rhs0, int32_t nrhs_blk, int use_smem) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int32_t sid = blockIdx.x;
+    rhs0 += (int32_t)blockIdx.y * nrhs_blk;  // right-hand-side block of this CTA
     const int64_t n = B.n[sid], ld = B.ld[sid];
     const T* A = B.A[sid];
     const int32_t nr = (int32_t)min((int64_t)nrhs_blk, (int64_t)B.nrhs[sid] - rhs0);
@@ -1833,10 +1834,11 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t 
     const size_t smem = use_smem ? full : sizeof(T) * (size_t)maxn;
     GB_REQUIRE(smem <= (size_t)TS_SMEM_BYTES, "triangular solve: n=%lld needs %zu bytes of shared memory",
                (long long)maxn, smem);
-    for (int32_t r0 = 0; r0 < max_nrhs; r0 += TS_MAXRHS) {
-        k_trsolve<T><<<nsys, TS_THREADS, smem, st>>>(B, r0, TS_MAXRHS, use_smem);
-        GB_LAUNCH_CHECK();
-    }
+    // one CTA per system and block of TS_MAXRHS right-hand sides, all in one launch
+    const int64_t blocks = cdiv(max_nrhs, TS_MAXRHS);
+    GB_REQUIRE(blocks <= 65535, "triangular solve: %d right-hand sides exceed one launch", max_nrhs);
+    k_trsolve<T><<<dim3((unsigned)nsys, (unsigned)blocks), TS_THREADS, smem, st>>>(B, 0, TS_MAXRHS, use_smem);
+    GB_LAUNCH_CHECK();
     return GBVLM_OK;
 }
 

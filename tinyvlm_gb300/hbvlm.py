@@ -155,28 +155,84 @@ class HBEngine:
         return out.reshape(3, N)
 
 
-def hb_arrays(assembly, N, dt, max_t_steps, t_start, period):
-    """Wake transforms per step, instance transforms/rates for the map and for the loads."""
-    nodes = assembly.surface_kinematics()
-    ns = len(nodes)
-    wake_T = np.zeros((max_t_steps, ns, 16))
-    tw = np.arange(max_t_steps) * dt
-    for m, nd in enumerate(nodes):
-        v, _ = nd.transform_series(tw)
-        wake_T[:, m] = v.transpose(0, 2, 1).reshape(-1, 16)
+def fourier_basis(H, omega, t):
+    """The phases of ``fourier`` on the dual number (t, 1), shared by every
+    coefficient row: per harmonic k, cos and sin of (t omega) k and the
+    phase rate omega k."""
+    out = []
+    for h in range(H):
+        k = float(h + 1)
+        ph = (t * omega) * k
+        out.append((np.cos(ph), np.sin(ph), omega * k))
+    return out
 
-    def inst(start):
-        ts = np.array([int(round((start + period * s / N) / dt)) for s in range(N)], np.int64)
-        tm = ts * dt
-        T = np.zeros((N, ns, 16))
-        Td = np.zeros((N, ns, 16))
-        for m, nd in enumerate(nodes):
-            v, d = nd.transform_series(tm)
-            T[:, m] = v.transpose(0, 2, 1).reshape(-1, 16)
-            Td[:, m] = d.transpose(0, 2, 1).reshape(-1, 16)
-        return ts, tm, T, Td
 
-    return wake_T, inst(t_start), inst(0.0)
+def fourier_dual(row, basis, t):
+    """``fourier`` on (t, 1) in closed form: value and d/dt with the
+    operations of the Dual evaluation, in its order."""
+    val = row[0] + 0.0 * t
+    grad = np.zeros(np.shape(val))
+    for h, (c, s, w) in enumerate(basis):
+        val = (val + c * row[2 * h + 1]) + s * row[2 * h + 2]
+        grad = (grad + (-s * w) * row[2 * h + 1]) + (c * w) * row[2 * h + 2]
+    return val, grad
+
+
+def _rot_y(px, a, ag):
+    """rotation_matrix([px, 0, 0], [0, 1, 0], (a, ag)): the nonzero entries
+    R00 = R22 = 1 - (1 - cos a), R02 = -R20 = sin a, the translation
+    T0 = px - R00 px, T2 = -R20 px, and their rates."""
+    s, c = np.sin(a), np.cos(a)
+    sg = c * ag
+    c1, c1g = 1.0 - c, 0.0 - (-s * ag)
+    r00, r00g = 1.0 - c1, -c1g
+    t0, t0g = px - r00 * px, 0.0 - r00g * px
+    t2, t2g = 0.0 - (-s) * px, 0.0 - (-sg) * px
+    return dict(r00=r00, r00g=r00g, r02=s, r02g=sg, t0=t0, t0g=t0g, t2=t2, t2g=t2g)
+
+
+def _stack(e00, e02, e03, e20, e22, e23, diag):
+    """(T, 4, 4) matrices with the given rows 0 and 2, row 1 = (0, diag, 0, 0), row 3 = (0, 0, 0, diag)."""
+    T = np.zeros((np.size(e00), 4, 4))
+    T[:, 0, 0], T[:, 0, 2], T[:, 0, 3] = e00, e02, e03
+    T[:, 2, 0], T[:, 2, 2], T[:, 2, 3] = e20, e22, e23
+    T[:, 1, 1] = T[:, 3, 3] = diag
+    return T
+
+
+def pitch_heave_series(t, sigma, heave, pitch, px, ctrl=None, qx=None):
+    """Transforms and rates of the libhbvlm kinematic chain in closed form:
+    free stream translation (-sigma t, 0, 0), heave (0, 0, -h), pitch about
+    (px, 0, 0) and, for the flap, a control rotation about (qx, 0, 0) after
+    the pitch (libhbvlm3.cpp:559-641; libhbvlm.cpp:470-515).  heave, pitch and
+    ctrl are (value, rate) pairs from ``fourier_dual``.  Returns per surface
+    (wing[, flap]) the (T, 4, 4) transform and rate stacks, each entry the
+    value the Dual evaluation of the same chain gives."""
+    d0, d0g = t * (-sigma), np.zeros_like(t) - sigma
+    d2, d2g = -heave[0], -heave[1]
+    P = _rot_y(px, *pitch)
+    a00, a00g, a02, a02g = P["r00"], P["r00g"], P["r02"], P["r02g"]
+    a03, a03g = P["t0"] + d0, P["t0g"] + d0g
+    a23, a23g = P["t2"] + d2, P["t2g"] + d2g
+    wing = (_stack(a00, a02, a03, -a02, a00, a23, 1.0), _stack(a00g, a02g, a03g, -a02g, a00g, a23g, 0.0))
+    if ctrl is None:
+        return [wing]
+    B = _rot_y(qx, *ctrl)
+    b00, b00g, b02, b02g = B["r00"], B["r00g"], B["r02"], B["r02g"]
+    b20, b20g = -b02, -b02g
+    u0, u0g, u2, u2g = B["t0"], B["t0g"], B["t2"], B["t2g"]
+    rows = []
+    for ar0, ar0g, ar2, ar2g, ar3, ar3g in ((a00, a00g, a02, a02g, a03, a03g), (-a02, -a02g, a00, a00g, a23, a23g)):
+        m0 = ar0 * b00 + ar2 * b20
+        m0g = (ar0 * b00g + ar0g * b00) + (ar2 * b20g + ar2g * b20)
+        m2 = ar0 * b02 + ar2 * b00
+        m2g = (ar0 * b02g + ar0g * b02) + (ar2 * b00g + ar2g * b00)
+        m3 = (ar0 * u0 + ar2 * u2) + ar3
+        m3g = ((ar0 * u0g + ar0g * u0) + (ar2 * u2g + ar2g * u2)) + ar3g
+        rows.append((m0, m0g, m2, m2g, m3, m3g))
+    (f00, f00g, f02, f02g, f03, f03g), (f20, f20g, f22, f22g, f23, f23g) = rows
+    flap = (_stack(f00, f02, f03, f20, f22, f23, 1.0), _stack(f00g, f02g, f03g, f20g, f22g, f23g, 0.0))
+    return [wing, flap]
 
 
 class _HBVLMBase:
@@ -204,68 +260,60 @@ class _HBVLMBase:
         self.engine = HBEngine(self.verts, self.lifting)
         self.gamma_coeffs = np.zeros((self.engine.n, self.m_coeffs), order="F")
 
-    def _run(self, t_start, omega, assembly, refs, forces_t, coupled_te):
-        N, H = self.m_coeffs, self.m_harmonics
-        period = TWO_PI_F / omega
-        interval = period / N
-        chord = last_panel_chord(self.verts[self.dt_surface])
-        if not interval > chord:
-            raise AssertionError("period interval %g must exceed the last panel chord %g" % (interval, chord))
-        dt = interval / math.ceil(interval / chord)
-        max_t = int((t_start + period + dt) / dt)
-        wake_T, (ts, tm, T, Td), (fts, ftm, fT, fTd) = hb_arrays(assembly, N, dt, max_t, t_start, period)
-        dft, ddft = dft_matrices(N, omega, period)
-        self.engine.prepare(H, max_t, wake_T, ts, tm, T, Td, dft)
-        self.iterations = self.engine.solve(self.gamma_coeffs, omega, dt, 100, self.tol, 10)
-        _, da = assembly.kinematics().transform_series(ftm)
-        fs = -da[:, :3, 3]
-        v0, _ = assembly.surface_kinematics()[0].transform_series(ftm)
-        ref_a = (v0 @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
-        ref_b = None
-        if len(refs) > 1:
-            v1, _ = assembly.surface_kinematics()[1].transform_series(ftm)
-            ref_b = (v1 @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
-        out = self.engine.loads(self.gamma_coeffs, dft, ddft, fT, fTd, fs, ref_a, ref_b, coupled_te, N)
-        rows = forces_t.shape[0]
-        forces_t[:, :] = out[:rows, :]
-        self._last = dict(dt=dt, max_t=max_t, period=period, wake_T=wake_T, inst=(ts, tm, T, Td),
-                          force_inst=(fts, ftm, fT, fTd), dft=dft, ddft=ddft, fs=fs, ref_a=ref_a, ref_b=ref_b)
-        return forces_t
+    def _run_sets(self, sets, refs, forces_list, coupled_te):
+        """HBVLM::run for K parameter sets (libhbvlm3.cpp:262-552), solved together.
 
-
-    def _run_batch(self, t_starts, omegas, assemblies, refs, forces_list, coupled_te):
-        """Every parameter set starts from the current coefficients; afterwards
-        they hold the last set's fixed point, as after the same runs in sequence."""
+        sets: dicts with ``omega``, ``t_start`` and the kinematic parameters
+        ``_series`` reads.  Each set's kinematics (wake steps, solve
+        instances, force instances) evaluate in one closed-form pass; every
+        set starts from the current coefficients, which afterwards hold the
+        last set's fixed point, as after the same runs in sequence."""
         N, H = self.m_coeffs, self.m_harmonics
         chord = last_panel_chord(self.verts[self.dt_surface])
-        K = len(omegas)
-        cols = []
-        for t_start, omega, asm in zip(t_starts, omegas, assemblies):
+        cols, times = [], []
+        for k, S in enumerate(sets):
+            omega, t_start = S["omega"], S["t_start"]
             period = TWO_PI_F / omega
             interval = period / N
             if not interval > chord:
                 raise AssertionError("period interval %g must exceed the last panel chord %g" % (interval, chord))
             dt = interval / math.ceil(interval / chord)
             max_t = int((t_start + period + dt) / dt)
-            wake_T, inst, finst = hb_arrays(asm, N, dt, max_t, t_start, period)
-            dft, ddft = dft_matrices(N, omega, period)
-            _, da = asm.kinematics().transform_series(finst[1])
-            fs = -da[:, :3, 3]
-            v0, _ = asm.surface_kinematics()[0].transform_series(finst[1])
-            ref_a = (v0 @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
-            ref_b = None
+            ts = np.array([int(round((t_start + period * q / N) / dt)) for q in range(N)], np.int64)
+            fts = np.array([int(round((0.0 + period * q / N) / dt)) for q in range(N)], np.int64)
+            c = dict(omega=omega, dt=dt, max_t=max_t, period=period, ts=ts, tm=ts * dt, fts=fts, ftm=fts * dt)
+            times += [np.arange(max_t) * dt, c["tm"], c["ftm"]]
+            cols.append(c)
+        for k, c in enumerate(cols):
+            series = self._series(sets[k], np.concatenate(times[3 * k:3 * k + 3]))
+            off, seg = 0, []
+            for length in (c["max_t"], N, N):
+                seg.append(slice(off, off + length))
+                off += length
+            flat = lambda A, sl: A[sl].transpose(0, 2, 1).reshape(-1, 16)
+            c["wake_T"] = np.stack([flat(v, seg[0]) for v, _ in series], axis=1)
+            T = np.stack([flat(v, seg[1]) for v, _ in series], axis=1)
+            Td = np.stack([flat(g, seg[1]) for _, g in series], axis=1)
+            fT = np.stack([flat(v, seg[2]) for v, _ in series], axis=1)
+            fTd = np.stack([flat(g, seg[2]) for _, g in series], axis=1)
+            c["inst"] = (c["ts"], c["tm"], T, Td)
+            c["finst"] = c["force_inst"] = (c["fts"], c["ftm"], fT, fTd)
+            c["dft"], c["ddft"] = dft_matrices(N, c["omega"], c["period"])
+            c["fs"] = np.tile(np.array([self._sigma(sets[k]), -0.0, -0.0]), (N, 1))  # -d/dt of the free stream
+            v0 = series[0][0][seg[2]]
+            c["ref_a"] = (v0 @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
+            c["ref_b"] = None
             if len(refs) > 1:
-                v1, _ = asm.surface_kinematics()[1].transform_series(finst[1])
-                ref_b = (v1 @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
-            cols.append(dict(dt=dt, max_t=max_t, wake_T=wake_T, inst=inst, finst=finst, dft=dft, ddft=ddft, fs=fs,
-                             ref_a=ref_a, ref_b=ref_b))
+                v1 = series[1][0][seg[2]]
+                c["ref_b"] = (v1 @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
+        K = len(cols)
         self.engine.prepare_batch(H, [c["max_t"] for c in cols], [c["wake_T"] for c in cols],
                                   np.concatenate([c["inst"][0] for c in cols]),
                                   np.concatenate([c["inst"][1] for c in cols]),
                                   np.concatenate([c["inst"][2] for c in cols]),
                                   np.concatenate([c["inst"][3] for c in cols]), [c["dft"] for c in cols])
         xs = np.repeat(self.gamma_coeffs[None], K, axis=0)
-        self.iterations = self.engine.solve_batch(xs, omegas, [c["dt"] for c in cols], 100, self.tol, 10)
+        its = self.engine.solve_batch(xs, [c["omega"] for c in cols], [c["dt"] for c in cols], 100, self.tol, 10)
         ref_b = np.concatenate([c["ref_b"] for c in cols]) if len(refs) > 1 else None
         out = self.engine.loads_batch(xs, [c["dft"] for c in cols], [c["ddft"] for c in cols],
                                       np.concatenate([c["finst"][2] for c in cols]),
@@ -276,7 +324,8 @@ class _HBVLMBase:
             f[:, :] = o[:f.shape[0], :]
         self.gamma_coeffs[:] = xs[-1]
         self._last_batch = cols
-        return forces_list
+        self._last = cols[-1]
+        return its
 
 
 class HBVLM3(_HBVLMBase):
@@ -305,16 +354,30 @@ class HBVLM3(_HBVLMBase):
         asm.add("flap", ctrl, True)
         return asm
 
+    def _sigma(self, S):
+        return S["U"] / (self.VARS["b"] * self.VARS["omega_alpha"])
+
+    def _series(self, S, t):
+        """The chain of ``assembly`` for parameter set S at the times t."""
+        v = self.VARS
+        r = np.asarray(S["dyn"], np.float64)
+        B = fourier_basis(self.m_harmonics, S["omega"], t)
+        return pitch_heave_series(t, self._sigma(S), fourier_dual(r[0], B, t), fourier_dual(r[1], B, t),
+                                  1.0 + v["a"], fourier_dual(r[2], B, t), 1.0 + v["c"])
+
+    def _refs(self):
+        return (1.0 + self.VARS["a"], 1.0 + self.VARS["c"])
+
     def run(self, omega, U, dyn_f, forces_t):
-        t_final = 2.0 * TWO_PI_F / omega
-        asm = self.assembly(omega, U, dyn_f)
-        return self._run(t_final, omega, asm, (1.0 + self.VARS["a"], 1.0 + self.VARS["c"]), forces_t, True)
+        S = dict(omega=omega, U=U, dyn=dyn_f, t_start=2.0 * TWO_PI_F / omega)
+        self.iterations = int(self._run_sets([S], self._refs(), [forces_t], True)[0])
+        return forces_t
 
     def run_batch(self, omegas, Us, dyn_fs, forces_list):
         """``run`` for K parameter sets solved together (one device solve)."""
-        asms = [self.assembly(om, U, d) for om, U, d in zip(omegas, Us, dyn_fs)]
-        return self._run_batch([2.0 * TWO_PI_F / om for om in omegas], list(omegas), asms,
-                               (1.0 + self.VARS["a"], 1.0 + self.VARS["c"]), forces_list, True)
+        sets = [dict(omega=om, U=U, dyn=d, t_start=2.0 * TWO_PI_F / om) for om, U, d in zip(omegas, Us, dyn_fs)]
+        self.iterations = self._run_sets(sets, self._refs(), forces_list, True)
+        return forces_list
 
 
 class HBVLM2(_HBVLMBase):
@@ -322,6 +385,7 @@ class HBVLM2(_HBVLMBase):
     qc = True
     tol = 1e-9
     dt_surface = 0
+    U_INF, A_H = 1.0, -0.5
 
     def __init__(self, backend_name, mesh):
         super().__init__(backend_name, [mesh], [True])
@@ -329,7 +393,7 @@ class HBVLM2(_HBVLMBase):
     def assembly(self, omega, dyn_f):
         H = self.m_harmonics
         r = np.asarray(dyn_f, np.float64)
-        u_inf, a_h = 1.0, -0.5
+        u_inf, a_h = self.U_INF, self.A_H
         tree = KinematicsTree()
         fsn = tree.add(lambda t: translation_matrix([-u_inf * t, 0.0, 0.0]))
         heave = tree.add(lambda t: translation_matrix([0.0, 0.0, -fourier(r[0], H, omega, t)])).after(fsn)
@@ -338,13 +402,21 @@ class HBVLM2(_HBVLMBase):
         asm.add("wing", pitch, True)
         return asm
 
+    def _sigma(self, S):
+        return self.U_INF
+
+    def _series(self, S, t):
+        r = np.asarray(S["dyn"], np.float64)
+        B = fourier_basis(self.m_harmonics, S["omega"], t)
+        return pitch_heave_series(t, self.U_INF, fourier_dual(r[0], B, t), fourier_dual(r[1], B, t), 1.0 + self.A_H)
+
     def run(self, omega, dyn_f, forces_t):
-        t_final = 3.0 * TWO_PI_F / omega
-        asm = self.assembly(omega, dyn_f)
-        return self._run(t_final, omega, asm, (0.5,), forces_t, False)
+        S = dict(omega=omega, dyn=dyn_f, t_start=3.0 * TWO_PI_F / omega)
+        self.iterations = int(self._run_sets([S], (0.5,), [forces_t], False)[0])
+        return forces_t
 
     def run_batch(self, omegas, dyn_fs, forces_list):
         """``run`` for K parameter sets solved together (one device solve)."""
-        asms = [self.assembly(om, d) for om, d in zip(omegas, dyn_fs)]
-        return self._run_batch([3.0 * TWO_PI_F / om for om in omegas], list(omegas), asms, (0.5,), forces_list,
-                               False)
+        sets = [dict(omega=om, dyn=d, t_start=3.0 * TWO_PI_F / om) for om, d in zip(omegas, dyn_fs)]
+        self.iterations = self._run_sets(sets, (0.5,), forces_list, False)
+        return forces_list
