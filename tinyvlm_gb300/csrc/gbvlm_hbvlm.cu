@@ -44,14 +44,6 @@ __global__ void k_rdft(const double* R, const double* D, int64_t n, int32_t N, d
     Y[g] = s;
 }
 
-template <class T>
-__global__ void k_vel_dual(const double* Td, const double* c0, double* vel, int64_t np) {
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= np) return;
-    const double x = c0[p], y = c0[np + p], z = c0[2 * np + p];
-    for (int r = 0; r < 3; r++) vel[r * np + p] = -(Td[r] * x + Td[r + 4] * y + Td[r + 8] * z + Td[r + 12]);
-}
-
 // wake pre-generation in one launch (libhbvlm3.cpp:307-319): wake row
 // nwv-1-i = T(i dt) applied to the trailing-edge vertices, every step i
 __global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, const double* vinit, int64_t ns, int64_t nc,
@@ -381,6 +373,67 @@ __global__ void __launch_bounds__(HBL_THREADS) k_hb_loads(LoadsArgs a) {
     }
 }
 
+// Instance geometry of every instance of every set in one launch (grid y:
+// instance): per panel the displaced vertices (k_displace), collocation
+// point and normal at zero angle of attack (k_mesh_metrics), and -V.n with
+// V = -(dT/dt) applied to the undisplaced collocation point (k_vel_dual,
+// k_rhs_velocities).  The instance buffer holds colloc (3n), normals (3n)
+// and -V.n (n) per instance, each surface's planes at 3 poff[m].
+struct GeomArgs {
+    int32_t nsurf;
+    int64_t n;
+    int64_t ns[GBVLM_MAX_SURFACES], nc[GBVLM_MAX_SURFACES], poff[GBVLM_MAX_SURFACES + 1];
+    const double* vinit[GBVLM_MAX_SURFACES];
+    const double* colloc_h[GBVLM_MAX_SURFACES];
+    const double *T, *Td;
+    double* inst;  // per instance 7 n
+};
+
+__global__ void k_hb_geom(GeomArgs a) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, e = blockIdx.y;
+    if (g >= a.n) return;
+    int m = 0;
+    while (m + 1 < a.nsurf && g >= a.poff[m + 1]) m++;
+    const int64_t ns = a.ns[m], nc = a.nc[m], np = ns * nc, nv = (ns + 1) * (nc + 1), p = g - a.poff[m];
+    const int64_t i = p % ns, j = p / ns;
+    const double* vin = a.vinit[m];
+    const double* tr = a.T + 16 * (e * a.nsurf + m);
+    const double* td = a.Td + 16 * (e * a.nsurf + m);
+    auto vert = [&](int64_t r) {
+        const double x[4] = {vin[r], vin[nv + r], vin[2 * nv + r], vin[3 * nv + r]};
+        double o[3];
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+            double acc = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc += x[k] * tr[cc + 4 * k];
+            o[cc] = acc;
+        }
+        return V3<double>{o[0], o[1], o[2]};
+    };
+    const int64_t ia = i + j * (ns + 1), ib = ia + 1, ic = ib + (ns + 1), id = ia + (ns + 1);
+    const V3<double> v0 = vert(ia), v1 = vert(ib), v2 = vert(ic), v3 = vert(id);
+    const V3<double> nn = cross(v3 - v1, v2 - v0);
+    const double l = sqrt(len2(nn));
+    const V3<double> nor{nn.x / l, nn.y / l, nn.z / l};
+    const V3<double> ch = 0.5 * (((v2 + v3) - v0) - v1);
+    const V3<double> cp = 0.5 * (v0 + v1) + 0.5 * ch;
+    const double* c0 = a.colloc_h[m];
+    const double x = c0[p], y = c0[np + p], z = c0[2 * np + p];
+    double vel[3];
+    for (int r = 0; r < 3; r++) vel[r] = -(td[r] * x + td[r + 4] * y + td[r + 8] * z + td[r + 12]);
+    double* base = a.inst + e * 7 * a.n;
+    double* col = base + 3 * a.poff[m];
+    double* nrm = base + 3 * a.n + 3 * a.poff[m];
+    col[p] = cp.x;
+    col[np + p] = cp.y;
+    col[2 * np + p] = cp.z;
+    nrm[p] = nor.x;
+    nrm[np + p] = nor.y;
+    nrm[2 * np + p] = nor.z;
+    base[6 * a.n + g] = 0.0 + -(vel[0] * nor.x + vel[1] * nor.y + vel[2] * nor.z);
+}
+
 // device buffer of doubles, grown on demand
 struct DBuf {
     double* p = nullptr;
@@ -424,7 +477,7 @@ struct HbState {
     int64_t n = 0;
     std::vector<int64_t> poff;
     std::vector<void*> allocs;
-    std::vector<double*> vinit, verts, colloc_h, normals, areas, vel;
+    std::vector<double*> vinit, verts, colloc_h, normals, areas;
     double* lhs = nullptr;
     gbvlm_lu lu = nullptr;
     bool aic_ready = false;
@@ -480,7 +533,7 @@ struct HbState {
             GB_CUDA(cudaMemcpy(p, vh[m], sizeof(double) * 4 * nv, cudaMemcpyHostToDevice));
             if ((rc = alloc(&p, 4 * nv))) return rc;
             verts.push_back(p);
-            for (auto* vec : {&colloc_h, &normals, &vel}) {
+            for (auto* vec : {&colloc_h, &normals}) {
                 if ((rc = alloc(&p, 3 * np))) return rc;
                 vec->push_back(p);
             }
@@ -523,7 +576,6 @@ struct HbState {
     int prepare(int32_t K_, int32_t harmonics, const int64_t* max_t, const double* const* wake_T,
                 const int64_t* t_steps, const double* times, const double* Th, const double* Tdh, const double* dft,
                 cudaStream_t st) {
-        gbvlm_stream s = (gbvlm_stream)st;
         int rc;
         if ((rc = aic(st))) return rc;
         K = K_;
@@ -569,9 +621,26 @@ struct HbState {
         GB_CUDA(cudaMemcpyAsync(tdev.p, Th, sizeof(double) * ninst * nsurf * 16, cudaMemcpyHostToDevice, st));
         GB_CUDA(cudaMemcpyAsync(tddev.p, Tdh, sizeof(double) * ninst * nsurf * 16, cudaMemcpyHostToDevice, st));
         GB_CUDA(cudaMemcpyAsync(D.p, dft, sizeof(double) * ninst * N, cudaMemcpyHostToDevice, st));
-        GB_CUDA(cudaMemsetAsync(inst_buf.p, 0, sizeof(double) * ninst * 7 * n, st));
         GB_CUDA(cudaMemsetAsync(gwake_buf.p, 0, sizeof(double) * std::max<int64_t>(gw_tot, 1), st));
-        std::vector<const double*> tp(nsurf);
+        {
+            GeomArgs ga;
+            memset(&ga, 0, sizeof(ga));
+            ga.nsurf = nsurf;
+            ga.n = n;
+            for (int m = 0; m < nsurf; m++) {
+                ga.ns[m] = dims[m].ns;
+                ga.nc[m] = dims[m].nc;
+                ga.poff[m] = poff[m];
+                ga.vinit[m] = vinit[m];
+                ga.colloc_h[m] = colloc_h[m];
+            }
+            ga.poff[nsurf] = poff[nsurf];
+            ga.T = tdev.p;
+            ga.Td = tddev.p;
+            ga.inst = inst_buf.p;
+            k_hb_geom<<<dim3((unsigned)cdiv(n, 128), (unsigned)ninst), 128, 0, st>>>(ga);
+            GB_LAUNCH_CHECK();
+        }
         int64_t gwo = 0;
         for (int c = 0; c < K; c++) {
             HbCol& col = cols[c];
@@ -590,25 +659,10 @@ struct HbState {
                 for (int m = 0; m < nsurf; m++) {
                     I.colloc[m] = base + 3 * poff[m];
                     I.normals[m] = base + 3 * n + 3 * poff[m];
-                    tp[m] = tdev.p + 16 * (e * nsurf + m);
                 }
                 I.rhs_vel = base + 6 * n;
                 I.gwake[wake_surf] = gwake_buf.p + gwo;
                 gwo += W.ns * (col.max_t - 1);
-                if ((rc = gbvlm_displace_wing_f64(nsurf, dims.data(), tp.data(), verts.data(), C(vinit).data(), s)))
-                    return rc;
-                if ((rc = gbvlm_mesh_metrics_f64(0.0, nsurf, dims.data(), C(verts).data(), I.colloc.data(),
-                                                 I.normals.data(), areas.data(), s)))
-                    return rc;
-                for (int m = 0; m < nsurf; m++) {
-                    const int64_t np = dims[m].ns * dims[m].nc;
-                    k_vel_dual<double><<<(unsigned)cdiv(np, 128), 128, 0, st>>>(tddev.p + 16 * (e * nsurf + m),
-                                                                                 colloc_h[m], vel[m], np);
-                    GB_LAUNCH_CHECK();
-                }
-                if ((rc = gbvlm_rhs_assemble_velocities_f64(I.rhs_vel, nsurf, dims.data(), C(I.normals).data(),
-                                                            C(vel).data(), s)))
-                    return rc;
             }
         }
         // the operator's instance table and basis rows
