@@ -526,8 +526,40 @@ def run_hbvlm(args):
         torch.cuda.synchronize()
         ms.append(1000.0 * (time.perf_counter() - t0))
         its.append(int(hb.iterations))
+    # the 3-point finite-difference Jacobian of the loads with respect to the 22 motion coefficients
+    # (scripts/finite_diff.py:26-48 as scripts/continuation.py:192-195 uses it): 44 HBVLM solves, as one
+    # batch (run_batch) and one run at a time
+    from tinyvlm_gb300.finite_diff import numerical_jac_batch, perturbed_points
+    om, dyn = reqs[0]
+    x = dyn.ravel().copy()
+    x[x == 0] = 1e-3
+
+    def f_batch(points):
+        fl = [np.zeros((2, 11)) for _ in points]
+        hb.gamma_coeffs[:] = 0.0
+        hb.run_batch([om] * len(points), [p.reshape(2, -1) for p in points], fl)
+        return [f.ravel() for f in fl]
+
+    numerical_jac_batch(f_batch, x)  # warm-up
+    jb = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        numerical_jac_batch(f_batch, x)
+        torch.cuda.synchronize()
+        jb.append(1000.0 * (time.perf_counter() - t0))
+    pts, _ = perturbed_points(x)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in pts:
+        hb.gamma_coeffs[:] = 0.0
+        hb.run(om, p.reshape(2, -1), ft)
+    torch.cuda.synchronize()
+    seq = 1000.0 * (time.perf_counter() - t0)
     print(json.dumps({"workload": "HBVLM 2-DOF section 45x1, H = 5, Anderson m = 10 on the device, 6 seeded requests",
-                      "ms_per_solve": ms, "median_ms": float(np.median(ms)), "anderson_iters": its}))
+                      "ms_per_solve": ms, "median_ms": float(np.median(ms)), "anderson_iters": its,
+                      "fd_jacobian": {"sets": len(pts), "batched_ms": float(np.median(jb)),
+                                      "one_run_per_set_ms": seq}}))
 
 
 def run_served(args):
