@@ -90,6 +90,7 @@ struct WopInst {
     int64_t it;             // active wake rows
     int64_t nwv;            // the column's wake vertex rows
     int64_t rps;            // wake rows per slice of k_wake_operator
+    int64_t np0;            // panels of surface 0 (the origin is its first collocation point)
     double t;               // instance time
     double omega, dt;       // the column's map parameters
 };
@@ -100,7 +101,73 @@ struct WopArgs {
     int64_t poff[GBVLM_MAX_SURFACES + 1];
     int64_t wns;
     double* partial;  // [slice][instance][n * wns][N]
+    const float* wshift;       // k_wake_shift's output
+    const int64_t* wshift_off; // per instance, into wshift
+    float* basis_f2;           // the basis rows as float pairs, 2 floats per entry of the double rows
+    const double* basis0;      // start of the double basis rows
 };
+
+// ---------------------------------------------------------------------------
+// Float-pair ("double-single") arithmetic for the operator's ring values:
+// a value is the unevaluated sum h + l of two floats, carried through the
+// error-free transformations of Knuth (two-sum), Dekker (fast two-sum) and
+// the fused multiply-add product, as in the double-double library of Hida,
+// Li and Bailey but on float pairs.  About 48 significant bits, on the fp32
+// pipe: GB300 issues fp32 arithmetic many times faster than fp64.  Division
+// and square root take the float quotient / root and correct it with the
+// residual formed in pairs (Karp and Markstein).  Every operation is written
+// with the _rn intrinsics so that no contraction changes an error term.
+// ---------------------------------------------------------------------------
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 f2_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return F2{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ F2 f2_fast(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return F2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    F2 s = f2_two_sum(a.h, b.h);
+    const F2 t = f2_two_sum(a.l, b.l);
+    s = f2_fast(s.h, __fadd_rn(s.l, t.h));
+    return f2_fast(s.h, __fadd_rn(s.l, t.l));
+}
+__device__ __forceinline__ F2 f2_neg(F2 a) { return F2{-a.h, -a.l}; }
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return f2_fast(p, e);
+}
+__device__ __forceinline__ F2 f2_mulf(F2 a, float b) {
+    const float p = __fmul_rn(a.h, b);
+    const float e = __fmaf_rn(a.l, b, __fmaf_rn(a.h, b, -p));
+    return f2_fast(p, e);
+}
+__device__ __forceinline__ F2 f2_div(F2 a, F2 b) {
+    const float q1 = __fdiv_rn(a.h, b.h);
+    F2 r = f2_sub(a, f2_mulf(b, q1));
+    const float q2 = __fdiv_rn(r.h, b.h);
+    r = f2_sub(r, f2_mulf(b, q2));
+    const float q3 = __fdiv_rn(r.h, b.h);
+    return f2_add(f2_fast(q1, q2), F2{q3, 0.f});
+}
+__device__ __forceinline__ F2 f2_sqrt(F2 a) {
+    if (!(a.h > 0.f)) return F2{0.f, 0.f};
+    const float x = __fsqrt_rn(a.h);
+    const F2 d = f2_sub(a, f2_mul(F2{x, 0.f}, F2{x, 0.f}));
+    return f2_add(F2{x, 0.f}, F2{__fdiv_rn(d.h, __fmul_rn(2.f, x)), 0.f});
+}
+__device__ __forceinline__ F2 f2_of(double x) {
+    const float h = __double2float_rn(x);
+    return F2{h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double f2_dbl(F2 a) { return (double)a.h + (double)a.l; }
 
 // basis_q(j, c) for the active rows of every instance (grid y: instance),
 // the same phases as k_gamma_wake in the operator library
@@ -112,20 +179,78 @@ __global__ void k_hb_basis(WopArgs a) {
     const int32_t U = a.N;
     const double s0 = 1.0 / sqrt((double)U), s2 = sqrt(2.0 / (double)U);
     double* b = I.basis + r * U;
-    b[0] = s0;
+    float* bf = a.basis_f2 + (b - a.basis0) * 2;
+    auto put = [&](int c, double v) {
+        b[c] = v;
+        const F2 f = f2_of(v);
+        bf[2 * c] = f.h;
+        bf[2 * c + 1] = f.l;
+    };
+    put(0, s0);
     for (int32_t h = 0; h < a.H; h++) {
         const double wk = omega * (double)(h + 1);
         const double ph = wk * (I.t - (double)(r + 1) * dt);
         double sn, cs;
         sincos(ph, &sn, &cs);
-        b[2 * h + 1] = cs * s2;
-        b[2 * h + 2] = sn * s2;
+        put(2 * h + 1, cs * s2);
+        put(2 * h + 2, sn * s2);
+    }
+}
+
+struct RelF2 {
+    F2 x, y, z, n;
+};
+__device__ __forceinline__ RelF2 rel_f2(F2 px, F2 py, F2 pz, F2 vx, F2 vy, F2 vz) {
+    RelF2 r;
+    r.x = f2_sub(px, vx);
+    r.y = f2_sub(py, vy);
+    r.z = f2_sub(pz, vz);
+    r.n = f2_sqrt(f2_add(f2_add(f2_mul(r.x, r.x), f2_mul(r.y, r.y)), f2_mul(r.z, r.z)));
+    return r;
+}
+// seg_normal of the operator library (4 pi (v(A->B) . n), no core) in float pairs
+__device__ __forceinline__ F2 seg_normal_f2(const RelF2& a, const RelF2& b, F2 nx, F2 ny, F2 nz) {
+    const F2 r0x = f2_sub(a.x, b.x), r0y = f2_sub(a.y, b.y), r0z = f2_sub(a.z, b.z);  // B - A
+    const F2 cx = f2_sub(f2_mul(r0y, a.z), f2_mul(r0z, a.y));
+    const F2 cy = f2_sub(f2_mul(r0z, a.x), f2_mul(r0x, a.z));
+    const F2 cz = f2_sub(f2_mul(r0x, a.y), f2_mul(r0y, a.x));
+    const F2 sq = f2_add(f2_add(f2_mul(cx, cx), f2_mul(cy, cy)), f2_mul(cz, cz));
+    if (sq.h < RCUT_SQ || a.n.h < (float)RCUT_NORM_D || b.n.h < (float)RCUT_NORM_D) return F2{0.f, 0.f};
+    const F2 ab = f2_add(f2_add(f2_mul(a.x, b.x), f2_mul(a.y, b.y)), f2_mul(a.z, b.z));
+    const F2 nab = f2_mul(a.n, b.n), sum = f2_add(a.n, b.n);
+    F2 num, den;
+    if (ab.h >= 0.f) {
+        num = sum;
+        den = f2_mul(nab, f2_add(nab, ab));
+    } else {
+        num = f2_mul(sum, f2_sub(nab, ab));
+        den = f2_mul(nab, sq);
+    }
+    const F2 cn = f2_add(f2_add(f2_mul(cx, nx), f2_mul(cy, ny)), f2_mul(cz, nz));
+    return f2_mul(f2_div(num, den), cn);
+}
+
+// the wake of each instance's set relative to the instance's origin (its
+// first collocation point), as float pairs: 6 planes (x h, x l, y h, ...)
+// of (wns+1) x nwv; the relative vectors of the operator are then
+// differences of small numbers near the wing and lose no accuracy
+__global__ void k_wake_shift(const WopInst* inst, int64_t wns, float* out, const int64_t* off) {
+    const WopInst& I = inst[blockIdx.y];
+    const int64_t nv = (wns + 1) * I.nwv;
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    float* o = out + off[blockIdx.y];
+    const double O[3] = {I.colloc[0][0], I.colloc[0][I.np0], I.colloc[0][2 * I.np0]};
+    for (int c = 0; c < 3; c++) {
+        const F2 f = f2_of(I.wake[c * nv + v] - O[c]);
+        o[(2 * c) * nv + v] = f.h;
+        o[(2 * c + 1) * nv + v] = f.l;
     }
 }
 
 // one thread per (target p, wake span i) of instance blockIdx.y over the
-// rows of slice blockIdx.z: the ring values along the rows, each line's
-// spanwise segment shared by the two rings it bounds
+// rows of slice blockIdx.z: the ring values along the rows in float pairs,
+// each line's spanwise segment shared by the two rings it bounds
 __global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
     const WopInst& I = a.inst[blockIdx.y];
     const int64_t n = a.poff[a.nsurf], npairs = n * a.wns;
@@ -135,49 +260,47 @@ __global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
     int m = 0;
     while (p >= a.poff[m + 1]) m++;
     const int64_t pl = p - a.poff[m], np = a.poff[m + 1] - a.poff[m];
+    const double O[3] = {I.colloc[0][0], I.colloc[0][I.np0], I.colloc[0][2 * I.np0]};
     const double px = I.colloc[m][pl], py = I.colloc[m][np + pl], pz = I.colloc[m][2 * np + pl];
-    const double nx = I.normals[m][pl], ny = I.normals[m][np + pl], nz = I.normals[m][2 * np + pl];
+    const F2 Px = f2_of(px - O[0]), Py = f2_of(py - O[1]), Pz = f2_of(pz - O[2]);
+    const F2 Qy = f2_of(-py - O[1]);  // the mirror point's y
+    const F2 nx = f2_of(I.normals[m][pl]), ny = f2_of(I.normals[m][np + pl]), nz = f2_of(I.normals[m][2 * np + pl]);
+    const F2 mny = f2_neg(ny);
     const int64_t start = I.nwv - 1 - I.it;
     const int64_t j0 = start + (int64_t)blockIdx.z * I.rps;
     const int64_t j1 = min(j0 + I.rps, I.nwv - 1);
-    double acc[WOP_NMAX];
+    F2 acc[WOP_NMAX];
 #pragma unroll
-    for (int c = 0; c < WOP_NMAX; c++) acc[c] = 0.0;
+    for (int c = 0; c < WOP_NMAX; c++) acc[c] = F2{0.f, 0.f};
     if (j0 < j1) {
-        const int64_t n1 = a.wns + 1, wl = n1 * I.nwv;
-        auto V = [&](int64_t row, int64_t k) {
+        const int64_t n1 = a.wns + 1, nv = n1 * I.nwv;
+        const float* W = a.wshift + a.wshift_off[blockIdx.y];
+        auto V = [&](int64_t row, int64_t k, F2& x, F2& y, F2& z) {
             const int64_t o = k + row * n1;
-            return V3<double>{I.wake[o], I.wake[wl + o], I.wake[2 * wl + o]};
+            x = F2{W[o], W[nv + o]};
+            y = F2{W[2 * nv + o], W[3 * nv + o]};
+            z = F2{W[4 * nv + o], W[5 * nv + o]};
         };
-        // line j: v0 = (j, i), v1 = (j, i + 1)
-        V3<double> v0 = V(j0, i), v1 = V(j0, i + 1);
-        Rel<double> A0 = make_rel<double>(px - v0.x, py - v0.y, pz - v0.z);
-        Rel<double> A1 = make_rel<double>(px - v1.x, py - v1.y, pz - v1.z);
-        Rel<double> B0 = make_rel<double>(px - v0.x, -py - v0.y, pz - v0.z);
-        Rel<double> B1 = make_rel<double>(px - v1.x, -py - v1.y, pz - v1.z);
-        double Ta = seg_normal<double, false>(A0, A1, v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, nx, ny, nz, 0.0);
-        double Tb = seg_normal<double, false>(B0, B1, v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, nx, -ny, nz, 0.0);
+        F2 x0, y0, z0, x1, y1, z1;
+        V(j0, i, x0, y0, z0);
+        V(j0, i + 1, x1, y1, z1);
+        RelF2 A0 = rel_f2(Px, Py, Pz, x0, y0, z0), A1 = rel_f2(Px, Py, Pz, x1, y1, z1);
+        RelF2 B0 = rel_f2(Px, Qy, Pz, x0, y0, z0), B1 = rel_f2(Px, Qy, Pz, x1, y1, z1);
+        F2 Ta = seg_normal_f2(A0, A1, nx, ny, nz), Tb = seg_normal_f2(B0, B1, nx, mny, nz);
         for (int64_t j = j0; j < j1; j++) {
-            // line j + 1: v3 = (j + 1, i), v2 = (j + 1, i + 1)
-            const V3<double> v3 = V(j + 1, i), v2 = V(j + 1, i + 1);
-            const Rel<double> A3 = make_rel<double>(px - v3.x, py - v3.y, pz - v3.z);
-            const Rel<double> A2 = make_rel<double>(px - v2.x, py - v2.y, pz - v2.z);
-            const Rel<double> B3 = make_rel<double>(px - v3.x, -py - v3.y, pz - v3.z);
-            const Rel<double> B2 = make_rel<double>(px - v2.x, -py - v2.y, pz - v2.z);
-            const double rx = v2.x - v1.x, ry = v2.y - v1.y, rz = v2.z - v1.z;  // v1 -> v2
-            const double lx = v0.x - v3.x, ly = v0.y - v3.y, lz = v0.z - v3.z;  // v3 -> v0
-            const double bx = v2.x - v3.x, by = v2.y - v3.y, bz = v2.z - v3.z;  // v3 -> v2: the next ring's top
-            const double Na = seg_normal<double, false>(A3, A2, bx, by, bz, nx, ny, nz, 0.0);
-            const double Nb = seg_normal<double, false>(B3, B2, bx, by, bz, nx, -ny, nz, 0.0);
-            double val = Ta + seg_normal<double, false>(A1, A2, rx, ry, rz, nx, ny, nz, 0.0) - Na +
-                         seg_normal<double, false>(A3, A0, lx, ly, lz, nx, ny, nz, 0.0);
-            val += Tb + seg_normal<double, false>(B1, B2, rx, ry, rz, nx, -ny, nz, 0.0) - Nb +
-                   seg_normal<double, false>(B3, B0, lx, ly, lz, nx, -ny, nz, 0.0);
-            const double* br = I.basis + (j - start) * a.N;
+            F2 x3, y3, z3, x2, y2, z2;  // line j + 1: v3 = (j + 1, i), v2 = (j + 1, i + 1)
+            V(j + 1, i, x3, y3, z3);
+            V(j + 1, i + 1, x2, y2, z2);
+            const RelF2 A3 = rel_f2(Px, Py, Pz, x3, y3, z3), A2 = rel_f2(Px, Py, Pz, x2, y2, z2);
+            const RelF2 B3 = rel_f2(Px, Qy, Pz, x3, y3, z3), B2 = rel_f2(Px, Qy, Pz, x2, y2, z2);
+            const F2 Na = seg_normal_f2(A3, A2, nx, ny, nz), Nb = seg_normal_f2(B3, B2, nx, mny, nz);
+            F2 val = f2_add(f2_sub(f2_add(Ta, seg_normal_f2(A1, A2, nx, ny, nz)), Na), seg_normal_f2(A3, A0, nx, ny, nz));
+            val = f2_add(val, f2_add(f2_sub(f2_add(Tb, seg_normal_f2(B1, B2, nx, mny, nz)), Nb),
+                                     seg_normal_f2(B3, B0, nx, mny, nz)));
+            const float* br = a.basis_f2 + (I.basis - a.basis0 + (j - start) * a.N) * 2;
 #pragma unroll
             for (int c = 0; c < WOP_NMAX; c++)
-                if (c < a.N) acc[c] += val * br[c];
-            v0 = v3, v1 = v2;
+                if (c < a.N) acc[c] = f2_add(acc[c], f2_mul(val, F2{br[2 * c], br[2 * c + 1]}));
             A0 = A3, A1 = A2, B0 = B3, B1 = B2;
             Ta = Na, Tb = Nb;
         }
@@ -185,7 +308,7 @@ __global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
     double* out = a.partial + (((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * npairs + g) * a.N;
 #pragma unroll
     for (int c = 0; c < WOP_NMAX; c++)
-        if (c < a.N) out[c] = acc[c];
+        if (c < a.N) out[c] = f2_dbl(acc[c]);
 }
 
 // M = sum over slices of the partial operators, in slice order
@@ -434,9 +557,10 @@ __global__ void k_hb_geom(GeomArgs a) {
     base[6 * a.n + g] = 0.0 + -(vel[0] * nor.x + vel[1] * nor.y + vel[2] * nor.z);
 }
 
-// device buffer of doubles, grown on demand
-struct DBuf {
-    double* p = nullptr;
+// device buffer, grown on demand
+template <class T>
+struct Buf {
+    T* p = nullptr;
     size_t cap = 0;
     int grow(size_t cnt) {
         cnt = std::max<size_t>(cnt, 1);
@@ -444,14 +568,15 @@ struct DBuf {
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
-        GB_CUDA(cudaMalloc((void**)&p, sizeof(double) * cnt));
+        GB_CUDA(cudaMalloc((void**)&p, sizeof(T) * cnt));
         cap = cnt;
         return GBVLM_OK;
     }
-    ~DBuf() {
+    ~Buf() {
         if (p) cudaFree(p);
     }
 };
+using DBuf = Buf<double>;
 
 // one time instance of one column; pointers into the batch buffers
 struct Inst {
@@ -493,6 +618,8 @@ struct HbState {
     WopInst* d_wop = nullptr;
     size_t d_wop_cap = 0;
     DBuf wop_basis, wop_part, wop_M;
+    Buf<float> wop_basis_f2, wop_shift;
+    Buf<int64_t> wop_shift_off;
     bool wop_valid = false;
     // inputs and outputs of k_hb_loads
     DBuf ld_C, ld_D, ld_DD, ld_T, ld_Td, ld_fs, ld_ra, ld_rb, ld_out;
@@ -669,7 +796,7 @@ struct HbState {
         int64_t rows = 0;
         for (const HbCol& col : cols)
             for (const Inst& I : col.inst) rows += std::max<int64_t>(I.t_steps, 1);
-        if ((rc = wop_basis.grow(rows * N))) return rc;
+        if ((rc = wop_basis.grow(rows * N)) || (rc = wop_basis_f2.grow(2 * rows * N))) return rc;
         if (d_wop_cap < (size_t)ninst) {
             if (d_wop) cudaFree(d_wop);
             d_wop = nullptr;
@@ -693,6 +820,7 @@ struct HbState {
                 w.basis = wop_basis.p + off * N;
                 w.it = I.t_steps;
                 w.nwv = cols[c].max_t;
+                w.np0 = dims[0].ns * dims[0].nc;
                 w.t = I.t;
                 off += std::max<int64_t>(I.t_steps, 1);
             }
@@ -740,6 +868,24 @@ struct HbState {
         int rc;
         if ((rc = wop_part.grow((size_t)(zs * len))) || (rc = wop_M.grow((size_t)len))) return rc;
         a.partial = wop_part.p;
+        a.basis_f2 = wop_basis_f2.p;
+        a.basis0 = wop_basis.p;
+        // each instance's wake relative to its origin, as float pairs
+        std::vector<int64_t> soff(ninst);
+        int64_t stot = 0, maxv = 1;
+        for (int64_t e = 0; e < ninst; e++) {
+            soff[e] = stot;
+            const int64_t nv = (W.ns + 1) * wtab[e].nwv;
+            stot += 6 * nv;
+            maxv = std::max(maxv, nv);
+        }
+        if ((rc = wop_shift.grow((size_t)stot)) || (rc = wop_shift_off.grow((size_t)ninst))) return rc;
+        GB_CUDA(cudaMemcpyAsync(wop_shift_off.p, soff.data(), sizeof(int64_t) * ninst, cudaMemcpyHostToDevice, st));
+        k_wake_shift<<<dim3((unsigned)cdiv(maxv, 256), (unsigned)ninst), 256, 0, st>>>(d_wop, W.ns, wop_shift.p,
+                                                                                       wop_shift_off.p);
+        GB_LAUNCH_CHECK();
+        a.wshift = wop_shift.p;
+        a.wshift_off = wop_shift_off.p;
         k_hb_basis<<<dim3((unsigned)cdiv(max_it, 128), (unsigned)ninst), 128, 0, st>>>(a);
         GB_LAUNCH_CHECK();
         k_wake_operator<<<dim3((unsigned)xb, (unsigned)ninst, (unsigned)zs), WOP_THREADS, 0, st>>>(a);
