@@ -557,6 +557,20 @@ __global__ void k_hb_geom(GeomArgs a) {
     base[6 * a.n + g] = 0.0 + -(vel[0] * nor.x + vel[1] * nor.y + vel[2] * nor.z);
 }
 
+// X (n x cols) = Ainv (n x n) . Y (n x cols), column-major, one thread per
+// entry with the sum over k in order: the map's solve for the AIC of a small
+// lattice, whose inverse is formed once from its LU factors
+constexpr int64_t HB_INV_MAX = 2048;  // largest n whose inverse is kept (32 MiB)
+__global__ void k_hb_inv_apply(const double* Ainv, const double* Y, int64_t n, int64_t cols, double* X) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n * cols) return;
+    const int64_t r = e % n, j = e / n;
+    const double* y = Y + j * n;
+    double s = 0;
+    for (int64_t k = 0; k < n; k++) s += Ainv[r + k * n] * y[k];
+    X[e] = s;
+}
+
 // device buffer, grown on demand
 template <class T>
 struct Buf {
@@ -606,6 +620,7 @@ struct HbState {
     double* lhs = nullptr;
     gbvlm_lu lu = nullptr;
     bool aic_ready = false;
+    DBuf ainv;  // the AIC's inverse when n <= HB_INV_MAX
     std::vector<HbCol> cols;
     // batch buffers: per instance colloc, normals (3n each) and -V.n (n);
     // the lifting wake's gammas for the per-map sums; wakes; transforms and
@@ -692,6 +707,14 @@ struct HbState {
                                          C(verts).data(), nullptr, 0, 0.0, s)))
             return rc;
         if ((rc = gbvlm_lu_factor_f64(lu, lhs, n, n, s))) return rc;
+        if (n <= HB_INV_MAX) {  // A^-1 from the factors: the identity solved for
+            if ((rc = ainv.grow(n * n))) return rc;
+            std::vector<double> I((size_t)(n * n), 0.0);
+            for (int64_t i = 0; i < n; i++) I[i + i * n] = 1.0;
+            GB_CUDA(cudaMemcpyAsync(ainv.p, I.data(), sizeof(double) * n * n, cudaMemcpyHostToDevice, st));
+            if ((rc = gbvlm_lu_solve_f64(lu, lhs, n, n, ainv.p, n, n, s))) return rc;
+            GB_CUDA(cudaStreamSynchronize(st));
+        }
         aic_ready = true;
         return GBVLM_OK;
     }
@@ -909,9 +932,16 @@ struct HbState {
             for (int c = 0; c < K && same; c++)
                 same = wtab[(int64_t)c * N].omega == omega[c] && wtab[(int64_t)c * N].dt == dt[c];
             if (!same && (rc = build_wop(omega, dt, st))) return rc;
+            double* Y = n <= HB_INV_MAX ? R.p : Xout.p;
             k_hb_rhs<<<dim3((unsigned)n, (unsigned)K), HBR_THREADS, 0, st>>>(d_wop, wop_M.p, Xin.p, n, te_off, W.ns,
-                                                                             N, D.p, Xout.p);
+                                                                             N, D.p, Y);
             GB_LAUNCH_CHECK();
+            if (n <= HB_INV_MAX) {
+                const int64_t cols = (int64_t)K * N;
+                k_hb_inv_apply<<<(unsigned)cdiv(n * cols, 128), 128, 0, st>>>(ainv.p, R.p, n, cols, Xout.p);
+                GB_LAUNCH_CHECK();
+                return GBVLM_OK;
+            }
         } else {
             for (int c = 0; c < K; c++) {
                 HbCol& col = cols[c];
