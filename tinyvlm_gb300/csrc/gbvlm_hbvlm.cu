@@ -77,7 +77,7 @@ __global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, cons
 // fraction of the fp32 rate on this part) then run once per solve instead of
 // once per map; each map reduces to the small contraction k_hb_rhs.
 // ---------------------------------------------------------------------------
-constexpr int WOP_THREADS = 128;
+constexpr int WOP_THREADS = 64;  // two warps: the idle warps of a wider block cost registers
 constexpr int WOP_NMAX = 32;  // Fourier coefficients a thread accumulates (harmonics <= 15)
 
 // one instance of one parameter set (column)
@@ -1003,12 +1003,13 @@ __device__ __forceinline__ double aa_wsum(double v) {
 // x_new = x + g - sum_j (X_j + G_j) gam_j with gam the least-squares
 // coefficients of G[:, :mk]; X[:, slot] = x_new - x; x = x_new (in place).
 // The CTA copies G[:, :mk] and g into shared memory (or, when they do not
-// fit, into the global work buffers Wg, bg) and runs the Householder QR
-// there: for each column j, warp 0 forms the reflector (its norm, the new
-// pivot, v^T v = 2 |a| (|a| + |a_j|)), then the warps reflect the later
-// columns and the right-hand side in parallel, one column per warp at a
-// time.  fp64 runs at a small fraction of the fp32 rate on this part, so the
-// work is spread over all four schedulers' fp64 units.
+// fit, into the global work buffers) and runs the Householder QR there:
+// for each column j, warp 0 forms the reflector (its norm, the new pivot,
+// v^T v = 2 |a| (|a| + |a_j|)), then the warps reflect the later columns
+// and the right-hand side in parallel, one column per warp at a time.  The
+// QR runs in float pairs on the fp32 pipe (one CTA's fp64 units made it a
+// 68 us step); the least-squares coefficients and the new iterate are
+// formed in double.
 constexpr int AA_STEP_THREADS = 256;
 
 // Per column c = blockIdx.x (its state at buf + c * stride: g (L), the
@@ -1026,66 +1027,72 @@ __global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, in
                                                                    double* xall, const int* act, int use_smem) {
     if (!act[blockIdx.x]) return;
     extern __shared__ double aa_sm[];
-    __shared__ double gam[16], diag[16];
-    __shared__ double s_nrm, s_rvv;
+    __shared__ double gam[16];
+    __shared__ F2 gamf[16], diag[16];
+    __shared__ F2 s_nrm, s_rvv;
     const AaCol cs = aa_col(buf, L, m);
     double* X = cs.X;
     const double* G = cs.G;
     const double* g = cs.g;
     double* x = xall + (int64_t)blockIdx.x * L;
-    double* Wg = cs.W;
-    double* bg = cs.b;
-    double* W = use_smem ? aa_sm : Wg;
-    double* b = use_smem ? aa_sm + L * mk : bg;
+    // the QR's work copy of G[:, :mk] and its right-hand side, as float pairs
+    F2* W = reinterpret_cast<F2*>(use_smem ? aa_sm : cs.W);
+    F2* b = reinterpret_cast<F2*>(use_smem ? aa_sm + L * mk : cs.b);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    for (int64_t e = tid; e < L * mk; e += blockDim.x) W[e] = G[e];
-    for (int64_t i = tid; i < L; i += blockDim.x) b[i] = g[i];
-    // dot products over rows j..L-1, four partial sums per lane, warp-reduced
-    auto dot = [&](const double* u, const double* w, int j) {
-        double t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+    for (int64_t e = tid; e < L * mk; e += blockDim.x) W[e] = f2_of(G[e]);
+    for (int64_t i = tid; i < L; i += blockDim.x) b[i] = f2_of(g[i]);
+    // dot products over rows j..L-1: four partial sums per lane, reduced
+    // down the warp and broadcast from lane 0
+    auto dot = [&](const F2* u, const F2* w, int j) {
+        F2 t0{0.f, 0.f}, t1{0.f, 0.f}, t2{0.f, 0.f}, t3{0.f, 0.f};
         int64_t i = j + lane;
         for (; i + 96 < L; i += 128) {
-            t0 += u[i] * w[i];
-            t1 += u[i + 32] * w[i + 32];
-            t2 += u[i + 64] * w[i + 64];
-            t3 += u[i + 96] * w[i + 96];
+            t0 = f2_add(t0, f2_mul(u[i], w[i]));
+            t1 = f2_add(t1, f2_mul(u[i + 32], w[i + 32]));
+            t2 = f2_add(t2, f2_mul(u[i + 64], w[i + 64]));
+            t3 = f2_add(t3, f2_mul(u[i + 96], w[i + 96]));
         }
-        for (; i < L; i += 32) t0 += u[i] * w[i];
-        return aa_wsum((t0 + t1) + (t2 + t3));
+        for (; i < L; i += 32) t0 = f2_add(t0, f2_mul(u[i], w[i]));
+        F2 t = f2_add(f2_add(t0, t1), f2_add(t2, t3));
+        for (int o = 16; o > 0; o >>= 1)
+            t = f2_add(t, F2{__shfl_down_sync(0xffffffffu, t.h, o), __shfl_down_sync(0xffffffffu, t.l, o)});
+        return F2{__shfl_sync(0xffffffffu, t.h, 0), __shfl_sync(0xffffffffu, t.l, 0)};
     };
     __syncthreads();
     for (int j = 0; j < mk; j++) {
-        double* wj = W + (int64_t)j * L;
+        F2* wj = W + (int64_t)j * L;
         if (wid == 0) {
-            const double nrm = sqrt(dot(wj, wj, j));
+            const F2 nrm = f2_sqrt(dot(wj, wj, j));
             if (lane == 0) {
                 s_nrm = nrm;
-                diag[j] = 0;
-                if (nrm != 0) {
-                    const double a0 = wj[j];
-                    const double alpha = a0 > 0 ? -nrm : nrm;
-                    wj[j] = a0 - alpha;
+                diag[j] = F2{0.f, 0.f};
+                if (nrm.h != 0.f) {
+                    const F2 a0 = wj[j];
+                    const F2 alpha = a0.h > 0.f ? f2_neg(nrm) : nrm;
+                    wj[j] = f2_sub(a0, alpha);
                     diag[j] = alpha;
-                    s_rvv = 1.0 / (2.0 * nrm * (nrm + fabs(a0)));
+                    const F2 aa = a0.h < 0.f ? f2_neg(a0) : a0;
+                    s_rvv = f2_div(F2{1.f, 0.f}, f2_mulf(f2_mul(nrm, f2_add(nrm, aa)), 2.f));
                 }
             }
         }
         __syncthreads();
-        if (s_nrm != 0) {  // uniform
-            const double rvv = s_rvv;
+        if (s_nrm.h != 0.f) {  // uniform
+            const F2 rvv = s_rvv;
             for (int t = wid; t < mk - j; t += nw) {  // the later columns, then the right-hand side
-                double* wc = t < mk - j - 1 ? W + (int64_t)(j + 1 + t) * L : b;
-                const double f = 2.0 * dot(wj, wc, j) * rvv;
-                for (int64_t i = j + lane; i < L; i += 32) wc[i] -= f * wj[i];
+                F2* wc = t < mk - j - 1 ? W + (int64_t)(j + 1 + t) * L : b;
+                const F2 f = f2_mulf(f2_mul(dot(wj, wc, j), rvv), 2.f);
+                for (int64_t i = j + lane; i < L; i += 32) wc[i] = f2_sub(wc[i], f2_mul(f, wj[i]));
             }
         }
         __syncthreads();
     }
     if (tid == 0)
         for (int j = mk - 1; j >= 0; j--) {
-            double sj = b[j];
-            for (int c = j + 1; c < mk; c++) sj -= W[j + (int64_t)c * L] * gam[c];
-            gam[j] = diag[j] != 0 ? sj / diag[j] : 0;
+            F2 sj = b[j];
+            for (int c = j + 1; c < mk; c++) sj = f2_sub(sj, f2_mul(W[j + (int64_t)c * L], gamf[c]));
+            gamf[j] = diag[j].h != 0.f ? f2_div(sj, diag[j]) : F2{0.f, 0.f};
+            gam[j] = f2_dbl(gamf[j]);
         }
     __syncthreads();
     for (int64_t i = tid; i < L; i += blockDim.x) {
