@@ -638,12 +638,25 @@ struct HbState {
     bool wop_valid = false;
     // inputs and outputs of k_hb_loads
     DBuf ld_C, ld_D, ld_DD, ld_T, ld_Td, ld_fs, ld_ra, ld_rb, ld_out;
+    // Anderson state of every set, and the Anderson loop as a graph (a
+    // while node), rebuilt when its arguments change
+    DBuf aa_buf;
+    cudaGraph_t aa_graph = nullptr;
+    cudaGraphExec_t aa_exec = nullptr;
+    cudaStream_t aa_cap = nullptr;
+    std::vector<char> aa_key;
 
     ~HbState() {
+        if (aa_exec) cudaGraphExecDestroy(aa_exec);
+        if (aa_graph) cudaGraphDestroy(aa_graph);
+        if (aa_cap) cudaStreamDestroy(aa_cap);
         if (lu) gbvlm_lu_destroy(lu);
         for (void* p : allocs) cudaFree(p);
         if (d_wop) cudaFree(d_wop);
     }
+
+    // the loop can be a graph when a map is k_hb_rhs + k_hb_inv_apply
+    bool anderson_graph_ok() const { return use_wop() && n <= HB_INV_MAX; }
 
     int alloc(double** p, size_t cnt) {
         GB_CUDA(cudaMalloc((void**)p, sizeof(double) * (cnt > 0 ? cnt : 1)));
@@ -1024,8 +1037,14 @@ __device__ __forceinline__ AaCol aa_col(double* buf, int64_t L, int m) {
 }
 
 __global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, int m, int mk, int slot, double* buf,
-                                                                   double* xall, const int* act, int use_smem) {
+                                                                   double* xall, const int* act, int use_smem,
+                                                                   const int* kdev) {
     if (!act[blockIdx.x]) return;
+    if (kdev) {  // the iteration k from device memory (the loop's graph): mk = min(m, k), slot = k mod m
+        const int k = *kdev;
+        mk = min(m, k);
+        slot = k % m;
+    }
     extern __shared__ double aa_sm[];
     __shared__ double gam[16];
     __shared__ F2 gamf[16], diag[16];
@@ -1107,8 +1126,9 @@ __global__ void __launch_bounds__(AA_STEP_THREADS) k_anderson_step(int64_t L, in
 // g = g_new; *norm = |g|
 __global__ void __launch_bounds__(AA_THREADS) k_anderson_post(int64_t L, int m, int slot, const double* fxall,
                                                               const double* xall, double* buf, double* norm,
-                                                              const int* act) {
+                                                              const int* act, const int* kdev) {
     if (!act[blockIdx.x]) return;
+    if (kdev) slot = *kdev % m;
     __shared__ double sh[32];
     const AaCol cs = aa_col(buf, L, m);
     double* g = cs.g;
@@ -1153,14 +1173,106 @@ __global__ void k_anderson_check(int K, const double* norm, double tol, int k, i
     if (threadIdx.x == 0) ctl[0] = live;
 }
 
+// The loop's test inside its graph: ctl[0] = k (incremented first when
+// `advance`), then k_anderson_check's test, and the while node continues
+// while some set iterates and k < max_iter
+__global__ void k_anderson_graph_test(int K, const double* norm, double tol, int max_iter, int* act, int* iters,
+                                      int* ctl, int advance, cudaGraphConditionalHandle loop) {
+    const int k = ctl[0] + (advance ? 1 : 0);
+    int live = 0;
+    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+        if (act[c] && !(norm[c] > tol)) {
+            act[c] = 0;
+            iters[c] = k;
+        }
+        live += act[c];
+    }
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    __syncwarp();
+    if (threadIdx.x == 0) {
+        ctl[0] = k;
+        ctl[1] = live;
+        cudaGraphSetConditional(loop, (live > 0 && k < max_iter) ? 1u : 0u);
+    }
+}
+
 // columns still iterating after max_iter steps report max_iter
-__global__ void k_anderson_finish(int K, int k, const int* act, int* iters) {
+__global__ void k_anderson_finish(int K, int k, const int* act, int* iters, const int* kdev) {
+    if (kdev) k = *kdev;
     for (int c = threadIdx.x; c < K; c += blockDim.x)
         if (act[c]) iters[c] = k;
 }
 
 __global__ void k_fill_i32(int* p, int n, int v) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
+}
+
+// The Anderson loop of gbvlm_hbvlm_solve_batch as one graph: a test node
+// (k = 1), then a while node whose body is the step, the map (k_hb_rhs,
+// k_hb_inv_apply), the residual update and the next test, which sets the
+// loop condition on the device.  k lives in ctl[0]; nothing returns to the
+// host until the loop ends.
+static int anderson_graph(HbState& S, int K, int64_t L, int m, int max_iter, double tol, double* buf, double* dnorm,
+                          int* act, int* iters, int* ctl, int use_smem, size_t smem) {
+    const gbvlm_dims& W = S.dims[S.wake_surf];
+    const int64_t te_off = S.poff[S.wake_surf] + (W.nc - 1) * W.ns;
+    struct Key {
+        const void* p[12];
+        int64_t v[8];
+        double tol;
+    } key;
+    memset(&key, 0, sizeof(key));
+    const void* ps[12] = {buf, dnorm, act, iters, ctl, S.d_wop, S.wop_M.p, S.Xin.p, S.D.p, S.R.p, S.ainv.p, S.Xout.p};
+    memcpy(key.p, ps, sizeof(ps));
+    const int64_t vs[8] = {K, L, m, max_iter, use_smem, (int64_t)smem, S.n, S.N};
+    memcpy(key.v, vs, sizeof(vs));
+    key.tol = tol;
+    if (S.aa_exec && S.aa_key.size() == sizeof(key) && memcmp(S.aa_key.data(), &key, sizeof(key)) == 0)
+        return GBVLM_OK;
+    if (S.aa_exec) cudaGraphExecDestroy(S.aa_exec);
+    if (S.aa_graph) cudaGraphDestroy(S.aa_graph);
+    S.aa_exec = nullptr;
+    S.aa_graph = nullptr;
+    S.aa_key.clear();
+    if (!S.aa_cap) GB_CUDA(cudaStreamCreateWithFlags(&S.aa_cap, cudaStreamNonBlocking));
+    GB_CUDA(cudaGraphCreate(&S.aa_graph, 0));
+    cudaGraphConditionalHandle loop;
+    GB_CUDA(cudaGraphConditionalHandleCreate(&loop, S.aa_graph, 0, cudaGraphCondAssignDefault));
+    cudaGraphNode_t nh, nw;
+    {
+        int adv = 0;
+        void* args[] = {&K, &dnorm, &tol, &max_iter, &act, &iters, &ctl, &adv, &loop};
+        cudaKernelNodeParams kp = {};
+        kp.func = (void*)k_anderson_graph_test;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(32);
+        kp.kernelParams = args;
+        GB_CUDA(cudaGraphAddKernelNode(&nh, S.aa_graph, nullptr, 0, &kp));
+    }
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    GB_CUDA(cudaGraphAddNode(&nw, S.aa_graph, &nh, nullptr, 1, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    cudaStream_t cs = S.aa_cap;
+    GB_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    const int64_t cols = (int64_t)K * S.N;
+    k_anderson_step<<<K, AA_STEP_THREADS, use_smem ? smem : 0, cs>>>(L, m, 0, 0, buf, S.Xin.p, act, use_smem, ctl);
+    k_hb_rhs<<<dim3((unsigned)S.n, (unsigned)K), HBR_THREADS, 0, cs>>>(S.d_wop, S.wop_M.p, S.Xin.p, S.n, te_off, W.ns,
+                                                                       S.N, S.D.p, S.R.p);
+    k_hb_inv_apply<<<(unsigned)cdiv(S.n * cols, 128), 128, 0, cs>>>(S.ainv.p, S.R.p, S.n, cols, S.Xout.p);
+    k_anderson_post<<<K, AA_THREADS, 0, cs>>>(L, m, 0, S.Xout.p, S.Xin.p, buf, dnorm, act, ctl);
+    k_anderson_graph_test<<<1, 32, 0, cs>>>(K, dnorm, tol, max_iter, act, iters, ctl, 1, loop);
+    const cudaError_t le = cudaGetLastError();
+    cudaGraph_t got = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &got);
+    GB_CUDA(le);
+    GB_CUDA(e);
+    GB_CUDA(cudaGraphInstantiate(&S.aa_exec, S.aa_graph, 0));
+    S.aa_key.assign((const char*)&key, (const char*)&key + sizeof(key));
+    return GBVLM_OK;
 }
 
 }  // namespace gbvlm
@@ -1242,18 +1354,15 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
     // g, the histories X and G, the QR work copy of G and its right-hand
     // side; then the residual norms and the loop's flags
     const size_t per = (size_t)L * (3 * m + 2);
-    double* buf = nullptr;
-    GB_CUDA(cudaMalloc((void**)&buf, sizeof(double) * (per * K + K) + sizeof(int) * (2 * K + 1)));
+    int rc = S.aa_buf.grow(per * K + K + (2 * K + 4 + 1) / 2);
+    if (rc) return rc;
+    double* buf = S.aa_buf.p;
     double* dnorm = buf + per * K;
     int* act = (int*)(dnorm + K);
     int* d_iters = act + K;
     int* ctl = d_iters + K;
     int* hctl = (int*)host_scratch(sizeof(int));
-    int rc = GBVLM_OK;
-    auto fail = [&](int r) {
-        cudaFree(buf);
-        return r;
-    };
+    auto fail = [&](int r) { return r; };
     auto check = [&](const char* what) {
         cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? GBVLM_OK : cuda_fail(e, what, __FILE__, __LINE__);
@@ -1267,10 +1376,10 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
     k_fill_i32<<<1, 256, 0, st>>>(d_iters, K, 0);
     // vlm_solvers.cpp:49-66: g0 = f(x0) - x0; X0 = g0; x1 = f(x0); g1 = f(x1) - x1; G0 = g1 - g0
     if ((rc = map())) return fail(rc);
-    k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, -1, S.Xout.p, S.Xin.p, buf, dnorm, act);
+    k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, -1, S.Xout.p, S.Xin.p, buf, dnorm, act, nullptr);
     k_anderson_first<<<dim3(g1, K), 256, 0, st>>>(L, m, S.Xout.p, S.Xin.p, buf);
     if ((rc = check("Anderson")) || (rc = map())) return fail(rc);
-    k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, 0, S.Xout.p, S.Xin.p, buf, dnorm, act);
+    k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, 0, S.Xout.p, S.Xin.p, buf, dnorm, act, nullptr);
     if ((rc = check("Anderson"))) return fail(rc);
     // the QR's columns in shared memory when m of them and g fit
     const size_t smem = sizeof(double) * (size_t)L * (m + 1);
@@ -1279,6 +1388,13 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
                         cudaSuccess)
         return fail(cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__));
     int k = 1;
+    if (S.anderson_graph_ok()) {  // the whole loop on the device
+        k_fill_i32<<<1, 32, 0, st>>>(ctl, 1, 1);
+        if ((rc = anderson_graph(S, K, L, m, max_iter, tol, buf, dnorm, act, d_iters, ctl, use_smem, smem)))
+            return fail(rc);
+        GB_CUDA(cudaGraphLaunch(S.aa_exec, st));
+        k = max_iter;  // the host loop below does not run
+    }
     while (k < max_iter) {
         k_anderson_check<<<1, 32, 0, st>>>(K, dnorm, tol, k, act, d_iters, ctl);
         if (cudaMemcpyAsync(hctl, ctl, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1287,19 +1403,18 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
         if (*hctl == 0) break;
         const int mk = std::min(m, k), slot = k % m;
         k_anderson_step<<<K, AA_STEP_THREADS, use_smem ? smem : 0, st>>>(L, m, mk, slot, buf, S.Xin.p, act,
-                                                                          use_smem);
+                                                                          use_smem, nullptr);
         if ((rc = check("Anderson")) || (rc = map())) return fail(rc);
-        k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, slot, S.Xout.p, S.Xin.p, buf, dnorm, act);
+        k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, slot, S.Xout.p, S.Xin.p, buf, dnorm, act, nullptr);
         if ((rc = check("Anderson"))) return fail(rc);
         k++;
     }
-    k_anderson_finish<<<1, 256, 0, st>>>(K, k, act, d_iters);
+    k_anderson_finish<<<1, 256, 0, st>>>(K, k, act, d_iters, S.anderson_graph_ok() ? ctl : nullptr);
     std::vector<int> hit(K);
     if (cudaMemcpyAsync(x, S.Xin.p, sizeof(double) * L * K, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(hit.data(), d_iters, sizeof(int) * K, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return fail(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__));
-    cudaFree(buf);
     if (iters)
         for (int c = 0; c < K; c++) iters[c] = hit[c];
     return GBVLM_OK;
