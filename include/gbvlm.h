@@ -451,6 +451,17 @@ int gbvlm_hbvlm_prepare_batch(gbvlm_hbvlm h, int32_t K, int32_t harmonics, const
                               const double* const* wake_transforms, const int64_t* t_steps, const double* times,
                               const double* transforms, const double* dtransforms, const double* dft,
                               gbvlm_stream stream);
+/* gbvlm_hbvlm_prepare_batch with the wake transforms evaluated on the device
+ * from the libhbvlm kinematic chain (libhbvlm3.cpp:559-641, libhbvlm.cpp:
+ * 470-515) instead of uploaded: per set, chain holds 6 + 3 (2H+1) doubles:
+ * sigma (free-stream speed), omega, dt, px (pitch axis x), qx (control
+ * axis x), flap (1 when the lifting surface follows the control rotation),
+ * then the heave, pitch and control Fourier rows.  Not in the reference:
+ * there the host evaluates every step's transform. */
+int gbvlm_hbvlm_prepare_batch_chain(gbvlm_hbvlm h, int32_t K, int32_t harmonics, const int64_t* max_t_steps,
+                                    const double* chain, const int64_t* t_steps, const double* times,
+                                    const double* transforms, const double* dtransforms, const double* dft,
+                                    gbvlm_stream stream);
 /* x: HOST K x (n x N) column-major iterates, updated in place; omega, dt,
  * iters: K each. */
 int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* omega, const double* dt,

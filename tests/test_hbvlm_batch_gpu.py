@@ -98,3 +98,23 @@ def test_fd_jacobian_batch_equals_columnwise(cuda):
     assert np.abs(J1).max() > 1e-3
     # a set's operator, iteration and solve do not depend on the rest of the batch
     np.testing.assert_allclose(J, J1, rtol=1e-9, atol=1e-9 * np.abs(J1).max())
+
+
+def test_device_wake_transforms_match_host(cuda):
+    """The wake transforms evaluated on the device from the chain parameters
+    against the host closed form (bitwise the dual-number tree): the same map
+    to rounding, for the 3-DOF chain (flap after the pitch)."""
+    wing = section(9, 0.0, 0.1905)
+    flap = section(3, 0.1905, 0.254)
+    hb = HBVLM3("gb300", [wing, flap])
+    hb.init(2, 1.0 / 0.127)
+    dyn = np.array([[0.0, 0.01, 0.0, 0.0, 0.0], [0.02, 0.0, 0.03, 0.0, 0.0], [0.0, 0.01, 0.0, 0.005, 0.0]])
+    hb.run(1.0, 10.0, dyn, np.zeros((3, 5)))
+    L = hb._last
+    x = np.asfortranarray(np.random.default_rng(5).standard_normal((hb.engine.n, 5)) * 0.01)
+    y_dev = hb.engine.map(x, 1.0, L["dt"])
+    ts, tm, T, Td = L["inst"]
+    hb.engine.prepare_batch(2, [L["max_t"]], [L["wake_T"]], ts, tm, T, Td, [L["dft"]])
+    y_host = hb.engine.map(x, 1.0, L["dt"])
+    print("device vs host wake transforms: map diff", np.abs(y_dev - y_host).max(), np.abs(y_host).max())
+    np.testing.assert_allclose(y_dev, y_host, rtol=1e-12, atol=1e-15)

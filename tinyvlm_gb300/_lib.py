@@ -102,6 +102,7 @@ def _protos():
     t["gbvlm_hbvlm_solve"] = [P, P, F64, F64, I32, F64, I32, P, P]
     t["gbvlm_hbvlm_loads"] = [P, P, P, P, P, P, P, P, P, I32, P, P]
     t["gbvlm_hbvlm_prepare_batch"] = [P, I32, I32, P, PP, P, P, P, P, P, P]
+    t["gbvlm_hbvlm_prepare_batch_chain"] = [P, I32, I32, P, P, P, P, P, P, P, P]
     t["gbvlm_hbvlm_solve_batch"] = [P, I32, P, P, P, I32, F64, I32, P, P]
     t["gbvlm_hbvlm_loads_batch"] = [P, I32, P, P, P, P, P, P, P, P, I32, P, P]
     return t

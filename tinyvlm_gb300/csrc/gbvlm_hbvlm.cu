@@ -44,6 +44,70 @@ __global__ void k_rdft(const double* R, const double* D, int64_t n, int32_t N, d
     Y[g] = s;
 }
 
+// The wake transforms of the libhbvlm kinematic chains (libhbvlm3.cpp:559-641,
+// libhbvlm.cpp:470-515) at the steps t = i dt, evaluated on the device:
+// free stream (-sigma t, 0, 0), heave (0, 0, -h(t)), pitch theta(t) about
+// (px, 0, 0) and, when the lifting surface is the flap, a control rotation
+// beta(t) about (qx, 0, 0) after the pitch.  h, theta, beta are Fourier
+// series sum_k c_k cos(w t k) + s_k sin(w t k) of their coefficient rows.
+// Parameters per set (HB_CHAIN_HEAD + 3 (2H+1) doubles): sigma, omega, dt,
+// px, qx, flap, then the heave, pitch and control rows.  Writes the
+// lifting surface's transform (column-major) at Tall[(i nsurf + m) 16].
+constexpr int HB_CHAIN_HEAD = 6;
+
+__device__ __forceinline__ void hb_rot_y(double px, double a, double& r00, double& r02, double& t0, double& t2) {
+    double sn, cs;
+    sincos(a, &sn, &cs);
+    const double c1 = 1.0 - cs;
+    r00 = 1.0 - c1;
+    r02 = sn;
+    t0 = px - r00 * px;
+    t2 = 0.0 - (-sn) * px;
+}
+
+__global__ void k_hb_chain(const double* prm, int H, int64_t rows, int32_t nsurf, int32_t m, double* Tall) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const int U = 2 * H + 1;
+    const double sigma = prm[0], omega = prm[1], dt = prm[2], px = prm[3], qx = prm[4];
+    const bool flap = prm[5] != 0.0;
+    const double* rh = prm + HB_CHAIN_HEAD;
+    const double* rp = rh + U;
+    const double* rc = rp + U;
+    const double t = (double)i * dt;
+    double h = rh[0] + 0.0 * t, th = rp[0] + 0.0 * t, be = rc[0] + 0.0 * t;
+    for (int k = 0; k < H; k++) {
+        double sn, cs;
+        sincos((t * omega) * (double)(k + 1), &sn, &cs);
+        h = (h + cs * rh[2 * k + 1]) + sn * rh[2 * k + 2];
+        th = (th + cs * rp[2 * k + 1]) + sn * rp[2 * k + 2];
+        be = (be + cs * rc[2 * k + 1]) + sn * rc[2 * k + 2];
+    }
+    double a00, a02, t0, t2;
+    hb_rot_y(px, th, a00, a02, t0, t2);
+    const double a03 = t0 + t * (-sigma), a23 = t2 + (-h);
+    double M[16] = {0};
+    M[5] = M[15] = 1.0;  // (1, 1), (3, 3)
+    if (!flap) {
+        M[0] = a00, M[8] = a02, M[12] = a03;   // row 0: (0,0), (0,2), (0,3)
+        M[2] = -a02, M[10] = a00, M[14] = a23; // row 2
+    } else {
+        double b00, b02, u0, u2;
+        hb_rot_y(qx, be, b00, b02, u0, u2);
+        const double b20 = -b02;
+        const double r0[3] = {a00, a02, a03}, r2[3] = {-a02, a00, a23};
+        for (int rr = 0; rr < 2; rr++) {
+            const double* ar = rr == 0 ? r0 : r2;
+            const int row = rr == 0 ? 0 : 2;
+            M[row] = ar[0] * b00 + ar[1] * b20;
+            M[8 + row] = ar[0] * b02 + ar[1] * b00;
+            M[12 + row] = (ar[0] * u0 + ar[1] * u2) + ar[2];
+        }
+    }
+    double* o = Tall + 16 * ((int64_t)i * nsurf + m);
+    for (int e = 0; e < 16; e++) o[e] = M[e];
+}
+
 // wake pre-generation in one launch (libhbvlm3.cpp:307-319): wake row
 // nwv-1-i = T(i dt) applied to the trailing-edge vertices, every step i
 __global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, const double* vinit, int64_t ns, int64_t nc,
@@ -626,7 +690,7 @@ struct HbState {
     // the lifting wake's gammas for the per-map sums; wakes; transforms and
     // rates of every instance; iterate, map output and right-hand sides
     // (K x n x N); DFT matrices (K x N x N); trailing-edge coefficients
-    DBuf inst_buf, gwake_buf, wake_buf, tw_buf, tdev, tddev, Xin, Xout, R, D, te;
+    DBuf inst_buf, gwake_buf, wake_buf, tw_buf, tdev, tddev, Xin, Xout, R, D, te, chain_buf;
     // the wake operator (k_wake_operator): instance table (host copy and
     // device), basis rows, partial sums and the operators
     std::vector<WopInst> wtab;
@@ -736,7 +800,9 @@ struct HbState {
     // part, per set): the lifting wake pre-generated over max_t[c] steps,
     // then per instance the displaced geometry and -V.n.  Nothing here
     // synchronises per instance: every transform is uploaded once.
-    int prepare(int32_t K_, int32_t harmonics, const int64_t* max_t, const double* const* wake_T,
+    // wake_T: per set its wake transforms (HOST), or chain: per set the
+    // chain parameters of k_hb_chain (HOST, K x (HB_CHAIN_HEAD + 3 (2H+1)))
+    int prepare(int32_t K_, int32_t harmonics, const int64_t* max_t, const double* const* wake_T, const double* chain,
                 const int64_t* t_steps, const double* times, const double* Th, const double* Tdh, const double* dft,
                 cudaStream_t st) {
         int rc;
@@ -750,7 +816,7 @@ struct HbState {
         int64_t wake_tot = 0, tw_tot = 0, gw_tot = 0;
         for (int c = 0; c < K; c++) {
             GB_REQUIRE(max_t[c] >= 2, "column %d: max_t_steps %lld < 2", c, (long long)max_t[c]);
-            GB_REQUIRE(wake_T[c] != nullptr, "column %d: wake transforms are null", c);
+            GB_REQUIRE(chain || wake_T[c] != nullptr, "column %d: wake transforms are null", c);
             wake_tot += 4 * wn1 * max_t[c];
             tw_tot += 16 * nsurf * max_t[c];
             gw_tot += (int64_t)N * W.ns * (max_t[c] - 1);
@@ -762,6 +828,11 @@ struct HbState {
             (rc = Xout.grow(ninst * n)) || (rc = R.grow(ninst * n)) || (rc = te.grow(ninst * W.ns)))
             return rc;
         // wakes (only the lifting surface's: the others shed none)
+        const int64_t cstride = HB_CHAIN_HEAD + 3 * (int64_t)N;
+        if (chain) {
+            if ((rc = chain_buf.grow(K * cstride))) return rc;
+            GB_CUDA(cudaMemcpyAsync(chain_buf.p, chain, sizeof(double) * K * cstride, cudaMemcpyHostToDevice, st));
+        }
         int64_t wo = 0, two = 0;
         for (int c = 0; c < K; c++) {
             HbCol& col = cols[c];
@@ -771,8 +842,14 @@ struct HbState {
             col.wake.assign(nsurf, nullptr);
             col.wake[wake_surf] = wake_buf.p + wo;
             double* Tall = tw_buf.p + two;
-            GB_CUDA(cudaMemcpyAsync(Tall, wake_T[c], sizeof(double) * 16 * nsurf * col.max_t, cudaMemcpyHostToDevice,
-                                    st));
+            if (chain) {
+                k_hb_chain<<<(unsigned)cdiv(col.max_t, 128), 128, 0, st>>>(chain_buf.p + c * cstride, harmonics,
+                                                                          col.max_t, nsurf, wake_surf, Tall);
+                GB_LAUNCH_CHECK();
+            } else {
+                GB_CUDA(cudaMemcpyAsync(Tall, wake_T[c], sizeof(double) * 16 * nsurf * col.max_t,
+                                        cudaMemcpyHostToDevice, st));
+            }
             const int64_t cnt = wn1 * col.max_t;
             k_pregen_wake<<<(unsigned)cdiv(cnt, 128), 128, 0, st>>>(Tall, nsurf, wake_surf, vinit[wake_surf], W.ns,
                                                                      W.nc, col.max_t, col.wake[wake_surf]);
@@ -1319,7 +1396,18 @@ int gbvlm_hbvlm_prepare_batch(gbvlm_hbvlm h, int32_t K, int32_t harmonics, const
                "null argument");
     GB_REQUIRE(harmonics >= 0 && harmonics <= 64, "harmonics %d outside [0, 64]", harmonics);
     GB_REQUIRE(K >= 1 && (int64_t)K * (2 * harmonics + 1) <= 65535, "K=%d: K (2H+1) must be in [1, 65535]", K);
-    return h->st.prepare(K, harmonics, max_t_steps, wake_transforms, t_steps, times, transforms, dtransforms, dft,
+    return h->st.prepare(K, harmonics, max_t_steps, wake_transforms, nullptr, t_steps, times, transforms, dtransforms,
+                         dft, to_cuda(stream));
+}
+
+int gbvlm_hbvlm_prepare_batch_chain(gbvlm_hbvlm h, int32_t K, int32_t harmonics, const int64_t* max_t_steps,
+                                    const double* chain, const int64_t* t_steps, const double* times,
+                                    const double* transforms, const double* dtransforms, const double* dft,
+                                    gbvlm_stream stream) {
+    GB_REQUIRE(h && max_t_steps && chain && t_steps && times && transforms && dtransforms && dft, "null argument");
+    GB_REQUIRE(harmonics >= 0 && harmonics <= 64, "harmonics %d outside [0, 64]", harmonics);
+    GB_REQUIRE(K >= 1 && (int64_t)K * (2 * harmonics + 1) <= 65535, "K=%d: K (2H+1) must be in [1, 65535]", K);
+    return h->st.prepare(K, harmonics, max_t_steps, nullptr, chain, t_steps, times, transforms, dtransforms, dft,
                          to_cuda(stream));
 }
 

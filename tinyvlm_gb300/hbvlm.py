@@ -121,6 +121,16 @@ class HBEngine:
         call("gbvlm_hbvlm_prepare_batch", self.h, K, int(harmonics), self._p(mt), ctypes.cast(wp, PP), self._p(ts),
              self._p(tm), self._p(T_), self._p(Td_), self._p(D_), None)
 
+    def prepare_batch_chain(self, harmonics, max_ts, chains, t_steps, times, T, Td, dfts):
+        """prepare_batch with each set's wake transforms evaluated on the device from its chain parameters."""
+        K = len(max_ts)
+        keep = [np.ascontiguousarray(np.asarray(max_ts, np.int64)), np.ascontiguousarray(np.stack(chains)),
+                np.ascontiguousarray(np.asarray(t_steps, np.int64)), np.ascontiguousarray(np.asarray(times, np.float64)),
+                np.ascontiguousarray(np.asarray(T, np.float64)), np.ascontiguousarray(np.asarray(Td, np.float64)),
+                np.ascontiguousarray(np.stack([self._colmajor(d) for d in dfts]))]
+        self._keep = keep
+        call("gbvlm_hbvlm_prepare_batch_chain", self.h, K, int(harmonics), *[self._p(a) for a in keep], None)
+
     def solve_batch(self, xs, omegas, dts, max_iter, tol, m):
         """xs: (K, n, N) iterates, updated in place (C-contiguous over sets, each set column-major)."""
         K = xs.shape[0]
@@ -235,6 +245,26 @@ def pitch_heave_series(t, sigma, heave, pitch, px, ctrl=None, qx=None):
     return [wing, flap]
 
 
+class _Lazy(dict):
+    """A dict whose keys in ``lazy`` are computed on first access (the host
+    copies of arrays the device evaluates, kept for inspection and tests)."""
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.lazy = {}
+
+    def __missing__(self, key):
+        if key in self.lazy:
+            self[key] = self.lazy.pop(key)()
+            return self[key]
+        raise KeyError(key)
+
+
+def _flat_stack(series, which, sl=slice(None)):
+    """(T, nsurf, 16) column-major transforms (which = 0) or rates (1) of every surface."""
+    return np.stack([s[which][sl].transpose(0, 2, 1).reshape(-1, 16) for s in series], axis=1)
+
+
 class _HBVLMBase:
     qc = False
     tol = 1e-12
@@ -260,14 +290,38 @@ class _HBVLMBase:
         self.engine = HBEngine(self.verts, self.lifting)
         self.gamma_coeffs = np.zeros((self.engine.n, self.m_coeffs), order="F")
 
+    def _chain_vector(self, S, dt):
+        """k_hb_chain's parameters for set S: sigma, omega, dt, px, qx, flap, the three coefficient rows."""
+        sigma, rows, px, qx, flap = self._chain_params(S)
+        U = self.m_coeffs
+        head = [sigma, S["omega"], dt, px, qx if qx is not None else 0.0, 1.0 if flap else 0.0]
+        return np.concatenate([np.array(head)] + [np.asarray(r, np.float64) if r is not None else np.zeros(U)
+                                                  for r in rows])
+
+    def _chain_series(self, sets, own, t):
+        """``_series`` for several sets at once: set own[i] at time t[i]."""
+        prm = [self._chain_params(S) for S in sets]
+        omega = np.array([S["omega"] for S in sets])[own]
+        sigma = np.array([q[0] for q in prm])[own]
+        px, qx, flap = prm[0][2], prm[0][3], prm[0][4]
+        rows = [np.stack([np.asarray(q[1][r], np.float64) for q in prm], axis=-1)[:, own] for r in range(3 if flap else 2)]
+        B = fourier_basis(self.m_harmonics, omega, t)
+        ctrl = fourier_dual(rows[2], B, t) if flap else None
+        return pitch_heave_series(t, sigma, fourier_dual(rows[0], B, t), fourier_dual(rows[1], B, t), px, ctrl, qx)
+
+    def _series(self, S, t):
+        """Transforms and rates of the surfaces' kinematic chain for parameter set S at the times t."""
+        return self._chain_series([S], np.zeros(np.size(t), np.int64), np.asarray(t, np.float64))
+
     def _run_sets(self, sets, refs, forces_list, coupled_te):
         """HBVLM::run for K parameter sets (libhbvlm3.cpp:262-552), solved together.
 
         sets: dicts with ``omega``, ``t_start`` and the kinematic parameters
-        ``_series`` reads.  Each set's kinematics (wake steps, solve
-        instances, force instances) evaluate in one closed-form pass; every
-        set starts from the current coefficients, which afterwards hold the
-        last set's fixed point, as after the same runs in sequence."""
+        ``_chain_params`` reads.  The wake transforms of every step are
+        evaluated on the device from the chain parameters; the instances'
+        transforms (2N per set) in one closed-form pass over all sets.
+        Every set starts from the current coefficients, which afterwards
+        hold the last set's fixed point, as after the same runs in sequence."""
         N, H = self.m_coeffs, self.m_harmonics
         chord = last_panel_chord(self.verts[self.dt_surface])
         cols, times = [], []
@@ -281,33 +335,25 @@ class _HBVLMBase:
             max_t = int((t_start + period + dt) / dt)
             ts = np.array([int(round((t_start + period * q / N) / dt)) for q in range(N)], np.int64)
             fts = np.array([int(round((0.0 + period * q / N) / dt)) for q in range(N)], np.int64)
-            c = dict(omega=omega, dt=dt, max_t=max_t, period=period, ts=ts, tm=ts * dt, fts=fts, ftm=fts * dt)
-            times += [np.arange(max_t) * dt, c["tm"], c["ftm"]]
+            c = _Lazy(omega=omega, dt=dt, max_t=max_t, period=period, ts=ts, tm=ts * dt, fts=fts, ftm=fts * dt)
+            c.lazy["wake_T"] = (lambda S=S, c=c: _flat_stack(self._series(S, np.arange(c["max_t"]) * c["dt"]), 0))
+            times += [c["tm"], c["ftm"]]
             cols.append(c)
+        K = len(cols)
+        own = np.repeat(np.arange(K), 2 * N)
+        series = self._chain_series(sets, own, np.concatenate(times))
         for k, c in enumerate(cols):
-            series = self._series(sets[k], np.concatenate(times[3 * k:3 * k + 3]))
-            off, seg = 0, []
-            for length in (c["max_t"], N, N):
-                seg.append(slice(off, off + length))
-                off += length
-            flat = lambda A, sl: A[sl].transpose(0, 2, 1).reshape(-1, 16)
-            c["wake_T"] = np.stack([flat(v, seg[0]) for v, _ in series], axis=1)
-            T = np.stack([flat(v, seg[1]) for v, _ in series], axis=1)
-            Td = np.stack([flat(g, seg[1]) for _, g in series], axis=1)
-            fT = np.stack([flat(v, seg[2]) for v, _ in series], axis=1)
-            fTd = np.stack([flat(g, seg[2]) for _, g in series], axis=1)
-            c["inst"] = (c["ts"], c["tm"], T, Td)
-            c["finst"] = c["force_inst"] = (c["fts"], c["ftm"], fT, fTd)
+            si, sf = slice(2 * N * k, 2 * N * k + N), slice(2 * N * k + N, 2 * N * (k + 1))
+            c["inst"] = (c["ts"], c["tm"], _flat_stack(series, 0, si), _flat_stack(series, 1, si))
+            c["finst"] = c["force_inst"] = (c["fts"], c["ftm"], _flat_stack(series, 0, sf), _flat_stack(series, 1, sf))
             c["dft"], c["ddft"] = dft_matrices(N, c["omega"], c["period"])
-            c["fs"] = np.tile(np.array([self._sigma(sets[k]), -0.0, -0.0]), (N, 1))  # -d/dt of the free stream
-            v0 = series[0][0][seg[2]]
-            c["ref_a"] = (v0 @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
+            c["fs"] = np.tile(np.array([self._chain_params(sets[k])[0], -0.0, -0.0]), (N, 1))  # -d/dt of the free stream
+            c["ref_a"] = (series[0][0][sf] @ np.array([refs[0], 0.0, 0.0, 1.0]))[:, :3]
             c["ref_b"] = None
             if len(refs) > 1:
-                v1 = series[1][0][seg[2]]
-                c["ref_b"] = (v1 @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
-        K = len(cols)
-        self.engine.prepare_batch(H, [c["max_t"] for c in cols], [c["wake_T"] for c in cols],
+                c["ref_b"] = (series[1][0][sf] @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
+        self.engine.prepare_batch_chain(H, [c["max_t"] for c in cols],
+                                  [self._chain_vector(S, c["dt"]) for S, c in zip(sets, cols)],
                                   np.concatenate([c["inst"][0] for c in cols]),
                                   np.concatenate([c["inst"][1] for c in cols]),
                                   np.concatenate([c["inst"][2] for c in cols]),
@@ -357,13 +403,11 @@ class HBVLM3(_HBVLMBase):
     def _sigma(self, S):
         return S["U"] / (self.VARS["b"] * self.VARS["omega_alpha"])
 
-    def _series(self, S, t):
-        """The chain of ``assembly`` for parameter set S at the times t."""
+    def _chain_params(self, S):
+        """The chain of ``assembly``: free stream speed, heave / pitch / control rows, axes; the flap lifts."""
         v = self.VARS
         r = np.asarray(S["dyn"], np.float64)
-        B = fourier_basis(self.m_harmonics, S["omega"], t)
-        return pitch_heave_series(t, self._sigma(S), fourier_dual(r[0], B, t), fourier_dual(r[1], B, t),
-                                  1.0 + v["a"], fourier_dual(r[2], B, t), 1.0 + v["c"])
+        return self._sigma(S), (r[0], r[1], r[2]), 1.0 + v["a"], 1.0 + v["c"], True
 
     def _refs(self):
         return (1.0 + self.VARS["a"], 1.0 + self.VARS["c"])
@@ -405,10 +449,9 @@ class HBVLM2(_HBVLMBase):
     def _sigma(self, S):
         return self.U_INF
 
-    def _series(self, S, t):
+    def _chain_params(self, S):
         r = np.asarray(S["dyn"], np.float64)
-        B = fourier_basis(self.m_harmonics, S["omega"], t)
-        return pitch_heave_series(t, self.U_INF, fourier_dual(r[0], B, t), fourier_dual(r[1], B, t), 1.0 + self.A_H)
+        return self.U_INF, (r[0], r[1], None), 1.0 + self.A_H, None, False
 
     def run(self, omega, dyn_f, forces_t):
         S = dict(omega=omega, dyn=dyn_f, t_start=3.0 * TWO_PI_F / omega)
