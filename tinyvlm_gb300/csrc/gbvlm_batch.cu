@@ -192,13 +192,16 @@ __device__ __forceinline__ int find_sys(const int64_t* pfx, int cnt, int64_t b) 
     return lo;
 }
 
-__global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, const int64_t* tpfx) {
+// tile0: the first tile of this launch (a size group's systems are a
+// contiguous range of tiles)
+__global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
     __shared__ float sw[2][2][3 * BA_W];  // [row][hi/lo][plane*W + s]
-    const int si = find_sys(tpfx, a.nsys, blockIdx.x);
+    const int64_t tile = tile0 + blockIdx.x;
+    const int si = find_sys(tpfx, a.nsys, tile);
     const SysDesc& S = a.sys[si];
     const int64_t ns = S.ns, nc = S.nc, n = S.n;
     const int64_t nchunk = (ns + BA_SPAN - 1) / BA_SPAN, nrb = (n + BA_THREADS - 1) / BA_THREADS;
-    int64_t t = blockIdx.x - tpfx[si];
+    int64_t t = tile - tpfx[si];
     const int64_t rb = t % nrb;
     t /= nrb;
     const int64_t z = t % nchunk, c = t / nchunk;
@@ -539,6 +542,8 @@ struct gbvlm_batch_s {
     int64_t* d_tpfx = nullptr;   // assembly tiles
     int64_t* d_rpfx = nullptr;   // residual tiles
     int64_t assembly_tiles = 0, residual_tiles = 0;
+    std::vector<int64_t> tpfx_host;   // assembly tile prefix over the sorted systems
+    int64_t gtile[4][2] = {};         // per size group: first tile, tiles
     int64_t maxn = 0;
     // the sorted systems in size groups, each factored by its own plan on its
     // own stream (graph branch), so the long step chain of the largest
@@ -597,40 +602,57 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     a.gamma_out = h->d_gamma;
     a.goff = h->d_goff;
     a.uidx = h->d_uidx;
-    mark(0);
-    k_batch_geom<<<h->nsys, 256, 0, st>>>(a);
-    GB_LAUNCH_CHECK();
-    {
+    // staged: every phase after the previous one on `st` (stage timing, or
+    // kernel timing without the groups' launches overlapping); otherwise each
+    // size group's assembly and factorisation run on its own branch, group 0
+    // (the largest systems, the critical path) at high priority, with the
+    // Trefftz kernel and the right-hand sides on the main stream beside them
+    const bool staged = ev != nullptr || serial_lu;
+    auto trefftz = [&]() {
         int64_t maxns = 1;
         for (auto& S : h->sys) maxns = std::max(maxns, S.ns);
         dim3 gk((unsigned)cdiv(maxns * maxns, 128), (unsigned)h->nsys);
         k_batch_trefftz_k<<<gk, 128, 0, st>>>(a);
+        return cudaGetLastError();
+    };
+    mark(0);
+    k_batch_geom<<<h->nsys, 256, 0, st>>>(a);
+    GB_LAUNCH_CHECK();
+    if (staged) GB_CUDA(trefftz());
+    mark(1);
+    if (staged) {
+        k_batch_assemble<<<(unsigned)h->assembly_tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, 0);
         GB_LAUNCH_CHECK();
     }
-    mark(1);
-    k_batch_assemble<<<(unsigned)h->assembly_tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx);
-    GB_LAUNCH_CHECK();
     mark(2);
-    dim3 g((unsigned)cdiv(h->maxn, 256), (unsigned)h->nsys);
-    k_batch_rhs<<<g, 256, 0, st>>>(a);
-    GB_LAUNCH_CHECK();
+    dim3 gp((unsigned)cdiv(h->maxn, 256), (unsigned)h->nsys);  // one thread per row of every system
+    if (staged) {
+        k_batch_rhs<<<gp, 256, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+    }
     mark(3);
-    // group 0 (the largest systems) on a high-priority side stream, the
-    // others beside it; the main stream waits for all of them
-    if (serial_lu) {
+    if (staged) {
         for (int g = 0; g < h->ngroups; g++) {
-            int rc = lu_batch_factor<float>(h->lub, h->plans[g], st, false);
+            int rc = lu_batch_factor<float>(h->lub, h->plans[g], st, !serial_lu);
             if (rc) return rc;
         }
     } else {
         GB_CUDA(cudaEventRecord(h->fork, st));
         for (int g = 0; g < h->ngroups; g++) {
             GB_CUDA(cudaStreamWaitEvent(h->side[g], h->fork, 0));
+            if (h->gtile[g][1] > 0) {
+                k_batch_assemble<<<(unsigned)h->gtile[g][1], BA_THREADS, 0, h->side[g]>>>(a, h->d_tpfx,
+                                                                                       h->gtile[g][0]);
+                GB_LAUNCH_CHECK();
+            }
             int rc = lu_batch_factor<float>(h->lub, h->plans[g], h->side[g], true);
             if (rc) return rc;
             GB_CUDA(cudaEventRecord(h->join[g], h->side[g]));
         }
-        for (int g = 0; g < h->ngroups; g++) GB_CUDA(cudaStreamWaitEvent(st, h->join[g], 0));
+        GB_CUDA(trefftz());
+        k_batch_rhs<<<gp, 256, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+        for (int gi = 0; gi < h->ngroups; gi++) GB_CUDA(cudaStreamWaitEvent(st, h->join[gi], 0));
     }
     int rc = GBVLM_OK;
     mark(4);
@@ -643,7 +665,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     };
     rc = solve();
     if (rc) return rc;
-    k_batch_accum<<<g, 256, 0, st>>>(a);
+    k_batch_accum<<<gp, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
     for (int it = 0; it < h->refine; it++) {
         k_batch_residual<<<dim3((unsigned)h->residual_tiles, (unsigned)cdiv(maxrhs, RS_MAXRHS)), RS_THREADS, 0, st>>>(
@@ -651,7 +673,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         GB_LAUNCH_CHECK();
         rc = solve();
         if (rc) return rc;
-        k_batch_accum<<<g, 256, 0, st>>>(a);
+        k_batch_accum<<<gp, 256, 0, st>>>(a);
         GB_LAUNCH_CHECK();
     }
     mark(5);
@@ -772,6 +794,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         rpfx[k + 1] = rpfx[k] + cdiv(n, RS_THREADS);
     }
     h->assembly_tiles = tpfx[h->nsys];
+    h->tpfx_host = tpfx;
     h->residual_tiles = rpfx[h->nsys];
     const size_t o_tpfx = reserve(sizeof(int64_t) * tpfx.size());
     const size_t o_rpfx = reserve(sizeof(int64_t) * rpfx.size());
@@ -913,6 +936,8 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
             while (i1 < h->nsys && (g == MAX_GROUPS_B || lun[i1] > bounds[g])) i1++;
             if (i1 == i0) continue;
             const int gi = h->ngroups++;
+            h->gtile[gi][0] = h->tpfx_host[i0];
+            h->gtile[gi][1] = h->tpfx_host[i1] - h->tpfx_host[i0];
             std::vector<int64_t> ns(lun.begin() + i0, lun.begin() + i1);
             rc = lu_plan_build(h->plans[gi], ns, 0, i0);
             if (rc == GBVLM_OK) {
