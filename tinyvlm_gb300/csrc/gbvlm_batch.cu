@@ -310,7 +310,8 @@ __global__ void k_batch_accum(BatchArgs a) {
 // where the fp64 units of this part run at a small fraction of the fp32 rate.
 constexpr int RS_THREADS = 128;
 constexpr int RS_MAXRHS = 8;  // (the inner loop reads them as two float4)
-constexpr int RS_CB = 32;  // columns of Xd staged per step
+constexpr int RS_CB = 16;  // columns of Xd staged per step
+constexpr int RS_ROWS = 2;  // rows per thread
 
 // (sh, sl) += a * (xh + xl)
 __device__ __forceinline__ void df_mac(float& sh, float& sl, float a, float xh, float xl) {
@@ -328,16 +329,26 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
     __shared__ __align__(16) float xl[RS_CB][RS_MAXRHS];
     const int si = find_sys(rpfx, a.nsys, blockIdx.x);
     const SysDesc& S = a.sys[si];
-    const int64_t r = (blockIdx.x - rpfx[si]) * RS_THREADS + threadIdx.x;
+    // RS_ROWS rows per thread, RS_THREADS apart: each staged value of X is
+    // read once from shared memory for all of them
+    const int64_t r0 = (blockIdx.x - rpfx[si]) * (RS_THREADS * RS_ROWS) + threadIdx.x;
     const int64_t n = S.n;
-    const bool rv = r < n;
-    const float* arow = S.A2 + (rv ? r : 0);
+    bool rv[RS_ROWS];
+    const float* arow[RS_ROWS];
+#pragma unroll
+    for (int k = 0; k < RS_ROWS; k++) {
+        const int64_t r = r0 + k * RS_THREADS;
+        rv[k] = r < n;
+        arow[k] = S.A2 + (rv[k] ? r : 0);
+    }
     // grid.y: blocks of RS_MAXRHS right-hand sides
     for (int q0 = blockIdx.y * RS_MAXRHS; q0 < S.nrhs; q0 += RS_MAXRHS * gridDim.y) {
         const int nq = min(RS_MAXRHS, S.nrhs - q0);
-        float sh[RS_MAXRHS], sl[RS_MAXRHS];
+        float sh[RS_ROWS][RS_MAXRHS], sl[RS_ROWS][RS_MAXRHS];
 #pragma unroll
-        for (int q = 0; q < RS_MAXRHS; q++) sh[q] = sl[q] = 0.f;
+        for (int k = 0; k < RS_ROWS; k++)
+#pragma unroll
+            for (int q = 0; q < RS_MAXRHS; q++) sh[k][q] = sl[k][q] = 0.f;
         for (int64_t c0 = 0; c0 < n; c0 += RS_CB) {
             __syncthreads();
             for (int e = threadIdx.x; e < RS_CB * RS_MAXRHS; e += RS_THREADS) {
@@ -348,11 +359,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
                 xl[cc][q] = (float)(v - (double)h);
             }
             __syncthreads();
-            if (rv) {
+            if (rv[0]) {
                 const int cn = (int)min((int64_t)RS_CB, n - c0);
-                float av[RS_CB];
+                float av[RS_ROWS][RS_CB];
 #pragma unroll
-                for (int cc = 0; cc < RS_CB; cc++) av[cc] = cc < cn ? arow[(c0 + cc) * n] : 0.f;
+                for (int k = 0; k < RS_ROWS; k++)
+#pragma unroll
+                    for (int cc = 0; cc < RS_CB; cc++) av[k][cc] = (cc < cn && rv[k]) ? arow[k][(c0 + cc) * n] : 0.f;
 #pragma unroll
                 for (int cc = 0; cc < RS_CB; cc++) {
                     // the 8 hi and 8 lo values of column cc as four 16-byte broadcasts
@@ -363,15 +376,20 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
                     const float hh[RS_MAXRHS] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
                     const float ll[RS_MAXRHS] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
 #pragma unroll
-                    for (int q = 0; q < RS_MAXRHS; q++) df_mac(sh[q], sl[q], av[cc], hh[q], ll[q]);
+                    for (int k = 0; k < RS_ROWS; k++)
+#pragma unroll
+                        for (int q = 0; q < RS_MAXRHS; q++) df_mac(sh[k][q], sl[k][q], av[k][cc], hh[q], ll[q]);
                 }
             }
         }
-        if (rv) {
+#pragma unroll
+        for (int k = 0; k < RS_ROWS; k++) {
+            if (!rv[k]) continue;
+            const int64_t r = r0 + k * RS_THREADS;
 #pragma unroll
             for (int q = 0; q < RS_MAXRHS; q++) {
                 if (q < nq) {
-                    const double res = S.B[r + (q0 + q) * n] - ((double)sh[q] + (double)sl[q]);
+                    const double res = S.B[r + (q0 + q) * n] - ((double)sh[k][q] + (double)sl[k][q]);
                     S.R[r + (q0 + q) * n] = res;
                     S.X[r + (q0 + q) * n] = (float)res;
                 }
@@ -791,7 +809,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         const gbvlm_dims& d = dims[protos[order[k]].case_id];
         const int64_t n = protos[order[k]].n;
         tpfx[k + 1] = tpfx[k] + cdiv(n, BA_THREADS) * cdiv(d.ns, BA_SPAN) * d.nc;
-        rpfx[k + 1] = rpfx[k] + cdiv(n, RS_THREADS);
+        rpfx[k + 1] = rpfx[k] + cdiv(n, RS_THREADS * RS_ROWS);
     }
     h->assembly_tiles = tpfx[h->nsys];
     h->tpfx_host = tpfx;
