@@ -310,7 +310,7 @@ __global__ void k_batch_accum(BatchArgs a) {
 // where the fp64 units of this part run at a small fraction of the fp32 rate.
 constexpr int RS_THREADS = 128;
 constexpr int RS_MAXRHS = 8;  // (the inner loop reads them as two float4)
-constexpr int RS_CB = 16;  // columns of Xd staged per step
+constexpr int RS_CB = 8;  // columns of Xd staged per step
 constexpr int RS_ROWS = 2;  // rows per thread
 
 // (sh, sl) += a * (xh + xl)
