@@ -1450,7 +1450,6 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
     int* d_iters = act + K;
     int* ctl = d_iters + K;
     int* hctl = (int*)host_scratch(sizeof(int));
-    auto fail = [&](int r) { return r; };
     auto check = [&](const char* what) {
         cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? GBVLM_OK : cuda_fail(e, what, __FILE__, __LINE__);
@@ -1459,27 +1458,27 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
     const unsigned g1 = (unsigned)std::min<int64_t>(cdiv(L, 256), 1024);
     if (cudaMemcpyAsync(S.Xin.p, x, sizeof(double) * L * K, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemsetAsync(buf, 0, sizeof(double) * per * K, st) != cudaSuccess)
-        return fail(cuda_fail(cudaGetLastError(), "Anderson setup", __FILE__, __LINE__));
+        return cuda_fail(cudaGetLastError(), "Anderson setup", __FILE__, __LINE__);
     k_fill_i32<<<1, 256, 0, st>>>(act, K, 1);
     k_fill_i32<<<1, 256, 0, st>>>(d_iters, K, 0);
     // vlm_solvers.cpp:49-66: g0 = f(x0) - x0; X0 = g0; x1 = f(x0); g1 = f(x1) - x1; G0 = g1 - g0
-    if ((rc = map())) return fail(rc);
+    if ((rc = map())) return rc;
     k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, -1, S.Xout.p, S.Xin.p, buf, dnorm, act, nullptr);
     k_anderson_first<<<dim3(g1, K), 256, 0, st>>>(L, m, S.Xout.p, S.Xin.p, buf);
-    if ((rc = check("Anderson")) || (rc = map())) return fail(rc);
+    if ((rc = check("Anderson")) || (rc = map())) return rc;
     k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, 0, S.Xout.p, S.Xin.p, buf, dnorm, act, nullptr);
-    if ((rc = check("Anderson"))) return fail(rc);
+    if ((rc = check("Anderson"))) return rc;
     // the QR's columns in shared memory when m of them and g fit
     const size_t smem = sizeof(double) * (size_t)L * (m + 1);
     const int use_smem = smem <= 200 * 1024 ? 1 : 0;
     if (use_smem && cudaFuncSetAttribute(k_anderson_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                         cudaSuccess)
-        return fail(cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__));
+        return cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__);
     int k = 1;
     if (S.anderson_graph_ok()) {  // the whole loop on the device
         k_fill_i32<<<1, 32, 0, st>>>(ctl, 1, 1);
         if ((rc = anderson_graph(S, K, L, m, max_iter, tol, buf, dnorm, act, d_iters, ctl, use_smem, smem)))
-            return fail(rc);
+            return rc;
         GB_CUDA(cudaGraphLaunch(S.aa_exec, st));
         k = max_iter;  // the host loop below does not run
     }
@@ -1487,14 +1486,14 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
         k_anderson_check<<<1, 32, 0, st>>>(K, dnorm, tol, k, act, d_iters, ctl);
         if (cudaMemcpyAsync(hctl, ctl, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
-            return fail(cuda_fail(cudaGetLastError(), "Anderson norm", __FILE__, __LINE__));
+            return cuda_fail(cudaGetLastError(), "Anderson norm", __FILE__, __LINE__);
         if (*hctl == 0) break;
         const int mk = std::min(m, k), slot = k % m;
         k_anderson_step<<<K, AA_STEP_THREADS, use_smem ? smem : 0, st>>>(L, m, mk, slot, buf, S.Xin.p, act,
                                                                           use_smem, nullptr);
-        if ((rc = check("Anderson")) || (rc = map())) return fail(rc);
+        if ((rc = check("Anderson")) || (rc = map())) return rc;
         k_anderson_post<<<K, AA_THREADS, 0, st>>>(L, m, slot, S.Xout.p, S.Xin.p, buf, dnorm, act, nullptr);
-        if ((rc = check("Anderson"))) return fail(rc);
+        if ((rc = check("Anderson"))) return rc;
         k++;
     }
     k_anderson_finish<<<1, 256, 0, st>>>(K, k, act, d_iters, S.anderson_graph_ok() ? ctl : nullptr);
@@ -1502,7 +1501,7 @@ int gbvlm_hbvlm_solve_batch(gbvlm_hbvlm h, int32_t K, double* x, const double* o
     if (cudaMemcpyAsync(x, S.Xin.p, sizeof(double) * L * K, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(hit.data(), d_iters, sizeof(int) * K, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
-        return fail(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__));
+        return cuda_fail(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__);
     if (iters)
         for (int c = 0; c < K; c++) iters[c] = hit[c];
     return GBVLM_OK;
