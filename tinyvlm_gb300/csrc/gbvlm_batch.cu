@@ -606,7 +606,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     for (int g = 0; g < h->ngroups; g++) nlaunch += lu_plan_launches(h->plans[g], 4);
     int32_t mr = 0;
     for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
-    const int64_t solves = (mr + 7) / 8;
+    const int64_t solves = h->use_flow ? trs_flow_launches(mr, h->flow.groups) : (mr + 7) / 8;
     h->launches = 5 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
     BatchArgs a;
     a.sys = h->d_sys;
@@ -972,13 +972,14 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         }
     }
     if (rc == GBVLM_OK) {
-        // a single large system solves faster in 128-row blocks on the tensor
-        // cores with every right-hand side at once (its dataflow chain would be
-        // the whole solve); up to that size a system gives the same bits alone
-        // and inside any batch
+        // every system and every block of 8 right-hand sides in one dataflow
+        // launch; GBVLM_TRS_FLOW=0 selects the per-system solves (k_trsolve,
+        // or 128-row blocks on the tensor cores for one large system)
         const char* fe = getenv("GBVLM_TRS_FLOW");
-        h->use_flow = !(fe && fe[0] == '0') && (h->nsys > 1 || h->maxn <= 4096);
-        if (h->use_flow) rc = trs_flow_build(h->flow, lun, 0);
+        h->use_flow = !(fe && fe[0] == '0');
+        int32_t mr = 1;
+        for (auto& sy : h->sys) mr = std::max(mr, sy.nrhs);
+        if (h->use_flow) rc = trs_flow_build(h->flow, lun, 0, (mr + 7) / 8);
     }
     if (rc) {
         delete h;

@@ -1039,6 +1039,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_trsolve(LuBatch<T> B, int32_t rh
 // 32-row steps.
 // ---------------------------------------------------------------------------
 constexpr int FL_B = 128;
+constexpr int FL_SYS_BITS = 20, FL_SYS_MASK = (1 << FL_SYS_BITS) - 1;  // item: system | group << 20
 constexpr int FL_THREADS = 256;
 constexpr int FL_R = 8;  // right-hand sides per launch
 constexpr int FL_LD = FL_B + 4;  // rows 16-byte aligned: a lane reads its row as float4, conflict-free
@@ -1140,8 +1141,10 @@ __device__ __forceinline__ void flow_invert_tri(float* Ld, int sb, int nb, bool 
     else flow_invert_upper(T, min(32, nb - sb * 32), lane);
 }
 
-// ctl: [0] dispatch counter, [1] error word, [2, 2 + nsys) forward blocks
-// finished per system, [2 + nsys, 2 + 2 nsys) backward blocks finished
+// ctl: [0] dispatch counter, [1] error word, then per group g of FL_R
+// right-hand sides: [2 + 2 g nsys, + nsys) forward blocks finished per
+// system, [2 + (2 g + 1) nsys, + nsys) backward blocks finished.  An item's
+// x holds its system in the low 20 bits and its group above them.
 __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, const int2* items, int nfwd, int nitems,
                                                             int nsys, int* ctl, float* const* Yp, int32_t rhs0) {
     extern __shared__ __align__(16) float fsm[];
@@ -1161,17 +1164,19 @@ __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, co
         if (it >= nitems) return;
         const bool fwd = it < nfwd;
         const int2 w = items[it];
-        const int s = w.x, bi = w.y;
-        const int nr = min(FL_R, B.nrhs[s] - rhs0);
+        const int s = w.x & FL_SYS_MASK, grp = w.x >> FL_SYS_BITS, bi = w.y;
+        const int32_t r0 = rhs0 + grp * FL_R;
+        int* gctl = ctl + 2 * (int64_t)grp * nsys;  // this group's progress words at gctl + 2
+        const int nr = min(FL_R, B.nrhs[s] - r0);
         if (nr <= 0) continue;  // no right-hand side of this launch: no item of the system waits
         const int64_t n = B.n[s], ld = B.ld[s], ldx = B.ldx[s];
         const int nblk = (int)((n + FL_B - 1) / FL_B);
         const int64_t R0 = (int64_t)bi * FL_B;
         const int nb = (int)min((int64_t)FL_B, n - R0);
         const float* A = B.A[s];
-        float* Y = Yp[s];  // n x FL_R, row-major: y (forward), then x (backward)
-        float* X = B.X[s] + (int64_t)rhs0 * ldx;
-        int* done = ctl + 2 + (fwd ? 0 : nsys) + s;
+        float* Y = Yp[(int64_t)grp * nsys + s];  // n x FL_R, row-major: y (forward), then x (backward)
+        float* X = B.X[s] + (int64_t)r0 * ldx;
+        int* done = gctl + 2 + (fwd ? 0 : nsys) + s;
         // diagonal block: the strict lower triangle (forward) or the upper one
         // with the diagonal (backward), zero elsewhere
         for (int e = tid; e < FL_B * FL_B; e += FL_THREADS) {
@@ -1200,7 +1205,7 @@ __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, co
                 }
             }
         } else {
-            if (!flow_wait(ctl + 2 + s, bi, err, &s_ok)) break;  // y_i
+            if (!flow_wait(gctl + 2 + s, bi, err, &s_ok)) break;  // y_i
             if (cq == 0) {
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
@@ -2140,10 +2145,13 @@ int64_t lu_plan_launches(const LuPlan& plan, int es) {
     return n + (plan.nsys > 0);  // + the permutation kernel
 }
 
-int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st) {
+int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st, int32_t groups) {
     f.release();
     f.nsys = (int32_t)n_sorted.size();
+    f.groups = std::max(1, groups);
     if (f.nsys == 0) return GBVLM_OK;
+    GB_REQUIRE(f.nsys <= FL_SYS_MASK + 1 && f.groups <= 1024, "dataflow solve: %d systems, %d groups", f.nsys,
+               f.groups);
     std::vector<int32_t> nblk(f.nsys);
     int32_t maxblk = 0;
     int64_t rows = 0;
@@ -2154,13 +2162,17 @@ int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_
         rows += n_sorted[s];
     }
     // forward items by block level, backward items by distance from the last
-    // block; within a level the largest systems (longest chains) first
+    // block; within a level the groups of right-hand sides, then the largest
+    // systems (longest chains) first
     std::vector<int2> items;
     for (int32_t i = 0; i < maxblk; i++)
-        for (int32_t s = 0; s < f.nsys && nblk[s] > i; s++) items.push_back(make_int2(s, i));
+        for (int32_t g = 0; g < f.groups; g++)
+            for (int32_t s = 0; s < f.nsys && nblk[s] > i; s++) items.push_back(make_int2(s | (g << FL_SYS_BITS), i));
     f.nfwd = (int32_t)items.size();
     for (int32_t d = 0; d < maxblk; d++)
-        for (int32_t s = 0; s < f.nsys && nblk[s] > d; s++) items.push_back(make_int2(s, nblk[s] - 1 - d));
+        for (int32_t g = 0; g < f.groups; g++)
+            for (int32_t s = 0; s < f.nsys && nblk[s] > d; s++)
+                items.push_back(make_int2(s | (g << FL_SYS_BITS), nblk[s] - 1 - d));
     f.nitems = (int32_t)items.size();
     GB_CUDA(cudaFuncSetAttribute(k_trs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, FL_SMEM));
     int dev = 0, sms = 0, per_sm = 0;
@@ -2169,31 +2181,37 @@ int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trs_flow, FL_THREADS, FL_SMEM));
     GB_REQUIRE(per_sm > 0, "dataflow solve: kernel does not fit on an SM");
     f.grid = (int32_t)std::min<int64_t>((int64_t)sms * per_sm, f.nitems);
-    std::vector<float*> yp(f.nsys);
+    const size_t G = (size_t)f.groups;
+    std::vector<float*> yp(G * f.nsys);
     GB_CUDA(cudaMalloc(&f.d_items, sizeof(int2) * items.size()));
-    GB_CUDA(cudaMalloc(&f.d_ctl, sizeof(int32_t) * (2 + 2 * (size_t)f.nsys)));
-    GB_CUDA(cudaMalloc(&f.d_y, sizeof(float) * FL_R * (size_t)rows));
-    GB_CUDA(cudaMalloc(&f.d_yp, sizeof(float*) * f.nsys));
+    GB_CUDA(cudaMalloc(&f.d_ctl, sizeof(int32_t) * (2 + 2 * G * f.nsys)));
+    GB_CUDA(cudaMalloc(&f.d_y, sizeof(float) * FL_R * G * (size_t)rows));
+    GB_CUDA(cudaMalloc(&f.d_yp, sizeof(float*) * G * f.nsys));
     int64_t off = 0;
-    for (int32_t s = 0; s < f.nsys; s++) {
-        yp[s] = f.d_y + off;
-        off += FL_R * n_sorted[s];
-    }
+    for (size_t g = 0; g < G; g++)
+        for (int32_t s = 0; s < f.nsys; s++) {
+            yp[g * f.nsys + s] = f.d_y + off;
+            off += FL_R * n_sorted[s];
+        }
     GB_CUDA(cudaMemcpyAsync(f.d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, st));
     GB_CUDA(cudaMemcpyAsync(f.d_yp, yp.data(), sizeof(float*) * yp.size(), cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemsetAsync(f.d_ctl, 0, sizeof(int32_t) * (2 + 2 * (size_t)f.nsys), st));
+    GB_CUDA(cudaMemsetAsync(f.d_ctl, 0, sizeof(int32_t) * (2 + 2 * G * f.nsys), st));
     GB_CUDA(cudaStreamSynchronize(st));  // the host tables above are about to go out of scope
     return GBVLM_OK;
 }
 
-int64_t trs_flow_launches(int32_t max_nrhs) { return (max_nrhs + FL_R - 1) / FL_R; }
+int64_t trs_flow_launches(int32_t max_nrhs, int32_t groups) {
+    const int32_t per = FL_R * std::max(1, groups);  // right-hand sides one launch covers
+    return (max_nrhs + per - 1) / per;
+}
 
 int trs_flow_solve(const LuBatch<float>& B, const TrsFlow& f, int32_t max_nrhs, cudaStream_t st) {
     if (f.nitems == 0) return GBVLM_OK;
-    for (int32_t r0 = 0; r0 < max_nrhs; r0 += FL_R) {
+    const int32_t per = FL_R * f.groups;
+    for (int32_t r0 = 0; r0 < max_nrhs; r0 += per) {
         // the counter and progress words restart; the error word is kept
         GB_CUDA(cudaMemsetAsync(f.d_ctl, 0, sizeof(int32_t), st));
-        GB_CUDA(cudaMemsetAsync(f.d_ctl + 2, 0, sizeof(int32_t) * 2 * (size_t)f.nsys, st));
+        GB_CUDA(cudaMemsetAsync(f.d_ctl + 2, 0, sizeof(int32_t) * 2 * (size_t)f.groups * f.nsys, st));
         k_trs_flow<<<f.grid, FL_THREADS, FL_SMEM, st>>>(B, f.d_items, f.nfwd, f.nitems, f.nsys, f.d_ctl, f.d_yp, r0);
         GB_LAUNCH_CHECK();
     }

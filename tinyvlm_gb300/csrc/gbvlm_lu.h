@@ -112,6 +112,7 @@ int lu_batch_solve(const LuBatch<T>& B, int32_t nsys, int32_t max_nrhs, int64_t 
 // system in 128-row blocks, items handed out in dependency order.
 struct TrsFlow {
     int32_t nsys = 0, nfwd = 0, nitems = 0, grid = 0;
+    int32_t groups = 1;        // blocks of FL_R right-hand sides solved by one launch
     int2* d_items = nullptr;   // (system, block) in dispatch order
     int32_t* d_ctl = nullptr;  // counter, error word, per-system forward and backward progress
     float* d_y = nullptr;      // per system n x 8 row-major
@@ -122,10 +123,11 @@ struct TrsFlow {
     TrsFlow(const TrsFlow&) = delete;
     TrsFlow& operator=(const TrsFlow&) = delete;
 };
-// n_sorted: sizes of all systems of the batch, in batch order
-int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st);
+// n_sorted: sizes of all systems of the batch, in batch order; groups: how
+// many blocks of 8 right-hand sides one launch solves side by side
+int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st, int32_t groups = 1);
 int trs_flow_solve(const LuBatch<float>& B, const TrsFlow& f, int32_t max_nrhs, cudaStream_t st);
-int64_t trs_flow_launches(int32_t max_nrhs);
+int64_t trs_flow_launches(int32_t max_nrhs, int32_t groups = 1);
 // GBVLM_OK, or an error if a wait of the last solve ran out (synchronises st)
 int trs_flow_check(const TrsFlow& f, cudaStream_t st);
 
