@@ -238,7 +238,7 @@ struct VlmState : VlmBase {
             GB_CUDA(cudaStreamSynchronize(st));
             for (int64_t i = 0; i < n; i++) gamma_out[i] = (double)h[i];
         }
-        return GBVLM_OK;
+        return lu_solve_check(lu, st);  // the solve finished its bounded waits
     }
 };
 

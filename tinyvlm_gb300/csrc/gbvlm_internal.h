@@ -47,6 +47,9 @@ int device_scratch(size_t bytes, void** out, cudaStream_t s);
 int lu_solve_prepare_f32(gbvlm_lu h, const float* A, int64_t n, float* X, void** tables, cudaStream_t st);
 int lu_solve_prepared_f32(gbvlm_lu h, void* tables, int64_t n, cudaStream_t st);
 void lu_solve_tables_free(void* tables);
+// GBVLM_OK, or an error if a bounded wait of a float solve since the last
+// factorisation ran out (synchronises st)
+int lu_solve_check(gbvlm_lu h, cudaStream_t st);
 // rhs -= wake influence with *it_dev active ring rows per lifting wake
 // (it_dev <= it_max); scratch of WAKE_DEV_MAX_SLICES x (total panels) floats
 constexpr int64_t WAKE_DEV_MAX_SLICES = 608;

@@ -2348,7 +2348,31 @@ struct gbvlm_lu_s {
     int64_t plan_n = -1;
     void* work = nullptr;
     size_t work_bytes = 0;
+    // float solves: the dataflow solve of the one system, built for flow_n
+    // unknowns and flow_groups blocks of 8 right-hand sides
+    TrsFlow flow;
+    int64_t flow_n = -1;
+    int32_t flow_groups = 0;
 };
+
+// the dataflow solve for nrhs right-hand sides of the handle's system, built
+// on first use; false for systems of up to two 128-row blocks (one CTA's
+// k_trsolve has no chain to overlap there: measured faster in the coupled
+// 2 x 2 + 2 x 2 panel time step) or when GBVLM_TRS_FLOW=0 selects the
+// per-system solves
+static int lu_flow_ready(gbvlm_lu h, int64_t n, int64_t nrhs, cudaStream_t st, bool* use) {
+    const char* fe = getenv("GBVLM_TRS_FLOW");
+    *use = !(fe && fe[0] == '0') && n > 2 * FL_B;
+    if (!*use) return GBVLM_OK;
+    const int32_t groups = (int32_t)((nrhs + 7) / 8);
+    if (h->flow_n == n && h->flow_groups >= groups) return GBVLM_OK;
+    h->flow_n = -1;
+    int rc = trs_flow_build(h->flow, std::vector<int64_t>{n}, st, groups);
+    if (rc) return rc;
+    h->flow_n = n;
+    h->flow_groups = groups;
+    return GBVLM_OK;
+}
 
 static int lu_ensure(gbvlm_lu h, int64_t n, cudaStream_t st) {
     if (h->plan_n == n && h->d_ipiv) return GBVLM_OK;
@@ -2387,6 +2411,7 @@ static int lu_factor_one(gbvlm_lu h, T* A, int64_t n, int64_t ld, cudaStream_t s
         set_error("LU: exactly zero pivot at column %d", *hi);
         return GBVLM_ERR_SINGULAR;
     }
+    if (h->flow_n >= 0 && (rc = trs_flow_check(h->flow, st))) return rc;  // a solve since the last factorisation
     return lu_plan_check(h->plan, st);
 }
 
@@ -2399,6 +2424,11 @@ static int lu_solve_one(gbvlm_lu h, const T* A, int64_t n, int64_t ld, T* X, int
     int rc = make_single_batch<T>(B, n, ld, (T*)A, h->d_ipiv, h->d_perm, h->d_info, X, ldx, (int32_t)nrhs,
                                   &h->work, &h->work_bytes, st);
     if (rc) return rc;
+    if constexpr (std::is_same<T, float>::value) {
+        bool flow = false;
+        if ((rc = lu_flow_ready(h, n, nrhs, st, &flow))) return rc;
+        if (flow) return trs_flow_solve(B, h->flow, (int32_t)nrhs, st);
+    }
     return lu_batch_solve<T>(B, 1, (int32_t)nrhs, n, st, h->plan.tc_passes ? h->plan.d_err : nullptr);
 }
 
@@ -2408,6 +2438,7 @@ struct LuSolveTables {
     LuBatch<float> B;
     void* work = nullptr;
     size_t work_bytes = 0;
+    bool flow = false;  // the handle's dataflow solve (built at prepare) serves the solves
 };
 
 int lu_solve_prepare_f32(gbvlm_lu h, const float* A, int64_t n, float* X, void** tables, cudaStream_t st) {
@@ -2416,6 +2447,7 @@ int lu_solve_prepare_f32(gbvlm_lu h, const float* A, int64_t n, float* X, void**
     auto* t = new LuSolveTables();
     int rc = make_single_batch<float>(t->B, n, n, (float*)A, h->d_ipiv, h->d_perm, h->d_info, X, n, 1, &t->work,
                                       &t->work_bytes, st);
+    if (!rc) rc = lu_flow_ready(h, n, 1, st, &t->flow);
     if (rc) {
         lu_solve_tables_free(t);
         return rc;
@@ -2427,7 +2459,13 @@ int lu_solve_prepare_f32(gbvlm_lu h, const float* A, int64_t n, float* X, void**
 int lu_solve_prepared_f32(gbvlm_lu h, void* tables, int64_t n, cudaStream_t st) {
     GB_REQUIRE(h && tables, "null argument");
     const LuSolveTables* t = (const LuSolveTables*)tables;
+    if (t->flow && h->flow_n == n) return trs_flow_solve(t->B, h->flow, 1, st);
     return lu_batch_solve<float>(t->B, 1, 1, n, st, h->plan.tc_passes ? h->plan.d_err : nullptr);
+}
+
+int lu_solve_check(gbvlm_lu h, cudaStream_t st) {
+    GB_REQUIRE(h, "null argument");
+    return h->flow_n >= 0 ? trs_flow_check(h->flow, st) : GBVLM_OK;
 }
 
 void lu_solve_tables_free(void* tables) {

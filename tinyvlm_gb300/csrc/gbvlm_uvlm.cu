@@ -400,7 +400,7 @@ struct UvlmState : UvlmBase {
         GB_CUDA(cudaStreamSynchronize(st));
         if (cl) *cl = h[0];
         if (cm) for (int k = 0; k < 3; k++) cm[k] = h[1 + k];
-        return GBVLM_OK;
+        return lu_solve_check(lu, st);  // the steps' solves finished their bounded waits
     }
 
     int results(double* cl, double* cm, double* gamma_last, cudaStream_t st) override {
@@ -423,7 +423,7 @@ struct UvlmState : UvlmBase {
         }
         if (gamma_last)
             for (int64_t q = 0; q < n; q++) gamma_last[q] = (double)g[q];
-        return GBVLM_OK;
+        return lu_solve_check(lu, st);  // the steps' solves finished their bounded waits
     }
 };
 
