@@ -607,7 +607,9 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     int32_t mr = 0;
     for (auto& s : h->sys) mr = std::max(mr, s.nrhs);
     const int64_t solves = h->use_flow ? trs_flow_launches(mr, h->flow.groups) : (mr + 7) / 8;
-    h->launches = 5 + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
+    // geometry, Trefftz, the groups' assemblies, RHS, the factorisations, the
+    // solves and accumulations, the refinement sweeps, the loads
+    h->launches = 3 + h->ngroups + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
     BatchArgs a;
     a.sys = h->d_sys;
     a.nsys = h->nsys;
