@@ -1,11 +1,13 @@
 """Dataflow triangular solves of the batched solver (k_trs_flow: one
-persistent launch per 8 right-hand sides, 128-row blocks of every system
-handed out in dependency order) against the one-CTA-per-system solve
-(GBVLM_TRS_FLOW=0) and the double oracle.
+persistent launch, 128-row blocks of every system and every group of 8
+right-hand sides handed out in dependency order) against the per-system
+solves (GBVLM_TRS_FLOW=0) and the double oracle.
 
 Sizes sit on both sides of the 128-row block edges (last blocks of 1, 127
 and 128 rows, single-block systems, 10 blocks) and 11 angles make two
-launches per solve, the second with 3 right-hand sides."""
+groups of right-hand sides, the second with 3.  A single system of 4560
+unknowns with 20 angles (three groups) runs against the blocked
+tensor-core solve it replaced."""
 import os
 
 import numpy as np
@@ -83,3 +85,16 @@ def test_flow_replay_is_deterministic(cuda):
         bs.run()
         b, _ = bs.results()
         np.testing.assert_array_equal(a, b)
+
+
+def test_flow_single_large_system_groups(cuda):
+    rng = np.random.default_rng(11)
+    v = M.trapezoid(24, 190, 9.0, 0.6, 20.0)
+    M.quarter_chord(v)
+    cases = [M.Case(v.astype(np.float32), np.radians(rng.uniform(-8, 8, size=20)), {})]
+    assert cases[0].n == 4560
+    co_f, g_f = _solve(cases, True, 1)
+    co_s, g_s = _solve(cases, False, 1)
+    for a, b in zip(g_f, g_s):
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b) + 1e-7
+    np.testing.assert_allclose(co_f[:, 0], co_s[:, 0], rtol=1e-5, atol=1e-7)

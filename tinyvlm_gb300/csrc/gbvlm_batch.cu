@@ -407,17 +407,6 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 // ---------------------------------------------------------------------------
 constexpr int LD_THREADS = 256;
 
-__device__ double block_sum_d(double v, double* sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    double r = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); k++) r += sh[k];
-    return r;
-}
-
 __device__ __forceinline__ V3<double> bs_d(V3<double> c, V3<double> a, V3<double> b) {
     // double Biot-Savart (same law, reference cut-offs), unscaled by 1/4pi
     V3<double> r1 = c - a, r2 = c - b, r0 = b - a;
@@ -453,7 +442,6 @@ __global__ void k_batch_trefftz_k(BatchArgs a) {
 }
 
 __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const int32_t* solve_sys, int32_t want_gamma) {
-    __shared__ double sh[32];
     const int32_t sol = blockIdx.x;
     const int32_t si = solve_sys[sol];
     const SysDesc& S = a.sys[si];
@@ -511,11 +499,24 @@ __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const i
         const int64_t j = e % ns, jj = e / ns;
         cd += gte[j] * S.K[e] * gte[jj];
     }
-    const double s_cl = block_sum_d(cl, sh), s_x = block_sum_d(cmx, sh);
-    const double s_y = block_sum_d(cmy, sh), s_z = block_sum_d(cmz, sh);
-    const double s_ar = block_sum_d(ar, sh), s_mac = block_sum_d(mac, sh);
-    const double s_cd = block_sum_d(cd, sh);
+    // the seven sums in one pass: each reduced down its warp, then the warps'
+    // partial sums added in warp order by thread 0
+    __shared__ double sh7[7][LD_THREADS / 32];
+    double vals[7] = {cl, cmx, cmy, cmz, ar, mac, cd};
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+        for (int o = 16; o > 0; o >>= 1) vals[k] += __shfl_down_sync(0xffffffffu, vals[k], o);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 7; k++) sh7[k][threadIdx.x >> 5] = vals[k];
+    __syncthreads();
     if (threadIdx.x == 0) {
+        double t[7];
+        for (int k = 0; k < 7; k++) {
+            t[k] = 0;
+            for (int w = 0; w < LD_THREADS / 32; w++) t[k] += sh7[k][w];
+        }
+        const double s_cl = t[0], s_x = t[1], s_y = t[2], s_z = t[3], s_ar = t[4], s_mac = t[5], s_cd = t[6];
         const double v2 = len2(V);
         const double macv = s_mac / s_ar;
         double* o = a.out + 5 * (int64_t)a.uidx[sol];
