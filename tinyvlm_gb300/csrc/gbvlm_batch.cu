@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 // and moment terms in float (this part's fp64 rate is a small fraction of its
 // fp32 rate) and summed in double.
 // ---------------------------------------------------------------------------
-constexpr int LD_THREADS = 256;
+constexpr int LD_THREADS = 64;
 
 __device__ __forceinline__ V3<double> bs_d(V3<double> c, V3<double> a, V3<double> b) {
     // double Biot-Savart (same law, reference cut-offs), unscaled by 1/4pi
