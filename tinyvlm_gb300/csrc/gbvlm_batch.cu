@@ -308,7 +308,7 @@ __global__ void k_batch_accum(BatchArgs a) {
 // hi + lo floats, each product a*hi exact through an FMA, running sums
 // (sh, sl) kept with a compensated addition): about 2^-44 relative per term,
 // where the fp64 units of this part run at a small fraction of the fp32 rate.
-constexpr int RS_THREADS = 128;
+constexpr int RS_THREADS = 64;
 constexpr int RS_MAXRHS = 8;  // (the inner loop reads them as two float4)
 constexpr int RS_CB = 8;  // columns of Xd staged per step
 constexpr int RS_ROWS = 2;  // rows per thread
