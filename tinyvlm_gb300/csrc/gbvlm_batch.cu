@@ -405,7 +405,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 // and moment terms in float (this part's fp64 rate is a small fraction of its
 // fp32 rate) and summed in double.
 // ---------------------------------------------------------------------------
-constexpr int LD_THREADS = 64;
+// threads per solve: 64 for batches of small systems (most of a block would
+// idle; measured faster on 24-2048 panels), 256 once a system exceeds 4096
+constexpr int LD_THREADS_SMALL = 64, LD_THREADS_LARGE = 256;
 
 __device__ __forceinline__ V3<double> bs_d(V3<double> c, V3<double> a, V3<double> b) {
     // double Biot-Savart (same law, reference cut-offs), unscaled by 1/4pi
@@ -441,6 +443,7 @@ __global__ void k_batch_trefftz_k(BatchArgs a) {
     S.K[j + jj * ns] = -dot(sv, nn) / (4.0 * (double)PI_F) * sqrt(len2(q1 - q0));
 }
 
+template <int LD_THREADS>
 __global__ void __launch_bounds__(LD_THREADS) k_batch_loads(BatchArgs a, const int32_t* solve_sys, int32_t want_gamma) {
     const int32_t sol = blockIdx.x;
     const int32_t si = solve_sys[sol];
@@ -698,7 +701,10 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         GB_LAUNCH_CHECK();
     }
     mark(5);
-    k_batch_loads<<<h->nsolve, LD_THREADS, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+    if (h->maxn > 4096)
+        k_batch_loads<LD_THREADS_LARGE><<<h->nsolve, LD_THREADS_LARGE, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+    else
+        k_batch_loads<LD_THREADS_SMALL><<<h->nsolve, LD_THREADS_SMALL, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
     GB_LAUNCH_CHECK();
     mark(6);
     return GBVLM_OK;
