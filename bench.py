@@ -65,6 +65,22 @@ def parse():
     return p.parse_args()
 
 
+def max_over_ranks(x, world, device):
+    """The largest of every rank's x (all ranks get it): the slowest replica's time."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, world, ms):
+    """Whole-job throughput of independent replicas: every rank's units over the slowest rank's time."""
+    return units_per_rank * world / (ms / 1000.0)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -207,14 +223,6 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     # warm-up: captures the graph
     bs.set_inputs(verts_d, alphas, ref_pt=(0.25, 0.0, 0.0), stream=stream)
     for _ in range(max(args.warmup, 3)):
@@ -232,8 +240,8 @@ def run_gpu(args):
         e1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    value = bs.nsolve * world / (ms / 1000.0)
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = replica_value(bs.nsolve, world, ms)
 
     # --- end to end through the public API with host buffers ----------------
     lat = []
@@ -247,8 +255,8 @@ def run_gpu(args):
         bs.results_into(co_h, g_h, stream=stream)
         lat.append(1000.0 * (time.perf_counter() - s0))
     torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(1000.0 * (time.perf_counter() - t0) / args.steps)
-    e2e = bs.nsolve * world / (e2e_ms / 1000.0)
+    e2e_ms = max_over_ranks(1000.0 * (time.perf_counter() - t0) / args.steps, world, dev)
+    e2e = replica_value(bs.nsolve, world, e2e_ms)
     h2d = verts_h.numel() * 4 + alphas.nbytes
     d2h = co_h.nbytes + g_h.nbytes
 
