@@ -12,7 +12,8 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "newma
 
 
 def test_oracle_newmark_matches_reference_script():
-    g = json.load(open(GOLD))
+    with open(GOLD) as f:
+        g = json.load(f)
     u, v, a = O.newmark_linear(np.array(g["M"]), np.array(g["C"]), np.array(g["K"]), np.array(g["u0"]),
                                np.array(g["v0"]), g["dt"], g["steps"])
     for name, x in (("u", u), ("v", v), ("a", a)):

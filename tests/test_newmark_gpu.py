@@ -45,7 +45,8 @@ def _drive(M, C, K, u0, v0, dt, steps, loads=None):
 
 
 def test_newmark_3dof_against_reference_script(cuda):
-    g = json.load(open(GOLD))
+    with open(GOLD) as f:
+        g = json.load(f)
     u, v, a = _drive(np.array(g["M"]), np.array(g["C"]), np.array(g["K"]), g["u0"], g["v0"], g["dt"], g["steps"])
     for name, x in (("u", u), ("v", v), ("a", a)):
         ref = np.array(g[name])

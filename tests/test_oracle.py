@@ -111,7 +111,8 @@ def test_golden_fixtures(name):
     if not os.path.exists(path):
         pytest.skip("fixture not generated")
     from tests.golden.make_golden import build_case
-    data = json.load(open(path))
+    with open(path) as f:
+        data = json.load(f)
     for case in data["cases"]:
         surfs = build_case(case)
         if surfs is None:
