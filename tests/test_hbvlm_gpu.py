@@ -115,3 +115,26 @@ def test_hbvlm2_multispan_matches_oracle(cuda):
                              L["ddft"], L["force_inst"], L["fs"], L["ref_a"], None, False, x0, 1e-9)
     print("gpu iterations", hb.iterations, "oracle", it, "forces", ft, out[:2])
     np.testing.assert_allclose(ft, out[:2], rtol=1e-7, atol=1e-9)
+
+
+def test_hbvlm_many_harmonics_operator_in_blocks(cuda, monkeypatch):
+    """16 harmonics (33 instances): the operator accumulates its coefficients
+    in two launches of at most 32; map against the direct sums and the run
+    against the oracle."""
+    v = M.rectangular(4, 1, 1.0, 40000.0)
+    H = 16
+    hb = HBVLM2("gb300", v)
+    hb.init(H, 1.0)
+    x0 = hb.gamma_coeffs.copy()
+    dyn = np.zeros((2, 2 * H + 1))
+    dyn[0, 1], dyn[1, 0], dyn[1, 2], dyn[1, 31] = 0.02, 0.01, 0.03, 0.002
+    ft = np.zeros((2, 2 * H + 1))
+    hb.run(0.4, dyn, ft)
+    L = hb._last
+    X, out, it = O.hbvlm_run(hb.verts, [True], H, 0.4, L["dt"], L["max_t"], L["wake_T"], L["inst"], L["dft"],
+                             L["ddft"], L["force_inst"], L["fs"], L["ref_a"], None, False, x0, 1e-9)
+    print("gpu iterations", hb.iterations, "oracle", it, "max diff", np.abs(ft - out[:2]).max())
+    np.testing.assert_allclose(ft, out[:2], rtol=1e-7, atol=1e-9)
+    x = np.asfortranarray(np.random.default_rng(2).standard_normal((hb.engine.n, 2 * H + 1)) * 0.01)
+    y_op, y_direct = _map_both(hb, x, 0.4, L["dt"], monkeypatch)
+    np.testing.assert_allclose(y_op, y_direct, rtol=1e-11, atol=1e-13)

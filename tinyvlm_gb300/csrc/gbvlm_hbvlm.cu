@@ -142,7 +142,8 @@ __global__ void k_pregen_wake(const double* Tall, int32_t nsurf, int32_t m, cons
 // once per map; each map reduces to the small contraction k_hb_rhs.
 // ---------------------------------------------------------------------------
 constexpr int WOP_THREADS = 64;  // two warps: the idle warps of a wider block cost registers
-constexpr int WOP_NMAX = 32;  // Fourier coefficients a thread accumulates (harmonics <= 15)
+constexpr int WOP_NMAX = 32;  // Fourier coefficients a launch accumulates per thread (more: several launches)
+constexpr int HB_NMAX = 2 * 64 + 1;  // time instances at most (64 harmonics)
 
 // one instance of one parameter set (column)
 struct WopInst {
@@ -169,6 +170,7 @@ struct WopArgs {
     const int64_t* wshift_off; // per instance, into wshift
     float* basis_f2;           // the basis rows as float pairs, 2 floats per entry of the double rows
     const double* basis0;      // start of the double basis rows
+    int32_t c0;                // the first Fourier coefficient this launch accumulates
 };
 
 // ---------------------------------------------------------------------------
@@ -333,6 +335,7 @@ __global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
     const int64_t start = I.nwv - 1 - I.it;
     const int64_t j0 = start + (int64_t)blockIdx.z * I.rps;
     const int64_t j1 = min(j0 + I.rps, I.nwv - 1);
+    const int nco = a.N - a.c0;  // coefficients of this launch (at most WOP_NMAX used)
     F2 acc[WOP_NMAX];
 #pragma unroll
     for (int c = 0; c < WOP_NMAX; c++) acc[c] = F2{0.f, 0.f};
@@ -361,18 +364,18 @@ __global__ void __launch_bounds__(WOP_THREADS) k_wake_operator(WopArgs a) {
             F2 val = f2_add(f2_sub(f2_add(Ta, seg_normal_f2(A1, A2, nx, ny, nz)), Na), seg_normal_f2(A3, A0, nx, ny, nz));
             val = f2_add(val, f2_add(f2_sub(f2_add(Tb, seg_normal_f2(B1, B2, nx, mny, nz)), Nb),
                                      seg_normal_f2(B3, B0, nx, mny, nz)));
-            const float* br = a.basis_f2 + (I.basis - a.basis0 + (j - start) * a.N) * 2;
+            const float* br = a.basis_f2 + (I.basis - a.basis0 + (j - start) * a.N + a.c0) * 2;
 #pragma unroll
             for (int c = 0; c < WOP_NMAX; c++)
-                if (c < a.N) acc[c] = f2_add(acc[c], f2_mul(val, F2{br[2 * c], br[2 * c + 1]}));
+                if (c < nco) acc[c] = f2_add(acc[c], f2_mul(val, F2{br[2 * c], br[2 * c + 1]}));
             A0 = A3, A1 = A2, B0 = B3, B1 = B2;
             Ta = Na, Tb = Nb;
         }
     }
-    double* out = a.partial + (((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * npairs + g) * a.N;
+    double* out = a.partial + (((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * npairs + g) * a.N + a.c0;
 #pragma unroll
     for (int c = 0; c < WOP_NMAX; c++)
-        if (c < a.N) out[c] = f2_dbl(acc[c]);
+        if (c < nco) out[c] = f2_dbl(acc[c]);
 }
 
 // M = sum over slices of the partial operators, in slice order
@@ -392,7 +395,7 @@ constexpr int HBR_THREADS = 128;
 __global__ void __launch_bounds__(HBR_THREADS) k_hb_rhs(const WopInst* inst, const double* M, const double* X,
                                                         int64_t n, int64_t te_off, int64_t wns, int32_t N,
                                                         const double* D, double* Y) {
-    __shared__ double R[WOP_NMAX];
+    __shared__ double R[HB_NMAX];
     const int64_t p = blockIdx.x, col = blockIdx.y;
     inst += col * N;
     M += col * (int64_t)N * n * wns * N;
@@ -941,11 +944,9 @@ struct HbState {
         return GBVLM_OK;
     }
 
-    // the wake term through the precomputed operator unless the harmonics
-    // exceed what a thread accumulates (or GBVLM_HB_DIRECT=1 asks for the
-    // per-map Biot-Savart sums)
+    // the wake term through the precomputed operator unless
+    // GBVLM_HB_DIRECT=1 asks for the per-map Biot-Savart sums
     bool use_wop() const {
-        if (N > WOP_NMAX) return false;
         const char* e = getenv("GBVLM_HB_DIRECT");
         return !(e && e[0] == '1');
     }
@@ -1001,8 +1002,10 @@ struct HbState {
         a.wshift_off = wop_shift_off.p;
         k_hb_basis<<<dim3((unsigned)cdiv(max_it, 128), (unsigned)ninst), 128, 0, st>>>(a);
         GB_LAUNCH_CHECK();
-        k_wake_operator<<<dim3((unsigned)xb, (unsigned)ninst, (unsigned)zs), WOP_THREADS, 0, st>>>(a);
-        GB_LAUNCH_CHECK();
+        for (a.c0 = 0; a.c0 < N; a.c0 += WOP_NMAX) {  // the ring values again for each block of coefficients
+            k_wake_operator<<<dim3((unsigned)xb, (unsigned)ninst, (unsigned)zs), WOP_THREADS, 0, st>>>(a);
+            GB_LAUNCH_CHECK();
+        }
         k_wake_operator_sum<<<(unsigned)cdiv(len, 256), 256, 0, st>>>(wop_part.p, zs, len, wop_M.p);
         GB_LAUNCH_CHECK();
         wop_valid = true;
