@@ -50,3 +50,40 @@ def test_hbvlm3_chain_wing_and_flap():
     S = sets[0]
     _, da = obj.assembly(S["omega"], S["U"], S["dyn"]).kinematics().transform_series(np.array([0.0, 1.0]))
     np.testing.assert_array_equal(-da[:, 0, 3], obj._sigma(S))
+
+
+def test_sets_evaluated_together_equal_one_at_a_time():
+    """The batch path evaluates the instances of all parameter sets in one
+    vectorised pass (per-element omega, speed and coefficient rows): each
+    set's transforms equal its own evaluation bitwise."""
+    for cls, nd, with_U, H in ((HB.HBVLM2, 2, False, 3), (HB.HBVLM3, 3, True, 2)):
+        obj = cls.__new__(cls)
+        obj.m_harmonics = H
+        sets = _sets(np.random.default_rng(4), 5, H, nd, with_U)
+        rng = np.random.default_rng(6)
+        times = [np.sort(rng.uniform(0.0, 30.0, 7)) for _ in sets]
+        own = np.concatenate([np.full(t.size, k) for k, t in enumerate(times)])
+        together = obj._chain_series(sets, own, np.concatenate(times))
+        off = 0
+        for S, t in zip(sets, times):
+            alone = obj._series(S, t)
+            for m in range(len(alone)):
+                np.testing.assert_array_equal(together[m][0][off:off + t.size], alone[m][0])
+                np.testing.assert_array_equal(together[m][1][off:off + t.size], alone[m][1])
+            off += t.size
+
+
+def test_chain_vector_layout():
+    """k_hb_chain's parameters: sigma, omega, dt, px, qx, flap, then the heave, pitch and control rows."""
+    obj = HB.HBVLM3.__new__(HB.HBVLM3)
+    obj.m_harmonics, obj.m_coeffs = 2, 5
+    S = dict(omega=0.9, U=8.0, dyn=np.arange(15.0).reshape(3, 5))
+    v = obj._chain_vector(S, 0.01)
+    assert v.shape == (6 + 3 * 5,)
+    np.testing.assert_array_equal(v[:6], [8.0 / (0.127 * 52.6506), 0.9, 0.01, 0.5, 1.5, 1.0])
+    np.testing.assert_array_equal(v[6:], np.arange(15.0))
+    obj2 = HB.HBVLM2.__new__(HB.HBVLM2)
+    obj2.m_harmonics, obj2.m_coeffs = 2, 5
+    v2 = obj2._chain_vector(dict(omega=0.4, dyn=np.ones((2, 5))), 0.02)
+    np.testing.assert_array_equal(v2[:6], [1.0, 0.4, 0.02, 0.5, 0.0, 0.0])
+    np.testing.assert_array_equal(v2[16:], np.zeros(5))
