@@ -2362,9 +2362,10 @@ struct gbvlm_lu_s {
 // per-system solves
 static int lu_flow_ready(gbvlm_lu h, int64_t n, int64_t nrhs, cudaStream_t st, bool* use) {
     const char* fe = getenv("GBVLM_TRS_FLOW");
-    *use = !(fe && fe[0] == '0') && n > 2 * FL_B;
+    const int64_t groups64 = (nrhs + 7) / 8;
+    *use = !(fe && fe[0] == '0') && n > 2 * FL_B && groups64 <= 1024;  // the dataflow solve's group limit
     if (!*use) return GBVLM_OK;
-    const int32_t groups = (int32_t)((nrhs + 7) / 8);
+    const int32_t groups = (int32_t)groups64;
     if (h->flow_n == n && h->flow_groups >= groups) return GBVLM_OK;
     h->flow_n = -1;
     int rc = trs_flow_build(h->flow, std::vector<int64_t>{n}, st, groups);
