@@ -35,3 +35,21 @@ def test_python_prototypes_cover_header():
 
 def test_library_is_in_tree():
     assert os.path.dirname(build.LIB) == os.path.dirname(os.path.abspath(_lib.__file__))
+
+
+def test_argument_checks_need_no_gpu():
+    """Entry points validate their arguments before touching the device and
+    report GBVLM_ERR_ARG (1) with a message; nothing aborts the process."""
+    L = _lib.lib()
+    P = None
+    cases = [
+        ("gbvlm_hbvlm_prepare_batch", (P, 2, 2, P, P, P, P, P, P, P, P), b"null argument"),
+        ("gbvlm_hbvlm_prepare_batch_chain", (P, 2, 2, P, P, P, P, P, P, P, P), b"null argument"),
+        ("gbvlm_hbvlm_solve_batch", (P, 2, P, P, P, 100, 1e-9, 10, P, P), b"solve before prepare"),
+        ("gbvlm_hbvlm_loads_batch", (P, 2, P, P, P, P, P, P, P, P, 0, P, P), b"null argument"),
+        ("gbvlm_test_flow_wait_timeout", (64, P), b"n must span"),
+    ]
+    for name, args, msg in cases:
+        rc = getattr(L, name)(*args)
+        assert rc == 1, (name, rc)
+        assert msg in L.gbvlm_last_error(), (name, L.gbvlm_last_error())
