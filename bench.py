@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--refine", type=int, default=1,
                    help="refinement sweeps (double residual); 1 keeps every solve of the batch within CL/CM 1e-5")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--ref-step-seconds", type=float, default=2.5,
+                   help="reference arm: CPU time one step's fixed subset of the batch is sized to")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-solves", type=int, default=48)
     p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof", "nlvlm", "hbvlm"],
@@ -106,14 +108,36 @@ def config(args, cases):
 # ---------------------------------------------------------------------------
 # CPU side: the oracle port of the reference backend, float, all threads
 # ---------------------------------------------------------------------------
+def stratified_order(cases):
+    """Case indices such that every prefix samples the batch's panel counts
+    evenly: the cases sorted by size, visited in van der Corput (base 2)
+    order, so a CPU sample of a few cases has the whole batch's size mix."""
+    by_size = sorted(range(len(cases)), key=lambda i: cases[i].n)
+    n, out, seen, k = len(cases), [], set(), 0
+    while len(out) < n:
+        x, f, q = 0.0, 0.5, k
+        while q:
+            x += f * (q & 1)
+            q >>= 1
+            f *= 0.5
+        i = by_size[min(n - 1, int(x * n))]
+        if i not in seen:
+            seen.add(i)
+            out.append(i)
+        k += 1
+        if k > 64 * n:  # every remaining index, in size order
+            out += [j for j in by_size if j not in seen]
+            break
+    return out
+
+
 def cpu_sample(args, cases, seconds):
     from oracle import oracle as O
     O.lib()
     threads = O.num_threads()
     done, t0 = 0, time.perf_counter()
     used = 0
-    # a fixed stride through the batch keeps the sample's size mix close to the whole batch
-    order = list(range(0, len(cases), 7)) + [i for i in range(len(cases)) if i % 7]
+    order = stratified_order(cases)
     for i in order:
         c = cases[i]
         if args.mode == "shared":
@@ -182,21 +206,58 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference backend (float,
+    all host threads) on the same workload.  One step is a fixed subset of the
+    batch: the cases of a stride-7 order (which keeps the subset's size mix
+    close to the whole batch's) that the first warm-up pass fits into
+    --ref-step-seconds.  --warmup untimed steps, then --steps timed steps of
+    exactly that subset; value = solves per step over the mean step time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    from oracle import oracle as O
+    O.lib()
+    threads = O.num_threads()
     cases = workload(args)
-    rate, threads, sample = cpu_sample(args, cases, args.cpu_seconds)
-    step_solves = sum(len(c.alphas) for c in cases)
+    order = stratified_order(cases)
+
+    def solve(c):
+        if args.mode == "shared":
+            O.vlm_shared([c.verts], c.alphas, dtype=np.float32)
+        else:
+            for a in c.alphas:
+                O.vlm_run([c.verts], a, dtype=np.float32)
+
+    picks, t0 = [], time.perf_counter()
+    for i in order:  # first warm-up step: size the subset
+        solve(cases[i])
+        picks.append(i)
+        if time.perf_counter() - t0 > args.ref_step_seconds:
+            break
+    for _ in range(max(args.warmup, 1) - 1):
+        for i in picks:
+            solve(cases[i])
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for i in picks:
+            solve(cases[i])
+        times.append(time.perf_counter() - t0)
+    step_solves = sum(len(cases[i].alphas) for i in picks)
+    ms = 1000.0 * float(np.mean(times))
+    rate = step_solves / (ms / 1000.0)
+    sample = "%d of %d cases per step (%d solves, %d panels max, size-stratified), %d timed steps" % (
+        len(picks), len(cases), step_solves, max(cases[i].n for i in picks), args.steps)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "solves/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * step_solves / rate,
+        "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config(args, cases),
+        "config": dict(config(args, cases), reference_step=sample),
         "cpu_baseline": {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement of the reference backend (OpenMP for its Taskflow loops, LAPACK sgetrf/sgetrs "
-                "through scipy's OpenBLAS); the reference's ISPC build needs ispc/xmake/Taskflow, absent here"}))
+                "through scipy's OpenBLAS), pinned to the reference's own drivers compiled here; the reference's "
+                "ISPC build needs ispc/xmake/Taskflow, absent on this box"}))
 
 
 def run_gpu(args):
@@ -361,13 +422,23 @@ def plain_path_rate(args, cases, dev, co):
 
 
 def run_large(args):
-    """128 x 128 elliptic wing (16,384 panels), 64 alphas in [-10, 10] deg on one AIC."""
+    """128 x 128 elliptic wing (16,384 panels), 64 alphas in [-10, 10] deg on one AIC.
+
+    Float AIC, tensor-core LU and double-float refinement (the batched path),
+    timed with CUDA events; then every alpha's error against the full double
+    solve of the same system on the device (double assembly, double LU,
+    gbvlm_vlm_run_shared at precision 64, which the tests hold to the
+    oracle's LAPACK dgetrf/dgetrs at 1e-9): ||gamma - gamma_64|| /
+    ||gamma_64||, and CL and CM_y relative errors guarded near zero lift
+    (denominator at least 1e-3 of the sweep's largest value)."""
     import torch
     from tinyvlm_gb300 import mesh as M
     from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+    from tinyvlm_gb300.vlm import VLM
     v = M.elliptic(args.large_n, args.large_n).astype(np.float32)
     M.quarter_chord(v)
-    case = M.Case(v, np.radians(np.linspace(-10.0, 10.0, 64)), {})
+    al = np.radians(np.linspace(-10.0, 10.0, 64))
+    case = M.Case(v, al, {})
     bs = BatchSolver([case], mode="shared", refine=args.refine)
     stream = torch.cuda.current_stream()
     bs.set_inputs(pack_verts([case]), pack_alphas([case]), ref_pt=(0.0, 0.0, 0.0), stream=stream)
@@ -381,14 +452,32 @@ def run_large(args):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
-    co, _ = bs.results(stream=stream)
+    bs.run(want_gamma=True, stream=stream)
+    co, gam = bs.results(gamma=True, stream=stream)
     lu = bs.lu_flops / (prof["lu_factor"] / 1000.0) / 1e12
     asm = FLOP_PER_INTERACTION * bs.interactions / (prof["assembly"] / 1000.0) / 1e12
+    # the full double solve of the same system, on the device
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref, g64 = VLM("gb300", [v], precision=64).run_shared(al, return_gamma=True)
+    t64 = time.perf_counter() - t0
+    cl64 = np.array([r.cl for r in ref])
+    cm64 = np.array([r.cm[1] for r in ref])
+    g_cl, g_cm = 1e-3 * np.abs(cl64).max(), 1e-3 * np.abs(cm64).max()
+    e_cl = [abs(co[k, 0] - cl64[k]) / max(abs(cl64[k]), g_cl) for k in range(64)]
+    e_cm = [abs(co[k, 3] - cm64[k]) / max(abs(cm64[k]), g_cm) for k in range(64)]
+    e_g = [float(np.linalg.norm(gam[k].astype(np.float64) - g64[k]) / np.linalg.norm(g64[k])) for k in range(64)]
     print(json.dumps({"workload": "large steady: elliptic %dx%d = %d panels, 64 alphas, one AIC" %
                                   (args.large_n, args.large_n, args.large_n ** 2),
                       "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof,
-                      "lu_tflops": lu, "assembly_tflops_alg": asm, "cl_range": [float(co[:, 0].min()), float(co[:, 0].max())],
-                      "refine_iters": args.refine}))
+                      "lu_tflops": lu, "assembly_tflops_alg": asm, "refine_iters": args.refine,
+                      "error_vs_fp64": {"alpha_deg": [round(float(a), 4) for a in np.degrees(al)],
+                                        "cl_rel": e_cl, "cm_rel": e_cm, "gamma_rel_norm": e_g,
+                                        "max": {"cl": max(e_cl), "cm": max(e_cm), "gamma": max(e_g)},
+                                        "target": 1e-5,
+                                        "reference": "device double assembly + double LU of the same system "
+                                                     "(plain per-operator path, gbvlm_vlm_run_shared precision 64)"},
+                      "plain_fp64_sweep_s": t64}))
 
 
 def run_uvlm(args):

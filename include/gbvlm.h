@@ -103,9 +103,10 @@ int gbvlm_rhs_assemble_wake_influence_f64(double* rhs, int32_t nsurf, const gbvl
 
 /* No counterpart in the reference.  Same as
  * gbvlm_rhs_assemble_wake_influence_f32, for callers that cannot allocate
- * device memory (inside a stream capture, in a latency path that must not
- * take cudaMalloc's synchronisation, or under another owner's allocator):
- * the split-K partial sums go to a fixed 4 MiB array in this library's
+ * device memory: a host application whose device memory is owned by its own
+ * allocator, a serving loop held to a fixed device-memory budget, or a
+ * latency path that must not take cudaMalloc's device-wide synchronisation.
+ * The split-K partial sums go to a fixed 4 MiB array in this library's
  * device image instead of scratch grown with cudaMalloc.  At most 1,048,576
  * collocation points (all surfaces); larger problems are rejected with
  * GBVLM_ERR_ARG.  The first call on a device looks the array up with
@@ -277,6 +278,14 @@ int gbvlm_vlm_destroy(gbvlm_vlm h);
  * gamma_out: optional HOST double array of n entries (surfaces packed). */
 int gbvlm_vlm_run(gbvlm_vlm h, double alpha, double beta, double u_inf, double rho, const double* ref_pt,
                   gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream);
+/* The shared-AIC sweep on the plain per-solve path, no single reference
+ * counterpart: the AIC of VLM::run at alpha = 0 (wake row along +x,
+ * vlm.cpp:104-126) assembled and factored once in the handle's precision,
+ * then for each of the nalpha angles the operator sequence of
+ * vlm.cpp:115-151 with the free stream V(alpha) as the right-hand side.
+ * out[k] and gamma_out + k*n (optional, HOST) per angle. */
+int gbvlm_vlm_run_shared(gbvlm_vlm h, int32_t nalpha, const double* alphas, double u_inf, double rho,
+                         const double* ref_pt, gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream);
 
 /* ---------------------------------------------------------------------------
  * Batched steady solves: many single-surface cases of uneven size, each with

@@ -80,7 +80,9 @@ def test_chain_vector_layout():
     S = dict(omega=0.9, U=8.0, dyn=np.arange(15.0).reshape(3, 5))
     v = obj._chain_vector(S, 0.01)
     assert v.shape == (6 + 3 * 5,)
-    np.testing.assert_array_equal(v[:6], [8.0 / (0.127 * 52.6506), 0.9, 0.01, 0.5, 1.5, 1.0])
+    # the free stream speed uses the reference's float-literal constants (libhbvlm3.cpp:562-581)
+    b, w_a = float(np.float32(0.127)), float(np.float32(52.6506))
+    np.testing.assert_array_equal(v[:6], [8.0 / (b * w_a), 0.9, 0.01, 0.5, 1.5, 1.0])
     np.testing.assert_array_equal(v[6:], np.arange(15.0))
     obj2 = HB.HBVLM2.__new__(HB.HBVLM2)
     obj2.m_harmonics, obj2.m_coeffs = 2, 5

@@ -15,6 +15,7 @@ import torch
 
 from oracle import oracle as O
 from tests.helpers import aero_inputs, close, synthetic_wake, wing
+from tinyvlm_gb300 import _lib
 from tinyvlm_gb300 import backend as B
 
 pytestmark = pytest.mark.gpu
@@ -129,6 +130,39 @@ def test_wake_influence(cuda, npd, td, rows, iteration):
             close(H(got), ref, 2e-4, 2e-5, "wake rhs")
         else:
             close(H(got), ref, 1e-10, 1e-12, "wake rhs")
+
+
+def test_wake_influence_float_window(cuda):
+    """The float kernel keeps only the newest 5000 wake ring rows (vlm_backend_cpu_kernels.ispc:158-162); the
+    double kernel keeps them all (:471).  5003 active rows on a small span: the float result equals the
+    double oracle restricted to the newest 5000 rows, and the 3 oldest rows, given a large circulation,
+    would change it if they were summed."""
+    rows, iteration = 5010, 5003
+    surf = [wing("rect", 2, 3, np.float32)]
+    col, nor, _ = O.mesh_metrics(0.0, surf, np.float32)
+    wake = synthetic_wake(surf[0], rows, dx=0.002, seed=3)
+    rng = np.random.default_rng(11)
+    gw = rng.standard_normal((rows - 1, surf[0].shape[2] - 1)).astype(np.float32)
+    start = rows - iteration - 1  # newest active ring row; older rows follow
+    gw[start + 5000:start + iteration] = 1e4  # outside the window
+    n = col[0].shape[1] * col[0].shape[2]
+    d64 = lambda xs: [np.ascontiguousarray(x, np.float64) for x in xs]
+    ref = np.zeros(n, np.float64)
+    O.rhs_assemble_wake_influence(ref, d64([gw[start:start + 5000]]), d64(col), d64(nor),
+                                  d64([wake[:, start:start + 5001]]), [True], 5000)
+    full = np.zeros(n, np.float64)
+    O.rhs_assemble_wake_influence(full, d64([gw]), d64(col), d64(nor), d64([wake]), [True], iteration)
+    assert np.abs(full - ref).max() > 1e-2 * np.abs(ref).max()
+    got = torch.zeros(n, dtype=torch.float32, device="cuda")
+    B.Backend(torch.float32).rhs_assemble_wake_influence(got, [T(gw)], [T(c) for c in col], [T(x) for x in nor],
+                                                        [T(wake)], [True], iteration)
+    # 15,000 rings summed in float: 1e-4 of the largest entry (the float oracle itself sits 4e-5 from ref)
+    close(H(got), ref, 2e-4, 1e-4, "windowed wake rhs")
+    got64 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    B.Backend(torch.float64).rhs_assemble_wake_influence(got64, [T(gw.astype(np.float64))], [T(c.astype(np.float64)) for c in col],
+                                                         [T(x.astype(np.float64)) for x in nor],
+                                                         [T(wake.astype(np.float64))], [True], iteration)
+    close(H(got64), full, 1e-10, 1e-12, "double wake rhs, no window")
 
 
 @pytest.mark.parametrize("npd,td", DT)
@@ -251,8 +285,9 @@ def test_lu_singular(cuda):
     At = T(A)
     lu = be.create_lu_solver()
     lu.init(At)
-    with pytest.raises(Exception):
+    with pytest.raises(_lib.GbvlmError, match="GBVLM_ERR_SINGULAR") as ei:
         lu.factorize(At)
+    assert ei.value.code == _lib.ERRORS_BY_NAME["GBVLM_ERR_SINGULAR"]
 
 
 @pytest.mark.parametrize("n,nrhs", [(2000, 3), (6500, 10)])

@@ -28,6 +28,7 @@ class Coeffs(ctypes.Structure):
 GBVLM_OK = 0
 ERRORS = {1: "GBVLM_ERR_ARG", 2: "GBVLM_ERR_CUDA", 3: "GBVLM_ERR_SINGULAR", 4: "GBVLM_ERR_NOMEM",
           5: "GBVLM_ERR_IO", 6: "GBVLM_ERR_STATE"}
+ERRORS_BY_NAME = {v: k for k, v in ERRORS.items()}
 
 
 class GbvlmError(RuntimeError):
@@ -65,6 +66,7 @@ def _protos():
     t["gbvlm_vlm_create"] = [P, I32, P, PP, I32]
     t["gbvlm_vlm_destroy"] = [P]
     t["gbvlm_vlm_run"] = [P, F64, F64, F64, F64, P, P, P, P]
+    t["gbvlm_vlm_run_shared"] = [P, I32, P, F64, F64, P, P, P, P]
     t["gbvlm_read_plot3d"] = [ctypes.c_char_p, I32, P, P]
     t["gbvlm_test_flow_wait_timeout"] = [I32, P]
     t["gbvlm_nlvlm_create"] = [P, I32, P, PP, I32]

@@ -90,6 +90,8 @@ struct VlmBase {
     virtual ~VlmBase() = default;
     virtual int run(double alpha, double beta, double u_inf, double rho, const double* ref_pt, gbvlm_coeffs* out,
                     double* gamma_out, cudaStream_t st) = 0;
+    virtual int run_shared(int32_t nalpha, const double* alphas, double u_inf, double rho, const double* ref_pt,
+                           gbvlm_coeffs* out, double* gamma_out, cudaStream_t st) = 0;
 };
 
 template <class T>
@@ -165,27 +167,36 @@ struct VlmState : VlmBase {
         return gbvlm_lu_init(lu, n);
     }
 
-    int run(double alpha_d, double beta_d, double u_inf_d, double rho_d, const double* ref_pt, gbvlm_coeffs* out,
-            double* gamma_out, cudaStream_t st) override {
-        gbvlm_stream s = (gbvlm_stream)st;
-        const T alpha = (T)alpha_d, beta = (T)beta_d, u = (T)u_inf_d, rho = (T)rho_d;
-        // FlowData (vlm_utils.cpp:5-19)
-        T fs[3] = {u * (T)cos(alpha) * (T)cos(beta), -(u * (T)cos(alpha) * (T)sin(beta)), u * (T)sin(alpha)};
-        T la[3] = {-fs[2], (T)0, fs[0]};
+    // FlowData (vlm_utils.cpp:5-19): free stream and lift axis
+    static void flow(T alpha, T beta, T u, T* fs, T* la) {
+        fs[0] = u * (T)cos(alpha) * (T)cos(beta);
+        fs[1] = -(u * (T)cos(alpha) * (T)sin(beta));
+        fs[2] = u * (T)sin(alpha);
+        la[0] = -fs[2];
+        la[1] = (T)0;
+        la[2] = fs[0];
         T ll = (T)sqrt(la[0] * la[0] + la[1] * la[1] + la[2] * la[2]);
         la[0] /= ll; la[1] /= ll; la[2] /= ll;
+    }
+
+    // Geometry, AIC and its factorisation for the angle alpha (vlm.cpp:97-126):
+    // the 100-chord wake row along the free stream, collocation points with the
+    // high-AoA factor of alpha; `tr` receives the wake translation.
+    int assemble(T alpha, T u, T* tr, gbvlm_stream s, cudaStream_t st) {
         GB_CUDA(cudaMemsetAsync(lhs, 0, sizeof(T) * n * n, st));
-        GB_CUDA(cudaMemsetAsync(rhs, 0, sizeof(T) * n, st));
         for (int m = 0; m < nsurf; m++) {
             int64_t nv = (dims[m].ns + 1) * (dims[m].nc + 1);
             GB_CUDA(cudaMemcpyAsync(verts[m], verts_init[m], sizeof(T) * 4 * nv, cudaMemcpyDeviceToDevice, st));
         }
         // 100-chord wake (vlm.cpp:104-114)
-        T tr[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, (T)-100 * u * (T)cos(alpha), 0, (T)-100 * u * (T)sin(alpha), 1};
-        for (int m = 0; m < nsurf; m++) GB_CUDA(cudaMemcpyAsync(transform[m], tr, sizeof(tr), cudaMemcpyHostToDevice, st));
+        const T t16[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, (T)-100 * u * (T)cos(alpha), 0,
+                           (T)-100 * u * (T)sin(alpha), 1};
+        for (int k = 0; k < 16; k++) tr[k] = t16[k];
+        for (int m = 0; m < nsurf; m++)
+            GB_CUDA(cudaMemcpyAsync(transform[m], t16, sizeof(t16), cudaMemcpyHostToDevice, st));
         std::vector<const T*> cverts(verts.begin(), verts.end()), cinit(verts_init.begin(), verts_init.end()),
             ctr(transform.begin(), transform.end()), ccol(colloc.begin(), colloc.end()),
-            cnor(normals.begin(), normals.end()), cwake(wake.begin(), wake.end()), cvel(vel.begin(), vel.end());
+            cnor(normals.begin(), normals.end()), cwake(wake.begin(), wake.end());
         int rc;
         if ((rc = Ops<T>::shed(nsurf, dims.data(), cverts.data(), wake.data(), 0, s))) return rc;
         if ((rc = Ops<T>::displace(nsurf, dims.data(), ctr.data(), verts.data(), cinit.data(), s))) return rc;
@@ -194,13 +205,22 @@ struct VlmState : VlmBase {
             return rc;
         if ((rc = Ops<T>::lhs(lhs, n, nsurf, dims.data(), ccol.data(), cnor.data(), cverts.data(), cwake.data(), 1, sigma, s)))
             return rc;
+        return Ops<T>::factor(lu, lhs, n, s);
+    }
+
+    // Right-hand side for the free stream fs, the solve, the circulation
+    // update and the loads (vlm.cpp:115-151) on the factored AIC.
+    int solve_loads(const T* fs, const T* la, T rho, const T* tr, const double* ref_pt, gbvlm_coeffs* out,
+                    double* gamma_out, gbvlm_stream s, cudaStream_t st) {
+        GB_CUDA(cudaMemsetAsync(rhs, 0, sizeof(T) * n, st));
+        std::vector<const T*> cnor(normals.begin(), normals.end()), cvel(vel.begin(), vel.end());
+        int rc;
         for (int m = 0; m < nsurf; m++) {
             int64_t np = dims[m].ns * dims[m].nc;
             k_fill3<T><<<(unsigned)cdiv(np, 256), 256, 0, st>>>(vel[m], np, fs[0], fs[1], fs[2]);
             GB_LAUNCH_CHECK();
         }
         if ((rc = Ops<T>::rhsv(rhs, nsurf, dims.data(), cnor.data(), cvel.data(), s))) return rc;
-        if ((rc = Ops<T>::factor(lu, lhs, n, s))) return rc;
         if ((rc = Ops<T>::solve(lu, lhs, n, rhs, s))) return rc;
         int64_t off = 0;
         for (int m = 0; m < nsurf; m++) {
@@ -239,6 +259,33 @@ struct VlmState : VlmBase {
             for (int64_t i = 0; i < n; i++) gamma_out[i] = (double)h[i];
         }
         return lu_solve_check(lu, st);  // the solve finished its bounded waits
+    }
+
+    int run(double alpha_d, double beta_d, double u_inf_d, double rho_d, const double* ref_pt, gbvlm_coeffs* out,
+            double* gamma_out, cudaStream_t st) override {
+        gbvlm_stream s = (gbvlm_stream)st;
+        const T alpha = (T)alpha_d, beta = (T)beta_d, u = (T)u_inf_d, rho = (T)rho_d;
+        T fs[3], la[3], tr[16];
+        flow(alpha, beta, u, fs, la);
+        int rc = assemble(alpha, u, tr, s, st);
+        if (rc) return rc;
+        return solve_loads(fs, la, rho, tr, ref_pt, out, gamma_out, s, st);
+    }
+
+    int run_shared(int32_t nalpha, const double* alphas, double u_inf_d, double rho_d, const double* ref_pt,
+                   gbvlm_coeffs* out, double* gamma_out, cudaStream_t st) override {
+        gbvlm_stream s = (gbvlm_stream)st;
+        const T u = (T)u_inf_d, rho = (T)rho_d;
+        T tr[16];
+        int rc = assemble((T)0, u, tr, s, st);
+        if (rc) return rc;
+        for (int32_t k = 0; k < nalpha; k++) {
+            T fs[3], la[3];
+            flow((T)alphas[k], (T)0, u, fs, la);
+            rc = solve_loads(fs, la, rho, tr, ref_pt, out + k, gamma_out ? gamma_out + (int64_t)k * n : nullptr, s, st);
+            if (rc) return rc;
+        }
+        return GBVLM_OK;
     }
 };
 
@@ -548,6 +595,13 @@ int gbvlm_vlm_run(gbvlm_vlm h, double alpha, double beta, double u_inf, double r
                   gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream) {
     GB_REQUIRE(h && h->impl && out, "null argument");
     return h->impl->run(alpha, beta, u_inf, rho, ref_pt, out, gamma_out, to_cuda(stream));
+}
+
+int gbvlm_vlm_run_shared(gbvlm_vlm h, int32_t nalpha, const double* alphas, double u_inf, double rho,
+                         const double* ref_pt, gbvlm_coeffs* out, double* gamma_out, gbvlm_stream stream) {
+    GB_REQUIRE(h && h->impl && out && alphas, "null argument");
+    GB_REQUIRE(nalpha >= 1, "nalpha=%d < 1", nalpha);
+    return h->impl->run_shared(nalpha, alphas, u_inf, rho, ref_pt, out, gamma_out, to_cuda(stream));
 }
 
 int gbvlm_nlvlm_create(gbvlm_nlvlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,

@@ -5,6 +5,7 @@
 // precision T; the float instantiation keeps the reference's float
 // semantics (cut-offs, 5000-row wake window), the double one the reference's
 // double kernels (vlm_backend_cpu_kernels.ispc:383-502).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -1313,20 +1314,22 @@ GB_BOTH(DEF_GUPDATE)
 // ===========================================================================
 // Allocation-free variant of the float wake-influence entry point.
 //
-// Some callers cannot call cudaMalloc: code that records into a CUDA stream
-// capture (an allocation there fails the capture or synchronises the
-// device), serving loops that must keep cudaMalloc's device-wide
-// synchronisation out of their latency path, and hosts whose device memory
-// belongs to another allocator.  For them the split-K partial sums of
-// gbvlm_rhs_assemble_wake_influence_f32 live in the fixed array below
-// instead of the library's grown-on-demand scratch buffer.
+// Some callers cannot call cudaMalloc: a host application whose device
+// memory is all owned by its own allocator or pool, a serving loop that
+// admits work by a fixed device-memory budget and must not grow it behind
+// the budget's back, and latency paths that must keep cudaMalloc's
+// device-wide synchronisation out of every step.  For them the split-K
+// partial sums of gbvlm_rhs_assemble_wake_influence_f32 live in the fixed
+// array below instead of the library's grown-on-demand scratch buffer.
 //
 // The array is GBVLM_WAKE_SCRATCH_FLOATS floats (4 MiB) in this library's
 // device image, so every GPU that loads the library holds it until the
 // process exits.  Host code cannot hand the array's name to a kernel (on the
 // host it is only a stand-in symbol), so the first call on each device looks
 // up its device address with cudaGetSymbolAddress while that device is
-// current and caches it; make that first call before any stream capture.
+// current and caches it with the context it belongs to; a later call from a
+// different context (the primary context released and created again) looks
+// it up again.  Make the first call on a device before any stream capture.
 // All calls share the one array and every call overwrites the part it uses
 // (each partial is written before it is read), so no contents carry over;
 // calls whose kernels overlap on the GPU (different streams, no ordering
@@ -1336,9 +1339,25 @@ GB_BOTH(DEF_GUPDATE)
 
 static __device__ __align__(256) float g_wake_scratch[GBVLM_WAKE_SCRATCH_FLOATS];
 
+// cuCtxGetCurrent, resolved through the runtime so that loading the library
+// needs no driver library (hosts without a GPU load it to check its exports)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+static CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = []() -> CtxGetCurrentFn {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return (CtxGetCurrentFn)p;
+    }();
+    return fn;
+}
+
 static float* wake_scratch_address(int* rc) {
     static std::mutex mu;
     static float* addr[64] = {nullptr};
+    static CUcontext owner[64] = {nullptr};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -1351,6 +1370,9 @@ static float* wake_scratch_address(int* rc) {
         return nullptr;
     }
     std::lock_guard<std::mutex> lk(mu);
+    CtxGetCurrentFn get_ctx = ctx_get_current();
+    CUcontext cur = nullptr;
+    if (addr[dev] && (!get_ctx || get_ctx(&cur) != CUDA_SUCCESS || cur != owner[dev])) addr[dev] = nullptr;
     if (!addr[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_wake_scratch);
@@ -1358,7 +1380,14 @@ static float* wake_scratch_address(int* rc) {
             *rc = cuda_fail(e, "cudaGetSymbolAddress(g_wake_scratch)", __FILE__, __LINE__);
             return nullptr;
         }
+        if (!get_ctx || get_ctx(&cur) != CUDA_SUCCESS || cur == nullptr) {
+            set_error("no current CUDA context after cudaGetSymbolAddress (cuCtxGetCurrent %s)",
+                      get_ctx ? "failed" : "unavailable");
+            *rc = GBVLM_ERR_CUDA;
+            return nullptr;
+        }
         addr[dev] = (float*)p;
+        owner[dev] = cur;
     }
     *rc = GBVLM_OK;
     return addr[dev];

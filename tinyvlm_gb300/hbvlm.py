@@ -287,8 +287,16 @@ class _HBVLMBase:
             w = v.copy()
             w[:3] *= scaling
             self.verts.append(w)
-        self.engine = HBEngine(self.verts, self.lifting)
-        self.gamma_coeffs = np.zeros((self.engine.n, self.m_coeffs), order="F")
+        self._engine = None
+        n = sum((v.shape[1] - 1) * (v.shape[2] - 1) for v in self.verts)
+        self.gamma_coeffs = np.zeros((n, self.m_coeffs), order="F")
+
+    @property
+    def engine(self):
+        """The device handle, created at first use (planning a run needs none)."""
+        if self._engine is None:
+            self._engine = HBEngine(self.verts, self.lifting)
+        return self._engine
 
     def _chain_vector(self, S, dt):
         """k_hb_chain's parameters for set S: sigma, omega, dt, px, qx, flap, the three coefficient rows."""
@@ -313,16 +321,13 @@ class _HBVLMBase:
         """Transforms and rates of the surfaces' kinematic chain for parameter set S at the times t."""
         return self._chain_series([S], np.zeros(np.size(t), np.int64), np.asarray(t, np.float64))
 
-    def _run_sets(self, sets, refs, forces_list, coupled_te):
-        """HBVLM::run for K parameter sets (libhbvlm3.cpp:262-552), solved together.
-
-        sets: dicts with ``omega``, ``t_start`` and the kinematic parameters
-        ``_chain_params`` reads.  The wake transforms of every step are
-        evaluated on the device from the chain parameters; the instances'
-        transforms (2N per set) in one closed-form pass over all sets.
-        Every set starts from the current coefficients, which afterwards
-        hold the last set's fixed point, as after the same runs in sequence."""
-        N, H = self.m_coeffs, self.m_harmonics
+    def plan(self, sets, refs):
+        """Host side of HBVLM::run for K parameter sets (libhbvlm3.cpp:262-347):
+        time step, wake length, instance and force-instance times with their
+        kinematics, DFT matrices, free stream and moment reference points.
+        The wake transforms of every step (``wake_T``) are computed only when
+        read; the device evaluates them itself from the chain parameters."""
+        N = self.m_coeffs
         chord = last_panel_chord(self.verts[self.dt_surface])
         cols, times = [], []
         for k, S in enumerate(sets):
@@ -352,6 +357,20 @@ class _HBVLMBase:
             c["ref_b"] = None
             if len(refs) > 1:
                 c["ref_b"] = (series[1][0][sf] @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
+        return cols
+
+    def _run_sets(self, sets, refs, forces_list, coupled_te):
+        """HBVLM::run for K parameter sets (libhbvlm3.cpp:262-552), solved together.
+
+        sets: dicts with ``omega``, ``t_start`` and the kinematic parameters
+        ``_chain_params`` reads.  The wake transforms of every step are
+        evaluated on the device from the chain parameters; the instances'
+        transforms (2N per set) in one closed-form pass over all sets.
+        Every set starts from the current coefficients, which afterwards
+        hold the last set's fixed point, as after the same runs in sequence."""
+        N, H = self.m_coeffs, self.m_harmonics
+        cols = self.plan(sets, refs)
+        K = len(cols)
         self.engine.prepare_batch_chain(H, [c["max_t"] for c in cols],
                                   [self._chain_vector(S, c["dt"]) for S, c in zip(sets, cols)],
                                   np.concatenate([c["inst"][0] for c in cols]),
@@ -379,7 +398,10 @@ class HBVLM3(_HBVLMBase):
     qc = False
     tol = 1e-12
     dt_surface = 1
-    VARS = dict(a=-0.5, b=0.127, c=0.5, omega_alpha=52.6506)
+    # libhbvlm3.cpp:562-581 assigns float literals (0.127f, 52.6506f, ...) to its double fields, so the
+    # kinematics use those constants rounded to float
+    VARS = dict(a=float(np.float32(-0.5)), b=float(np.float32(0.127)), c=float(np.float32(0.5)),
+                omega_alpha=float(np.float32(52.6506)))
 
     def __init__(self, backend_name, meshes):
         if len(meshes) != 2:
@@ -412,8 +434,13 @@ class HBVLM3(_HBVLMBase):
     def _refs(self):
         return (1.0 + self.VARS["a"], 1.0 + self.VARS["c"])
 
+    @staticmethod
+    def parameter_set(omega, U, dyn_f):
+        """One run's parameters (libhbvlm3.cpp:558-641): two cycles of wake before the period."""
+        return dict(omega=omega, U=U, dyn=dyn_f, t_start=2.0 * TWO_PI_F / omega)
+
     def run(self, omega, U, dyn_f, forces_t):
-        S = dict(omega=omega, U=U, dyn=dyn_f, t_start=2.0 * TWO_PI_F / omega)
+        S = self.parameter_set(omega, U, dyn_f)
         self.iterations = int(self._run_sets([S], self._refs(), [forces_t], True)[0])
         return forces_t
 

@@ -85,6 +85,23 @@ class VLM:
             return res, g
         return res
 
+    def run_shared(self, alphas, u_inf=1.0, rho=1.0, ref_pt=(0.0, 0.0, 0.0), return_gamma=False, stream=None):
+        """One AIC at alpha = 0 factored once, every angle a right-hand side (the
+        classical linear sweep of the large steady workload), on this
+        handle's precision; returns one AeroCoefficients per angle."""
+        al = np.ascontiguousarray(alphas, np.float64)
+        out = (Coeffs * len(al))()
+        rp = (ctypes.c_double * 3)(*ref_pt)
+        g = np.zeros((len(al), self.n), np.float64) if return_gamma else None
+        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        call("gbvlm_vlm_run_shared", self.h, len(al), ctypes.c_void_p(al.ctypes.data), float(u_inf), float(rho),
+             ctypes.cast(rp, ctypes.c_void_p), ctypes.cast(out, ctypes.c_void_p),
+             ctypes.c_void_p(g.ctypes.data) if g is not None else None, s)
+        res = [AeroCoefficients(o.cl, o.cdi, tuple(o.cm)) for o in out]
+        if return_gamma:
+            return res, g
+        return res
+
 
 class WingProfile:
     """A 2D section polar (vlm/include/vlm_data.hpp:40-77): coefficients
