@@ -60,6 +60,99 @@ const char* gbvlm_last_error(void);
 int gbvlm_version(void);
 
 /* ---------------------------------------------------------------------------
+ * Memory: replaces vlm::Memory (vlm/include/vlm_memory.hpp:22-37), the
+ * manager Backend::create_memory_manager returns (vlm_backend.hpp:72).
+ * Locations follow vlm::Location: Device memory is cudaMalloc'd, Host memory
+ * is pinned (cudaMallocHost), as the reference's CUDA backend allocates it
+ * (vlm_backend_cuda.cu:90-107).
+ * ------------------------------------------------------------------------- */
+enum { GBVLM_LOC_DEVICE = 0, GBVLM_LOC_HOST = 1 };
+/* Memory::alloc / Memory::free.  GBVLM_ERR_NOMEM when the allocation fails. */
+int gbvlm_mem_alloc(int32_t location, int64_t bytes, void** out);
+int gbvlm_mem_free(int32_t location, void* ptr);
+/* Memory::copy: `size` elements of `elem_size` bytes, element strides
+ * dst_stride and src_stride (>= 1).  Stream-ordered between device buffers;
+ * synchronous when either side is host memory (the reference's copy returns
+ * with the data in place, vlm_backend_cuda.cu:109-126). */
+int gbvlm_mem_copy(int32_t dst_loc, void* dst, int64_t dst_stride, int32_t src_loc, const void* src,
+                   int64_t src_stride, int64_t elem_size, int64_t size, gbvlm_stream stream);
+/* Memory::fill (float and double overloads). */
+int gbvlm_mem_fill_f32(int32_t location, float* ptr, int64_t stride, float value, int64_t size, gbvlm_stream stream);
+int gbvlm_mem_fill_f64(int32_t location, double* ptr, int64_t stride, double value, int64_t size,
+                       gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * BLAS: replaces vlm::BLAS (vlm_backend.hpp:78-97) with the argument meaning
+ * of the reference's CBLAS/cuBLAS calls (vlm_backend_cpu_blas.cpp,
+ * vlm_backend_cuda_blas.cu): column-major, trans = 0 (Trans::No) or 1
+ * (Trans::Yes), element strides inc >= 1.  Stream-ordered except nrm2,
+ * which returns its scalar synchronously like BLAS::norm.
+ * ------------------------------------------------------------------------- */
+/* BLAS::gemv: y = alpha op(A) x + beta y, A m x n (beta = 0: y is not read). */
+int gbvlm_blas_gemv_f32(int32_t trans, int64_t m, int64_t n, float alpha, const float* A, int64_t lda,
+                        const float* x, int64_t incx, float beta, float* y, int64_t incy, gbvlm_stream stream);
+int gbvlm_blas_gemv_f64(int32_t trans, int64_t m, int64_t n, double alpha, const double* A, int64_t lda,
+                        const double* x, int64_t incx, double beta, double* y, int64_t incy, gbvlm_stream stream);
+/* BLAS::gemm: C = alpha op(A) op(B) + beta C, C m x n, inner size k. */
+int gbvlm_blas_gemm_f32(int32_t trans_a, int32_t trans_b, int64_t m, int64_t n, int64_t k, float alpha,
+                        const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                        gbvlm_stream stream);
+int gbvlm_blas_gemm_f64(int32_t trans_a, int32_t trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                        const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+                        int64_t ldc, gbvlm_stream stream);
+/* BLAS::axpy, 1-D: y += alpha x. */
+int gbvlm_blas_axpy_f32(int64_t n, float alpha, const float* x, int64_t incx, float* y, int64_t incy,
+                        gbvlm_stream stream);
+int gbvlm_blas_axpy_f64(int64_t n, double alpha, const double* x, int64_t incx, double* y, int64_t incy,
+                        gbvlm_stream stream);
+/* BLAS::axpy, 2-D (vlm_backend_cpu_blas.cpp:101-106): y(i, j) += alpha x(i, j)
+ * over an m x n view, element strides (s0, s1) for each operand. */
+int gbvlm_blas_axpy2d_f32(int64_t m, int64_t n, float alpha, const float* x, int64_t x_s0, int64_t x_s1, float* y,
+                          int64_t y_s0, int64_t y_s1, gbvlm_stream stream);
+int gbvlm_blas_axpy2d_f64(int64_t m, int64_t n, double alpha, const double* x, int64_t x_s0, int64_t x_s1, double* y,
+                          int64_t y_s0, int64_t y_s1, gbvlm_stream stream);
+/* BLAS::scal: x *= alpha. */
+int gbvlm_blas_scal_f32(int64_t n, float alpha, float* x, int64_t incx, gbvlm_stream stream);
+int gbvlm_blas_scal_f64(int64_t n, double alpha, double* x, int64_t incx, gbvlm_stream stream);
+/* BLAS::norm: Euclidean norm into *out (host), scaled so no finite input
+ * overflows. */
+int gbvlm_blas_nrm2_f32(int64_t n, const float* x, int64_t incx, float* out, gbvlm_stream stream);
+int gbvlm_blas_nrm2_f64(int64_t n, const double* x, int64_t incx, double* out, gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * LSQ: replaces vlm::LSQ::solve (vlm_backend.hpp:121-133;
+ * vlm_backend_cpu_lapack.cpp:123-205, LAPACK ?gels with trans = 'N'):
+ * min ||A x - B|| for A m x n (m >= n, full column rank) by Householder QR.
+ * The first n rows of B receive x, rows n..m-1 the residual components; A is
+ * overwritten (R in its upper triangle).  Synchronous; GBVLM_ERR_SINGULAR if
+ * R has an exactly zero diagonal.  LSQ::init has nothing to size: the
+ * solver keeps no workspace.
+ * ------------------------------------------------------------------------- */
+int gbvlm_lsq_solve_f32(int64_t m, int64_t n, float* A, int64_t lda, float* B, int64_t nrhs, int64_t ldb,
+                        gbvlm_stream stream);
+int gbvlm_lsq_solve_f64(int64_t m, int64_t n, double* A, int64_t lda, double* B, int64_t nrhs, int64_t ldb,
+                        gbvlm_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Streams, events and device queries: no reference counterpart (the
+ * reference's CUDA backend runs on the legacy default stream).  They let a
+ * host without another CUDA binding order, time and size its work.
+ * ------------------------------------------------------------------------- */
+typedef struct CUevent_st* gbvlm_event; /* same handle as cudaEvent_t */
+int gbvlm_stream_create(gbvlm_stream* out); /* non-blocking stream */
+int gbvlm_stream_destroy(gbvlm_stream s);
+int gbvlm_stream_synchronize(gbvlm_stream s);
+int gbvlm_device_synchronize(void);
+int gbvlm_event_create(gbvlm_event* out);
+int gbvlm_event_destroy(gbvlm_event e);
+int gbvlm_event_record(gbvlm_event e, gbvlm_stream s);
+int gbvlm_event_synchronize(gbvlm_event e);
+int gbvlm_event_elapsed_ms(gbvlm_event start, gbvlm_event end, float* ms);
+/* Current device: SM count and free / total device memory in bytes (NULL
+ * pointers are skipped). */
+int gbvlm_device_info(int32_t* sm_count, int64_t* free_bytes, int64_t* total_bytes);
+
+/* ---------------------------------------------------------------------------
  * Backend operators.  Replaces the pure virtuals of vlm::Backend
  * (vlm/include/vlm_backend.hpp:31-55); semantics follow the CPU backend
  * vlm/backends/cpu/src/vlm_backend_cpu.cpp (f32) and vlm_backend_cpud.cpp (f64).
@@ -176,6 +269,13 @@ int gbvlm_gamma_wake_from_coeffs_f64(double* gamma_wake, int64_t ns, int64_t nco
 /* Backend::sum (vlm_backend.hpp:41-42/55-56; vlm_backend_cpu.cpp:506-523). *out synchronous. */
 int gbvlm_sum_f32(const float* x, int64_t n, float* out, gbvlm_stream stream);
 int gbvlm_sum_f64(const double* x, int64_t n, double* out, gbvlm_stream stream);
+/* Backend::sum(TV2f&) (vlm_backend.hpp:43/54; vlm_backend_cpu.cpp:515-523):
+ * the sum of an m x n view with element strides (stride0, stride1),
+ * compensated in double, returned synchronously. */
+int gbvlm_sum2d_f32(const float* x, int64_t m, int64_t n, int64_t stride0, int64_t stride1, float* out,
+                    gbvlm_stream stream);
+int gbvlm_sum2d_f64(const double* x, int64_t m, int64_t n, int64_t stride0, int64_t stride1, double* out,
+                    gbvlm_stream stream);
 
 /* Backend::displace_wing (vlm_backend.hpp:59/66; vlm_backend.cpp:50-69):
  * verts = verts_init . T^T per surface; transforms: device 4x4 column-major. */

@@ -58,6 +58,28 @@ def _protos():
         t["gbvlm_gamma_update_" + sfx] = [I64, I64, P, P, P, P, I64, P, P, R, P]
         t["gbvlm_lu_factor_" + sfx] = [P, P, I64, I64, P]
         t["gbvlm_lu_solve_" + sfx] = [P, P, I64, I64, P, I64, I64, P]
+        t["gbvlm_sum2d_" + sfx] = [P, I64, I64, I64, I64, P, P]
+        t["gbvlm_mem_fill_" + sfx] = [I32, P, I64, R, I64, P]
+        t["gbvlm_blas_gemv_" + sfx] = [I32, I64, I64, R, P, I64, P, I64, R, P, I64, P]
+        t["gbvlm_blas_gemm_" + sfx] = [I32, I32, I64, I64, I64, R, P, I64, P, I64, R, P, I64, P]
+        t["gbvlm_blas_axpy_" + sfx] = [I64, R, P, I64, P, I64, P]
+        t["gbvlm_blas_axpy2d_" + sfx] = [I64, I64, R, P, I64, I64, P, I64, I64, P]
+        t["gbvlm_blas_scal_" + sfx] = [I64, R, P, I64, P]
+        t["gbvlm_blas_nrm2_" + sfx] = [I64, P, I64, P, P]
+        t["gbvlm_lsq_solve_" + sfx] = [I64, I64, P, I64, P, I64, I64, P]
+    t["gbvlm_mem_alloc"] = [I32, I64, P]
+    t["gbvlm_mem_free"] = [I32, P]
+    t["gbvlm_mem_copy"] = [I32, P, I64, I32, P, I64, I64, I64, P]
+    t["gbvlm_stream_create"] = [P]
+    t["gbvlm_stream_destroy"] = [P]
+    t["gbvlm_stream_synchronize"] = [P]
+    t["gbvlm_device_synchronize"] = []
+    t["gbvlm_event_create"] = [P]
+    t["gbvlm_event_destroy"] = [P]
+    t["gbvlm_event_record"] = [P, P]
+    t["gbvlm_event_synchronize"] = [P]
+    t["gbvlm_event_elapsed_ms"] = [P, P, P]
+    t["gbvlm_device_info"] = [P, P, P]
     t["gbvlm_rhs_assemble_wake_influence_f32_noalloc"] = [P, I32, P, PP, PP, PP, PP, P, I32, F32, P]
     t["gbvlm_lu_create"] = [P]
     t["gbvlm_lu_destroy"] = [P]

@@ -15,6 +15,7 @@ import ctypes
 import numpy as np
 
 from ._lib import P, PP, call, dims_array
+from .device import stream_handle
 
 __all__ = ["UVLM_2DOF", "VARS_FIELDS", "reference_vars"]
 
@@ -88,4 +89,4 @@ class UVLM_2DOF:
 
     @staticmethod
     def _s(stream):
-        return ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        return stream_handle(stream)

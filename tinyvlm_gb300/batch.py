@@ -11,6 +11,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import P, call, dims_array
+from .device import stream_handle
 
 MODES = {"exact": 0, "shared": 1}
 STAGES = ("geometry", "assembly", "rhs", "lu_factor", "solve_refine", "loads")
@@ -66,7 +67,7 @@ class BatchSolver:
 
     @staticmethod
     def _s(stream):
-        return ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        return stream_handle(stream)
 
     def run(self, want_gamma=False, stream=None, graph=True):
         """Enqueue the solve; graph=False launches it kernel by kernel (a batch solved once)."""

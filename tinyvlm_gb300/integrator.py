@@ -2,25 +2,20 @@
 reference (vlm/include/vlm_integrator.hpp:7-41) over the C ABI
 (gbvlm_newmark_*), in double.
 
-Matrices and vectors are CUDA float64 tensors.  Matrices are read
-column-major, element (r, c) at r + c * ndof, like the reference's
-TensorView2fD; pass ``M.t().contiguous()`` for a row-major torch matrix (or
-nothing, for the symmetric mass, damping and stiffness matrices).
+Matrices and vectors are float64 device arrays (``device.DeviceArray`` or any
+object with ``data_ptr()`` and ``shape``).  Matrices are read column-major,
+element (r, c) at r + c * ndof, like the reference's TensorView2fD: upload
+the transpose of a row-major matrix (or the matrix itself, for the symmetric
+mass, damping and stiffness matrices).
 """
 import ctypes
 
 from ._lib import P, call
+from .device import stream_handle as _s
 
 
 def _p(t):
     return ctypes.c_void_p(t.data_ptr())
-
-
-def _s(stream):
-    if stream is None:
-        import torch
-        stream = torch.cuda.current_stream()
-    return ctypes.c_void_p(stream.cuda_stream)
 
 
 class NewmarkBeta:
@@ -42,8 +37,8 @@ class NewmarkBeta:
         """K_eff = K + M/(beta dt^2) + gamma C/(beta dt), factored on the device."""
         n = int(M.shape[0])
         for X in (M, C, K):
-            if X.dim() != 2 or tuple(X.shape) != (n, n) or not X.is_contiguous():
-                raise ValueError("Newmark matrices must be contiguous (ndof, ndof) tensors")
+            if len(X.shape) != 2 or tuple(X.shape) != (n, n) or (hasattr(X, "is_contiguous") and not X.is_contiguous()):
+                raise ValueError("Newmark matrices must be contiguous (ndof, ndof) device arrays")
         call("gbvlm_newmark_init", self.h, n, _p(M), _p(C), _p(K), float(dt), _s(stream))
 
     def step(self, M, C, v_i, a_i, du, dv, da, delta_F, dt, stream=None):

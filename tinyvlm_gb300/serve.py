@@ -32,6 +32,7 @@ import numpy as np
 
 from . import mesh as M
 from .batch import BatchSolver, pack_alphas, pack_verts
+from .device import Stream
 
 
 class Request:
@@ -56,8 +57,6 @@ def steady_bytes(n, nalpha=1):
 
 class Server:
     def __init__(self, lanes=3, hbm_budget=32 << 30, max_batch=64, uvlm=None, hbvlm=None, mode="exact"):
-        import torch
-        self.torch = torch
         self.lanes = lanes
         self.budget = int(hbm_budget)
         self.used = 0
@@ -138,35 +137,33 @@ class Server:
             return group
 
     def _lane(self, k):
-        torch = self.torch
-        stream = torch.cuda.Stream()
+        stream = Stream()
         hb = self.hbvlm_factory() if self.hbvlm_factory else None
-        with torch.cuda.stream(stream):
-            while True:
-                group = self._take()
-                if group is None:
-                    return
-                t0 = time.perf_counter()
+        while True:
+            group = self._take()
+            if group is None:
+                return
+            t0 = time.perf_counter()
+            for r in group:
+                r.start = t0
+            try:
+                kind = group[0].kind
+                if kind == "steady":
+                    self._steady(group, stream)
+                elif kind == "uvlm":
+                    self._uvlm(group[0], stream)
+                elif kind == "hbvlm":
+                    self._hbvlm(group[0], hb)
+                else:
+                    raise ValueError("unknown request kind " + kind)
+            except Exception as e:  # the request fails, the lane keeps serving
                 for r in group:
-                    r.start = t0
-                try:
-                    kind = group[0].kind
-                    if kind == "steady":
-                        self._steady(group, stream)
-                    elif kind == "uvlm":
-                        self._uvlm(group[0], stream)
-                    elif kind == "hbvlm":
-                        self._hbvlm(group[0], hb)
-                    else:
-                        raise ValueError("unknown request kind " + kind)
-                except Exception as e:  # the request fails, the lane keeps serving
-                    for r in group:
-                        r.error = e
-                t1 = time.perf_counter()
-                for r in group:
-                    r.finish = t1
-                    r.done.set()
-                self.stats[group[0].kind + "_groups"] += 1
+                    r.error = e
+            t1 = time.perf_counter()
+            for r in group:
+                r.finish = t1
+                r.done.set()
+            self.stats[group[0].kind + "_groups"] += 1
 
     def _steady(self, group, stream):
         cases = [r.payload[0] for r in group]

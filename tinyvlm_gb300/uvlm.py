@@ -16,6 +16,7 @@ from . import _lib
 from ._lib import P, PP, call, dims_array
 from .kinematics import to_colmajor
 from .vlm import read_plot3d
+from .device import stream_handle
 
 __all__ = ["UVLM", "kinematics_arrays"]
 
@@ -78,7 +79,7 @@ class UVLM:
         self.h = h
         keep = [np.ascontiguousarray(x) for x in (T, Td, fs, ref)]
         call("gbvlm_uvlm_set_kinematics", h, *[ctypes.c_void_p(x.ctypes.data) for x in keep])
-        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        s = stream_handle(stream)
         call("gbvlm_uvlm_run", h, float(dt), 1 if rollup else 0, float(sigma), s)
         cl = np.zeros(t_steps)
         cm = np.zeros((t_steps, 3))

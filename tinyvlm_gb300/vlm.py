@@ -12,6 +12,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import Coeffs, call, dims_array
+from .device import stream_handle
 
 __all__ = ["FlowData", "AeroCoefficients", "VLM", "NLVLM", "WingProfile", "Database", "read_plot3d"]
 
@@ -76,7 +77,7 @@ class VLM:
         out = Coeffs()
         rp = (ctypes.c_double * 3)(*ref_pt)
         g = np.zeros(self.n, np.float64) if return_gamma else None
-        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        s = stream_handle(stream)
         call("gbvlm_vlm_run", self.h, flow.alpha, flow.beta, flow.u_inf, flow.rho, ctypes.cast(rp, ctypes.c_void_p),
              ctypes.cast(ctypes.pointer(out), ctypes.c_void_p),
              ctypes.c_void_p(g.ctypes.data) if g is not None else None, s)
@@ -93,7 +94,7 @@ class VLM:
         out = (Coeffs * len(al))()
         rp = (ctypes.c_double * 3)(*ref_pt)
         g = np.zeros((len(al), self.n), np.float64) if return_gamma else None
-        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        s = stream_handle(stream)
         call("gbvlm_vlm_run_shared", self.h, len(al), ctypes.c_void_p(al.ctypes.data), float(u_inf), float(rho),
              ctypes.cast(rp, ctypes.c_void_p), ctypes.cast(out, ctypes.c_void_p),
              ctypes.c_void_p(g.ctypes.data) if g is not None else None, s)
@@ -166,7 +167,7 @@ class NLVLM:
         it = ctypes.c_int32()
         err = ctypes.c_double()
         strips = np.zeros(sum(ns for ns, _, _ in self.dims), np.float32)
-        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        s = stream_handle(stream)
         call("gbvlm_nlvlm_run", self.h, flow.alpha, flow.beta, flow.u_inf, flow.rho,
              ctypes.c_void_p(prof.alphas.ctypes.data), ctypes.c_void_p(prof.CL.ctypes.data), len(prof.alphas),
              float(self.tol), int(self.max_iter), ctypes.cast(ctypes.pointer(cl), ctypes.c_void_p),
