@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--ref-step-seconds", type=float, default=2.5,
                    help="reference arm: CPU time one step's fixed subset of the batch is sized to")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the short records of configurations A, B, C, E and the exact formulation")
     p.add_argument("--plain-solves", type=int, default=48)
     p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof", "nlvlm", "hbvlm"],
                    help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
@@ -339,6 +341,21 @@ def run_gpu(args):
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     roof = roofline(bs, stream, peaks, ms)
+    configs = None
+    if not args.no_configs:
+        # the other configurations, one short record each (outside the timed region of the headline)
+        configs = {}
+        for name, fn in (("A_elliptic16x16", lambda: config_a()),
+                         ("B_uvlm_20x80_500_steps", lambda: config_b(500)),
+                         ("C_elliptic128x128_64_alphas", lambda: config_c(128, 3, args.refine)),
+                         ("D_exact_formulation", lambda: exact_mode_rate(cases, 5, args.refine)),
+                         ("E_served_mixed_stream", lambda: config_e((16.0,), 30))):
+            t0 = time.perf_counter()
+            try:
+                configs[name] = fn()
+            except Exception as e:  # a failing side workload must not hide the headline
+                configs[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+            configs[name]["wall_s"] = time.perf_counter() - t0
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -353,15 +370,17 @@ def run_gpu(args):
         "stage_ms": prof,
         "plain_fp64_gpu": plain,
         "cpu_baseline": cpu,
+        "tuning": bs.tuning,
+        "configs": configs,
     }
     print(json.dumps(out))
 
 
-# DRAM bytes per algorithmic byte of the tensor-core trailing update, from
-# one ncu capture of k_update_tc on the 64-case batch (dram__bytes_read.sum +
-# dram__bytes_write.sum over the launch's algorithmic bytes; the operands are
-# re-read from L2, not DRAM).  Summary and command: profiles/k_update_tc_batch64.md
-TC_TRAFFIC_PER_ALG_BYTE = 0.747  # 140.4 MB DRAM / 187.9 MB algorithmic (outer block 128..256 of the 64-case batch)
+# DRAM bytes per algorithmic byte of the tensor-core trailing update
+# (dram__bytes_read.sum + dram__bytes_write.sum of k_update_tc over the
+# launches' algorithmic bytes; the operands are re-read from L2, not DRAM),
+# from one ncu capture of the 64-case batch
+TC_TRAFFIC_PER_ALG_BYTE = 0.747  # 140.4 MB DRAM / 187.9 MB algorithmic
 
 
 def roofline(bs, stream, peaks, ms_step):
@@ -421,8 +440,8 @@ def plain_path_rate(args, cases, dev, co):
     return out
 
 
-def run_large(args):
-    """128 x 128 elliptic wing (16,384 panels), 64 alphas in [-10, 10] deg on one AIC.
+def config_c(n=128, steps=3, refine=1):
+    """Config C: elliptic n x n wing (16,384 panels at n = 128), 64 alphas in [-10, 10] deg on one AIC.
 
     Float AIC, tensor-core LU and double-float refinement (the batched path),
     timed with CUDA events; then every alpha's error against the full double
@@ -431,96 +450,154 @@ def run_large(args):
     oracle's LAPACK dgetrf/dgetrs at 1e-9): ||gamma - gamma_64|| /
     ||gamma_64||, and CL and CM_y relative errors guarded near zero lift
     (denominator at least 1e-3 of the sweep's largest value)."""
-    import torch
+    from tinyvlm_gb300 import device as D
     from tinyvlm_gb300 import mesh as M
     from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
     from tinyvlm_gb300.vlm import VLM
-    v = M.elliptic(args.large_n, args.large_n).astype(np.float32)
+    v = M.elliptic(n, n).astype(np.float32)
     M.quarter_chord(v)
     al = np.radians(np.linspace(-10.0, 10.0, 64))
     case = M.Case(v, al, {})
-    bs = BatchSolver([case], mode="shared", refine=args.refine)
-    stream = torch.cuda.current_stream()
+    bs = BatchSolver([case], mode="shared", refine=refine)
+    stream = D.Stream()
     bs.set_inputs(pack_verts([case]), pack_alphas([case]), ref_pt=(0.0, 0.0, 0.0), stream=stream)
     bs.run(stream=stream)
-    torch.cuda.synchronize()
+    stream.synchronize()
     prof = bs.profile(stream=stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0, e1 = D.Event(), D.Event()
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         bs.run(stream=stream)
     e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    stream.synchronize()
+    ms = e0.elapsed_time(e1) / steps
     bs.run(want_gamma=True, stream=stream)
     co, gam = bs.results(gamma=True, stream=stream)
     lu = bs.lu_flops / (prof["lu_factor"] / 1000.0) / 1e12
     asm = FLOP_PER_INTERACTION * bs.interactions / (prof["assembly"] / 1000.0) / 1e12
-    # the full double solve of the same system, on the device
-    torch.cuda.synchronize()
+    D.synchronize()
     t0 = time.perf_counter()
     ref, g64 = VLM("gb300", [v], precision=64).run_shared(al, return_gamma=True)
     t64 = time.perf_counter() - t0
     cl64 = np.array([r.cl for r in ref])
     cm64 = np.array([r.cm[1] for r in ref])
     g_cl, g_cm = 1e-3 * np.abs(cl64).max(), 1e-3 * np.abs(cm64).max()
-    e_cl = [abs(co[k, 0] - cl64[k]) / max(abs(cl64[k]), g_cl) for k in range(64)]
-    e_cm = [abs(co[k, 3] - cm64[k]) / max(abs(cm64[k]), g_cm) for k in range(64)]
+    e_cl = [float(abs(co[k, 0] - cl64[k]) / max(abs(cl64[k]), g_cl)) for k in range(64)]
+    e_cm = [float(abs(co[k, 3] - cm64[k]) / max(abs(cm64[k]), g_cm)) for k in range(64)]
     e_g = [float(np.linalg.norm(gam[k].astype(np.float64) - g64[k]) / np.linalg.norm(g64[k])) for k in range(64)]
-    print(json.dumps({"workload": "large steady: elliptic %dx%d = %d panels, 64 alphas, one AIC" %
-                                  (args.large_n, args.large_n, args.large_n ** 2),
-                      "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof,
-                      "lu_tflops": lu, "assembly_tflops_alg": asm, "refine_iters": args.refine,
-                      "error_vs_fp64": {"alpha_deg": [round(float(a), 4) for a in np.degrees(al)],
-                                        "cl_rel": e_cl, "cm_rel": e_cm, "gamma_rel_norm": e_g,
-                                        "max": {"cl": max(e_cl), "cm": max(e_cm), "gamma": max(e_g)},
-                                        "target": 1e-5,
-                                        "reference": "device double assembly + double LU of the same system "
-                                                     "(plain per-operator path, gbvlm_vlm_run_shared precision 64)"},
-                      "plain_fp64_sweep_s": t64}))
+    return {"workload": "large steady: elliptic %dx%d = %d panels, 64 alphas, one AIC" % (n, n, n * n),
+            "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof, "lu_tflops": lu,
+            "assembly_tflops_alg": asm, "refine_iters": refine, "tuning": bs.tuning,
+            "error_vs_fp64": {"alpha_deg": [round(float(a), 4) for a in np.degrees(al)], "cl_rel": e_cl,
+                              "cm_rel": e_cm, "gamma_rel_norm": e_g,
+                              "max": {"cl": max(e_cl), "cm": max(e_cm), "gamma": max(e_g)}, "target": 1e-5,
+                              "reference": "device double assembly + double LU of the same system (plain "
+                                           "per-operator path, gbvlm_vlm_run_shared precision 64)"},
+            "plain_fp64_sweep_s": t64, "plain_fp64_solves_per_s": 64 / t64}
 
 
-def run_uvlm(args):
-    """20 x 80 rectangular half wing (chord 1, semispan 4), heave 0.1 sin(kt), pitch 3 deg sin(kt + 90 deg)
-    about the quarter chord, k = 0.5, dt = 0.05, 500 steps; float (reference semantics)."""
-    import torch
+def run_large(args):
+    print(json.dumps(config_c(args.large_n, args.steps, args.refine)))
+
+
+def config_a(repeats=50):
+    """Config A: the elliptic 16 x 16 half wing (b = 10, root chord 1, cosine spanwise spacing), alpha = 5
+    deg, one VLM::run per call through the plain per-solve path: float (the reference's semantics) and
+    double; latency per solve (median over `repeats` calls, each with its read-back) and CL."""
     from tinyvlm_gb300 import mesh as M
-    from tinyvlm_gb300.kinematics import Assembly, KinematicsTree, rotation_matrix, sin, translation_matrix
-    from tinyvlm_gb300.uvlm import UVLM, kinematics_arrays
-    v = M.rectangular(20, 80, 1.0, 4.0).astype(np.float32)
+    from tinyvlm_gb300.vlm import VLM, FlowData
+    v = M.elliptic(16, 16).astype(np.float32)
     M.quarter_chord(v)
-    k = 0.5
+    out = {"workload": "elliptic 16x16 = 256 panels, alpha 5 deg, VLM::run per call"}
+    for prec in (32, 64):
+        sim = VLM("gb300", [v], precision=prec)
+        fl = FlowData(math.radians(5.0))
+        sim.run(fl)
+        lat = []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            r = sim.run(fl)
+            lat.append(1000.0 * (time.perf_counter() - t0))
+        out["fp%d" % prec] = {"cl": r.cl, "cdi": r.cd, "p50_ms": float(np.percentile(lat, 50)),
+                              "p99_ms": float(np.percentile(lat, 99)), "solves_per_s": 1000.0 / float(np.median(lat))}
+    out["cl_fp32_vs_fp64"] = abs(out["fp32"]["cl"] - out["fp64"]["cl"]) / abs(out["fp64"]["cl"])
+    return out
+
+
+def pitch_plunge_assembly(k=0.5):
+    """Config B's motion: heave 0.1 sin(kt), pitch 3 deg sin(kt + 90 deg) about the quarter chord, u = 1."""
+    from tinyvlm_gb300.kinematics import Assembly, KinematicsTree, rotation_matrix, sin, translation_matrix
     tree = KinematicsTree()
     fs = tree.add(lambda t: translation_matrix([-t, 0.0, 0.0]))
     heave = tree.add(lambda t: translation_matrix([0.0, 0.0, 0.1 * sin(k * t)])).after(fs)
     pitch = tree.add(lambda t: rotation_matrix([0.25, 0, 0], [0, 1, 0], math.radians(3.0) * sin(k * t + math.pi / 2))).after(heave)
     asm = Assembly(fs)
     asm.add("wing", pitch)
+    return asm
+
+
+def config_b(steps=500, rollup=False):
+    """Config B: 20 x 80 rectangular half wing (chord 1, semispan 4), the pitch-plunge motion, dt = 0.05.
+    The float device time loop (reference semantics) timed end to end, and its CL(t) and CM_y(t) against
+    the double device time loop of the same run at every step (the double path matches the oracle's
+    double time loop to 1e-9 in the tests; the reference's own float CL(t) is pinned there to 2e-5)."""
+    from tinyvlm_gb300 import device as D
+    from tinyvlm_gb300 import mesh as M
+    from tinyvlm_gb300.uvlm import UVLM
+    v = M.rectangular(20, 80, 1.0, 4.0).astype(np.float32)
+    M.quarter_chord(v)
+    asm = pitch_plunge_assembly()
     sim = UVLM("gb300", [v], precision=32)
-    out = {"workload": "UVLM pitch-plunge: rectangular 20x80 = 1600 panels, %d steps, rollup=%d" %
-                       (args.uvlm_steps, args.rollup)}
-    for roll in sorted({0, args.rollup}):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = sim.run(asm, t_steps=args.uvlm_steps, dt=0.05, rollup=bool(roll))
-        torch.cuda.synchronize()
-        out["gpu_s_rollup%d" % roll] = time.perf_counter() - t0
-        out["cl_last_rollup%d" % roll] = float(r["cl"][-2])
+    sim.run(asm, t_steps=8, dt=0.05)  # warm-up
+    D.synchronize()
+    t0 = time.perf_counter()
+    r32 = sim.run(asm, t_steps=steps, dt=0.05, rollup=rollup)
+    D.synchronize()
+    s32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r64 = UVLM("gb300", [v], precision=64).run(asm, t_steps=steps, dt=0.05, rollup=rollup)
+    D.synchronize()
+    s64 = time.perf_counter() - t0
+    rec = slice(1, steps - 1)
+    cl_scale = float(np.abs(r64["cl"][rec]).max())
+    cm_scale = float(np.abs(r64["cm"][rec, 1]).max())
+    e_cl = np.abs(r32["cl"][rec] - r64["cl"][rec]) / cl_scale
+    e_cm = np.abs(r32["cm"][rec, 1] - r64["cm"][rec, 1]) / cm_scale
+    return {"workload": "UVLM pitch-plunge: rectangular 20x80 = 1600 panels, %d steps, dt 0.05, rollup %d, "
+                        "wake %d rings at the end" % (steps, int(rollup), 80 * (steps - 1)),
+            "float_s": s32, "steps_per_s": steps / s32, "double_s": s64,
+            "tuning": getattr(sim, "tuning", None),
+            "error_float_vs_double": {"cl_max_over_max_abs": float(e_cl.max()),
+                                      "cm_y_max_over_max_abs": float(e_cm.max()),
+                                      "cl_at_step_100_200_300_400_498": [float(e_cl[k - 1]) for k in
+                                                                         (100, 200, 300, 400, steps - 2) if
+                                                                         k - 1 < e_cl.size]},
+            "cl_last": float(r32["cl"][steps - 2])}
+
+
+def run_uvlm(args):
+    """Config B (see config_b), plus the CPU restatement timed on its first 40 steps."""
+    out = config_b(args.uvlm_steps, bool(args.rollup))
     if not args.no_cpu_baseline:
         from oracle import oracle as O
+        from tinyvlm_gb300 import device as D
+        from tinyvlm_gb300 import mesh as M
+        from tinyvlm_gb300.uvlm import UVLM, kinematics_arrays
+        v = M.rectangular(20, 80, 1.0, 4.0).astype(np.float32)
+        M.quarter_chord(v)
+        asm = pitch_plunge_assembly()
         steps = 40
         T, Td, fsv, ref = kinematics_arrays(asm, steps, 0.05)
         t0 = time.perf_counter()
         O.uvlm_run([v], [True], T, Td, fsv, ref, steps, 0.05, dtype=np.float32, rollup=False)
         cpu = time.perf_counter() - t0
-        torch.cuda.synchronize()
+        sim = UVLM("gb300", [v], precision=32)
+        D.synchronize()
         t0 = time.perf_counter()
         sim.run(asm, t_steps=steps, dt=0.05, rollup=False)
-        torch.cuda.synchronize()
-        out["sample_first_steps"] = steps
-        out["cpu_s_sample"] = cpu
-        out["gpu_s_sample"] = time.perf_counter() - t0
-        out["cpu_threads"] = O.num_threads()
+        D.synchronize()
+        out["cpu_baseline"] = {"sample": "first %d steps" % steps, "cpu_s": cpu, "gpu_s": time.perf_counter() - t0,
+                               "cores": O.num_threads(), "kind": "port"}
     print(json.dumps(out))
 
 
@@ -659,24 +736,24 @@ def run_hbvlm(args):
                                       "one_run_per_set_ms": seq}}))
 
 
-def run_served(args):
-    """Poisson mixed stream in equal thirds: steady VLM on trapezoids of 256-16,384 panels (log-uniform),
-    single UVLM steps on a resident 20x80 wing with a 500-row (40,000-ring) wake, 2-DOF HBVLM residuals
-    (45 x 1 section, 5 harmonics = 11 instances); p50/p99 latency and throughput per arrival rate."""
-    import torch
+def config_e(rates=(2.0, 8.0, 32.0), requests=45, seed=SEED):
+    """Config E: Poisson mixed stream in equal thirds -- steady VLM on trapezoids of 256-16,384 panels
+    (log-uniform), single UVLM steps on a resident 20x80 wing with a 500-row (40,000-ring) wake, 2-DOF
+    HBVLM residuals (45 x 1 section, 5 harmonics = 11 instances) -- through the server's lanes; per
+    arrival rate: p50/p99 latency (arrival to result), throughput, steady solves/s."""
     from tinyvlm_gb300 import serve as S
-    rng = np.random.default_rng(SEED)
-    rates = [float(x) for x in args.rates.split(",")]
-    total = len(rates) * args.requests
+    rng = np.random.default_rng(seed)
+    total = len(rates) * requests
     uvlm = S.resident_uvlm(warm_steps=500, capacity=total + 8)
     srv = S.Server(lanes=3, hbm_budget=48 << 30, max_batch=64, uvlm=uvlm, hbvlm=S.hbvlm_factory(45, 5)).start()
     out = {"workload": "served mixed stream (steady 256-16384 panels / UVLM step on a 40,000-ring wake / "
-                       "HBVLM 2-DOF 45x1, H=5), Poisson arrivals", "lanes": 3, "rates": []}
+                       "HBVLM 2-DOF 45x1, H=5), Poisson arrivals", "lanes": 3, "budget_bytes": srv.budget,
+           "rates": []}
     rid = 0
     for lam in rates:
         reqs = []
         t = time.perf_counter()
-        for _ in range(args.requests):
+        for _ in range(requests):
             t += rng.exponential(1.0 / lam)
             kind = ("steady", "uvlm", "hbvlm")[int(rng.integers(0, 3))]
             payload = (S.steady_case(rng),) if kind == "steady" else (S.hbvlm_request(rng) if kind == "hbvlm" else None)
@@ -689,21 +766,54 @@ def run_served(args):
             done.append(srv.submit(S.Request(rid, kind, payload, arrival=ta)))
             rid += 1
         for r in done:
-            r.done.wait()
-        lat = np.array([r.latency for r in done]) * 1000.0
-        span = max(r.finish for r in done) - min(r.arrival for r in done)
-        row = {"rate_req_s": lam, "completed": len(done), "errors": sum(r.error is not None for r in done),
-               "throughput_req_s": len(done) / span, "p50_ms": float(np.percentile(lat, 50)),
-               "p99_ms": float(np.percentile(lat, 99))}
+            r.done.wait(srv.wait_s)
+        fin = [r for r in done if r.finish is not None]
+        lat = np.array([r.latency for r in fin]) * 1000.0
+        span = max(r.finish for r in fin) - min(r.arrival for r in done)
+        steady = sum(len(r.payload[0].alphas) for r in fin if r.kind == "steady" and r.error is None)
+        row = {"rate_req_s": lam, "completed": len(fin), "errors": sum(r.error is not None for r in done),
+               "throughput_req_s": len(fin) / span, "steady_solves_per_s": steady / span,
+               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
         for kind in ("steady", "uvlm", "hbvlm"):
-            lk = np.array([r.latency for r in done if r.kind == kind]) * 1000.0
+            lk = np.array([r.latency for r in fin if r.kind == kind]) * 1000.0
             if lk.size:
                 row[kind] = {"n": int(lk.size), "p50_ms": float(np.percentile(lk, 50)),
                              "p99_ms": float(np.percentile(lk, 99))}
         out["rates"].append(row)
     srv.shutdown()
     out["stats"] = dict(srv.stats)
+    return out
+
+
+def run_served(args):
+    from tinyvlm_gb300 import device as D
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        out = config_e([float(x) for x in args.rates.split(",")], args.requests)
+        D.synchronize()
+    out["clocks"] = clk.summary()
     print(json.dumps(out))
+
+
+def exact_mode_rate(cases, steps=5, refine=1):
+    """The headline batch in the exact formulation (one AIC per case and alpha, the reference's
+    alpha-dependent system, VLM::run semantics): solves/s of graph replays, CUDA events."""
+    from tinyvlm_gb300 import device as D
+    from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+    bs = BatchSolver(cases, mode="exact", refine=refine)
+    stream = D.Stream()
+    bs.set_inputs(D.DeviceArray.from_numpy(pack_verts(cases)), pack_alphas(cases), ref_pt=(0.25, 0.0, 0.0),
+                  stream=stream)
+    for _ in range(3):
+        bs.run(stream=stream)
+    e0, e1 = D.Event(), D.Event()
+    e0.record(stream)
+    for _ in range(steps):
+        bs.run(stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"workload": "the headline batch, exact formulation (%d systems)" % bs.nsys, "ms_per_step": ms,
+            "solves_per_s": bs.nsolve / (ms / 1000.0), "tuning": bs.tuning}
 
 
 def main():

@@ -153,6 +153,30 @@ int gbvlm_event_elapsed_ms(gbvlm_event start, gbvlm_event end, float* ms);
 int gbvlm_device_info(int32_t* sm_count, int64_t* free_bytes, int64_t* total_bytes);
 
 /* ---------------------------------------------------------------------------
+ * Launch-shape tuning: no reference counterpart (the reference fixes its
+ * launch shapes, e.g. kernel_influence's (32, 16) blocks,
+ * vlm_backend_cuda.cu:171).  A process-wide table of named integer
+ * parameters; tinyvlm_gb300/autotune.py searches them per workload shape and
+ * keeps the choices in a committed table.  Defaults are the hand-measured
+ * shapes.  A batch plan copies the values when it is created; the other
+ * calls read them at each launch.
+ *   wake.waves           1..16   split-K slices of the wake sums: about
+ *                                waves x SMs CTAs (default 4)
+ *   hbvlm.waves          1..16   slices of the HBVLM wake operator (4)
+ *   hbvlm.min_rows       8..512  wake rows per operator slice at least (32)
+ *   batch.group_hi/lo            batch LU size groups: n > hi, lo < n <= hi,
+ *                                n <= lo (1024, 384); hi > lo
+ *   batch.loads_threads  0, 32, 64, 128, 256: the loads block (0: by size)
+ *   batch.assembly_span  64, 128, 256: rings per assembly span chunk (128)
+ * ------------------------------------------------------------------------- */
+int gbvlm_tune_set(const char* name, int64_t value);
+int gbvlm_tune_get(const char* name, int64_t* value);
+int gbvlm_tune_reset(void);
+/* The parameters: their number, and name and range by index. */
+int gbvlm_tune_count(int32_t* n);
+int gbvlm_tune_name(int32_t i, const char** name, int64_t* lo, int64_t* hi);
+
+/* ---------------------------------------------------------------------------
  * Backend operators.  Replaces the pure virtuals of vlm::Backend
  * (vlm/include/vlm_backend.hpp:31-55); semantics follow the CPU backend
  * vlm/backends/cpu/src/vlm_backend_cpu.cpp (f32) and vlm_backend_cpud.cpp (f64).

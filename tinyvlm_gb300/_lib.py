@@ -67,6 +67,11 @@ def _protos():
         t["gbvlm_blas_scal_" + sfx] = [I64, R, P, I64, P]
         t["gbvlm_blas_nrm2_" + sfx] = [I64, P, I64, P, P]
         t["gbvlm_lsq_solve_" + sfx] = [I64, I64, P, I64, P, I64, I64, P]
+    t["gbvlm_tune_set"] = [ctypes.c_char_p, I64]
+    t["gbvlm_tune_get"] = [ctypes.c_char_p, P]
+    t["gbvlm_tune_reset"] = []
+    t["gbvlm_tune_count"] = [P]
+    t["gbvlm_tune_name"] = [I32, P, P, P]
     t["gbvlm_mem_alloc"] = [I32, I64, P]
     t["gbvlm_mem_free"] = [I32, P]
     t["gbvlm_mem_copy"] = [I32, P, I64, I32, P, I64, I64, I64, P]

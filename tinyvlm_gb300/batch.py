@@ -27,8 +27,17 @@ def pack_alphas(cases):
 
 
 class BatchSolver:
-    def __init__(self, cases, mode="shared", refine=1):
+    def __init__(self, cases, mode="shared", refine=1, tuned=True):
+        """``tuned``: take the plan's launch shapes from the autotuner's table
+        for this workload's shape (autotune.batch_key); otherwise the
+        library's current parameters."""
         self.mode = mode
+        self.tuning = None
+        if tuned:
+            from . import autotune
+            self.tuning = autotune.apply(autotune.batch_key([(c.ns, c.nc) for c in cases],
+                                                            [len(c.alphas) for c in cases], mode, refine,
+                                                            autotune.device_sms()))
         self.dims = [(c.ns, c.nc, 0) for c in cases]
         self.nalpha = [len(c.alphas) for c in cases]
         d = dims_array(self.dims)

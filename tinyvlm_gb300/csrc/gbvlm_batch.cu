@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
 // assembly: tiles (system, 128-row block, chordwise ring row, span chunk)
 // ---------------------------------------------------------------------------
 constexpr int BA_THREADS = 128;
-constexpr int BA_SPAN = 128;  // rings per span chunk
-constexpr int BA_W = BA_SPAN + 1;
+// rings per span chunk: a template parameter (64, 128 or 256) chosen per
+// plan from the tuning table (batch.assembly_span), 128 by default
 
 struct HL {
     float h, l;
@@ -146,7 +146,7 @@ struct HL {
 
 // Walk a strip of rings with double-float positions (top/bot: hi planes at
 // topH[k*BA_W], lo planes at topL[k*BA_W]); f(ring, 4*pi*(v.n + v'.n')).
-template <class F>
+template <int BA_W, class F>
 __device__ __forceinline__ void strip_hl(const float* topH, const float* topL, const float* botH, const float* botL,
                                          int nvs, HL px, HL py, HL pz, float nx, float ny, float nz, F&& f) {
     auto rel = [&](const float* H, const float* L, int sl, bool mir) {
@@ -194,7 +194,9 @@ __device__ __forceinline__ int find_sys(const int64_t* pfx, int cnt, int64_t b) 
 
 // tile0: the first tile of this launch (a size group's systems are a
 // contiguous range of tiles)
+template <int BA_SPAN>
 __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
+    constexpr int BA_W = BA_SPAN + 1;
     __shared__ float sw[2][2][3 * BA_W];  // [row][hi/lo][plane*W + s]
     const int64_t tile = tile0 + blockIdx.x;
     const int si = find_sys(tpfx, a.nsys, tile);
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
     float* colB = S.A2 ? S.A2 + i + (c * ns + s0) * n : nullptr;
     const bool te = (c == nc - 1);
     if (!te) {
-        strip_hl(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz, [&](int kk, float v) {
+        strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz, [&](int kk, float v) {
             const float val = v * k4;
             colA[(int64_t)kk * n] = val;
             if (colB) colB[(int64_t)kk * n] = val;
@@ -233,8 +235,8 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
     }
     // trailing-edge ring row: wing ring plus the wake ring behind it (Kutta
     // condition, vlm_backend_cpu.cpp:121-139 with iteration = 1)
-    strip_hl(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz,
-             [&](int kk, float v) { colA[(int64_t)kk * n] = v; });
+    strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz,
+                   [&](int kk, float v) { colA[(int64_t)kk * n] = v; });
     const int64_t wl = 2 * (ns + 1);
     for (int64_t s = s0; s < s1; s++) {
         // wake ring: v0=(s,TE) v1=(s+1,TE) v2=(s+1,far) v3=(s,far)
@@ -541,6 +543,7 @@ using namespace gbvlm;
 // ===========================================================================
 struct gbvlm_batch_s {
     int32_t ncases = 0, nsys = 0, nsolve = 0, mode = 0, refine = 1;
+    TuneParams tp;                    // launch shapes, copied from the tuning table at creation
     std::vector<gbvlm_dims> dims;
     std::vector<int32_t> nalpha;
     std::vector<int64_t> case_voff;   // float offsets of case vertices in the input buffer
@@ -604,6 +607,16 @@ constexpr int MAX_GROUPS_B = 2;  // size-group boundaries (gbvlm_batch_s::MAX_GR
 
 // serial_lu: factor the size groups one after another on `st` (kernel timing
 // without the groups' launches overlapping)
+// the assembly kernel of the plan's span chunk over `tiles` tiles from tile0
+static cudaError_t launch_assemble(gbvlm_batch h, unsigned tiles, int64_t tile0, const BatchArgs& a, cudaStream_t st) {
+    switch (h->tp.batch_assembly_span) {
+        case 64: k_batch_assemble<64><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
+        case 256: k_batch_assemble<256><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
+        default: k_batch_assemble<128><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
+    }
+    return cudaGetLastError();
+}
+
 static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullptr, bool serial_lu = false) {
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     int64_t nlaunch = 0;
@@ -645,8 +658,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     if (staged) GB_CUDA(trefftz());
     mark(1);
     if (staged) {
-        k_batch_assemble<<<(unsigned)h->assembly_tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, 0);
-        GB_LAUNCH_CHECK();
+        GB_CUDA(launch_assemble(h, (unsigned)h->assembly_tiles, 0, a, st));
     }
     mark(2);
     dim3 gp((unsigned)cdiv(h->maxn, 256), (unsigned)h->nsys);  // one thread per row of every system
@@ -665,9 +677,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         for (int g = 0; g < h->ngroups; g++) {
             GB_CUDA(cudaStreamWaitEvent(h->side[g], h->fork, 0));
             if (h->gtile[g][1] > 0) {
-                k_batch_assemble<<<(unsigned)h->gtile[g][1], BA_THREADS, 0, h->side[g]>>>(a, h->d_tpfx,
-                                                                                       h->gtile[g][0]);
-                GB_LAUNCH_CHECK();
+                GB_CUDA(launch_assemble(h, (unsigned)h->gtile[g][1], h->gtile[g][0], a, h->side[g]));
             }
             int rc = lu_batch_factor<float>(h->lub, h->plans[g], h->side[g], true);
             if (rc) return rc;
@@ -701,11 +711,20 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         GB_LAUNCH_CHECK();
     }
     mark(5);
-    if (h->maxn > 4096)
-        k_batch_loads<LD_THREADS_LARGE><<<h->nsolve, LD_THREADS_LARGE, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
-    else
-        k_batch_loads<LD_THREADS_SMALL><<<h->nsolve, LD_THREADS_SMALL, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
-    GB_LAUNCH_CHECK();
+    {
+        // the loads block: by the largest system, or the tuned width
+        const int64_t lt = h->tp.batch_loads_threads ? h->tp.batch_loads_threads
+                                                     : (h->maxn > 4096 ? LD_THREADS_LARGE : LD_THREADS_SMALL);
+        if (lt == 32)
+            k_batch_loads<32><<<h->nsolve, 32, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+        else if (lt == 64)
+            k_batch_loads<64><<<h->nsolve, 64, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+        else if (lt == 128)
+            k_batch_loads<128><<<h->nsolve, 128, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+        else
+            k_batch_loads<256><<<h->nsolve, 256, 0, st>>>(a, h->d_solve_sys, h->want_gamma);
+        GB_LAUNCH_CHECK();
+    }
     mark(6);
     return GBVLM_OK;
 }
@@ -717,7 +736,11 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     GB_REQUIRE(out && dims && nalpha && ncases >= 1, "bad batch arguments");
     GB_REQUIRE(mode == GBVLM_BATCH_EXACT || mode == GBVLM_BATCH_SHARED, "unknown batch mode %d", mode);
     GB_REQUIRE(refine_iters >= 0 && refine_iters <= 8, "refine_iters outside [0, 8]");
+    const TuneParams tp = tune();
+    GB_REQUIRE(tp.batch_group_hi > tp.batch_group_lo, "batch.group_hi (%lld) must exceed batch.group_lo (%lld)",
+               (long long)tp.batch_group_hi, (long long)tp.batch_group_lo);
     auto* h = new gbvlm_batch_s();
+    h->tp = tp;
     h->ncases = ncases;
     h->mode = mode;
     h->refine = refine_iters;
@@ -817,7 +840,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     for (int k = 0; k < h->nsys; k++) {
         const gbvlm_dims& d = dims[protos[order[k]].case_id];
         const int64_t n = protos[order[k]].n;
-        tpfx[k + 1] = tpfx[k] + cdiv(n, BA_THREADS) * cdiv(d.ns, BA_SPAN) * d.nc;
+        tpfx[k + 1] = tpfx[k] + cdiv(n, BA_THREADS) * cdiv(d.ns, h->tp.batch_assembly_span) * d.nc;
         rpfx[k + 1] = rpfx[k] + cdiv(n, RS_THREADS * RS_ROWS);
     }
     h->assembly_tiles = tpfx[h->nsys];
@@ -952,9 +975,10 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
     h->lub.nrhs = (const int32_t*)(base + o_lurhs);
     h->lub.perm = (int32_t* const*)(base + o_luperm);
     h->lub.mv = (int32_t*)(base + o_lumv);
-    // size groups: n > 1024, 384 < n <= 1024, n <= 384 (empty groups dropped)
+    // size groups: n > hi, lo < n <= hi, n <= lo (by default 1024 and 384;
+    // empty groups dropped)
     {
-        const int64_t bounds[MAX_GROUPS_B] = {1024, 384};
+        const int64_t bounds[MAX_GROUPS_B] = {h->tp.batch_group_hi, h->tp.batch_group_lo};
         int i0 = 0;
         int greatest = 0, least = 0;
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
@@ -984,10 +1008,11 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         // every system and every block of 8 right-hand sides in one dataflow
         // launch; GBVLM_TRS_FLOW=0 selects the per-system solves (k_trsolve,
         // or 128-row blocks on the tensor cores for one large system)
+        // (beyond the dataflow solve's limits the plan keeps the per-system solves)
         const char* fe = getenv("GBVLM_TRS_FLOW");
-        h->use_flow = !(fe && fe[0] == '0');
         int32_t mr = 1;
         for (auto& sy : h->sys) mr = std::max(mr, sy.nrhs);
+        h->use_flow = !(fe && fe[0] == '0') && trs_flow_fits(h->nsys, (mr + 7) / 8);
         if (h->use_flow) rc = trs_flow_build(h->flow, lun, 0, (mr + 7) / 8);
     }
     if (rc) {

@@ -958,18 +958,19 @@ struct HbState {
         const gbvlm_dims& W = dims[wake_surf];
         const int64_t ninst = (int64_t)K * N;
         const int64_t npairs = n * W.ns, xb = cdiv(npairs, WOP_THREADS);
-        // each instance's rows in about four waves' worth of slices of one
-        // instance (at least 32 rows each): its partial sums, and so its
-        // result, do not depend on the other sets of the batch
-        const int64_t slices = std::max<int64_t>(1, cdiv(4 * 152, xb));
+        // each instance's rows in about `hbvlm.waves` waves' worth of slices
+        // of one instance (at least `hbvlm.min_rows` rows each): its partial
+        // sums, and so its result, do not depend on the other sets of the batch
+        const TuneParams tp = tune();
+        const int64_t slices = std::max<int64_t>(1, cdiv(tp.hbvlm_waves * sm_count(), xb));
         int64_t max_it = 1;
         for (int64_t e = 0; e < ninst; e++) {
             wtab[e].omega = omega[e / N];
             wtab[e].dt = dt[e / N];
-            wtab[e].rps = std::max<int64_t>(32, cdiv(wtab[e].it, slices));
+            wtab[e].rps = std::max<int64_t>(tp.hbvlm_min_rows, cdiv(wtab[e].it, slices));
             max_it = std::max(max_it, wtab[e].it);
         }
-        const int64_t zs = std::min(slices, cdiv(max_it, 32));
+        const int64_t zs = std::min(slices, cdiv(max_it, tp.hbvlm_min_rows));
         GB_CUDA(cudaMemcpyAsync(d_wop, wtab.data(), sizeof(WopInst) * ninst, cudaMemcpyHostToDevice, st));
         WopArgs a;
         a.inst = d_wop;

@@ -31,6 +31,21 @@ inline cudaStream_t to_cuda(gbvlm_stream s) { return reinterpret_cast<cudaStream
 
 inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Launch-shape parameters (gbvlm_tune_set); defaults are the hand-measured
+// shapes, the autotuner's table overrides them per workload shape.
+struct TuneParams {
+    int64_t wake_waves = 4;            // split-K slices of the wake sums: about waves x SMs CTAs
+    int64_t hbvlm_waves = 4;           // slices of the HBVLM wake operator, likewise
+    int64_t hbvlm_min_rows = 32;       // wake rows per operator slice at least
+    int64_t batch_group_hi = 1024;     // batch LU size groups: n > hi, lo < n <= hi, n <= lo
+    int64_t batch_group_lo = 384;
+    int64_t batch_loads_threads = 0;   // loads block: 0 = 64 up to 4096 unknowns, 256 beyond
+    int64_t batch_assembly_span = 128; // rings per span chunk of a batch assembly tile
+};
+TuneParams tune();
+// SM count of the current device (cached per device)
+int sm_count();
+
 // Per-thread pinned staging buffer for synchronous scalar read-backs.
 void* host_scratch(size_t bytes);
 // Per-device small device buffer for reductions (grown on demand).

@@ -2363,7 +2363,7 @@ struct gbvlm_lu_s {
 static int lu_flow_ready(gbvlm_lu h, int64_t n, int64_t nrhs, cudaStream_t st, bool* use) {
     const char* fe = getenv("GBVLM_TRS_FLOW");
     const int64_t groups64 = (nrhs + 7) / 8;
-    *use = !(fe && fe[0] == '0') && n > 2 * FL_B && groups64 <= 1024;  // the dataflow solve's group limit
+    *use = !(fe && fe[0] == '0') && n > 2 * FL_B && trs_flow_fits(1, groups64);
     if (!*use) return GBVLM_OK;
     const int32_t groups = (int32_t)groups64;
     if (h->flow_n == n && h->flow_groups >= groups) return GBVLM_OK;

@@ -126,6 +126,9 @@ struct TrsFlow {
 // n_sorted: sizes of all systems of the batch, in batch order; groups: how
 // many blocks of 8 right-hand sides one launch solves side by side
 int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_t st, int32_t groups = 1);
+// whether one dataflow solve can take nsys systems with `groups` groups of
+// 8 right-hand sides (item words hold the system in 20 bits)
+inline bool trs_flow_fits(int64_t nsys, int64_t groups) { return nsys <= (1 << 20) && groups <= 1024; }
 int trs_flow_solve(const LuBatch<float>& B, const TrsFlow& f, int32_t max_nrhs, cudaStream_t st);
 int64_t trs_flow_launches(int32_t max_nrhs, int32_t groups = 1);
 // GBVLM_OK, or an error if a wait of the last solve ran out (synchronises st)

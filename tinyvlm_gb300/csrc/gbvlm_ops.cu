@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -568,8 +569,11 @@ static int wake_influence(T* rhs, int32_t nsurf, const gbvlm_dims* dims, const T
     if (total == 0) return GBVLM_OK;
     const int64_t ntg = w.s.poff[nsurf];
     const int64_t xblocks = cdiv(ntg, WK_THREADS);
-    // enough slices to cover ~4 waves of 152 SMs, at least WK_ROWS rows each
-    int64_t want = cdiv(4 * 152, xblocks);
+    // enough slices to cover about `wake.waves` waves of the device's SMs
+    // (tuned per shape), at least WK_ROWS rows each; a caller-owned scratch
+    // caps the slice count at what it holds
+    int64_t want = cdiv(tune().wake_waves * sm_count(), xblocks);
+    if (scratch != nullptr) want = std::min<int64_t>(want, (int64_t)(scratch_elems / (size_t)ntg));
     int64_t slices = want < 1 ? 1 : want;
     int64_t rps = cdiv(total, slices);
     if (rps < WK_ROWS) rps = WK_ROWS;

@@ -359,7 +359,7 @@ class _HBVLMBase:
                 c["ref_b"] = (series[1][0][sf] @ np.array([refs[1], 0.0, 0.0, 1.0]))[:, :3]
         return cols
 
-    def _run_sets(self, sets, refs, forces_list, coupled_te):
+    def _run_sets(self, sets, refs, forces_list, coupled_te, params=None):
         """HBVLM::run for K parameter sets (libhbvlm3.cpp:262-552), solved together.
 
         sets: dicts with ``omega``, ``t_start`` and the kinematic parameters
@@ -371,6 +371,13 @@ class _HBVLMBase:
         N, H = self.m_coeffs, self.m_harmonics
         cols = self.plan(sets, refs)
         K = len(cols)
+        from . import autotune
+        if params is not None:  # the autotuner's search sets the shapes itself
+            autotune.set_params(params)
+            self.tuning = {"params": dict(params), "source": "given"}
+        else:
+            self.tuning = autotune.apply(autotune.hbvlm_key(self.engine.n, K * N, max(c["max_t"] for c in cols),
+                                                            autotune.device_sms()))
         self.engine.prepare_batch_chain(H, [c["max_t"] for c in cols],
                                   [self._chain_vector(S, c["dt"]) for S, c in zip(sets, cols)],
                                   np.concatenate([c["inst"][0] for c in cols]),
@@ -480,8 +487,13 @@ class HBVLM2(_HBVLMBase):
         r = np.asarray(S["dyn"], np.float64)
         return self.U_INF, (r[0], r[1], None), 1.0 + self.A_H, None, False
 
+    @staticmethod
+    def parameter_set(omega, dyn_f):
+        """One run's parameters (libhbvlm.cpp:470-515): three cycles of wake before the period."""
+        return dict(omega=omega, dyn=dyn_f, t_start=3.0 * TWO_PI_F / omega)
+
     def run(self, omega, dyn_f, forces_t):
-        S = dict(omega=omega, dyn=dyn_f, t_start=3.0 * TWO_PI_F / omega)
+        S = self.parameter_set(omega, dyn_f)
         self.iterations = int(self._run_sets([S], (0.5,), [forces_t], False)[0])
         return forces_t
 

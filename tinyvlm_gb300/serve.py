@@ -4,21 +4,28 @@ single-step advances of a resident unsteady case, and harmonic-balance
 
 Design
 ------
-* ``lanes`` worker threads, each with its own CUDA stream; the library
-  calls release the GIL, so work of different lanes overlaps on the device.
+* ``lanes`` dispatcher threads, each with its own CUDA stream (a slot on the
+  device); the library calls release the GIL, so the work of different
+  lanes overlaps on the device.
 * One FIFO queue.  A lane that takes a steady request also takes every
   other steady request already waiting (continuous batching) up to
   ``max_batch`` cases and the free HBM budget, and solves them as one
-  batched graph (``tinyvlm_gb300.batch``); requests arriving meanwhile wait
-  for the next free lane.
-* Admission by HBM budget: each request reserves its device footprint
-  (AIC + work arrays for steady batches, the resident states are reserved
-  at start-up) before launch and releases it when done; a request that does
-  not fit waits at the head of the queue.
+  batched plan (``tinyvlm_gb300.batch``, one refinement sweep); requests
+  arriving meanwhile wait for the next free lane.
+* Admission by HBM budget: the budget is the smaller of ``hbm_budget`` and
+  the device memory free when the server starts; each request reserves its
+  device footprint (AIC and work arrays of its batch) before launch and
+  releases it when done; a request that does not fit waits at the head of
+  the queue.
+* Every wait is bounded: lanes sleep on the queue's condition until a
+  request or shutdown arrives, and a reservation, a UVLM step's turn or a
+  request's completion that takes longer than ``wait_s`` fails with
+  TimeoutError instead of hanging the server.
 * The UVLM case (wing, wake, AIC factors) and one HBVLM engine per lane
-  stay resident; a UVLM request advances the case by one time step (steps
-  are serialised, they depend on each other), an HBVLM request runs the
-  harmonic-balance fixed point for its own frequency and amplitudes.
+  stay resident on the device; a UVLM request advances the case by one time
+  step (steps run in arrival order, they depend on each other), an HBVLM
+  request runs the harmonic-balance fixed point for its own frequency and
+  amplitudes from rest.
 
 Every result carries its arrival, start and finish times; ``latency`` is
 finish - arrival.
@@ -32,7 +39,7 @@ import numpy as np
 
 from . import mesh as M
 from .batch import BatchSolver, pack_alphas, pack_verts
-from .device import Stream
+from .device import Stream, stream_handle
 
 
 class Request:
@@ -56,9 +63,14 @@ def steady_bytes(n, nalpha=1):
 
 
 class Server:
-    def __init__(self, lanes=3, hbm_budget=32 << 30, max_batch=64, uvlm=None, hbvlm=None, mode="exact"):
+    def __init__(self, lanes=3, hbm_budget=32 << 30, max_batch=64, uvlm=None, hbvlm=None, mode="exact", refine=1,
+                 wait_s=120.0):
+        from .device import device_info
         self.lanes = lanes
-        self.budget = int(hbm_budget)
+        free = device_info()[1]
+        self.budget = int(min(hbm_budget, free))
+        self.refine = refine
+        self.wait_s = float(wait_s)
         self.used = 0
         self.max_batch = max_batch
         self.mode = mode
@@ -75,11 +87,16 @@ class Server:
 
     # -- resident state -----------------------------------------------------
     def reserve(self, nbytes, block=True):
+        """Reserve device bytes of the budget; waits (bounded) for releases."""
+        deadline = time.monotonic() + self.wait_s
         with self.cv:
             while self.used + nbytes > self.budget:
+                left = deadline - time.monotonic()
                 if not block:
                     return False
-                self.cv.wait(0.01)
+                if left <= 0:
+                    raise TimeoutError("no %d bytes of the device budget freed within %.0f s" % (nbytes, self.wait_s))
+                self.cv.wait(left)
             self.used += nbytes
             return True
 
@@ -113,7 +130,7 @@ class Server:
     def _take(self):
         with self.cv:
             while not self.q and not self.stop:
-                self.cv.wait(0.05)
+                self.cv.wait()  # submit() and shutdown() notify
             if not self.q:
                 return None
             head = self.q.popleft()
@@ -172,7 +189,7 @@ class Server:
             raise MemoryError("steady request needs %d bytes, above the %d-byte device budget" % (need, self.budget))
         self.reserve(need)
         try:
-            bs = BatchSolver(cases, mode=self.mode, refine=0)
+            bs = BatchSolver(cases, mode=self.mode, refine=self.refine)
             bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=(0.25, 0.0, 0.0), stream=stream)
             bs.run(want_gamma=False, stream=stream, graph=False)  # solved once: no graph capture
             co, _ = bs.results(stream=stream)
@@ -189,16 +206,20 @@ class Server:
         import ctypes
         from ._lib import P, call
         ticket = req.payload
+        deadline = time.monotonic() + self.wait_s
         with self.uvlm_cv:
             while self.uvlm_turn != ticket:
-                self.uvlm_cv.wait(0.01)
+                left = deadline - time.monotonic()
+                if left <= 0:
+                    raise TimeoutError("UVLM step %d did not get its turn within %.0f s" % (ticket, self.wait_s))
+                self.uvlm_cv.wait(left)
         try:
             sim = self.uvlm
             step = ctypes.c_int64()
             cl = ctypes.c_double()
             cm = (ctypes.c_double * 3)()
             call("gbvlm_uvlm_step", sim.h, ctypes.cast(ctypes.pointer(step), P), ctypes.cast(ctypes.pointer(cl), P),
-                 ctypes.cast(cm, P), ctypes.c_void_p(stream.cuda_stream))
+                 ctypes.cast(cm, P), stream_handle(stream))
             req.result = (step.value, cl.value, tuple(cm))
         finally:
             with self.uvlm_cv:
@@ -255,6 +276,7 @@ def resident_uvlm(ns=80, nc=20, warm_steps=500, capacity=4096, rollup=False):
 
     sim = Sim()
     sim.verts = v
+    sim.assembly = asm
     d = dims_array([(ns, nc, 0)])
     arr = (ctypes.c_void_p * 1)(v.ctypes.data)
     lf = (ctypes.c_int32 * 1)(1)

@@ -67,6 +67,9 @@ class UVLM:
         if t_steps is None:
             t_steps = int(t_final / dt)
         T, Td, fs, ref = kinematics_arrays(assembly, t_steps, dt)
+        from . import autotune
+        npts = sum((v.shape[1] - 1) * (v.shape[2] - 1) for v in self.verts)
+        self.tuning = autotune.apply(autotune.wake_key(npts, t_steps // 2, autotune.device_sms()))
         lifting = assembly.lifting if assembly.lifting else [True] * len(self.verts)
         dims = dims_array([(v.shape[2] - 1, v.shape[1] - 1, 0) for v in self.verts])
         arr = (ctypes.c_void_p * len(self.verts))(*[v.ctypes.data for v in self.verts])
