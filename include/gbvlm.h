@@ -624,6 +624,13 @@ int gbvlm_read_plot3d(const char* path, int32_t quarter_chord, gbvlm_dims* dims,
  * timeout message when the bounded wait works; the CUDA context stays
  * usable. */
 int gbvlm_test_flow_wait_timeout(int32_t n, gbvlm_stream stream);
+/* Test hook with no counterpart in the reference: one tensor-core update tile
+ * (128 x 128, K = 32) whose MMA-issuing thread issues and commits nothing, so
+ * the tile's bounded mbarrier wait must run out (after 2 s).  No MMA is in
+ * flight; the tile frees its tensor memory and sets its error word.  Returns
+ * GBVLM_ERR_CUDA with the timeout message when the bounded wait works; the
+ * CUDA context stays usable. */
+int gbvlm_test_tc_wait_timeout(gbvlm_stream stream);
 
 /* ---------------------------------------------------------------------------
  * Nonlinear VLM: NLVLM::run (vlm/include/vlm.hpp:87-115, vlm/src/vlm.cpp:

@@ -2,7 +2,7 @@
 
 Run from the repository root:  python -m tests.golden.make_golden
 Writes tests/golden/vlm_generated.json (generated planforms) and, when the
-reference tree is mounted at /root/reference, vlm_reference_meshes.json
+reference tree is found (TINYVLM_REF, default /root/reference), vlm_reference_meshes.json
 (the reference's own test meshes, read with its plot3d conventions).  Each
 case stores the oracle's CL, CDi, CM and a checksum of gamma so later runs
 (and the GPU path) can be compared without the reference tree.
@@ -20,7 +20,7 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 from tinyvlm_gb300 import mesh as M  # noqa: E402
 
-REF_MESH = "/root/reference/mesh"
+REF_MESH = os.path.join(os.environ.get("TINYVLM_REF", "/root/reference"), "mesh")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -1,8 +1,8 @@
 """Golden vectors of the Newmark-beta integrator from the reference's own
 Python implementation (scripts/newmark.py, numpy only).
 
-Run from the repository root with the reference tree mounted at
-/root/reference:  python -m tests.golden.make_newmark_golden
+Run from the repository root with the reference tree at TINYVLM_REF
+(default /root/reference):  python -m tests.golden.make_newmark_golden
 Writes tests/golden/newmark_3dof.json: the 3-DOF free response that the
 reference's tests/newmark.cpp integrates (M = I, its C and K, u0 = 0,
 v0 = 1, dt = 0.1, t = 0..20), stepped with scripts/newmark.py's
@@ -15,7 +15,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SCRIPT = "/root/reference/scripts/newmark.py"
+SCRIPT = os.path.join(os.environ.get("TINYVLM_REF", "/root/reference"), "scripts", "newmark.py")
 
 # the system of tests/newmark.cpp:66-92 (column-major there; symmetric here)
 K = np.array([[400.0, -200.0, 0.0], [-200.0, 400.0, -200.0], [0.0, -200.0, 200.0]])

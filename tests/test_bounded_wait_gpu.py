@@ -1,8 +1,10 @@
 """Failure path of the bounded waits: the dataflow triangular solve's wait
-for a block that never finishes runs out (2 s), the launch reports it as an
+for a block that never finishes, and a tensor-core update tile's wait for
+MMAs that are never committed, run out (2 s); the launch reports it as an
 error with its message, and the CUDA context stays usable (a batch solve
-afterwards gives the right answer).  No fault, trap or hang: the wait is a
-polled counter with a time limit."""
+afterwards gives the right answer).  No fault, trap or hang: the waits are
+polled (a counter, an mbarrier) with a time limit, and the withheld work is
+work that is never issued."""
 import numpy as np
 import pytest
 
@@ -29,3 +31,11 @@ def test_wait_runs_out_and_context_survives(cuda):
         for r in O.vlm_shared([c.verts.astype(np.float64)], c.alphas, ref_pt=(0.25, 0.0, 0.0)):
             assert abs(co[k, 0] - float(r["cl"])) <= 1e-5 * max(abs(float(r["cl"])), 1e-3)
             k += 1
+
+
+def test_tensor_core_tile_wait_runs_out_and_context_survives(cuda):
+    L = _lib.lib()
+    rc = L.gbvlm_test_tc_wait_timeout(None)
+    assert rc == 2, (rc, L.gbvlm_last_error())  # GBVLM_ERR_CUDA
+    assert b"timed out" in L.gbvlm_last_error()
+    test_wait_runs_out_and_context_survives(cuda)

@@ -56,10 +56,7 @@ def test_akima_nodes_and_lines():
         assert abs(O.akima_eval(lin, q) - (2.0 * q - 1.0)) < 1e-12
 
 
-REF_MESH = "/root/reference/mesh"
-
-
-@pytest.mark.skipif(not os.path.isdir(REF_MESH), reason="reference meshes not mounted")
 def test_reference_mesh_is_the_generated_one():
-    v = O.read_plot3d(os.path.join(REF_MESH, "infinite_rectangular_5x200.x"))
+    from tests import ref_fixtures as R
+    v = R.mesh("infinite_rectangular_5x200")
     assert np.abs(v - rectangle_5x200()).max() == 0.0

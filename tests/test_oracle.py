@@ -5,10 +5,11 @@ The reference stores no golden arrays; its tests pin this path analytically:
     lifting-line 2 pi alpha / (1 + 2/AR), alpha in {0,1,2,3,4,5,10,15} deg;
   * tests/vlm_square_coeffs.cpp:15-57    "infinite" rectangles (semispan
     40000) incl. a two-surface split, CL within 1 % of 2 pi alpha.
-The reference meshes are used when the reference tree is mounted; the
-generated equivalents always run.  Golden fixtures made by
-tests/golden/make_golden.py (which also read the reference meshes) are
-re-checked here so a change to the oracle is caught.
+The reference meshes come from tests/golden/ref_meshes.npz (the numbers
+the reference's own plot3d reader returns for its mesh files, written by
+tests/golden/make_ref_golden.py); the generated equivalents run too.
+Golden fixtures made by tests/golden/make_golden.py are re-checked here so a
+change to the oracle is caught.
 """
 import json
 import math
@@ -18,9 +19,9 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from tests import ref_fixtures as R
 from tinyvlm_gb300 import mesh as M
 
-REF_MESH = "/root/reference/mesh"
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 ALPHAS = [0, 1, 2, 3, 4, 5, 10, 15]
 
@@ -66,22 +67,18 @@ def test_square_kat_generated():
     _check_square([a, b])
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MESH), reason="reference meshes not mounted")
 def test_elliptic_kat_reference_mesh():
-    _check_elliptic(O.read_plot3d(os.path.join(REF_MESH, "elliptic_45x45.x")))
+    _check_elliptic(R.mesh("elliptic_45x45"))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MESH), reason="reference meshes not mounted")
 def test_square_kat_reference_meshes():
-    _check_square([O.read_plot3d(os.path.join(REF_MESH, "infinite_rectangular_2x2_part0.x")),
-                   O.read_plot3d(os.path.join(REF_MESH, "infinite_rectangular_2x2_part1.x"))])
-    for m in ("infinite_rectangular_2x4.x", "infinite_rectangular_10x5.x", "infinite_rectangular_20x5.x"):
-        _check_square([O.read_plot3d(os.path.join(REF_MESH, m))])
+    _check_square([R.mesh("infinite_rectangular_2x2_part0"), R.mesh("infinite_rectangular_2x2_part1")])
+    for m in ("infinite_rectangular_2x4", "infinite_rectangular_10x5", "infinite_rectangular_20x5"):
+        _check_square([R.mesh(m)])
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MESH), reason="reference meshes not mounted")
 def test_generated_square_equals_reference_mesh():
-    ref = O.read_plot3d(os.path.join(REF_MESH, "infinite_rectangular_10x5.x"))
+    ref = R.mesh("infinite_rectangular_10x5")
     v = M.rectangular(10, 5, 1.0, 40000.0).astype(np.float32)
     M.quarter_chord(v)
     np.testing.assert_allclose(v, ref, rtol=1e-6, atol=1e-6)

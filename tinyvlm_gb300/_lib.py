@@ -96,6 +96,7 @@ def _protos():
     t["gbvlm_vlm_run_shared"] = [P, I32, P, F64, F64, P, P, P, P]
     t["gbvlm_read_plot3d"] = [ctypes.c_char_p, I32, P, P]
     t["gbvlm_test_flow_wait_timeout"] = [I32, P]
+    t["gbvlm_test_tc_wait_timeout"] = [P]
     t["gbvlm_nlvlm_create"] = [P, I32, P, PP, I32]
     t["gbvlm_nlvlm_destroy"] = [P]
     t["gbvlm_nlvlm_run"] = [P, F64, F64, F64, F64, P, P, I32, F64, I32, P, P, P, P, P]

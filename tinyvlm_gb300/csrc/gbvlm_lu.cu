@@ -2476,9 +2476,47 @@ void lu_solve_tables_free(void* tables) {
     delete t;
 }
 
+// test hook kernel: one tensor-core tile whose MMA thread withholds its
+// MMAs and commit (update_tile<1, true>), over a 128 x 128 matrix, K = 32
+__global__ void __launch_bounds__(tc::THREADS) k_test_tc_withhold(float* A, int* err) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tslot;
+    tc::update_tile<1, true>(A, 128, A, 128, A, 128, 128, 128, tc::BK, tc_smem, bar, &tslot, err);
+}
+
 }  // namespace gbvlm
 
 extern "C" {
+
+int gbvlm_test_tc_wait_timeout(gbvlm_stream stream) {
+    cudaStream_t st = to_cuda(stream);
+    float* A = nullptr;
+    int* err = nullptr;
+    auto run = [&]() -> int {
+        GB_CUDA(cudaMalloc(&A, sizeof(float) * 128 * 128));
+        GB_CUDA(cudaMalloc(&err, sizeof(int)));
+        GB_CUDA(cudaMemsetAsync(A, 0, sizeof(float) * 128 * 128, st));
+        GB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        GB_CUDA(cudaFuncSetAttribute(k_test_tc_withhold, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+        k_test_tc_withhold<<<1, tc::THREADS, tc::SMEM_BYTES, st>>>(A, err);
+        GB_LAUNCH_CHECK();
+        int h = 0;
+        GB_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        if (h != 0) {
+            set_error("tensor-core update tile: the wait for its MMAs timed out");
+            return GBVLM_ERR_CUDA;
+        }
+        set_error("tensor-core update tile: the withheld MMAs were not detected");
+        return GBVLM_ERR_STATE;
+    };
+    const int rc = run();
+    cudaStreamSynchronize(st);
+    if (A) cudaFree(A);
+    if (err) cudaFree(err);
+    return rc;
+}
 
 int gbvlm_test_flow_wait_timeout(int32_t n, gbvlm_stream stream) {
     GB_REQUIRE(n > FL_B && n <= 4 * FL_B, "n must span 2 to 4 blocks of %d rows", FL_B);

@@ -163,7 +163,10 @@ __device__ __forceinline__ void st_shared_f32(uint32_t addr, float a) {
 // One 128 x 128 tile: C(r0.., c0..) -= L(r0.., 0..K) * U(0..K, c0..).
 //   L(r, kk) = Lp[r + kk * ldl], U(kk, c) = Up[kk + c * ldu], C(r, c) = Cp[r + c * ldc];
 //   rows r < m_rows and columns c < n_cols exist (tile-relative bounds).
-template <int PASSES>
+// WITHHOLD (a test hook's instantiation only): the MMA thread issues and
+// commits nothing, so the bounded mbarrier waits must run out; no MMA is
+// ever in flight, the CTA frees its tensor memory and sets the error word.
+template <int PASSES, bool WITHHOLD = false>
 __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const float* Up, int64_t ldu, float* Cp,
                                             int64_t ldc, int m_rows, int n_cols, int K, unsigned char* smem_raw,
                                             uint64_t* bar, uint32_t* tslot, int* err) {
@@ -234,7 +237,7 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
         fence_before_sync();
         ok = __syncthreads_and(free_) != 0;  // uniform over the CTA
         if (!ok) break;
-        if (tid == 0) {
+        if (tid == 0 && !WITHHOLD) {
             fence_after_sync();
 #pragma unroll
             for (int ks = 0; ks < BK / 8; ks++) {
