@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--requests", type=int, default=45, help="served: requests per rate")
     p.add_argument("--rollup", type=int, default=1)
     p.add_argument("--large-n", type=int, default=128, help="large: chordwise = spanwise panels of the elliptic wing")
+    p.add_argument("--large-geometry", default="reference", choices=["reference", "generated"],
+                   help="large: the reference's elliptic mesh (tip chord 0.0707) or the zero-tip-chord analytic one")
     return p.parse_args()
 
 
@@ -440,8 +442,22 @@ def plain_path_rate(args, cases, dev, co):
     return out
 
 
-def config_c(n=128, steps=3, refine=1):
+def reference_mesh(name):
+    """A mesh of the reference's mesh/ directory, (4, nc+1, ns+1) float32, quarter-chord shifted, from the
+    committed fixture tests/golden/ref_meshes.npz (the numbers the reference's own plot3d reader returns)."""
+    from tinyvlm_gb300 import mesh as M
+    xyz = np.load(os.path.join(ROOT, "tests", "golden", "ref_meshes.npz"))[name]
+    v = np.ones((4,) + xyz.shape[1:], np.float32)
+    v[:3] = xyz
+    M.quarter_chord(v)
+    return v
+
+
+def config_c(n=128, steps=3, refine=1, geometry="reference"):
     """Config C: elliptic n x n wing (16,384 panels at n = 128), 64 alphas in [-10, 10] deg on one AIC.
+    geometry "reference": the reference's mesh/elliptic_128x128.x (tip chord 0.0707); "generated": the
+    literal analytic planform with a zero tip chord, whose AIC is singular to working precision at this
+    spanwise count (its errors measure the conditioning, not the solver).
 
     Float AIC, tensor-core LU and double-float refinement (the batched path),
     timed with CUDA events; then every alpha's error against the full double
@@ -454,8 +470,11 @@ def config_c(n=128, steps=3, refine=1):
     from tinyvlm_gb300 import mesh as M
     from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
     from tinyvlm_gb300.vlm import VLM
-    v = M.elliptic(n, n).astype(np.float32)
-    M.quarter_chord(v)
+    if geometry == "reference":
+        v = reference_mesh("elliptic_%dx%d" % (n, n))
+    else:
+        v = M.elliptic(n, n).astype(np.float32)
+        M.quarter_chord(v)
     al = np.radians(np.linspace(-10.0, 10.0, 64))
     case = M.Case(v, al, {})
     bs = BatchSolver([case], mode="shared", refine=refine)
@@ -485,7 +504,8 @@ def config_c(n=128, steps=3, refine=1):
     e_cl = [float(abs(co[k, 0] - cl64[k]) / max(abs(cl64[k]), g_cl)) for k in range(64)]
     e_cm = [float(abs(co[k, 3] - cm64[k]) / max(abs(cm64[k]), g_cm)) for k in range(64)]
     e_g = [float(np.linalg.norm(gam[k].astype(np.float64) - g64[k]) / np.linalg.norm(g64[k])) for k in range(64)]
-    return {"workload": "large steady: elliptic %dx%d = %d panels, 64 alphas, one AIC" % (n, n, n * n),
+    return {"workload": "large steady: elliptic %dx%d = %d panels (%s geometry), 64 alphas, one AIC" %
+                        (n, n, n * n, geometry),
             "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof, "lu_tflops": lu,
             "assembly_tflops_alg": asm, "refine_iters": refine, "tuning": bs.tuning,
             "error_vs_fp64": {"alpha_deg": [round(float(a), 4) for a in np.degrees(al)], "cl_rel": e_cl,
@@ -497,7 +517,7 @@ def config_c(n=128, steps=3, refine=1):
 
 
 def run_large(args):
-    print(json.dumps(config_c(args.large_n, args.steps, args.refine)))
+    print(json.dumps(config_c(args.large_n, args.steps, args.refine, args.large_geometry)))
 
 
 def config_a(repeats=50):

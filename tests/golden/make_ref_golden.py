@@ -44,7 +44,7 @@ from tinyvlm_gb300 import mesh as M  # noqa: E402
 HERE = os.path.dirname(os.path.abspath(__file__))
 ALPHAS = [0, 1, 2, 3, 4, 5, 10, 15]
 
-REF_MESHES = ["elliptic_16x16.x", "elliptic_45x45.x", "infinite_rectangular_2x2_part0.x",
+REF_MESHES = ["elliptic_16x16.x", "elliptic_45x45.x", "elliptic_128x128.x", "infinite_rectangular_2x2_part0.x",
               "infinite_rectangular_2x2_part1.x", "infinite_rectangular_2x4.x", "infinite_rectangular_10x5.x",
               "infinite_rectangular_20x5.x", "swept_4x4.x", "rectangular_5x10.x", "infinite_rectangular_5x100.x",
               "infinite_rectangular_5x200.x", "3dof_wing_9x5.x", "3dof_flap_3x5.x", "3dof_wing_45x1.x",

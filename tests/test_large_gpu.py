@@ -1,7 +1,14 @@
 """Large steady path: one AIC, many right-hand sides (the 64-alpha sweep of
 the 16,384-panel workload), against the full double solve at 1e-5: on a
 24 x 32 elliptic wing with and without refinement, and at the configured
-128 x 128 size."""
+128 x 128 size on the reference's own elliptic wing.
+
+The literal analytic planform, chord sqrt(1 - (2y/b)^2) down to a zero tip
+chord with cosine spanwise spacing, is not used at the large size.  Its
+degenerate tip rings make the AIC singular to working precision as the
+spanwise count grows (cond_1 4.6e6 at 64 x 64, 1.5e13 at 80 x 80), beyond
+any solve that stores the AIC in float.  The reference's elliptic meshes
+end at a 0.0707 tip chord (cond_1 1.6e3 at 16 x 16, 6.4e3 at 45 x 45)."""
 import math
 
 import numpy as np
@@ -50,12 +57,13 @@ def _errors(co, gam, ref):
 
 
 def test_config_c_16384_panels_64_alphas_vs_full_double(cuda):
-    """Config C at its configured size: elliptic 128 x 128 = 16,384 panels, 64 alphas in [-10, 10] deg on
-    one AIC; float AIC, tensor-core LU and one double-float refinement sweep against the oracle's full double
-    solve (double assembly, LAPACK dgetrf/dgetrs).  Every alpha: CL and CM_y (guarded near zero lift) and
-    ||gamma - gamma_64|| / ||gamma_64|| within 1e-5."""
-    v = M.elliptic(128, 128).astype(np.float32)
-    M.quarter_chord(v)
+    """Config C at its configured size: the reference's elliptic 128 x 128 = 16,384-panel wing
+    (mesh/elliptic_128x128.x), 64 alphas in [-10, 10] deg on one AIC; float AIC, tensor-core LU and one
+    double-float refinement sweep against the oracle's full double solve (double assembly, LAPACK
+    dgetrf/dgetrs).  Every alpha: CL and CM_y (guarded near zero lift) and ||gamma - gamma_64|| /
+    ||gamma_64|| within 1e-5."""
+    from tests import ref_fixtures as R
+    v = R.mesh("elliptic_128x128")
     al = np.radians(np.linspace(-10.0, 10.0, 64))
     case = M.Case(v, al, {})
     bs = BatchSolver([case], mode="shared", refine=1)

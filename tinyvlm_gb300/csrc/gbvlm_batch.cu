@@ -8,7 +8,9 @@
 //                       (vlm/src/vlm.cpp:97-116, vlm_backend_cpu.cpp:391-433);
 //                       positions stored as float hi/lo pairs
 //   assembly  (float)   AIC from relative vectors formed in double-float, so
-//                       input rounding does not enter (vlm_backend_cpu.cpp:84-148)
+//                       input rounding does not enter (vlm_backend_cpu.cpp:84-148);
+//                       the double kernel's cut-offs (ispc:393), since the
+//                       path solves the FP64 system
 //   factor    (float)   variable-size batched LU (gbvlm_lu.cu)
 //   solve     (float + double refinement) residual b - A x in double against
 //                       an unfactored copy of A
@@ -163,8 +165,8 @@ __device__ __forceinline__ void strip_hl(const float* topH, const float* topL, c
     Rel<float> B0 = rel(topH, topL, 0, true), B3 = rel(botH, botL, 0, true);
     float lx, ly, lz;
     sv(botH, botL, 0, topH, topL, 0, lx, ly, lz);
-    float Ca = seg_normal<float, false>(A0, A3, lx, ly, lz, nx, ny, nz, 0.f);
-    float Cb = seg_normal<float, false>(B0, B3, lx, ly, lz, nx, -ny, nz, 0.f);
+    float Ca = seg_normal<float, false, true>(A0, A3, lx, ly, lz, nx, ny, nz, 0.f);
+    float Cb = seg_normal<float, false, true>(B0, B3, lx, ly, lz, nx, -ny, nz, 0.f);
     for (int k = 1; k < nvs; k++) {
         const Rel<float> A1 = rel(topH, topL, k, false), A2 = rel(botH, botL, k, false);
         const Rel<float> B1 = rel(topH, topL, k, true), B2 = rel(botH, botL, k, true);
@@ -172,12 +174,12 @@ __device__ __forceinline__ void strip_hl(const float* topH, const float* topL, c
         sv(botH, botL, k, topH, topL, k, cx, cy, cz);          // v1 -> v2
         sv(topH, topL, k, topH, topL, k - 1, tx, ty, tz);      // v0 -> v1
         sv(botH, botL, k - 1, botH, botL, k, bx, by, bz);      // v2 -> v3
-        const float Cra = seg_normal<float, false>(A1, A2, cx, cy, cz, nx, ny, nz, 0.f);
-        const float Crb = seg_normal<float, false>(B1, B2, cx, cy, cz, nx, -ny, nz, 0.f);
-        float val = seg_normal<float, false>(A0, A1, tx, ty, tz, nx, ny, nz, 0.f) + Cra +
-                    seg_normal<float, false>(A2, A3, bx, by, bz, nx, ny, nz, 0.f) - Ca;
-        val += seg_normal<float, false>(B0, B1, tx, ty, tz, nx, -ny, nz, 0.f) + Crb +
-               seg_normal<float, false>(B2, B3, bx, by, bz, nx, -ny, nz, 0.f) - Cb;
+        const float Cra = seg_normal<float, false, true>(A1, A2, cx, cy, cz, nx, ny, nz, 0.f);
+        const float Crb = seg_normal<float, false, true>(B1, B2, cx, cy, cz, nx, -ny, nz, 0.f);
+        float val = seg_normal<float, false, true>(A0, A1, tx, ty, tz, nx, ny, nz, 0.f) + Cra +
+                    seg_normal<float, false, true>(A2, A3, bx, by, bz, nx, ny, nz, 0.f) - Ca;
+        val += seg_normal<float, false, true>(B0, B1, tx, ty, tz, nx, -ny, nz, 0.f) + Crb +
+               seg_normal<float, false, true>(B2, B3, bx, by, bz, nx, -ny, nz, 0.f) - Cb;
         f(k - 1, val);
         A0 = A1; A3 = A2; B0 = B1; B3 = B2; Ca = Cra; Cb = Crb;
     }
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
                 const float rx = df_sub(Qh[e][0], Ql[e][0], Qh[q][0], Ql[q][0]);
                 const float ry = df_sub(Qh[e][1], Ql[e][1], Qh[q][1], Ql[q][1]);
                 const float rz = df_sub(Qh[e][2], Ql[e][2], Qh[q][2], Ql[q][2]);
-                val += seg_normal<float, false>(R[q], R[e], rx, ry, rz, nx, mir ? -ny : ny, nz, 0.f);
+                val += seg_normal<float, false, true>(R[q], R[e], rx, ry, rz, nx, mir ? -ny : ny, nz, 0.f);
             }
         }
         float* dst = colA + (s - s0) * n;

@@ -109,8 +109,12 @@ __device__ __forceinline__ Rel<T> make_rel(T x, T y, T z) {
     return r;
 }
 
-// scalar k with v(A->B) = k * (r0 x a) / (4 pi); the cross product is returned in c
-template <class T, bool SIGMA>
+// scalar k with v(A->B) = k * (r0 x a) / (4 pi); the cross product is returned in c.
+// DCUT: the double kernel's |r1|, |r2| cut-off (1e-10) in T's arithmetic: the
+// batched mixed-precision path solves the FP64 system, whose near field is
+// not cut at the float kernel's 1e-5 (a wing with panels smaller than 1e-4
+// -- the tip strips of a finely cosine-spaced elliptic wing -- differs there)
+template <class T, bool SIGMA, bool DCUT = false>
 __device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T r0x, T r0y, T r0z, T sigma2, T& cx,
                                        T& cy, T& cz) {
     cx = r0y * a.z - r0z * a.y;
@@ -120,7 +124,8 @@ __device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T r0x, 
     const T ab = a.x * b.x + a.y * b.y + a.z * b.z;
     const T nab = a.n * b.n;
     const T sum = a.n + b.n;
-    const bool cut = (sq < (T)RCUT_SQ) | (a.n < Prec<T>::rcut_norm) | (b.n < Prec<T>::rcut_norm);
+    constexpr T rcut = DCUT ? (T)RCUT_NORM_D : Prec<T>::rcut_norm;
+    const bool cut = (sq < (T)RCUT_SQ) | (a.n < rcut) | (b.n < rcut);
     const bool pos = ab >= (T)0;
     T num = pos ? sum : sum * (nab - ab);
     T den = pos ? nab * (nab + ab) : nab * sq;
@@ -136,11 +141,11 @@ __device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T r0x, 
 }
 
 // 4*pi * (velocity of segment A->B) . nrm
-template <class T, bool SIGMA>
+template <class T, bool SIGMA, bool DCUT = false>
 __device__ __forceinline__ T seg_normal(const Rel<T>& a, const Rel<T>& b, T r0x, T r0y, T r0z, T nx, T ny, T nz,
                                         T sigma2) {
     T cx, cy, cz;
-    const T k = seg_coeff<T, SIGMA>(a, b, r0x, r0y, r0z, sigma2, cx, cy, cz);
+    const T k = seg_coeff<T, SIGMA, DCUT>(a, b, r0x, r0y, r0z, sigma2, cx, cy, cz);
     return k * (cx * nx + cy * ny + cz * nz);
 }
 

@@ -69,7 +69,8 @@ class UVLM:
         T, Td, fs, ref = kinematics_arrays(assembly, t_steps, dt)
         from . import autotune
         npts = sum((v.shape[1] - 1) * (v.shape[2] - 1) for v in self.verts)
-        self.tuning = autotune.apply(autotune.wake_key(npts, t_steps // 2, autotune.device_sms()))
+        # keyed by the final wake length: the last, longest wake sums take most of a run's time
+        self.tuning = autotune.apply(autotune.wake_key(npts, t_steps, autotune.device_sms()))
         lifting = assembly.lifting if assembly.lifting else [True] * len(self.verts)
         dims = dims_array([(v.shape[2] - 1, v.shape[1] - 1, 0) for v in self.verts])
         arr = (ctypes.c_void_p * len(self.verts))(*[v.ctypes.data for v in self.verts])
