@@ -411,8 +411,9 @@ def roofline(bs, stream, peaks, ms_step):
 
 
 def plain_path_rate(args, cases, dev, co):
-    """The plain per-solve double path on the GPU (one VLM::run per solve) on
-    a sample of the cases, and the batched path's CL/CM deviation from it."""
+    """The plain per-solve GPU path (one VLM::run per solve) on a sample of the
+    cases, in double (the comparison the batched path is held to) and in
+    float, and the batched path's CL/CM deviation from the double results."""
     if args.plain_solves <= 0:
         return None
     import torch
@@ -424,17 +425,26 @@ def plain_path_rate(args, cases, dev, co):
         total += len(cases[i].alphas)
         if total >= args.plain_solves:
             break
-    sims = {i: VLM("gb300", [cases[i].verts], precision=64) for i in picks}
-    res = []
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in picks:
-        for q, a in enumerate(cases[i].alphas):
-            res.append((start[i] + q, sims[i].run(FlowData(a), ref_pt=(0.25, 0.0, 0.0))))
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+
+    def timed(prec):
+        sims = {i: VLM("gb300", [cases[i].verts], precision=prec) for i in picks}
+        res = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in picks:
+            for q, a in enumerate(cases[i].alphas):
+                res.append((start[i] + q, sims[i].run(FlowData(a), ref_pt=(0.25, 0.0, 0.0))))
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t0
+
+    res, dt = timed(64)
+    res32, dt32 = timed(32)
     out = {"value": len(res) / dt, "unit": "solves/s", "solves": len(res),
-           "what": "plain per-solve double GPU path (VLM::run semantics, one solve per call, double throughout)"}
+           "what": "plain per-solve double GPU path (VLM::run semantics, one solve per call, double throughout)",
+           "fp32": {"value": len(res32) / dt32, "unit": "solves/s", "solves": len(res32),
+                    "what": "the same calls with the float kernels (the reference's float backend semantics)",
+                    "max_rel_err_cl_vs_fp64": max(abs(b.cl - a.cl) / max(abs(a.cl), 1e-3)
+                                                  for (_, a), (_, b) in zip(res, res32))}}
     if co is not None:  # same formulation (per-alpha AIC) only
         cl_err = max(abs(co[k, 0] - r.cl) / max(abs(r.cl), 1e-3) for k, r in res)
         cm_err = max(float(np.abs(co[k, 2:5] - np.array(r.cm)).max() / max(np.abs(r.cm).max(), 1e-6)) for k, r in res)
@@ -459,13 +469,16 @@ def config_c(n=128, steps=3, refine=1, geometry="reference"):
     literal analytic planform with a zero tip chord, whose AIC is singular to working precision at this
     spanwise count (its errors measure the conditioning, not the solver).
 
-    Float AIC, tensor-core LU and double-float refinement (the batched path),
-    timed with CUDA events; then every alpha's error against the full double
-    solve of the same system on the device (double assembly, double LU,
-    gbvlm_vlm_run_shared at precision 64, which the tests hold to the
-    oracle's LAPACK dgetrf/dgetrs at 1e-9): ||gamma - gamma_64|| /
-    ||gamma_64||, and CL and CM_y relative errors guarded near zero lift
-    (denominator at least 1e-3 of the sweep's largest value)."""
+    Float AIC, tensor-core LU and refinement with the FP64 residual (the
+    batched path with GBVLM_BATCH_FP64_RESIDUAL: the residual's AIC is the
+    float one plus its float-pair correction), timed with CUDA events; then
+    every alpha's error against the full double solve of the same system on
+    the device (double assembly, double LU, gbvlm_vlm_run_shared at
+    precision 64, which the tests hold to the oracle's LAPACK dgetrf/dgetrs
+    at 1e-9): ||gamma - gamma_64|| / ||gamma_64||, and CL and CM_y relative
+    errors guarded near zero lift (denominator at least 1e-3 of the sweep's
+    largest value).  The same plan without the correction (residual of the
+    stored float AIC) is timed and its errors reported beside it."""
     from tinyvlm_gb300 import device as D
     from tinyvlm_gb300 import mesh as M
     from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
@@ -477,42 +490,67 @@ def config_c(n=128, steps=3, refine=1, geometry="reference"):
         M.quarter_chord(v)
     al = np.radians(np.linspace(-10.0, 10.0, 64))
     case = M.Case(v, al, {})
-    bs = BatchSolver([case], mode="shared", refine=refine)
-    stream = D.Stream()
-    bs.set_inputs(pack_verts([case]), pack_alphas([case]), ref_pt=(0.0, 0.0, 0.0), stream=stream)
-    bs.run(stream=stream)
-    stream.synchronize()
-    prof = bs.profile(stream=stream)
-    e0, e1 = D.Event(), D.Event()
-    e0.record(stream)
-    for _ in range(steps):
+
+    def measure(fp64_residual):
+        bs = BatchSolver([case], mode="shared", refine=refine, fp64_residual=fp64_residual)
+        stream = D.Stream()
+        bs.set_inputs(pack_verts([case]), pack_alphas([case]), ref_pt=(0.0, 0.0, 0.0), stream=stream)
         bs.run(stream=stream)
-    e1.record(stream)
-    stream.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    bs.run(want_gamma=True, stream=stream)
-    co, gam = bs.results(gamma=True, stream=stream)
-    lu = bs.lu_flops / (prof["lu_factor"] / 1000.0) / 1e12
-    asm = FLOP_PER_INTERACTION * bs.interactions / (prof["assembly"] / 1000.0) / 1e12
-    D.synchronize()
+        stream.synchronize()
+        prof = bs.profile(stream=stream)
+        e0, e1 = D.Event(), D.Event()
+        e0.record(stream)
+        for _ in range(steps):
+            bs.run(stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        bs.run(want_gamma=True, stream=stream)
+        co, gam = bs.results(gamma=True, stream=stream)
+        out = dict(ms=ms, prof=prof, co=co, gam=gam, lu_flops=bs.lu_flops, interactions=bs.interactions,
+                   tuning=bs.tuning, arena_bytes=bs.arena_bytes)
+        del bs
+        D.synchronize()
+        return out
+
+    flt = measure(False)
+    m = measure(True)
     t0 = time.perf_counter()
     ref, g64 = VLM("gb300", [v], precision=64).run_shared(al, return_gamma=True)
     t64 = time.perf_counter() - t0
     cl64 = np.array([r.cl for r in ref])
     cm64 = np.array([r.cm[1] for r in ref])
     g_cl, g_cm = 1e-3 * np.abs(cl64).max(), 1e-3 * np.abs(cm64).max()
-    e_cl = [float(abs(co[k, 0] - cl64[k]) / max(abs(cl64[k]), g_cl)) for k in range(64)]
-    e_cm = [float(abs(co[k, 3] - cm64[k]) / max(abs(cm64[k]), g_cm)) for k in range(64)]
-    e_g = [float(np.linalg.norm(gam[k].astype(np.float64) - g64[k]) / np.linalg.norm(g64[k])) for k in range(64)]
+
+    def errors(r):
+        co, gam = r["co"], r["gam"]
+        e_cl = [float(abs(co[k, 0] - cl64[k]) / max(abs(cl64[k]), g_cl)) for k in range(64)]
+        e_cm = [float(abs(co[k, 3] - cm64[k]) / max(abs(cm64[k]), g_cm)) for k in range(64)]
+        e_g = [float(np.linalg.norm(gam[k].astype(np.float64) - g64[k]) / np.linalg.norm(g64[k])) for k in range(64)]
+        return e_cl, e_cm, e_g
+
+    e_cl, e_cm, e_g = errors(m)
+    f_cl, f_cm, f_g = errors(flt)
+    prof = m["prof"]
+    lu = m["lu_flops"] / (prof["lu_factor"] / 1000.0) / 1e12
+    asm = FLOP_PER_INTERACTION * m["interactions"] / (flt["prof"]["assembly"] / 1000.0) / 1e12
+    ms = m["ms"]
     return {"workload": "large steady: elliptic %dx%d = %d panels (%s geometry), 64 alphas, one AIC" %
                         (n, n, n * n, geometry),
             "ms_per_run": ms, "solves_per_s": 64 / (ms / 1000.0), "stage_ms": prof, "lu_tflops": lu,
-            "assembly_tflops_alg": asm, "refine_iters": refine, "tuning": bs.tuning,
+            "assembly_tflops_alg": asm,
+            "assembly_correction_ms": prof["assembly"] - flt["prof"]["assembly"],
+            "refine_iters": refine, "residual": "fp64 (float AIC + float-pair correction)",
+            "arena_bytes": m["arena_bytes"], "tuning": m["tuning"],
             "error_vs_fp64": {"alpha_deg": [round(float(a), 4) for a in np.degrees(al)], "cl_rel": e_cl,
                               "cm_rel": e_cm, "gamma_rel_norm": e_g,
                               "max": {"cl": max(e_cl), "cm": max(e_cm), "gamma": max(e_g)}, "target": 1e-5,
                               "reference": "device double assembly + double LU of the same system (plain "
                                            "per-operator path, gbvlm_vlm_run_shared precision 64)"},
+            "float_residual": {"what": "the same plan, residual of the stored float AIC",
+                               "ms_per_run": flt["ms"], "solves_per_s": 64 / (flt["ms"] / 1000.0),
+                               "stage_ms": flt["prof"],
+                               "max_error_vs_fp64": {"cl": max(f_cl), "cm": max(f_cm), "gamma": max(f_g)}},
             "plain_fp64_sweep_s": t64, "plain_fp64_solves_per_s": 64 / t64}
 
 

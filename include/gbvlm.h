@@ -428,11 +428,24 @@ int gbvlm_vlm_run_shared(gbvlm_vlm h, int32_t nalpha, const double* alphas, doub
  *                       VLM; fewer factorizations).
  * ------------------------------------------------------------------------- */
 enum { GBVLM_BATCH_EXACT = 0, GBVLM_BATCH_SHARED = 1 };
+/* Plan flags of gbvlm_batch_create_ex.
+ *   GBVLM_BATCH_FP64_RESIDUAL: the refinement residual b - A x measures the
+ *     FP64 system, not its float-rounded copy.  The plan also evaluates the
+ *     AIC in float-pair arithmetic (about 44 bits, fp32 pipes) and keeps the
+ *     difference from the stored float AIC (one more n x n float per
+ *     system), so the refined circulations converge to the FP64 system's
+ *     solution: gamma, not only CL/CM, within 1e-5 of the FP64 LU solve of a
+ *     system whose condition number is near 1e4 (the reference's elliptic
+ *     128 x 128 wing).  Needs refine_iters >= 1. */
+enum { GBVLM_BATCH_FP64_RESIDUAL = 1 };
 typedef struct gbvlm_batch_s* gbvlm_batch;
 
 /* dims[c].ns/.nc: panels of case c; nalpha[c] in [1, 64] angles. */
 int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims, const int32_t* nalpha,
                        int32_t mode, int32_t refine_iters);
+/* gbvlm_batch_create with plan flags (GBVLM_BATCH_FP64_RESIDUAL). */
+int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims, const int32_t* nalpha,
+                          int32_t mode, int32_t refine_iters, int32_t flags);
 int gbvlm_batch_destroy(gbvlm_batch h);
 /* Sizes of the plan: solves (= sum nalpha), systems, gamma floats, Biot-Savart
  * ring-point interactions and LU flops per run, device bytes held. */

@@ -61,6 +61,49 @@ def test_batch_matches_double_oracle(cuda, mode, refine):
     _check(co2, None, cases, mode)
 
 
+@pytest.mark.parametrize("mode", ["shared", "exact"])
+def test_fp64_residual_converges_to_the_double_solution(cuda, mode):
+    """GBVLM_BATCH_FP64_RESIDUAL: the residual's AIC is the stored float AIC plus its float-pair correction, so
+    the refinement converges to the double system's solution.  Two sweeps bring every gamma within 3e-7 of
+    ||gamma_64|| (the float rounding of the stored result is 6e-8) and CL/CM within 1e-7.  Cases in all three
+    LU size groups (n > 1024, 384 < n <= 1024, n <= 384), each group's correction on its own graph branch;
+    the graph, its replay, the eager launch sequence and the staged (profiled) run agree."""
+    cases = M.batch_cases(12, seed=17, n_alpha=2, nc_range=(4, 32), ns_range=(4, 64))
+    n = [c.n for c in cases]
+    assert max(n) > 1024 and min(n) <= 384 and any(384 < x <= 1024 for x in n)
+    bs = BatchSolver(cases, mode=mode, refine=2, fp64_residual=True)
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run(want_gamma=True)
+    co, gam = bs.results(gamma=True)
+    k = 0
+    for c in cases:
+        for r in _ref(mode, c):
+            g = np.concatenate([x.ravel() for x in r["gamma"]])
+            assert np.linalg.norm(gam[k] - g) <= 3e-7 * np.linalg.norm(g), ("gamma", mode, k)
+            cl = float(r["cl"])
+            assert abs(co[k, 0] - cl) <= 1e-7 * max(abs(cl), 1e-3), ("CL", mode, k, co[k, 0], cl)
+            assert np.abs(co[k, 2:5] - r["cm"]).max() <= 1e-7 * max(np.abs(r["cm"]).max(), 1e-6), ("CM", mode, k)
+            k += 1
+    bs.run(want_gamma=True)  # replay
+    co2, gam2 = bs.results(gamma=True)
+    np.testing.assert_array_equal(co2, co)
+    for a, b in zip(gam2, gam):
+        np.testing.assert_array_equal(a, b)
+    bs.run(want_gamma=True, graph=False)
+    co3, _ = bs.results(gamma=True)
+    np.testing.assert_allclose(co3, co, rtol=1e-12, atol=1e-15)
+    bs.profile()
+    co4, _ = bs.results()
+    np.testing.assert_allclose(co4, co, rtol=1e-12, atol=1e-15)
+
+
+def test_fp64_residual_needs_a_refinement_sweep(cuda):
+    from tinyvlm_gb300._lib import GbvlmError
+    cases = M.batch_cases(2, seed=1, n_alpha=1, nc_range=(4, 6), ns_range=(4, 6))
+    with pytest.raises(GbvlmError, match="GBVLM_ERR_ARG"):
+        BatchSolver(cases, mode="shared", refine=0, fp64_residual=True)
+
+
 def test_batch_large_cases(cuda):
     """Sizes up to the full workload's largest (32 x 64 = 2048 panels)."""
     cases = M.batch_cases(4, seed=3, n_alpha=2, nc_range=(28, 32), ns_range=(56, 64))

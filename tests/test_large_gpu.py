@@ -59,14 +59,15 @@ def _errors(co, gam, ref):
 def test_config_c_16384_panels_64_alphas_vs_full_double(cuda):
     """Config C at its configured size: the reference's elliptic 128 x 128 = 16,384-panel wing
     (mesh/elliptic_128x128.x), 64 alphas in [-10, 10] deg on one AIC; float AIC, tensor-core LU and one
-    double-float refinement sweep against the oracle's full double solve (double assembly, LAPACK
+    refinement sweep with the FP64 residual (float AIC plus its float-pair correction) against the oracle's
+    full double solve (double assembly, LAPACK
     dgetrf/dgetrs).  Every alpha: CL and CM_y (guarded near zero lift) and ||gamma - gamma_64|| /
     ||gamma_64|| within 1e-5."""
     from tests import ref_fixtures as R
     v = R.mesh("elliptic_128x128")
     al = np.radians(np.linspace(-10.0, 10.0, 64))
     case = M.Case(v, al, {})
-    bs = BatchSolver([case], mode="shared", refine=1)
+    bs = BatchSolver([case], mode="shared", refine=1, fp64_residual=True)
     bs.set_inputs(pack_verts([case]), pack_alphas([case]))
     bs.run(want_gamma=True)
     co, gam = bs.results(gamma=True)

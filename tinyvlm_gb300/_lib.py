@@ -101,6 +101,7 @@ def _protos():
     t["gbvlm_nlvlm_destroy"] = [P]
     t["gbvlm_nlvlm_run"] = [P, F64, F64, F64, F64, P, P, I32, F64, I32, P, P, P, P, P]
     t["gbvlm_batch_create"] = [P, I32, P, P, I32, I32]
+    t["gbvlm_batch_create_ex"] = [P, I32, P, P, I32, I32, I32]
     t["gbvlm_batch_destroy"] = [P]
     t["gbvlm_batch_info"] = [P, P, P, P, P, P, P]
     t["gbvlm_batch_set_inputs"] = [P, P, P, F64, F64, P, P]

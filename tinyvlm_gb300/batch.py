@@ -14,6 +14,7 @@ from ._lib import P, call, dims_array
 from .device import stream_handle
 
 MODES = {"exact": 0, "shared": 1}
+FP64_RESIDUAL = 1  # GBVLM_BATCH_FP64_RESIDUAL
 STAGES = ("geometry", "assembly", "rhs", "lu_factor", "solve_refine", "loads")
 
 
@@ -27,11 +28,16 @@ def pack_alphas(cases):
 
 
 class BatchSolver:
-    def __init__(self, cases, mode="shared", refine=1, tuned=True):
+    def __init__(self, cases, mode="shared", refine=1, tuned=True, fp64_residual=False):
         """``tuned``: take the plan's launch shapes from the autotuner's table
         for this workload's shape (autotune.batch_key); otherwise the
-        library's current parameters."""
+        library's current parameters.  ``fp64_residual``: the refinement
+        residual measures the FP64 system (GBVLM_BATCH_FP64_RESIDUAL: a
+        float-pair evaluation of the AIC corrects the stored float one), so
+        the circulations, not only CL/CM, converge to the FP64 solution;
+        needs refine >= 1."""
         self.mode = mode
+        self.fp64_residual = bool(fp64_residual)
         self.tuning = None
         if tuned:
             from . import autotune
@@ -43,8 +49,8 @@ class BatchSolver:
         d = dims_array(self.dims)
         na = (ctypes.c_int32 * len(cases))(*self.nalpha)
         h = ctypes.c_void_p()
-        call("gbvlm_batch_create", ctypes.cast(ctypes.pointer(h), P), len(cases), d, ctypes.cast(na, P),
-             MODES[mode], int(refine))
+        call("gbvlm_batch_create_ex", ctypes.cast(ctypes.pointer(h), P), len(cases), d, ctypes.cast(na, P),
+             MODES[mode], int(refine), FP64_RESIDUAL if fp64_residual else 0)
         self.h = h
         ns, nsys, gf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         inter, luf, ab = ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()

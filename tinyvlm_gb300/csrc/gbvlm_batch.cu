@@ -35,6 +35,7 @@
 #include "gbvlm_internal.h"
 #include "gbvlm_lu.h"
 #include "gbvlm_math.cuh"
+#include "gbvlm_walk.cuh"
 
 namespace gbvlm {
 
@@ -58,6 +59,7 @@ struct SysDesc {
     double* nrmd;           // normals double
     float* A;               // AIC (factored in place)
     float* A2;              // unfactored copy (refinement), may be null
+    float* Alo;             // A64 - A2, the stored AIC's correction (FP64 residual plans), may be null
     int32_t* ipiv;
     float* X;               // float rhs / solutions (n x nrhs)
     double* B;              // double rhs (n x nrhs)
@@ -276,6 +278,62 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
     }
 }
 
+// The correction Alo = A - A2 of the stored float AIC, A evaluated in
+// float-pair arithmetic (about 44 bits: the FP64 system's AIC to far below
+// float rounding) by the same strip walk over the same tiles as
+// k_batch_assemble, with the double kernel's cut-offs.  The refinement
+// residual b - (A2 + Alo) x then measures the FP64 system, so the refined
+// circulations converge to its solution instead of the float-rounded one's.
+// Reads A2, which the tile's k_batch_assemble launch has written.
+template <int BA_SPAN>
+__global__ void __launch_bounds__(BA_THREADS) k_batch_assemble_lo(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
+    constexpr int BA_W = BA_SPAN + 1;
+    __shared__ Fe sw[2][3 * BA_W];  // [row][plane*W + s]
+    const int64_t tile = tile0 + blockIdx.x;
+    const int si = find_sys(tpfx, a.nsys, tile);
+    const SysDesc& S = a.sys[si];
+    const int64_t ns = S.ns, nc = S.nc, n = S.n;
+    const int64_t nchunk = (ns + BA_SPAN - 1) / BA_SPAN, nrb = (n + BA_THREADS - 1) / BA_THREADS;
+    int64_t t = tile - tpfx[si];
+    const int64_t rb = t % nrb;
+    t /= nrb;
+    const int64_t z = t % nchunk, c = t / nchunk;
+    const int64_t s0 = z * BA_SPAN, s1 = min(s0 + (int64_t)BA_SPAN, ns);
+    const int nvs = (int)(s1 - s0 + 1);
+    const int64_t nv = (ns + 1) * (nc + 1);
+    for (int e = threadIdx.x; e < 2 * 3 * nvs; e += BA_THREADS) {
+        const int r = e / (3 * nvs), rem = e - r * 3 * nvs, k = rem / nvs, sl = rem - k * nvs;
+        const int64_t vi = k * nv + (s0 + sl) + (c + r) * (ns + 1);
+        sw[r][k * BA_W + sl] = Fe(S.vh[vi], S.vl[vi]);
+    }
+    __syncthreads();
+    const int64_t i = rb * BA_THREADS + threadIdx.x;
+    if (i >= n) return;
+    const Fe px(S.ch[i], S.cl_[i]), py(S.ch[n + i], S.cl_[n + i]), pz(S.ch[2 * n + i], S.cl_[2 * n + i]);
+    const Fe nx(S.nrmd[i]), ny(S.nrmd[n + i]), nz(S.nrmd[2 * n + i]);
+    const Fe k4(1.0 / (double)(4.0f * PI_F));
+    const float* colB = S.A2 + i + (c * ns + s0) * n;
+    float* colL = S.Alo + i + (c * ns + s0) * n;
+    const bool te = (c == nc - 1);
+    const int64_t wl = 2 * (ns + 1);
+    strip_normal<Fe, false, true>(sw[0], sw[1], BA_W, nvs, px, py, pz, nx, ny, nz, Fe(0), [&](int kk, Fe v) {
+        if (te) {
+            // the wake ring behind this trailing-edge ring (Kutta condition)
+            const int64_t s = s0 + kk;
+            const int64_t idx[4] = {s, s + 1, (ns + 1) + s + 1, (ns + 1) + s};
+            V3<Fe> q[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+                q[m] = V3<Fe>{Fe(S.wh[idx[m]], S.wl[idx[m]]), Fe(S.wh[wl + idx[m]], S.wl[wl + idx[m]]),
+                              Fe(S.wh[2 * wl + idx[m]], S.wl[2 * wl + idx[m]])};
+            v += ring_normal_full<Fe, false, true>(px, py, pz, nx, ny, nz, q, Fe(0));
+        }
+        const Fe tot = v * k4;
+        const float a2 = colB[(int64_t)kk * n];
+        colL[(int64_t)kk * n] = __fadd_rn(__fsub_rn(tot.v, a2), tot.e);
+    });
+}
+
 // ---------------------------------------------------------------------------
 // right-hand sides: b = -V_inf(alpha).n in double, float copy into X
 // grid: (blocks over max n, systems)
@@ -306,7 +364,8 @@ __global__ void k_batch_accum(BatchArgs a) {
     for (int q = 0; q < S.nrhs; q++) S.Xd[p + q * S.n] += (double)S.X[p + q * S.n];
 }
 
-// R = B - A2 Xd; X = (float)R.  One thread per row, tiles (system, row
+// R = B - A2 Xd (B - (A2 + Alo) Xd in FP64 residual plans); X = (float)R.
+// One thread per row, tiles (system, row
 // block).  The products of the float matrix A2 with the double solution Xd
 // are accumulated in double-float arithmetic on the fp32 units (Xd split as
 // hi + lo floats, each product a*hi exact through an FMA, running sums
@@ -328,6 +387,10 @@ __device__ __forceinline__ void df_mac(float& sh, float& sl, float a, float xh, 
     sl = __fmaf_rn(a, xl, __fadd_rn(sl, __fadd_rn(e, pe)));
 }
 
+// LO: the plan keeps the correction Alo of the stored AIC; its products with
+// the hi part of Xd join the low-order sums (Alo is about 2^-24 of A, so
+// the float product is exact to far below the residual's accuracy)
+template <bool LO>
 __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, const int64_t* rpfx) {
     __shared__ __align__(16) float xh[RS_CB][RS_MAXRHS];
     __shared__ __align__(16) float xl[RS_CB][RS_MAXRHS];
@@ -339,11 +402,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
     const int64_t n = S.n;
     bool rv[RS_ROWS];
     const float* arow[RS_ROWS];
+    const float* lrow[RS_ROWS];
 #pragma unroll
     for (int k = 0; k < RS_ROWS; k++) {
         const int64_t r = r0 + k * RS_THREADS;
         rv[k] = r < n;
         arow[k] = S.A2 + (rv[k] ? r : 0);
+        lrow[k] = LO ? S.Alo + (rv[k] ? r : 0) : nullptr;
     }
     // grid.y: blocks of RS_MAXRHS right-hand sides
     for (int q0 = blockIdx.y * RS_MAXRHS; q0 < S.nrhs; q0 += RS_MAXRHS * gridDim.y) {
@@ -365,11 +430,14 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
             __syncthreads();
             if (rv[0]) {
                 const int cn = (int)min((int64_t)RS_CB, n - c0);
-                float av[RS_ROWS][RS_CB];
+                float av[RS_ROWS][RS_CB], lv[RS_ROWS][RS_CB];
 #pragma unroll
                 for (int k = 0; k < RS_ROWS; k++)
 #pragma unroll
-                    for (int cc = 0; cc < RS_CB; cc++) av[k][cc] = (cc < cn && rv[k]) ? arow[k][(c0 + cc) * n] : 0.f;
+                    for (int cc = 0; cc < RS_CB; cc++) {
+                        av[k][cc] = (cc < cn && rv[k]) ? arow[k][(c0 + cc) * n] : 0.f;
+                        if (LO) lv[k][cc] = (cc < cn && rv[k]) ? lrow[k][(c0 + cc) * n] : 0.f;
+                    }
 #pragma unroll
                 for (int cc = 0; cc < RS_CB; cc++) {
                     // the 8 hi and 8 lo values of column cc as four 16-byte broadcasts
@@ -382,7 +450,10 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 #pragma unroll
                     for (int k = 0; k < RS_ROWS; k++)
 #pragma unroll
-                        for (int q = 0; q < RS_MAXRHS; q++) df_mac(sh[k][q], sl[k][q], av[k][cc], hh[q], ll[q]);
+                        for (int q = 0; q < RS_MAXRHS; q++) {
+                            df_mac(sh[k][q], sl[k][q], av[k][cc], hh[q], ll[q]);
+                            if (LO) sl[k][q] = __fmaf_rn(lv[k][cc], hh[q], sl[k][q]);
+                        }
                 }
             }
         }
@@ -580,6 +651,12 @@ struct gbvlm_batch_s {
     LuPlan plans[MAX_GROUPS];
     cudaStream_t side[MAX_GROUPS] = {};
     cudaEvent_t fork = nullptr, join[MAX_GROUPS] = {};
+    // FP64 residual plans: the AIC correction of each size group on its own
+    // low-priority branch, after the group's assembly and beside its
+    // factorisation; joined before the first refinement residual
+    bool fp64_residual = false;
+    cudaStream_t lo_side = nullptr;
+    cudaEvent_t asm_done[MAX_GROUPS] = {}, lo_join = nullptr;
     LuBatch<float> lub;
     TrsFlow flow;  // triangular solves of all systems (unless GBVLM_TRS_FLOW=0: one CTA per system)
     bool use_flow = true;
@@ -600,7 +677,10 @@ struct gbvlm_batch_s {
             plans[g].release();
             if (side[g]) cudaStreamDestroy(side[g]);
             if (join[g]) cudaEventDestroy(join[g]);
+            if (asm_done[g]) cudaEventDestroy(asm_done[g]);
         }
+        if (lo_side) cudaStreamDestroy(lo_side);
+        if (lo_join) cudaEventDestroy(lo_join);
         if (fork) cudaEventDestroy(fork);
     }
 };
@@ -619,6 +699,16 @@ static cudaError_t launch_assemble(gbvlm_batch h, unsigned tiles, int64_t tile0,
     return cudaGetLastError();
 }
 
+static cudaError_t launch_assemble_lo(gbvlm_batch h, unsigned tiles, int64_t tile0, const BatchArgs& a,
+                                      cudaStream_t st) {
+    switch (h->tp.batch_assembly_span) {
+        case 64: k_batch_assemble_lo<64><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
+        case 256: k_batch_assemble_lo<256><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
+        default: k_batch_assemble_lo<128><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
+    }
+    return cudaGetLastError();
+}
+
 static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullptr, bool serial_lu = false) {
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     int64_t nlaunch = 0;
@@ -628,7 +718,8 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     const int64_t solves = h->use_flow ? trs_flow_launches(mr, h->flow.groups) : (mr + 7) / 8;
     // geometry, Trefftz, the groups' assemblies, RHS, the factorisations, the
     // solves and accumulations, the refinement sweeps, the loads
-    h->launches = 3 + h->ngroups + nlaunch + solves + 1 + (int64_t)h->refine * (1 + solves + 1) + 1;
+    h->launches = 3 + h->ngroups * (h->fp64_residual ? 2 : 1) + nlaunch + solves + 1 +
+                  (int64_t)h->refine * (1 + solves + 1) + 1;
     BatchArgs a;
     a.sys = h->d_sys;
     a.nsys = h->nsys;
@@ -661,6 +752,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     mark(1);
     if (staged) {
         GB_CUDA(launch_assemble(h, (unsigned)h->assembly_tiles, 0, a, st));
+        if (h->fp64_residual) GB_CUDA(launch_assemble_lo(h, (unsigned)h->assembly_tiles, 0, a, st));
     }
     mark(2);
     dim3 gp((unsigned)cdiv(h->maxn, 256), (unsigned)h->nsys);  // one thread per row of every system
@@ -680,6 +772,11 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
             GB_CUDA(cudaStreamWaitEvent(h->side[g], h->fork, 0));
             if (h->gtile[g][1] > 0) {
                 GB_CUDA(launch_assemble(h, (unsigned)h->gtile[g][1], h->gtile[g][0], a, h->side[g]));
+                if (h->fp64_residual) {
+                    GB_CUDA(cudaEventRecord(h->asm_done[g], h->side[g]));
+                    GB_CUDA(cudaStreamWaitEvent(h->lo_side, h->asm_done[g], 0));
+                    GB_CUDA(launch_assemble_lo(h, (unsigned)h->gtile[g][1], h->gtile[g][0], a, h->lo_side));
+                }
             }
             int rc = lu_batch_factor<float>(h->lub, h->plans[g], h->side[g], true);
             if (rc) return rc;
@@ -689,6 +786,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         k_batch_rhs<<<gp, 256, 0, st>>>(a);
         GB_LAUNCH_CHECK();
         for (int gi = 0; gi < h->ngroups; gi++) GB_CUDA(cudaStreamWaitEvent(st, h->join[gi], 0));
+        if (h->fp64_residual) GB_CUDA(cudaEventRecord(h->lo_join, h->lo_side));
     }
     int rc = GBVLM_OK;
     mark(4);
@@ -703,9 +801,13 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     if (rc) return rc;
     k_batch_accum<<<gp, 256, 0, st>>>(a);
     GB_LAUNCH_CHECK();
+    if (h->fp64_residual && !staged && h->refine > 0) GB_CUDA(cudaStreamWaitEvent(st, h->lo_join, 0));
     for (int it = 0; it < h->refine; it++) {
-        k_batch_residual<<<dim3((unsigned)h->residual_tiles, (unsigned)cdiv(maxrhs, RS_MAXRHS)), RS_THREADS, 0, st>>>(
-            a, h->d_rpfx);
+        const dim3 rg((unsigned)h->residual_tiles, (unsigned)cdiv(maxrhs, RS_MAXRHS));
+        if (h->fp64_residual)
+            k_batch_residual<true><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+        else
+            k_batch_residual<false><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
         GB_LAUNCH_CHECK();
         rc = solve();
         if (rc) return rc;
@@ -735,14 +837,23 @@ extern "C" {
 
 int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims, const int32_t* nalpha, int32_t mode,
                        int32_t refine_iters) {
+    return gbvlm_batch_create_ex(out, ncases, dims, nalpha, mode, refine_iters, 0);
+}
+
+int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims, const int32_t* nalpha,
+                          int32_t mode, int32_t refine_iters, int32_t flags) {
     GB_REQUIRE(out && dims && nalpha && ncases >= 1, "bad batch arguments");
     GB_REQUIRE(mode == GBVLM_BATCH_EXACT || mode == GBVLM_BATCH_SHARED, "unknown batch mode %d", mode);
     GB_REQUIRE(refine_iters >= 0 && refine_iters <= 8, "refine_iters outside [0, 8]");
+    GB_REQUIRE((flags & ~GBVLM_BATCH_FP64_RESIDUAL) == 0, "unknown batch flags 0x%x", (unsigned)flags);
+    const bool fp64_residual = (flags & GBVLM_BATCH_FP64_RESIDUAL) != 0;
+    GB_REQUIRE(!fp64_residual || refine_iters >= 1, "GBVLM_BATCH_FP64_RESIDUAL needs refine_iters >= 1");
     const TuneParams tp = tune();
     GB_REQUIRE(tp.batch_group_hi > tp.batch_group_lo, "batch.group_hi (%lld) must exceed batch.group_lo (%lld)",
                (long long)tp.batch_group_hi, (long long)tp.batch_group_lo);
     auto* h = new gbvlm_batch_s();
     h->tp = tp;
+    h->fp64_residual = fp64_residual;
     h->ncases = ncases;
     h->mode = mode;
     h->refine = refine_iters;
@@ -786,7 +897,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         return o;
     };
     struct Off {
-        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, ipiv, perm, X, B, Xd, R, K;
+        size_t vh, vl, wh, wl, ch, cl, nrm, area, vd, wd, nrmd, A, A2, Alo, ipiv, perm, X, B, Xd, R, K;
     };
     std::vector<Off> offs(h->nsys);
     const size_t o_vin = reserve(sizeof(float) * h->vin_floats);
@@ -808,6 +919,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         o.nrmd = reserve(sizeof(double) * 3 * n);
         o.A = reserve(sizeof(float) * n * n);
         o.A2 = refine_iters > 0 ? reserve(sizeof(float) * n * n) : (size_t)-1;
+        o.Alo = fp64_residual ? reserve(sizeof(float) * n * n) : (size_t)-1;
         o.ipiv = reserve(sizeof(int32_t) * n);
         o.perm = reserve(sizeof(int32_t) * n);
         o.X = reserve(sizeof(float) * n * P.nrhs);
@@ -912,6 +1024,7 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
         S.nrmd = (double*)(base + o.nrmd);
         S.A = (float*)(base + o.A);
         S.A2 = o.A2 == (size_t)-1 ? nullptr : (float*)(base + o.A2);
+        S.Alo = o.Alo == (size_t)-1 ? nullptr : (float*)(base + o.Alo);
         S.ipiv = (int32_t*)(base + o.ipiv);
         S.X = (float*)(base + o.X);
         S.B = (double*)(base + o.B);
@@ -997,12 +1110,17 @@ int gbvlm_batch_create(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* dims,
                 cudaError_t ee = cudaStreamCreateWithPriority(&h->side[gi], cudaStreamNonBlocking,
                                                               gi == 0 ? greatest : least);
                 if (ee == cudaSuccess) ee = cudaEventCreateWithFlags(&h->join[gi], cudaEventDisableTiming);
+                if (ee == cudaSuccess && fp64_residual)
+                    ee = cudaEventCreateWithFlags(&h->asm_done[gi], cudaEventDisableTiming);
                 if (ee != cudaSuccess) rc = cuda_fail(ee, "batch streams", __FILE__, __LINE__);
             }
             i0 = i1;
         }
         if (rc == GBVLM_OK) {
             cudaError_t ee = cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+            if (ee == cudaSuccess && fp64_residual)
+                ee = cudaStreamCreateWithPriority(&h->lo_side, cudaStreamNonBlocking, least);
+            if (ee == cudaSuccess && fp64_residual) ee = cudaEventCreateWithFlags(&h->lo_join, cudaEventDisableTiming);
             if (ee != cudaSuccess) rc = cuda_fail(ee, "batch streams", __FILE__, __LINE__);
         }
     }

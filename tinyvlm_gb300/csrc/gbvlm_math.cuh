@@ -175,4 +175,65 @@ struct CSum {
     __device__ __forceinline__ double value() const { return s + c; }
 };
 
+// ---------------------------------------------------------------------------
+// Float-pair arithmetic: x = v + e held as two floats (Dekker's double-length
+// arithmetic; Knuth's TwoSum and an FMA-exact product), about 44 significant
+// bits evaluated on the fp32 pipes.  Sums are renormalised, products are
+// left with |e| of a few ulp(v).  The intrinsics keep every rounding as
+// written (no contraction).  Used where the float AIC must be corrected
+// toward its FP64 value (the refinement residual of the batched solver).
+// ---------------------------------------------------------------------------
+struct Fe {
+    float v, e;
+    Fe() = default;
+    __host__ __device__ constexpr Fe(float a, float b) : v(a), e(b) {}
+    __host__ __device__ constexpr Fe(float a) : v(a), e(0.f) {}
+    __host__ __device__ constexpr Fe(int a) : v((float)a), e(0.f) {}
+    __host__ __device__ constexpr Fe(double a) : v((float)a), e((float)(a - (double)(float)a)) {}
+};
+
+__device__ __forceinline__ Fe fe_fast2sum(float s, float t) {  // |s| >= |t| or s == 0
+    const float h = __fadd_rn(s, t);
+    return Fe(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ Fe operator+(Fe a, Fe b) {
+    const float s = __fadd_rn(a.v, b.v);
+    const float bb = __fsub_rn(s, a.v);
+    const float err = __fadd_rn(__fsub_rn(a.v, __fsub_rn(s, bb)), __fsub_rn(b.v, bb));
+    return fe_fast2sum(s, __fadd_rn(err, __fadd_rn(a.e, b.e)));
+}
+__device__ __forceinline__ Fe operator-(Fe a) { return Fe(-a.v, -a.e); }
+__device__ __forceinline__ Fe operator-(Fe a, Fe b) { return a + (-b); }
+__device__ __forceinline__ Fe operator*(Fe a, Fe b) {
+    const float p = __fmul_rn(a.v, b.v);
+    float t = __fmaf_rn(a.v, b.v, -p);  // a.v*b.v - p exactly
+    t = __fmaf_rn(a.v, b.e, t);
+    t = __fmaf_rn(a.e, b.v, t);
+    return Fe(p, t);
+}
+__device__ __forceinline__ Fe& operator+=(Fe& a, Fe b) { return a = a + b; }
+// comparisons of the pair's value (v first; e breaks ties)
+__device__ __forceinline__ bool operator<(Fe a, Fe b) { return a.v < b.v || (a.v == b.v && a.e < b.e); }
+__device__ __forceinline__ bool operator>=(Fe a, Fe b) { return !(a < b); }
+
+template <> struct Prec<Fe> {
+    static constexpr double rcut_norm = RCUT_NORM_D;  // (a scalar: device code may read it)
+};
+template <> __device__ __forceinline__ Fe fast_len<Fe>(Fe n2) {
+    // s = sqrt(v) to a few ulp, then one Newton correction from the exact
+    // residual v - s^2 (plus e): sqrt(v + e) = s + (v - s^2 + e) / (2 s)
+    const float r = rsqrtf(n2.v + 1e-37f);
+    const float s = __fmul_rn(n2.v, r);
+    const float d = __fadd_rn(__fmaf_rn(-s, s, n2.v), n2.e);
+    return Fe(s, __fmul_rn(__fmul_rn(d, 0.5f), r));
+}
+template <> __device__ __forceinline__ Fe dsqrt<Fe>(Fe x) { return fast_len<Fe>(x); }
+template <> __device__ __forceinline__ Fe fast_div<Fe>(Fe a, Fe b) {
+    // q to a few ulp, then the correction (a - q b) / b from the FMA residual
+    const float rb = __fdividef(1.0f, b.v);
+    const float q = __fmul_rn(a.v, rb);
+    const float r = __fadd_rn(__fmaf_rn(-q, b.v, a.v), __fmaf_rn(-q, b.e, a.e));
+    return Fe(q, __fmul_rn(r, rb));
+}
+
 }  // namespace gbvlm

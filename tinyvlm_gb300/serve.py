@@ -253,7 +253,10 @@ def steady_case(rng, n_lo=256, n_hi=16384):
 def resident_uvlm(ns=80, nc=20, warm_steps=500, capacity=4096, rollup=False):
     """The resident unsteady case: 20 x 80 pitch-plunge wing advanced
     ``warm_steps`` steps (wake of warm_steps x ns rings); ``capacity`` bounds
-    the further steps it can serve."""
+    the further steps it can serve.  The warm-up steps run on the legacy
+    default stream; the served steps run on the lanes' non-blocking streams,
+    which do not order themselves after it, so the warm-up ends with a device
+    synchronisation."""
     import ctypes
     from . import _lib
     from ._lib import P, PP, call, dims_array
@@ -289,6 +292,7 @@ def resident_uvlm(ns=80, nc=20, warm_steps=500, capacity=4096, rollup=False):
     call("gbvlm_uvlm_begin", h, 0.05, 1 if rollup else 0, 0.0, None)
     for _ in range(warm_steps):
         call("gbvlm_uvlm_step", h, None, None, None, None)
+    call("gbvlm_device_synchronize")
     return sim
 
 
