@@ -354,7 +354,9 @@ def run_gpu(args):
                          ("E_served_mixed_stream", lambda: config_e((16.0,), 30))):
             t0 = time.perf_counter()
             try:
-                configs[name] = fn()
+                with ClockSampler(local) as cclk:
+                    configs[name] = fn()
+                configs[name]["clocks"] = cclk.summary()
             except Exception as e:  # a failing side workload must not hide the headline
                 configs[name] = {"error": "%s: %s" % (type(e).__name__, e)}
             configs[name]["wall_s"] = time.perf_counter() - t0

@@ -65,7 +65,8 @@ def test_batch_matches_double_oracle(cuda, mode, refine):
 def test_fp64_residual_converges_to_the_double_solution(cuda, mode):
     """GBVLM_BATCH_FP64_RESIDUAL: the residual's AIC is the stored float AIC plus its float-pair correction, so
     the refinement converges to the double system's solution.  Two sweeps bring every gamma within 3e-7 of
-    ||gamma_64|| (the float rounding of the stored result is 6e-8) and CL/CM within 1e-7.  Cases in all three
+    ||gamma_64|| (the float rounding of the stored result is 6e-8) and CL/CM within 5e-7 (the loads form their
+    force and moment terms in float and sum them in double; 1e-7 in the shared formulation).  Cases in all three
     LU size groups (n > 1024, 384 < n <= 1024, n <= 384), each group's correction on its own graph branch;
     the graph, its replay, the eager launch sequence and the staged (profiled) run agree."""
     cases = M.batch_cases(12, seed=17, n_alpha=2, nc_range=(4, 32), ns_range=(4, 64))
@@ -81,8 +82,8 @@ def test_fp64_residual_converges_to_the_double_solution(cuda, mode):
             g = np.concatenate([x.ravel() for x in r["gamma"]])
             assert np.linalg.norm(gam[k] - g) <= 3e-7 * np.linalg.norm(g), ("gamma", mode, k)
             cl = float(r["cl"])
-            assert abs(co[k, 0] - cl) <= 1e-7 * max(abs(cl), 1e-3), ("CL", mode, k, co[k, 0], cl)
-            assert np.abs(co[k, 2:5] - r["cm"]).max() <= 1e-7 * max(np.abs(r["cm"]).max(), 1e-6), ("CM", mode, k)
+            assert abs(co[k, 0] - cl) <= 5e-7 * max(abs(cl), 1e-3), ("CL", mode, k, co[k, 0], cl)
+            assert np.abs(co[k, 2:5] - r["cm"]).max() <= 5e-7 * max(np.abs(r["cm"]).max(), 1e-6), ("CM", mode, k)
             k += 1
     bs.run(want_gamma=True)  # replay
     co2, gam2 = bs.results(gamma=True)

@@ -785,12 +785,13 @@ __global__ void __launch_bounds__(256) k_update(LuBatch<T> B, int64_t k, const i
 // update on the tensor cores: the same A22 -= L21 U12 on 128 x 128 tiles
 // (gbvlm_tc.cuh), tiles enumerated over all systems through a prefix table
 // ---------------------------------------------------------------------------
-template <int PASSES>
+template <int PASSES, int TBN>
 __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, int64_t k0, int w, const int32_t* act,
                                                              const int64_t* pfx, int cnt, int* err, int part) {
     // outer update of the block [k0, k0 + w): rows and columns [k0 + w, n), K = w.
     // part 0: all tiles; part 1: the first column of tiles (the next outer
-    // panel, BN = w); part 2: the other columns of tiles
+    // panel, w = 128 columns, TBN = 128); part 2: the columns right of it.
+    // Tiles are 128 rows x TBN columns, row tiles fastest.
     extern __shared__ __align__(16) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tslot;
@@ -800,11 +801,12 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_update_tc(LuBatch<float> B, 
     float* A = B.A[sid];
     const int64_t lo = k0 + w;  // systems here have n > k0 + w
     const int64_t tiles = (n - lo + tc::BM - 1) / tc::BM;
-    const int64_t t = blockIdx.x - pfx[a] + (part == 2 ? tiles : 0);
-    const int64_t r0 = lo + (t % tiles) * tc::BM, c0 = lo + (t / tiles) * tc::BN;
-    tc::update_tile<PASSES>(A + r0 + k0 * ld, ld, A + k0 + c0 * ld, ld, A + r0 + c0 * ld, ld,
-                            (int)min((int64_t)tc::BM, n - r0), (int)min((int64_t)tc::BN, n - c0), w, tc_smem, bar,
-                            &tslot, err);
+    const int64_t t = blockIdx.x - pfx[a];
+    const int64_t cbase = lo + (part == 2 ? (int64_t)tc::BN : 0);
+    const int64_t r0 = lo + (t % tiles) * tc::BM, c0 = cbase + (t / tiles) * TBN;
+    tc::update_tile<PASSES, false, TBN>(A + r0 + k0 * ld, ld, A + k0 + c0 * ld, ld, A + r0 + c0 * ld, ld,
+                                        (int)min((int64_t)tc::BM, n - r0), (int)min((int64_t)TBN, n - c0), w, tc_smem,
+                                        bar, &tslot, err);
 }
 
 // persistent warp-specialised form of k_update_tc (gbvlm_tc.cuh): one CTA per
@@ -1793,12 +1795,23 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
                                                                                         plan.d_err, part, blocks);
                         return;
                     }
+                    // the next outer panel (part 1) in 128-column tiles, the rest in the plan's width
+                    if (part != 1 && plan.tc_wide) {
+                        constexpr int SM_ = tc::smem_bytes<tc::BN_WIDE>();
+                        if (plan.tc_passes == 1)
+                            k_update_tc<1, tc::BN_WIDE><<<(unsigned)blocks, tc::THREADS, SM_, s_>>>(
+                                B, k0, plan.W, act, pfx, S.n_tc, plan.d_err, part);
+                        else
+                            k_update_tc<3, tc::BN_WIDE><<<(unsigned)blocks, tc::THREADS, SM_, s_>>>(
+                                B, k0, plan.W, act, pfx, S.n_tc, plan.d_err, part);
+                        return;
+                    }
                     if (plan.tc_passes == 1)
-                        k_update_tc<1><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx,
-                                                                                           S.n_tc, plan.d_err, part);
+                        k_update_tc<1, tc::BN><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(
+                            B, k0, plan.W, act, pfx, S.n_tc, plan.d_err, part);
                     else
-                        k_update_tc<3><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(B, k0, plan.W, act, pfx,
-                                                                                           S.n_tc, plan.d_err, part);
+                        k_update_tc<3, tc::BN><<<(unsigned)blocks, tc::THREADS, tc::SMEM_BYTES, s_>>>(
+                            B, k0, plan.W, act, pfx, S.n_tc, plan.d_err, part);
                 };
                 if (!lookahead) {
                     tc_launch(S.tc_blocks, S.tc_pfx, 0, st);
@@ -1879,9 +1892,19 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             plan.tc_passes = (v == 1 || v == 3) && major >= 10 ? v : 0;
         }
         plan.W = plan.tc_passes ? LU_OUTER : GK;
+        {
+            const char* e = getenv("GBVLM_TC_WIDE");
+            plan.tc_wide = plan.tc_passes && !tc_persistent() && !(e && e[0] == '0');
+        }
         if (plan.tc_passes) {
-            GB_CUDA(cudaFuncSetAttribute(k_update_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
-            GB_CUDA(cudaFuncSetAttribute(k_update_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tc<1, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tc<3, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tc<1, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::smem_bytes<tc::BN_WIDE>()));
+            GB_CUDA(cudaFuncSetAttribute(k_update_tc<3, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::smem_bytes<tc::BN_WIDE>()));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsm_wide_smem<LU_OUTER>()));
             GB_CUDA(cudaFuncSetAttribute(k_trs_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2073,11 +2096,12 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         S.btrsm_blocks = acc;
         S.tc_pfx = (int64_t)pfx.size();
         acc = 0;
+        const int64_t cw = plan.tc_wide ? tc::BN_WIDE : tc::BN;  // tile columns of parts 0 and 2
         for (int i = 0; i < ci; i++) {
             pfx.push_back(acc);
             const int64_t m = n_sorted[i] - S.kend;
             const int64_t t = cdiv(m, tc::BM);
-            acc += t * t;
+            acc += t * cdiv(m, cw);
             plan.tc_flops += 2.0 * (double)m * (double)m * plan.W;
             plan.tc_bytes += 8.0 * (double)m * (double)m + 8.0 * (double)m * plan.W;
         }
@@ -2097,8 +2121,8 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         acc = 0;
         for (int i = 0; i < ci; i++) {
             pfx.push_back(acc);
-            const int64_t t = cdiv(n_sorted[i] - S.kend, tc::BM);
-            acc += t * (t - 1);
+            const int64_t m = n_sorted[i] - S.kend;
+            acc += cdiv(m, tc::BM) * (m > tc::BN ? cdiv(m - tc::BN, cw) : 0);
         }
         pfx.push_back(acc);
         S.tcr_blocks = acc;

@@ -69,6 +69,7 @@ struct LuPlan {
     int64_t maxn = 0;
     int cluster = 1;  // largest cluster the register panel can be launched with
     int tc_passes = 0;  // float trailing update: 0 CUDA cores, 1 TF32, 3 3xTF32 tensor cores
+    bool tc_wide = false;  // the update right of the next outer panel in 128 x 256 tiles (GBVLM_TC_WIDE=0: 128 x 128)
     int W = LU_NB;      // outer block width of the float factorisation
     int32_t* d_act = nullptr;
     int64_t* d_pfx = nullptr;

@@ -11,19 +11,20 @@
 // (the dropped lo*lo term is ~2^-22 relative).  PASSES = 1 keeps hi*hi only
 // (plain TF32).
 //
-// Per CTA (256 threads, one output tile, two CTAs per SM):
+// Per CTA (256 threads, one output tile of 128 x 128 or 128 x 256, two CTAs
+// per SM; a wide tile moves twice the C bytes per operand-load round trip):
 //   * operands are staged in shared memory per 32-wide K chunk, in the
 //     K-major, 128-byte-swizzled layout the MMA reads: row r of a chunk is
 //     128 bytes (32 tf32), its 16-byte pieces permuted by XOR with r % 8,
 //     8-row groups 1024 bytes apart.  With STAGES = 2 threads fill chunk
 //     c+1 while the tensor core works on chunk c; with one stage the other
 //     CTA on the SM fills that time;
-//   * one thread issues tcgen05.mma (M = 128, N = 128, K = 8 per
-//     instruction) into a 128-column fp32 accumulator in tensor memory and
-//     commits each chunk to that stage's mbarrier;
-//   * epilogue: warp w reads accumulator lanes 32(w%4)..+31 (tile rows),
-//     columns 64(w/4)..+63, with tcgen05.ld and subtracts them from C, a warp
-//     covering 32 consecutive rows of one column per store.
+//   * one thread issues tcgen05.mma (M = 128, N = tile width, K = 8 per
+//     instruction) into an fp32 accumulator of that many tensor-memory
+//     columns and commits each chunk to that stage's mbarrier;
+//   * epilogue: warp w reads accumulator lanes 32(w%4)..+31 (tile rows) and
+//     the (w/4) half of the columns with tcgen05.ld and subtracts them from C,
+//     a warp covering 32 consecutive rows of one column per store.
 // Every wait on an mbarrier is bounded in time; a CTA that runs out sets the
 // error word, skips its epilogue and still frees its tensor memory.
 #pragma once
@@ -34,12 +35,17 @@ namespace gbvlm {
 namespace tc {
 
 constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int BN_WIDE = 256;                    // wide tiles: 128 x 256, the A chunk serves twice the columns
 constexpr int THREADS = 256;
 constexpr int CHUNK_BYTES = BM * BK * 4;        // one operand chunk, 16 KB
 constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;    // A hi, A lo, B hi, B lo
 constexpr int STAGES = 1;                       // one stage: two CTAs share an SM and hide each other's latency
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + alignment slack
 constexpr int TMEM_COLS = BN;
+// a tile of TBN columns: A hi/lo chunks of 128 rows, B hi/lo chunks of TBN rows
+template <int TBN> constexpr int stage_bytes() { return 2 * CHUNK_BYTES + 2 * TBN * BK * 4; }
+template <int TBN> constexpr int smem_bytes() { return STAGES * stage_bytes<TBN>() + 1024; }
+static_assert(smem_bytes<BN>() == SMEM_BYTES, "tile shared-memory layout");
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -166,15 +172,22 @@ __device__ __forceinline__ void st_shared_f32(uint32_t addr, float a) {
 // WITHHOLD (a test hook's instantiation only): the MMA thread issues and
 // commits nothing, so the bounded mbarrier waits must run out; no MMA is
 // ever in flight, the CTA frees its tensor memory and sets the error word.
-template <int PASSES, bool WITHHOLD = false>
+// TBN: tile columns, 128 or 256 (one MMA of N = TBN per K step; TBN
+// accumulator columns of tensor memory; shared memory smem_bytes<TBN>()).
+template <int PASSES, bool WITHHOLD = false, int TBN = BN>
 __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const float* Up, int64_t ldu, float* Cp,
                                             int64_t ldc, int m_rows, int n_cols, int K, unsigned char* smem_raw,
                                             uint64_t* bar, uint32_t* tslot, int* err) {
+    static_assert(TBN == 128 || TBN == 256, "tile width");
+    constexpr int SB = stage_bytes<TBN>();
+    constexpr int BCHUNK = TBN * BK * 4;
+    constexpr int BW = TBN / 8;        // B columns per warp in the operand loads
+    constexpr int EQ = TBN / 64;       // 32-column accumulator groups per thread in the epilogue
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     if (wid == 0) {
-        tmem_alloc(tslot, TMEM_COLS);
+        tmem_alloc(tslot, TBN);
         tmem_relinquish();
     }
     if (tid == 0) {
@@ -185,24 +198,24 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tslot;
-    constexpr uint32_t idesc = idesc_tf32(BM, BN);
+    constexpr uint32_t idesc = idesc_tf32(BM, TBN);
     const int nchunks = (K + BK - 1) / BK;
     bool ok = true;
     int committed = -1;  // last chunk whose MMAs were committed
     // operand chunks pass through registers: chunk c + 1 is loaded from global
     // memory while the MMAs of chunk c run (one shared-memory stage)
     const int arow = tid & (BM - 1), akh = (tid >> 7) * 16;
-    float va[16], vb[16];
+    float va[16], vb[BW];
     auto load_chunk = [&](int c) {
         const int kc = c * BK;
         const bool rv = arow < m_rows;  // A: thread = tile row, 16 K values of its half
 #pragma unroll
         for (int kk = 0; kk < 16; kk++)
             va[kk] = (rv && kc + akh + kk < K) ? Lp[arow + (int64_t)(kc + akh + kk) * ldl] : 0.f;
-        const bool kv = kc + lane < K;  // B: warp w, tile columns 16w..16w+15, lane = K index
+        const bool kv = kc + lane < K;  // B: warp w, tile columns BW*w..BW*w+BW-1, lane = K index
 #pragma unroll
-        for (int cc = 0; cc < 16; cc++) {
-            const int col = 16 * wid + cc;
+        for (int cc = 0; cc < BW; cc++) {
+            const int col = BW * wid + cc;
             vb[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ldu] : 0.f;
         }
     };
@@ -211,8 +224,8 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
         const int s = c % STAGES;
         // stage s is free once the MMAs of chunk c - STAGES are done
         const bool free_ = c < STAGES || mbar_wait(&bar[s], ((c - STAGES) / STAGES) & 1);
-        const uint32_t a_hi = base + s * STAGE_BYTES, a_lo = a_hi + CHUNK_BYTES;
-        const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+        const uint32_t a_hi = base + s * SB, a_lo = a_hi + CHUNK_BYTES;
+        const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = b_hi + BCHUNK;
         if (free_) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -225,8 +238,8 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
                                  va[4 * j + 3] - h3);
             }
 #pragma unroll
-            for (int cc = 0; cc < 16; cc++) {
-                const uint32_t off = sw128_off(16 * wid + cc, lane);
+            for (int cc = 0; cc < BW; cc++) {
+                const uint32_t off = sw128_off(BW * wid + cc, lane);
                 const float h = tf32_hi(vb[cc]);
                 st_shared_f32(b_hi + off, h);
                 if (PASSES > 1) st_shared_f32(b_lo + off, vb[cc] - h);
@@ -253,12 +266,12 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
         }
         committed = c;
     }
-    // the first half of this thread's C in flight while the last MMAs finish
+    // the first 32 columns of this thread's C in flight while the last MMAs finish
     const int erow = 32 * (wid & 3) + lane;
     const bool erv = erow < m_rows;
     float cpre[32];
     {
-        const int cb = 64 * (wid >> 2);
+        const int cb = (TBN / 2) * (wid >> 2);
 #pragma unroll
         for (int j = 0; j < 32; j++) cpre[j] = (ok && erv && cb + j < n_cols) ? Cp[erow + (int64_t)(cb + j) * ldc] : 0.f;
     }
@@ -268,8 +281,8 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     fence_after_sync();
     if (ok && done) {
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-            const int cb = 64 * (wid >> 2) + 32 * q;
+        for (int q = 0; q < EQ; q++) {
+            const int cb = (TBN / 2) * (wid >> 2) + 32 * q;
             float v[32];
             tmem_ld32(tmem + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)cb, v);
             if (erv) {
@@ -292,7 +305,7 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     }
     fence_before_sync();
     __syncthreads();
-    if (wid == 0) tmem_dealloc(tmem, TMEM_COLS);
+    if (wid == 0) tmem_dealloc(tmem, TBN);
 }
 
 }  // namespace tc
