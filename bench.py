@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--alphas", type=int, default=8)
     p.add_argument("--refine", type=int, default=1,
                    help="refinement sweeps (double residual); 1 keeps every solve of the batch within CL/CM 1e-5")
+    p.add_argument("--fp64-residual", action="store_true",
+                   help="refinement residual of the FP64 system (float AIC plus its float-pair correction)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--ref-step-seconds", type=float, default=2.5,
                    help="reference arm: CPU time one step's fixed subset of the batch is sized to")
@@ -105,7 +107,7 @@ def config(args, cases):
                         (len(cases), args.alphas, "shared" if args.mode == "shared" else "per-alpha"),
             "cases": len(cases), "alphas_per_case": args.alphas, "mode": args.mode,
             "panels_min": int(min(n)), "panels_max": int(max(n)), "panels_sum": int(sum(n)),
-            "seed": SEED, "refine_iters": args.refine,
+            "seed": SEED, "refine_iters": args.refine, "fp64_residual": bool(args.fp64_residual),
             "l2": "not flushed: the step's AIC set is larger than the 129 MB L2"}
 
 
@@ -275,7 +277,7 @@ def run_gpu(args):
     from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
 
     cases = workload(args)
-    bs = BatchSolver(cases, mode=args.mode, refine=args.refine)
+    bs = BatchSolver(cases, mode=args.mode, refine=args.refine, fp64_residual=args.fp64_residual)
     verts_h = torch.from_numpy(pack_verts(cases)).pin_memory()
     alphas = pack_alphas(cases)
     verts_d = verts_h.to(dev)

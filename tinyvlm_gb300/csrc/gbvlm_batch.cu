@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
 // circulations converge to its solution instead of the float-rounded one's.
 // Reads A2, which the tile's k_batch_assemble launch has written.
 template <int BA_SPAN>
-__global__ void __launch_bounds__(BA_THREADS) k_batch_assemble_lo(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
+__global__ void __launch_bounds__(BA_THREADS, 4) k_batch_assemble_lo(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
     constexpr int BA_W = BA_SPAN + 1;
     __shared__ Fe sw[2][3 * BA_W];  // [row][plane*W + s]
     const int64_t tile = tile0 + blockIdx.x;
@@ -657,6 +657,13 @@ struct gbvlm_batch_s {
     bool fp64_residual = false;
     cudaStream_t lo_side = nullptr;
     cudaEvent_t asm_done[MAX_GROUPS] = {}, lo_join = nullptr;
+    // the plan's device memory is stream-ordered on `mem` (dev_alloc), so
+    // creating and destroying a plan does not synchronise the device while
+    // other streams run; `done` marks the end of the last enqueued work, and
+    // the releases wait for it
+    cudaStream_t mem = nullptr;
+    cudaEvent_t done = nullptr;
+    size_t status_bytes = 0;
     LuBatch<float> lub;
     TrsFlow flow;  // triangular solves of all systems (unless GBVLM_TRS_FLOW=0: one CTA per system)
     bool use_flow = true;
@@ -671,17 +678,21 @@ struct gbvlm_batch_s {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (cap) cudaStreamDestroy(cap);
-        if (arena) cudaFree(arena);
-        if (status) cudaFreeHost(status);
+        if (mem && done) cudaStreamWaitEvent(mem, done, 0);  // releases after the last enqueued work
+        dev_free(arena, mem);
+        pinned_give(status, status_bytes);
         for (int g = 0; g < MAX_GROUPS; g++) {
             plans[g].release();
             if (side[g]) cudaStreamDestroy(side[g]);
             if (join[g]) cudaEventDestroy(join[g]);
             if (asm_done[g]) cudaEventDestroy(asm_done[g]);
         }
+        flow.release();
         if (lo_side) cudaStreamDestroy(lo_side);
         if (lo_join) cudaEventDestroy(lo_join);
         if (fork) cudaEventDestroy(fork);
+        if (done) cudaEventDestroy(done);
+        if (mem) cudaStreamDestroy(mem);  // returns at once; the stream goes when its frees are done
     }
 };
 
@@ -971,10 +982,12 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     const size_t o_lurhs = reserve(sizeof(int32_t) * h->nsys);
     const size_t o_luperm = reserve(sizeof(int32_t*) * h->nsys);
     const size_t o_lumv = reserve(sizeof(int32_t) * 64 * h->nsys);
-    cudaError_t e = cudaMalloc(&h->arena, bytes);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->mem, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = dev_alloc(&h->arena, bytes, h->mem);
     if (e != cudaSuccess) {
         delete h;
-        return cuda_fail(e, "cudaMalloc(batch arena)", __FILE__, __LINE__);
+        return cuda_fail(e, "batch arena", __FILE__, __LINE__);
     }
     h->arena_bytes = bytes;
     char* base = (char*)h->arena;
@@ -1105,6 +1118,7 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
             h->gtile[gi][0] = h->tpfx_host[i0];
             h->gtile[gi][1] = h->tpfx_host[i1] - h->tpfx_host[i0];
             std::vector<int64_t> ns(lun.begin() + i0, lun.begin() + i1);
+            h->plans[gi].mem = h->mem;
             rc = lu_plan_build(h->plans[gi], ns, 0, i0);
             if (rc == GBVLM_OK) {
                 cudaError_t ee = cudaStreamCreateWithPriority(&h->side[gi], cudaStreamNonBlocking,
@@ -1133,6 +1147,7 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
         int32_t mr = 1;
         for (auto& sy : h->sys) mr = std::max(mr, sy.nrhs);
         h->use_flow = !(fe && fe[0] == '0') && trs_flow_fits(h->nsys, (mr + 7) / 8);
+        h->flow.mem = h->mem;
         if (h->use_flow) rc = trs_flow_build(h->flow, lun, 0, (mr + 7) / 8);
     }
     if (rc) {
@@ -1211,7 +1226,9 @@ int gbvlm_batch_run_eager(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream
         cudaGraphExecDestroy(h->exec);
         h->exec = nullptr;
     }
-    return batch_enqueue(h, to_cuda(stream));
+    int rc = batch_enqueue(h, to_cuda(stream));
+    if (rc == GBVLM_OK) GB_CUDA(cudaEventRecord(h->done, to_cuda(stream)));
+    return rc;
 }
 
 int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream) {
@@ -1241,6 +1258,7 @@ int gbvlm_batch_run(gbvlm_batch h, int32_t want_gamma, gbvlm_stream stream) {
         GB_CUDA(cudaGraphInstantiate(&h->exec, h->graph, cudaGraphInstantiateFlagUseNodePriority));
     }
     GB_CUDA(cudaGraphLaunch(h->exec, st));
+    GB_CUDA(cudaEventRecord(h->done, st));
     return GBVLM_OK;
 }
 
@@ -1251,6 +1269,7 @@ int gbvlm_batch_profile(gbvlm_batch h, float* stage_ms, gbvlm_stream stream) {
     for (int k = 0; k < 7; k++) GB_CUDA(cudaEventCreate(&ev[k]));
     int rc = batch_enqueue(h, st, ev);
     if (rc == GBVLM_OK) {
+        cudaEventRecord(h->done, st);
         cudaError_t e = cudaEventSynchronize(ev[6]);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__);
         for (int k = 0; k < 6 && rc == GBVLM_OK; k++) {
@@ -1271,6 +1290,7 @@ int gbvlm_batch_update_profile(gbvlm_batch h, double* out, gbvlm_stream stream) 
     for (int g = 0; g < h->ngroups; g++) h->plans[g].tc_events = nullptr;
     double ms = 0;
     if (rc == GBVLM_OK) {
+        cudaEventRecord(h->done, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
         for (size_t k = 0; k + 1 < ev.size() && rc == GBVLM_OK; k += 2) {
@@ -1304,7 +1324,14 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
     // status words (bounded-wait errors of the LU plans and the triangular
     // solve, pivot flags) with the same synchronisation
     const size_t sbytes = sizeof(int32_t) * (G + 1 + (size_t)h->nsys);
-    if (!h->status) GB_CUDA(cudaMallocHost(&h->status, sbytes));
+    if (!h->status) {
+        h->status = pinned_take(sbytes);
+        if (!h->status) {
+            set_error("no pinned host memory for the batch status words");
+            return GBVLM_ERR_NOMEM;
+        }
+        h->status_bytes = sbytes;
+    }
     int32_t* hs = (int32_t*)h->status;
     memset(hs, 0, sizeof(int32_t) * (G + 1));
     for (int g = 0; g < h->ngroups; g++)

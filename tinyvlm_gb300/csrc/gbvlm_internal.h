@@ -46,6 +46,19 @@ TuneParams tune();
 // SM count of the current device (cached per device)
 int sm_count();
 
+// Device memory for plans created and destroyed while other streams run (a
+// served batch): mem == nullptr takes cudaMalloc / cudaFree; otherwise the
+// memory comes stream-ordered from the device's default pool on stream
+// `mem` (its release threshold raised once per device, so freed blocks stay
+// in the pool), and neither allocation nor release synchronises the device
+// as cudaMalloc / cudaFree do.  dev_alloc returns memory usable on any
+// stream; dev_free is ordered after what `mem` waits on.
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t mem);
+void dev_free(void* p, cudaStream_t mem);
+// Small pinned host blocks kept for reuse (cudaFreeHost would synchronise).
+void* pinned_take(size_t bytes);
+void pinned_give(void* p, size_t bytes);
+
 // Per-thread pinned staging buffer for synchronous scalar read-backs.
 void* host_scratch(size_t bytes);
 // Per-device small device buffer for reductions (grown on demand).

@@ -1918,7 +1918,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             GB_CUDA(cudaFuncSetAttribute(k_trs_tcp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::P_SMEM_BYTES));
             GB_CUDA(cudaFuncSetAttribute(k_trs_tcp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::P_SMEM_BYTES));
         }
-        GB_CUDA(cudaMalloc(&plan.d_err, sizeof(int)));
+        GB_CUDA(dev_alloc((void**)&plan.d_err, sizeof(int), plan.mem));
         GB_CUDA(cudaMemsetAsync(plan.d_err, 0, sizeof(int), st));
         if (plan.tc_passes) {  // lookahead stream (lowest priority) and its events
             int least = 0, greatest = 0;
@@ -2129,11 +2129,11 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         plan.steps.push_back(S);
     }
     if (!act.empty()) {
-        GB_CUDA(cudaMalloc(&plan.d_act, act.size() * sizeof(int32_t)));
+        GB_CUDA(dev_alloc((void**)&plan.d_act, act.size() * sizeof(int32_t), plan.mem));
         GB_CUDA(cudaMemcpyAsync(plan.d_act, act.data(), act.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     }
     if (!pfx.empty()) {
-        GB_CUDA(cudaMalloc(&plan.d_pfx, pfx.size() * sizeof(int64_t)));
+        GB_CUDA(dev_alloc((void**)&plan.d_pfx, pfx.size() * sizeof(int64_t), plan.mem));
         GB_CUDA(cudaMemcpyAsync(plan.d_pfx, pfx.data(), pfx.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
     }
     GB_CUDA(cudaStreamSynchronize(st));
@@ -2207,10 +2207,10 @@ int trs_flow_build(TrsFlow& f, const std::vector<int64_t>& n_sorted, cudaStream_
     f.grid = (int32_t)std::min<int64_t>((int64_t)sms * per_sm, f.nitems);
     const size_t G = (size_t)f.groups;
     std::vector<float*> yp(G * f.nsys);
-    GB_CUDA(cudaMalloc(&f.d_items, sizeof(int2) * items.size()));
-    GB_CUDA(cudaMalloc(&f.d_ctl, sizeof(int32_t) * (2 + 2 * G * f.nsys)));
-    GB_CUDA(cudaMalloc(&f.d_y, sizeof(float) * FL_R * G * (size_t)rows));
-    GB_CUDA(cudaMalloc(&f.d_yp, sizeof(float*) * G * f.nsys));
+    GB_CUDA(dev_alloc((void**)&f.d_items, sizeof(int2) * items.size(), f.mem));
+    GB_CUDA(dev_alloc((void**)&f.d_ctl, sizeof(int32_t) * (2 + 2 * G * f.nsys), f.mem));
+    GB_CUDA(dev_alloc((void**)&f.d_y, sizeof(float) * FL_R * G * (size_t)rows, f.mem));
+    GB_CUDA(dev_alloc((void**)&f.d_yp, sizeof(float*) * G * f.nsys, f.mem));
     int64_t off = 0;
     for (size_t g = 0; g < G; g++)
         for (int32_t s = 0; s < f.nsys; s++) {
@@ -2255,10 +2255,10 @@ int trs_flow_check(const TrsFlow& f, cudaStream_t st) {
 }
 
 void TrsFlow::release() {
-    if (d_items) cudaFree(d_items);
-    if (d_ctl) cudaFree(d_ctl);
-    if (d_y) cudaFree(d_y);
-    if (d_yp) cudaFree(d_yp);
+    dev_free(d_items, mem);
+    dev_free(d_ctl, mem);
+    dev_free(d_y, mem);
+    dev_free(d_yp, mem);
     d_items = nullptr;
     d_ctl = nullptr;
     d_y = nullptr;
@@ -2267,9 +2267,9 @@ void TrsFlow::release() {
 }
 
 void LuPlan::release() {
-    if (d_act) cudaFree(d_act);
-    if (d_pfx) cudaFree(d_pfx);
-    if (d_err) cudaFree(d_err);
+    dev_free(d_act, mem);
+    dev_free(d_pfx, mem);
+    dev_free(d_err, mem);
     if (la_stream) cudaStreamDestroy(la_stream);
     if (la_fork) cudaEventDestroy(la_fork);
     if (la_join) cudaEventDestroy(la_join);

@@ -70,6 +70,7 @@ struct LuPlan {
     int cluster = 1;  // largest cluster the register panel can be launched with
     int tc_passes = 0;  // float trailing update: 0 CUDA cores, 1 TF32, 3 3xTF32 tensor cores
     bool tc_wide = false;  // the update right of the next outer panel in 128 x 256 tiles (GBVLM_TC_WIDE=0: 128 x 128)
+    cudaStream_t mem = nullptr;  // device memory stream-ordered on this stream (dev_alloc), or cudaMalloc
     int W = LU_NB;      // outer block width of the float factorisation
     int32_t* d_act = nullptr;
     int64_t* d_pfx = nullptr;
@@ -118,6 +119,7 @@ struct TrsFlow {
     int32_t* d_ctl = nullptr;  // counter, error word, per-system forward and backward progress
     float* d_y = nullptr;      // per system n x 8 row-major
     float** d_yp = nullptr;    // per-system pointers into d_y
+    cudaStream_t mem = nullptr;  // device memory stream-ordered on this stream (dev_alloc), or cudaMalloc
     void release();
     ~TrsFlow() { release(); }
     TrsFlow() = default;
