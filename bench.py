@@ -385,8 +385,9 @@ def run_gpu(args):
 # DRAM bytes per algorithmic byte of the tensor-core trailing update
 # (dram__bytes_read.sum + dram__bytes_write.sum of k_update_tc over the
 # launches' algorithmic bytes; the operands are re-read from L2, not DRAM),
-# from one ncu capture of the 64-case batch
-TC_TRAFFIC_PER_ALG_BYTE = 0.747  # 140.4 MB DRAM / 187.9 MB algorithmic
+# from one ncu capture of this batch (512 cases): its first graph replay,
+# 44 launches, 7.10 GB of DRAM traffic over 7.60 GB algorithmic
+TC_TRAFFIC_PER_ALG_BYTE = 0.935
 
 
 def roofline(bs, stream, peaks, ms_step):

@@ -506,6 +506,35 @@ int gbvlm_uvlm_run(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_
  * (synchronous then).  At most t_steps-1 steps. */
 int gbvlm_uvlm_begin(gbvlm_uvlm h, double dt, int32_t rollup, double sigma, gbvlm_stream stream);
 int gbvlm_uvlm_step(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, gbvlm_stream stream);
+/* The same step (vlm.cpp:410-508) as one CUDA-graph launch: every
+ * step-dependent argument (wake rows, wake column, pose at t_{i+1}) is read
+ * from a device counter, so the graph captured on the first call replays for
+ * every later step.  Float runs without roll-up, from the second step on
+ * (take the first with gbvlm_uvlm_step); the two may be mixed.  Results equal
+ * gbvlm_uvlm_step's within float rounding (the wake sums are sliced for the
+ * run's last row count). */
+int gbvlm_uvlm_step_graph(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, gbvlm_stream stream);
+
+/* Device-resident request loop over a resident case (serving; no reference
+ * counterpart: it advances the case as gbvlm_uvlm_step_graph does, one step
+ * per request).  One CUDA graph whose while node takes a step, writes that
+ * step's coefficients into mapped host memory and waits on the GPU, for at
+ * most poll_s (0 < poll_s <= 1), for the next request; without one it ends,
+ * and the next submit launches it again.  submit raises a counter in mapped
+ * host memory (a graph launch only when the loop had ended) and returns a
+ * ticket; wait polls that ticket's completion for at most timeout_s.  Steps
+ * run in ticket order.  While a loop exists the case takes no other step or
+ * begin and cannot be destroyed; after gbvlm_uvlm_loop_destroy it continues
+ * from the loop's last step.  Needs a float case without roll-up, its first
+ * step taken, and native atomics on host memory (GB300 with Grace). */
+typedef struct gbvlm_uvlm_loop_s* gbvlm_uvlm_loop;
+int gbvlm_uvlm_loop_create(gbvlm_uvlm_loop* out, gbvlm_uvlm h, double poll_s);
+int gbvlm_uvlm_loop_submit(gbvlm_uvlm_loop l, int64_t* ticket);
+int gbvlm_uvlm_loop_wait(gbvlm_uvlm_loop l, int64_t ticket, double timeout_s, int64_t* step_index, double* cl,
+                         double* cm);
+/* requests submitted and completed so far, and graph launches they took */
+int gbvlm_uvlm_loop_stats(gbvlm_uvlm_loop l, int64_t* submitted, int64_t* completed, int64_t* launches);
+int gbvlm_uvlm_loop_destroy(gbvlm_uvlm_loop l);
 /* cl: t_steps doubles, cm: 3*t_steps, gamma_last: n doubles of the last step (each may be NULL). Synchronous. */
 int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream);
 

@@ -105,6 +105,28 @@ def test_fp64_residual_needs_a_refinement_sweep(cuda):
         BatchSolver(cases, mode="shared", refine=0, fp64_residual=True)
 
 
+def test_non_finite_input_is_reported(cuda):
+    """A case whose vertices hold a NaN is reported by gbvlm_batch_results (GBVLM_ERR_ARG naming the case), the
+    next set_inputs/run with clean vertices is valid again, and a non-finite angle is refused at set_inputs."""
+    from tinyvlm_gb300._lib import GbvlmError
+    cases = M.batch_cases(4, seed=2, n_alpha=2, nc_range=(4, 6), ns_range=(4, 8))
+    bs = BatchSolver(cases, mode="shared", refine=1)
+    v = pack_verts(cases).copy()
+    v[sum(4 * (c.ns + 1) * (c.nc + 1) for c in cases[:2])] = np.nan  # x of case 2's first vertex
+    bs.set_inputs(v, pack_alphas(cases), ref_pt=REF)
+    bs.run()
+    with pytest.raises(GbvlmError, match="case 2: non-finite"):
+        bs.results()
+    bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    bs.run()
+    co, _ = bs.results()
+    _check(co, None, cases, "shared")
+    al = pack_alphas(cases).copy()
+    al[3] = np.inf
+    with pytest.raises(GbvlmError, match="GBVLM_ERR_ARG"):
+        bs.set_inputs(pack_verts(cases), al, ref_pt=REF)
+
+
 def test_batch_large_cases(cuda):
     """Sizes up to the full workload's largest (32 x 64 = 2048 panels)."""
     cases = M.batch_cases(4, seed=3, n_alpha=2, nc_range=(28, 32), ns_range=(56, 64))

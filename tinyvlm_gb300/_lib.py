@@ -118,6 +118,12 @@ def _protos():
     t["gbvlm_uvlm_results"] = [P, P, P, P, P]
     t["gbvlm_uvlm_begin"] = [P, F64, I32, F64, P]
     t["gbvlm_uvlm_step"] = [P, P, P, P, P]
+    t["gbvlm_uvlm_step_graph"] = [P, P, P, P, P]
+    t["gbvlm_uvlm_loop_create"] = [P, P, F64]
+    t["gbvlm_uvlm_loop_submit"] = [P, P]
+    t["gbvlm_uvlm_loop_wait"] = [P, I64, F64, P, P, P]
+    t["gbvlm_uvlm_loop_stats"] = [P, P, P, P]
+    t["gbvlm_uvlm_loop_destroy"] = [P]
     t["gbvlm_newmark_create"] = [P, F64, F64]
     t["gbvlm_newmark_destroy"] = [P]
     t["gbvlm_newmark_init"] = [P, I32, P, P, P, F64, P]

@@ -78,6 +78,7 @@ struct BatchArgs {
     float* gamma_out;       // per solve, n floats at goff[solve] (the caller's order; may be null)
     const int64_t* goff;
     const int32_t* uidx;    // batch solve -> the caller's solve index
+    int32_t* bad;           // per system: 1 if its case's vertices hold a non-finite coordinate
 };
 
 __device__ __forceinline__ void split_hl(double x, float& h, float& l) {
@@ -92,13 +93,19 @@ __global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
     SysDesc& S = a.sys[blockIdx.x];
     const int64_t ns = S.ns, nc = S.nc, nv = (ns + 1) * (nc + 1), np = ns * nc;
     const double al = S.alpha_geom;
+    int bad = 0;
     for (int64_t v = threadIdx.x; v < nv; v += blockDim.x) {
         for (int k = 0; k < 3; k++) {
             double x = (double)S.vinit[k * nv + v];
+            bad |= !isfinite(x);
             S.vd[k * nv + v] = x;
             split_hl(x, S.vh[k * nv + v], S.vl[k * nv + v]);
         }
     }
+    // a case with a non-finite coordinate is reported by gbvlm_batch_results
+    // (its solves come out non-finite; the other cases are unaffected)
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) a.bad[blockIdx.x] = bad;
     // wake (vlm.cpp:104-114 seen from the displaced wing): row 0 = trailing
     // edge, row 1 = trailing edge + 100 u (cos a, 0, sin a)
     const double dx = 100.0 * a.u_inf * cos(al), dz = 100.0 * a.u_inf * sin(al);
@@ -634,6 +641,7 @@ struct gbvlm_batch_s {
     float* d_gamma = nullptr;
     int64_t* d_goff = nullptr;
     int32_t* d_uidx = nullptr;   // batch solve -> the caller's solve
+    int32_t* d_bad = nullptr;    // per system: non-finite input vertices
     void* status = nullptr;      // pinned: error words and pivot flags read back with the results
     SysDesc* d_sys = nullptr;
     int32_t* d_solve_sys = nullptr;
@@ -743,6 +751,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     a.gamma_out = h->d_gamma;
     a.goff = h->d_goff;
     a.uidx = h->d_uidx;
+    a.bad = h->d_bad;
     // staged: every phase after the previous one on `st` (stage timing, or
     // kernel timing without the groups' launches overlapping); otherwise each
     // size group's assembly and factorisation run on its own branch, group 0
@@ -960,6 +969,7 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     const size_t o_sys = reserve(sizeof(SysDesc) * h->nsys);
     const size_t o_ssys = reserve(sizeof(int32_t) * solve_sys.size());
     const size_t o_uidx = reserve(sizeof(int32_t) * solve_sys.size());
+    const size_t o_bad = reserve(sizeof(int32_t) * h->nsys);
     // tile prefix tables
     std::vector<int64_t> tpfx(h->nsys + 1, 0), rpfx(h->nsys + 1, 0);
     for (int k = 0; k < h->nsys; k++) {
@@ -999,6 +1009,7 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     h->d_sys = (SysDesc*)(base + o_sys);
     h->d_solve_sys = (int32_t*)(base + o_ssys);
     h->d_uidx = (int32_t*)(base + o_uidx);
+    h->d_bad = (int32_t*)(base + o_bad);
     h->d_tpfx = (int64_t*)(base + o_tpfx);
     h->d_rpfx = (int64_t*)(base + o_rpfx);
     // system descriptors
@@ -1186,6 +1197,8 @@ int gbvlm_batch_set_inputs(gbvlm_batch h, const float* verts, const double* alph
                            const double* ref_pt, gbvlm_stream stream) {
     GB_REQUIRE(h && verts && alphas, "null argument");
     GB_REQUIRE(u_inf > 0 && rho > 0, "u_inf and rho must be positive");
+    for (int32_t u = 0; u < h->nsolve; u++)
+        GB_REQUIRE(isfinite(alphas[u]), "alpha %d is not finite", u);
     cudaStream_t st = to_cuda(stream);
     // conditions baked into the graph: rebuild it if they change
     const double r[3] = {ref_pt ? ref_pt[0] : 0, ref_pt ? ref_pt[1] : 0, ref_pt ? ref_pt[2] : 0};
@@ -1323,7 +1336,7 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
         GB_CUDA(cudaMemcpyAsync(gamma, h->d_gamma, sizeof(float) * h->gamma_floats, cudaMemcpyDeviceToHost, st));
     // status words (bounded-wait errors of the LU plans and the triangular
     // solve, pivot flags) with the same synchronisation
-    const size_t sbytes = sizeof(int32_t) * (G + 1 + (size_t)h->nsys);
+    const size_t sbytes = sizeof(int32_t) * (G + 1 + 2 * (size_t)h->nsys);
     if (!h->status) {
         h->status = pinned_take(sbytes);
         if (!h->status) {
@@ -1340,6 +1353,7 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
     if (h->use_flow && h->flow.d_ctl)
         GB_CUDA(cudaMemcpyAsync(hs + G, h->flow.d_ctl + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaMemcpyAsync(hs + G + 1, h->lub.info, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(hs + G + 1 + h->nsys, h->d_bad, sizeof(int32_t) * h->nsys, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     for (int g = 0; g < h->ngroups; g++)
         if (hs[g]) {
@@ -1349,6 +1363,12 @@ int gbvlm_batch_results(gbvlm_batch h, double* coeffs, float* gamma, gbvlm_strea
     if (hs[G]) {
         set_error("triangular solve: a block timed out waiting for the blocks it depends on");
         return GBVLM_ERR_CUDA;
+    }
+    for (int k = 0; k < h->nsys; k++) {
+        if (hs[G + 1 + h->nsys + k] != 0) {
+            set_error("batch case %d: non-finite vertex coordinates (its solves are not valid)", h->sys[k].case_id);
+            return GBVLM_ERR_ARG;
+        }
     }
     for (int k = 0; k < h->nsys; k++) {
         if (hs[G + 1 + k] != 0) {

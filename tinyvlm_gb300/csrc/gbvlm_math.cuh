@@ -176,15 +176,13 @@ struct CSum {
 };
 
 // ---------------------------------------------------------------------------
-// Float-pair arithmetic: x = v + e held as two floats, evaluated on the fp32
-// pipes.  v follows the plain float evaluation; e collects the rounding
-// errors to first order: each sum's error exactly (Knuth's TwoSum), each
-// product's exactly (an FMA), plus the operands' e carried through linearly.
-// The pairs are not renormalised: a term dropped by that (e times e) is of
-// order 2^-48 of the operands' magnitudes, far below what the correction of
-// a float AIC needs (its entries to about 1e-10).  The intrinsics keep every
-// rounding as written (no contraction).  Used where the float AIC must be
-// corrected toward its FP64 value (the refinement residual of the batched
+// Float-pair arithmetic: x = v + e held as two floats (Dekker's double-length
+// arithmetic; Knuth's TwoSum and an FMA-exact product), about 44 significant
+// bits evaluated on the fp32 pipes.  Sums are renormalised (a difference
+// whose float parts cancel exactly keeps its value in v, so later products
+// see it), products are left with |e| of a few ulp(v).  The intrinsics keep
+// every rounding as written (no contraction).  Used where the float AIC must
+// be corrected toward its FP64 value (the refinement residual of the batched
 // solver).
 // ---------------------------------------------------------------------------
 struct Fe {
@@ -196,11 +194,15 @@ struct Fe {
     __host__ __device__ constexpr Fe(double a) : v((float)a), e((float)(a - (double)(float)a)) {}
 };
 
+__device__ __forceinline__ Fe fe_fast2sum(float s, float t) {  // |s| >= |t| or s == 0
+    const float h = __fadd_rn(s, t);
+    return Fe(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
 __device__ __forceinline__ Fe operator+(Fe a, Fe b) {
     const float s = __fadd_rn(a.v, b.v);
     const float bb = __fsub_rn(s, a.v);
     const float err = __fadd_rn(__fsub_rn(a.v, __fsub_rn(s, bb)), __fsub_rn(b.v, bb));  // a.v + b.v - s exactly
-    return Fe(s, __fadd_rn(err, __fadd_rn(a.e, b.e)));
+    return fe_fast2sum(s, __fadd_rn(err, __fadd_rn(a.e, b.e)));
 }
 __device__ __forceinline__ Fe operator-(Fe a) { return Fe(-a.v, -a.e); }
 __device__ __forceinline__ Fe operator-(Fe a, Fe b) { return a + (-b); }
@@ -221,8 +223,7 @@ template <> struct Prec<Fe> {
 };
 template <> __device__ __forceinline__ Fe fast_len<Fe>(Fe n2) {
     // s = sqrt(v) to a few ulp, then one Newton correction from the exact
-    // residual v - s^2 (plus e): sqrt(v + e) = s + (v - s^2 + e) / (2 s) to
-    // first order (n2 is a sum of squares: |e| is a few ulp of v)
+    // residual v - s^2 (plus e): sqrt(v + e) = s + (v - s^2 + e) / (2 s)
     const float r = rsqrtf(n2.v + 1e-37f);
     const float s = __fmul_rn(n2.v, r);
     const float d = __fadd_rn(__fmaf_rn(-s, s, n2.v), n2.e);

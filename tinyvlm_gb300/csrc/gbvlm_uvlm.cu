@@ -16,6 +16,11 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
+#include <chrono>
+#include <mutex>
+#include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "gbvlm_internal.h"
@@ -162,16 +167,44 @@ struct Ops2;
 OPS2(float, f32)
 OPS2(double, f64)
 
+// Device-indexed UVLM step (float, no roll-up): the step index i lives in
+// idx[0] on the device.  The pose kernel stages T(i+1) and Td(i) of every
+// surface and the step's free stream and moment point into fixed buffers,
+// so one captured graph advances the case any number of times.
+template <class T>
+__global__ void k_uvlm_dev_pose(const int64_t* idx, const T* Tm, const T* Tdm, const T* fs, const T* ref, int nsurf,
+                                T* pose) {
+    const int64_t i = idx[0];
+    for (int q = threadIdx.x; q < 16 * nsurf; q += blockDim.x) {
+        pose[q] = Tm[16 * (i + 1) * nsurf + q];
+        pose[16 * nsurf + q] = Tdm[16 * i * nsurf + q];
+    }
+    if (threadIdx.x < 3) {
+        pose[32 * nsurf + threadIdx.x] = fs[3 * i + threadIdx.x];
+        pose[32 * nsurf + 3 + threadIdx.x] = ref[3 * i + threadIdx.x];
+    }
+}
+
+// the step's coefficients into the run's record, then i -> i + 1
+__global__ void k_uvlm_dev_end(int64_t* idx, const double* coef, double* res) {
+    const int64_t i = idx[0];
+    if (threadIdx.x < 4) res[4 * i + threadIdx.x] = coef[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) idx[0] = i + 1;
+}
+
 struct UvlmBase {
     virtual ~UvlmBase() = default;
     virtual int set_kinematics(const double* T, const double* Td, const double* fs, const double* ref) = 0;
     virtual int run(double dt, int32_t rollup, double sigma, cudaStream_t st) = 0;
     virtual int begin(double dt, int32_t rollup, double sigma, cudaStream_t st) = 0;
     virtual int step(cudaStream_t st) = 0;
+    virtual int step_graph(cudaStream_t st) = 0;
     virtual int step_result(int64_t i, double* cl, double* cm, cudaStream_t st) = 0;
     virtual int64_t last_step() const = 0;
     virtual int results(double* cl, double* cm, double* gamma_last, cudaStream_t st) = 0;
     int64_t t_steps = 0, n = 0;
+    bool looping = false;  // a request loop (gbvlm_uvlm_loop_*) owns the steps
 };
 
 template <class T>
@@ -186,7 +219,25 @@ struct UvlmState : UvlmBase {
     double* res = nullptr;  // [t_steps][4]
     gbvlm_lu lu = nullptr;
 
+    // device-indexed step (step_graph): counter, staged pose, wake scratch,
+    // coefficients, the staged LU solve and the captured graph
+    int64_t* d_idx = nullptr;
+    T* d_pose = nullptr;
+    float* wsc = nullptr;
+    double* d_coef = nullptr;
+    void* dmem = nullptr;
+    void* lut = nullptr;
+    int64_t dev_idx = -1;  // the value idx[0] holds on the device (-1: unknown)
+    cudaStream_t scap = nullptr;
+    cudaGraph_t sgraph = nullptr;
+    cudaGraphExec_t sexec = nullptr;
+
     ~UvlmState() override {
+        if (sexec) cudaGraphExecDestroy(sexec);
+        if (sgraph) cudaGraphDestroy(sgraph);
+        if (scap) cudaStreamDestroy(scap);
+        if (lut) lu_solve_tables_free(lut);
+        if (dmem) cudaFree(dmem);
         if (lu) gbvlm_lu_destroy(lu);
         if (mem) cudaFree(mem);
     }
@@ -302,7 +353,16 @@ struct UvlmState : UvlmBase {
         sigma_ = sigma;
         roll_ = roll;
         next_step = 0;
+        GB_REQUIRE(!looping, "UVLM: a request loop advances this case (destroy it first)");
         int rc;
+        // a new run refactors the AIC: the staged solve and the step graph are rebuilt on first use
+        if (sexec) cudaGraphExecDestroy(sexec);
+        if (sgraph) cudaGraphDestroy(sgraph);
+        sexec = nullptr;
+        sgraph = nullptr;
+        if (lut) lu_solve_tables_free(lut);
+        lut = nullptr;
+        dev_idx = -1;
         // t = 0 placement (vlm.cpp:368-376): verts_pos = T(0) verts_init; metrics; colloc at t = 0 kept
         auto t0 = tr_at(Tm, 0);
         if ((rc = Ops2<T>::displace(nsurf, dims.data(), t0.data(), vpos.data(), C(vinit).data(), s))) return rc;
@@ -337,6 +397,7 @@ struct UvlmState : UvlmBase {
     // one time step (vlm.cpp:410-508); steps run in order 0, 1, ..., t_steps-2
     int step(cudaStream_t st) override {
         gbvlm_stream s = (gbvlm_stream)st;
+        GB_REQUIRE(!looping, "UVLM: a request loop advances this case (destroy it first)");
         GB_REQUIRE(next_step + 1 < t_steps, "UVLM: all %lld steps done (wake capacity)", (long long)t_steps);
         const int64_t i = next_step++;
         const T dt = dt_, sigma = sigma_;
@@ -389,6 +450,127 @@ struct UvlmState : UvlmBase {
                 return rc;
         }
         return GBVLM_OK;
+    }
+
+    // The step of step() with every step-dependent argument read from the
+    // device (float, no roll-up, from step 1 on): captured into one graph on
+    // first use and replayed, one launch per step.  Results equal step()'s
+    // within float rounding (the wake sums are sliced for the run's last row
+    // count, not the step's).
+    int step_graph(cudaStream_t st) override {
+        if constexpr (!std::is_same<T, float>::value) {
+            set_error("UVLM graph step: float runs only");
+            return GBVLM_ERR_ARG;
+        } else {
+            GB_REQUIRE(!looping, "UVLM: a request loop advances this case (destroy it first)");
+            GB_REQUIRE(!roll_, "UVLM graph step: roll-up runs step on the host");
+            GB_REQUIRE(next_step >= 1, "UVLM graph step: take the first step with gbvlm_uvlm_step");
+            GB_REQUIRE(next_step + 1 < t_steps, "UVLM: all %lld steps done (wake capacity)", (long long)t_steps);
+            int rc;
+            if (!sexec && (rc = build_step_graph(st))) return rc;
+            if (dev_idx != next_step) {
+                GB_CUDA(cudaMemcpyAsync(d_idx, &next_step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+                GB_CUDA(cudaStreamSynchronize(st));  // next_step is host memory that changes below
+            }
+            GB_CUDA(cudaGraphLaunch(sexec, st));
+            next_step++;
+            dev_idx = next_step;
+            return GBVLM_OK;
+        }
+    }
+
+    // the device-indexed step on stream c (captured by step_graph and by the
+    // request loop of gbvlm_uvlm_loop_*)
+    int enqueue_dev_step(cudaStream_t c) {
+        gbvlm_stream cs = (gbvlm_stream)c;
+        int r;
+        k_uvlm_dev_pose<T><<<1, 128, 0, c>>>(d_idx, Tm, Tdm, fs, ref, nsurf, d_pose);
+        GB_LAUNCH_CHECK();
+        if ((r = wake_shed_dev_f32(nsurf, dims.data(), C(verts).data(), wake.data(), d_idx, c))) return r;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t np = dims[m].ns * dims[m].nc;
+            k_dual_velocity<T><<<(unsigned)cdiv(np, 256), 256, 0, c>>>(d_pose + 16 * nsurf + 16 * m,
+                                                                      colloc0[m], vel[m], np);
+            GB_LAUNCH_CHECK();
+        }
+        GB_CUDA(cudaMemsetAsync(rhs, 0, sizeof(T) * n, c));
+        if ((r = Ops2<T>::rhsv(rhs, nsurf, dims.data(), C(normals).data(), C(vel).data(), cs))) return r;
+        if ((r = wake_influence_dev_f32(rhs, nsurf, dims.data(), C(gwake).data(), C(colloc).data(),
+                                        C(normals).data(), C(wake).data(), lifting.data(), d_idx,
+                                        (int32_t)(t_steps - 2), wsc, c)))
+            return r;
+        if ((r = lu_solve_prepared_f32(lu, lut, n, c))) return r;
+        int64_t off = 0;
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t ns = dims[m].ns, nc = dims[m].nc;
+            if ((r = gamma_update_dev_f32(ns, nc, rhs + off, gamma[m], gdelta[m], gwake[m], t_steps - 2, d_idx,
+                                          gprev[m], gdt[m], dt_, c)))
+                return r;
+            off += ns * nc;
+        }
+        for (int m = 0; m < nsurf; m++)
+            if ((r = Ops2<T>::forces(dims[m].ns, dims[m].nc, verts[m], gdelta[m], gdt[m], vel[m], areas[m],
+                                     normals[m], forces[m], cs)))
+                return r;
+        k_step_coeffs<T><<<1, 512, 0, c>>>(ca, d_pose + 32 * nsurf, d_pose + 32 * nsurf + 3, 0, 1.0, d_coef);
+        GB_LAUNCH_CHECK();
+        for (int m = 0; m < nsurf; m++) {
+            const int64_t np = dims[m].ns * dims[m].nc;
+            GB_CUDA(cudaMemcpyAsync(gprev[m], gamma[m], sizeof(T) * np, cudaMemcpyDeviceToDevice, c));
+        }
+        std::vector<const T*> tn(nsurf);
+        for (int m = 0; m < nsurf; m++) tn[m] = d_pose + 16 * m;
+        if ((r = Ops2<T>::displace(nsurf, dims.data(), tn.data(), verts.data(), C(vpos).data(), cs))) return r;
+        if ((r = Ops2<T>::metrics(nsurf, dims.data(), C(verts).data(), colloc.data(), normals.data(),
+                                  areas.data(), cs)))
+            return r;
+        k_uvlm_dev_end<<<1, 32, 0, c>>>(d_idx, d_coef, res);
+        GB_LAUNCH_CHECK();
+        return GBVLM_OK;
+    }
+
+    // device buffers of the device-indexed step and the staged LU solve
+    int prepare_dev(cudaStream_t st) {
+        if (!dmem) {
+            const size_t pose = sizeof(T) * (32 * nsurf + 6), wb = sizeof(float) * WAKE_DEV_MAX_SLICES * n;
+            GB_CUDA(cudaMalloc(&dmem, 256 + 256 + (pose + 255) / 256 * 256 + wb));
+            d_idx = (int64_t*)dmem;
+            d_coef = (double*)((char*)dmem + 256);
+            d_pose = (T*)((char*)dmem + 512);
+            wsc = (float*)((char*)dmem + 512 + (pose + 255) / 256 * 256);
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (!lut) {
+                int rc = lu_solve_prepare_f32(lu, lhs, n, rhs, &lut, st);
+                if (rc) return rc;
+            }
+        }
+        return GBVLM_OK;
+    }
+
+    int build_step_graph(cudaStream_t st) {
+        if constexpr (std::is_same<T, float>::value) {
+            int rc = prepare_dev(st);
+            if (rc) return rc;
+            if (!scap) GB_CUDA(cudaStreamCreateWithFlags(&scap, cudaStreamNonBlocking));
+            GB_CUDA(cudaStreamSynchronize(st));
+            GB_CUDA(cudaStreamBeginCapture(scap, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_dev_step(scap);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(scap, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            GB_CUDA(e);
+            sgraph = g;
+            GB_CUDA(cudaGraphInstantiate(&sexec, sgraph, 0));
+            dev_idx = -1;
+            return GBVLM_OK;
+        } else {
+            (void)st;
+            return GBVLM_ERR_ARG;
+        }
     }
 
     int64_t last_step() const override { return next_step - 1; }
@@ -928,6 +1110,103 @@ struct gbvlm_uvlm_s {
     UvlmBase* impl = nullptr;
 };
 
+// ===========================================================================
+// Device-resident request loop over a resident UVLM case.  One CUDA graph: a
+// while node whose body is the device-indexed step followed by
+// k_uvlm_loop_next.  The host submits a request by raising a counter in
+// mapped host memory; the running graph takes one step per request, writes
+// each step's coefficients into a mapped record and raises the done
+// counter, then waits (bounded) for the next request.  After poll_ns
+// without one it marks itself stopped and ends; the next submit launches
+// the graph again.  Between requests no CUDA call is made.
+// ===========================================================================
+namespace gbvlm {
+
+struct LoopCtl {
+    int64_t enq;    // requests submitted (host)
+    int64_t done;   // requests completed (device)
+    int32_t state;  // 0: no graph running or about to run, 1: running (both sides, system-scope atomics)
+    int32_t stop;   // host: end the loop
+    int32_t error;  // device: 1 = the wake is full
+    int32_t pad;
+};
+struct LoopRec {
+    int64_t step;
+    double c[4];  // CL, CM x, y, z
+};
+
+__device__ __forceinline__ uint64_t loop_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// last_idx: the largest step index the wake holds
+__global__ void k_uvlm_loop_next(LoopCtl* ctl, LoopRec* rec, const int64_t* idx, const double* res, int64_t last_idx,
+                                 uint64_t poll_ns, cudaGraphConditionalHandle loop) {
+    if (threadIdx.x != 0) return;
+    volatile LoopCtl* vc = ctl;
+    const int64_t i = idx[0] - 1;  // the step this iteration took
+    const int64_t t = vc->done;
+    rec[t].step = i;
+    for (int k = 0; k < 4; k++) rec[t].c[k] = res[4 * i + k];
+    __threadfence_system();
+    vc->done = t + 1;
+    __threadfence_system();
+    unsigned cont = 0;
+    bool released = false;
+    if (idx[0] > last_idx) {
+        vc->error = 1;
+    } else {
+        const uint64_t t0 = loop_ns();
+        while (true) {
+            if (vc->stop) break;
+            if (vc->enq > t + 1) {
+                cont = 1;
+                break;
+            }
+            if (loop_ns() - t0 > poll_ns) {
+                // stop, unless a request came in meanwhile and the host has
+                // not already taken the running state to launch a new graph
+                atomicExch_system(&ctl->state, 0);
+                released = true;
+                __threadfence_system();
+                if (vc->enq > t + 1 && atomicCAS_system(&ctl->state, 0, 1) == 0) {
+                    cont = 1;
+                    released = false;
+                }
+                break;
+            }
+            __nanosleep(2000);
+        }
+    }
+    if (!cont && !released) atomicExch_system(&ctl->state, 0);
+    cudaGraphSetConditional(loop, cont);
+}
+
+}  // namespace gbvlm
+
+struct gbvlm_uvlm_loop_s {
+    gbvlm_uvlm owner = nullptr;
+    UvlmState<float>* u = nullptr;
+    LoopCtl* ctl = nullptr;  // mapped host memory
+    LoopRec* rec = nullptr;
+    LoopCtl* ctl_d = nullptr;
+    LoopRec* rec_d = nullptr;
+    int64_t cap = 0, base_step = 0, enq = 0, launches = 0;
+    cudaStream_t st = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::mutex mu;
+    ~gbvlm_uvlm_loop_s() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (st) cudaStreamDestroy(st);
+        if (ctl) cudaFreeHost(ctl);
+        if (rec) cudaFreeHost(rec);
+    }
+};
+
 extern "C" {
 
 int gbvlm_uvlm_create(gbvlm_uvlm* out, int32_t nsurf, const gbvlm_dims* dims, const float* const* verts_init,
@@ -959,6 +1238,7 @@ int gbvlm_uvlm_create(gbvlm_uvlm* out, int32_t nsurf, const gbvlm_dims* dims, co
 
 int gbvlm_uvlm_destroy(gbvlm_uvlm h) {
     if (!h) return GBVLM_OK;
+    GB_REQUIRE(!h->impl || !h->impl->looping, "UVLM: destroy its request loop first");
     delete h->impl;
     delete h;
     return GBVLM_OK;
@@ -989,6 +1269,159 @@ int gbvlm_uvlm_step(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, g
     if (step_index) *step_index = i;
     if (cl || cm) return u->step_result(i, cl, cm, to_cuda(stream));
     return GBVLM_OK;
+}
+
+int gbvlm_uvlm_step_graph(gbvlm_uvlm h, int64_t* step_index, double* cl, double* cm, gbvlm_stream stream) {
+    GB_REQUIRE(h && h->impl, "null argument");
+    int rc = h->impl->step_graph(to_cuda(stream));
+    if (rc) return rc;
+    auto* u = h->impl;
+    const int64_t i = u->last_step();
+    if (step_index) *step_index = i;
+    if (cl || cm) return u->step_result(i, cl, cm, to_cuda(stream));
+    return GBVLM_OK;
+}
+
+int gbvlm_uvlm_loop_create(gbvlm_uvlm_loop* out, gbvlm_uvlm h, double poll_s) {
+    GB_REQUIRE(out && h && h->impl, "null argument");
+    GB_REQUIRE(poll_s > 0 && poll_s <= 1.0, "poll_s=%g outside (0, 1] s", poll_s);
+    auto* u = dynamic_cast<UvlmState<float>*>(h->impl);
+    GB_REQUIRE(u, "UVLM request loop: float runs only");
+    GB_REQUIRE(!u->looping, "UVLM request loop: this case already has one");
+    GB_REQUIRE(!u->roll_, "UVLM request loop: roll-up runs step on the host");
+    GB_REQUIRE(u->next_step >= 1, "UVLM request loop: take the first step with gbvlm_uvlm_step");
+    GB_REQUIRE(u->next_step + 1 < u->t_steps, "UVLM: all %lld steps done (wake capacity)", (long long)u->t_steps);
+    int dev = 0, native = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&native, cudaDevAttrHostNativeAtomicSupported, dev));
+    GB_REQUIRE(native, "UVLM request loop: the device has no native atomics on host memory");
+    auto* l = new gbvlm_uvlm_loop_s();
+    l->owner = h;
+    l->u = u;
+    l->base_step = u->next_step;
+    l->cap = u->t_steps - 1 - u->next_step;
+    auto fail = [&](int rc) {
+        delete l;
+        return rc;
+    };
+    int rc = u->prepare_dev(0);
+    if (rc) return fail(rc);
+    cudaError_t e = cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&l->ctl, sizeof(LoopCtl), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&l->rec, sizeof(LoopRec) * (size_t)l->cap, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&l->ctl_d, l->ctl, 0);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&l->rec_d, l->rec, 0);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "UVLM request loop set-up", __FILE__, __LINE__));
+    memset(l->ctl, 0, sizeof(LoopCtl));
+    memset(l->rec, 0, sizeof(LoopRec) * (size_t)l->cap);
+    // the device step counter at the case's next step
+    e = cudaMemcpy(u->d_idx, &u->next_step, sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "UVLM request loop set-up", __FILE__, __LINE__));
+    u->dev_idx = u->next_step;
+    // graph: while (cond) { device-indexed step; next }
+    cudaGraphConditionalHandle cond;
+    cudaGraphNode_t nw;
+    cudaGraphNodeParams wp = {};
+    e = cudaGraphCreate(&l->graph, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, l->graph, 1, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) {
+        wp.type = cudaGraphNodeTypeConditional;
+        wp.conditional.handle = cond;
+        wp.conditional.type = cudaGraphCondTypeWhile;
+        wp.conditional.size = 1;
+        e = cudaGraphAddNode(&nw, l->graph, nullptr, nullptr, 0, &wp);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(l->st, wp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "UVLM request loop graph", __FILE__, __LINE__));
+    rc = u->enqueue_dev_step(l->st);
+    if (rc == GBVLM_OK) {
+        const uint64_t poll_ns = (uint64_t)(poll_s * 1e9);
+        k_uvlm_loop_next<<<1, 32, 0, l->st>>>(l->ctl_d, l->rec_d, u->d_idx, u->res, u->t_steps - 2, poll_ns, cond);
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) rc = cuda_fail(le, "k_uvlm_loop_next", __FILE__, __LINE__);
+    }
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(l->st, &got);
+    if (rc) return fail(rc);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&l->exec, l->graph, 0);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "UVLM request loop graph", __FILE__, __LINE__));
+    u->looping = true;
+    *out = l;
+    return GBVLM_OK;
+}
+
+int gbvlm_uvlm_loop_submit(gbvlm_uvlm_loop l, int64_t* ticket) {
+    GB_REQUIRE(l && ticket, "null argument");
+    std::lock_guard<std::mutex> g(l->mu);
+    GB_REQUIRE(l->enq < l->cap, "UVLM request loop: the wake holds %lld more steps", (long long)l->cap);
+    GB_REQUIRE(!__atomic_load_n(&l->ctl->stop, __ATOMIC_SEQ_CST), "UVLM request loop: stopped");
+    const int64_t t = ++l->enq;
+    __atomic_store_n(&l->ctl->enq, t, __ATOMIC_SEQ_CST);
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    int32_t idle = 0;
+    if (__atomic_load_n(&l->ctl->state, __ATOMIC_SEQ_CST) == 0 &&
+        __atomic_compare_exchange_n(&l->ctl->state, &idle, 1, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+        GB_CUDA(cudaGraphLaunch(l->exec, l->st));
+        l->launches++;
+    }
+    *ticket = t;
+    return GBVLM_OK;
+}
+
+int gbvlm_uvlm_loop_wait(gbvlm_uvlm_loop l, int64_t ticket, double timeout_s, int64_t* step_index, double* cl,
+                         double* cm) {
+    GB_REQUIRE(l && ticket >= 1 && timeout_s >= 0, "bad arguments");
+    GB_REQUIRE(ticket <= l->enq, "UVLM request loop: ticket %lld not submitted", (long long)ticket);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    while (__atomic_load_n(&l->ctl->done, __ATOMIC_ACQUIRE) < ticket) {
+        if (__atomic_load_n(&l->ctl->error, __ATOMIC_ACQUIRE)) {
+            set_error("UVLM request loop: the wake is full");
+            return GBVLM_ERR_ARG;
+        }
+        const cudaError_t q = cudaStreamQuery(l->st);
+        if (q != cudaSuccess && q != cudaErrorNotReady) return cuda_fail(q, "UVLM request loop", __FILE__, __LINE__);
+        if (std::chrono::steady_clock::now() > deadline) {
+            set_error("UVLM request loop: ticket %lld not done within %g s", (long long)ticket, timeout_s);
+            return GBVLM_ERR_CUDA;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    const LoopRec& r = l->rec[ticket - 1];
+    if (step_index) *step_index = r.step;
+    if (cl) *cl = r.c[0];
+    if (cm)
+        for (int k = 0; k < 3; k++) cm[k] = r.c[1 + k];
+    return GBVLM_OK;
+}
+
+int gbvlm_uvlm_loop_stats(gbvlm_uvlm_loop l, int64_t* submitted, int64_t* completed, int64_t* launches) {
+    GB_REQUIRE(l, "null argument");
+    std::lock_guard<std::mutex> g(l->mu);
+    if (submitted) *submitted = l->enq;
+    if (completed) *completed = __atomic_load_n(&l->ctl->done, __ATOMIC_ACQUIRE);
+    if (launches) *launches = l->launches;
+    return GBVLM_OK;
+}
+
+int gbvlm_uvlm_loop_destroy(gbvlm_uvlm_loop l) {
+    if (!l) return GBVLM_OK;
+    int rc = GBVLM_OK;
+    {
+        std::lock_guard<std::mutex> g(l->mu);
+        __atomic_store_n(&l->ctl->stop, 1, __ATOMIC_SEQ_CST);
+    }
+    // a running graph sees the stop flag within its poll wait and ends
+    cudaError_t e = cudaStreamSynchronize(l->st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "UVLM request loop", __FILE__, __LINE__);
+    // the case continues host-stepped from where the loop left it
+    const int64_t done = __atomic_load_n(&l->ctl->done, __ATOMIC_ACQUIRE);
+    l->u->next_step = l->base_step + done;
+    l->u->dev_idx = l->u->next_step;
+    l->u->looping = false;
+    delete l;
+    return rc;
 }
 
 int gbvlm_uvlm_results(gbvlm_uvlm h, double* cl, double* cm, double* gamma_last, gbvlm_stream stream) {

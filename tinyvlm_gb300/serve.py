@@ -26,6 +26,12 @@ Design
   step (steps run in arrival order, they depend on each other), an HBVLM
   request runs the harmonic-balance fixed point for its own frequency and
   amplitudes from rest.
+* UVLM requests bypass the lanes: they go to a device-resident request loop
+  (``device_loop``, gbvlm_uvlm_loop_*).  Submitting one raises a counter in
+  mapped host memory; a CUDA graph running on the GPU takes the step, writes
+  its coefficients back and waits (on the GPU, bounded by ``poll_s``) for
+  the next request, so back-to-back steps make no CUDA call at all.  One
+  host thread collects the completions in ticket order.
 
 Every result carries its arrival, start and finish times; ``latency`` is
 finish - arrival.
@@ -64,7 +70,7 @@ def steady_bytes(n, nalpha=1):
 
 class Server:
     def __init__(self, lanes=3, hbm_budget=32 << 30, max_batch=64, uvlm=None, hbvlm=None, mode="exact", refine=1,
-                 wait_s=120.0):
+                 wait_s=120.0, device_loop=True, poll_s=0.05):
         from .device import device_info
         self.lanes = lanes
         free = device_info()[1]
@@ -82,6 +88,12 @@ class Server:
         self.uvlm_next_ticket = 0  # issued at dequeue time: steps run in arrival order
         self.uvlm_turn = 0
         self.hbvlm_factory = hbvlm
+        self.device_loop = device_loop and uvlm is not None
+        self.poll_s = poll_s
+        self.uloop = None
+        self.device_loop_error = None
+        self.uq = collections.deque()
+        self.ucv = threading.Condition()
         self.threads = []
         self.stats = collections.Counter()
 
@@ -111,20 +123,61 @@ class Server:
             t = threading.Thread(target=self._lane, args=(k,), daemon=True)
             t.start()
             self.threads.append(t)
+        if self.device_loop:
+            from ._lib import GbvlmError
+            try:
+                self.uloop = UvlmLoop(self.uvlm, self.poll_s)
+            except GbvlmError as e:  # e.g. no native atomics on host memory: the lanes step the case
+                self.device_loop = False
+                self.stats["device_loop_unavailable"] += 1
+                self.device_loop_error = str(e)
+        if self.device_loop:
+            t = threading.Thread(target=self._uvlm_completions, daemon=True)
+            t.start()
+            self.threads.append(t)
         return self
 
     def shutdown(self):
         with self.cv:
             self.stop = True
             self.cv.notify_all()
+        with self.ucv:
+            self.ucv.notify_all()
         for t in self.threads:
             t.join()
+        if self.uloop is not None:
+            self.uloop.close()
+            self.uloop = None
 
     def submit(self, req):
+        if req.kind == "uvlm" and self.uloop is not None:
+            with self.ucv:  # tickets and the completion queue in the same order
+                req.start = time.perf_counter()
+                req.payload = self.uloop.submit()
+                self.uq.append(req)
+                self.ucv.notify()
+            return req
         with self.cv:
             self.q.append(req)
             self.cv.notify()
         return req
+
+    def _uvlm_completions(self):
+        """Completions of the device loop, in ticket order."""
+        while True:
+            with self.ucv:
+                while not self.uq and not self.stop:
+                    self.ucv.wait()
+                if not self.uq:
+                    return
+                req = self.uq.popleft()
+            try:
+                req.result = self.uloop.wait(req.payload, self.wait_s)
+            except Exception as e:  # the request fails, the loop keeps serving
+                req.error = e
+            req.finish = time.perf_counter()
+            req.done.set()
+            self.stats["uvlm_loop_steps"] += 1
 
     # -- workers ------------------------------------------------------------
     def _take(self):
@@ -294,6 +347,46 @@ def resident_uvlm(ns=80, nc=20, warm_steps=500, capacity=4096, rollup=False):
         call("gbvlm_uvlm_step", h, None, None, None, None)
     call("gbvlm_device_synchronize")
     return sim
+
+
+class UvlmLoop:
+    """The device-resident request loop of a resident UVLM case
+    (gbvlm_uvlm_loop_*): submit() returns a ticket at once, wait() returns
+    that step's (step index, CL, CM) when the GPU has taken it."""
+
+    def __init__(self, sim, poll_s=0.05):
+        import ctypes
+        from ._lib import P, call
+        self.h = ctypes.c_void_p()
+        call("gbvlm_uvlm_loop_create", ctypes.cast(ctypes.pointer(self.h), P), sim.h, float(poll_s))
+
+    def submit(self):
+        import ctypes
+        from ._lib import P, call
+        t = ctypes.c_int64()
+        call("gbvlm_uvlm_loop_submit", self.h, ctypes.cast(ctypes.pointer(t), P))
+        return t.value
+
+    def wait(self, ticket, timeout_s=120.0):
+        import ctypes
+        from ._lib import P, call
+        step, cl, cm = ctypes.c_int64(), ctypes.c_double(), (ctypes.c_double * 3)()
+        call("gbvlm_uvlm_loop_wait", self.h, int(ticket), float(timeout_s), ctypes.cast(ctypes.pointer(step), P),
+             ctypes.cast(ctypes.pointer(cl), P), ctypes.cast(cm, P))
+        return step.value, cl.value, tuple(cm)
+
+    def stats(self):
+        import ctypes
+        from ._lib import P, call
+        v = [ctypes.c_int64() for _ in range(3)]
+        call("gbvlm_uvlm_loop_stats", self.h, *[ctypes.cast(ctypes.pointer(x), P) for x in v])
+        return {"submitted": v[0].value, "completed": v[1].value, "launches": v[2].value}
+
+    def close(self):
+        from ._lib import call
+        if self.h:
+            call("gbvlm_uvlm_loop_destroy", self.h)
+            self.h = None
 
 
 def hbvlm_factory(nc=45, harmonics=5):
