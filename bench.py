@@ -353,7 +353,8 @@ def run_gpu(args):
                          ("B_uvlm_20x80_500_steps", lambda: config_b(500)),
                          ("C_elliptic128x128_64_alphas", lambda: config_c(128, 3, args.refine)),
                          ("D_exact_formulation", lambda: exact_mode_rate(cases, 5, args.refine)),
-                         ("E_served_mixed_stream", lambda: config_e((16.0,), 30))):
+                         ("E_served_mixed_stream", lambda: config_e((16.0,), 30)),
+                         ("E_uvlm_step_paths", lambda: uvlm_step_paths(50))):
             t0 = time.perf_counter()
             try:
                 with ClockSampler(local) as cclk:
@@ -848,10 +849,50 @@ def config_e(rates=(2.0, 8.0, 32.0), requests=45, seed=SEED):
     return out
 
 
+def uvlm_step_paths(n=50):
+    """One served UVLM step on the resident 20 x 80 wing with a 500-row (40,000-ring) wake, three ways:
+    host-launched operators (gbvlm_uvlm_step), one graph launch (gbvlm_uvlm_step_graph) and the
+    device-resident request loop (gbvlm_uvlm_loop_*), each with its coefficients read back; per-step
+    latency p50/p99 over n steps each, and the loop's throughput with n requests in flight."""
+    import ctypes
+    from tinyvlm_gb300 import serve as S
+    from tinyvlm_gb300._lib import P, call
+    sim = S.resident_uvlm(warm_steps=500, capacity=5 * n + 8)
+    i, cl, cm = ctypes.c_int64(), ctypes.c_double(), (ctypes.c_double * 3)()
+
+    def lat(fn):
+        out = []
+        for _ in range(n):
+            t0 = time.perf_counter()
+            fn()
+            out.append((time.perf_counter() - t0) * 1000.0)
+        return {"p50_ms": float(np.percentile(out, 50)), "p99_ms": float(np.percentile(out, 99))}
+
+    res = {"workload": "UVLM step on the resident 20x80 wing, wake of 500+ rows (40,000+ rings)"}
+    res["host_launched"] = lat(lambda: call("gbvlm_uvlm_step", sim.h, ctypes.cast(ctypes.pointer(i), P),
+                                            ctypes.cast(ctypes.pointer(cl), P), ctypes.cast(cm, P), None))
+    res["graph"] = lat(lambda: call("gbvlm_uvlm_step_graph", sim.h, ctypes.cast(ctypes.pointer(i), P),
+                                    ctypes.cast(ctypes.pointer(cl), P), ctypes.cast(cm, P), None))
+    loop = S.UvlmLoop(sim, 0.05)
+    try:
+        res["device_loop"] = lat(lambda: loop.wait(loop.submit(), 60.0))
+        t0 = time.perf_counter()
+        tickets = [loop.submit() for _ in range(n)]
+        for t in tickets:
+            loop.wait(t, 60.0)
+        dt = time.perf_counter() - t0
+        res["device_loop_pipelined"] = {"steps": n, "steps_per_s": n / dt}
+        res["device_loop_stats"] = loop.stats()
+    finally:
+        loop.close()
+    return res
+
+
 def run_served(args):
     from tinyvlm_gb300 import device as D
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         out = config_e([float(x) for x in args.rates.split(",")], args.requests)
+        out["uvlm_step_paths"] = uvlm_step_paths(50)
         D.synchronize()
     out["clocks"] = clk.summary()
     print(json.dumps(out))
