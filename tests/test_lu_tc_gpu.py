@@ -1,7 +1,9 @@
 """Float LU of the library against LAPACK's float LU (sgetrf/sgetrs) on the
 same matrices: the tensor-core trailing update (3xTF32, the default) must keep
 the solution error at the level of a plain fp32 factorisation; the CUDA-core
-path (GBVLM_LU_TC=0) likewise; plain TF32 (GBVLM_LU_TC=1) only to TF32
+path (GBVLM_LU_TC=0) likewise, and so must U12 = L11^-1 A12 formed as an
+explicit inverse and a tensor-core product (the default) or by the
+triangular solve (GBVLM_TC_TRSM=0); plain TF32 (GBVLM_LU_TC=1) only to TF32
 accuracy.  Sizes cover one and several 128-column outer blocks, ragged
 edges, panels split over a thread-block cluster, and a system taller than
 4096 rows."""
@@ -17,9 +19,11 @@ from tinyvlm_gb300 import backend as B
 pytestmark = pytest.mark.gpu
 
 
-def _solve(A, b, mode):
+def _solve(A, b, mode, trsm="1"):
     old = os.environ.get("GBVLM_LU_TC")
+    old_t = os.environ.get("GBVLM_TC_TRSM")
     os.environ["GBVLM_LU_TC"] = mode
+    os.environ["GBVLM_TC_TRSM"] = trsm
     try:
         be = B.Backend(torch.float32)
         At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()  # column-major storage
@@ -31,10 +35,11 @@ def _solve(A, b, mode):
         torch.cuda.synchronize()
         return X.cpu().numpy().astype(np.float64)
     finally:
-        if old is None:
-            del os.environ["GBVLM_LU_TC"]
-        else:
-            os.environ["GBVLM_LU_TC"] = old
+        for k, v in (("GBVLM_LU_TC", old), ("GBVLM_TC_TRSM", old_t)):
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
 
 
 def _matrix(n, seed, boost):
@@ -59,10 +64,12 @@ def test_lu_float_accuracy(cuda, n, boost):
     A, b = _matrix(n, 1000 + n, boost)
     x_true = np.linalg.solve(A.astype(np.float64), b.T.astype(np.float64)).T
     ref = _lapack_err(A, b, x_true)
-    for mode in ("3", "0"):
-        x = _solve(A, b, mode)
+    # tensor-core update with U12 through the explicit inverse of L11 (the
+    # default) and through the triangular solve, and the CUDA-core path
+    for mode, trsm in (("3", "1"), ("3", "0"), ("0", "1")):
+        x = _solve(A, b, mode, trsm)
         err = np.abs(x - x_true).max() / np.abs(x_true).max()
-        assert err <= 8.0 * ref + 1e-6, (mode, n, err, ref)
+        assert err <= 8.0 * ref + 1e-6, (mode, trsm, n, err, ref)
 
 
 @pytest.mark.parametrize("n", [300, 1100])

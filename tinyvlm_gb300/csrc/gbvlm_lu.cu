@@ -550,30 +550,49 @@ constexpr int TW_XS = TW_COLS + 1;   // X row stride (odd: conflict-free columns
 template <int WW>
 constexpr size_t trsm_wide_smem() { return sizeof(float) * ((size_t)WW * TW_LS + (size_t)WW * TW_XS); }
 
-template <int WW>
+// U12 through the explicit inverse when a step has at least this many
+// systems (GBVLM_TC_TRSM=1: always; =0: never): it stages each L11 once
+// instead of once per 64 columns, which saves SM time in a batch (config D:
+// 249,600 -> 256,300 solves/s); for one large system the two dependent
+// launches add latency to the critical path (config C: 88.8 -> 90.3 ms), so
+// the triangular solve stays
+constexpr int TC_TRSM_MIN_SYSTEMS = 2;
+
+// INV: the same solve on the identity, two CTAs per system (64 columns
+// each): writes M = I - L11^-1 (strictly lower, column-major, ld WW) to
+// minv + (sid - base) * WW * WW, for U12 = A12 - M A12 on the tensor cores
+template <int WW, bool INV = false>
 __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t k0, const int32_t* act,
-                                                     const int64_t* pfx, int cnt) {
+                                                     const int64_t* pfx, int cnt, float* minv, int32_t base) {
     static_assert(WW == LU_OUTER, "row stride sized for the outer block");
     static_assert(TW_COLS == 8 * 8, "eight warps of eight columns");
     extern __shared__ __align__(16) float tw_smem[];
     float* L = tw_smem;            // L[r * TW_LS + c]
     float* X = L + WW * TW_LS;     // X[r * TW_XS + j]
-    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int a = INV ? (int)(blockIdx.x >> 1) : find_block(pfx, cnt, blockIdx.x);
     const int32_t sid = act[a];
     const int64_t n = B.n[sid], ld = B.ld[sid];
     float* A = B.A[sid];
-    const int64_t c0 = k0 + WW + (int64_t)(blockIdx.x - pfx[a]) * TW_COLS;  // systems here have n > k0 + WW
-    const int ncols = (int)min((int64_t)TW_COLS, n - c0);
+    // columns of A12 (systems here have n > k0 + WW), or of the identity
+    const int64_t c0 = INV ? (int64_t)(blockIdx.x & 1) * TW_COLS : k0 + WW + (int64_t)(blockIdx.x - pfx[a]) * TW_COLS;
+    const int ncols = INV ? TW_COLS : (int)min((int64_t)TW_COLS, n - c0);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const float* Ab = A + k0 + k0 * ld;
     staged_copy<16>(
         WW * WW, tid, 256, [&](int64_t e) { return Ab[(int)(e & (WW - 1)) + (e >> 7) * ld]; },
         [&](int64_t e, float v) { L[(int)(e & (WW - 1)) * TW_LS + (int)(e >> 7)] = v; });
-    const float* Xb = A + k0 + c0 * ld;
-    staged_copy<16>(
-        WW * TW_COLS, tid, 256,
-        [&](int64_t e) { return (int)(e >> 7) < ncols ? Xb[(int)(e & (WW - 1)) + (e >> 7) * ld] : 0.f; },
-        [&](int64_t e, float v) { X[(int)(e & (WW - 1)) * TW_XS + (int)(e >> 7)] = v; });
+    if constexpr (INV) {
+        for (int e = tid; e < WW * TW_COLS; e += 256) {
+            const int r = e & (WW - 1), j = e >> 7;
+            X[r * TW_XS + j] = (r == (int)c0 + j) ? 1.f : 0.f;
+        }
+    } else {
+        const float* Xb = A + k0 + c0 * ld;
+        staged_copy<16>(
+            WW * TW_COLS, tid, 256,
+            [&](int64_t e) { return (int)(e >> 7) < ncols ? Xb[(int)(e & (WW - 1)) + (e >> 7) * ld] : 0.f; },
+            [&](int64_t e, float v) { X[(int)(e & (WW - 1)) * TW_XS + (int)(e >> 7)] = v; });
+    }
     __syncthreads();
 #pragma unroll 1
     for (int b = 0; b < WW / 32; b++) {
@@ -620,11 +639,41 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
         }
         __syncthreads();
     }
-    float* Xo = A + k0 + c0 * ld;
-    for (int e = tid; e < WW * TW_COLS; e += 256) {
-        const int r = e & (WW - 1), j = e >> 7;
-        if (j < ncols) Xo[r + (int64_t)j * ld] = X[r * TW_XS + j];
+    if constexpr (INV) {
+        float* Mo = minv + (int64_t)(sid - base) * WW * WW + c0 * WW;
+        for (int e = tid; e < WW * TW_COLS; e += 256) {
+            const int r = e & (WW - 1), j = e >> 7;
+            Mo[r + j * WW] = r > (int)c0 + j ? -X[r * TW_XS + j] : 0.f;
+        }
+    } else {
+        float* Xo = A + k0 + c0 * ld;
+        for (int e = tid; e < WW * TW_COLS; e += 256) {
+            const int r = e & (WW - 1), j = e >> 7;
+            if (j < ncols) Xo[r + (int64_t)j * ld] = X[r * TW_XS + j];
+        }
     }
+}
+
+// U12 = L11^-1 A12 = A12 - M A12 (M = I - L11^-1 from k_trsm_wide<.., true>)
+// in place, on the tensor cores: one 128-row tile of TBN columns of A12 per
+// CTA.  The tile's operand chunks are all read before its epilogue writes,
+// and tiles own disjoint columns.
+template <int PASSES, int TBN>
+__global__ void __launch_bounds__(tc::THREADS, 2) k_trsm_tc12(LuBatch<float> B, int64_t k0, const int32_t* act,
+                                                              const int64_t* pfx, int cnt, const float* minv,
+                                                              int32_t base, int* err) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tslot;
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    float* A = B.A[sid];
+    const int64_t c0 = k0 + LU_OUTER + (int64_t)(blockIdx.x - pfx[a]) * TBN;
+    const float* M = minv + (int64_t)(sid - base) * LU_OUTER * LU_OUTER;
+    float* X = A + k0 + c0 * ld;
+    tc::update_tile<PASSES, false, TBN>(M, LU_OUTER, X, ld, X, ld, LU_OUTER, (int)min((int64_t)TBN, n - c0), LU_OUTER,
+                                        tc_smem, bar, &tslot, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1772,9 +1821,33 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
         }
         if constexpr (sizeof(T) == 4) {
             if (S.tc_blocks > 0) {
-                k_trsm_wide<LU_OUTER><<<(unsigned)S.btrsm_blocks, 256, trsm_wide_smem<LU_OUTER>(), st>>>(
-                    B, k0, act, plan.d_pfx + S.btrsm_pfx, S.n_tc);
-                GB_LAUNCH_CHECK();
+                if (plan.tc_trsm && S.n_tc >= plan.tc_trsm_min) {
+                    k_trsm_wide<LU_OUTER, true><<<(unsigned)(2 * S.n_tc), 256, trsm_wide_smem<LU_OUTER>(), st>>>(
+                        B, k0, act, nullptr, S.n_tc, plan.d_minv, plan.base);
+                    GB_LAUNCH_CHECK();
+                    const int64_t* tp = plan.d_pfx + S.tcs_pfx;
+                    if (plan.tc_wide) {
+                        constexpr int SM_ = tc::smem_bytes<tc::BN_WIDE>();
+                        if (plan.tc_passes == 1)
+                            k_trsm_tc12<1, tc::BN_WIDE><<<(unsigned)S.tcs_blocks, tc::THREADS, SM_, st>>>(
+                                B, k0, act, tp, S.n_tc, plan.d_minv, plan.base, plan.d_err);
+                        else
+                            k_trsm_tc12<3, tc::BN_WIDE><<<(unsigned)S.tcs_blocks, tc::THREADS, SM_, st>>>(
+                                B, k0, act, tp, S.n_tc, plan.d_minv, plan.base, plan.d_err);
+                    } else {
+                        if (plan.tc_passes == 1)
+                            k_trsm_tc12<1, tc::BN><<<(unsigned)S.tcs_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(
+                                B, k0, act, tp, S.n_tc, plan.d_minv, plan.base, plan.d_err);
+                        else
+                            k_trsm_tc12<3, tc::BN><<<(unsigned)S.tcs_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(
+                                B, k0, act, tp, S.n_tc, plan.d_minv, plan.base, plan.d_err);
+                    }
+                    GB_LAUNCH_CHECK();
+                } else {
+                    k_trsm_wide<LU_OUTER><<<(unsigned)S.btrsm_blocks, 256, trsm_wide_smem<LU_OUTER>(), st>>>(
+                        B, k0, act, plan.d_pfx + S.btrsm_pfx, S.n_tc, nullptr, 0);
+                    GB_LAUNCH_CHECK();
+                }
                 if (plan.tc_events) {
                     cudaEvent_t e0, e1;
                     GB_CUDA(cudaEventCreate(&e0));
@@ -1895,6 +1968,9 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         {
             const char* e = getenv("GBVLM_TC_WIDE");
             plan.tc_wide = plan.tc_passes && !tc_persistent() && !(e && e[0] == '0');
+            const char* t = getenv("GBVLM_TC_TRSM");
+            plan.tc_trsm = plan.tc_passes && !(t && t[0] == '0');
+            plan.tc_trsm_min = (t && t[0] == '1') ? 1 : TC_TRSM_MIN_SYSTEMS;
         }
         if (plan.tc_passes) {
             GB_CUDA(cudaFuncSetAttribute(k_update_tc<1, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1904,6 +1980,16 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             GB_CUDA(cudaFuncSetAttribute(k_update_tc<1, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::smem_bytes<tc::BN_WIDE>()));
             GB_CUDA(cudaFuncSetAttribute(k_update_tc<3, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::smem_bytes<tc::BN_WIDE>()));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trsm_wide_smem<LU_OUTER>()));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<1, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<3, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<1, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::smem_bytes<tc::BN_WIDE>()));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<3, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::smem_bytes<tc::BN_WIDE>()));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsm_wide_smem<LU_OUTER>()));
@@ -2126,8 +2212,18 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         }
         pfx.push_back(acc);
         S.tcr_blocks = acc;
+        S.tcs_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < ci; i++) {
+            pfx.push_back(acc);
+            acc += cdiv(n_sorted[i] - S.kend, cw);
+        }
+        pfx.push_back(acc);
+        S.tcs_blocks = acc;
         plan.steps.push_back(S);
     }
+    if (plan.tc_trsm && plan.nsys > 0)
+        GB_CUDA(dev_alloc((void**)&plan.d_minv, sizeof(float) * LU_OUTER * LU_OUTER * (size_t)plan.nsys, plan.mem));
     if (!act.empty()) {
         GB_CUDA(dev_alloc((void**)&plan.d_act, act.size() * sizeof(int32_t), plan.mem));
         GB_CUDA(cudaMemcpyAsync(plan.d_act, act.data(), act.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
@@ -2163,7 +2259,8 @@ int64_t lu_plan_launches(const LuPlan& plan, int es) {
             n += (S.swap_total > 0) + (S.trsm_blocks > 0) + (S.upd_blocks > 0);
         } else {
             n += (S.ik_blocks > 0) + (S.in_blocks > 0) + (S.bswap_total > 0) +
-                 2 * (S.tc_blocks > 0) + (S.tc_blocks > 0 && plan.la_stream && S.tcr_blocks > 0);
+                 (2 + (plan.tc_trsm && S.n_tc >= plan.tc_trsm_min)) * (S.tc_blocks > 0) +
+                 (S.tc_blocks > 0 && plan.la_stream && S.tcr_blocks > 0);
         }
     }
     return n + (plan.nsys > 0);  // + the permutation kernel
@@ -2267,6 +2364,8 @@ void TrsFlow::release() {
 }
 
 void LuPlan::release() {
+    dev_free(d_minv, mem);
+    d_minv = nullptr;
     dev_free(d_act, mem);
     dev_free(d_pfx, mem);
     dev_free(d_err, mem);

@@ -60,6 +60,7 @@ struct LuStep {
     int64_t tc_pfx = 0, tc_blocks = 0;        // outer update, 128 x 128 tensor-core tiles
     int64_t tcn_pfx = 0, tcn_blocks = 0;      // its first column of tiles (the next outer panel)
     int64_t tcr_pfx = 0, tcr_blocks = 0;      // its other columns of tiles (lookahead)
+    int64_t tcs_pfx = 0, tcs_blocks = 0;      // U12 on the tensor cores: tiles of 128 rows x the update's tile width
 };
 
 struct LuPlan {
@@ -71,6 +72,12 @@ struct LuPlan {
     int tc_passes = 0;  // float trailing update: 0 CUDA cores, 1 TF32, 3 3xTF32 tensor cores
     bool tc_wide = false;  // the update right of the next outer panel in 128 x 256 tiles (GBVLM_TC_WIDE=0: 128 x 128)
     cudaStream_t mem = nullptr;  // device memory stream-ordered on this stream (dev_alloc), or cudaMalloc
+    // U12 = L11^-1 A12 as an explicit inverse (one triangular solve on the
+    // identity per system and outer block) and a tensor-core tile product,
+    // instead of the triangular solve per 64 columns (GBVLM_TC_TRSM=0)
+    bool tc_trsm = false;
+    int32_t tc_trsm_min = 2;  // ... for steps with at least this many systems
+    float* d_minv = nullptr;  // nsys x 128 x 128: I - L11^-1 of each system's current outer block
     int W = LU_NB;      // outer block width of the float factorisation
     int32_t* d_act = nullptr;
     int64_t* d_pfx = nullptr;
