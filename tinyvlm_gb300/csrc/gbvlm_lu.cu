@@ -550,13 +550,14 @@ constexpr int TW_XS = TW_COLS + 1;   // X row stride (odd: conflict-free columns
 template <int WW>
 constexpr size_t trsm_wide_smem() { return sizeof(float) * ((size_t)WW * TW_LS + (size_t)WW * TW_XS); }
 
-// U12 through the explicit inverse when a step has at least this many
-// systems (GBVLM_TC_TRSM=1: always; =0: never): it stages each L11 once
-// instead of once per 64 columns, which saves SM time in a batch (config D:
-// 249,600 -> 256,300 solves/s); for one large system the two dependent
-// launches add latency to the critical path (config C: 88.8 -> 90.3 ms), so
-// the triangular solve stays
-constexpr int TC_TRSM_MIN_SYSTEMS = 2;
+// U12 through the explicit inverse for every system (GBVLM_TC_TRSM=0: the
+// triangular solve).  It stages each L11 once instead of once per 64 columns,
+// which saves SM time in a batch (config D: 249,600 -> 256,300 solves/s);
+// for one large system its two dependent launches add latency to the
+// critical path (config C: 88.8 -> 90.3 ms).  The choice does not depend on
+// what else is in the batch, so a system's factors are the same alone and in
+// any batch.
+constexpr int TC_TRSM_MIN_SYSTEMS = 1;
 
 // INV: the same solve on the identity, two CTAs per system (64 columns
 // each): writes M = I - L11^-1 (strictly lower, column-major, ld WW) to
@@ -1970,7 +1971,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             plan.tc_wide = plan.tc_passes && !tc_persistent() && !(e && e[0] == '0');
             const char* t = getenv("GBVLM_TC_TRSM");
             plan.tc_trsm = plan.tc_passes && !(t && t[0] == '0');
-            plan.tc_trsm_min = (t && t[0] == '1') ? 1 : TC_TRSM_MIN_SYSTEMS;
+            plan.tc_trsm_min = TC_TRSM_MIN_SYSTEMS;
         }
         if (plan.tc_passes) {
             GB_CUDA(cudaFuncSetAttribute(k_update_tc<1, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -76,7 +76,7 @@ struct LuPlan {
     // identity per system and outer block) and a tensor-core tile product,
     // instead of the triangular solve per 64 columns (GBVLM_TC_TRSM=0)
     bool tc_trsm = false;
-    int32_t tc_trsm_min = 2;  // ... for steps with at least this many systems
+    int32_t tc_trsm_min = 1;  // ... for steps with at least this many systems
     float* d_minv = nullptr;  // nsys x 128 x 128: I - L11^-1 of each system's current outer block
     int W = LU_NB;      // outer block width of the float factorisation
     int32_t* d_act = nullptr;

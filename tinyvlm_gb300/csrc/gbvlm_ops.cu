@@ -396,8 +396,11 @@ __global__ void __launch_bounds__(WK_THREADS) k_wake_influence(WakeArgs<T> w) {
                 total_rows += c_;
             }
     }
-    const int64_t R0 = (int64_t)blockIdx.y * w.rows_per_slice;
-    const int64_t R1 = min(R0 + w.rows_per_slice, total_rows);
+    // the device-iteration form spreads the current rows over all its slices
+    // (its grid is sized for the largest row count, at capture)
+    const int64_t rps = w.it_dev ? max((total_rows + gridDim.y - 1) / gridDim.y, (int64_t)WK_ROWS) : w.rows_per_slice;
+    const int64_t R0 = (int64_t)blockIdx.y * rps;
+    const int64_t R1 = min(R0 + rps, total_rows);
     T acc = 0;
     int64_t base = 0;
     for (int m = 0; m < w.s.n && base < R1; m++) {
