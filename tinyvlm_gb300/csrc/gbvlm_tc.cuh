@@ -181,7 +181,7 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     static_assert(TBN == 128 || TBN == 256, "tile width");
     constexpr int SB = stage_bytes<TBN>();
     constexpr int BCHUNK = TBN * BK * 4;
-    constexpr int BW = TBN / 8;        // B columns per warp in the operand loads
+    constexpr int BP = TBN / 32;       // B loads per thread: (column, 4 consecutive K) pairs
     constexpr int EQ = TBN / 64;       // 32-column accumulator groups per thread in the epilogue
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const uint32_t raw = smem_u32(smem_raw);
@@ -205,18 +205,25 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     // operand chunks pass through registers: chunk c + 1 is loaded from global
     // memory while the MMAs of chunk c run (one shared-memory stage)
     const int arow = tid & (BM - 1), akh = (tid >> 7) * 16;
-    float va[16], vb[BW];
+    // B: pair j of this thread is column (tid + 256 j) / 8 and K values
+    // 4 ((tid + 256 j) % 8) .. +3, consecutive in memory (U is K-contiguous):
+    // a warp reads four columns' 128-byte runs, and each pair lands in the
+    // swizzled tile as one 16-byte store
+    const int bk = 4 * (tid & 7), bc = tid >> 3;
+    float va[16], vb[BP][4];
     auto load_chunk = [&](int c) {
         const int kc = c * BK;
         const bool rv = arow < m_rows;  // A: thread = tile row, 16 K values of its half
 #pragma unroll
         for (int kk = 0; kk < 16; kk++)
             va[kk] = (rv && kc + akh + kk < K) ? Lp[arow + (int64_t)(kc + akh + kk) * ldl] : 0.f;
-        const bool kv = kc + lane < K;  // B: warp w, tile columns BW*w..BW*w+BW-1, lane = K index
 #pragma unroll
-        for (int cc = 0; cc < BW; cc++) {
-            const int col = BW * wid + cc;
-            vb[cc] = (kv && col < n_cols) ? Up[(kc + lane) + (int64_t)col * ldu] : 0.f;
+        for (int j = 0; j < BP; j++) {
+            const int col = bc + 32 * j;
+            const bool cv = col < n_cols;
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                vb[j][e] = (cv && kc + bk + e < K) ? Up[(kc + bk + e) + (int64_t)col * ldu] : 0.f;
         }
     };
     if (nchunks > 0) load_chunk(0);
@@ -238,11 +245,13 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
                                  va[4 * j + 3] - h3);
             }
 #pragma unroll
-            for (int cc = 0; cc < BW; cc++) {
-                const uint32_t off = sw128_off(BW * wid + cc, lane);
-                const float h = tf32_hi(vb[cc]);
-                st_shared_f32(b_hi + off, h);
-                if (PASSES > 1) st_shared_f32(b_lo + off, vb[cc] - h);
+            for (int j = 0; j < BP; j++) {
+                const uint32_t off = sw128_off(bc + 32 * j, bk);
+                const float h0 = tf32_hi(vb[j][0]), h1 = tf32_hi(vb[j][1]);
+                const float h2 = tf32_hi(vb[j][2]), h3 = tf32_hi(vb[j][3]);
+                st_shared_v4(b_hi + off, h0, h1, h2, h3);
+                if (PASSES > 1)
+                    st_shared_v4(b_lo + off, vb[j][0] - h0, vb[j][1] - h1, vb[j][2] - h2, vb[j][3] - h3);
             }
             if (c + 1 < nchunks) load_chunk(c + 1);
         }
