@@ -159,6 +159,10 @@ __device__ __forceinline__ float tf32_hi(float x) {
     return __uint_as_float(r);
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
     asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
 }
@@ -186,18 +190,13 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
-    if (wid == 0) {
-        tmem_alloc(tslot, TBN);
-        tmem_relinquish();
+    // the tile's C lines into L2 while the K loop runs, so the epilogue's
+    // reads of C hit L2: the first and last row of each 32-row run of each
+    // column (a run may straddle two 128-byte lines)
+    for (int e = tid; e < TBN * 8; e += THREADS) {
+        const int col = e >> 3, row = 32 * ((e >> 1) & 3) + 31 * (e & 1);
+        if (col < n_cols && row < m_rows) prefetch_l2(Cp + row + (int64_t)col * ldc);
     }
-    if (tid == 0) {
-        for (int i = 0; i < STAGES; i++) mbar_init(&bar[i], 1);
-        fence_mbar_init();
-    }
-    fence_before_sync();
-    __syncthreads();
-    fence_after_sync();
-    const uint32_t tmem = *tslot;
     constexpr uint32_t idesc = idesc_tf32(BM, TBN);
     const int nchunks = (K + BK - 1) / BK;
     bool ok = true;
@@ -226,7 +225,20 @@ __device__ __forceinline__ void update_tile(const float* Lp, int64_t ldl, const 
                 vb[j][e] = (cv && kc + bk + e < K) ? Up[(kc + bk + e) + (int64_t)col * ldu] : 0.f;
         }
     };
+    // the first chunk's loads in flight while tensor memory and the barrier are set up
     if (nchunks > 0) load_chunk(0);
+    if (wid == 0) {
+        tmem_alloc(tslot, TBN);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < STAGES; i++) mbar_init(&bar[i], 1);
+        fence_mbar_init();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tslot;
     for (int c = 0; c < nchunks; c++) {
         const int s = c % STAGES;
         // stage s is free once the MMAs of chunk c - STAGES are done
