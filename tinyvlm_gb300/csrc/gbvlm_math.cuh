@@ -101,11 +101,17 @@ template <class T> __device__ __forceinline__ T fast_div(T a, T b);
 template <> __device__ __forceinline__ float fast_div<float>(float a, float b) { return __fdividef(a, b); }
 template <> __device__ __forceinline__ double fast_div<double>(double a, double b) { return a / b; }
 
+// a + b where the two cannot cancel (both non-negative, or the result is
+// only used when they are): plain addition; the float pair skips its
+// renormalisation (its value stays in v without it)
+template <class T> __device__ __forceinline__ T add_nc(T a, T b) { return a + b; }
+template <class T> __device__ __forceinline__ T sub_nc(T a, T b) { return a - b; }
+
 template <class T>
 __device__ __forceinline__ Rel<T> make_rel(T x, T y, T z) {
     Rel<T> r;
     r.x = x; r.y = y; r.z = z;
-    r.n = fast_len<T>(x * x + y * y + z * z);
+    r.n = fast_len<T>(add_nc(add_nc(x * x, y * y), z * z));
     return r;
 }
 
@@ -120,15 +126,16 @@ __device__ __forceinline__ T seg_coeff(const Rel<T>& a, const Rel<T>& b, T r0x, 
     cx = r0y * a.z - r0z * a.y;
     cy = r0z * a.x - r0x * a.z;
     cz = r0x * a.y - r0y * a.x;
-    const T sq = cx * cx + cy * cy + cz * cz;
+    const T sq = add_nc(add_nc(cx * cx, cy * cy), cz * cz);
     const T ab = a.x * b.x + a.y * b.y + a.z * b.z;
     const T nab = a.n * b.n;
-    const T sum = a.n + b.n;
+    const T sum = add_nc(a.n, b.n);
     constexpr T rcut = DCUT ? (T)RCUT_NORM_D : Prec<T>::rcut_norm;
     const bool cut = (sq < (T)RCUT_SQ) | (a.n < rcut) | (b.n < rcut);
     const bool pos = ab >= (T)0;
-    T num = pos ? sum : sum * (nab - ab);
-    T den = pos ? nab * (nab + ab) : nab * sq;
+    // |ab| <= nab: nab - ab cannot cancel when it is used (ab < 0), nor nab + ab (ab >= 0)
+    T num = pos ? sum : sum * sub_nc(nab, ab);
+    T den = pos ? nab * add_nc(nab, ab) : nab * sq;
     if (SIGMA) {
         // reference core smoothing: sq -> sqrt(sq^2 + (sigma^2 |r0|^2)^2)
         const T sm = sigma2 * (r0x * r0x + r0y * r0y + r0z * r0z);
@@ -205,6 +212,13 @@ __device__ __forceinline__ Fe operator+(Fe a, Fe b) {
     return fe_fast2sum(s, __fadd_rn(err, __fadd_rn(a.e, b.e)));
 }
 __device__ __forceinline__ Fe operator-(Fe a) { return Fe(-a.v, -a.e); }
+template <> __device__ __forceinline__ Fe add_nc<Fe>(Fe a, Fe b) {
+    const float s = __fadd_rn(a.v, b.v);
+    const float bb = __fsub_rn(s, a.v);
+    const float err = __fadd_rn(__fsub_rn(a.v, __fsub_rn(s, bb)), __fsub_rn(b.v, bb));
+    return Fe(s, __fadd_rn(err, __fadd_rn(a.e, b.e)));
+}
+template <> __device__ __forceinline__ Fe sub_nc<Fe>(Fe a, Fe b) { return add_nc<Fe>(a, Fe(-b.v, -b.e)); }
 __device__ __forceinline__ Fe operator-(Fe a, Fe b) { return a + (-b); }
 __device__ __forceinline__ Fe operator*(Fe a, Fe b) {
     const float p = __fmul_rn(a.v, b.v);
