@@ -655,6 +655,29 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
     }
 }
 
+// The inner update of the two-level factorisation on the tensor cores: after
+// the 32-column panel [k, k + 32) of the outer block [.., kend), rows and
+// columns [k + 32, min(n, kend)) -= L21 U12 with K = 32, one 128-row tile of
+// at most 96 columns per CTA (the CUDA-core k_update in mode 1 does the same
+// in 64 x 64 tiles)
+template <int PASSES>
+__global__ void __launch_bounds__(tc::THREADS, 2) k_inner_tc(LuBatch<float> B, int64_t k, int64_t kend,
+                                                             const int32_t* act, const int64_t* pfx, int cnt,
+                                                             int* err) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tslot;
+    const int a = find_block(pfx, cnt, blockIdx.x);
+    const int32_t sid = act[a];
+    const int64_t n = B.n[sid], ld = B.ld[sid];
+    float* A = B.A[sid];
+    const int64_t lo = k + GK, ke = min(n, kend);
+    const int64_t r0 = lo + (int64_t)(blockIdx.x - pfx[a]) * tc::BM;
+    tc::update_tile<PASSES, false, tc::BN>(A + r0 + k * ld, ld, A + k + lo * ld, ld, A + r0 + lo * ld, ld,
+                                           (int)min((int64_t)tc::BM, n - r0), (int)(ke - lo), GK, tc_smem, bar,
+                                           &tslot, err);
+}
+
 // U12 = L11^-1 A12 = A12 - M A12 (M = I - L11^-1 from k_trsm_wide<.., true>)
 // in place, on the tensor cores: one 128-row tile of TBN columns of A12 per
 // CTA.  The tile's operand chunks are all read before its epilogue writes,
@@ -1802,7 +1825,15 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
                                                                       S.n_panel);
                 GB_LAUNCH_CHECK();
             }
-            if (S.in_blocks > 0) {
+            if (S.in_blocks > 0 && plan.tc_inner) {
+                if (plan.tc_passes == 1)
+                    k_inner_tc<1><<<(unsigned)S.inc_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(
+                        B, S.k, S.kend, act, plan.d_pfx + S.inc_pfx, S.n_in, plan.d_err);
+                else
+                    k_inner_tc<3><<<(unsigned)S.inc_blocks, tc::THREADS, tc::SMEM_BYTES, st>>>(
+                        B, S.k, S.kend, act, plan.d_pfx + S.inc_pfx, S.n_in, plan.d_err);
+                GB_LAUNCH_CHECK();
+            } else if (S.in_blocks > 0) {
                 k_update<T><<<(unsigned)S.in_blocks, 256, 0, st>>>(B, S.k, act, plan.d_pfx + S.in_pfx, S.n_in, S.kend, 1);
                 GB_LAUNCH_CHECK();
             }
@@ -1969,6 +2000,8 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         {
             const char* e = getenv("GBVLM_TC_WIDE");
             plan.tc_wide = plan.tc_passes && !tc_persistent() && !(e && e[0] == '0');
+            const char* ti = getenv("GBVLM_TC_INNER");
+            plan.tc_inner = plan.tc_passes && !(ti && ti[0] == '0');
             const char* t = getenv("GBVLM_TC_TRSM");
             plan.tc_trsm = plan.tc_passes && !(t && t[0] == '0');
             plan.tc_trsm_min = TC_TRSM_MIN_SYSTEMS;
@@ -1982,6 +2015,8 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
                                          tc::smem_bytes<tc::BN_WIDE>()));
             GB_CUDA(cudaFuncSetAttribute(k_update_tc<3, tc::BN_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::smem_bytes<tc::BN_WIDE>()));
+            GB_CUDA(cudaFuncSetAttribute(k_inner_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+            GB_CUDA(cudaFuncSetAttribute(k_inner_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsm_wide_smem<LU_OUTER>()));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<1, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2145,6 +2180,14 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         pfx.push_back(acc);
         S.n_in = ci;
         S.in_blocks = acc;
+        S.inc_pfx = (int64_t)pfx.size();
+        acc = 0;
+        for (int i = 0; i < ci; i++) {
+            pfx.push_back(acc);
+            acc += cdiv(n_sorted[i] - k - GK, tc::BM);
+        }
+        pfx.push_back(acc);
+        S.inc_blocks = acc;
         // k_inner: IN_COLS-column chunks of [k0, k) and [k + nb, min(n, kend))
         S.ik_pfx = (int64_t)pfx.size();
         acc = 0;

@@ -61,6 +61,7 @@ struct LuStep {
     int64_t tcn_pfx = 0, tcn_blocks = 0;      // its first column of tiles (the next outer panel)
     int64_t tcr_pfx = 0, tcr_blocks = 0;      // its other columns of tiles (lookahead)
     int64_t tcs_pfx = 0, tcs_blocks = 0;      // U12 on the tensor cores: tiles of 128 rows x the update's tile width
+    int64_t inc_pfx = 0, inc_blocks = 0;      // the inner update on the tensor cores: 128-row tiles
 };
 
 struct LuPlan {
@@ -75,6 +76,7 @@ struct LuPlan {
     // U12 = L11^-1 A12 as an explicit inverse (one triangular solve on the
     // identity per system and outer block) and a tensor-core tile product,
     // instead of the triangular solve per 64 columns (GBVLM_TC_TRSM=0)
+    bool tc_inner = false;  // inner updates in 128-row tensor-core tiles, K = 32 (GBVLM_TC_INNER=0: CUDA cores)
     bool tc_trsm = false;
     int32_t tc_trsm_min = 1;  // ... for steps with at least this many systems
     float* d_minv = nullptr;  // nsys x 128 x 128: I - L11^-1 of each system's current outer block
