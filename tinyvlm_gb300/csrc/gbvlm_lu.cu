@@ -595,8 +595,9 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
             [&](int64_t e, float v) { X[(int)(e & (WW - 1)) * TW_XS + (int)(e >> 7)] = v; });
     }
     __syncthreads();
+    // on the identity, rows above the CTA's first column stay zero: start there
 #pragma unroll 1
-    for (int b = 0; b < WW / 32; b++) {
+    for (int b = INV ? (int)(c0 / 32) : 0; b < WW / 32; b++) {
         const int rb = 32 * b;
         // diagonal block
         {
