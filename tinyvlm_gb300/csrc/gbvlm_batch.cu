@@ -349,14 +349,24 @@ __device__ __forceinline__ V3<double> freestream_d(double u, double al, double b
     return {u * cos(al) * cos(be), -(u * cos(al) * sin(be)), u * sin(al)};
 }
 
+// the system's free-stream vectors are formed once per block (double cos and
+// sin are long on this part's fp64 units), not once per panel
 __global__ void k_batch_rhs(BatchArgs a) {
+    __shared__ double sv[64][3];  // a system has at most 64 right-hand sides
     const SysDesc& S = a.sys[blockIdx.y];
+    if ((int64_t)blockIdx.x * blockDim.x >= S.n) return;  // uniform over the block
+    for (int q = threadIdx.x; q < S.nrhs; q += blockDim.x) {
+        const V3<double> V = freestream_d(a.u_inf, a.alphas[S.rhs_off + q], a.beta);
+        sv[q][0] = V.x;
+        sv[q][1] = V.y;
+        sv[q][2] = V.z;
+    }
+    __syncthreads();
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= S.n) return;
     const double nx = S.nrmd[p], ny = S.nrmd[S.n + p], nz = S.nrmd[2 * S.n + p];
     for (int q = 0; q < S.nrhs; q++) {
-        const V3<double> V = freestream_d(a.u_inf, a.alphas[S.rhs_off + q], a.beta);
-        const double b = -(V.x * nx + V.y * ny + V.z * nz);
+        const double b = -(sv[q][0] * nx + sv[q][1] * ny + sv[q][2] * nz);
         S.B[p + q * S.n] = b;
         S.X[p + q * S.n] = (float)b;
         S.Xd[p + q * S.n] = 0.0;
@@ -491,16 +501,6 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
 // idle; measured faster on 24-2048 panels), 256 once a system exceeds 4096
 constexpr int LD_THREADS_SMALL = 64, LD_THREADS_LARGE = 256;
 
-__device__ __forceinline__ V3<double> bs_d(V3<double> c, V3<double> a, V3<double> b) {
-    // double Biot-Savart (same law, reference cut-offs), unscaled by 1/4pi
-    V3<double> r1 = c - a, r2 = c - b, r0 = b - a;
-    V3<double> cr = cross(r1, r2);
-    double n1 = sqrt(len2(r1)), n2 = sqrt(len2(r2)), sq = len2(cr);
-    if (sq < 1e-10 || n1 < 1e-10 || n2 < 1e-10) return {0, 0, 0};
-    double k = (dot(r0, r1) * n2 - dot(r0, r2) * n1) / (sq * n1 * n2);
-    return k * cr;
-}
-
 // Trefftz influence matrix of one system: K[j, jj] = -(induced velocity of
 // the trailing legs of wake ring jj with unit gamma, plus mirror, at the
 // centre of wake ring j) . n_j * |dl_j| / (4 pi); CDi = gamma^T K gamma / (|V|^2 S)
@@ -519,9 +519,20 @@ __global__ void k_batch_trefftz_k(BatchArgs a) {
     nn = (1.0 / sqrt(len2(nn))) * nn;
     const V3<double> w0 = WP(jj), w1 = WP(jj + 1), w2 = WP((ns + 1) + jj + 1), w3 = WP((ns + 1) + jj);
     const V3<double> cm_{c.x, -c.y, c.z};
-    const V3<double> t = bs_d(c, w1, w2) + bs_d(c, w3, w0);
-    const V3<double> tm = bs_d(cm_, w1, w2) + bs_d(cm_, w3, w0);
-    const V3<double> sv{t.x + tm.x, t.y - tm.y, t.z + tm.z};
+    // ring jj's two streamwise segments at c and at its mirror image: relative
+    // vectors and segment vectors formed in double and rounded to float, the
+    // segment law in float (the fp64 units of this part are slow; K enters
+    // CDi through gamma^T K gamma, with no cancellation to amplify ~1e-7)
+    auto rel = [](V3<double> p, V3<double> q) {
+        return make_rel<float>((float)(p.x - q.x), (float)(p.y - q.y), (float)(p.z - q.z));
+    };
+    const V3<double> s12 = w2 - w1, s30 = w0 - w3;
+    auto seg = [&](V3<double> p, V3<double> a, V3<double> b, V3<double> r0) {
+        return seg_vec<float, false>(rel(p, a), rel(p, b), (float)r0.x, (float)r0.y, (float)r0.z, 0.f);
+    };
+    const V3<float> t = seg(c, w1, w2, s12) + seg(c, w3, w0, s30);
+    const V3<float> tm = seg(cm_, w1, w2, s12) + seg(cm_, w3, w0, s30);
+    const V3<double> sv{(double)t.x + tm.x, (double)t.y - tm.y, (double)t.z + tm.z};
     S.K[j + jj * ns] = -dot(sv, nn) / (4.0 * (double)PI_F) * sqrt(len2(q1 - q0));
 }
 
