@@ -106,9 +106,18 @@ __global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
     // (its solves come out non-finite; the other cases are unaffected)
     bad = __syncthreads_or(bad);
     if (threadIdx.x == 0) a.bad[blockIdx.x] = bad;
+    // the angle's double trigonometry once per block (long on the fp64 units)
+    __shared__ double s_trig[3];
+    if (threadIdx.x == 0) {
+        const double sa = sin(al);
+        s_trig[0] = 100.0 * a.u_inf * cos(al);
+        s_trig[1] = 100.0 * a.u_inf * sa;
+        s_trig[2] = (al < (double)EPS_F) ? 0.5 : 0.5 * (al / (sa + (double)EPS_F));
+    }
+    __syncthreads();
     // wake (vlm.cpp:104-114 seen from the displaced wing): row 0 = trailing
     // edge, row 1 = trailing edge + 100 u (cos a, 0, sin a)
-    const double dx = 100.0 * a.u_inf * cos(al), dz = 100.0 * a.u_inf * sin(al);
+    const double dx = s_trig[0], dz = s_trig[1];
     const int64_t wl = 2 * (ns + 1);
     for (int64_t i = threadIdx.x; i <= ns; i += blockDim.x) {
         const int64_t te = i + nc * (ns + 1);
@@ -122,7 +131,7 @@ __global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
         }
     }
     __syncthreads();
-    const double factor = (al < (double)EPS_F) ? 0.5 : 0.5 * (al / (sin(al) + (double)EPS_F));
+    const double factor = s_trig[2];
     const double* v = S.vd;
     for (int64_t p = threadIdx.x; p < np; p += blockDim.x) {
         const int64_t i = p % ns, j = p / ns;
@@ -157,32 +166,29 @@ struct HL {
 
 // Walk a strip of rings with double-float positions (top/bot: hi planes at
 // topH[k*BA_W], lo planes at topL[k*BA_W]); f(ring, 4*pi*(v.n + v'.n')).
+// seg[0][k]: the chordwise segment top(k) -> bot(k); seg[1][k], k >= 1: the
+// top segment top(k-1) -> top(k); seg[2][k], k >= 1: the bottom segment
+// bot(k) -> bot(k-1) (the tile's, formed once per block in shared memory)
 template <int BA_W, class F>
 __device__ __forceinline__ void strip_hl(const float* topH, const float* topL, const float* botH, const float* botL,
-                                         int nvs, HL px, HL py, HL pz, float nx, float ny, float nz, F&& f) {
+                                         const float4 (*seg)[BA_W], int nvs, HL px, HL py, HL pz, float nx, float ny,
+                                         float nz, F&& f) {
     auto rel = [&](const float* H, const float* L, int sl, bool mir) {
         const float y = mir ? df_sub(-py.h, -py.l, H[BA_W + sl], L[BA_W + sl]) : df_sub(py.h, py.l, H[BA_W + sl], L[BA_W + sl]);
         return make_rel<float>(df_sub(px.h, px.l, H[sl], L[sl]), y, df_sub(pz.h, pz.l, H[2 * BA_W + sl], L[2 * BA_W + sl]));
     };
-    auto sv = [&](const float* H1, const float* L1, int s1, const float* H0, const float* L0, int s0, float& x, float& y,
-                  float& z) {
-        x = df_sub(H1[s1], L1[s1], H0[s0], L0[s0]);
-        y = df_sub(H1[BA_W + s1], L1[BA_W + s1], H0[BA_W + s0], L0[BA_W + s0]);
-        z = df_sub(H1[2 * BA_W + s1], L1[2 * BA_W + s1], H0[2 * BA_W + s0], L0[2 * BA_W + s0]);
-    };
     Rel<float> A0 = rel(topH, topL, 0, false), A3 = rel(botH, botL, 0, false);
     Rel<float> B0 = rel(topH, topL, 0, true), B3 = rel(botH, botL, 0, true);
-    float lx, ly, lz;
-    sv(botH, botL, 0, topH, topL, 0, lx, ly, lz);
-    float Ca = seg_normal<float, false, true>(A0, A3, lx, ly, lz, nx, ny, nz, 0.f);
-    float Cb = seg_normal<float, false, true>(B0, B3, lx, ly, lz, nx, -ny, nz, 0.f);
+    const float4 l0 = seg[0][0];
+    float Ca = seg_normal<float, false, true>(A0, A3, l0.x, l0.y, l0.z, nx, ny, nz, 0.f);
+    float Cb = seg_normal<float, false, true>(B0, B3, l0.x, l0.y, l0.z, nx, -ny, nz, 0.f);
     for (int k = 1; k < nvs; k++) {
         const Rel<float> A1 = rel(topH, topL, k, false), A2 = rel(botH, botL, k, false);
         const Rel<float> B1 = rel(topH, topL, k, true), B2 = rel(botH, botL, k, true);
-        float cx, cy, cz, tx, ty, tz, bx, by, bz;
-        sv(botH, botL, k, topH, topL, k, cx, cy, cz);          // v1 -> v2
-        sv(topH, topL, k, topH, topL, k - 1, tx, ty, tz);      // v0 -> v1
-        sv(botH, botL, k - 1, botH, botL, k, bx, by, bz);      // v2 -> v3
+        const float4 c4 = seg[0][k], t4 = seg[1][k], b4 = seg[2][k];
+        const float cx = c4.x, cy = c4.y, cz = c4.z;  // v1 -> v2
+        const float tx = t4.x, ty = t4.y, tz = t4.z;  // v0 -> v1
+        const float bx = b4.x, by = b4.y, bz = b4.z;  // v2 -> v3
         const float Cra = seg_normal<float, false, true>(A1, A2, cx, cy, cz, nx, ny, nz, 0.f);
         const float Crb = seg_normal<float, false, true>(B1, B2, cx, cy, cz, nx, -ny, nz, 0.f);
         float val = seg_normal<float, false, true>(A0, A1, tx, ty, tz, nx, ny, nz, 0.f) + Cra +
@@ -209,6 +215,7 @@ template <int BA_SPAN>
 __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
     constexpr int BA_W = BA_SPAN + 1;
     __shared__ float sw[2][2][3 * BA_W];  // [row][hi/lo][plane*W + s]
+    __shared__ float4 sseg[3][BA_W];      // the strip's segment vectors (strip_hl)
     const int64_t tile = tile0 + blockIdx.x;
     const int si = find_sys(tpfx, a.nsys, tile);
     const SysDesc& S = a.sys[si];
@@ -228,6 +235,22 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
         sw[r][1][k * BA_W + sl] = S.vl[vi];
     }
     __syncthreads();
+    // segment vectors from the double-float positions, once per tile
+    for (int e = threadIdx.x; e < 3 * nvs; e += BA_THREADS) {
+        const int t = e / nvs, k = e - t * nvs;
+        // t = 0: top(k) -> bot(k); 1: top(k-1) -> top(k); 2: bot(k) -> bot(k-1)
+        const int r1 = t == 0 ? 1 : (t == 1 ? 0 : 1), k1 = t == 2 ? k - 1 : k;
+        const int r0 = t == 0 ? 0 : (t == 1 ? 0 : 1), k0 = t == 1 ? k - 1 : k;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (k1 >= 0 && k0 >= 0) {
+            v.x = df_sub(sw[r1][0][k1], sw[r1][1][k1], sw[r0][0][k0], sw[r0][1][k0]);
+            v.y = df_sub(sw[r1][0][BA_W + k1], sw[r1][1][BA_W + k1], sw[r0][0][BA_W + k0], sw[r0][1][BA_W + k0]);
+            v.z = df_sub(sw[r1][0][2 * BA_W + k1], sw[r1][1][2 * BA_W + k1], sw[r0][0][2 * BA_W + k0],
+                         sw[r0][1][2 * BA_W + k0]);
+        }
+        sseg[t][k] = v;
+    }
+    __syncthreads();
     const int64_t i = rb * BA_THREADS + threadIdx.x;
     if (i >= n) return;
     const HL px{S.ch[i], S.cl_[i]}, py{S.ch[n + i], S.cl_[n + i]}, pz{S.ch[2 * n + i], S.cl_[2 * n + i]};
@@ -237,7 +260,7 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
     float* colB = S.A2 ? S.A2 + i + (c * ns + s0) * n : nullptr;
     const bool te = (c == nc - 1);
     if (!te) {
-        strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz, [&](int kk, float v) {
+        strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], sseg, nvs, px, py, pz, nx, ny, nz, [&](int kk, float v) {
             const float val = v * k4;
             colA[(int64_t)kk * n] = val;
             if (colB) colB[(int64_t)kk * n] = val;
@@ -246,7 +269,7 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
     }
     // trailing-edge ring row: wing ring plus the wake ring behind it (Kutta
     // condition, vlm_backend_cpu.cpp:121-139 with iteration = 1)
-    strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], nvs, px, py, pz, nx, ny, nz,
+    strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], sseg, nvs, px, py, pz, nx, ny, nz,
                    [&](int kk, float v) { colA[(int64_t)kk * n] = v; });
     const int64_t wl = 2 * (ns + 1);
     for (int64_t s = s0; s < s1; s++) {
