@@ -337,6 +337,19 @@ __global__ void __launch_bounds__(BA_THREADS, 4) k_batch_assemble_lo(BatchArgs a
         sw[r][k * BA_W + sl] = Fe(S.vh[vi], S.vl[vi]);
     }
     __syncthreads();
+    // the strip's segment vectors once per tile (strip_normal's SEG layout)
+    __shared__ V3<Fe> sseg[3 * BA_W];
+    for (int e = threadIdx.x; e < 3 * nvs; e += BA_THREADS) {
+        const int t = e / nvs, k = e - t * nvs;
+        const int r1 = t == 1 ? 0 : 1, k1 = t == 2 ? k - 1 : k;
+        const int r0 = t == 2 ? 1 : 0, k0 = t == 1 ? k - 1 : k;
+        V3<Fe> v{Fe(0), Fe(0), Fe(0)};
+        if (k1 >= 0 && k0 >= 0)
+            v = V3<Fe>{sw[r1][k1] - sw[r0][k0], sw[r1][BA_W + k1] - sw[r0][BA_W + k0],
+                       sw[r1][2 * BA_W + k1] - sw[r0][2 * BA_W + k0]};
+        sseg[t * BA_W + k] = v;
+    }
+    __syncthreads();
     const int64_t i = rb * BA_THREADS + threadIdx.x;
     if (i >= n) return;
     const Fe px(S.ch[i], S.cl_[i]), py(S.ch[n + i], S.cl_[n + i]), pz(S.ch[2 * n + i], S.cl_[2 * n + i]);
@@ -346,7 +359,7 @@ __global__ void __launch_bounds__(BA_THREADS, 4) k_batch_assemble_lo(BatchArgs a
     float* colL = S.Alo + i + (c * ns + s0) * n;
     const bool te = (c == nc - 1);
     const int64_t wl = 2 * (ns + 1);
-    strip_normal<Fe, false, true>(sw[0], sw[1], BA_W, nvs, px, py, pz, nx, ny, nz, Fe(0), [&](int kk, Fe v) {
+    strip_normal<Fe, false, true, true>(sw[0], sw[1], BA_W, nvs, px, py, pz, nx, ny, nz, Fe(0), [&](int kk, Fe v) {
         if (te) {
             // the wake ring behind this trailing-edge ring (Kutta condition)
             const int64_t s = s0 + kk;
@@ -361,7 +374,7 @@ __global__ void __launch_bounds__(BA_THREADS, 4) k_batch_assemble_lo(BatchArgs a
         const Fe tot = v * k4;
         const float a2 = colB[(int64_t)kk * n];
         colL[(int64_t)kk * n] = __fadd_rn(__fsub_rn(tot.v, a2), tot.e);
-    });
+    }, sseg);
 }
 
 // ---------------------------------------------------------------------------

@@ -37,22 +37,30 @@ __device__ __forceinline__ T ring_normal_full(T px, T py, T pz, T nx, T ny, T nz
 // Walk the rings of one strip whose vertex lines sit in shared memory
 // (top/bot: 3 planes W apart), local vertices 0..nvs-1; calls
 // f(ring_index, 4*pi*(v.n + v_mirror.n_mirror)) for rings 0..nvs-2.
-template <class T, bool SIGMA, bool DCUT = false, class F>
+// SEG: the segment vectors come precomputed in seg[t * W + k] (shared by all
+// evaluation points of a tile): t = 0 the chordwise segment top(k) -> bot(k),
+// t = 1 the top segment top(k-1) -> top(k), t = 2 the bottom segment
+// bot(k) -> bot(k-1); otherwise each walk forms them.
+template <class T, bool SIGMA, bool DCUT = false, bool SEG = false, class F>
 __device__ __forceinline__ void strip_normal(const T* top, const T* bot, int W, int nvs, T px, T py, T pz, T nx, T ny,
-                                             T nz, T sg, F&& f) {
+                                             T nz, T sg, F&& f, const V3<T>* seg = nullptr) {
     auto V = [&](const T* line, int sl) { return V3<T>{line[sl], line[W + sl], line[2 * W + sl]}; };
     V3<T> v0 = V(top, 0), v3 = V(bot, 0);
     Rel<T> A0 = make_rel<T>(px - v0.x, py - v0.y, pz - v0.z), A3 = make_rel<T>(px - v3.x, py - v3.y, pz - v3.z);
     Rel<T> B0 = make_rel<T>(px - v0.x, -py - v0.y, pz - v0.z), B3 = make_rel<T>(px - v3.x, -py - v3.y, pz - v3.z);
-    T Ca = seg_normal<T, SIGMA, DCUT>(A0, A3, v3.x - v0.x, v3.y - v0.y, v3.z - v0.z, nx, ny, nz, sg);
-    T Cb = seg_normal<T, SIGMA, DCUT>(B0, B3, v3.x - v0.x, v3.y - v0.y, v3.z - v0.z, nx, -ny, nz, sg);
+    const V3<T> l0 = SEG ? seg[0] : V3<T>{v3.x - v0.x, v3.y - v0.y, v3.z - v0.z};
+    T Ca = seg_normal<T, SIGMA, DCUT>(A0, A3, l0.x, l0.y, l0.z, nx, ny, nz, sg);
+    T Cb = seg_normal<T, SIGMA, DCUT>(B0, B3, l0.x, l0.y, l0.z, nx, -ny, nz, sg);
     for (int k = 1; k < nvs; k++) {
         const V3<T> v1 = V(top, k), v2 = V(bot, k);
         const Rel<T> A1 = make_rel<T>(px - v1.x, py - v1.y, pz - v1.z), A2 = make_rel<T>(px - v2.x, py - v2.y, pz - v2.z);
         const Rel<T> B1 = make_rel<T>(px - v1.x, -py - v1.y, pz - v1.z), B2 = make_rel<T>(px - v2.x, -py - v2.y, pz - v2.z);
-        const T cx = v2.x - v1.x, cy = v2.y - v1.y, cz = v2.z - v1.z;  // right chordwise segment
-        const T tx = v1.x - v0.x, ty = v1.y - v0.y, tz = v1.z - v0.z;  // top segment v0->v1
-        const T bx = v3.x - v2.x, by = v3.y - v2.y, bz = v3.z - v2.z;  // bottom segment v2->v3
+        const V3<T> c3 = SEG ? seg[k] : V3<T>{v2.x - v1.x, v2.y - v1.y, v2.z - v1.z};          // right chordwise segment
+        const V3<T> t3 = SEG ? seg[W + k] : V3<T>{v1.x - v0.x, v1.y - v0.y, v1.z - v0.z};      // top segment v0->v1
+        const V3<T> b3 = SEG ? seg[2 * W + k] : V3<T>{v3.x - v2.x, v3.y - v2.y, v3.z - v2.z};  // bottom segment v2->v3
+        const T cx = c3.x, cy = c3.y, cz = c3.z;
+        const T tx = t3.x, ty = t3.y, tz = t3.z;
+        const T bx = b3.x, by = b3.y, bz = b3.z;
         const T Cra = seg_normal<T, SIGMA, DCUT>(A1, A2, cx, cy, cz, nx, ny, nz, sg);
         const T Crb = seg_normal<T, SIGMA, DCUT>(B1, B2, cx, cy, cz, nx, -ny, nz, sg);
         T val = seg_normal<T, SIGMA, DCUT>(A0, A1, tx, ty, tz, nx, ny, nz, sg) + Cra +
