@@ -9,12 +9,17 @@ default) builds one AIC per wing at alpha = 0 and solves the 8 angles as
 right-hand sides; ``--mode exact`` builds one AIC per wing and angle with
 the reference's alpha-dependent collocation points and wake.
 
-``value`` is solves/s with inputs resident on the device (the CUDA graph of
-one step replayed K times, timed with CUDA events on the launching stream;
-the AIC set is larger than L2, so no flush is needed).  ``e2e`` times the
-same through the public API with host buffers: H2D of the packed vertices
-and angles from pinned memory, the graph, and D2H of the coefficients and
-every gamma.  ``cpu_baseline`` times the CPU restatement of the reference
+``value`` is solves/s with inputs resident on the device: K steps, each one
+replay of a step's CUDA graph, with ``--in-flight`` (default 2) batches in
+flight on their own streams (BatchPipeline: the next batch's assembly and
+small systems fill the SMs that the current batch's largest factorisations
+leave idle), timed with CUDA events from the launching stream over all of
+them; the AIC set is larger than L2, so no flush is needed.  The
+``one_in_flight`` record gives the same with one batch at a time.  ``e2e``
+times the same through the public API with host buffers: H2D of the packed
+vertices and angles from pinned memory, the graph, and D2H of the
+coefficients and every gamma, per batch, with the next batch submitted
+before the current one is collected.  ``cpu_baseline`` times the CPU restatement of the reference
 backend (float, all host threads) on a bounded sample of the same cases.
 
 ``--impl reference`` times only that CPU implementation and prints its own
@@ -60,6 +65,9 @@ def parse():
     p.add_argument("--no-configs", action="store_true",
                    help="skip the short records of configurations A, B, C, E and the exact formulation")
     p.add_argument("--plain-solves", type=int, default=48)
+    p.add_argument("--in-flight", type=int, default=2,
+                   help="batches in flight (BatchPipeline depth) for the headline and its end-to-end number; "
+                        "the one-in-flight rate and latency are reported beside them")
     p.add_argument("--workload", default="batch", choices=["batch", "large", "uvlm", "served", "aero2dof", "nlvlm", "hbvlm"],
                    help="batch: the headline batched workload; large: one 128x128 elliptic wing, 64 alphas; "
                         "uvlm: 20x80 rectangular wing, 500 pitch-plunge steps")
@@ -274,10 +282,13 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    from tinyvlm_gb300.batch import BatchSolver, pack_alphas, pack_verts
+    from tinyvlm_gb300.batch import BatchPipeline, pack_alphas, pack_verts
 
     cases = workload(args)
-    bs = BatchSolver(cases, mode=args.mode, refine=args.refine, fp64_residual=args.fp64_residual)
+    depth = max(1, args.in_flight)
+    pipe = BatchPipeline(cases, depth=depth, mode=args.mode, refine=args.refine, fp64_residual=args.fp64_residual,
+                         streams=[torch.cuda.Stream(dev) for _ in range(depth)])
+    bs = pipe.slots[0]
     verts_h = torch.from_numpy(pack_verts(cases)).pin_memory()
     alphas = pack_alphas(cases)
     verts_d = verts_h.to(dev)
@@ -290,20 +301,41 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
-    # warm-up: captures the graph
+    # warm-up: captures every slot's graph
+    torch.cuda.synchronize()
+    pipe.set_inputs(verts_d, alphas, ref_pt=(0.25, 0.0, 0.0))
+    for _ in range(max(args.warmup, 3) * depth):
+        pipe.run()
     bs.set_inputs(verts_d, alphas, ref_pt=(0.25, 0.0, 0.0), stream=stream)
-    for _ in range(max(args.warmup, 3)):
-        bs.run(stream=stream)
     torch.cuda.synchronize()
 
-    # --- device-resident throughput -----------------------------------------
+    # --- device-resident throughput, one batch in flight ----------------------
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bs.run(stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms1 = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    value1 = replica_value(bs.nsolve, world, ms1)
+
+    # --- device-resident throughput, `depth` batches in flight ---------------
+    # each slot's stream starts after e0; the timed region ends when every
+    # slot's last batch has finished
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         e0.record(stream)
+        for st in pipe.streams:
+            st.wait_event(e0)
         for _ in range(args.steps):
-            bs.run(stream=stream)
+            pipe.run()
+        for st in pipe.streams:
+            stream.wait_stream(st)
         e1.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -311,16 +343,32 @@ def run_gpu(args):
     value = replica_value(bs.nsolve, world, ms)
 
     # --- end to end through the public API with host buffers ----------------
-    lat = []
+    # one batch in flight: inputs in, solve, results out, per step
+    lat1 = []
     barrier()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     for _ in range(args.steps):
         s0 = time.perf_counter()
         bs.set_inputs(verts_h, alphas, ref_pt=(0.25, 0.0, 0.0), stream=stream)
         bs.run(want_gamma=True, stream=stream)
         bs.results_into(co_h, g_h, stream=stream)
-        lat.append(1000.0 * (time.perf_counter() - s0))
+        lat1.append(1000.0 * (time.perf_counter() - s0))
+    torch.cuda.synchronize()
+    # `depth` in flight: batch i+1 is submitted before batch i is collected;
+    # a batch's latency runs from its submit to the end of its collect
+    lat, t_sub = [], {}
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        if pipe.full():
+            t, _, _ = pipe.collect(co_h, g_h)
+            lat.append(1000.0 * (time.perf_counter() - t_sub.pop(t)))
+        s0 = time.perf_counter()
+        t_sub[pipe.submit(verts_h, alphas, ref_pt=(0.25, 0.0, 0.0), want_gamma=True)] = s0
+    while pipe.pending():
+        t, _, _ = pipe.collect(co_h, g_h)
+        lat.append(1000.0 * (time.perf_counter() - t_sub.pop(t)))
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(1000.0 * (time.perf_counter() - t0) / args.steps, world, dev)
     e2e = replica_value(bs.nsolve, world, e2e_ms)
@@ -367,10 +415,14 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded trapezoidal wings)",
-        "config": config(args, cases),
+        "config": dict(config(args, cases), in_flight=depth),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                       "what": "per step (one batch of %d solves) through the public API" % bs.nsolve},
+                       "what": "per batch of %d solves, submit to collected results, %d batches in flight "
+                               "(BatchPipeline)" % (bs.nsolve, depth)},
+        "one_in_flight": {"value": value1, "ms_per_step": ms1, "unit": "solves/s",
+                          "latency_ms": {"p50": float(np.percentile(lat1, 50)), "p99": float(np.percentile(lat1, 99)),
+                                         "what": "per batch, set_inputs + run + results through BatchSolver"}},
         "gpu_launches": int(bs.launches()) * args.steps,
         "clocks": clk.summary(),
         "roofline": roof,

@@ -189,3 +189,64 @@ def test_eager_equals_graph_across_size_groups(cuda):
     one.run(graph=False)
     alone, _ = one.results()
     np.testing.assert_allclose(alone, graph[0:2], rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("depth", [1, 2, 3])
+def test_pipeline_equals_single_solver(cuda, depth):
+    """BatchPipeline: batches with different angles submitted back to back, up to `depth` in flight, each
+    collected first in first out; every batch's coefficients and circulations are bitwise those of one
+    BatchSolver run on the same inputs.  Then the device-resident run() path on every slot in turn."""
+    cases = M.batch_cases(24, seed=11, n_alpha=3, nc_range=(4, 24), ns_range=(4, 48))
+    from tinyvlm_gb300.batch import BatchPipeline
+    rng = np.random.default_rng(5)
+    batches = [np.deg2rad(rng.uniform(-8, 8, len(pack_alphas(cases)))) for _ in range(7)]
+    single = BatchSolver(cases, mode="shared", refine=1)
+    want = []
+    for al in batches:
+        single.set_inputs(pack_verts(cases), al, ref_pt=REF)
+        single.run(want_gamma=True)
+        co, g = single.results(gamma=True)
+        want.append((co, np.concatenate(g)))
+    pipe = BatchPipeline(cases, depth=depth, mode="shared", refine=1)
+    got, tickets = {}, []
+    for al in batches:
+        if pipe.full():
+            g = np.zeros(pipe.gamma_floats, np.float32)
+            t, co, _ = pipe.collect(g=g)
+            got[t] = (co, g)
+        tickets.append(pipe.submit(pack_verts(cases), al, ref_pt=REF, want_gamma=True))
+        assert pipe.pending() <= depth
+    while pipe.pending():
+        g = np.zeros(pipe.gamma_floats, np.float32)
+        t, co, _ = pipe.collect(g=g)
+        got[t] = (co, g)
+    assert sorted(got) == tickets == list(range(len(batches)))
+    for t, (co, g) in got.items():
+        np.testing.assert_array_equal(co, want[t][0])
+        np.testing.assert_array_equal(g, want[t][1])
+    # resident inputs: each slot solves the last batch again
+    pipe.set_inputs(pack_verts(cases), batches[-1], ref_pt=REF)
+    slots = [pipe.run() for _ in range(2 * depth)]
+    assert slots == [(i + len(batches)) % depth for i in range(2 * depth)]
+    for s, st in zip(pipe.slots, pipe.streams):
+        co, _ = s.results(stream=st)
+        np.testing.assert_array_equal(co, want[-1][0])
+
+
+def test_pipeline_refusals(cuda):
+    cases = M.batch_cases(3, seed=12, n_alpha=2, nc_range=(4, 6), ns_range=(4, 8))
+    from tinyvlm_gb300.batch import BatchPipeline
+    pipe = BatchPipeline(cases, depth=2)
+    with pytest.raises(RuntimeError, match="no batch in flight"):
+        pipe.collect()
+    pipe.submit(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    with pytest.raises(ValueError, match="without want_gamma"):
+        pipe.collect(g=np.zeros(pipe.gamma_floats, np.float32))
+    pipe.submit(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    with pytest.raises(RuntimeError, match="collect one first"):
+        pipe.submit(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+    with pytest.raises(RuntimeError, match="in flight first"):
+        pipe.run()
+    assert [pipe.collect()[0] for _ in range(2)] == [0, 1]
+    with pytest.raises(ValueError):
+        BatchPipeline(cases, depth=0)

@@ -5,6 +5,7 @@ solved in one CUDA graph; see include/gbvlm.h for the two formulations
 (``exact``: one AIC per case and angle with the reference's alpha-dependent
 geometry; ``shared``: one AIC per case, angles as right-hand sides).
 """
+import collections
 import ctypes
 
 import numpy as np
@@ -126,6 +127,113 @@ class BatchSolver:
         out = (ctypes.c_double * 4)()
         call("gbvlm_batch_update_profile", self.h, ctypes.cast(out, P), self._s(stream))
         return {"ms": out[0], "launches": int(out[1]), "flops": out[2], "bytes": out[3]}
+
+
+class BatchPipeline:
+    """Several batches of one workload in flight at once.
+
+    ``depth`` solver instances (each with its own device buffers and CUDA
+    graph) on their own streams, used in turn.  A batch's step ends with the
+    factorisations of its largest systems, a chain of launches that leaves
+    most SMs idle; with the next batch already enqueued on another stream,
+    its assembly and small systems fill them.  Each batch's results are
+    bitwise those of a single BatchSolver; a batch's latency grows with the
+    depth, since it shares the GPU with the batches around it.
+
+    Two ways to drive it:
+
+    - ``submit`` / ``collect``: host inputs in, results out, first in first
+      out.  ``submit`` copies the inputs and enqueues the solve on the next
+      free slot, returning a ticket; ``collect`` waits for the oldest batch
+      in flight and reads it back.  At most ``depth`` batches are in flight.
+    - ``set_inputs`` once, then ``run``: inputs resident on the device, the
+      same batch solved again on each slot in turn, nothing read back.
+
+    ``streams``: one stream per slot (any object ``stream_handle`` accepts);
+    by default the library's own non-blocking streams.
+    """
+
+    def __init__(self, cases, depth=2, mode="shared", refine=1, tuned=True, fp64_residual=False, streams=None):
+        if depth < 1:
+            raise ValueError("depth must be at least 1")
+        if streams is None:
+            from .device import Stream
+            streams = [Stream() for _ in range(depth)]
+        if len(streams) != depth:
+            raise ValueError("need one stream per slot (%d), got %d" % (depth, len(streams)))
+        self.slots = [BatchSolver(cases, mode=mode, refine=refine, tuned=tuned, fp64_residual=fp64_residual)
+                      for _ in range(depth)]
+        self.streams = list(streams)
+        self.depth = depth
+        self.nsolve = self.slots[0].nsolve
+        self.gamma_floats = self.slots[0].gamma_floats
+        self.tuning = self.slots[0].tuning
+        self._turn = 0  # the slot the next batch goes to
+        self._inflight = collections.deque()  # (ticket, slot, want_gamma), oldest first
+        self._tickets = 0
+
+    def pending(self):
+        """Batches submitted and not yet collected."""
+        return len(self._inflight)
+
+    def full(self):
+        return len(self._inflight) == self.depth
+
+    def submit(self, verts, alphas, u_inf=1.0, rho=1.0, ref_pt=(0.0, 0.0, 0.0), want_gamma=False):
+        """Copy one batch's inputs to the next free slot and enqueue its solve;
+        returns the batch's ticket.  The inputs are as for
+        BatchSolver.set_inputs; the call returns once they are copied."""
+        if self.full():
+            raise RuntimeError("all %d slots hold a batch: collect one first" % self.depth)
+        # first in first out over a ring: the slots in flight are the `pending`
+        # ones before _turn, so _turn itself is free
+        slot = self._turn
+        s, st = self.slots[slot], self.streams[slot]
+        s.set_inputs(verts, alphas, u_inf=u_inf, rho=rho, ref_pt=ref_pt, stream=st)
+        s.run(want_gamma=want_gamma, stream=st)
+        self._turn = (slot + 1) % self.depth
+        ticket = self._tickets
+        self._tickets += 1
+        self._inflight.append((ticket, slot, bool(want_gamma)))
+        return ticket
+
+    def collect(self, co=None, g=None):
+        """Wait for the oldest batch in flight and read it back: coefficients
+        (nsolve, 5) into ``co`` (allocated when None), circulations into
+        ``g`` when that batch was submitted with want_gamma.  Returns
+        (ticket, co, g).  Status errors of the batch raise as in
+        BatchSolver.results."""
+        if not self._inflight:
+            raise RuntimeError("no batch in flight")
+        ticket, slot, wg = self._inflight[0]
+        if g is not None and not wg:
+            raise ValueError("batch %d was submitted without want_gamma" % ticket)
+        if co is None:
+            co = np.zeros((self.nsolve, 5), np.float64)
+        self._inflight.popleft()
+        self.slots[slot].results_into(co, g, stream=self.streams[slot])
+        return ticket, co, g
+
+    def set_inputs(self, verts, alphas, u_inf=1.0, rho=1.0, ref_pt=(0.0, 0.0, 0.0)):
+        """The same inputs on every slot, for ``run``."""
+        if self._inflight:
+            raise RuntimeError("collect the batches in flight first")
+        for s, st in zip(self.slots, self.streams):
+            s.set_inputs(verts, alphas, u_inf=u_inf, rho=rho, ref_pt=ref_pt, stream=st)
+
+    def run(self, want_gamma=False):
+        """Enqueue one solve of the resident inputs on the next slot's stream;
+        returns the slot.  Nothing is read back."""
+        if self._inflight:
+            raise RuntimeError("collect the batches in flight first")
+        slot = self._turn
+        self.slots[slot].run(want_gamma=want_gamma, stream=self.streams[slot])
+        self._turn = (slot + 1) % self.depth
+        return slot
+
+    def launches(self):
+        """Kernel launches of one batch."""
+        return self.slots[0].launches()
 
 
 def smoke_check():
