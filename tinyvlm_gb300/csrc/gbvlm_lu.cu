@@ -264,17 +264,22 @@ __device__ __forceinline__ double rcp_rn(double d) { return __drcp_rn(d); }
 // pivot row's shared-memory address.  Kept out of line: called once per column from the
 // unrolled column loop, it is the same code for all 32 columns.
 template <class T, int NT, bool CLUSTER>
-__device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank) {
+__device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank, int nwa) {
     namespace cg = cooperative_groups;
     using Key = PivKey<T>;
     using SM = PanelSmem<T, NT, CLUSTER>;
     extern __shared__ __align__(16) unsigned char pr_smem[];
     SM& sm = *reinterpret_cast<SM*>(pr_smem);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    const Key mine = lane < SM::NW ? sm.s_key[buf][lane] : Key::none();
+    if constexpr (CLUSTER) {
+        __syncthreads();
+    } else {
+        // the CTA's first nwa warps; the others left at entry
+        asm volatile("bar.sync 1, %0;" ::"r"(nwa * 32) : "memory");
+    }
+    const Key mine = lane < nwa ? sm.s_key[buf][lane] : Key::none();
     const Key best = mine.warp_max();
-    const int w = __ffs(__ballot_sync(0xffffffffu, lane < SM::NW && mine == best)) - 1;
+    const int w = __ffs(__ballot_sync(0xffffffffu, lane < nwa && mine == best)) - 1;
     PivotOut<T> o;
     if constexpr (CLUSTER) {
         // warp 0 pushes this CTA's candidate (key and row) into every CTA of the
@@ -301,7 +306,7 @@ __device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank)
 }
 
 template <class T, int NT, bool CLUSTER, int RPT>
-__global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab) {
+__global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab, int trim) {
     namespace cg = cooperative_groups;
     using Key = PivKey<T>;
     using SM = PanelSmem<T, NT, CLUSTER>;
@@ -320,6 +325,16 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
     const int nb = (int)min((int64_t)GK, n - k);
     const int rows = (int)(n - k);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // one CTA per system: the launch is sized for the group's tallest
+    // system, and a warp without rows of this one leaves at once (the
+    // per-column barrier counts the remaining warps)
+    int nwa = SM::NW;
+    if constexpr (!CLUSTER) {
+        if (trim) {
+            nwa = (min(rows, NT) + 31) >> 5;
+            if (wid >= nwa) return;
+        }
+    }
 
     // own rows: slab-relative tid, tid + NT, ...; lid = logical position, -1: no row
     int lid[RPT];
@@ -363,7 +378,7 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
                 if (lane == 0) sm.s_key[buf][wid] = w;
             }
             // 2. pivot: (p, row) known to every warp
-            const PivotOut<T> po = panel_exchange<T, NT, CLUSTER>(buf, csize, rank);
+            const PivotOut<T> po = panel_exchange<T, NT, CLUSTER>(buf, csize, rank, nwa);
             const int p = po.p;
             const T d = lds1(po.row + jj * (uint32_t)sizeof(T), T(0));
             if (tid == 0 && rank == 0) {
@@ -1740,10 +1755,21 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
 // ---------------------------------------------------------------------------
 // panel launch: register panel with the thread count of the group
 // ---------------------------------------------------------------------------
+// GBVLM_PANEL_TRIM=0 keeps every warp of a one-CTA panel in the column loop
+static bool panel_trim() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("GBVLM_PANEL_TRIM");
+        mode = (e && atoi(e) == 0) ? 0 : 1;
+    }
+    return mode == 1;
+}
+
 template <class T, int NT, int RPT>
 static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
     if (g.csize == 1) {
-        k_panel_reg<T, NT, false, RPT><<<g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(B, k, act, g.slab);
+        k_panel_reg<T, NT, false, RPT><<<g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(B, k, act, g.slab,
+                                                                                           panel_trim() ? 1 : 0);
         GB_LAUNCH_CHECK();
         return GBVLM_OK;
     }
@@ -1759,7 +1785,7 @@ static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, c
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true, RPT>, B, k, act, g.slab));
+    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true, RPT>, B, k, act, g.slab, 0));
     return GBVLM_OK;
 }
 
