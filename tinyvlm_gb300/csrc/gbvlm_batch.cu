@@ -429,7 +429,8 @@ constexpr int RS_MAXRHS = 8;  // (the inner loop reads them as two float4)
 constexpr int RS_CB = 8;  // columns of Xd staged per step
 constexpr int RS_ROWS = 2;  // rows per thread
 
-// (sh, sl) += a * (xh + xl)
+// (sh, sl) += a * (xh + xl); XL = false: xl is zero
+template <bool XL>
 __device__ __forceinline__ void df_mac(float& sh, float& sl, float a, float xh, float xl) {
     const float p = __fmul_rn(a, xh);
     const float pe = __fmaf_rn(a, xh, -p);  // a*xh - p exactly
@@ -437,13 +438,15 @@ __device__ __forceinline__ void df_mac(float& sh, float& sl, float a, float xh, 
     const float bb = __fsub_rn(s, sh);
     const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));  // sh + p - s exactly
     sh = s;
-    sl = __fmaf_rn(a, xl, __fadd_rn(sl, __fadd_rn(e, pe)));
+    sl = XL ? __fmaf_rn(a, xl, __fadd_rn(sl, __fadd_rn(e, pe))) : __fadd_rn(sl, __fadd_rn(e, pe));
 }
 
 // LO: the plan keeps the correction Alo of the stored AIC; its products with
 // the hi part of Xd join the low-order sums (Alo is about 2^-24 of A, so
-// the float product is exact to far below the residual's accuracy)
-template <bool LO>
+// the float product is exact to far below the residual's accuracy).
+// XL = false: Xd holds float values (the first sweep: Xd = 0 + the float
+// solve), so its lo part is zero and its products are left out.
+template <bool LO, bool XL>
 __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, const int64_t* rpfx) {
     __shared__ __align__(16) float xh[RS_CB][RS_MAXRHS];
     __shared__ __align__(16) float xl[RS_CB][RS_MAXRHS];
@@ -478,7 +481,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
                 const double v = (c0 + cc < n && q < nq) ? S.Xd[(c0 + cc) + (q0 + q) * n] : 0.0;
                 const float h = (float)v;
                 xh[cc][q] = h;
-                xl[cc][q] = (float)(v - (double)h);
+                if (XL) xl[cc][q] = (float)(v - (double)h);
             }
             __syncthreads();
             if (rv[0]) {
@@ -496,15 +499,19 @@ __global__ void __launch_bounds__(RS_THREADS) k_batch_residual(BatchArgs a, cons
                     // the 8 hi and 8 lo values of column cc as four 16-byte broadcasts
                     const float4 h0 = *reinterpret_cast<const float4*>(&xh[cc][0]);
                     const float4 h1 = *reinterpret_cast<const float4*>(&xh[cc][4]);
-                    const float4 l0 = *reinterpret_cast<const float4*>(&xl[cc][0]);
-                    const float4 l1 = *reinterpret_cast<const float4*>(&xl[cc][4]);
                     const float hh[RS_MAXRHS] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
-                    const float ll[RS_MAXRHS] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+                    float ll[RS_MAXRHS] = {};
+                    if (XL) {
+                        const float4 l0 = *reinterpret_cast<const float4*>(&xl[cc][0]);
+                        const float4 l1 = *reinterpret_cast<const float4*>(&xl[cc][4]);
+                        ll[0] = l0.x, ll[1] = l0.y, ll[2] = l0.z, ll[3] = l0.w;
+                        ll[4] = l1.x, ll[5] = l1.y, ll[6] = l1.z, ll[7] = l1.w;
+                    }
 #pragma unroll
                     for (int k = 0; k < RS_ROWS; k++)
 #pragma unroll
                         for (int q = 0; q < RS_MAXRHS; q++) {
-                            df_mac(sh[k][q], sl[k][q], av[k][cc], hh[q], ll[q]);
+                            df_mac<XL>(sh[k][q], sl[k][q], av[k][cc], hh[q], ll[q]);
                             if (LO) sl[k][q] = __fmaf_rn(lv[k][cc], hh[q], sl[k][q]);
                         }
                 }
@@ -871,10 +878,13 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     if (h->fp64_residual && !staged && h->refine > 0) GB_CUDA(cudaStreamWaitEvent(st, h->lo_join, 0));
     for (int it = 0; it < h->refine; it++) {
         const dim3 rg((unsigned)h->residual_tiles, (unsigned)cdiv(maxrhs, RS_MAXRHS));
-        if (h->fp64_residual)
-            k_batch_residual<true><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
-        else
-            k_batch_residual<false><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+        if (h->fp64_residual) {
+            if (it == 0) k_batch_residual<true, false><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+            else k_batch_residual<true, true><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+        } else {
+            if (it == 0) k_batch_residual<false, false><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+            else k_batch_residual<false, true><<<rg, RS_THREADS, 0, st>>>(a, h->d_rpfx);
+        }
         GB_LAUNCH_CHECK();
         rc = solve();
         if (rc) return rc;

@@ -1797,8 +1797,8 @@ static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, cons
         return GBVLM_OK;
     }
     if constexpr (sizeof(T) == 4) {  // one row per thread (two per thread, half the warps, measured
-                                     // slower with both shuffled and shared-memory pivot rows, and for
-                                     // the cluster panels alone)
+                                     // slower with both shuffled and shared-memory pivot rows, for
+                                     // the cluster panels alone, and with two batches in flight)
         switch (g.nt) {
             case 128: return launch_panel_nt<T, 128, 1>(B, k, act, g, st);
             case 256: return launch_panel_nt<T, 256, 1>(B, k, act, g, st);
