@@ -68,3 +68,11 @@ def test_headline_workload_has_a_tuned_entry():
     if not os.path.exists(A.TABLE):
         pytest.skip("no tuning table yet")
     assert A.lookup(key) is not None, key
+
+
+def test_batch_key_in_flight():
+    """Batches in flight enter the key only when more than one, so one-in-flight keys stay as they were."""
+    dims, na = [(8, 4), (16, 8)], [8, 8]
+    k1 = A.batch_key(dims, na, "shared", 1, 152)
+    assert A.batch_key(dims, na, "shared", 1, 152, in_flight=1) == k1
+    assert A.batch_key(dims, na, "shared", 1, 152, in_flight=2) == k1 + "/f2"

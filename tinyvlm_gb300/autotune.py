@@ -91,12 +91,15 @@ def _p2(x):
     return 1 << max(0, int(round(math.log2(max(1, int(x))))))
 
 
-def batch_key(ns_nc, nalpha, mode, refine, sms):
+def batch_key(ns_nc, nalpha, mode, refine, sms, in_flight=1):
     """A batched steady workload: cases (ns, nc), angles per case, formulation,
-    refinement sweeps and the device's SM count."""
+    refinement sweeps, the device's SM count and, when more than one, the
+    batches in flight at once (BatchPipeline: other batches take the SMs a
+    batch leaves idle, which moves the best size groups)."""
     n = [int(a) * int(b) for a, b in ns_nc]
-    return "batch/%s/r%d/sm%d/c%d/p%d/m%d/a%d" % (mode, int(refine), int(sms), _p2(len(n)), _p2(sum(n)), _p2(max(n)),
-                                                 int(max(nalpha)))
+    key = "batch/%s/r%d/sm%d/c%d/p%d/m%d/a%d" % (mode, int(refine), int(sms), _p2(len(n)), _p2(sum(n)), _p2(max(n)),
+                                                int(max(nalpha)))
+    return key + ("/f%d" % int(in_flight) if int(in_flight) > 1 else "")
 
 
 def wake_key(points, rows, sms):
@@ -189,38 +192,50 @@ def _descend(space, run, base, repeats=3):
 
 BATCH_SPACE = [
     [{"batch.group_hi": hi, "batch.group_lo": lo} for hi, lo in
-     ((1024, 384), (1536, 512), (768, 320), (1024, 256), (1280, 448), (896, 384), (2048, 512), (1024, 512))],
+     ((1024, 384), (1536, 512), (768, 320), (1024, 256), (1280, 448), (896, 384), (2048, 512), (1024, 512),
+      (1280, 640), (2048, 768), (768, 256), (640, 256), (896, 320), (768, 384))],
     [{"batch.assembly_span": s} for s in (64, 128, 256)],
     [{"batch.loads_threads": t} for t in (0, 32, 64, 128, 256)],
 ]
 
 
-def tune_batch(cases, mode="shared", refine=1, steps=5, repeats=3, persist=True):
+def tune_batch(cases, mode="shared", refine=1, steps=5, repeats=3, persist=True, in_flight=1):
     """Search the batch plan's shapes for these cases on the device; the time
-    of a point is a CUDA-event measurement of `steps` graph replays."""
-    from .batch import BatchSolver, pack_alphas, pack_verts
+    of a point is a CUDA-event measurement of `steps` graph replays per slot,
+    with `in_flight` batches in flight (BatchPipeline, one stream per slot,
+    every slot's last batch finished before the closing event)."""
+    from .batch import BatchPipeline, pack_alphas, pack_verts
     from .device import DeviceArray, Event, Stream
     sms = device_sms()
-    key = batch_key([(c.ns, c.nc) for c in cases], [len(c.alphas) for c in cases], mode, refine, sms)
-    stream = Stream()
+    key = batch_key([(c.ns, c.nc) for c in cases], [len(c.alphas) for c in cases], mode, refine, sms, in_flight)
     verts = DeviceArray.from_numpy(pack_verts(cases))
     alphas = pack_alphas(cases)
 
     def run(p):
         set_params(p)
-        bs = BatchSolver(cases, mode=mode, refine=refine, tuned=False)
-        bs.set_inputs(verts, alphas, ref_pt=(0.25, 0.0, 0.0), stream=stream)
-        for _ in range(2):
-            bs.run(stream=stream)
-        e0, e1 = Event(), Event()
-        e0.record(stream)
-        for _ in range(steps):
-            bs.run(stream=stream)
-        e1.record(stream)
-        stream.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        del bs
-        return ms
+        pipe = BatchPipeline(cases, depth=in_flight, mode=mode, refine=refine, tuned=False)
+        pipe.set_inputs(verts, alphas, ref_pt=(0.25, 0.0, 0.0))
+        for _ in range(2 * in_flight):
+            pipe.run()
+        for st in pipe.streams:
+            st.synchronize()
+        # the slots' streams are independent: time each slot's replays with its
+        # own events, all slots enqueued together; a point's time per batch is
+        # the span from the earliest start to the latest end over all batches
+        e0 = [Event() for _ in pipe.streams]
+        e1 = [Event() for _ in pipe.streams]
+        for e, st in zip(e0, pipe.streams):
+            e.record(st)
+        for _ in range(steps * in_flight):
+            pipe.run()
+        for e, st in zip(e1, pipe.streams):
+            e.record(st)
+        for st in pipe.streams:
+            st.synchronize()
+        first = min(range(in_flight), key=lambda i: e0[0].elapsed_time(e0[i]))
+        span = max(e0[first].elapsed_time(e1[i]) for i in range(in_flight))
+        del pipe
+        return span / (steps * in_flight)
 
     base = {k: v for k, v in defaults().items() if k.startswith("batch.")}
     t0 = time.perf_counter()
@@ -341,6 +356,7 @@ def main():
     cases = M.batch_cases(512, seed=20261203, n_alpha=8)
     for mode in ("shared", "exact"):
         print(json.dumps(tune_batch(cases, mode=mode, refine=1)))
+    print(json.dumps(tune_batch(cases, mode="shared", refine=1, in_flight=2)))
     for rows in (500, 4000, 20000, 40000):
         print(json.dumps(tune_wake((80, 20), rows)))
     for sets in (1, 44):

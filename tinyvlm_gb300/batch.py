@@ -29,10 +29,11 @@ def pack_alphas(cases):
 
 
 class BatchSolver:
-    def __init__(self, cases, mode="shared", refine=1, tuned=True, fp64_residual=False):
+    def __init__(self, cases, mode="shared", refine=1, tuned=True, fp64_residual=False, in_flight=1):
         """``tuned``: take the plan's launch shapes from the autotuner's table
-        for this workload's shape (autotune.batch_key); otherwise the
-        library's current parameters.  ``fp64_residual``: the refinement
+        for this workload's shape and ``in_flight``, the batches the caller
+        keeps in flight at once (autotune.batch_key); otherwise the library's
+        current parameters.  ``fp64_residual``: the refinement
         residual measures the FP64 system (GBVLM_BATCH_FP64_RESIDUAL: a
         float-pair evaluation of the AIC corrects the stored float one), so
         the circulations, not only CL/CM, converge to the FP64 solution;
@@ -44,7 +45,7 @@ class BatchSolver:
             from . import autotune
             self.tuning = autotune.apply(autotune.batch_key([(c.ns, c.nc) for c in cases],
                                                             [len(c.alphas) for c in cases], mode, refine,
-                                                            autotune.device_sms()))
+                                                            autotune.device_sms(), in_flight))
         self.dims = [(c.ns, c.nc, 0) for c in cases]
         self.nalpha = [len(c.alphas) for c in cases]
         d = dims_array(self.dims)
@@ -161,8 +162,8 @@ class BatchPipeline:
             streams = [Stream() for _ in range(depth)]
         if len(streams) != depth:
             raise ValueError("need one stream per slot (%d), got %d" % (depth, len(streams)))
-        self.slots = [BatchSolver(cases, mode=mode, refine=refine, tuned=tuned, fp64_residual=fp64_residual)
-                      for _ in range(depth)]
+        self.slots = [BatchSolver(cases, mode=mode, refine=refine, tuned=tuned, fp64_residual=fp64_residual,
+                                  in_flight=depth) for _ in range(depth)]
         self.streams = list(streams)
         self.depth = depth
         self.nsolve = self.slots[0].nsolve
