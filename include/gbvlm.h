@@ -168,6 +168,8 @@ int gbvlm_device_info(int32_t* sm_count, int64_t* free_bytes, int64_t* total_byt
  *                                n <= lo (1024, 384); hi > lo
  *   batch.loads_threads  0, 32, 64, 128, 256: the loads block (0: by size)
  *   batch.assembly_span  64, 128, 256: rings per assembly span chunk (128)
+ *   batch.assembly_rows  1-4: chordwise ring rows per float assembly tile (4; at most 2 with
+ *                        span 256)
  * ------------------------------------------------------------------------- */
 int gbvlm_tune_set(const char* name, int64_t value);
 int gbvlm_tune_get(const char* name, int64_t* value);

@@ -250,3 +250,38 @@ def test_pipeline_refusals(cuda):
     assert [pipe.collect()[0] for _ in range(2)] == [0, 1]
     with pytest.raises(ValueError):
         BatchPipeline(cases, depth=0)
+
+
+@pytest.mark.parametrize("mode", ["shared", "exact"])
+@pytest.mark.parametrize("rows", [1, 2, 3, 4])
+def test_assembly_rows_per_tile(cuda, rows, mode):
+    """Float assembly tiles of 1-4 chordwise ring rows (batch.assembly_rows; k_batch_assemble_rows beyond one):
+    the batch matches the double oracle, CDi included.  The cases include ring-row counts that are not multiples
+    of the rows per tile (the trailing-edge row, with its wake rings, in a shorter last tile) and spans wider
+    than one 128-ring chunk: up to 150 spanwise panels, whose narrow wake panels 50 chords from the wing are
+    where the Trefftz influence needs the wake's own frame (exact mode, the wake tilted by alpha).  With the
+    FP64 residual (whose correction kernel keeps one-row tiles and reads the float AIC these tiles write) the
+    circulations still converge to the double solution."""
+    from tinyvlm_gb300 import autotune as A
+    cases = M.batch_cases(8, seed=21, n_alpha=2, nc_range=(4, 11), ns_range=(4, 150))
+    assert (rows == 1 or any(c.nc % rows for c in cases)) and max(c.ns for c in cases) > 128
+    saved = A.current()
+    try:
+        A.set_params({"batch.assembly_rows": rows})
+        bs = BatchSolver(cases, mode=mode, refine=1, tuned=False)
+        bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+        bs.run(want_gamma=True)
+        co, gam = bs.results(gamma=True)
+        _check(co, gam, cases, mode)
+        bf = BatchSolver(cases, mode=mode, refine=2, fp64_residual=True, tuned=False)
+        bf.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+        bf.run(want_gamma=True)
+        _, gam64 = bf.results(gamma=True)
+    finally:
+        A.set_params(saved)
+    k = 0
+    for c in cases:
+        for r in _ref(mode, c):
+            g = np.concatenate([x.ravel() for x in r["gamma"]])
+            assert np.linalg.norm(gam64[k] - g) <= 3e-7 * np.linalg.norm(g), ("gamma fp64 residual", mode, rows, k)
+            k += 1

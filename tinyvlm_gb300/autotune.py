@@ -2,7 +2,7 @@
 
 The kernels' launch shapes are named integer parameters of the library
 (gbvlm_tune_*, include/gbvlm.h): the batch LU's size-group boundaries, the
-batch loads block, the batch assembly's span chunk, the split-K slice count
+batch loads block, the batch assembly's span chunk and ring rows per tile, the split-K slice count
 of the wake sums and of the HBVLM wake operator.  The reference fixes its
 shapes (kernel_influence at (32, 16) blocks, vlm_backend_cuda.cu:171); here
 they are searched per workload shape and kept in a table.
@@ -195,6 +195,7 @@ BATCH_SPACE = [
      ((1024, 384), (1536, 512), (768, 320), (1024, 256), (1280, 448), (896, 384), (2048, 512), (1024, 512),
       (1280, 640), (2048, 768), (768, 256), (640, 256), (896, 320), (768, 384))],
     [{"batch.assembly_span": s} for s in (64, 128, 256)],
+    [{"batch.assembly_rows": r} for r in (1, 2, 3, 4)],
     [{"batch.loads_threads": t} for t in (0, 32, 64, 128, 256)],
 ]
 

@@ -55,7 +55,8 @@ struct SysDesc {
     float* nrm;             // normals float (3 planes)
     double* area;           // panel areas
     double* vd;             // wing vertices double (3 planes)
-    double* wd;             // wake vertices double (3 planes, 2 rows)
+    double* wd;             // wake vertices double (3 planes, 2 rows) in the wake's frame (x along the wake;
+                            // the Trefftz influence only)
     double* nrmd;           // normals double
     float* A;               // AIC (factored in place)
     float* A2;              // unfactored copy (refinement), may be null
@@ -107,27 +108,39 @@ __global__ void __launch_bounds__(256) k_batch_geom(BatchArgs a) {
     bad = __syncthreads_or(bad);
     if (threadIdx.x == 0) a.bad[blockIdx.x] = bad;
     // the angle's double trigonometry once per block (long on the fp64 units)
-    __shared__ double s_trig[3];
+    __shared__ double s_trig[5];
     if (threadIdx.x == 0) {
-        const double sa = sin(al);
-        s_trig[0] = 100.0 * a.u_inf * cos(al);
+        const double sa = sin(al), ca = cos(al);
+        s_trig[0] = 100.0 * a.u_inf * ca;
         s_trig[1] = 100.0 * a.u_inf * sa;
         s_trig[2] = (al < (double)EPS_F) ? 0.5 : 0.5 * (al / (sa + (double)EPS_F));
+        s_trig[3] = ca;
+        s_trig[4] = sa;
     }
     __syncthreads();
     // wake (vlm.cpp:104-114 seen from the displaced wing): row 0 = trailing
     // edge, row 1 = trailing edge + 100 u (cos a, 0, sin a)
-    const double dx = s_trig[0], dz = s_trig[1];
+    const double dx = s_trig[0], dz = s_trig[1], ca = s_trig[3], sa = s_trig[4];
     const int64_t wl = 2 * (ns + 1);
     for (int64_t i = threadIdx.x; i <= ns; i += blockDim.x) {
         const int64_t te = i + nc * (ns + 1);
         double x = S.vinit[te], y = S.vinit[nv + te], z = S.vinit[2 * nv + te];
         double w0[3] = {x, y, z}, w1[3] = {x + dx, y, z + dz};
         for (int k = 0; k < 3; k++) {
-            S.wd[k * wl + i] = w0[k];
-            S.wd[k * wl + (ns + 1) + i] = w1[k];
             split_hl(w0[k], S.wh[k * wl + i], S.wl[k * wl + i]);
             split_hl(w1[k], S.wh[k * wl + (ns + 1) + i], S.wl[k * wl + (ns + 1) + i]);
+        }
+        // the Trefftz copy turned about y by -a, so the wake runs along x: a
+        // point's offsets across the 100-chord trailing legs are then small
+        // coordinates of their own, which keep float precision when the
+        // Trefftz kernel rounds its relative vectors (in the wing's frame
+        // they are differences of ~50-chord coordinates; identity at a = 0)
+        for (int r = 0; r < 2; r++) {
+            const double* q = r ? w1 : w0;
+            const int64_t o = r * (ns + 1) + i;
+            S.wd[o] = fma(ca, q[0], sa * q[2]);
+            S.wd[wl + o] = q[1];
+            S.wd[2 * wl + o] = fma(ca, q[2], -(sa * q[0]));
         }
     }
     __syncthreads();
@@ -200,6 +213,51 @@ __device__ __forceinline__ void strip_hl(const float* topH, const float* topL, c
     }
 }
 
+// The wake rings behind a trailing-edge ring row, span rings [s0, s1): each
+// one's value is added to the wing ring's unscaled value already stored at
+// colA (Kutta condition, vlm_backend_cpu.cpp:121-139 with iteration = 1), and
+// the sum is scaled and stored in A and the A2 copy.
+__device__ __forceinline__ void te_wake(const SysDesc& S, int64_t s0, int64_t s1, HL px, HL py, HL pz, float nx,
+                                        float ny, float nz, float* colA, float* colB) {
+    const int64_t ns = S.ns, n = S.n;
+    const float k4 = 1.0f / (4.0f * PI_F);
+    const int64_t wl = 2 * (ns + 1);
+    for (int64_t s = s0; s < s1; s++) {
+        // wake ring: v0=(s,TE) v1=(s+1,TE) v2=(s+1,far) v3=(s,far)
+        float Qh[4][3], Ql[4][3];
+        const int64_t idx[4] = {s, s + 1, (ns + 1) + s + 1, (ns + 1) + s};
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                Qh[q][k] = S.wh[k * wl + idx[q]];
+                Ql[q][k] = S.wl[k * wl + idx[q]];
+            }
+        float val = 0.f;
+#pragma unroll
+        for (int mir = 0; mir < 2; mir++) {
+            Rel<float> R[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float y = mir ? df_sub(-py.h, -py.l, Qh[q][1], Ql[q][1]) : df_sub(py.h, py.l, Qh[q][1], Ql[q][1]);
+                R[q] = make_rel<float>(df_sub(px.h, px.l, Qh[q][0], Ql[q][0]), y, df_sub(pz.h, pz.l, Qh[q][2], Ql[q][2]));
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int e = (q + 1) & 3;
+                const float rx = df_sub(Qh[e][0], Ql[e][0], Qh[q][0], Ql[q][0]);
+                const float ry = df_sub(Qh[e][1], Ql[e][1], Qh[q][1], Ql[q][1]);
+                const float rz = df_sub(Qh[e][2], Ql[e][2], Qh[q][2], Ql[q][2]);
+                val += seg_normal<float, false, true>(R[q], R[e], rx, ry, rz, nx, mir ? -ny : ny, nz, 0.f);
+            }
+        }
+        float* dst = colA + (s - s0) * n;
+        const float tot = (*dst + val) * k4;
+        *dst = tot;
+        if (colB) colB[(s - s0) * n] = tot;
+    }
+}
+
 __device__ __forceinline__ int find_sys(const int64_t* pfx, int cnt, int64_t b) {
     int lo = 0, hi = cnt - 1;
     while (lo < hi) {
@@ -212,7 +270,7 @@ __device__ __forceinline__ int find_sys(const int64_t* pfx, int cnt, int64_t b) 
 // tile0: the first tile of this launch (a size group's systems are a
 // contiguous range of tiles)
 template <int BA_SPAN>
-__global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
+__global__ void __launch_bounds__(BA_THREADS, 8) k_batch_assemble(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
     constexpr int BA_W = BA_SPAN + 1;
     __shared__ float sw[2][2][3 * BA_W];  // [row][hi/lo][plane*W + s]
     __shared__ float4 sseg[3][BA_W];      // the strip's segment vectors (strip_hl)
@@ -271,40 +329,127 @@ __global__ void __launch_bounds__(BA_THREADS) k_batch_assemble(BatchArgs a, cons
     // condition, vlm_backend_cpu.cpp:121-139 with iteration = 1)
     strip_hl<BA_W>(sw[0][0], sw[0][1], sw[1][0], sw[1][1], sseg, nvs, px, py, pz, nx, ny, nz,
                    [&](int kk, float v) { colA[(int64_t)kk * n] = v; });
-    const int64_t wl = 2 * (ns + 1);
-    for (int64_t s = s0; s < s1; s++) {
-        // wake ring: v0=(s,TE) v1=(s+1,TE) v2=(s+1,far) v3=(s,far)
-        float Qh[4][3], Ql[4][3];
-        const int64_t idx[4] = {s, s + 1, (ns + 1) + s + 1, (ns + 1) + s};
+    te_wake(S, s0, s1, px, py, pz, nx, ny, nz, colA, colB);
+}
+
+// Tiles of R chordwise ring rows (system, 128-point block, R ring rows, span
+// chunk).  The rows' R + 1 vertex lines are walked together along the span:
+// a spanwise segment of a line inside the tile is evaluated once (forward,
+// vertex k-1 -> k) and enters the ring above the line with + and the ring
+// below it with -, and each vertex's distances to the point are formed once
+// for the rings on both sides of it.  Per ring: (2R + 1) / R segment pairs
+// (direct and mirror) and (R + 1) / R vertex distances, against 3 and 2 for
+// one row per tile.  Ring value in the order of strip_hl: top + right - bottom
+// - left, then the mirror image's four terms.  Up to three rows the kernel
+// fits 64 registers and 8 CTAs per SM; four rows take 34 KB of shared
+// memory (6 CTAs).
+template <int BA_SPAN, int R>
+__global__ void __launch_bounds__(BA_THREADS, R <= 3 ? 8 : 6) k_batch_assemble_rows(BatchArgs a, const int64_t* tpfx, int64_t tile0) {
+    constexpr int BA_W = BA_SPAN + 1;
+    __shared__ float sw[R + 1][2][3 * BA_W];  // [line][hi/lo][plane*W + s]
+    __shared__ float4 sspan[R + 1][BA_W];     // line l: vertex k-1 -> k (k >= 1)
+    __shared__ float4 schord[R][BA_W];        // ring row r: line r -> line r+1 at vertex k
+    const int64_t tile = tile0 + blockIdx.x;
+    const int si = find_sys(tpfx, a.nsys, tile);
+    const SysDesc& S = a.sys[si];
+    const int64_t ns = S.ns, nc = S.nc, n = S.n;
+    const int64_t nchunk = (ns + BA_SPAN - 1) / BA_SPAN, nrb = (n + BA_THREADS - 1) / BA_THREADS;
+    int64_t t = tile - tpfx[si];
+    const int64_t rb = t % nrb;
+    t /= nrb;
+    const int64_t z = t % nchunk, c0 = (t / nchunk) * R;
+    const int rows = (int)min((int64_t)R, nc - c0);  // ring rows of this tile
+    const int64_t s0 = z * BA_SPAN, s1 = min(s0 + (int64_t)BA_SPAN, ns);
+    const int nvs = (int)(s1 - s0 + 1);
+    const int64_t nv = (ns + 1) * (nc + 1);
+    for (int e = threadIdx.x; e < (rows + 1) * 3 * nvs; e += BA_THREADS) {
+        const int l = e / (3 * nvs), rem = e - l * 3 * nvs, k = rem / nvs, sl = rem - k * nvs;
+        const int64_t vi = k * nv + (s0 + sl) + (c0 + l) * (ns + 1);
+        sw[l][0][k * BA_W + sl] = S.vh[vi];
+        sw[l][1][k * BA_W + sl] = S.vl[vi];
+    }
+    __syncthreads();
+    // segment vectors from the double-float positions, once per tile
+    for (int e = threadIdx.x; e < (2 * rows + 1) * nvs; e += BA_THREADS) {
+        const int q = e / nvs, k = e - q * nvs;
+        const bool span = q <= rows;  // q <= rows: line q's spanwise segment; else row q - rows - 1's chordwise
+        const int l0 = span ? q : q - rows - 1, l1 = span ? q : l0 + 1, k0 = span ? k - 1 : k;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (k0 >= 0) {
+            v.x = df_sub(sw[l1][0][k], sw[l1][1][k], sw[l0][0][k0], sw[l0][1][k0]);
+            v.y = df_sub(sw[l1][0][BA_W + k], sw[l1][1][BA_W + k], sw[l0][0][BA_W + k0], sw[l0][1][BA_W + k0]);
+            v.z = df_sub(sw[l1][0][2 * BA_W + k], sw[l1][1][2 * BA_W + k], sw[l0][0][2 * BA_W + k0],
+                         sw[l0][1][2 * BA_W + k0]);
+        }
+        if (span) sspan[q][k] = v;
+        else schord[q - rows - 1][k] = v;
+    }
+    __syncthreads();
+    const int64_t i = rb * BA_THREADS + threadIdx.x;
+    if (i >= n) return;
+    const HL px{S.ch[i], S.cl_[i]}, py{S.ch[n + i], S.cl_[n + i]}, pz{S.ch[2 * n + i], S.cl_[2 * n + i]};
+    const float nx = S.nrm[i], ny = S.nrm[n + i], nz = S.nrm[2 * n + i];
+    const float k4 = 1.0f / (4.0f * PI_F);
+    const int te_row = (c0 + rows == nc) ? rows - 1 : -1;  // the trailing-edge ring row, if in the tile
+    auto rel = [&](int l, int sl, bool mir) {
+        const float* H = sw[l][0];
+        const float* L = sw[l][1];
+        const float y = mir ? df_sub(-py.h, -py.l, H[BA_W + sl], L[BA_W + sl]) : df_sub(py.h, py.l, H[BA_W + sl], L[BA_W + sl]);
+        return make_rel<float>(df_sub(px.h, px.l, H[sl], L[sl]), y, df_sub(pz.h, pz.l, H[2 * BA_W + sl], L[2 * BA_W + sl]));
+    };
+    Rel<float> A[R + 1], B[R + 1];  // the lines' distances at the previous vertex (direct, mirror)
+    float Ca[R], Cb[R];             // the rows' left chordwise segments
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+    for (int l = 0; l <= R; l++)
+        if (l <= rows) {
+            A[l] = rel(l, 0, false);
+            B[l] = rel(l, 0, true);
+        }
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                Qh[q][k] = S.wh[k * wl + idx[q]];
-                Ql[q][k] = S.wl[k * wl + idx[q]];
-            }
-        float val = 0.f;
+    for (int r = 0; r < R; r++)
+        if (r < rows) {
+            const float4 cv = schord[r][0];
+            Ca[r] = seg_normal<float, false, true>(A[r], A[r + 1], cv.x, cv.y, cv.z, nx, ny, nz, 0.f);
+            Cb[r] = seg_normal<float, false, true>(B[r], B[r + 1], cv.x, cv.y, cv.z, nx, -ny, nz, 0.f);
+        }
+    float* col0 = S.A + i + (c0 * ns + s0) * n;
+    float* colB0 = S.A2 ? S.A2 + i + (c0 * ns + s0) * n : nullptr;
+    for (int k = 1; k < nvs; k++) {
+        float Sp = 0.f, Spm = 0.f;  // the line above's spanwise segment (direct, mirror)
 #pragma unroll
-        for (int mir = 0; mir < 2; mir++) {
-            Rel<float> R[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float y = mir ? df_sub(-py.h, -py.l, Qh[q][1], Ql[q][1]) : df_sub(py.h, py.l, Qh[q][1], Ql[q][1]);
-                R[q] = make_rel<float>(df_sub(px.h, px.l, Qh[q][0], Ql[q][0]), y, df_sub(pz.h, pz.l, Qh[q][2], Ql[q][2]));
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int e = (q + 1) & 3;
-                const float rx = df_sub(Qh[e][0], Ql[e][0], Qh[q][0], Ql[q][0]);
-                const float ry = df_sub(Qh[e][1], Ql[e][1], Qh[q][1], Ql[q][1]);
-                const float rz = df_sub(Qh[e][2], Ql[e][2], Qh[q][2], Ql[q][2]);
-                val += seg_normal<float, false, true>(R[q], R[e], rx, ry, rz, nx, mir ? -ny : ny, nz, 0.f);
+        for (int l = 0; l <= R; l++) {
+            if (l <= rows) {
+                const Rel<float> An = rel(l, k, false), Bn = rel(l, k, true);
+                const float4 sv = sspan[l][k];
+                const float Sc = seg_normal<float, false, true>(A[l], An, sv.x, sv.y, sv.z, nx, ny, nz, 0.f);
+                const float Scm = seg_normal<float, false, true>(B[l], Bn, sv.x, sv.y, sv.z, nx, -ny, nz, 0.f);
+                A[l] = An;
+                B[l] = Bn;
+                if (l >= 1) {
+                    const int r = l - 1;
+                    const float4 cv = schord[r][k];
+                    const float Cr = seg_normal<float, false, true>(A[r], A[l], cv.x, cv.y, cv.z, nx, ny, nz, 0.f);
+                    const float Crm = seg_normal<float, false, true>(B[r], B[l], cv.x, cv.y, cv.z, nx, -ny, nz, 0.f);
+                    float val = Sp + Cr - Sc - Ca[r];
+                    val += Spm + Crm - Scm - Cb[r];
+                    Ca[r] = Cr;
+                    Cb[r] = Crm;
+                    const int64_t off = ((int64_t)r * ns + (k - 1)) * n;
+                    if (r == te_row) {
+                        col0[off] = val;  // unscaled: te_wake adds the wake ring
+                    } else {
+                        col0[off] = val * k4;
+                        if (colB0) colB0[off] = val * k4;
+                    }
+                }
+                Sp = Sc;
+                Spm = Scm;
             }
         }
-        float* dst = colA + (s - s0) * n;
-        const float tot = (*dst + val) * k4;
-        *dst = tot;
-        if (colB) colB[(s - s0) * n] = tot;
+    }
+    if (te_row >= 0) {
+        const int64_t off = (int64_t)te_row * ns * n;
+        te_wake(S, s0, s1, px, py, pz, nx, ny, nz, col0 + off, colB0 ? colB0 + off : nullptr);
     }
 }
 
@@ -564,8 +709,11 @@ __global__ void k_batch_trefftz_k(BatchArgs a) {
     const V3<double> cm_{c.x, -c.y, c.z};
     // ring jj's two streamwise segments at c and at its mirror image: relative
     // vectors and segment vectors formed in double and rounded to float, the
-    // segment law in float (the fp64 units of this part are slow; K enters
-    // CDi through gamma^T K gamma, with no cancellation to amplify ~1e-7)
+    // segment law in float (the fp64 units of this part are slow).  The wake
+    // vertices are in the wake's frame (x along the trailing legs), so the
+    // offsets across a leg, which the cross product takes, are coordinates
+    // of their own and keep float precision; a rotation about y leaves K
+    // (a normal velocity) and the mirror image in y as they are
     auto rel = [](V3<double> p, V3<double> q) {
         return make_rel<float>((float)(p.x - q.x), (float)(p.y - q.y), (float)(p.z - q.z));
     };
@@ -700,10 +848,15 @@ struct gbvlm_batch_s {
     SysDesc* d_sys = nullptr;
     int32_t* d_solve_sys = nullptr;
     int64_t* d_tpfx = nullptr;   // assembly tiles
+    int64_t* d_tpfx_rows = nullptr;  // float assembly tiles of asm_rows ring rows (asm_rows > 1)
+    int asm_rows = 1;
     int64_t* d_rpfx = nullptr;   // residual tiles
     int64_t assembly_tiles = 0, residual_tiles = 0;
     std::vector<int64_t> tpfx_host;   // assembly tile prefix over the sorted systems
     int64_t gtile[4][2] = {};         // per size group: first tile, tiles
+    int64_t gtile_rows[4][2] = {};    // the same over the float assembly's tiles of asm_rows rows
+    int64_t assembly_tiles_rows = 0;
+    std::vector<int64_t> tpfx_rows_host;
     int64_t maxn = 0;
     // the sorted systems in size groups, each factored by its own plan on its
     // own stream (graph branch), so the long step chain of the largest
@@ -763,7 +916,31 @@ constexpr int MAX_GROUPS_B = 2;  // size-group boundaries (gbvlm_batch_s::MAX_GR
 // serial_lu: factor the size groups one after another on `st` (kernel timing
 // without the groups' launches overlapping)
 // the assembly kernel of the plan's span chunk over `tiles` tiles from tile0
+template <int SPAN>
+static void launch_assemble_rows(int rows, unsigned tiles, int64_t tile0, const BatchArgs& a, const int64_t* tpfx,
+                                 cudaStream_t st) {
+    switch (rows) {
+        case 2: k_batch_assemble_rows<SPAN, 2><<<tiles, BA_THREADS, 0, st>>>(a, tpfx, tile0); break;
+        case 3:
+            if constexpr (SPAN <= 128) k_batch_assemble_rows<SPAN, 3><<<tiles, BA_THREADS, 0, st>>>(a, tpfx, tile0);
+            break;
+        default:
+            if constexpr (SPAN <= 128) k_batch_assemble_rows<SPAN, 4><<<tiles, BA_THREADS, 0, st>>>(a, tpfx, tile0);
+            break;
+    }
+}
+
+// the float assembly's tiles: one ring row each (k_batch_assemble), or
+// asm_rows rows (k_batch_assemble_rows, its own tile prefix)
 static cudaError_t launch_assemble(gbvlm_batch h, unsigned tiles, int64_t tile0, const BatchArgs& a, cudaStream_t st) {
+    if (h->asm_rows > 1) {
+        switch (h->tp.batch_assembly_span) {
+            case 64: launch_assemble_rows<64>(h->asm_rows, tiles, tile0, a, h->d_tpfx_rows, st); break;
+            case 256: launch_assemble_rows<256>(h->asm_rows, tiles, tile0, a, h->d_tpfx_rows, st); break;
+            default: launch_assemble_rows<128>(h->asm_rows, tiles, tile0, a, h->d_tpfx_rows, st); break;
+        }
+        return cudaGetLastError();
+    }
     switch (h->tp.batch_assembly_span) {
         case 64: k_batch_assemble<64><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
         case 256: k_batch_assemble<256><<<tiles, BA_THREADS, 0, st>>>(a, h->d_tpfx, tile0); break;
@@ -825,7 +1002,7 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
     if (staged) GB_CUDA(trefftz());
     mark(1);
     if (staged) {
-        GB_CUDA(launch_assemble(h, (unsigned)h->assembly_tiles, 0, a, st));
+        GB_CUDA(launch_assemble(h, (unsigned)(h->asm_rows > 1 ? h->assembly_tiles_rows : h->assembly_tiles), 0, a, st));
         if (h->fp64_residual) GB_CUDA(launch_assemble_lo(h, (unsigned)h->assembly_tiles, 0, a, st));
     }
     mark(2);
@@ -845,7 +1022,8 @@ static int batch_enqueue(gbvlm_batch h, cudaStream_t st, cudaEvent_t* ev = nullp
         for (int g = 0; g < h->ngroups; g++) {
             GB_CUDA(cudaStreamWaitEvent(h->side[g], h->fork, 0));
             if (h->gtile[g][1] > 0) {
-                GB_CUDA(launch_assemble(h, (unsigned)h->gtile[g][1], h->gtile[g][0], a, h->side[g]));
+                const int64_t(&gt)[2] = h->asm_rows > 1 ? h->gtile_rows[g] : h->gtile[g];
+                GB_CUDA(launch_assemble(h, (unsigned)gt[1], gt[0], a, h->side[g]));
                 if (h->fp64_residual) {
                     GB_CUDA(cudaEventRecord(h->asm_done[g], h->side[g]));
                     GB_CUDA(cudaStreamWaitEvent(h->lo_side, h->asm_done[g], 0));
@@ -1028,17 +1206,24 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     const size_t o_uidx = reserve(sizeof(int32_t) * solve_sys.size());
     const size_t o_bad = reserve(sizeof(int32_t) * h->nsys);
     // tile prefix tables
-    std::vector<int64_t> tpfx(h->nsys + 1, 0), rpfx(h->nsys + 1, 0);
+    // ring rows per float assembly tile: at most 4, at most 2 with 256-ring span chunks (shared memory)
+    h->asm_rows = (int)std::min<int64_t>(h->tp.batch_assembly_rows, h->tp.batch_assembly_span > 128 ? 2 : 4);
+    std::vector<int64_t> tpfx(h->nsys + 1, 0), tpfx_rows(h->nsys + 1, 0), rpfx(h->nsys + 1, 0);
     for (int k = 0; k < h->nsys; k++) {
         const gbvlm_dims& d = dims[protos[order[k]].case_id];
         const int64_t n = protos[order[k]].n;
-        tpfx[k + 1] = tpfx[k] + cdiv(n, BA_THREADS) * cdiv(d.ns, h->tp.batch_assembly_span) * d.nc;
+        const int64_t per_row = cdiv(n, BA_THREADS) * cdiv(d.ns, h->tp.batch_assembly_span);
+        tpfx[k + 1] = tpfx[k] + per_row * d.nc;
+        tpfx_rows[k + 1] = tpfx_rows[k] + per_row * cdiv(d.nc, (int64_t)h->asm_rows);
         rpfx[k + 1] = rpfx[k] + cdiv(n, RS_THREADS * RS_ROWS);
     }
     h->assembly_tiles = tpfx[h->nsys];
     h->tpfx_host = tpfx;
+    h->assembly_tiles_rows = tpfx_rows[h->nsys];
+    h->tpfx_rows_host = tpfx_rows;
     h->residual_tiles = rpfx[h->nsys];
     const size_t o_tpfx = reserve(sizeof(int64_t) * tpfx.size());
+    const size_t o_tpfx_rows = reserve(sizeof(int64_t) * tpfx_rows.size());
     const size_t o_rpfx = reserve(sizeof(int64_t) * rpfx.size());
     // LU tables
     const size_t o_lun = reserve(sizeof(int64_t) * h->nsys);
@@ -1068,6 +1253,7 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     h->d_uidx = (int32_t*)(base + o_uidx);
     h->d_bad = (int32_t*)(base + o_bad);
     h->d_tpfx = (int64_t*)(base + o_tpfx);
+    h->d_tpfx_rows = (int64_t*)(base + o_tpfx_rows);
     h->d_rpfx = (int64_t*)(base + o_rpfx);
     // system descriptors
     h->sys.resize(h->nsys);
@@ -1146,6 +1332,7 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     up(h->d_goff, goff.data(), sizeof(int64_t) * goff.size());
     up(h->d_uidx, uidx.data(), sizeof(int32_t) * uidx.size());
     up(h->d_tpfx, tpfx.data(), sizeof(int64_t) * tpfx.size());
+    up(h->d_tpfx_rows, tpfx_rows.data(), sizeof(int64_t) * tpfx_rows.size());
     up(h->d_rpfx, rpfx.data(), sizeof(int64_t) * rpfx.size());
     up(base + o_lun, lun.data(), sizeof(int64_t) * h->nsys);
     up(base + o_luA, luA.data(), sizeof(float*) * h->nsys);
@@ -1185,6 +1372,8 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
             const int gi = h->ngroups++;
             h->gtile[gi][0] = h->tpfx_host[i0];
             h->gtile[gi][1] = h->tpfx_host[i1] - h->tpfx_host[i0];
+            h->gtile_rows[gi][0] = h->tpfx_rows_host[i0];
+            h->gtile_rows[gi][1] = h->tpfx_rows_host[i1] - h->tpfx_rows_host[i0];
             std::vector<int64_t> ns(lun.begin() + i0, lun.begin() + i1);
             h->plans[gi].mem = h->mem;
             rc = lu_plan_build(h->plans[gi], ns, 0, i0);

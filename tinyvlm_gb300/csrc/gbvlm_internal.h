@@ -41,6 +41,7 @@ struct TuneParams {
     int64_t batch_group_lo = 384;
     int64_t batch_loads_threads = 0;   // loads block: 0 = 64 up to 4096 unknowns, 256 beyond
     int64_t batch_assembly_span = 128; // rings per span chunk of a batch assembly tile
+    int64_t batch_assembly_rows = 4;   // chordwise ring rows per float assembly tile (1-4; at most 2 with span 256)
 };
 TuneParams tune();
 // SM count of the current device (cached per device)

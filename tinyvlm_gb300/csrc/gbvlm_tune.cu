@@ -29,6 +29,7 @@ const Param kParams[] = {
     {"batch.group_lo", &TuneParams::batch_group_lo, 16, 16384},
     {"batch.loads_threads", &TuneParams::batch_loads_threads, 0, 256},
     {"batch.assembly_span", &TuneParams::batch_assembly_span, 64, 256},
+    {"batch.assembly_rows", &TuneParams::batch_assembly_rows, 1, 4},
 };
 
 std::mutex g_mu;
