@@ -36,6 +36,7 @@ namespace gbvlm {
 constexpr int PANEL_THREADS = 512;
 constexpr int PR_THREADS_F64 = 256;  // register panel, double: 32 doubles of panel per thread
 constexpr int PR_MAX_CLUSTER = 16;   // largest cluster of the register panel
+constexpr int PACK_MIN_SLICE = 128;  // narrowest slice of a packed one-CTA panel (at most 8 systems per CTA)
 constexpr int TRSM_COLS = 128;
 constexpr int GT = 64;  // update tile edge
 constexpr int GK = LU_NB;
@@ -264,7 +265,7 @@ __device__ __forceinline__ double rcp_rn(double d) { return __drcp_rn(d); }
 // pivot row's shared-memory address.  Kept out of line: called once per column from the
 // unrolled column loop, it is the same code for all 32 columns.
 template <class T, int NT, bool CLUSTER>
-__device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank, int nwa) {
+__device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank, int nwa, int wbase, int bar) {
     namespace cg = cooperative_groups;
     using Key = PivKey<T>;
     using SM = PanelSmem<T, NT, CLUSTER>;
@@ -274,12 +275,18 @@ __device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank,
     if constexpr (CLUSTER) {
         __syncthreads();
     } else {
-        // the CTA's first nwa warps; the others left at entry
-        asm volatile("bar.sync 1, %0;" ::"r"(nwa * 32) : "memory");
+        // the slice's first nwa warps (warps wbase ..); the others left at
+        // entry.  Barrier 1 + slice, as an immediate: the kernel then holds
+        // only the barriers its slices can use
+        constexpr int MS = NT >= 2 * PACK_MIN_SLICE ? NT / PACK_MIN_SLICE : 1;
+        static_for<1, MS + 1>([&](auto BI) {
+            constexpr int id = decltype(BI)::value;
+            if (bar == id) asm volatile("bar.sync %0, %1;" ::"n"(id), "r"(nwa * 32) : "memory");
+        });
     }
-    const Key mine = lane < nwa ? sm.s_key[buf][lane] : Key::none();
+    const Key mine = lane < nwa ? sm.s_key[buf][wbase + lane] : Key::none();
     const Key best = mine.warp_max();
-    const int w = __ffs(__ballot_sync(0xffffffffu, lane < nwa && mine == best)) - 1;
+    const int w = wbase + __ffs(__ballot_sync(0xffffffffu, lane < nwa && mine == best)) - 1;
     PivotOut<T> o;
     if constexpr (CLUSTER) {
         // warp 0 pushes this CTA's candidate (key and row) into every CTA of the
@@ -306,7 +313,8 @@ __device__ __noinline__ PivotOut<T> panel_exchange(int buf, int csize, int rank,
 }
 
 template <class T, int NT, bool CLUSTER, int RPT>
-__global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab, int trim) {
+__global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const int32_t* act, int slab, int trim,
+                                                   const int32_t* pack, int count) {
     namespace cg = cooperative_groups;
     using Key = PivKey<T>;
     using SM = PanelSmem<T, NT, CLUSTER>;
@@ -317,22 +325,35 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
         csize = (int)cg::this_cluster().num_blocks();
         rank = (int)cg::this_cluster().block_rank();
     }
-    const int32_t sid = act[blockIdx.x / csize];
+    // one CTA: one system, or (pack) P systems side by side in slices of
+    // NT / P threads, each with its own barrier; the launch is sized for the
+    // group's tallest system, and a warp without rows of its system leaves
+    // at once (the per-column barrier counts the remaining warps)
+    int sidx = blockIdx.x / csize, snt = NT, slice = 0;
+    if constexpr (!CLUSTER) {
+        if (pack) {
+            const int P = pack[2 * blockIdx.x + 1];
+            snt = NT / P;
+            slice = (int)threadIdx.x / snt;
+            sidx = pack[2 * blockIdx.x] + slice;
+            if (sidx >= count) return;  // a slice of the last CTA without a system
+        }
+    }
+    const int32_t sid = act[sidx];
     const int64_t n = B.n[sid], ld = B.ld[sid];
     T* A = B.A[sid];
     int32_t* ipiv = B.ipiv[sid];
     int zero_col = -1;  // first exactly zero pivot of this panel (thread 0 of rank 0)
     const int nb = (int)min((int64_t)GK, n - k);
     const int rows = (int)(n - k);
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    // one CTA per system: the launch is sized for the group's tallest
-    // system, and a warp without rows of this one leaves at once (the
-    // per-column barrier counts the remaining warps)
-    int nwa = SM::NW;
+    const int tid = (int)threadIdx.x - slice * snt, lane = tid & 31;  // tid: within the slice
+    const int wbase = slice * (snt >> 5), wid = wbase + (tid >> 5);    // wid: the CTA's warp
+    const int bar = 1 + slice;
+    int nwa = snt >> 5;
     if constexpr (!CLUSTER) {
         if (trim) {
-            nwa = (min(rows, NT) + 31) >> 5;
-            if (wid >= nwa) return;
+            nwa = (min(rows, snt) + 31) >> 5;
+            if (wid - wbase >= nwa) return;
         }
     }
 
@@ -341,8 +362,8 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
     T x[RPT][GK];
 #pragma unroll
     for (int i = 0; i < RPT; i++) {
-        const int rr = tid + i * NT, r = rank * slab + rr;
-        lid[i] = (rr < slab && r < rows) ? r : -1;
+        const int rr = tid + i * snt, r = rank * slab + rr;
+        lid[i] = ((CLUSTER ? rr < slab : rr < snt) && r < rows) ? r : -1;
         const T* src = A + (k + r) + k * ld;
 #pragma unroll
         for (int t = 0; t < GK; t++) x[i][t] = (lid[i] >= 0 && t < nb) ? src[t * ld] : (T)0;
@@ -378,7 +399,7 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
                 if (lane == 0) sm.s_key[buf][wid] = w;
             }
             // 2. pivot: (p, row) known to every warp
-            const PivotOut<T> po = panel_exchange<T, NT, CLUSTER>(buf, csize, rank, nwa);
+            const PivotOut<T> po = panel_exchange<T, NT, CLUSTER>(buf, csize, rank, nwa, wbase, bar);
             const int p = po.p;
             const T d = lds1(po.row + jj * (uint32_t)sizeof(T), T(0));
             if (tid == 0 && rank == 0) {
@@ -432,7 +453,7 @@ __global__ void __launch_bounds__(NT) k_panel_reg(LuBatch<T> B, int64_t k, const
 #pragma unroll
         for (int i = 0; i < RPT; i++)
             if (lid[i] >= 0) {
-                const int r = rank * slab + tid + i * NT;
+                const int r = rank * slab + tid + i * snt;
                 if (lid[i] < GK) mv[lid[i]] = r;
                 if (r < GK) mv[GK + r] = lid[i];
             }
@@ -1755,6 +1776,16 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
 // ---------------------------------------------------------------------------
 // panel launch: register panel with the thread count of the group
 // ---------------------------------------------------------------------------
+// GBVLM_PANEL_PACK=0 keeps one system per one-CTA panel
+static bool panel_pack() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("GBVLM_PANEL_PACK");
+        mode = (e && atoi(e) == 0) ? 0 : 1;
+    }
+    return mode == 1;
+}
+
 // GBVLM_PANEL_TRIM=0 keeps every warp of a one-CTA panel in the column loop
 static bool panel_trim() {
     static int mode = -1;
@@ -1766,10 +1797,12 @@ static bool panel_trim() {
 }
 
 template <class T, int NT, int RPT>
-static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
+static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g,
+                           const int32_t* d_pack, cudaStream_t st) {
     if (g.csize == 1) {
-        k_panel_reg<T, NT, false, RPT><<<g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(B, k, act, g.slab,
-                                                                                           panel_trim() ? 1 : 0);
+        const bool packed = g.ctas > 0 && d_pack;
+        k_panel_reg<T, NT, false, RPT><<<packed ? g.ctas : g.count, NT, sizeof(PanelSmem<T, NT, false>), st>>>(
+            B, k, act, g.slab, panel_trim() ? 1 : 0, packed ? d_pack + 2 * g.pack_off : nullptr, g.count);
         GB_LAUNCH_CHECK();
         return GBVLM_OK;
     }
@@ -1785,12 +1818,14 @@ static int launch_panel_nt(const LuBatch<T>& B, int64_t k, const int32_t* act, c
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true, RPT>, B, k, act, g.slab, 0));
+    GB_CUDA(cudaLaunchKernelEx(&cfg, k_panel_reg<T, NT, true, RPT>, B, k, act, g.slab, 0, (const int32_t*)nullptr,
+                               g.count));
     return GBVLM_OK;
 }
 
 template <class T>
-static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g, cudaStream_t st) {
+static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, const PanelGroup& g,
+                        const int32_t* d_pack, cudaStream_t st) {
     if (g.csize == 0) {
         k_panel<T><<<g.count, PANEL_THREADS, 0, st>>>(B, k, act);
         GB_LAUNCH_CHECK();
@@ -1800,13 +1835,13 @@ static int launch_panel(const LuBatch<T>& B, int64_t k, const int32_t* act, cons
                                      // slower with both shuffled and shared-memory pivot rows, for
                                      // the cluster panels alone, and with two batches in flight)
         switch (g.nt) {
-            case 128: return launch_panel_nt<T, 128, 1>(B, k, act, g, st);
-            case 256: return launch_panel_nt<T, 256, 1>(B, k, act, g, st);
-            case 512: return launch_panel_nt<T, 512, 1>(B, k, act, g, st);
-            default: return launch_panel_nt<T, 1024, 1>(B, k, act, g, st);
+            case 128: return launch_panel_nt<T, 128, 1>(B, k, act, g, d_pack, st);
+            case 256: return launch_panel_nt<T, 256, 1>(B, k, act, g, d_pack, st);
+            case 512: return launch_panel_nt<T, 512, 1>(B, k, act, g, d_pack, st);
+            default: return launch_panel_nt<T, 1024, 1>(B, k, act, g, d_pack, st);
         }
     } else {
-        return launch_panel_nt<T, PR_THREADS_F64, 1>(B, k, act, g, st);
+        return launch_panel_nt<T, PR_THREADS_F64, 1>(B, k, act, g, nullptr, st);
     }
 }
 
@@ -1821,7 +1856,7 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
         const LuStep& S = plan.steps[s];
         if (S.n_panel == 0) continue;
         for (const PanelGroup& g : S.panels[sizeof(T) == 4 ? 0 : 1]) {
-            const int rc = launch_panel<T>(B, S.k, plan.d_act + S.act_off + g.first, g, st);
+            const int rc = launch_panel<T>(B, S.k, plan.d_act + S.act_off + g.first, g, plan.d_pack, st);
             if (rc) return rc;
         }
         const bool two_level = sizeof(T) == 4 && plan.W > GK;
@@ -2119,7 +2154,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
     }
     const int nsys = (int)n_sorted.size();
     for (int i = 1; i < nsys; i++) GB_REQUIRE(n_sorted[i] <= n_sorted[i - 1], "lu plan: sizes not sorted");
-    std::vector<int32_t> act;
+    std::vector<int32_t> act, pack;
     std::vector<int64_t> pfx;
     const int64_t maxn = nsys ? n_sorted[0] : 0;
     for (int64_t k = 0; k < maxn; k += GK) {
@@ -2153,6 +2188,20 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
                     while (j < cnt && n_sorted[j] - k > (int64_t)(cs / 2) * slab_max) j++;
                 }
                 g.count = j - i;
+                if (e == 0 && g.csize == 1 && g.nt >= 2 * PACK_MIN_SLICE && panel_pack() && panel_trim()) {
+                    // systems sorted by size: a CTA takes the next system and
+                    // as many after it as slices of that one's width fit
+                    g.pack_off = (int64_t)pack.size() / 2;
+                    for (int q = i; q < j;) {
+                        int w = PACK_MIN_SLICE;
+                        while (w < n_sorted[q] - k) w *= 2;
+                        const int P = std::min(g.nt / w, j - q);
+                        pack.push_back(q - i);
+                        pack.push_back(g.nt / w);
+                        g.ctas++;
+                        q += P;
+                    }
+                }
                 S.panels[e].push_back(g);
                 i = j;
             }
@@ -2299,6 +2348,10 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         GB_CUDA(dev_alloc((void**)&plan.d_act, act.size() * sizeof(int32_t), plan.mem));
         GB_CUDA(cudaMemcpyAsync(plan.d_act, act.data(), act.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     }
+    if (!pack.empty()) {
+        GB_CUDA(dev_alloc((void**)&plan.d_pack, pack.size() * sizeof(int32_t), plan.mem));
+        GB_CUDA(cudaMemcpyAsync(plan.d_pack, pack.data(), pack.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    }
     if (!pfx.empty()) {
         GB_CUDA(dev_alloc((void**)&plan.d_pfx, pfx.size() * sizeof(int64_t), plan.mem));
         GB_CUDA(cudaMemcpyAsync(plan.d_pfx, pfx.data(), pfx.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
@@ -2438,12 +2491,14 @@ void LuPlan::release() {
     dev_free(d_minv, mem);
     d_minv = nullptr;
     dev_free(d_act, mem);
+    dev_free(d_pack, mem);
     dev_free(d_pfx, mem);
     dev_free(d_err, mem);
     if (la_stream) cudaStreamDestroy(la_stream);
     if (la_fork) cudaEventDestroy(la_fork);
     if (la_join) cudaEventDestroy(la_join);
     d_act = nullptr;
+    d_pack = nullptr;
     d_pfx = nullptr;
     d_err = nullptr;
     la_stream = nullptr;

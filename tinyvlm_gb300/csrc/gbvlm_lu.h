@@ -36,6 +36,11 @@ struct LuBatch {
 struct PanelGroup {
     int32_t first = 0, count = 0;
     int32_t csize = 1, slab = 0, nt = 0;
+    // one-CTA panels with several systems per CTA: ctas CTAs, entries
+    // (first system of the CTA relative to `first`, systems in it) at
+    // LuPlan::d_pack + 2 * pack_off; ctas = 0: one system per CTA
+    int32_t ctas = 0;
+    int64_t pack_off = 0;
 };
 
 struct LuStep {
@@ -82,6 +87,7 @@ struct LuPlan {
     float* d_minv = nullptr;  // nsys x 128 x 128: I - L11^-1 of each system's current outer block
     int W = LU_NB;      // outer block width of the float factorisation
     int32_t* d_act = nullptr;
+    int32_t* d_pack = nullptr;  // PanelGroup pack entries
     int64_t* d_pfx = nullptr;
     int* d_err = nullptr;  // set by a tensor-core tile whose bounded wait ran out
     // algorithmic work of the outer (tensor-core) updates of one factorisation:
