@@ -36,6 +36,7 @@ namespace gbvlm {
 constexpr int PANEL_THREADS = 512;
 constexpr int PR_THREADS_F64 = 256;  // register panel, double: 32 doubles of panel per thread
 constexpr int PR_MAX_CLUSTER = 16;   // largest cluster of the register panel
+constexpr int SW2_THREADS = 256;     // k_swap2: columns per CTA
 constexpr int PACK_MIN_SLICE = 128;  // narrowest slice of a packed one-CTA panel (at most 8 systems per CTA)
 constexpr int TRSM_COLS = 128;
 constexpr int GT = 64;  // update tile edge
@@ -509,21 +510,33 @@ __global__ void k_swap(LuBatch<T> B, int64_t k, const int32_t* act, const int64_
 // thread per column (two-level blocking: inner swaps stay inside the outer
 // panel, the outer block's swaps reach the other columns in one pass).
 template <class T>
-__global__ void k_swap2(LuBatch<T> B, const int32_t* act, const int64_t* pfx, int cnt, int64_t r_lo, int64_t r_hi,
-                        int64_t a_lo, int64_t a_hi, int64_t b_lo, int64_t b_hi) {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= pfx[cnt]) return;
-    const int a = find_block(pfx, cnt, g);
+__global__ void __launch_bounds__(SW2_THREADS) k_swap2(LuBatch<T> B, const int32_t* act, const int64_t* pfx, int cnt,
+                                                      int64_t r_lo, int64_t r_hi, int64_t a_lo, int64_t a_hi,
+                                                      int64_t b_lo, int64_t b_hi) {
+    // a CTA owns SW2_THREADS columns of one system (pfx: CTAs per system);
+    // it stages the block's pivots once, and leaves when none moved a row
+    // (a diagonally dominant AIC keeps every row in place)
+    __shared__ int32_t s_ip[LU_OUTER];
+    const int a = find_block(pfx, cnt, blockIdx.x);
     const int32_t sid = act[a];
     const int64_t n = B.n[sid], ld = B.ld[sid];
+    const int32_t* ip = B.ipiv[sid];
+    const int nr = (int)(min(n, r_hi) - r_lo);
+    int moved = 0;
+    for (int t = threadIdx.x; t < nr; t += SW2_THREADS) {
+        const int32_t p = ip[r_lo + t];
+        s_ip[t] = p;
+        moved |= p != (int32_t)(r_lo + t);
+    }
+    if (!__syncthreads_or(moved)) return;
     const int64_t na = max((int64_t)0, min(n, a_hi) - a_lo);
-    int64_t j = g - pfx[a];
+    const int64_t ncols = na + (n - min(n, b_lo));
+    int64_t j = (int64_t)(blockIdx.x - pfx[a]) * SW2_THREADS + threadIdx.x;
+    if (j >= ncols) return;
     j = j < na ? a_lo + j : min(n, b_lo) + (j - na);
     T* col = B.A[sid] + j * ld;
-    const int32_t* ip = B.ipiv[sid];
-    const int64_t rh = min(n, r_hi);
-    for (int64_t r = r_lo; r < rh; r++) {
-        const int64_t p = ip[r];
+    for (int t = 0; t < nr; t++) {
+        const int64_t r = r_lo + t, p = s_ip[t];
         if (p != r) {
             const T tmp = col[r];
             col[r] = col[p];
@@ -1908,7 +1921,7 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
             pending = false;
         }
         if (S.bswap_total > 0) {
-            k_swap2<T><<<(unsigned)cdiv(S.bswap_total, 256), 256, 0, st>>>(
+            k_swap2<T><<<(unsigned)S.bswap_total, SW2_THREADS, 0, st>>>(
                 B, act + S.bswap_first, plan.d_pfx + S.bswap_pfx, S.n_panel - S.bswap_first, k0, S.kend, 0, k0, S.kend,
                 INT64_MAX);
             GB_LAUNCH_CHECK();
@@ -2283,7 +2296,7 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
         for (int i = S.bswap_first; i < cnt; i++) {
             pfx.push_back(acc);
             const int64_t n = n_sorted[i];
-            acc += k0 + (n - std::min(n, S.kend));
+            acc += cdiv(k0 + (n - std::min(n, S.kend)), (int64_t)SW2_THREADS);  // CTAs of the system
         }
         pfx.push_back(acc);
         S.bswap_total = acc;

@@ -59,7 +59,7 @@ struct LuStep {
     int64_t in_pfx = 0, in_blocks = 0;        // inner update of the outer panel, 64 x 64 tiles
     int64_t ik_pfx = 0, ik_blocks = 0;        // k_inner: row moves and U rows, 16-column chunks of the outer panel
     int32_t bswap_first = 0;                  // systems [bswap_first, n_panel) end the outer block here
-    int64_t bswap_pfx = 0, bswap_total = 0;   // the block's swaps on the columns outside it
+    int64_t bswap_pfx = 0, bswap_total = 0;   // the block's swaps on the columns outside it: CTAs per system
     int32_t n_tc = 0;                         // systems with n > kend at the block's last step (a prefix)
     int64_t btrsm_pfx = 0, btrsm_blocks = 0;  // U12 = L11^-1 A12, 32 columns per CTA
     int64_t tc_pfx = 0, tc_blocks = 0;        // outer update, 128 x 128 tensor-core tiles
