@@ -166,6 +166,8 @@ int gbvlm_device_info(int32_t* sm_count, int64_t* free_bytes, int64_t* total_byt
  *   hbvlm.min_rows       8..512  wake rows per operator slice at least (32)
  *   batch.group_hi/lo            batch LU size groups: n > hi, lo < n <= hi,
  *                                n <= lo (1024, 384); hi > lo
+ *   batch.group_mid      0 or hi > mid > lo: a fourth group, lo < n <= hi split at
+ *                        mid (0)
  *   batch.loads_threads  0, 32, 64, 128, 256: the loads block (0: by size)
  *   batch.assembly_span  64, 128, 256: rings per assembly span chunk (128)
  *   batch.assembly_rows  1-4: chordwise ring rows per float assembly tile (4; at most 2 with

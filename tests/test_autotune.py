@@ -19,10 +19,11 @@ def _restore():
 def test_parameters_and_defaults():
     p = A.params()
     assert set(p) >= {"wake.waves", "hbvlm.waves", "hbvlm.min_rows", "batch.group_hi", "batch.group_lo",
-                      "batch.loads_threads", "batch.assembly_span", "batch.assembly_rows"}
+                      "batch.loads_threads", "batch.assembly_span", "batch.assembly_rows", "batch.group_mid"}
     d = A.defaults()
     assert d["wake.waves"] == 4 and d["batch.group_hi"] == 1024 and d["batch.group_lo"] == 384
     assert d["batch.assembly_span"] == 128 and d["batch.loads_threads"] == 0 and d["batch.assembly_rows"] == 4
+    assert d["batch.group_mid"] == 0
     with pytest.raises(Exception):
         A.set_params({"batch.assembly_span": 96})
     with pytest.raises(Exception):

@@ -285,3 +285,43 @@ def test_assembly_rows_per_tile(cuda, rows, mode):
             g = np.concatenate([x.ravel() for x in r["gamma"]])
             assert np.linalg.norm(gam64[k] - g) <= 3e-7 * np.linalg.norm(g), ("gamma fp64 residual", mode, rows, k)
             k += 1
+
+
+def test_four_size_groups(cuda):
+    """batch.group_mid: a fourth LU size group (n > 1024, 640 < n <= 1024, 256 < n <= 640, n <= 256), each on its
+    own graph branch: the batch matches the double oracle, the graph equals the kernel-by-kernel launch and its
+    replay, and the same batch in three groups gives the same coefficients to float rounding."""
+    from tinyvlm_gb300 import autotune as A
+    big = M.batch_cases(2, seed=31, n_alpha=2, nc_range=(28, 32), ns_range=(48, 64))
+    upper = M.batch_cases(2, seed=32, n_alpha=2, nc_range=(20, 24), ns_range=(36, 42))
+    lower = M.batch_cases(2, seed=33, n_alpha=2, nc_range=(12, 16), ns_range=(24, 36))
+    small = M.batch_cases(3, seed=34, n_alpha=2, nc_range=(4, 8), ns_range=(4, 24))
+    cases = big + upper + lower + small
+    n = sorted(c.n for c in cases)
+    assert n[-1] > 1024 and any(640 < x <= 1024 for x in n) and any(256 < x <= 640 for x in n) and n[0] <= 256
+    saved = A.current()
+    try:
+        A.set_params({"batch.group_hi": 1024, "batch.group_mid": 640, "batch.group_lo": 256})
+        bs = BatchSolver(cases, mode="shared", refine=1, tuned=False)
+        bs.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+        bs.run(want_gamma=True)
+        co, gam = bs.results(gamma=True)
+        bs.run(want_gamma=True)
+        co_r, _ = bs.results()
+        bs.run(graph=False)
+        co_e, _ = bs.results()
+        A.set_params({"batch.group_mid": 0})
+        b3 = BatchSolver(cases, mode="shared", refine=1, tuned=False)
+        b3.set_inputs(pack_verts(cases), pack_alphas(cases), ref_pt=REF)
+        b3.run()
+        co3, _ = b3.results()
+        from tinyvlm_gb300._lib import GbvlmError
+        A.set_params({"batch.group_mid": 2048})
+        with pytest.raises(GbvlmError, match="group_mid"):
+            BatchSolver(cases, mode="shared", refine=1, tuned=False)
+    finally:
+        A.set_params(saved)
+    _check(co, gam, cases, "shared")
+    np.testing.assert_array_equal(co_r, co)
+    np.testing.assert_array_equal(co_e, co)
+    np.testing.assert_allclose(co3, co, rtol=1e-12, atol=1e-14)

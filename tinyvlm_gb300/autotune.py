@@ -191,9 +191,10 @@ def _descend(space, run, base, repeats=3):
 
 
 BATCH_SPACE = [
-    [{"batch.group_hi": hi, "batch.group_lo": lo} for hi, lo in
-     ((1024, 384), (1536, 512), (768, 320), (1024, 256), (1280, 448), (896, 384), (2048, 512), (1024, 512),
-      (1280, 640), (2048, 768), (768, 256), (640, 256), (896, 320), (768, 384))],
+    [{"batch.group_hi": hi, "batch.group_mid": mid, "batch.group_lo": lo} for hi, mid, lo in
+     ((1024, 0, 384), (1536, 0, 512), (768, 0, 320), (1024, 0, 256), (1280, 0, 448), (896, 0, 384), (2048, 0, 512),
+      (1024, 0, 512), (1280, 0, 640), (2048, 0, 768), (768, 0, 256), (640, 0, 256), (896, 0, 320), (768, 0, 384),
+      (1280, 768, 384), (1024, 640, 320), (1536, 896, 448), (1280, 640, 320), (1024, 512, 256), (768, 512, 256))],
     [{"batch.assembly_span": s} for s in (64, 128, 256)],
     [{"batch.assembly_rows": r} for r in (1, 2, 3, 4)],
     [{"batch.loads_threads": t} for t in (0, 32, 64, 128, 256)],

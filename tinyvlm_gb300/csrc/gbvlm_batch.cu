@@ -861,7 +861,7 @@ struct gbvlm_batch_s {
     // the sorted systems in size groups, each factored by its own plan on its
     // own stream (graph branch), so the long step chain of the largest
     // systems runs beside the shorter chains of the others
-    static constexpr int MAX_GROUPS = 3;
+    static constexpr int MAX_GROUPS = 4;
     int ngroups = 0;
     LuPlan plans[MAX_GROUPS];
     cudaStream_t side[MAX_GROUPS] = {};
@@ -911,7 +911,7 @@ struct gbvlm_batch_s {
     }
 };
 
-constexpr int MAX_GROUPS_B = 2;  // size-group boundaries (gbvlm_batch_s::MAX_GROUPS - 1)
+constexpr int MAX_GROUPS_B = 3;  // size-group boundaries (gbvlm_batch_s::MAX_GROUPS - 1)
 
 // serial_lu: factor the size groups one after another on `st` (kernel timing
 // without the groups' launches overlapping)
@@ -1106,6 +1106,9 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     const TuneParams tp = tune();
     GB_REQUIRE(tp.batch_group_hi > tp.batch_group_lo, "batch.group_hi (%lld) must exceed batch.group_lo (%lld)",
                (long long)tp.batch_group_hi, (long long)tp.batch_group_lo);
+    GB_REQUIRE(tp.batch_group_mid == 0 || (tp.batch_group_hi > tp.batch_group_mid && tp.batch_group_mid > tp.batch_group_lo),
+               "batch.group_mid (%lld) must be 0 or between batch.group_lo and batch.group_hi",
+               (long long)tp.batch_group_mid);
     auto* h = new gbvlm_batch_s();
     h->tp = tp;
     h->fp64_residual = fp64_residual;
@@ -1359,15 +1362,21 @@ int gbvlm_batch_create_ex(gbvlm_batch* out, int32_t ncases, const gbvlm_dims* di
     h->lub.perm = (int32_t* const*)(base + o_luperm);
     h->lub.mv = (int32_t*)(base + o_lumv);
     // size groups: n > hi, lo < n <= hi, n <= lo (by default 1024 and 384;
-    // empty groups dropped)
+    // with batch.group_mid, lo < n <= hi splits at mid; empty groups dropped)
     {
-        const int64_t bounds[MAX_GROUPS_B] = {h->tp.batch_group_hi, h->tp.batch_group_lo};
+        int64_t bounds[MAX_GROUPS_B] = {h->tp.batch_group_hi, h->tp.batch_group_lo, 0};
+        int nb = 2;
+        if (h->tp.batch_group_mid > 0) {
+            bounds[1] = h->tp.batch_group_mid;
+            bounds[2] = h->tp.batch_group_lo;
+            nb = 3;
+        }
         int i0 = 0;
         int greatest = 0, least = 0;
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
-        for (int g = 0; g <= MAX_GROUPS_B && rc == GBVLM_OK; g++) {
+        for (int g = 0; g <= nb && rc == GBVLM_OK; g++) {
             int i1 = i0;
-            while (i1 < h->nsys && (g == MAX_GROUPS_B || lun[i1] > bounds[g])) i1++;
+            while (i1 < h->nsys && (g == nb || lun[i1] > bounds[g])) i1++;
             if (i1 == i0) continue;
             const int gi = h->ngroups++;
             h->gtile[gi][0] = h->tpfx_host[i0];

@@ -39,6 +39,7 @@ struct TuneParams {
     int64_t hbvlm_min_rows = 32;       // wake rows per operator slice at least
     int64_t batch_group_hi = 1024;     // batch LU size groups: n > hi, lo < n <= hi, n <= lo
     int64_t batch_group_lo = 384;
+    int64_t batch_group_mid = 0;       // 0, or a fourth group: hi > mid > lo splits lo < n <= hi at mid
     int64_t batch_loads_threads = 0;   // loads block: 0 = 64 up to 4096 unknowns, 256 beyond
     int64_t batch_assembly_span = 128; // rings per span chunk of a batch assembly tile
     int64_t batch_assembly_rows = 4;   // chordwise ring rows per float assembly tile (1-4; at most 2 with span 256)

@@ -782,17 +782,20 @@ __global__ void __launch_bounds__(IN_THREADS) k_inner(LuBatch<float> B, int64_t 
     const int64_t c0 = right ? k + nb + (cidx - nleft) : k0 + cidx;
     const int cw = (int)min((int64_t)IN_COLS, (right ? min(n, kend) : k) - c0);
     const int tid = threadIdx.x, t = tid & 31, c = tid >> 5;
+    int moved = 0;
     if (tid < GK) {
         const int32_t* mv = B.mv + (int64_t)sid * 64;
         msrc[tid] = tid < nb ? mv[tid] : tid;
         mdst[tid] = tid < nb ? mv[GK + tid] : tid;
+        moved = msrc[tid] != tid || mdst[tid] != tid;
     }
     if (right)
         for (int e = tid; e < GK * GK; e += IN_THREADS) {
             const int rr = e & (GK - 1), cc = e >> 5;
             L11[rr][cc] = rr < nb && cc < nb ? A[(k + rr) + (k + cc) * ld] : 0.f;
         }
-    __syncthreads();
+    // a chunk left of the panel only takes the row moves: none, nothing to do
+    if (!__syncthreads_or(moved) && !right) return;
     const bool live = c < cw && t < nb;
     float* col = A + (c0 + c) * ld;
     float top = 0.f, out = 0.f;

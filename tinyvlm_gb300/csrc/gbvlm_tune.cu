@@ -27,6 +27,7 @@ const Param kParams[] = {
     {"hbvlm.min_rows", &TuneParams::hbvlm_min_rows, 8, 512},
     {"batch.group_hi", &TuneParams::batch_group_hi, 64, 16384},
     {"batch.group_lo", &TuneParams::batch_group_lo, 16, 16384},
+    {"batch.group_mid", &TuneParams::batch_group_mid, 0, 16384},
     {"batch.loads_threads", &TuneParams::batch_loads_threads, 0, 256},
     {"batch.assembly_span", &TuneParams::batch_assembly_span, 64, 256},
     {"batch.assembly_rows", &TuneParams::batch_assembly_rows, 1, 4},
