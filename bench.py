@@ -48,7 +48,7 @@ FLOP_PER_INTERACTION = 558  # Biot-Savart ring-point interaction, counted from t
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--mode", default="shared", choices=["shared", "exact"])
