@@ -1333,7 +1333,10 @@ __global__ void __launch_bounds__(FL_THREADS, 2) k_trs_flow(LuBatch<float> B, co
                 }
             }
         } else {
-            if (!flow_wait(gctl + 2 + s, bi, err, &s_ok)) break;  // y_i
+            if (!flow_wait(gctl + 2 + s, bi, err, &s_ok)) {  // y_i
+                asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy into shared memory outlives the CTA
+                break;
+            }
             if (cq == 0) {
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
