@@ -231,8 +231,8 @@ int gbvlm_rhs_assemble_wake_influence_f64(double* rhs, int32_t nsurf, const gbvl
  * device image instead of scratch grown with cudaMalloc.  At most 1,048,576
  * collocation points (all surfaces); larger problems are rejected with
  * GBVLM_ERR_ARG.  The first call on a device looks the array up with
- * cudaGetSymbolAddress: make it before any stream capture.  Calls share the
- * array, so calls whose kernels overlap on the GPU race. */
+ * cudaGetSymbolAddress.  Calls share the array, so calls whose kernels
+ * overlap on the GPU race. */
 int gbvlm_rhs_assemble_wake_influence_f32_noalloc(float* rhs, int32_t nsurf, const gbvlm_dims* dims,
                                                   const float* const* gamma_wake, const float* const* colloc,
                                                   const float* const* normals, const float* const* verts_wake,

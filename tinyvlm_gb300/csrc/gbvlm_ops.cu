@@ -1256,7 +1256,7 @@ GB_BOTH(DEF_GUPDATE)
 // up its device address with cudaGetSymbolAddress while that device is
 // current and caches it with the context it belongs to; a later call from a
 // different context (the primary context released and created again) looks
-// it up again.  Make the first call on a device before any stream capture.
+// it up again.
 // All calls share the one array and every call overwrites the part it uses
 // (each partial is written before it is read), so no contents carry over;
 // calls whose kernels overlap on the GPU (different streams, no ordering
