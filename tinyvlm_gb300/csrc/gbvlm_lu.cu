@@ -584,20 +584,19 @@ __global__ void __launch_bounds__(TRSM_COLS) k_trsm(LuBatch<T> B, int64_t k, con
 // ---------------------------------------------------------------------------
 // two-level blocking, end of an outer block [k0, k0 + WW): U12 = L11^-1 A12
 // for the columns right of the block, L11 the WW x WW unit lower triangle.
-// One CTA per TW_COLS columns: L11 and the columns in shared memory, solved
-// in 32-row blocks:
+// One CTA per COLS (64, or 32 on the identity) columns: L11 and the columns
+// in shared memory, solved in 32-row blocks:
 //   * diagonal block: a lane per row holding its row of the 32 x 32 block
-//     in registers, eight columns in flight per warp (8 warps x 8 columns);
+//     in registers, COLS / 8 columns in flight per warp;
 //   * rows below: thread (column j, row group g) keeps the 32 solved values
 //     of column j in registers and sweeps rows g, g+4, ... with the L rows
 //     read as float4 broadcasts.
 // ---------------------------------------------------------------------------
 constexpr int TW_COLS = 64;
 constexpr int TW_LS = LU_OUTER + 4;  // L row stride (float4-aligned rows)
-constexpr int TW_XS = TW_COLS + 1;   // X row stride (odd: conflict-free columns)
 
-template <int WW>
-constexpr size_t trsm_wide_smem() { return sizeof(float) * ((size_t)WW * TW_LS + (size_t)WW * TW_XS); }
+template <int WW, int COLS = TW_COLS>
+constexpr size_t trsm_wide_smem() { return sizeof(float) * ((size_t)WW * TW_LS + (size_t)WW * (COLS + 1)); }
 
 // U12 through the explicit inverse for every system (GBVLM_TC_TRSM=0: the
 // triangular solve).  It stages each L11 once instead of once per 64 columns,
@@ -611,35 +610,44 @@ constexpr int TC_TRSM_MIN_SYSTEMS = 1;
 // INV: the same solve on the identity, two CTAs per system (64 columns
 // each): writes M = I - L11^-1 (strictly lower, column-major, ld WW) to
 // minv + (sid - base) * WW * WW, for U12 = A12 - M A12 on the tensor cores
-template <int WW, bool INV = false>
+template <int WW, bool INV = false, int COLS = TW_COLS>
 __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t k0, const int32_t* act,
                                                      const int64_t* pfx, int cnt, float* minv, int32_t base) {
     static_assert(WW == LU_OUTER, "row stride sized for the outer block");
-    static_assert(TW_COLS == 8 * 8, "eight warps of eight columns");
+    static_assert(COLS == 64 || COLS == 32, "eight warps of COLS / 8 columns");
+    constexpr int TW_XS = COLS + 1;      // X row stride (odd: conflict-free columns)
+    constexpr int CPW = COLS / 8;        // columns per warp on the diagonal block
+    constexpr int CTAS = WW / COLS;      // CTAs per system on the identity
     extern __shared__ __align__(16) float tw_smem[];
     float* L = tw_smem;            // L[r * TW_LS + c]
     float* X = L + WW * TW_LS;     // X[r * TW_XS + j]
-    const int a = INV ? (int)(blockIdx.x >> 1) : find_block(pfx, cnt, blockIdx.x);
+    const int a = INV ? (int)(blockIdx.x / CTAS) : find_block(pfx, cnt, blockIdx.x);
     const int32_t sid = act[a];
     const int64_t n = B.n[sid], ld = B.ld[sid];
     float* A = B.A[sid];
     // columns of A12 (systems here have n > k0 + WW), or of the identity
-    const int64_t c0 = INV ? (int64_t)(blockIdx.x & 1) * TW_COLS : k0 + WW + (int64_t)(blockIdx.x - pfx[a]) * TW_COLS;
-    const int ncols = INV ? TW_COLS : (int)min((int64_t)TW_COLS, n - c0);
+    const int64_t c0 = INV ? (int64_t)(blockIdx.x % CTAS) * COLS : k0 + WW + (int64_t)(blockIdx.x - pfx[a]) * COLS;
+    const int ncols = INV ? COLS : (int)min((int64_t)COLS, n - c0);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const float* Ab = A + k0 + k0 * ld;
+    // on the identity the CTA reads L11 only from its first column block on
+    const int cs = INV ? (int)c0 : 0;
     staged_copy<16>(
-        WW * WW, tid, 256, [&](int64_t e) { return Ab[(int)(e & (WW - 1)) + (e >> 7) * ld]; },
+        WW * WW, tid, 256,
+        [&](int64_t e) {
+            const int r = (int)(e & (WW - 1)), c = (int)(e >> 7);
+            return (r >= cs && c >= cs) ? Ab[r + c * ld] : 0.f;
+        },
         [&](int64_t e, float v) { L[(int)(e & (WW - 1)) * TW_LS + (int)(e >> 7)] = v; });
     if constexpr (INV) {
-        for (int e = tid; e < WW * TW_COLS; e += 256) {
+        for (int e = tid; e < WW * COLS; e += 256) {
             const int r = e & (WW - 1), j = e >> 7;
             X[r * TW_XS + j] = (r == (int)c0 + j) ? 1.f : 0.f;
         }
     } else {
         const float* Xb = A + k0 + c0 * ld;
         staged_copy<16>(
-            WW * TW_COLS, tid, 256,
+            WW * COLS, tid, 256,
             [&](int64_t e) { return (int)(e >> 7) < ncols ? Xb[(int)(e & (WW - 1)) + (e >> 7) * ld] : 0.f; },
             [&](int64_t e, float v) { X[(int)(e & (WW - 1)) * TW_XS + (int)(e >> 7)] = v; });
     }
@@ -653,31 +661,32 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
             float lrow[32];
 #pragma unroll
             for (int l = 0; l < 32; l++) lrow[l] = L[(rb + lane) * TW_LS + rb + l];
-            // warp w: columns 8w..8w+7, all eight in flight
-            const int j0 = 8 * wid;
-            float x[8];
+            // warp w: columns CPW w .. CPW w + CPW - 1, all in flight
+            const int j0 = CPW * wid;
+            float x[CPW];
 #pragma unroll
-            for (int c = 0; c < 8; c++) x[c] = X[(rb + lane) * TW_XS + j0 + c];
+            for (int c = 0; c < CPW; c++) x[c] = X[(rb + lane) * TW_XS + j0 + c];
 #pragma unroll
             for (int l = 0; l < 32; l++) {
 #pragma unroll
-                for (int c = 0; c < 8; c++) {
+                for (int c = 0; c < CPW; c++) {
                     const float xl = __shfl_sync(0xffffffffu, x[c], l);
                     if (lane > l) x[c] -= lrow[l] * xl;
                 }
             }
 #pragma unroll
-            for (int c = 0; c < 8; c++) X[(rb + lane) * TW_XS + j0 + c] = x[c];
+            for (int c = 0; c < CPW; c++) X[(rb + lane) * TW_XS + j0 + c] = x[c];
         }
         __syncthreads();
         // rows below the block
         if (rb + 32 < WW) {
-            const int j = tid & (TW_COLS - 1), g = tid >> 6;
+            constexpr int RG = 256 / COLS;  // row groups
+            const int j = tid & (COLS - 1), g = tid / COLS;
             float xb[32];
 #pragma unroll
             for (int l = 0; l < 32; l++) xb[l] = X[(rb + l) * TW_XS + j];
 #pragma unroll 1
-            for (int r = rb + 32 + g; r < WW; r += 4) {
+            for (int r = rb + 32 + g; r < WW; r += RG) {
                 const float4* lr = reinterpret_cast<const float4*>(L + r * TW_LS + rb);
                 float acc = 0.f;
 #pragma unroll
@@ -692,13 +701,13 @@ __global__ void __launch_bounds__(256, 2) k_trsm_wide(LuBatch<float> B, int64_t 
     }
     if constexpr (INV) {
         float* Mo = minv + (int64_t)(sid - base) * WW * WW + c0 * WW;
-        for (int e = tid; e < WW * TW_COLS; e += 256) {
+        for (int e = tid; e < WW * COLS; e += 256) {
             const int r = e & (WW - 1), j = e >> 7;
             Mo[r + j * WW] = r > (int)c0 + j ? -X[r * TW_XS + j] : 0.f;
         }
     } else {
         float* Xo = A + k0 + c0 * ld;
-        for (int e = tid; e < WW * TW_COLS; e += 256) {
+        for (int e = tid; e < WW * COLS; e += 256) {
             const int r = e & (WW - 1), j = e >> 7;
             if (j < ncols) Xo[r + (int64_t)j * ld] = X[r * TW_XS + j];
         }
@@ -1795,6 +1804,16 @@ int lu_large_solve(const LuBatch<T>& B, int64_t n, int32_t nrhs, cudaStream_t st
 // ---------------------------------------------------------------------------
 // panel launch: register panel with the thread count of the group
 // ---------------------------------------------------------------------------
+// GBVLM_INV_COLS=32 or 64 fixes the CTA width of L11^-1 (by default chosen per step)
+static int inv_cols() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("GBVLM_INV_COLS");
+        mode = (e && (atoi(e) == 32 || atoi(e) == 64)) ? atoi(e) : 0;
+    }
+    return mode;
+}
+
 // GBVLM_PANEL_PACK=0 keeps one system per one-CTA panel
 static bool panel_pack() {
     static int mode = -1;
@@ -1935,8 +1954,16 @@ int lu_batch_factor(const LuBatch<T>& B, const LuPlan& plan, cudaStream_t st, bo
         if constexpr (sizeof(T) == 4) {
             if (S.tc_blocks > 0) {
                 if (plan.tc_trsm && S.n_tc >= plan.tc_trsm_min) {
-                    k_trsm_wide<LU_OUTER, true><<<(unsigned)(2 * S.n_tc), 256, trsm_wide_smem<LU_OUTER>(), st>>>(
-                        B, k0, act, nullptr, S.n_tc, plan.d_minv, plan.base);
+                    // four CTAs of 32 columns per system when the step's systems fill
+                    // less than a wave (the chain of few large systems is shorter), two
+                    // of 64 otherwise (fewer CTAs when the SMs are busy); the same arithmetic
+                    const int ic = inv_cols();
+                    if (ic == 32 || (ic == 0 && 4 * (int64_t)S.n_tc <= tc_num_sms()))
+                        k_trsm_wide<LU_OUTER, true, 32><<<(unsigned)(4 * S.n_tc), 256, trsm_wide_smem<LU_OUTER, 32>(),
+                                                          st>>>(B, k0, act, nullptr, S.n_tc, plan.d_minv, plan.base);
+                    else
+                        k_trsm_wide<LU_OUTER, true><<<(unsigned)(2 * S.n_tc), 256, trsm_wide_smem<LU_OUTER>(), st>>>(
+                            B, k0, act, nullptr, S.n_tc, plan.d_minv, plan.base);
                     GB_LAUNCH_CHECK();
                     const int64_t* tp = plan.d_pfx + S.tcs_pfx;
                     if (plan.tc_wide) {
@@ -2100,6 +2127,8 @@ int lu_plan_build(LuPlan& plan, const std::vector<int64_t>& n_sorted, cudaStream
             GB_CUDA(cudaFuncSetAttribute(k_inner_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsm_wide_smem<LU_OUTER>()));
+            GB_CUDA(cudaFuncSetAttribute(k_trsm_wide<LU_OUTER, true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trsm_wide_smem<LU_OUTER, 32>()));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<1, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::SMEM_BYTES));
             GB_CUDA(cudaFuncSetAttribute(k_trsm_tc12<3, tc::BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
