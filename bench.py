@@ -426,7 +426,7 @@ def run_gpu(args):
         "one_in_flight": {"value": value1, "ms_per_step": ms1, "unit": "solves/s", "tuning": bs.tuning,
                           "latency_ms": {"p50": float(np.percentile(lat1, 50)), "p99": float(np.percentile(lat1, 99)),
                                          "what": "per batch, set_inputs + run + results through BatchSolver"}},
-        "gpu_launches": int(bs.launches()) * args.steps,
+        "gpu_launches": int(pipe.launches()) * args.steps,  # the pipeline's plan: the headline's timed region
         "clocks": clk.summary(),
         "roofline": roof,
         "stage_ms": prof,
