@@ -441,9 +441,10 @@ def run_gpu(args):
 # DRAM bytes per algorithmic byte of the tensor-core trailing update
 # (dram__bytes_read.sum + dram__bytes_write.sum of k_update_tc over the
 # launches' algorithmic bytes; the operands are re-read from L2, not DRAM),
-# from one ncu capture of this batch (512 cases): its first graph replay,
-# 44 launches, 7.10 GB of DRAM traffic over 7.60 GB algorithmic
-TC_TRAFFIC_PER_ALG_BYTE = 0.935
+# from one ncu capture of this batch (512 cases, the one-in-flight plan whose
+# update the roofline entry times): one step, 31 launches, 4.88 GB of DRAM
+# traffic over 7.60 GB algorithmic
+TC_TRAFFIC_PER_ALG_BYTE = 0.643
 
 
 def roofline(bs, stream, peaks, ms_step):
